@@ -1,0 +1,239 @@
+/*
+ * rdn.h — C ABI of the GB300 ray-query library (librdn.so).
+ *
+ * This is the drop-in boundary for the reference's ray-query path
+ * (mikialex/rendiation, shader/ray-tracing). Each entry point names the
+ * reference interface it replaces. The reference exposes Rust traits whose
+ * device half returns shader-EDSL nodes, so the boundary a Rust host binds is
+ * this C ABI: an `extern "C"` block plus a trait implementation that forwards
+ * to it.
+ *
+ * Conventions
+ *  - Every entry point returns rdn_status; nothing aborts or traps. The text
+ *    of the last error of a context is available from rdn_last_error().
+ *  - Source arrays passed to *_create are copied, as the reference clones its
+ *    sources (naive/mod.rs:98-109).
+ *  - Handles are dense u32 slots; deleting leaves an empty slot, as in the
+ *    reference (naive/mod.rs:110-119).
+ *  - Ray and hit buffers passed to rdn_trace are DEVICE pointers owned by the
+ *    caller; work is stream-ordered on the given cudaStream_t (NULL = legacy
+ *    default stream). Acceleration-structure buffers are owned by the context.
+ *  - Create/delete/bind/build take the context's lock (the reference's
+ *    Arc<RwLock> write lock, naive/mod.rs:497-609); traces on distinct
+ *    streams may run concurrently once the structure is built.
+ */
+#ifndef RDN_H
+#define RDN_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RDN_API_VERSION 1u
+
+typedef int32_t rdn_status;
+#define RDN_OK 0
+#define RDN_ERR_INVALID_ARG (-1)
+#define RDN_ERR_INVALID_HANDLE (-2)
+#define RDN_ERR_OOM (-3)
+#define RDN_ERR_CUDA (-4)
+#define RDN_ERR_QUEUE_OVERFLOW (-5)
+#define RDN_ERR_TIMEOUT (-6)
+#define RDN_ERR_NOT_BUILT (-7)
+#define RDN_ERR_UNSUPPORTED (-8)
+
+/* Ray flags: the reference's RayFlagConfigRaw values (api/ty.rs:102-114). */
+#define RDN_RAY_FLAG_NONE 0x00u
+#define RDN_RAY_FLAG_FORCE_OPAQUE 0x01u
+#define RDN_RAY_FLAG_FORCE_NON_OPAQUE 0x02u
+#define RDN_RAY_FLAG_ACCEPT_FIRST_HIT_AND_END_SEARCH 0x04u
+#define RDN_RAY_FLAG_SKIP_CLOSEST_HIT_SHADER 0x08u
+#define RDN_RAY_FLAG_CULL_BACK_FACING_TRIANGLES 0x10u
+#define RDN_RAY_FLAG_CULL_FRONT_FACING_TRIANGLES 0x20u
+#define RDN_RAY_FLAG_CULL_OPAQUE 0x40u
+#define RDN_RAY_FLAG_CULL_NON_OPAQUE 0x80u
+#define RDN_RAY_FLAG_SKIP_TRIANGLES 0x100u
+#define RDN_RAY_FLAG_SKIP_PROCEDURAL_PRIMITIVES 0x200u
+
+/* Instance flags (api/ty.rs:142-151) and geometry flags (api/ty.rs:153-159). */
+#define RDN_INSTANCE_TRIANGLE_FACING_CULL_DISABLE 0x1u
+#define RDN_INSTANCE_TRIANGLE_FLIP_FACING 0x2u
+#define RDN_INSTANCE_FORCE_OPAQUE 0x4u
+#define RDN_INSTANCE_FORCE_NO_OPAQUE 0x8u
+#define RDN_GEOMETRY_OPAQUE 0x1u
+#define RDN_GEOMETRY_NO_DUPLICATE_ANYHIT_INVOCATION 0x2u
+
+/* Hit kinds (api/ty.rs:138-140). */
+#define RDN_HIT_KIND_FRONT_FACING_TRIANGLE 0xFEu
+#define RDN_HIT_KIND_BACK_FACING_TRIANGLE 0xFFu
+
+#define RDN_MISS 0xFFFFFFFFu
+
+typedef struct rdn_ctx rdn_ctx;
+
+/* BottomLevelAccelerationStructureBuildSource (api/backend.rs:103-118).
+ * type 0 = triangles (positions xyz f32 per vertex; indices nullable: NULL
+ * means non-indexed, every 3 vertices form a triangle, naive/mod.rs:158-162);
+ * type 1 = AABBs, accepted and ignored exactly as the reference's naive
+ * system ignores them (naive/mod.rs:201-237). */
+typedef struct rdn_geometry {
+  uint32_t type;
+  uint32_t flags; /* RDN_GEOMETRY_* */
+  const float* positions;
+  uint32_t vertex_count;
+  uint32_t index_count;
+  const uint32_t* indices;
+} rdn_geometry;
+
+/* TopLevelAccelerationStructureSourceInstance (api/backend.rs:160-167).
+ * transform is a Mat4 in the reference's memory order (columns a, b, c, d;
+ * translation in elements 12..14). */
+typedef struct rdn_instance {
+  float transform[16];
+  uint32_t custom_index;
+  uint32_t mask;
+  uint32_t sbt_offset;
+  uint32_t flags; /* RDN_INSTANCE_* */
+  uint32_t blas_handle;
+} rdn_instance;
+
+/* TreeBuildOption (content/space/src/utils.rs:20-38) for BLAS and TLAS. The
+ * reference hard-codes BLAS {max_tree_depth 50, bin_size 2} and TLAS
+ * {50, 10} with SAH::new(4) (naive/mod.rs:173-177,280-284); those are the
+ * defaults (a zero field selects its default). host_threads 0 = all cores. */
+typedef struct rdn_build_opts {
+  uint32_t blas_bin_size;
+  uint32_t blas_max_depth;
+  uint32_t tlas_bin_size;
+  uint32_t tlas_max_depth;
+  uint32_t host_threads;
+  uint32_t reserved[3];
+} rdn_build_opts;
+
+/* One ray, 32 B: ShaderRayTraceCallStoragePayload's origin, direction and
+ * range (backend/wavefront_compute/ctx.rs:15-29). */
+typedef struct rdn_ray {
+  float org[3];
+  float tmin;
+  float dir[3];
+  float tmax;
+} rdn_ray;
+
+/* Closest/any hit, 16 B. prim = primitive index within its geometry
+ * (traverse_cpu.rs:160), RDN_MISS for a miss; t = world distance
+ * (traverse_cpu.rs:157); u, v = barycentric weights of vertices 1 and 2
+ * (geometry/mod.rs:144-154). On a miss t = the ray's tmax and u = v = 0. */
+typedef struct rdn_hit {
+  float t;
+  float u;
+  float v;
+  uint32_t prim;
+} rdn_hit;
+
+/* Optional per-ray hit context, 16 B (HitCtxStorage, ctx.rs:46-57):
+ * geometry index within the BLAS, instance slot (position in the built
+ * instance array, traverse_gpu.rs:556-570), the instance's custom index and
+ * the hit kind. All RDN_MISS (hit_kind 0) on a miss. */
+typedef struct rdn_hit_ext {
+  uint32_t geometry;
+  uint32_t instance;
+  uint32_t instance_custom;
+  uint32_t hit_kind;
+} rdn_hit_ext;
+
+/* Traversal order.
+ * RDN_TRAVERSAL_ORDERED: near-child-first stack traversal over 64 B two-child
+ *   nodes. Closest hits equal the reference's except among hits at exactly
+ *   equal distance; first-hit (shadow) queries agree on hit/miss.
+ * RDN_TRAVERSAL_REFERENCE: the reference's stackless threaded hit/miss walk
+ *   (traverse_cpu.rs:291-319) over its own 48 B node layout; bit-identical to
+ *   the reference CPU traversal, including ties and which hit ends a search. */
+#define RDN_TRAVERSAL_ORDERED 0u
+#define RDN_TRAVERSAL_REFERENCE 1u
+
+/* Fixed any-hit policies for non-opaque geometry, standing in for a user
+ * any-hit shader (RayAnyHitBehavior, api/ty.rs:134-136). */
+#define RDN_ANYHIT_ACCEPT 0u
+#define RDN_ANYHIT_ACCEPT_AND_END 1u
+#define RDN_ANYHIT_ACCEPT_EVEN_PRIMS 2u
+
+typedef struct rdn_trace_desc {
+  const rdn_ray* rays;      /* device, count entries */
+  rdn_hit* hits;            /* device, count entries */
+  rdn_hit_ext* hits_ext;    /* device, nullable */
+  const uint32_t* tlas_idx; /* device, nullable: per-ray index into the bound TLAS list */
+  uint32_t count;
+  uint32_t tlas_uniform;    /* used when tlas_idx is NULL */
+  uint32_t ray_flags;       /* RDN_RAY_FLAG_* */
+  uint32_t cull_mask;       /* low 8 bits used */
+  uint32_t traversal;       /* RDN_TRAVERSAL_* */
+  uint32_t anyhit_mode;     /* RDN_ANYHIT_* */
+  uint32_t block_size;      /* 0 = tuned default */
+  uint32_t reserved;
+} rdn_trace_desc;
+
+/* Counters of node visits and triangle tests, the reference's
+ * BVH_VISIT_COUNT / TRI_VISIT_COUNT (traverse_cpu.rs:38-41). */
+typedef struct rdn_counters {
+  uint64_t node_visits;
+  uint64_t tri_tests;
+  uint64_t tri_hits;
+  uint64_t bad_tlas_rays;
+} rdn_counters;
+
+/* ---- context ---------------------------------------------------------- */
+
+/* Replaces NaiveSahBVHSystem::new (naive/mod.rs:508-519). device >= 0 selects a
+ * CUDA device; device == -1 creates a host-only context that can build (and
+ * export the built arrays) but rejects traces with RDN_ERR_UNSUPPORTED. */
+rdn_status rdn_create(rdn_ctx** out, int device);
+rdn_status rdn_destroy(rdn_ctx* ctx);
+const char* rdn_last_error(const rdn_ctx* ctx);
+uint32_t rdn_api_version(void);
+
+/* ---- acceleration structures (GPUAccelerationStructureSystemProvider,
+ *      api/backend.rs:120-142; naive/mod.rs:560-609) ------------------- */
+
+/* create_bottom_level_acceleration_structure */
+rdn_status rdn_blas_create(rdn_ctx* ctx, const rdn_geometry* geometries, uint32_t count, uint32_t* out_handle);
+/* delete_bottom_level_acceleration_structure */
+rdn_status rdn_blas_delete(rdn_ctx* ctx, uint32_t handle);
+/* create_top_level_acceleration_structure */
+rdn_status rdn_tlas_create(rdn_ctx* ctx, const rdn_instance* instances, uint32_t count, uint32_t* out_handle);
+/* delete_top_level_acceleration_structure */
+rdn_status rdn_tlas_delete(rdn_ctx* ctx, uint32_t handle);
+/* bind_tlas; bind_tlas_max_len is u32::MAX in the reference */
+rdn_status rdn_bind_tlas(rdn_ctx* ctx, const uint32_t* handles, uint32_t count);
+/* Explicit build + upload (the reference builds lazily in
+ * get_or_build_gpu_data, naive/mod.rs:521-537; rdn_trace does the same when
+ * the structure is dirty). opts may be NULL. */
+rdn_status rdn_build(rdn_ctx* ctx, const rdn_build_opts* opts);
+/* Seconds spent in the last build: [0] host BVH build + flattening, [1] upload. */
+rdn_status rdn_build_times(const rdn_ctx* ctx, double* out2);
+
+/* Copies one of the built arrays in the reference's flattened layout
+ * (NaiveSahBvhCpu fields, traverse_cpu.rs:9-35) to host memory `dst` of
+ * `capacity` bytes; the byte size is written to *size. which:
+ * 0 tlas_binding, 1 tlas_bvh_root, 2 tlas_bvh_forest, 3 tlas_data,
+ * 4 tlas_bounding, 5 blas_meta_info, 6 tri_bvh_root, 7 tri_bvh_forest,
+ * 8 indices_redirect, 9 indices, 10 vertices. dst may be NULL to query. */
+rdn_status rdn_get_built_array(const rdn_ctx* ctx, uint32_t which, void* dst, size_t capacity, size_t* size);
+
+/* ---- queries -------------------------------------------------------- */
+
+/* Batch closest/any-hit query with NaiveSahBvhCpu::traverse semantics
+ * (traverse_cpu.rs:52-245), one result per ray. */
+rdn_status rdn_trace(rdn_ctx* ctx, const rdn_trace_desc* desc, void* stream);
+
+/* Same as rdn_trace, additionally accumulating node-visit and triangle-test
+ * counts (slower; for measurement). */
+rdn_status rdn_trace_counted(rdn_ctx* ctx, const rdn_trace_desc* desc, void* stream, rdn_counters* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RDN_H */

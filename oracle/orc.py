@@ -1,0 +1,208 @@
+"""ctypes wrapper of the oracle library (oracle/_build/liborc.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, the smoke check and bench.py's
+CPU-baseline / reference arm, as the checker. The product never imports it.
+The oracle is a C++ restatement of the reference's CPU ray-query path
+(see rdn_oracle.cpp for the file:line map); parity with the reference's own
+outputs is unpinned because the Rust reference cannot be built here.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "liborc.so")
+_lib = None
+
+HIT_DTYPE = np.dtype(
+    [("t", np.float32), ("u", np.float32), ("v", np.float32), ("prim", np.uint32),
+     ("geometry", np.uint32), ("instance", np.uint32), ("custom", np.uint32), ("hit_kind", np.uint32)]
+)
+MISS = 0xFFFFFFFF
+
+BUF_TLAS_BINDING, BUF_TLAS_BVH_ROOT, BUF_TLAS_BVH_FOREST, BUF_TLAS_DATA, BUF_TLAS_BOUNDING = 0, 1, 2, 3, 4
+BUF_BLAS_META_INFO, BUF_TRI_BVH_ROOT, BUF_TRI_BVH_FOREST, BUF_INDICES_REDIRECT, BUF_INDICES, BUF_VERTICES = 5, 6, 7, 8, 9, 10
+
+
+class _Geometry(C.Structure):
+    _fields_ = [("positions", C.c_void_p), ("vertex_count", C.c_uint32), ("indices", C.c_void_p),
+                ("index_count", C.c_uint32), ("flags", C.c_uint32), ("type", C.c_uint32)]
+
+
+class _Instance(C.Structure):
+    _fields_ = [("transform", C.c_float * 16), ("custom_index", C.c_uint32), ("mask", C.c_uint32),
+                ("sbt_offset", C.c_uint32), ("flags", C.c_uint32), ("blas_handle", C.c_uint32)]
+
+
+def build_library() -> str:
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            build_library()
+        L = C.CDLL(_LIB_PATH)
+        vp, u32, i32 = C.c_void_p, C.c_uint32, C.c_int
+        L.orc_create.restype = vp
+        L.orc_destroy.argtypes = [vp]
+        L.orc_last_error.restype = C.c_char_p
+        L.orc_last_error.argtypes = [vp]
+        L.orc_blas_create.argtypes = [vp, vp, u32, C.POINTER(u32)]
+        L.orc_blas_delete.argtypes = [vp, u32]
+        L.orc_tlas_create.argtypes = [vp, vp, u32, C.POINTER(u32)]
+        L.orc_tlas_delete.argtypes = [vp, u32]
+        L.orc_bind_tlas.argtypes = [vp, vp, u32]
+        L.orc_build.argtypes = [vp, u32, u32, u32, u32]
+        L.orc_build_stats.argtypes = [vp, vp]
+        L.orc_get_buffer.restype = C.c_size_t
+        L.orc_get_buffer.argtypes = [vp, i32, vp, C.c_size_t]
+        L.orc_trace.argtypes = [vp, vp, u32, vp, u32, u32, u32, u32, vp, vp, vp, i32, C.POINTER(C.c_double)]
+        L.orc_eval_fp64.argtypes = [vp, vp, u32, vp, vp]
+        L.orc_bruteforce_fp64.argtypes = [vp, vp, u32, u32, vp, i32]
+        L.orc_intersect_triangle.argtypes = [vp, vp, C.c_float, C.c_float, vp, vp, vp, i32, i32, vp]
+        L.orc_intersect_aabb.argtypes = [vp, vp, C.c_float, C.c_float, vp, vp]
+        L.orc_select_nth.argtypes = [vp, vp, C.c_size_t, C.c_size_t]
+        _lib = L
+    return _lib
+
+
+def _ptr(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data
+
+
+class OracleSystem:
+    """Mirror of the reference's NaiveSahBVHSystem (naive/mod.rs:496-609) on the CPU."""
+
+    def __init__(self):
+        self._L = lib()
+        self._h = self._L.orc_create()
+        self._keep = []
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._L.orc_destroy(self._h)
+            self._h = None
+
+    def _check(self, rc):
+        if rc != 0:
+            raise RuntimeError(f"oracle error {rc}: {self._L.orc_last_error(self._h).decode()}")
+
+    def create_blas(self, geometries) -> int:
+        """geometries: list of (positions (V,3) f32, indices u32 or None, flags)."""
+        arr = (_Geometry * len(geometries))()
+        keep = []
+        for g, (pos, idx, flags) in zip(arr, geometries):
+            pos = np.ascontiguousarray(pos, np.float32)
+            keep.append(pos)
+            g.positions = pos.ctypes.data
+            g.vertex_count = pos.shape[0]
+            if idx is not None:
+                idx = np.ascontiguousarray(idx, np.uint32)
+                keep.append(idx)
+                g.indices = idx.ctypes.data
+                g.index_count = idx.shape[0]
+            g.flags = flags
+            g.type = 0
+        out = C.c_uint32()
+        self._check(self._L.orc_blas_create(self._h, C.addressof(arr), len(geometries), C.byref(out)))
+        return out.value
+
+    def delete_blas(self, h: int):
+        self._check(self._L.orc_blas_delete(self._h, h))
+
+    def create_tlas(self, instances) -> int:
+        """instances: list of dicts with transform (4x4, column-major flat 16), blas, custom, mask, sbt, flags."""
+        arr = (_Instance * len(instances))()
+        for dst, s in zip(arr, instances):
+            tf = np.asarray(s.get("transform", np.eye(4, dtype=np.float32).reshape(-1)), np.float32).reshape(-1)
+            for k in range(16):
+                dst.transform[k] = float(tf[k])
+            dst.custom_index = s.get("custom", 0)
+            dst.mask = s.get("mask", 0xFF)
+            dst.sbt_offset = s.get("sbt", 0)
+            dst.flags = s.get("flags", 0)
+            dst.blas_handle = s["blas"]
+        out = C.c_uint32()
+        self._check(self._L.orc_tlas_create(self._h, C.addressof(arr), len(instances), C.byref(out)))
+        return out.value
+
+    def delete_tlas(self, h: int):
+        self._check(self._L.orc_tlas_delete(self._h, h))
+
+    def bind_tlas(self, handles):
+        a = np.ascontiguousarray(handles, np.uint32)
+        self._check(self._L.orc_bind_tlas(self._h, _ptr(a), a.shape[0]))
+
+    def build(self, blas_bin_size=2, blas_max_depth=50, tlas_bin_size=10, tlas_max_depth=50):
+        self._check(self._L.orc_build(self._h, blas_bin_size, blas_max_depth, tlas_bin_size, tlas_max_depth))
+
+    def build_stats(self):
+        s = np.zeros(2, np.uint64)
+        self._check(self._L.orc_build_stats(self._h, _ptr(s)))
+        return {"sah_splits": int(s[0]), "median_fallbacks": int(s[1])}
+
+    def buffer(self, which: int) -> bytes:
+        n = self._L.orc_get_buffer(self._h, which, None, 0)
+        b = np.zeros(n, np.uint8)
+        self._L.orc_get_buffer(self._h, which, _ptr(b), n)
+        return b.tobytes()
+
+    def trace(self, rays: np.ndarray, tlas_idx=None, tlas_uniform=0, ray_flags=0, cull_mask=0xFF, anyhit_mode=0,
+              threads=1, counts=False):
+        rays = np.ascontiguousarray(rays)
+        n = rays.shape[0]
+        out = np.zeros(n, HIT_DTYPE)
+        rc = np.zeros((n, 2), np.uint32) if counts else None
+        tot = np.zeros(6, np.uint64)
+        ti = None if tlas_idx is None else np.ascontiguousarray(tlas_idx, np.uint32)
+        sec = C.c_double()
+        self._check(self._L.orc_trace(self._h, _ptr(rays), n, _ptr(ti), tlas_uniform, ray_flags, cull_mask,
+                                      anyhit_mode, _ptr(out), _ptr(rc), _ptr(tot), threads, C.byref(sec)))
+        totals = dict(zip(["tri_visit", "tri_hit", "bvh_visit", "bvh_hit", "far_assert", "bad_tlas"],
+                          (int(x) for x in tot)))
+        totals["seconds"] = sec.value
+        if counts:
+            return out, totals, rc
+        return out, totals
+
+    def eval_fp64(self, rays: np.ndarray, hits: np.ndarray) -> np.ndarray:
+        out = np.zeros((rays.shape[0], 3), np.float64)
+        self._check(self._L.orc_eval_fp64(self._h, _ptr(np.ascontiguousarray(rays)), rays.shape[0],
+                                          _ptr(np.ascontiguousarray(hits)), _ptr(out)))
+        return out
+
+    def bruteforce_fp64(self, rays: np.ndarray, tlas_uniform=0, threads=4) -> np.ndarray:
+        out = np.zeros((rays.shape[0], 5), np.float64)
+        self._check(self._L.orc_bruteforce_fp64(self._h, _ptr(np.ascontiguousarray(rays)), rays.shape[0],
+                                                tlas_uniform, _ptr(out), threads))
+        return out
+
+
+def intersect_triangle(o, d, near, far, v0, v1, v2, cull_enable=False, cull_back=False):
+    f = lambda a: np.ascontiguousarray(a, np.float32)
+    o, d, v0, v1, v2 = f(o), f(d), f(v0), f(v1), f(v2)
+    out = np.zeros(4, np.float32)
+    lib().orc_intersect_triangle(_ptr(o), _ptr(d), near, far, _ptr(v0), _ptr(v1), _ptr(v2), int(cull_enable),
+                                 int(cull_back), _ptr(out))
+    return out
+
+
+def intersect_aabb(o, d, tmin, tmax, bmin, bmax) -> bool:
+    f = lambda a: np.ascontiguousarray(a, np.float32)
+    o, d, bmin, bmax = f(o), f(d), f(bmin), f(bmax)
+    return bool(lib().orc_intersect_aabb(_ptr(o), _ptr(d), tmin, tmax, _ptr(bmin), _ptr(bmax)))
+
+
+def select_nth(keys: np.ndarray, index: int) -> np.ndarray:
+    keys = np.ascontiguousarray(keys, np.float32)
+    idx = np.arange(keys.shape[0], dtype=np.uint64)
+    lib().orc_select_nth(_ptr(keys), _ptr(idx), keys.shape[0], index)
+    return idx

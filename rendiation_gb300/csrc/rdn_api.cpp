@@ -1,0 +1,399 @@
+// C ABI of librdn (include/rdn.h): the acceleration-structure system
+// (GPUAccelerationStructureSystemProvider, shader/ray-tracing/src/api/backend.rs:120-142,
+// implemented by NaiveSahBVHSystem, .../geometry/naive/mod.rs:496-609) and the
+// batch trace entry points.
+#include <chrono>
+#include <cstring>
+#include <exception>
+#include <new>
+
+#include "rdn_core.h"
+#include "trace_kernels.h"
+
+using rdn::DevBuf;
+
+namespace {
+
+rdn_status fail(rdn_ctx* c, rdn_status code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+rdn_status cuda_fail(rdn_ctx* c, cudaError_t e, const char* what) {
+  return fail(c, e == cudaErrorMemoryAllocation ? RDN_ERR_OOM : RDN_ERR_CUDA,
+              std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+template <class T>
+void free_buf(DevBuf<T>& b) {
+  if (b.ptr) cudaFree(b.ptr);
+  b.ptr = nullptr;
+  b.count = 0;
+}
+
+void free_device(rdn::DeviceBuilt& d) {
+  free_buf(d.tlas_binding);
+  free_buf(d.tlas_bvh_root);
+  free_buf(d.indices_redirect);
+  free_buf(d.leaf_ranges);
+  free_buf(d.geom_root_code);
+  free_buf(d.tlas_bvh_forest);
+  free_buf(d.tri_bvh_forest);
+  free_buf(d.tlas_data);
+  free_buf(d.tlas_bounding);
+  free_buf(d.blas_meta_info);
+  free_buf(d.tri_bvh_root);
+  free_buf(d.tri_records);
+  free_buf(d.wide_nodes);
+  d.bytes = 0;
+}
+
+// Uploads one array; an empty array still gets one zeroed element, as the
+// reference's create_gpu_buffer does (naive/mod.rs:401-416).
+template <class T>
+cudaError_t upload(DevBuf<T>& dst, const std::vector<T>& src, uint64_t& bytes) {
+  const size_t n = src.empty() ? 1 : src.size();
+  cudaError_t e = cudaMalloc(&dst.ptr, n * sizeof(T));
+  if (e != cudaSuccess) return e;
+  dst.count = src.size();
+  bytes += n * sizeof(T);
+  if (src.empty()) return cudaMemset(dst.ptr, 0, sizeof(T));
+  return cudaMemcpy(dst.ptr, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+rdn_status do_build(rdn_ctx* c) {
+  auto t0 = std::chrono::steady_clock::now();
+  auto hb = std::make_unique<rdn::HostBuilt>();
+  std::string err;
+  try {
+    err = rdn::build_host(c->blas, c->tlas, c->binding, c->opts, *hb);
+  } catch (const std::bad_alloc&) {
+    return fail(c, RDN_ERR_OOM, "host allocation failed during build");
+  } catch (const std::exception& ex) {
+    return fail(c, RDN_ERR_INVALID_ARG, ex.what());
+  }
+  if (!err.empty()) return fail(c, RDN_ERR_INVALID_HANDLE, err);
+  auto t1 = std::chrono::steady_clock::now();
+  c->build_seconds = std::chrono::duration<double>(t1 - t0).count();
+  c->upload_seconds = 0.0;
+  if (c->device >= 0) {
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaSetDevice");
+    e = cudaDeviceSynchronize();  // no trace may still read the buffers being replaced
+    if (e != cudaSuccess) return cuda_fail(c, e, "synchronize before upload");
+    free_device(c->dev);
+    rdn::DeviceBuilt& d = c->dev;
+    uint64_t bytes = 0;
+#define UP(field, src)                                      \
+  e = upload(d.field, hb->src, bytes);                      \
+  if (e != cudaSuccess) {                                   \
+    free_device(d);                                         \
+    return cuda_fail(c, e, "upload " #src);                 \
+  }
+    UP(tlas_binding, tlas_binding)
+    UP(tlas_bvh_root, tlas_bvh_root)
+    UP(tlas_bvh_forest, tlas_bvh_forest)
+    UP(tlas_data, tlas_data)
+    UP(tlas_bounding, tlas_bounding)
+    UP(blas_meta_info, blas_meta_info)
+    UP(tri_bvh_root, tri_bvh_root)
+    UP(tri_bvh_forest, tri_bvh_forest)
+    UP(indices_redirect, indices_redirect)
+    UP(tri_records, tri_records)
+    UP(wide_nodes, wide_nodes)
+    UP(leaf_ranges, leaf_ranges)
+    UP(geom_root_code, geom_root_code)
+#undef UP
+    d.max_blas_depth = hb->max_blas_depth;
+    d.bytes = bytes;
+    c->upload_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t1).count();
+  }
+  c->host = std::move(hb);
+  c->dirty = false;
+  return RDN_OK;
+}
+
+uint32_t stack_depth_for(uint32_t max_depth) {
+  uint32_t d = max_depth + 1;
+  d = (d + 3) & ~3u;
+  return d < 8 ? 8 : d;
+}
+
+rdn_status fill_params(rdn_ctx* c, const rdn_trace_desc* desc, rdn::TraceParams& p) {
+  const rdn::DeviceBuilt& d = c->dev;
+  std::memset(&p, 0, sizeof(p));
+  p.rays = reinterpret_cast<const float4*>(desc->rays);
+  p.hits = desc->hits;
+  p.hits_ext = desc->hits_ext;
+  p.tlas_idx = desc->tlas_idx;
+  p.count = desc->count;
+  p.tlas_uniform = desc->tlas_uniform;
+  p.ray_flags = desc->ray_flags;
+  p.cull_mask = desc->cull_mask;
+  p.anyhit_mode = desc->anyhit_mode;
+  p.stack_depth = stack_depth_for(d.max_blas_depth);
+  p.n_binding = (uint32_t)d.tlas_binding.count;
+  p.n_tlas_root = (uint32_t)d.tlas_bvh_root.count;
+  p.tlas_binding = d.tlas_binding.ptr;
+  p.tlas_bvh_root = d.tlas_bvh_root.ptr;
+  p.tlas_forest = d.tlas_bvh_forest.ptr;
+  p.tlas_data = d.tlas_data.ptr;
+  p.tlas_bounding = d.tlas_bounding.ptr;
+  p.blas_meta = d.blas_meta_info.ptr;
+  p.tri_root = d.tri_bvh_root.ptr;
+  p.tri_forest = d.tri_bvh_forest.ptr;
+  p.redirect = d.indices_redirect.ptr;
+  p.tris = reinterpret_cast<const float4*>(d.tri_records.ptr);
+  p.wide = reinterpret_cast<const float4*>(d.wide_nodes.ptr);
+  p.leaves = reinterpret_cast<const uint2*>(d.leaf_ranges.ptr);
+  p.geom_root_code = d.geom_root_code.ptr;
+  p.counters = reinterpret_cast<unsigned long long*>(c->d_counters);
+  p.error_word = c->d_counters + 8;
+  return RDN_OK;
+}
+
+rdn_status validate_trace(rdn_ctx* c, const rdn_trace_desc* desc) {
+  if (!c || !desc) return fail(c, RDN_ERR_INVALID_ARG, "null context or descriptor");
+  if (c->device < 0) return fail(c, RDN_ERR_UNSUPPORTED, "host-only context cannot trace");
+  if (desc->count && (!desc->rays || !desc->hits)) return fail(c, RDN_ERR_INVALID_ARG, "null ray or hit buffer");
+  if ((reinterpret_cast<uintptr_t>(desc->rays) & 15) || (reinterpret_cast<uintptr_t>(desc->hits) & 15) ||
+      (reinterpret_cast<uintptr_t>(desc->hits_ext) & 15))
+    return fail(c, RDN_ERR_INVALID_ARG, "ray and hit buffers must be 16-byte aligned");
+  if (desc->traversal > RDN_TRAVERSAL_REFERENCE) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
+  if (desc->anyhit_mode > RDN_ANYHIT_ACCEPT_EVEN_PRIMS) return fail(c, RDN_ERR_INVALID_ARG, "unknown any-hit mode");
+  if (desc->block_size && (desc->block_size % 32 || desc->block_size > 256))
+    return fail(c, RDN_ERR_INVALID_ARG, "block_size must be a multiple of 32 up to 256");
+  return RDN_OK;
+}
+
+rdn_status ensure_built(rdn_ctx* c) {
+  if (!c->dirty && c->host) return RDN_OK;
+  return do_build(c);
+}
+
+}  // namespace
+
+extern "C" {
+
+uint32_t rdn_api_version(void) { return RDN_API_VERSION; }
+
+rdn_status rdn_create(rdn_ctx** out, int device) {
+  if (!out) return RDN_ERR_INVALID_ARG;
+  *out = nullptr;
+  rdn_ctx* c = new (std::nothrow) rdn_ctx();
+  if (!c) return RDN_ERR_OOM;
+  c->device = device;
+  if (device >= 0) {
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_counters, 64);
+    if (e == cudaSuccess) e = cudaMemset(c->d_counters, 0, 64);
+    if (e != cudaSuccess) {
+      delete c;
+      return e == cudaErrorMemoryAllocation ? RDN_ERR_OOM : RDN_ERR_CUDA;
+    }
+  } else if (device != -1) {
+    delete c;
+    return RDN_ERR_INVALID_ARG;
+  }
+  *out = c;
+  return RDN_OK;
+}
+
+rdn_status rdn_destroy(rdn_ctx* c) {
+  if (!c) return RDN_ERR_INVALID_ARG;
+  if (c->device >= 0) {
+    cudaSetDevice(c->device);
+    cudaDeviceSynchronize();
+    free_device(c->dev);
+    if (c->d_counters) cudaFree(c->d_counters);
+  }
+  delete c;
+  return RDN_OK;
+}
+
+const char* rdn_last_error(const rdn_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+rdn_status rdn_blas_create(rdn_ctx* c, const rdn_geometry* g, uint32_t count, uint32_t* out_handle) {
+  if (!c || !out_handle || (count && !g)) return fail(c, RDN_ERR_INVALID_ARG, "null argument");
+  std::lock_guard<std::mutex> lk(c->lock);
+  auto v = std::make_unique<std::vector<rdn::GeometrySource>>();
+  try {
+    for (uint32_t i = 0; i < count; i++) {
+      rdn::GeometrySource s;
+      s.type = g[i].type;
+      s.flags = g[i].flags;
+      if (s.type > 1) return fail(c, RDN_ERR_INVALID_ARG, "unknown geometry type");
+      if (s.type == 0) {
+        if (g[i].vertex_count && !g[i].positions) return fail(c, RDN_ERR_INVALID_ARG, "null positions");
+        s.positions.assign(g[i].positions, g[i].positions + (size_t)g[i].vertex_count * 3);
+        s.indexed = g[i].indices != nullptr;
+        if (s.indexed) {
+          s.indices.assign(g[i].indices, g[i].indices + g[i].index_count);
+          for (uint32_t k = 0; k < (s.indices.size() / 3) * 3; k++)
+            if (s.indices[k] >= g[i].vertex_count) return fail(c, RDN_ERR_INVALID_ARG, "index out of range");
+        }
+      } else {
+        s.indexed = false;
+      }
+      v->push_back(std::move(s));
+    }
+  } catch (const std::bad_alloc&) {
+    return fail(c, RDN_ERR_OOM, "host allocation failed");
+  }
+  c->blas.push_back(std::move(v));
+  c->dirty = true;
+  *out_handle = (uint32_t)(c->blas.size() - 1);
+  return RDN_OK;
+}
+
+rdn_status rdn_blas_delete(rdn_ctx* c, uint32_t h) {
+  if (!c) return RDN_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(c->lock);
+  if (h >= c->blas.size() || !c->blas[h]) return fail(c, RDN_ERR_INVALID_HANDLE, "no such BLAS");
+  c->blas[h].reset();
+  c->dirty = true;
+  return RDN_OK;
+}
+
+rdn_status rdn_tlas_create(rdn_ctx* c, const rdn_instance* inst, uint32_t count, uint32_t* out_handle) {
+  if (!c || !out_handle || (count && !inst)) return fail(c, RDN_ERR_INVALID_ARG, "null argument");
+  std::lock_guard<std::mutex> lk(c->lock);
+  auto v = std::make_unique<std::vector<rdn::InstanceSource>>();
+  for (uint32_t i = 0; i < count; i++) {
+    rdn::InstanceSource s;
+    std::memcpy(s.transform, inst[i].transform, 64);
+    s.custom_index = inst[i].custom_index;
+    s.mask = inst[i].mask;
+    s.sbt_offset = inst[i].sbt_offset;
+    s.flags = inst[i].flags;
+    s.blas_handle = inst[i].blas_handle;
+    v->push_back(s);
+  }
+  c->tlas.push_back(std::move(v));
+  c->dirty = true;
+  *out_handle = (uint32_t)(c->tlas.size() - 1);
+  return RDN_OK;
+}
+
+rdn_status rdn_tlas_delete(rdn_ctx* c, uint32_t h) {
+  if (!c) return RDN_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(c->lock);
+  if (h >= c->tlas.size() || !c->tlas[h]) return fail(c, RDN_ERR_INVALID_HANDLE, "no such TLAS");
+  c->tlas[h].reset();
+  c->dirty = true;
+  return RDN_OK;
+}
+
+rdn_status rdn_bind_tlas(rdn_ctx* c, const uint32_t* handles, uint32_t count) {
+  if (!c || (count && !handles)) return fail(c, RDN_ERR_INVALID_ARG, "null argument");
+  std::lock_guard<std::mutex> lk(c->lock);
+  std::vector<uint32_t> nb(handles, handles + count);
+  if (nb != c->binding) {
+    c->binding = std::move(nb);
+    c->dirty = true;
+  }
+  return RDN_OK;
+}
+
+rdn_status rdn_build(rdn_ctx* c, const rdn_build_opts* o) {
+  if (!c) return RDN_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(c->lock);
+  rdn::BuildOptions opts;
+  if (o) {
+    if (o->blas_bin_size) opts.blas_bin_size = o->blas_bin_size;
+    if (o->blas_max_depth) opts.blas_max_depth = o->blas_max_depth;
+    if (o->tlas_bin_size) opts.tlas_bin_size = o->tlas_bin_size;
+    if (o->tlas_max_depth) opts.tlas_max_depth = o->tlas_max_depth;
+    opts.host_threads = o->host_threads;
+    if (opts.blas_max_depth > 64 || opts.tlas_max_depth > 64)
+      return fail(c, RDN_ERR_INVALID_ARG, "max tree depth above 64 is not supported");
+  }
+  c->opts = opts;
+  return do_build(c);
+}
+
+rdn_status rdn_build_times(const rdn_ctx* c, double* out2) {
+  if (!c || !out2) return RDN_ERR_INVALID_ARG;
+  out2[0] = c->build_seconds;
+  out2[1] = c->upload_seconds;
+  return RDN_OK;
+}
+
+rdn_status rdn_get_built_array(const rdn_ctx* cc, uint32_t which, void* dst, size_t capacity, size_t* size) {
+  rdn_ctx* c = const_cast<rdn_ctx*>(cc);
+  if (!c || !size) return RDN_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(c->lock);
+  if (!c->host || c->dirty) return fail(c, RDN_ERR_NOT_BUILT, "structure not built");
+  const rdn::HostBuilt& B = *c->host;
+  const void* src = nullptr;
+  size_t bytes = 0;
+#define CASE(i, v)                       \
+  case i:                                \
+    src = B.v.data();                    \
+    bytes = B.v.size() * sizeof(B.v[0]); \
+    break;
+  switch (which) {
+    CASE(0, tlas_binding)
+    CASE(1, tlas_bvh_root)
+    CASE(2, tlas_bvh_forest)
+    CASE(3, tlas_data)
+    CASE(4, tlas_bounding)
+    CASE(5, blas_meta_info)
+    CASE(6, tri_bvh_root)
+    CASE(7, tri_bvh_forest)
+    CASE(8, indices_redirect)
+    CASE(9, indices)
+    CASE(10, vertices)
+    default:
+      return fail(c, RDN_ERR_INVALID_ARG, "unknown array");
+  }
+#undef CASE
+  *size = bytes;
+  if (dst) {
+    if (capacity < bytes) return fail(c, RDN_ERR_INVALID_ARG, "destination too small");
+    if (bytes) std::memcpy(dst, src, bytes);
+  }
+  return RDN_OK;
+}
+
+rdn_status rdn_trace(rdn_ctx* c, const rdn_trace_desc* desc, void* stream) {
+  rdn_status st = validate_trace(c, desc);
+  if (st != RDN_OK) return st;
+  std::lock_guard<std::mutex> lk(c->lock);
+  st = ensure_built(c);
+  if (st != RDN_OK) return st;
+  rdn::TraceParams p;
+  fill_params(c, desc, p);
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e == cudaSuccess)
+    e = rdn::launch_trace(p, desc->traversal == RDN_TRAVERSAL_ORDERED, false, desc->block_size,
+                          static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(c, e, "trace launch");
+  return RDN_OK;
+}
+
+rdn_status rdn_trace_counted(rdn_ctx* c, const rdn_trace_desc* desc, void* stream, rdn_counters* out) {
+  rdn_status st = validate_trace(c, desc);
+  if (st != RDN_OK) return st;
+  if (!out) return fail(c, RDN_ERR_INVALID_ARG, "null counters");
+  std::lock_guard<std::mutex> lk(c->lock);
+  st = ensure_built(c);
+  if (st != RDN_OK) return st;
+  rdn::TraceParams p;
+  fill_params(c, desc, p);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e == cudaSuccess) e = cudaMemsetAsync(c->d_counters, 0, 64, s);
+  if (e == cudaSuccess) e = rdn::launch_trace(p, desc->traversal == RDN_TRAVERSAL_ORDERED, true, desc->block_size, s);
+  uint64_t h[8];
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h, c->d_counters, 64, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(c, e, "counted trace");
+  out->node_visits = h[0];
+  out->tri_tests = h[1];
+  out->tri_hits = h[2];
+  out->bad_tlas_rays = h[3];
+  return RDN_OK;
+}
+
+}  // extern "C"

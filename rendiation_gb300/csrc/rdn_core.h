@@ -1,0 +1,160 @@
+// Internal types of librdn: host-side acceleration-structure system and the
+// device layouts it uploads. Host float code here must be compiled with
+// -ffp-contract=off so that every f32 value it precomputes equals the value the
+// reference computes at run time (Rust never fuses multiply-adds).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/rdn.h"
+
+namespace rdn {
+
+static const uint32_t INVALID_NEXT = 0xFFFFFFFFu;
+
+struct f3 {
+  float x, y, z;
+};
+struct Box {
+  f3 lo, hi;
+};
+
+// ---- reference flattened layout (naive/mod.rs:22-71), bit-compatible ----
+struct DeviceBVHNode {
+  float aabb_min[3];
+  uint32_t hit_next;
+  float aabb_max[3];
+  uint32_t miss_next;
+  uint32_t content_range[2];
+  uint32_t tail[2];
+};
+static_assert(sizeof(DeviceBVHNode) == 48, "48 B node");
+struct DeviceInstance {
+  float transform[16];
+  float transform_inv[16];
+  uint32_t instance_custom_index;
+  uint32_t sbt_offset;
+  uint32_t flags;
+  uint32_t acceleration_structure_handle;
+};
+static_assert(sizeof(DeviceInstance) == 144, "144 B instance");
+struct TlasBounding {
+  float world_min[3];
+  uint32_t mask;
+  float world_max[3];
+  uint32_t flags;
+};
+struct BlasMetaInfo {
+  uint32_t tri_root_range[2];
+};
+struct GeometryMetaInfo {
+  uint32_t bvh_root_idx, geometry_idx, primitive_start, geometry_flags;
+};
+
+// ---- GB300 layout ----
+// Precomputed triangle, 64 B, in BVH-sorted order (same index space as the
+// reference's content_range / indices_redirect):
+//   q0 = (v0.xyz, n.x)  q1 = (e1.xyz, n.y)  q2 = (e2.xyz, n.z)  q3 = (uu, uv, vv, inv_d)
+// with e1 = v1-v0, e2 = v2-v0, n = normalize(cross(e1,e2)), uu = e1.e1,
+// uv = e1.e2, vv = e2.e2, inv_d = 1/(uv*uv - uu*vv): exactly the f32 values the
+// reference's intersect_ray_triangle_cpu computes per test (geometry/mod.rs:115-144).
+struct TriRecord {
+  float q[16];
+};
+static_assert(sizeof(TriRecord) == 64, "64 B triangle");
+// Two-child node, 64 B: children's boxes and child codes.
+//   w0 = (c0.lo.x, c0.lo.y, c0.lo.z, c0.hi.x)  w1 = (c0.hi.y, c0.hi.z, c1.lo.x, c1.lo.y)
+//   w2 = (c1.lo.z, c1.hi.x, c1.hi.y, c1.hi.z)  w3 = (code0, code1, 0, 0)
+// code: bit 31 clear = index of a child WideNode, set = index of a leaf range.
+struct WideNode {
+  float w[12];
+  uint32_t code[4];
+};
+static_assert(sizeof(WideNode) == 64, "64 B node");
+static const uint32_t LEAF_BIT = 0x80000000u;
+
+struct GeometrySource {
+  uint32_t type;
+  uint32_t flags;
+  std::vector<float> positions;
+  bool indexed;
+  std::vector<uint32_t> indices;
+};
+struct InstanceSource {
+  float transform[16];
+  uint32_t custom_index, mask, sbt_offset, flags, blas_handle;
+};
+
+// Host copy of everything a build produces.
+struct HostBuilt {
+  // reference layout
+  std::vector<uint32_t> tlas_binding;
+  std::vector<uint32_t> tlas_bvh_root;
+  std::vector<DeviceBVHNode> tlas_bvh_forest;
+  std::vector<DeviceInstance> tlas_data;
+  std::vector<TlasBounding> tlas_bounding;
+  std::vector<BlasMetaInfo> blas_meta_info;
+  std::vector<GeometryMetaInfo> tri_bvh_root;
+  std::vector<DeviceBVHNode> tri_bvh_forest;
+  std::vector<uint32_t> indices_redirect;
+  std::vector<uint32_t> indices;
+  std::vector<float> vertices;
+  // GB300 layout
+  std::vector<TriRecord> tri_records;
+  std::vector<WideNode> wide_nodes;
+  std::vector<uint32_t> leaf_ranges;  // 2 per leaf: [start, end)
+  std::vector<uint32_t> geom_root_code;  // per tri_bvh_root entry
+  uint32_t max_blas_depth = 0;
+  uint64_t sah_splits = 0, median_fallbacks = 0;
+};
+
+template <class T>
+struct DevBuf {
+  T* ptr = nullptr;
+  size_t count = 0;
+};
+
+struct DeviceBuilt {
+  DevBuf<uint32_t> tlas_binding, tlas_bvh_root, indices_redirect, leaf_ranges, geom_root_code;
+  DevBuf<DeviceBVHNode> tlas_bvh_forest, tri_bvh_forest;
+  DevBuf<DeviceInstance> tlas_data;
+  DevBuf<TlasBounding> tlas_bounding;
+  DevBuf<BlasMetaInfo> blas_meta_info;
+  DevBuf<GeometryMetaInfo> tri_bvh_root;
+  DevBuf<TriRecord> tri_records;
+  DevBuf<WideNode> wide_nodes;
+  uint32_t max_blas_depth = 0;
+  uint64_t bytes = 0;
+};
+
+struct BuildOptions {
+  uint32_t blas_bin_size = 2, blas_max_depth = 50, tlas_bin_size = 10, tlas_max_depth = 50, host_threads = 0;
+};
+
+// Builds the whole structure from the sources (reference: NaiveSahBvhSource::build,
+// naive/mod.rs:322-494). Returns an empty string on success, else the error.
+std::string build_host(const std::vector<std::unique_ptr<std::vector<GeometrySource>>>& blas,
+                       const std::vector<std::unique_ptr<std::vector<InstanceSource>>>& tlas,
+                       const std::vector<uint32_t>& binding, const BuildOptions& opt, HostBuilt& out);
+
+}  // namespace rdn
+
+struct rdn_ctx {
+  std::mutex lock;
+  int device = -1;
+  std::vector<std::unique_ptr<std::vector<rdn::GeometrySource>>> blas;
+  std::vector<std::unique_ptr<std::vector<rdn::InstanceSource>>> tlas;
+  std::vector<uint32_t> binding;
+  rdn::BuildOptions opts;
+  bool dirty = true;
+  std::unique_ptr<rdn::HostBuilt> host;
+  rdn::DeviceBuilt dev;
+  uint32_t* d_counters = nullptr;  // 4 x u64 counters + error words
+  double build_seconds = 0.0, upload_seconds = 0.0;
+  std::string err;
+};

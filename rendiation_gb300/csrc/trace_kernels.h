@@ -1,0 +1,37 @@
+// Launch interface of the ray-query kernels (trace.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "rdn_core.h"
+
+namespace rdn {
+
+struct TraceParams {
+  const float4* rays;  // 2 per ray (rdn_ray)
+  rdn_hit* hits;
+  rdn_hit_ext* hits_ext;
+  const uint32_t* tlas_idx;
+  uint32_t count, tlas_uniform, ray_flags, cull_mask, anyhit_mode, stack_depth;
+  uint32_t n_binding, n_tlas_root;
+  const uint32_t* tlas_binding;
+  const uint32_t* tlas_bvh_root;
+  const DeviceBVHNode* tlas_forest;
+  const DeviceInstance* tlas_data;
+  const TlasBounding* tlas_bounding;
+  const BlasMetaInfo* blas_meta;
+  const GeometryMetaInfo* tri_root;
+  const DeviceBVHNode* tri_forest;
+  const uint32_t* redirect;
+  const float4* tris;   // 4 per triangle (TriRecord)
+  const float4* wide;   // 4 per node (WideNode)
+  const uint2* leaves;
+  const uint32_t* geom_root_code;
+  unsigned long long* counters;  // 4 x u64, used by counted launches
+  uint32_t* error_word;          // bit 0 stack overflow, bit 1 bad tlas index
+};
+
+cudaError_t launch_trace(const TraceParams& p, bool ordered, bool counted, uint32_t block, cudaStream_t stream);
+
+}  // namespace rdn

@@ -1,0 +1,103 @@
+"""ctypes binding of librdn.so (include/rdn.h).
+
+The library is built in-tree by ``rendiation_gb300.build_native.build()``.
+Loading fails loudly when it is missing: there is no CPU fallback for any
+query in this package.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "librdn.so")
+
+RDN_OK = 0
+STATUS_NAMES = {
+    0: "RDN_OK", -1: "RDN_ERR_INVALID_ARG", -2: "RDN_ERR_INVALID_HANDLE", -3: "RDN_ERR_OOM", -4: "RDN_ERR_CUDA",
+    -5: "RDN_ERR_QUEUE_OVERFLOW", -6: "RDN_ERR_TIMEOUT", -7: "RDN_ERR_NOT_BUILT", -8: "RDN_ERR_UNSUPPORTED",
+}
+
+# every symbol include/rdn.h declares; tests check the library exports each one
+EXPORTED_SYMBOLS = [
+    "rdn_api_version", "rdn_create", "rdn_destroy", "rdn_last_error", "rdn_blas_create", "rdn_blas_delete",
+    "rdn_tlas_create", "rdn_tlas_delete", "rdn_bind_tlas", "rdn_build", "rdn_build_times", "rdn_get_built_array",
+    "rdn_trace", "rdn_trace_counted",
+]
+
+
+class RdnError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+class Geometry(C.Structure):
+    _fields_ = [("type", C.c_uint32), ("flags", C.c_uint32), ("positions", C.c_void_p), ("vertex_count", C.c_uint32),
+                ("index_count", C.c_uint32), ("indices", C.c_void_p)]
+
+
+class Instance(C.Structure):
+    _fields_ = [("transform", C.c_float * 16), ("custom_index", C.c_uint32), ("mask", C.c_uint32),
+                ("sbt_offset", C.c_uint32), ("flags", C.c_uint32), ("blas_handle", C.c_uint32)]
+
+
+class BuildOpts(C.Structure):
+    _fields_ = [("blas_bin_size", C.c_uint32), ("blas_max_depth", C.c_uint32), ("tlas_bin_size", C.c_uint32),
+                ("tlas_max_depth", C.c_uint32), ("host_threads", C.c_uint32), ("reserved", C.c_uint32 * 3)]
+
+
+class TraceDesc(C.Structure):
+    _fields_ = [("rays", C.c_void_p), ("hits", C.c_void_p), ("hits_ext", C.c_void_p), ("tlas_idx", C.c_void_p),
+                ("count", C.c_uint32), ("tlas_uniform", C.c_uint32), ("ray_flags", C.c_uint32),
+                ("cull_mask", C.c_uint32), ("traversal", C.c_uint32), ("anyhit_mode", C.c_uint32),
+                ("block_size", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+class Counters(C.Structure):
+    _fields_ = [("node_visits", C.c_uint64), ("tri_tests", C.c_uint64), ("tri_hits", C.c_uint64),
+                ("bad_tlas_rays", C.c_uint64)]
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(
+            f"{LIB_PATH} is missing: build it with rendiation_gb300.build_native.build() (nvcc, sm_103a)")
+    L = C.CDLL(LIB_PATH)
+    vp, u32, i32 = C.c_void_p, C.c_uint32, C.c_int32
+    L.rdn_api_version.restype = u32
+    L.rdn_create.argtypes = [C.POINTER(vp), C.c_int]
+    L.rdn_create.restype = i32
+    L.rdn_destroy.argtypes = [vp]
+    L.rdn_destroy.restype = i32
+    L.rdn_last_error.argtypes = [vp]
+    L.rdn_last_error.restype = C.c_char_p
+    L.rdn_blas_create.argtypes = [vp, vp, u32, C.POINTER(u32)]
+    L.rdn_blas_create.restype = i32
+    L.rdn_blas_delete.argtypes = [vp, u32]
+    L.rdn_blas_delete.restype = i32
+    L.rdn_tlas_create.argtypes = [vp, vp, u32, C.POINTER(u32)]
+    L.rdn_tlas_create.restype = i32
+    L.rdn_tlas_delete.argtypes = [vp, u32]
+    L.rdn_tlas_delete.restype = i32
+    L.rdn_bind_tlas.argtypes = [vp, vp, u32]
+    L.rdn_bind_tlas.restype = i32
+    L.rdn_build.argtypes = [vp, vp]
+    L.rdn_build.restype = i32
+    L.rdn_build_times.argtypes = [vp, vp]
+    L.rdn_build_times.restype = i32
+    L.rdn_get_built_array.argtypes = [vp, u32, vp, C.c_size_t, C.POINTER(C.c_size_t)]
+    L.rdn_get_built_array.restype = i32
+    L.rdn_trace.argtypes = [vp, C.POINTER(TraceDesc), vp]
+    L.rdn_trace.restype = i32
+    L.rdn_trace_counted.argtypes = [vp, C.POINTER(TraceDesc), vp, C.POINTER(Counters)]
+    L.rdn_trace_counted.restype = i32
+    _lib = L
+    return L

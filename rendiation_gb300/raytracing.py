@@ -1,0 +1,206 @@
+"""Host-side mirror of the reference's acceleration-structure and trace interfaces.
+
+``AccelerationStructureSystem`` mirrors ``GPUAccelerationStructureSystemProvider``
+(shader/ray-tracing/src/api/backend.rs:120-142) as implemented by the naive SAH
+system (shader/ray-tracing/src/backend/wavefront_compute/geometry/naive/mod.rs:560-609):
+same method names, same argument meaning, dense handles, deleted slots stay
+empty. Queries run through librdn's CUDA kernels via the C ABI (include/rdn.h);
+device buffers are torch CUDA tensors (plumbing only).
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import native
+
+# flags (shader/ray-tracing/src/api/ty.rs:102-159)
+RAY_FLAG_NONE = 0x00
+RAY_FLAG_FORCE_OPAQUE = 0x01
+RAY_FLAG_FORCE_NON_OPAQUE = 0x02
+RAY_FLAG_ACCEPT_FIRST_HIT_AND_END_SEARCH = 0x04
+RAY_FLAG_SKIP_CLOSEST_HIT_SHADER = 0x08
+RAY_FLAG_CULL_BACK_FACING_TRIANGLES = 0x10
+RAY_FLAG_CULL_FRONT_FACING_TRIANGLES = 0x20
+RAY_FLAG_CULL_OPAQUE = 0x40
+RAY_FLAG_CULL_NON_OPAQUE = 0x80
+RAY_FLAG_SKIP_TRIANGLES = 0x100
+GEOMETRY_INSTANCE_TRIANGLE_FACING_CULL_DISABLE = 0x1
+GEOMETRY_INSTANCE_TRIANGLE_FLIP_FACING = 0x2
+GEOMETRY_INSTANCE_FORCE_OPAQUE = 0x4
+GEOMETRY_INSTANCE_FORCE_NO_OPAQUE = 0x8
+GEOMETRY_FLAG_OPAQUE = 0x1
+HIT_KIND_FRONT_FACING_TRIANGLE = 0xFE
+HIT_KIND_BACK_FACING_TRIANGLE = 0xFF
+MISS = 0xFFFFFFFF
+
+TRAVERSAL_ORDERED = 0
+TRAVERSAL_REFERENCE = 1
+ANYHIT_ACCEPT = 0
+ANYHIT_ACCEPT_AND_END = 1
+ANYHIT_ACCEPT_EVEN_PRIMS = 2
+
+# built-array ids of rdn_get_built_array
+BUILT_ARRAYS = ["tlas_binding", "tlas_bvh_root", "tlas_bvh_forest", "tlas_data", "tlas_bounding",
+                "blas_meta_info", "tri_bvh_root", "tri_bvh_forest", "indices_redirect", "indices", "vertices"]
+
+
+@dataclass
+class BottomLevelAccelerationStructureBuildSource:
+    """Triangles: positions (V,3) f32, optional u32 indices (None = non-indexed)."""
+
+    positions: np.ndarray
+    indices: np.ndarray | None = None
+    flags: int = GEOMETRY_FLAG_OPAQUE
+
+
+@dataclass
+class TopLevelAccelerationStructureSourceInstance:
+    """transform: Mat4 in the reference's element order (columns; translation at 12..14)."""
+
+    acceleration_structure_handle: int
+    transform: np.ndarray = field(default_factory=lambda: np.eye(4, dtype=np.float32).reshape(-1))
+    instance_custom_index: int = 0
+    mask: int = 0xFF
+    instance_shader_binding_table_record_offset: int = 0
+    flags: int = 0
+
+
+def _check(ctx, status: int):
+    if status != native.RDN_OK:
+        msg = native.lib().rdn_last_error(ctx).decode() if ctx else ""
+        raise native.RdnError(status, msg)
+
+
+class AccelerationStructureSystem:
+    """One librdn context. device=-1 gives a host-only system (build + export, no trace)."""
+
+    def __init__(self, device: int = 0):
+        self._L = native.lib()
+        h = C.c_void_p()
+        st = self._L.rdn_create(C.byref(h), device)
+        if st != native.RDN_OK:
+            raise native.RdnError(st, f"rdn_create(device={device}) failed")
+        self._h = h
+        self.device = device
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.rdn_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # --- GPUAccelerationStructureSystemProvider ---
+    def bind_tlas_max_len(self) -> int:
+        return 0xFFFFFFFF
+
+    def create_bottom_level_acceleration_structure(self, sources) -> int:
+        arr = (native.Geometry * len(sources))()
+        keep = []
+        for g, s in zip(arr, sources):
+            pos = np.ascontiguousarray(s.positions, np.float32).reshape(-1, 3)
+            keep.append(pos)
+            g.type = 0
+            g.flags = s.flags
+            g.positions = pos.ctypes.data
+            g.vertex_count = pos.shape[0]
+            if s.indices is not None:
+                idx = np.ascontiguousarray(s.indices, np.uint32).reshape(-1)
+                keep.append(idx)
+                g.indices = idx.ctypes.data
+                g.index_count = idx.shape[0]
+        out = C.c_uint32()
+        _check(self._h, self._L.rdn_blas_create(self._h, C.addressof(arr), len(sources), C.byref(out)))
+        return out.value
+
+    def delete_bottom_level_acceleration_structure(self, handle: int):
+        _check(self._h, self._L.rdn_blas_delete(self._h, handle))
+
+    def create_top_level_acceleration_structure(self, instances) -> int:
+        arr = (native.Instance * len(instances))()
+        for d, s in zip(arr, instances):
+            tf = np.asarray(s.transform, np.float32).reshape(-1)
+            for k in range(16):
+                d.transform[k] = float(tf[k])
+            d.custom_index = s.instance_custom_index
+            d.mask = s.mask
+            d.sbt_offset = s.instance_shader_binding_table_record_offset
+            d.flags = s.flags
+            d.blas_handle = s.acceleration_structure_handle
+        out = C.c_uint32()
+        _check(self._h, self._L.rdn_tlas_create(self._h, C.addressof(arr), len(instances), C.byref(out)))
+        return out.value
+
+    def delete_top_level_acceleration_structure(self, handle: int):
+        _check(self._h, self._L.rdn_tlas_delete(self._h, handle))
+
+    def bind_tlas(self, handles):
+        a = np.ascontiguousarray(handles, np.uint32)
+        _check(self._h, self._L.rdn_bind_tlas(self._h, a.ctypes.data, a.shape[0]))
+
+    # --- build / inspection ---
+    def build(self, blas_bin_size=0, blas_max_depth=0, tlas_bin_size=0, tlas_max_depth=0, host_threads=0):
+        o = native.BuildOpts(blas_bin_size, blas_max_depth, tlas_bin_size, tlas_max_depth, host_threads)
+        _check(self._h, self._L.rdn_build(self._h, C.byref(o)))
+
+    def build_times(self) -> tuple[float, float]:
+        t = (C.c_double * 2)()
+        _check(self._h, self._L.rdn_build_times(self._h, t))
+        return t[0], t[1]
+
+    def built_array(self, name: str) -> bytes:
+        which = BUILT_ARRAYS.index(name)
+        size = C.c_size_t()
+        _check(self._h, self._L.rdn_get_built_array(self._h, which, None, 0, C.byref(size)))
+        buf = (C.c_uint8 * max(1, size.value))()
+        _check(self._h, self._L.rdn_get_built_array(self._h, which, buf, size.value, C.byref(size)))
+        return bytes(buf)[: size.value]
+
+    # --- queries ---
+    def _desc(self, rays, hits, hits_ext, tlas_idx, ray_flags, cull_mask, tlas_uniform, traversal, anyhit_mode,
+              block_size, count=None):
+        n = rays.shape[0] if count is None else count
+        return native.TraceDesc(rays.data_ptr(), hits.data_ptr(), 0 if hits_ext is None else hits_ext.data_ptr(),
+                                0 if tlas_idx is None else tlas_idx.data_ptr(), n, tlas_uniform, ray_flags,
+                                cull_mask, traversal, anyhit_mode, block_size, 0)
+
+    def trace(self, rays, hits, hits_ext=None, tlas_idx=None, ray_flags=0, cull_mask=0xFF, tlas_uniform=0,
+              traversal=TRAVERSAL_ORDERED, anyhit_mode=ANYHIT_ACCEPT, block_size=0, stream=None, count=None):
+        """rays: CUDA f32 tensor (N, 8); hits: CUDA f32 tensor (N, 4) (prim id stored as u32 bits);
+        hits_ext: optional CUDA int32 tensor (N, 4); tlas_idx: optional CUDA int32 tensor (N,).
+        count overrides N (e.g. 0 for an empty batch)."""
+        import torch
+
+        d = self._desc(rays, hits, hits_ext, tlas_idx, ray_flags, cull_mask, tlas_uniform, traversal, anyhit_mode,
+                       block_size, count)
+        s = (stream or torch.cuda.current_stream()).cuda_stream
+        _check(self._h, self._L.rdn_trace(self._h, C.byref(d), C.c_void_p(s)))
+
+    def trace_counted(self, rays, hits, hits_ext=None, tlas_idx=None, ray_flags=0, cull_mask=0xFF, tlas_uniform=0,
+                      traversal=TRAVERSAL_ORDERED, anyhit_mode=ANYHIT_ACCEPT, block_size=0, stream=None) -> dict:
+        import torch
+
+        d = self._desc(rays, hits, hits_ext, tlas_idx, ray_flags, cull_mask, tlas_uniform, traversal, anyhit_mode,
+                       block_size)
+        s = (stream or torch.cuda.current_stream()).cuda_stream
+        c = native.Counters()
+        _check(self._h, self._L.rdn_trace_counted(self._h, C.byref(d), C.c_void_p(s), C.byref(c)))
+        return {"node_visits": c.node_visits, "tri_tests": c.tri_tests, "tri_hits": c.tri_hits,
+                "bad_tlas_rays": c.bad_tlas_rays}
+
+
+def hits_to_numpy(hits) -> np.ndarray:
+    """(N,4) f32 CUDA tensor -> structured array (t, u, v, prim)."""
+    h = hits.detach().cpu().numpy().astype(np.float32, copy=False)
+    out = np.zeros(h.shape[0], dtype=[("t", np.float32), ("u", np.float32), ("v", np.float32), ("prim", np.uint32)])
+    out["t"], out["u"], out["v"] = h[:, 0], h[:, 1], h[:, 2]
+    out["prim"] = h[:, 3].view(np.uint32)
+    return out
