@@ -1,0 +1,418 @@
+"""Benchmark of the GB300 ray-query path.
+
+Default workload ("wavefront"): heightfield on a 1024x1024 vertex grid
+(2,093,058 triangles, SAH build with <= 4 primitives per leaf), 1920x1080
+pinhole primary rays from (0.5,-0.5,0.8) aimed at the grid centre, then per hit
+one any-hit shadow ray to a point light at (0.2,0.2,2.0) and one
+cosine-weighted diffuse bounce ray. One step = one frame of the wavefront
+executor (rdn_wavefront_shadow_bounce). Metric: Mrays/s over all rays traced.
+
+Other workloads: "plain" (10k-triangle soup, 256x256 pinhole closest-hit rays,
+rdn_trace with host rays).
+
+--impl reference times the reference's CPU path for the same workload: the
+oracle (a C++ restatement of the reference's CPU traversal, the Rust reference
+cannot be built here) on all host cores over a bounded sample of the frame.
+
+Multi-GPU: rays and frames are independent, so N ranks run N replicas of the
+workload (weak scaling, no collective on the data path); the timed region is
+bracketed by barriers and the max over ranks is reported.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+LIGHT = (0.2, 0.2, 2.0)
+METRIC = "Mrays/s closest-hit: batched & fwd+adjoint vs plain, at stated FP64 error"
+
+
+def node_bytes_per_ray(counts: dict, n: int) -> float:
+    """Algorithmic bytes per ray: 32 (ray in) + 16 (hit out) + 48 per node visit
+    + 36 per triangle test, visits and tests counted in the reference's traversal
+    order on the reference-built BVH."""
+    return 32.0 + 16.0 + 48.0 * counts["node_visits"] / n + 36.0 * counts["tri_tests"] / n
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def measured_peak_gbs():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_from_profile(workload: str, kernel: str):
+    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    e = d.get(workload, {}).get(kernel)
+    return None if e is None else float(e["dram_bytes_per_launch"])
+
+
+# --------------------------------------------------------------------------- workloads
+
+def build_heightfield_system(n_grid: int):
+    from rendiation_gb300 import raytracing as rt
+    from rendiation_gb300 import scenes
+
+    mesh = scenes.heightfield(n_grid, seed=1)
+    P = rt.AccelerationStructureSystem(device=0)
+    b = P.create_bottom_level_acceleration_structure([rt.BottomLevelAccelerationStructureBuildSource(
+        mesh.positions, mesh.indices)])
+    t = P.create_top_level_acceleration_structure([rt.TopLevelAccelerationStructureSourceInstance(b)])
+    P.bind_tlas([t])
+    P.build(blas_bin_size=4)
+    return mesh, P
+
+
+def reference_counts_of_queues(P, wf, n_secondary):
+    """Reference-order node visits / triangle tests of the rays one frame traced:
+    the primaries (regenerated on the host, bit-identical to the kernel's camera
+    rays) and the shadow and bounce queues read back from the scratch."""
+    import torch
+
+    from rendiation_gb300 import raytracing as rt
+    from rendiation_gb300 import scenes
+
+    prim = scenes.pinhole_rays(wf.camera)
+    d_prim = torch.from_numpy(prim.view(np.float32).reshape(-1, 8).copy()).cuda()
+    hits = torch.empty((prim.shape[0], 4), dtype=torch.float32, device="cuda")
+    c_prim = P.trace_counted(d_prim, hits, traversal=rt.TRAVERSAL_REFERENCE)
+    n = wf.n
+    base = wf.scratch_ptr - wf.scratch.data_ptr()
+    up = lambda b: (b + 255) & ~255  # noqa: E731
+    sh = wf.scratch[base + 256: base + 256 + n_secondary * 32].view(torch.float32).reshape(-1, 8)
+    bo_off = base + 256 + up(n * 32)
+    bo = wf.scratch[bo_off: bo_off + n_secondary * 32].view(torch.float32).reshape(-1, 8)
+    h2 = torch.empty((max(1, n_secondary), 4), dtype=torch.float32, device="cuda")
+    c_sh = P.trace_counted(sh.contiguous(), h2, traversal=rt.TRAVERSAL_REFERENCE,
+                           ray_flags=rt.RAY_FLAG_ACCEPT_FIRST_HIT_AND_END_SEARCH)
+    c_bo = P.trace_counted(bo.contiguous(), h2, traversal=rt.TRAVERSAL_REFERENCE)
+    return c_prim, c_sh, c_bo
+
+
+def bench_wavefront(args, ws, rank):
+    import torch
+
+    from rendiation_gb300 import raytracing as rt
+    from rendiation_gb300 import scenes
+
+    W, H = args.width, args.height
+    mesh, P = build_heightfield_system(args.grid)
+    cam = scenes.heightfield_camera(W, H)
+    traversal = rt.TRAVERSAL_REFERENCE if args.traversal == "reference" else rt.TRAVERSAL_ORDERED
+    wf = rt.Wavefront(P, cam, LIGHT, traversal=traversal, block_size=args.block)
+    stream = torch.cuda.current_stream()
+
+    # one frame to learn the ray counts, then the reference-order visit counts of those rays
+    wf.run(0)
+    torch.cuda.synchronize()
+    n_prim, n_sh, n_bo = wf.rays_traced()
+    rays_per_step = n_prim + n_sh + n_bo
+    c_prim, c_sh, c_bo = reference_counts_of_queues(P, wf, n_sh)
+    bytes_primary = n_prim * node_bytes_per_ray(c_prim, n_prim)
+    bytes_secondary = n_sh * node_bytes_per_ray(c_sh, max(1, n_sh)) + n_bo * node_bytes_per_ray(c_bo, max(1, n_bo))
+
+    for s in range(args.warmup):
+        wf.run(1 + s)
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+
+    # device-timed region: K frames, events around every kernel launch pair
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+        start.record(stream)
+        for s in range(args.steps):
+            ev[s][0].record(stream)
+            wf.run(100 + s)
+            ev[s][1].record(stream)
+        stop.record(stream)
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+    total_ms = start.elapsed_time(stop)
+
+    # per-kernel split of a frame, outside the timed region: events on the
+    # launching stream around the primary kernel and the secondary kernel
+    import ctypes as C
+
+    k_prim, k_sec = [], []
+    for s in range(max(3, min(args.steps, 10))):
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record(stream)
+        wf.run(200 + s, phases=1)
+        e1.record(stream)
+        wf.run(200 + s, phases=2)
+        e2.record(stream)
+        torch.cuda.synchronize()
+        k_prim.append(e0.elapsed_time(e1))
+        k_sec.append(e1.elapsed_time(e2))
+    prim_ms, sec_ms = float(np.mean(k_prim)), float(np.mean(k_sec))
+    frame_ms = total_ms / args.steps
+    elapsed = total_ms / 1000.0
+    if ws > 1:
+        t = torch.tensor([elapsed], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        elapsed = float(t.item())
+    value = rays_per_step * args.steps * ws / elapsed / 1e6
+
+    # e2e through the C ABI: each step launches the frame and reads the pixel
+    # records back into pinned host memory
+    host_out = torch.empty(wf.out.shape, dtype=wf.out.dtype, pin_memory=True)
+    for s in range(2):
+        wf.run(300 + s)
+        host_out.copy_(wf.out, non_blocking=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for s in range(args.steps):
+        wf.run(400 + s)
+        host_out.copy_(wf.out, non_blocking=True)
+        stream.synchronize()
+    e2e_s = time.perf_counter() - t0
+    e2e_value = rays_per_step * args.steps / e2e_s / 1e6
+    d2h = int(wf.out.numel() * 4)
+    h2d = C.sizeof(wf.desc)
+
+    peak, peak_kind = measured_peak_gbs()
+    if sec_ms >= prim_ms:
+        dom_name, dom_bytes, dom_ms = "secondary_kernel (shadow + bounce queues)", bytes_secondary, sec_ms
+    else:
+        dom_name, dom_bytes, dom_ms = "primary_kernel (raygen + trace + shade + enqueue)", bytes_primary, prim_ms
+    achieved = dom_bytes / (dom_ms / 1000.0) / 1e9
+    out = {
+        "metric": METRIC,
+        "value": round(value, 3),
+        "unit": "Mrays/s",
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(frame_ms, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded heightfield, PCG64 seed 1)",
+        "config": {
+            "workload": f"wavefront primary+shadow+bounce, heightfield {args.grid}^2 "
+                        f"({mesh.triangle_count} tris, SAH <=4/leaf), {W}x{H} primaries",
+            "rays_per_step": rays_per_step,
+            "rays_primary": n_prim, "rays_shadow": n_sh, "rays_bounce": n_bo,
+            "traversal": args.traversal,
+            "l2": f"no flush: acceleration structure {P.device_bytes() / 1e6:.0f} MB on device > 129 MB L2",
+        },
+        "e2e": {"value": round(e2e_value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": 2 * args.steps,
+        "roofline": {
+            "bound": "hbm",
+            "achieved": round(achieved, 1),
+            "peak": peak,
+            "unit": "GB/s",
+            "frac": round(achieved / peak, 4),
+            "traffic": traffic_from_profile("wavefront", dom_name.split()[0]),
+            "kernel": dom_name,
+            "kernel_ms": round(dom_ms, 4),
+            "kernel_ms_split": {"primary": round(prim_ms, 4), "secondary": round(sec_ms, 4)},
+            "algorithmic_bytes_per_launch": int(dom_bytes),
+            "bytes_per_ray": {"primary": round(node_bytes_per_ray(c_prim, n_prim), 1),
+                              "shadow": round(node_bytes_per_ray(c_sh, max(1, n_sh)), 1),
+                              "bounce": round(node_bytes_per_ray(c_bo, max(1, n_bo)), 1)},
+            "peak_kind": peak_kind,
+        },
+        "clocks": clk.summary(),
+    }
+    return out, P, mesh, cam
+
+
+def oracle_heightfield(mesh):
+    from oracle import orc
+
+    S = orc.OracleSystem()
+    b = S.create_blas([(mesh.positions, mesh.indices, 1)])
+    t = S.create_tlas([{"blas": b}])
+    S.bind_tlas([t])
+    S.build(blas_bin_size=4)
+    return S
+
+
+def cpu_baseline_wavefront(S, cam, threads: int, budget_s: float, steps: int = 1):
+    """The oracle's pipeline on host cores over a bounded band of rows (BVH built beforehand)."""
+    from oracle import orc
+
+    W, H = cam.width, cam.height
+    # calibrate on a small band around the image centre, then size the sample
+    r0 = H // 2 - 4
+    _, rays, sec = orc.wavefront_shadow_bounce(S, cam.as_floats(), W, H, LIGHT, 0, row0=r0, row1=r0 + 8,
+                                               threads=threads)
+    rate = sum(rays) / max(sec, 1e-6)
+    rows = int(max(8, min(H, budget_s * rate / max(1.0, sum(rays) / 8.0))))
+    r0 = max(0, H // 2 - rows // 2)
+    results = []
+    for s in range(steps):
+        _, rays, sec = orc.wavefront_shadow_bounce(S, cam.as_floats(), W, H, LIGHT, s, row0=r0, row1=r0 + rows,
+                                                   threads=threads)
+        results.append((sum(rays), sec))
+    total_rays = sum(r for r, _ in results)
+    total_s = sum(s for _, s in results)
+    return {"value": round(total_rays / total_s / 1e6, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
+            "sample": f"rows {r0}..{r0 + rows} of the {W}x{H} frame ({total_rays // steps} rays per step)"}, total_s
+
+
+def run_reference(args, ws, rank):
+    """--impl reference: the oracle port of the reference's CPU path on all host threads."""
+    if rank != 0:
+        return None
+    from rendiation_gb300 import scenes
+
+    threads = os.cpu_count() or 1
+    mesh = scenes.heightfield(args.grid, seed=1)
+    cam = scenes.heightfield_camera(args.width, args.height)
+    S = oracle_heightfield(mesh)
+    for _ in range(args.warmup):
+        cpu_baseline_wavefront(S, cam, threads, budget_s=1.0)
+    cb, total_s = cpu_baseline_wavefront(S, cam, threads, budget_s=args.cpu_budget / max(1, args.steps),
+                                         steps=args.steps)
+    return {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": cb["value"],
+        "unit": "Mrays/s",
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(total_s * 1000.0 / args.steps, 3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded heightfield, PCG64 seed 1)",
+        "config": {"workload": f"wavefront primary+shadow+bounce, heightfield {args.grid}^2, "
+                               f"{args.width}x{args.height} primaries (bounded row sample per step)"},
+        "cpu_baseline": cb,
+        "e2e": {"value": cb["value"], "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="wavefront", choices=["wavefront"])
+    ap.add_argument("--grid", type=int, default=1024)
+    ap.add_argument("--width", type=int, default=1920)
+    ap.add_argument("--height", type=int, default=1080)
+    ap.add_argument("--traversal", default="ordered", choices=["ordered", "reference"])
+    ap.add_argument("--block", type=int, default=0)
+    ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU work for the CPU baseline")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        out = run_reference(args, ws, rank)
+        if out is not None:
+            print(json.dumps(out), flush=True)
+        return
+
+    import torch
+
+    torch.cuda.set_device(local)
+    if ws > 1:
+        torch.distributed.init_process_group("nccl")
+    out, P, mesh, cam = bench_wavefront(args, ws, rank)
+    if rank == 0:
+        if not args.no_cpu_baseline:
+            cb, _ = cpu_baseline_wavefront(oracle_heightfield(mesh), cam, os.cpu_count() or 1,
+                                           budget_s=args.cpu_budget)
+            out["cpu_baseline"] = cb
+        print(json.dumps(out), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

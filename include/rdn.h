@@ -211,8 +211,19 @@ rdn_status rdn_bind_tlas(rdn_ctx* ctx, const uint32_t* handles, uint32_t count);
  * get_or_build_gpu_data, naive/mod.rs:521-537; rdn_trace does the same when
  * the structure is dirty). opts may be NULL. */
 rdn_status rdn_build(rdn_ctx* ctx, const rdn_build_opts* opts);
-/* Seconds spent in the last build: [0] host BVH build + flattening, [1] upload. */
-rdn_status rdn_build_times(const rdn_ctx* ctx, double* out2);
+/* Statistics of the last build. */
+typedef struct rdn_build_stats {
+  uint64_t device_bytes;      /* acceleration-structure bytes resident on the device */
+  uint64_t triangles;
+  uint64_t nodes;             /* BLAS nodes in the reference's forest */
+  uint64_t sah_splits;
+  uint64_t median_fallbacks;  /* degenerate binning -> BalanceTree median split */
+  uint32_t max_blas_depth;
+  uint32_t reserved;
+  double build_seconds;       /* host SAH build + flattening */
+  double upload_seconds;
+} rdn_build_stats;
+rdn_status rdn_get_build_stats(const rdn_ctx* ctx, rdn_build_stats* out);
 
 /* Copies one of the built arrays in the reference's flattened layout
  * (NaiveSahBvhCpu fields, traverse_cpu.rs:9-35) to host memory `dst` of
@@ -231,6 +242,60 @@ rdn_status rdn_trace(rdn_ctx* ctx, const rdn_trace_desc* desc, void* stream);
 /* Same as rdn_trace, additionally accumulating node-visit and triangle-test
  * counts (slower; for measurement). */
 rdn_status rdn_trace_counted(rdn_ctx* ctx, const rdn_trace_desc* desc, void* stream, rdn_counters* out);
+
+/* ---- wavefront executor -------------------------------------------- */
+
+/* Pinhole camera: ray(px, py) = normalize(forward + sx*right + sy*up) with
+ * sx = ((px+0.5)/width*2-1)*tan_half*aspect, sy = (1-(py+0.5)/height*2)*tan_half. */
+typedef struct rdn_camera {
+  float origin[3];
+  float forward[3];
+  float right[3];
+  float up[3];
+  float tan_half;
+  float aspect;
+  uint32_t width;
+  uint32_t height;
+} rdn_camera;
+
+/* One pixel of the primary + shadow + bounce workload, 32 B. */
+typedef struct rdn_pixel_result {
+  uint32_t primary_prim;     /* RDN_MISS when the primary ray misses */
+  float primary_t;
+  uint32_t bounce_prim;      /* RDN_MISS when no bounce hit */
+  float bounce_t;
+  uint32_t primary_flags;    /* bit 0: primary hit */
+  uint32_t light;            /* 0 no shadow ray, 1 light visible, 2 occluded */
+  float direct;              /* max(0, n.l)/|L|^2 when visible, else 0 */
+  uint32_t primary_instance; /* instance slot of the primary hit */
+} rdn_pixel_result;
+
+typedef struct rdn_wavefront_desc {
+  rdn_camera camera;
+  float light[3];
+  uint32_t sample_index;     /* seeds the bounce sampler: xxhash32(px, py, 3*sample_index) */
+  uint32_t tlas_uniform;
+  uint32_t traversal;        /* RDN_TRAVERSAL_* */
+  uint32_t block_size;       /* 0 = 128 */
+  rdn_pixel_result* out;     /* device, width*height records */
+  void* scratch;             /* device, >= rdn_wavefront_scratch_size() bytes, 256-byte aligned */
+  size_t scratch_bytes;
+  uint32_t* ray_counts;      /* device, nullable: [primary, shadow, bounce] rays traced */
+  uint32_t phases;           /* 0 = both; bit 0: primary kernel (raygen, trace, shade, enqueue),
+                                bit 1: secondary kernel (shadow + bounce queues of the last primary run) */
+  uint32_t reserved;
+} rdn_wavefront_desc;
+
+/* Scratch size for the secondary-ray queues of a width x height launch. */
+rdn_status rdn_wavefront_scratch_size(uint32_t width, uint32_t height, size_t* bytes);
+
+/* RayTracingEncoderProvider::trace_ray (api/backend.rs:48-56) running the
+ * fixed pipeline of the path tracer's first bounce
+ * (feature/path_tracing/ray_gen.rs, ray_hit.rs): pinhole primary ray, closest
+ * hit, one ACCEPT_FIRST_HIT_AND_END_SEARCH shadow ray over [EPSILON, light
+ * distance] and one cosine-weighted diffuse bounce over [EPSILON, f32::MAX]
+ * from offset_ray_hit origins. Two kernels, stream-ordered, no host sync. */
+rdn_status rdn_wavefront_shadow_bounce(rdn_ctx* ctx, const rdn_wavefront_desc* desc, void* stream);
 
 #ifdef __cplusplus
 }

@@ -70,6 +70,8 @@ def lib():
         L.orc_intersect_triangle.argtypes = [vp, vp, C.c_float, C.c_float, vp, vp, vp, i32, i32, vp]
         L.orc_intersect_aabb.argtypes = [vp, vp, C.c_float, C.c_float, vp, vp]
         L.orc_select_nth.argtypes = [vp, vp, C.c_size_t, C.c_size_t]
+        L.orc_wavefront_shadow_bounce.argtypes = [vp, vp, u32, u32, vp, u32, u32, u32, u32, vp, vp, i32,
+                                                  C.POINTER(C.c_double)]
         _lib = L
     return _lib
 
@@ -184,6 +186,27 @@ class OracleSystem:
         self._check(self._L.orc_bruteforce_fp64(self._h, _ptr(np.ascontiguousarray(rays)), rays.shape[0],
                                                 tlas_uniform, _ptr(out), threads))
         return out
+
+
+PIXEL_DTYPE = np.dtype([("primary_prim", np.uint32), ("primary_t", np.float32), ("bounce_prim", np.uint32),
+                        ("bounce_t", np.float32), ("primary_flags", np.uint32), ("light", np.uint32),
+                        ("direct", np.float32), ("primary_instance", np.uint32)])
+
+
+def wavefront_shadow_bounce(system: OracleSystem, cam_floats, width, height, light, sample_index=0, tlas=0,
+                            row0=0, row1=None, threads=1):
+    """The oracle's primary + shadow + bounce pipeline over rows [row0, row1).
+    Returns (pixel records, [primary, shadow, bounce] rays, seconds)."""
+    row1 = height if row1 is None else row1
+    cam = np.ascontiguousarray(cam_floats, np.float32)
+    li = np.ascontiguousarray(light, np.float32)
+    out = np.zeros((row1 - row0) * width, PIXEL_DTYPE)
+    rays = np.zeros(3, np.uint64)
+    sec = C.c_double()
+    system._check(system._L.orc_wavefront_shadow_bounce(system._h, _ptr(cam), width, height, _ptr(li), sample_index,
+                                                        tlas, row0, row1, _ptr(out), _ptr(rays), threads,
+                                                        C.byref(sec)))
+    return out, [int(x) for x in rays], sec.value
 
 
 def intersect_triangle(o, d, near, far, v0, v1, v2, cull_enable=False, cull_back=False):

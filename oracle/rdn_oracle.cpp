@@ -48,6 +48,7 @@
 
 #include "orc_math.h"
 #include "orc_select.h"
+#include "orc_shade.h"
 
 namespace orc {
 
@@ -615,7 +616,8 @@ static inline uint32_t any_hit_policy(uint32_t mode, uint32_t primitive_idx) {
 }
 
 static void traverse(const Built& B, const RayIn& ray, uint32_t tlas_idx, uint32_t ray_flags, uint32_t cull_mask,
-                     uint32_t anyhit_mode, HitOut& out, Counters& cn, uint32_t* ray_counts) {
+                     uint32_t anyhit_mode, HitOut& out, Counters& cn, uint32_t* ray_counts,
+                     uint32_t* tri_out = nullptr) {
   out = HitOut{ray.tmax, 0.0f, 0.0f, INVALID_NEXT, INVALID_NEXT, INVALID_NEXT, INVALID_NEXT, 0};
   uint32_t node_visits = 0, tri_tests = 0;
   bool have = false;
@@ -690,6 +692,7 @@ static void traverse(const Built& B, const RayIn& ray, uint32_t tlas_idx, uint32
                   out.instance = ti;
                   out.custom = inst.instance_custom_index;
                   out.hit_kind = (r.s < 0.0f) ? 0xFFu : 0xFEu;
+                  if (tri_out) *tri_out = tri_idx;
                   if (iflags & TF_ACCEPT_FIRST_HIT_AND_END_SEARCH) behavior |= ANYHIT_END_SEARCH;
                 }
                 if (behavior & ANYHIT_END_SEARCH) goto done;
@@ -757,6 +760,95 @@ static void eval_fp64(const Built& B, const RayIn& ray, const HitOut& h, double*
   out3[0] = t / sc;
   out3[1] = (uv * wv - vv * wu) / den;
   out3[2] = (uv * wu - uu * wv) / den;
+}
+
+// ---- wavefront workload: primary -> closest hit -> shadow + diffuse bounce ----
+// One pixel of the fixed-function pipeline that the product's wavefront kernels
+// run (the first bounce of DeviceReferencePathTracingRenderer,
+// scene/rendering/gpu-ray-tracing/src/feature/path_tracing/{ray_gen.rs,ray_hit.rs}):
+// pinhole primary ray, closest hit, geometric normal facing the ray, offset
+// origin, one any-hit shadow ray to a point light and one cosine-weighted
+// diffuse bounce ray.
+struct PixelOut {
+  uint32_t primary_prim;
+  float primary_t;
+  uint32_t bounce_prim;
+  float bounce_t;
+  uint32_t primary_flags;  // bit 0: primary hit
+  uint32_t light;          // 0 no shadow ray, 1 light visible, 2 occluded
+  float direct;            // max(0, n.l) / |L|^2 when visible, else 0
+  uint32_t primary_instance;
+};
+static_assert(sizeof(PixelOut) == 32, "32 B pixel");
+
+struct Camera {
+  V3 origin, forward, right, up;
+  float tan_half, aspect;
+};
+
+static inline V3 camera_dir(const Camera& c, uint32_t px, uint32_t py, uint32_t W, uint32_t H) {
+  float sx = (((float)px + 0.5f) / (float)W * 2.0f - 1.0f) * c.tan_half * c.aspect;
+  float sy = (1.0f - ((float)py + 0.5f) / (float)H * 2.0f) * c.tan_half;
+  V3 d = v3((c.forward.x + sx * c.right.x) + sy * c.up.x, (c.forward.y + sx * c.right.y) + sy * c.up.y,
+            (c.forward.z + sx * c.right.z) + sy * c.up.z);
+  return normalize(d);
+}
+
+// geometric normal of a hit, in world space: normalize(cross(e1, e2)) of the
+// object-space triangle, then normalize(transpose(transform_inv) * n).
+static inline V3 world_normal(const Built& B, uint32_t tri_idx, uint32_t inst) {
+  uint32_t i0 = B.indices[tri_idx * 3], i1 = B.indices[tri_idx * 3 + 1], i2 = B.indices[tri_idx * 3 + 2];
+  V3 v0 = ld3(&B.vertices[i0 * 3]), v1 = ld3(&B.vertices[i1 * 3]), v2 = ld3(&B.vertices[i2 * 3]);
+  V3 n = normalize(cross(v1 - v0, v2 - v0));
+  const float* m = B.tlas_data[inst].transform_inv;
+  V3 w = v3(n.x * m[0] + n.y * m[1] + n.z * m[2], n.x * m[4] + n.y * m[5] + n.z * m[6],
+            n.x * m[8] + n.y * m[9] + n.z * m[10]);
+  return normalize(w);
+}
+
+static const float F32_EPSILON = 1.1920929e-7f;
+static const float F32_MAX = 3.40282347e+38f;
+static const uint32_t RAY_FLAG_END_SEARCH = 0x04;
+
+static void wavefront_pixel(const Built& B, const Camera& cam, uint32_t W, uint32_t H, uint32_t px, uint32_t py,
+                            V3 light, uint32_t sample_index, uint32_t tlas, PixelOut& o, Counters& cn,
+                            uint64_t* rays) {
+  V3 d = camera_dir(cam, px, py, W, H);
+  RayIn r{{cam.origin.x, cam.origin.y, cam.origin.z}, 0.0f, {d.x, d.y, d.z}, F_INF};
+  HitOut h;
+  uint32_t tri = 0;
+  traverse(B, r, tlas, 0, 0xFFu, 0, h, cn, nullptr, &tri);
+  rays[0]++;
+  o = PixelOut{h.prim, h.t, INVALID_NEXT, F32_MAX, 0u, 0u, 0.0f, h.instance};
+  if (h.prim == INVALID_NEXT) return;
+  o.primary_flags = 1u;
+  V3 p = cam.origin + d * h.t;
+  V3 n = world_normal(B, tri, h.instance);
+  V3 nf = dot(n, d) < 0.0f ? n : v3(-n.x, -n.y, -n.z);
+  V3 org = offset_ray_hit(p, nf);
+  // shadow ray to the point light
+  V3 L = light - org;
+  float dist2 = dot(L, L);
+  float dist = std::sqrt(dist2);
+  V3 ldir = normalize(L);
+  float direct = rmax(0.0f, dot(nf, ldir)) / dist2;
+  RayIn sr{{org.x, org.y, org.z}, F32_EPSILON, {ldir.x, ldir.y, ldir.z}, dist};
+  HitOut sh;
+  traverse(B, sr, tlas, RAY_FLAG_END_SEARCH, 0xFFu, 0, sh, cn, nullptr);
+  rays[1]++;
+  o.light = sh.prim == INVALID_NEXT ? 1u : 2u;
+  o.direct = sh.prim == INVALID_NEXT ? direct : 0.0f;
+  // cosine-weighted diffuse bounce
+  uint32_t state = xxhash32(px, py, sample_index * 3u);
+  float s0 = sample_next(state);
+  float s1 = sample_next(state);
+  V3 bdir = cosine_sample_in_dir(nf, s0, s1);
+  RayIn br{{org.x, org.y, org.z}, F32_EPSILON, {bdir.x, bdir.y, bdir.z}, F32_MAX};
+  HitOut bh;
+  traverse(B, br, tlas, 0, 0xFFu, 0, bh, cn, nullptr);
+  rays[2]++;
+  o.bounce_prim = bh.prim;
+  o.bounce_t = bh.t;
 }
 
 }  // namespace orc
@@ -1053,6 +1145,53 @@ int orc_select_nth(const float* keys, uint64_t* idx, size_t len, size_t index) {
   };
   RustSelect<uint64_t, decltype(less)> sel{less};
   sel.select_nth(idx, len, index);
+  return 0;
+}
+
+
+// Wavefront workload over pixel rows [row0, row1) of a W x H image. cam = 14
+// floats (origin, forward, right, up, tan_half, aspect). out receives W*(row1-row0)
+// 32 B pixel records; rays3 receives [primary, shadow, bounce] rays traced.
+int orc_wavefront_shadow_bounce(void* cp, const float* cam, uint32_t W, uint32_t H, const float* light,
+                                uint32_t sample_index, uint32_t tlas, uint32_t row0, uint32_t row1, void* out,
+                                uint64_t* rays3, int threads, double* seconds) {
+  Ctx& c = *(Ctx*)cp;
+  if (!c.built) {
+    int rc = build_all(c);
+    if (rc) return rc;
+  }
+  const Built& B = *c.built;
+  Camera cm{ld3(cam), ld3(cam + 3), ld3(cam + 6), ld3(cam + 9), cam[12], cam[13]};
+  V3 L = ld3(light);
+  if (row1 > H) row1 = H;
+  if (row0 > row1) row0 = row1;
+  if (threads < 1) threads = 1;
+  uint32_t rows = row1 - row0;
+  PixelOut* po = (PixelOut*)out;
+  std::vector<Counters> cn(threads);
+  std::vector<uint64_t> rc(3 * (size_t)threads, 0);
+  std::atomic<uint32_t> next_row{row0};
+  auto t0 = std::chrono::steady_clock::now();
+  auto work = [&](int w) {
+    for (;;) {
+      uint32_t y = next_row.fetch_add(1);
+      if (y >= row1) break;
+      for (uint32_t x = 0; x < W; x++)
+        wavefront_pixel(B, cm, W, H, x, y, L, sample_index, tlas, po[(size_t)(y - row0) * W + x], cn[w],
+                        &rc[3 * (size_t)w]);
+    }
+  };
+  std::vector<std::thread> th;
+  for (int w = 0; w < threads; w++) th.emplace_back(work, w);
+  for (auto& t : th) t.join();
+  auto t1 = std::chrono::steady_clock::now();
+  if (seconds) *seconds = std::chrono::duration<double>(t1 - t0).count();
+  if (rays3) {
+    rays3[0] = rays3[1] = rays3[2] = 0;
+    for (int w = 0; w < threads; w++)
+      for (int k = 0; k < 3; k++) rays3[k] += rc[3 * (size_t)w + k];
+  }
+  (void)rows;
   return 0;
 }
 

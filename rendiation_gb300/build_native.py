@@ -26,6 +26,7 @@ UNITS = {
     "as_build.cpp": [],
     "rdn_api.cpp": [],
     "trace.cu": ["-fmad=false"],
+    "wavefront.cu": ["-fmad=false"],
 }
 
 

@@ -9,6 +9,7 @@
 
 #include "rdn_core.h"
 #include "trace_kernels.h"
+#include "wavefront.h"
 
 using rdn::DevBuf;
 
@@ -185,6 +186,7 @@ rdn_status rdn_create(rdn_ctx** out, int device) {
   c->device = device;
   if (device >= 0) {
     cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_counters, 64);
     if (e == cudaSuccess) e = cudaMemset(c->d_counters, 0, 64);
     if (e != cudaSuccess) {
@@ -312,10 +314,20 @@ rdn_status rdn_build(rdn_ctx* c, const rdn_build_opts* o) {
   return do_build(c);
 }
 
-rdn_status rdn_build_times(const rdn_ctx* c, double* out2) {
-  if (!c || !out2) return RDN_ERR_INVALID_ARG;
-  out2[0] = c->build_seconds;
-  out2[1] = c->upload_seconds;
+rdn_status rdn_get_build_stats(const rdn_ctx* cc, rdn_build_stats* out) {
+  rdn_ctx* c = const_cast<rdn_ctx*>(cc);
+  if (!c || !out) return RDN_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(c->lock);
+  if (!c->host || c->dirty) return fail(c, RDN_ERR_NOT_BUILT, "structure not built");
+  std::memset(out, 0, sizeof(*out));
+  out->device_bytes = c->dev.bytes;
+  out->triangles = c->host->indices_redirect.size();
+  out->nodes = c->host->tri_bvh_forest.size();
+  out->sah_splits = c->host->sah_splits;
+  out->median_fallbacks = c->host->median_fallbacks;
+  out->max_blas_depth = c->host->max_blas_depth;
+  out->build_seconds = c->build_seconds;
+  out->upload_seconds = c->upload_seconds;
   return RDN_OK;
 }
 
@@ -393,6 +405,59 @@ rdn_status rdn_trace_counted(rdn_ctx* c, const rdn_trace_desc* desc, void* strea
   out->tri_tests = h[1];
   out->tri_hits = h[2];
   out->bad_tlas_rays = h[3];
+  return RDN_OK;
+}
+
+rdn_status rdn_wavefront_scratch_size(uint32_t width, uint32_t height, size_t* bytes) {
+  if (!bytes) return RDN_ERR_INVALID_ARG;
+  *bytes = rdn::wavefront_scratch_bytes(width, height);
+  return RDN_OK;
+}
+
+rdn_status rdn_wavefront_shadow_bounce(rdn_ctx* c, const rdn_wavefront_desc* d, void* stream) {
+  if (!c || !d) return fail(c, RDN_ERR_INVALID_ARG, "null context or descriptor");
+  if (c->device < 0) return fail(c, RDN_ERR_UNSUPPORTED, "host-only context cannot trace");
+  const uint32_t W = d->camera.width, H = d->camera.height;
+  if ((uint64_t)W * H > 0xFFFFFFFFull / 2) return fail(c, RDN_ERR_INVALID_ARG, "launch too large");
+  if (W && H && (!d->out || !d->scratch)) return fail(c, RDN_ERR_INVALID_ARG, "null output or scratch");
+  if (d->scratch_bytes < rdn::wavefront_scratch_bytes(W, H)) return fail(c, RDN_ERR_INVALID_ARG, "scratch too small");
+  if ((reinterpret_cast<uintptr_t>(d->scratch) & 255) || (reinterpret_cast<uintptr_t>(d->out) & 15))
+    return fail(c, RDN_ERR_INVALID_ARG, "scratch must be 256-byte and output 16-byte aligned");
+  if (d->traversal > RDN_TRAVERSAL_REFERENCE) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
+  if (d->phases > 3) return fail(c, RDN_ERR_INVALID_ARG, "unknown phase mask");
+  if (d->block_size && (d->block_size % 32 || d->block_size > 128))
+    return fail(c, RDN_ERR_INVALID_ARG, "block_size must be a multiple of 32 up to 128");
+  std::lock_guard<std::mutex> lk(c->lock);
+  rdn_status st = ensure_built(c);
+  if (st != RDN_OK) return st;
+  rdn_trace_desc td;
+  std::memset(&td, 0, sizeof(td));
+  td.tlas_uniform = d->tlas_uniform;
+  td.cull_mask = 0xFF;
+  rdn::TraceParams p;
+  fill_params(c, &td, p);
+  rdn::WavefrontParams w;
+  std::memset(&w, 0, sizeof(w));
+  const rdn_camera& cam = d->camera;
+  w.origin = make_float3(cam.origin[0], cam.origin[1], cam.origin[2]);
+  w.forward = make_float3(cam.forward[0], cam.forward[1], cam.forward[2]);
+  w.right = make_float3(cam.right[0], cam.right[1], cam.right[2]);
+  w.up = make_float3(cam.up[0], cam.up[1], cam.up[2]);
+  w.light = make_float3(d->light[0], d->light[1], d->light[2]);
+  w.tan_half = cam.tan_half;
+  w.aspect = cam.aspect;
+  w.width = W;
+  w.height = H;
+  w.sample_index = d->sample_index;
+  w.tlas = d->tlas_uniform;
+  w.out = reinterpret_cast<rdn::PixelResult*>(d->out);
+  w.ray_counts = d->ray_counts;
+  rdn::wavefront_bind_scratch(w, d->scratch);
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e == cudaSuccess)
+    e = rdn::launch_wavefront(p, w, d->traversal == RDN_TRAVERSAL_ORDERED, d->block_size, c->sm_count,
+                              d->phases, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(c, e, "wavefront launch");
   return RDN_OK;
 }
 

@@ -147,6 +147,7 @@ std::string build_host(const std::vector<std::unique_ptr<std::vector<GeometrySou
 struct rdn_ctx {
   std::mutex lock;
   int device = -1;
+  int sm_count = 0;
   std::vector<std::unique_ptr<std::vector<rdn::GeometrySource>>> blas;
   std::vector<std::unique_ptr<std::vector<rdn::InstanceSource>>> tlas;
   std::vector<uint32_t> binding;

@@ -1,305 +1,22 @@
-// Ray-query kernels for sm_103a.
-//
-// Semantics: NaiveSahBvhCpu::traverse (shader/ray-tracing/src/backend/
-// wavefront_compute/geometry/naive/traverse_cpu.rs:52-245) — TLAS threaded walk,
-// per-instance AABB + mask test, object-space ray with distance scaling, flag
-// merging and culling (naive/flag.rs:24-117), BLAS walk, triangle tests
-// (geometry/mod.rs:104-155), commit / any-hit / end-search, shared far.
-//
-// Arithmetic: IEEE f32 exactly as the reference orders it. This file is built
-// with -fmad=false (no contraction of a*b+c), IEEE division and square root,
-// and min/max with NaN-ignoring fminf/fmaxf (Rust f32::min/max), so every
-// intersection value equals the reference CPU's bit for bit.
-//
-// Two traversal orders over the same tree (the reference's SAH build):
-//   trace_reference: the reference's stackless threaded walk over its 48 B
-//     DeviceBVHNode forest (traverse_cpu.rs:291-319); identical results,
-//     including equal-distance ties and which hit ends a first-hit search.
-//   trace_ordered: near-child-first traversal over 64 B two-child nodes with a
-//     per-thread stack in shared memory; each child box is tested with the
-//     reference's slab test, popped entries are re-checked against the current
-//     far with the reference's strict `t_near_max < t_max`.
-// Both read triangles as 64 B precomputed records (v0, e1, e2, normal, uu, uv,
-// vv, 1/(uv^2-uu*vv)) — values the reference recomputes for every test.
+// Batch ray-query kernel for sm_103a (rdn_trace): one thread per ray, the
+// traversal of traverse.cuh, one 16 B hit (+ optional 16 B context) out.
+// Built with -fmad=false: see traverse.cuh.
 #include <cuda_runtime.h>
 
 #include <cstdint>
 
-#include "rdn_core.h"
-#include "trace_kernels.h"
+#include "traverse.cuh"
 
 namespace rdn {
-
 namespace {
 
-constexpr uint32_t TF_FORCE_OPAQUE = 0x01, TF_FORCE_NON_OPAQUE = 0x02, TF_END_SEARCH = 0x04;
-constexpr uint32_t TF_CULL_BACK = 0x10, TF_CULL_FRONT = 0x20, TF_CULL_OPAQUE = 0x40, TF_CULL_NON_OPAQUE = 0x80;
-constexpr uint32_t TF_SKIP_TRIANGLES = 0x100, TF_FLIP = 0x400;
-constexpr uint32_t ANYHIT_ACCEPT = 1, ANYHIT_END = 2;
-
-__device__ __forceinline__ uint32_t merge_instance_flags(uint32_t f, uint32_t gi) {
-  if (gi & 0x1u) f &= ~(TF_CULL_BACK | TF_CULL_FRONT);
-  if (gi & 0x2u) f ^= TF_FLIP;
-  if (gi & 0x4u) f |= TF_FORCE_OPAQUE;
-  if (gi & 0x8u) f |= TF_FORCE_NON_OPAQUE;
-  return f;
-}
-
-__device__ __forceinline__ float signum_f(float x) {
-  if (isnan(x)) return x;
-  return signbit(x) ? -1.0f : 1.0f;
-}
-
-// intersect_ray_aabb_cpu with the reciprocal direction precomputed (1/d is
-// the same IEEE value the reference forms per test).
-__device__ __forceinline__ bool slab(float3 o, float3 inv_d, float tmin, float tmax, float lx, float ly, float lz,
-                                     float hx, float hy, float hz, float& t_near_max) {
-  const float t0x = (lx - o.x) * inv_d.x, t0y = (ly - o.y) * inv_d.y, t0z = (lz - o.z) * inv_d.z;
-  const float t1x = (hx - o.x) * inv_d.x, t1y = (hy - o.y) * inv_d.y, t1z = (hz - o.z) * inv_d.z;
-  const float nx = fminf(t0x, t1x), ny = fminf(t0y, t1y), nz = fminf(t0z, t1z);
-  const float fx = fmaxf(t0x, t1x), fy = fmaxf(t0y, t1y), fz = fmaxf(t0z, t1z);
-  const float tn = fmaxf(fmaxf(nx, ny), nz);
-  const float tf = fminf(fminf(fx, fy), fz);
-  t_near_max = tn;
-  return tn <= tf && tmin < tf && tn < tmax;
-}
-
-struct TriOut {
-  float t, u, v, s;
-};
-
-// intersect_ray_triangle_cpu on a precomputed record.
-__device__ __forceinline__ bool tri_test(const float4* __restrict__ rec, float3 o, float3 d, float near_, float far_,
-                                         bool cull_enable, bool cull_back, TriOut& r) {
-  const float4 q0 = __ldg(rec), q1 = __ldg(rec + 1), q2 = __ldg(rec + 2);
-  const float b = q0.w * d.x + q1.w * d.y + q2.w * d.z;
-  if (cull_enable) {
-    const bool pass = cull_back != (b < 0.0f);
-    if (!pass) return false;
-  }
-  const float w0x = o.x - q0.x, w0y = o.y - q0.y, w0z = o.z - q0.z;
-  const float a = -(q0.w * w0x + q1.w * w0y + q2.w * w0z);
-  const float t = a / b;
-  if (t < near_ || t > far_) return false;
-  const float4 q3 = __ldg(rec + 3);
-  const float px = o.x + t * d.x, py = o.y + t * d.y, pz = o.z + t * d.z;
-  const float wx = px - q0.x, wy = py - q0.y, wz = pz - q0.z;
-  const float wu = wx * q1.x + wy * q1.y + wz * q1.z;
-  const float wv = wx * q2.x + wy * q2.y + wz * q2.z;
-  const float uu = q3.x, uv = q3.y, vv = q3.z, inv_d = q3.w;
-  const float u = (uv * wv - vv * wu) * inv_d;
-  if (u < 0.0f || u > 1.0f) return false;
-  const float v = (uv * wu - uu * wv) * inv_d;
-  if (v < 0.0f || (u + v) > 1.0f) return false;
-  r.t = t;
-  r.u = u;
-  r.v = v;
-  r.s = signum_f(b);
-  return true;
-}
-
-struct Best {
-  float t, u, v, s;
-  uint32_t k, geom_slot, inst;
-  bool have;
-};
-
-struct InstanceRay {
-  float3 o, d, inv_d;
-  float scaling;
-  uint32_t flags;
-};
-
-// Object-space ray: transform_inv * (o, 1) / w, to_mat3() * d, scaling = |d'|,
-// d' normalised (traverse_cpu.rs:99-104).
-__device__ __forceinline__ InstanceRay to_instance(const DeviceInstance* __restrict__ inst, float3 o, float3 d,
-                                                   uint32_t ray_flags) {
-  const float* m = inst->transform_inv;
-  const float x = o.x * __ldg(m + 0) + o.y * __ldg(m + 4) + o.z * __ldg(m + 8) + 1.0f * __ldg(m + 12);
-  const float y = o.x * __ldg(m + 1) + o.y * __ldg(m + 5) + o.z * __ldg(m + 9) + 1.0f * __ldg(m + 13);
-  const float z = o.x * __ldg(m + 2) + o.y * __ldg(m + 6) + o.z * __ldg(m + 10) + 1.0f * __ldg(m + 14);
-  const float w = o.x * __ldg(m + 3) + o.y * __ldg(m + 7) + o.z * __ldg(m + 11) + 1.0f * __ldg(m + 15);
-  InstanceRay r;
-  r.o = make_float3(x / w, y / w, z / w);
-  float dx = d.x * __ldg(m + 0) + d.y * __ldg(m + 4) + d.z * __ldg(m + 8);
-  float dy = d.x * __ldg(m + 1) + d.y * __ldg(m + 5) + d.z * __ldg(m + 9);
-  float dz = d.x * __ldg(m + 2) + d.y * __ldg(m + 6) + d.z * __ldg(m + 10);
-  const float mag_sq = dx * dx + dy * dy + dz * dz;
-  r.scaling = sqrtf(mag_sq);
-  if (mag_sq > 0.0f) {
-    const float inv = 1.0f / sqrtf(mag_sq);
-    dx = dx * inv;
-    dy = dy * inv;
-    dz = dz * inv;
-  }
-  r.d = make_float3(dx, dy, dz);
-  r.inv_d = make_float3(1.0f / dx, 1.0f / dy, 1.0f / dz);
-  r.flags = merge_instance_flags(ray_flags, __ldg(&inst->flags));
-  return r;
-}
-
-__device__ __forceinline__ void geometry_cull(uint32_t f, uint32_t gf, bool& pass, bool& is_opaque, bool& cull_enable,
-                                              bool& cull_back) {
-  const bool geometry_opaque = (gf & 1u) != 0;
-  const bool op = (geometry_opaque || (f & TF_FORCE_OPAQUE)) && !(f & TF_FORCE_NON_OPAQUE);
-  pass = (op && !(f & TF_CULL_OPAQUE)) || (!op && !(f & TF_CULL_NON_OPAQUE));
-  is_opaque = op;
-  const bool flip = (f & TF_FLIP) != 0, cf = (f & TF_CULL_FRONT) != 0, cb = (f & TF_CULL_BACK) != 0;
-  cull_enable = cf || cb;
-  cull_back = (flip && cb) || (!flip && cf);
-}
-
-__device__ __forceinline__ uint32_t anyhit_policy(uint32_t mode, uint32_t primitive_idx) {
-  if (mode == 1) return ANYHIT_ACCEPT | ANYHIT_END;
-  if (mode == 2) return (primitive_idx & 1u) ? 0u : ANYHIT_ACCEPT;
-  return ANYHIT_ACCEPT;
-}
-
-struct RayCtx {
-  float3 o, d, inv_d;
-  float tmin, tmax;
-  float far_world;  // the shared far of RayRange
-  uint32_t cull_mask, ray_flags;
-  Best best;
-  uint32_t node_visits, tri_tests, tri_hits;
-  bool end_search;
-};
-
-// Tests the triangles of sorted range [k0, k1) and commits hits; returns true
-// when the search must end. Follows traverse_cpu.rs:133-193.
-template <bool COUNT>
-__device__ __forceinline__ bool leaf_triangles(const TraceParams& p, RayCtx& R, const InstanceRay& ir, uint32_t k0,
-                                               uint32_t k1, uint32_t gslot, uint32_t inst_slot, bool is_opaque,
-                                               bool cull_enable, bool cull_back, uint32_t prim_start) {
-  for (uint32_t k = k0; k < k1; k++) {
-    if (COUNT) R.tri_tests++;
-    TriOut h;
-    const float near_ = R.tmin * ir.scaling, far_ = R.far_world * ir.scaling;
-    if (!tri_test(p.tris + 4 * (size_t)k, ir.o, ir.d, near_, far_, cull_enable, cull_back, h)) continue;
-    if (COUNT) R.tri_hits++;
-    const float distance = h.t / ir.scaling;
-    uint32_t behavior = ANYHIT_ACCEPT;
-    if (!is_opaque) behavior = anyhit_policy(p.anyhit_mode, __ldg(p.redirect + k) - prim_start);
-    if (behavior & ANYHIT_ACCEPT) {
-      R.far_world = distance;
-      R.best.t = distance;
-      R.best.u = h.u;
-      R.best.v = h.v;
-      R.best.s = h.s;
-      R.best.k = k;
-      R.best.geom_slot = gslot;
-      R.best.inst = inst_slot;
-      R.best.have = true;
-      if (ir.flags & TF_END_SEARCH) behavior |= ANYHIT_END;
-    }
-    if (behavior & ANYHIT_END) return true;
-  }
-  return false;
-}
-
-// BLAS of one geometry, reference threaded order (traverse_cpu.rs:122-195).
-template <bool COUNT>
-__device__ __forceinline__ bool blas_threaded(const TraceParams& p, RayCtx& R, const InstanceRay& ir, uint32_t root,
-                                              uint32_t gslot, uint32_t inst_slot, bool is_opaque, bool cull_enable,
-                                              bool cull_back, uint32_t prim_start) {
-  uint32_t curr = root;
-  while (curr != INVALID_NEXT) {
-    if (COUNT) R.node_visits++;
-    const float4* nd = reinterpret_cast<const float4*>(p.tri_forest + curr);
-    const float4 a = __ldg(nd), b = __ldg(nd + 1);
-    float tn;
-    const uint32_t hit_next = __float_as_uint(a.w), miss_next = __float_as_uint(b.w);
-    if (slab(ir.o, ir.inv_d, R.tmin * ir.scaling, R.far_world * ir.scaling, a.x, a.y, a.z, b.x, b.y, b.z, tn)) {
-      const uint32_t leaf = curr;
-      curr = hit_next;
-      if (hit_next == miss_next) {
-        const uint2 cr = __ldg(reinterpret_cast<const uint2*>(nd + 2));
-        (void)leaf;
-        if (leaf_triangles<COUNT>(p, R, ir, cr.x, cr.y, gslot, inst_slot, is_opaque, cull_enable, cull_back,
-                                  prim_start))
-          return true;
-      }
-    } else {
-      curr = miss_next;
-    }
-  }
-  return false;
-}
-
-// BLAS of one geometry, near-child-first over two-child nodes.
-template <bool COUNT>
-__device__ __forceinline__ bool blas_ordered(const TraceParams& p, RayCtx& R, const InstanceRay& ir, uint32_t root_node,
-                                             uint32_t gslot, uint32_t inst_slot, bool is_opaque, bool cull_enable,
-                                             bool cull_back, uint32_t prim_start, uint2* stack, uint32_t stride,
-                                             uint32_t depth) {
-  // root box test with the reference node of this geometry
-  {
-    if (COUNT) R.node_visits++;
-    const float4* nd = reinterpret_cast<const float4*>(p.tri_forest + root_node);
-    const float4 a = __ldg(nd), b = __ldg(nd + 1);
-    float tn;
-    if (!slab(ir.o, ir.inv_d, R.tmin * ir.scaling, R.far_world * ir.scaling, a.x, a.y, a.z, b.x, b.y, b.z, tn))
-      return false;
-  }
-  uint32_t code = __ldg(p.geom_root_code + gslot);
-  uint32_t sp = 0;
-  for (;;) {
-    bool have_node = true;
-    // descend through interior nodes until a leaf is reached or no child is hit
-    while (!(code & LEAF_BIT)) {
-      const float4* w = p.wide + 4 * (size_t)code;
-      const float4 w0 = __ldg(w), w1 = __ldg(w + 1), w2 = __ldg(w + 2);
-      const uint2 cc = __ldg(reinterpret_cast<const uint2*>(w + 3));
-      if (COUNT) R.node_visits += 2;
-      const float near_ = R.tmin * ir.scaling, far_ = R.far_world * ir.scaling;
-      float tn0, tn1;
-      const bool h0 = slab(ir.o, ir.inv_d, near_, far_, w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, tn0);
-      const bool h1 = slab(ir.o, ir.inv_d, near_, far_, w1.z, w1.w, w2.x, w2.y, w2.z, w2.w, tn1);
-      if (h0 && h1) {
-        const bool second_first = tn1 < tn0;
-        const uint32_t later = second_first ? cc.x : cc.y;
-        const float later_tn = second_first ? tn0 : tn1;
-        if (sp < depth) {
-          stack[sp * stride] = make_uint2(later, __float_as_uint(later_tn));
-          sp++;
-        } else {
-          atomicOr(p.error_word, 1u);  // the stack is sized from the tree depth: unreachable
-        }
-        code = second_first ? cc.y : cc.x;
-      } else if (h0 || h1) {
-        code = h0 ? cc.x : cc.y;
-      } else {
-        have_node = false;
-        break;
-      }
-    }
-    if (have_node) {
-      const uint2 lr = __ldg(p.leaves + (code & ~LEAF_BIT));
-      if (leaf_triangles<COUNT>(p, R, ir, lr.x, lr.y, gslot, inst_slot, is_opaque, cull_enable, cull_back,
-                                prim_start))
-        return true;
-    }
-    // pop the next pending child whose box still passes `t_near_max < t_max`
-    for (;;) {
-      if (sp == 0) return false;
-      sp--;
-      const uint2 e = stack[sp * stride];
-      if (__uint_as_float(e.y) < R.far_world * ir.scaling) {
-        code = e.x;
-        break;
-      }
-    }
-  }
-}
+using namespace dev;
 
 template <bool ORDERED, bool COUNT>
 __global__ void __launch_bounds__(256) trace_kernel(TraceParams p) {
   extern __shared__ uint2 smem_stack[];
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= p.count) return;
-  uint2* stack = smem_stack + threadIdx.x;
-  const uint32_t stride = blockDim.x;
-
   const float4* rp = p.rays + 2 * (size_t)i;
   const float4 r0 = __ldg(rp), r1 = __ldg(rp + 1);
   RayCtx R;
@@ -307,68 +24,11 @@ __global__ void __launch_bounds__(256) trace_kernel(TraceParams p) {
   R.tmin = r0.w;
   R.d = make_float3(r1.x, r1.y, r1.z);
   R.tmax = r1.w;
-  R.inv_d = make_float3(1.0f / R.d.x, 1.0f / R.d.y, 1.0f / R.d.z);
-  R.far_world = R.tmax;
   R.cull_mask = p.cull_mask;
   R.ray_flags = p.ray_flags;
-  R.best.have = false;
-  R.node_visits = R.tri_tests = R.tri_hits = 0;
-
   const uint32_t tidx = p.tlas_idx ? __ldg(p.tlas_idx + i) : p.tlas_uniform;
-  bool bad = false;
-  uint32_t curr = INVALID_NEXT;
-  if (tidx >= p.n_binding) {
-    bad = true;
-  } else {
-    const uint32_t handle = __ldg(p.tlas_binding + tidx);
-    if (handle >= p.n_tlas_root) bad = true;
-    else curr = __ldg(p.tlas_bvh_root + handle);
-  }
-
-  bool done = false;
-  // TLAS: threaded walk with the shared far (scaling 1)
-  while (curr != INVALID_NEXT && !done) {
-    if (COUNT) R.node_visits++;
-    const float4* nd = reinterpret_cast<const float4*>(p.tlas_forest + curr);
-    const float4 a = __ldg(nd), b = __ldg(nd + 1);
-    const uint32_t hit_next = __float_as_uint(a.w), miss_next = __float_as_uint(b.w);
-    float tn;
-    if (!slab(R.o, R.inv_d, R.tmin * 1.0f, R.far_world * 1.0f, a.x, a.y, a.z, b.x, b.y, b.z, tn)) {
-      curr = miss_next;
-      continue;
-    }
-    curr = hit_next;
-    if (hit_next != miss_next) continue;
-    const uint2 cr = __ldg(reinterpret_cast<const uint2*>(nd + 2));
-    for (uint32_t ti = cr.x; ti < cr.y && !done; ti++) {
-      const float4* tb = reinterpret_cast<const float4*>(p.tlas_bounding + ti);
-      const float4 ba = __ldg(tb), bb = __ldg(tb + 1);
-      float tn2;
-      if (!slab(R.o, R.inv_d, R.tmin, R.tmax, ba.x, ba.y, ba.z, bb.x, bb.y, bb.z, tn2)) continue;
-      if ((R.cull_mask & __float_as_uint(ba.w)) == 0) continue;
-      const DeviceInstance* inst = p.tlas_data + ti;
-      const InstanceRay ir = to_instance(inst, R.o, R.d, R.ray_flags);
-      if (ir.flags & TF_SKIP_TRIANGLES) continue;
-      const uint32_t blas = __ldg(&inst->acceleration_structure_handle);
-      const uint2 range = __ldg(reinterpret_cast<const uint2*>(p.blas_meta + blas));
-      for (uint32_t g = range.x; g < range.y; g++) {
-        const uint4 gm = __ldg(reinterpret_cast<const uint4*>(p.tri_root + g));
-        bool pass, is_opaque, cull_enable, cull_back;
-        geometry_cull(ir.flags, gm.w, pass, is_opaque, cull_enable, cull_back);
-        if (!pass) continue;
-        bool end;
-        if (ORDERED)
-          end = blas_ordered<COUNT>(p, R, ir, gm.x, g, ti, is_opaque, cull_enable, cull_back, gm.z, stack, stride,
-                                    p.stack_depth);
-        else
-          end = blas_threaded<COUNT>(p, R, ir, gm.x, g, ti, is_opaque, cull_enable, cull_back, gm.z);
-        if (end) {
-          done = true;
-          break;
-        }
-      }
-    }
-  }
+  bool bad;
+  traverse_ray<ORDERED, COUNT>(p, R, tidx, smem_stack + threadIdx.x, blockDim.x, bad);
 
   float4 out;
   uint4 ext;

@@ -1,0 +1,45 @@
+// Launch interface of the wavefront kernels (wavefront.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "trace_kernels.h"
+
+namespace rdn {
+
+// Per-pixel result, 32 B (rdn_pixel_result in include/rdn.h).
+struct PixelResult {
+  uint32_t primary_prim;
+  float primary_t;
+  uint32_t bounce_prim;
+  float bounce_t;
+  uint32_t primary_flags;
+  uint32_t light;
+  float direct;
+  uint32_t primary_instance;
+};
+static_assert(sizeof(PixelResult) == 32, "32 B pixel");
+
+struct WavefrontParams {
+  float3 origin, forward, right, up, light;
+  float tan_half, aspect;
+  uint32_t width, height, sample_index, tlas;
+  PixelResult* out;
+  uint32_t* ray_counts;  // nullable: [primary, shadow, bounce]
+  // scratch (wavefront_bind_scratch)
+  uint32_t* queue_count;
+  uint32_t* work_counter;
+  void* shadow_rays;
+  void* bounce_rays;
+  uint32_t* shadow_pixel;
+  uint32_t* bounce_pixel;
+};
+
+size_t wavefront_scratch_bytes(uint32_t width, uint32_t height);
+void wavefront_bind_scratch(WavefrontParams& w, void* scratch);
+// phases: bit 0 primary kernel, bit 1 secondary kernel (0 = both).
+cudaError_t launch_wavefront(const TraceParams& p, const WavefrontParams& w, bool ordered, uint32_t block,
+                             int sm_count, uint32_t phases, cudaStream_t stream);
+
+}  // namespace rdn

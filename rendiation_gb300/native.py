@@ -22,8 +22,8 @@ STATUS_NAMES = {
 # every symbol include/rdn.h declares; tests check the library exports each one
 EXPORTED_SYMBOLS = [
     "rdn_api_version", "rdn_create", "rdn_destroy", "rdn_last_error", "rdn_blas_create", "rdn_blas_delete",
-    "rdn_tlas_create", "rdn_tlas_delete", "rdn_bind_tlas", "rdn_build", "rdn_build_times", "rdn_get_built_array",
-    "rdn_trace", "rdn_trace_counted",
+    "rdn_tlas_create", "rdn_tlas_delete", "rdn_bind_tlas", "rdn_build", "rdn_get_build_stats", "rdn_get_built_array",
+    "rdn_trace", "rdn_trace_counted", "rdn_wavefront_scratch_size", "rdn_wavefront_shadow_bounce",
 ]
 
 
@@ -48,6 +48,12 @@ class BuildOpts(C.Structure):
                 ("tlas_max_depth", C.c_uint32), ("host_threads", C.c_uint32), ("reserved", C.c_uint32 * 3)]
 
 
+class BuildStats(C.Structure):
+    _fields_ = [("device_bytes", C.c_uint64), ("triangles", C.c_uint64), ("nodes", C.c_uint64),
+                ("sah_splits", C.c_uint64), ("median_fallbacks", C.c_uint64), ("max_blas_depth", C.c_uint32),
+                ("reserved", C.c_uint32), ("build_seconds", C.c_double), ("upload_seconds", C.c_double)]
+
+
 class TraceDesc(C.Structure):
     _fields_ = [("rays", C.c_void_p), ("hits", C.c_void_p), ("hits_ext", C.c_void_p), ("tlas_idx", C.c_void_p),
                 ("count", C.c_uint32), ("tlas_uniform", C.c_uint32), ("ray_flags", C.c_uint32),
@@ -58,6 +64,19 @@ class TraceDesc(C.Structure):
 class Counters(C.Structure):
     _fields_ = [("node_visits", C.c_uint64), ("tri_tests", C.c_uint64), ("tri_hits", C.c_uint64),
                 ("bad_tlas_rays", C.c_uint64)]
+
+
+class Camera(C.Structure):
+    _fields_ = [("origin", C.c_float * 3), ("forward", C.c_float * 3), ("right", C.c_float * 3),
+                ("up", C.c_float * 3), ("tan_half", C.c_float), ("aspect", C.c_float), ("width", C.c_uint32),
+                ("height", C.c_uint32)]
+
+
+class WavefrontDesc(C.Structure):
+    _fields_ = [("camera", Camera), ("light", C.c_float * 3), ("sample_index", C.c_uint32),
+                ("tlas_uniform", C.c_uint32), ("traversal", C.c_uint32), ("block_size", C.c_uint32),
+                ("out", C.c_void_p), ("scratch", C.c_void_p), ("scratch_bytes", C.c_size_t),
+                ("ray_counts", C.c_void_p), ("phases", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 _lib = None
@@ -91,13 +110,17 @@ def lib() -> C.CDLL:
     L.rdn_bind_tlas.restype = i32
     L.rdn_build.argtypes = [vp, vp]
     L.rdn_build.restype = i32
-    L.rdn_build_times.argtypes = [vp, vp]
-    L.rdn_build_times.restype = i32
+    L.rdn_get_build_stats.argtypes = [vp, C.POINTER(BuildStats)]
+    L.rdn_get_build_stats.restype = i32
     L.rdn_get_built_array.argtypes = [vp, u32, vp, C.c_size_t, C.POINTER(C.c_size_t)]
     L.rdn_get_built_array.restype = i32
     L.rdn_trace.argtypes = [vp, C.POINTER(TraceDesc), vp]
     L.rdn_trace.restype = i32
     L.rdn_trace_counted.argtypes = [vp, C.POINTER(TraceDesc), vp, C.POINTER(Counters)]
     L.rdn_trace_counted.restype = i32
+    L.rdn_wavefront_scratch_size.argtypes = [u32, u32, C.POINTER(C.c_size_t)]
+    L.rdn_wavefront_scratch_size.restype = i32
+    L.rdn_wavefront_shadow_bounce.argtypes = [vp, C.POINTER(WavefrontDesc), vp]
+    L.rdn_wavefront_shadow_bounce.restype = i32
     _lib = L
     return L

@@ -151,10 +151,13 @@ class AccelerationStructureSystem:
         o = native.BuildOpts(blas_bin_size, blas_max_depth, tlas_bin_size, tlas_max_depth, host_threads)
         _check(self._h, self._L.rdn_build(self._h, C.byref(o)))
 
-    def build_times(self) -> tuple[float, float]:
-        t = (C.c_double * 2)()
-        _check(self._h, self._L.rdn_build_times(self._h, t))
-        return t[0], t[1]
+    def build_stats(self) -> dict:
+        st = native.BuildStats()
+        _check(self._h, self._L.rdn_get_build_stats(self._h, C.byref(st)))
+        return {name: getattr(st, name) for name, _ in native.BuildStats._fields_ if name != "reserved"}
+
+    def device_bytes(self) -> int:
+        return int(self.build_stats()["device_bytes"])
 
     def built_array(self, name: str) -> bytes:
         which = BUILT_ARRAYS.index(name)
@@ -195,6 +198,75 @@ class AccelerationStructureSystem:
         _check(self._h, self._L.rdn_trace_counted(self._h, C.byref(d), C.c_void_p(s), C.byref(c)))
         return {"node_visits": c.node_visits, "tri_tests": c.tri_tests, "tri_hits": c.tri_hits,
                 "bad_tlas_rays": c.bad_tlas_rays}
+
+
+PIXEL_DTYPE = np.dtype([("primary_prim", np.uint32), ("primary_t", np.float32), ("bounce_prim", np.uint32),
+                        ("bounce_t", np.float32), ("primary_flags", np.uint32), ("light", np.uint32),
+                        ("direct", np.float32), ("primary_instance", np.uint32)])
+
+
+def camera_struct(cam) -> "native.Camera":
+    """rendiation_gb300.scenes.PinholeCamera -> rdn_camera."""
+    c = native.Camera()
+    for name in ("origin", "forward", "right", "up"):
+        v = getattr(cam, name)
+        arr = getattr(c, name)
+        for k in range(3):
+            arr[k] = float(v[k])
+    c.tan_half = float(cam.tan_half)
+    c.aspect = float(cam.aspect)
+    c.width = cam.width
+    c.height = cam.height
+    return c
+
+
+class Wavefront:
+    """Primary + shadow + bounce wavefront (rdn_wavefront_shadow_bounce) on one
+    AccelerationStructureSystem, with its scratch queues and outputs held as
+    torch CUDA tensors."""
+
+    def __init__(self, system: AccelerationStructureSystem, camera, light, traversal=TRAVERSAL_ORDERED,
+                 tlas_uniform=0, block_size=0):
+        import torch
+
+        self.system = system
+        self.camera = camera
+        self.n = camera.width * camera.height
+        size = C.c_size_t()
+        _check(None, system._L.rdn_wavefront_scratch_size(camera.width, camera.height, C.byref(size)))
+        self.scratch = torch.empty(size.value + 256, dtype=torch.uint8, device="cuda")
+        base = self.scratch.data_ptr()
+        self.scratch_ptr = (base + 255) & ~255
+        self.out = torch.empty((self.n, 8), dtype=torch.int32, device="cuda")
+        self.ray_counts = torch.zeros(4, dtype=torch.int32, device="cuda")
+        self.desc = native.WavefrontDesc()
+        self.desc.camera = camera_struct(camera)
+        for k in range(3):
+            self.desc.light[k] = float(light[k])
+        self.desc.tlas_uniform = tlas_uniform
+        self.desc.traversal = traversal
+        self.desc.block_size = block_size
+        self.desc.out = self.out.data_ptr()
+        self.desc.scratch = self.scratch_ptr
+        self.desc.scratch_bytes = size.value
+        self.desc.ray_counts = self.ray_counts.data_ptr()
+
+    def run(self, sample_index=0, stream=None, phases=0):
+        """phases: 0 both kernels, 1 primary only, 2 secondary only (queues of the last primary run)."""
+        import torch
+
+        self.desc.sample_index = sample_index
+        self.desc.phases = phases
+        s = (stream or torch.cuda.current_stream()).cuda_stream
+        _check(self.system._h, self.system._L.rdn_wavefront_shadow_bounce(self.system._h, C.byref(self.desc),
+                                                                          C.c_void_p(s)))
+
+    def results(self) -> np.ndarray:
+        return self.out.cpu().numpy().view(PIXEL_DTYPE).reshape(-1)
+
+    def rays_traced(self) -> tuple[int, int, int]:
+        c = self.ray_counts.cpu().numpy()
+        return int(c[0]), int(c[1]), int(c[2])
 
 
 def hits_to_numpy(hits) -> np.ndarray:
