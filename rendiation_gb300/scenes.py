@@ -194,8 +194,11 @@ def soup_camera(width: int = 256, height: int = 256) -> PinholeCamera:
     )
 
 
-def heightfield_camera(width: int = 1920, height: int = 1080, vfov_deg: float = 45.0) -> PinholeCamera:
-    """Wavefront workload camera: eye (0.5,-0.5,0.8) aimed at the grid centre (0.5,0.5,0)."""
+def heightfield_camera(width: int = 1920, height: int = 1080, vfov_deg: float = 20.0) -> PinholeCamera:
+    """Wavefront workload camera: eye (0.5,-0.5,0.8) aimed at the grid centre (0.5,0.5,0).
+    A 20 degree vertical field of view keeps the far edge of the grid (10.6 degrees
+    above the view axis) and the near edge (19.3 degrees below) in frame, so almost
+    every primary ray hits the field and spawns a shadow and a bounce ray."""
     return PinholeCamera.look_at((0.5, -0.5, 0.8), (0.5, 0.5, 0.0), vfov_deg, width, height)
 
 

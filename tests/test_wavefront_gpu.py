@@ -31,7 +31,7 @@ def test_wavefront_reference_order_bit_identical(sample_index, cuda):
     cam = scenes.heightfield_camera(160, 96)
     got, exp, rays, counts = run_both(mesh, cam, rt.TRAVERSAL_REFERENCE, sample_index)
     assert counts == tuple(rays)
-    assert rays[1] > 0.5 * rays[0]  # most primaries hit the field
+    assert rays[1] > 0.9 * rays[0]  # the field fills the frame
     for f in exp.dtype.names:
         assert np.array_equal(got[f].view(np.uint32), exp[f].view(np.uint32)), f
 
