@@ -297,6 +297,21 @@ rdn_status rdn_wavefront_scratch_size(uint32_t width, uint32_t height, size_t* b
  * from offset_ray_hit origins. Two kernels, stream-ordered, no host sync. */
 rdn_status rdn_wavefront_shadow_bounce(rdn_ctx* ctx, const rdn_wavefront_desc* desc, void* stream);
 
+/* Allocation-free variant of rdn_wavefront_shadow_bounce; it has no
+ * counterpart in the reference. For callers that cannot allocate device
+ * memory (a host that hands out all device memory from its own budget fixed at
+ * start-up, or a foreign-language host that only sees this C ABI): the shadow
+ * and bounce queues live in one array compiled into the library, of
+ * RDN_WAVEFRONT_STATIC_SCRATCH_BYTES, held on every GPU that loads the library
+ * until exit. desc->scratch must be NULL and desc->scratch_bytes 0; launches
+ * whose queues do not fit (rdn_wavefront_scratch_size() above the array size,
+ * about 466,000 pixels) are rejected with RDN_ERR_INVALID_ARG. The call
+ * allocates nothing. The first call on a device looks up the array's device
+ * address, so make it before any stream capture. Every call reuses the same
+ * array: calls that overlap on the GPU race and must be ordered by the caller. */
+#define RDN_WAVEFRONT_STATIC_SCRATCH_BYTES (32u * 1024u * 1024u)
+rdn_status rdn_wavefront_shadow_bounce_static(rdn_ctx* ctx, const rdn_wavefront_desc* desc, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -27,6 +27,7 @@ UNITS = {
     "rdn_api.cpp": [],
     "trace.cu": ["-fmad=false"],
     "wavefront.cu": ["-fmad=false"],
+    "wavefront_static.cu": [],
 }
 
 

@@ -461,4 +461,58 @@ rdn_status rdn_wavefront_shadow_bounce(rdn_ctx* c, const rdn_wavefront_desc* d, 
   return RDN_OK;
 }
 
+// Allocation-free wavefront: identical work to rdn_wavefront_shadow_bounce with
+// the queues in the library's static device array (see wavefront_static.cu).
+rdn_status rdn_wavefront_shadow_bounce_static(rdn_ctx* c, const rdn_wavefront_desc* d, void* stream) {
+  if (!c || !d) return fail(c, RDN_ERR_INVALID_ARG, "null context or descriptor");
+  if (c->device < 0) return fail(c, RDN_ERR_UNSUPPORTED, "host-only context cannot trace");
+  if (d->scratch || d->scratch_bytes)
+    return fail(c, RDN_ERR_INVALID_ARG, "the static variant uses the library's own scratch: pass scratch = NULL, 0");
+  const uint32_t W = d->camera.width, H = d->camera.height;
+  if ((uint64_t)W * H > 0xFFFFFFFFull / 2) return fail(c, RDN_ERR_INVALID_ARG, "launch too large");
+  const size_t need = rdn::wavefront_scratch_bytes(W, H);
+  if (need > RDN_WAVEFRONT_STATIC_SCRATCH_BYTES)
+    return fail(c, RDN_ERR_INVALID_ARG,
+                "launch of " + std::to_string(W) + "x" + std::to_string(H) + " needs " + std::to_string(need) +
+                    " bytes of queue scratch; the static array holds " +
+                    std::to_string(RDN_WAVEFRONT_STATIC_SCRATCH_BYTES) + " (about 466,000 pixels)");
+  if (W && H && !d->out) return fail(c, RDN_ERR_INVALID_ARG, "null output");
+  if (reinterpret_cast<uintptr_t>(d->out) & 15) return fail(c, RDN_ERR_INVALID_ARG, "output must be 16-byte aligned");
+  if (d->traversal > RDN_TRAVERSAL_REFERENCE) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
+  if (d->phases > 3) return fail(c, RDN_ERR_INVALID_ARG, "unknown phase mask");
+  if (d->block_size && (d->block_size % 32 || d->block_size > 128))
+    return fail(c, RDN_ERR_INVALID_ARG, "block_size must be a multiple of 32 up to 128");
+  std::lock_guard<std::mutex> lk(c->lock);
+  rdn_status st = ensure_built(c);
+  if (st != RDN_OK) return st;
+  rdn_trace_desc td;
+  std::memset(&td, 0, sizeof(td));
+  td.tlas_uniform = d->tlas_uniform;
+  td.cull_mask = 0xFF;
+  rdn::TraceParams p;
+  fill_params(c, &td, p);
+  rdn::WavefrontParams w;
+  std::memset(&w, 0, sizeof(w));
+  const rdn_camera& cam = d->camera;
+  w.origin = make_float3(cam.origin[0], cam.origin[1], cam.origin[2]);
+  w.forward = make_float3(cam.forward[0], cam.forward[1], cam.forward[2]);
+  w.right = make_float3(cam.right[0], cam.right[1], cam.right[2]);
+  w.up = make_float3(cam.up[0], cam.up[1], cam.up[2]);
+  w.light = make_float3(d->light[0], d->light[1], d->light[2]);
+  w.tan_half = cam.tan_half;
+  w.aspect = cam.aspect;
+  w.width = W;
+  w.height = H;
+  w.sample_index = d->sample_index;
+  w.tlas = d->tlas_uniform;
+  w.out = reinterpret_cast<rdn::PixelResult*>(d->out);
+  w.ray_counts = d->ray_counts;
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e == cudaSuccess)
+    e = rdn::launch_wavefront_static(p, w, d->traversal == RDN_TRAVERSAL_ORDERED, d->block_size, c->sm_count,
+                                     d->phases, c->device, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(c, e, "static wavefront launch");
+  return RDN_OK;
+}
+
 }  // extern "C"

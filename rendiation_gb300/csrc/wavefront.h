@@ -42,4 +42,9 @@ void wavefront_bind_scratch(WavefrontParams& w, void* scratch);
 cudaError_t launch_wavefront(const TraceParams& p, const WavefrontParams& w, bool ordered, uint32_t block,
                              int sm_count, uint32_t phases, cudaStream_t stream);
 
+// Same launch with the queues in the library's static device array
+// (wavefront_static.cu); `device` must be current.
+cudaError_t launch_wavefront_static(const TraceParams& p, WavefrontParams w, bool ordered, uint32_t block,
+                                    int sm_count, uint32_t phases, int device, cudaStream_t stream);
+
 }  // namespace rdn

@@ -24,6 +24,7 @@ EXPORTED_SYMBOLS = [
     "rdn_api_version", "rdn_create", "rdn_destroy", "rdn_last_error", "rdn_blas_create", "rdn_blas_delete",
     "rdn_tlas_create", "rdn_tlas_delete", "rdn_bind_tlas", "rdn_build", "rdn_get_build_stats", "rdn_get_built_array",
     "rdn_trace", "rdn_trace_counted", "rdn_wavefront_scratch_size", "rdn_wavefront_shadow_bounce",
+    "rdn_wavefront_shadow_bounce_static",
 ]
 
 
@@ -122,5 +123,7 @@ def lib() -> C.CDLL:
     L.rdn_wavefront_scratch_size.restype = i32
     L.rdn_wavefront_shadow_bounce.argtypes = [vp, C.POINTER(WavefrontDesc), vp]
     L.rdn_wavefront_shadow_bounce.restype = i32
+    L.rdn_wavefront_shadow_bounce_static.argtypes = [vp, C.POINTER(WavefrontDesc), vp]
+    L.rdn_wavefront_shadow_bounce_static.restype = i32
     _lib = L
     return L
