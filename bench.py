@@ -316,6 +316,100 @@ def oracle_heightfield(mesh):
     return S
 
 
+def bench_batched(args):
+    """Batched multi-scene paths: 256 soups (log-uniform 1k..200k triangles),
+    log-uniform 4k..256k rays per scene, <= 4 diffuse bounces with Russian
+    roulette from bounce 2. One persistent launch per bounce for all scenes,
+    captured in a CUDA graph, against the plain per-scene launch loop (the same
+    executor called once per scene)."""
+    import ctypes as C
+
+    import torch
+
+    from rendiation_gb300 import native
+    from rendiation_gb300 import raytracing as rt
+    from rendiation_gb300 import scenes
+
+    b = scenes.batched_soups(n_scenes=args.scenes)
+    P = rt.AccelerationStructureSystem(device=0)
+    for m in b.meshes:
+        P.create_bottom_level_acceleration_structure([rt.BottomLevelAccelerationStructureBuildSource(m.positions)])
+    handles = [P.create_top_level_acceleration_structure([rt.TopLevelAccelerationStructureSourceInstance(s)])
+               for s in range(len(b.meshes))]
+    P.bind_tlas(handles)
+    t0 = time.perf_counter()
+    P.build(blas_bin_size=4)
+    build_s = time.perf_counter() - t0
+    rays = torch.from_numpy(b.rays.view(np.float32).reshape(-1, 8).copy()).cuda()
+    tidx = torch.from_numpy(b.tlas_idx.astype(np.int32)).cuda()
+    traversal = rt.TRAVERSAL_REFERENCE if args.traversal == "reference" else rt.TRAVERSAL_ORDERED
+    stream = torch.cuda.current_stream()
+
+    batched = rt.Paths(P, rays, tidx, max_bounces=4, rr_start=2, seed=1, traversal=traversal)
+    batched.capture()
+    for _ in range(args.warmup):
+        batched.launch_graph()
+    torch.cuda.synchronize()
+    segs = batched.segments()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = max(3, args.batched_steps)
+    e0.record(stream)
+    for _ in range(reps):
+        batched.launch_graph()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    batched_ms = e0.elapsed_time(e1) / reps
+    res_batched = batched.results()
+
+    # plain per-scene loop: the same executor, one scene per call
+    L = native.lib()
+    max_n = int(np.max(np.diff(b.ray_offsets)))
+    size = C.c_size_t()
+    L.rdn_paths_scratch_size(max_n, 4, C.byref(size))
+    scratch = torch.empty(size.value + 256, dtype=torch.uint8, device="cuda")
+    sptr = (scratch.data_ptr() + 255) & ~255
+    out = torch.empty((b.rays.shape[0], 2), dtype=torch.float32, device="cuda")
+    desc = native.PathDesc()
+    desc.max_bounces, desc.rr_start, desc.albedo, desc.rr_survive, desc.seed = 4, 2, 0.5, 0.5, 1
+    desc.traversal, desc.scratch, desc.scratch_bytes = traversal, sptr, size.value
+
+    def plain_loop():
+        for sidx in range(len(b.meshes)):
+            o0, o1 = int(b.ray_offsets[sidx]), int(b.ray_offsets[sidx + 1])
+            desc.rays = rays.data_ptr() + o0 * 32
+            desc.tlas_idx = None
+            desc.count = o1 - o0
+            desc.tlas_uniform = sidx
+            desc.out = out.data_ptr() + o0 * 8
+            st = L.rdn_trace_paths(P._h, C.byref(desc), C.c_void_p(stream.cuda_stream))
+            if st != native.RDN_OK:
+                raise native.RdnError(st, L.rdn_last_error(P._h).decode())
+
+    plain_loop()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        plain_loop()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = e0.elapsed_time(e1) / reps
+    # per-scene seeds equal the batched ones only when ids match: compare statistics, not records
+    total = int(sum(segs))
+    return {
+        "workload": f"{len(b.meshes)} soups, {sum(m.triangle_count for m in b.meshes)} tris, "
+                    f"{b.rays.shape[0]} primaries, <=4 bounces, roulette p=0.5 from bounce 2",
+        "segments_per_step": total,
+        "segments_per_bounce": segs,
+        "batched_graph_mrays": round(total / (batched_ms / 1e3) / 1e6, 2),
+        "batched_ms": round(batched_ms, 3),
+        "plain_loop_mrays": round(total / (plain_ms / 1e3) / 1e6, 2),
+        "plain_loop_ms": round(plain_ms, 3),
+        "speedup_vs_plain_loop": round(plain_ms / batched_ms, 3),
+        "host_build_s": round(build_s, 2),
+        "escaped_fraction": round(float(np.mean(res_batched["depth_flags"] >> 31)), 4),
+    }
+
+
 def cpu_baseline_wavefront(S, cam, threads: int, budget_s: float, steps: int = 1):
     """The oracle's pipeline on host cores over a bounded band of rows (BVH built beforehand)."""
     from oracle import orc
@@ -388,6 +482,9 @@ def main():
     ap.add_argument("--block", type=int, default=0)
     ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU work for the CPU baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--scenes", type=int, default=256)
+    ap.add_argument("--batched-steps", type=int, default=5)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -404,6 +501,9 @@ def main():
     if ws > 1:
         torch.distributed.init_process_group("nccl")
     out, P, mesh, cam = bench_wavefront(args, ws, rank)
+    if not args.no_batched:
+        P.close()
+        out["batched"] = bench_batched(args)
     if rank == 0:
         if not args.no_cpu_baseline:
             cb, _ = cpu_baseline_wavefront(oracle_heightfield(mesh), cam, os.cpu_count() or 1,

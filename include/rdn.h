@@ -297,6 +297,59 @@ rdn_status rdn_wavefront_scratch_size(uint32_t width, uint32_t height, size_t* b
  * from offset_ray_hit origins. Two kernels, stream-ordered, no host sync. */
 rdn_status rdn_wavefront_shadow_bounce(rdn_ctx* ctx, const rdn_wavefront_desc* desc, void* stream);
 
+/* ---- batched multi-scene paths ---------------------------------------- */
+
+/* depth_flags of a path result: bits 0..15 = bounce at which the path ended. */
+#define RDN_PATH_ESCAPED 0x80000000u  /* ended by a miss: radiance = throughput (sky = 1) */
+#define RDN_PATH_ROULETTE 0x40000000u /* ended by Russian roulette: radiance 0 */
+
+typedef struct rdn_path_result {
+  float radiance;
+  uint32_t depth_flags;
+} rdn_path_result;
+
+/* Diffuse paths over many scenes at once: every ray carries its own index into
+ * the bound TLAS list (the reference's payload tlas_idx, traverse_cpu.rs:63),
+ * so all scenes share one persistent launch per bounce. Per bounce k of ray i:
+ * closest hit; a miss writes radiance = throughput; a hit at k == max_bounces
+ * writes 0; otherwise the sampler xxhash32(i, k, seed) gives a cosine bounce
+ * around the facing geometric normal from an offset_ray_hit origin with
+ * throughput *= albedo, and from bounce rr_start on the path survives with
+ * probability rr_survive (throughput /= rr_survive). */
+typedef struct rdn_path_desc {
+  const rdn_ray* rays;          /* device, primary rays */
+  const uint32_t* tlas_idx;     /* device, nullable: per-ray TLAS index */
+  uint32_t count;
+  uint32_t tlas_uniform;        /* used when tlas_idx is NULL */
+  uint32_t max_bounces;         /* <= 16 */
+  uint32_t rr_start;
+  float albedo;
+  float rr_survive;
+  uint32_t seed;
+  uint32_t traversal;           /* RDN_TRAVERSAL_* */
+  uint32_t block_size;          /* 0 = 128 */
+  uint32_t reserved;
+  rdn_path_result* out;         /* device, count entries */
+  void* scratch;                /* device, >= rdn_paths_scratch_size() bytes, 256-byte aligned */
+  size_t scratch_bytes;
+  uint32_t* segment_counts;     /* device, nullable: rays traced per bounce (max_bounces + 1) */
+} rdn_path_desc;
+
+rdn_status rdn_paths_scratch_size(uint32_t count, uint32_t max_bounces, size_t* bytes);
+
+/* Stream-ordered: one counter reset and max_bounces + 1 persistent launches;
+ * queue sizes stay on the device (no host synchronisation). Replaces the
+ * reference's per-round task polling of the path tracer
+ * (feature/path_tracing/mod.rs:127-235, task_group.rs:176-278). */
+rdn_status rdn_trace_paths(rdn_ctx* ctx, const rdn_path_desc* desc, void* stream);
+
+/* The same launches captured once into an executable CUDA graph; the
+ * descriptor's pointers and sizes are baked in. Launch it any number of times. */
+typedef struct rdn_graph rdn_graph;
+rdn_status rdn_trace_paths_graph(rdn_ctx* ctx, const rdn_path_desc* desc, rdn_graph** out);
+rdn_status rdn_graph_launch(rdn_graph* graph, void* stream);
+rdn_status rdn_graph_destroy(rdn_graph* graph);
+
 /* Allocation-free variant of rdn_wavefront_shadow_bounce; it has no
  * counterpart in the reference. For callers that cannot allocate device
  * memory (a host that hands out all device memory from its own budget fixed at

@@ -70,6 +70,8 @@ def lib():
         L.orc_intersect_triangle.argtypes = [vp, vp, C.c_float, C.c_float, vp, vp, vp, i32, i32, vp]
         L.orc_intersect_aabb.argtypes = [vp, vp, C.c_float, C.c_float, vp, vp]
         L.orc_select_nth.argtypes = [vp, vp, C.c_size_t, C.c_size_t]
+        L.orc_trace_paths.argtypes = [vp, vp, u32, vp, u32, u32, u32, C.c_float, C.c_float, u32, vp, vp, i32,
+                                      C.POINTER(C.c_double)]
         L.orc_wavefront_shadow_bounce.argtypes = [vp, vp, u32, u32, vp, u32, u32, u32, u32, vp, vp, i32,
                                                   C.POINTER(C.c_double)]
         _lib = L
@@ -207,6 +209,23 @@ def wavefront_shadow_bounce(system: OracleSystem, cam_floats, width, height, lig
                                                         tlas, row0, row1, _ptr(out), _ptr(rays), threads,
                                                         C.byref(sec)))
     return out, [int(x) for x in rays], sec.value
+
+
+PATH_DTYPE = np.dtype([("radiance", np.float32), ("depth_flags", np.uint32)])
+
+
+def trace_paths(system: OracleSystem, rays, tlas_idx=None, tlas_uniform=0, max_bounces=4, rr_start=2, albedo=0.5,
+                rr_survive=0.5, seed=0, threads=1):
+    """The oracle's batched diffuse paths. Returns (results, rays per bounce, seconds)."""
+    rays = np.ascontiguousarray(rays)
+    n = rays.shape[0]
+    out = np.zeros(n, PATH_DTYPE)
+    seg = np.zeros(max_bounces + 1, np.uint64)
+    ti = None if tlas_idx is None else np.ascontiguousarray(tlas_idx, np.uint32)
+    sec = C.c_double()
+    system._check(system._L.orc_trace_paths(system._h, _ptr(rays), n, _ptr(ti), tlas_uniform, max_bounces, rr_start,
+                                            albedo, rr_survive, seed, _ptr(out), _ptr(seg), threads, C.byref(sec)))
+    return out, [int(x) for x in seg], sec.value
 
 
 def intersect_triangle(o, d, near, far, v0, v1, v2, cull_enable=False, cull_back=False):

@@ -851,6 +851,64 @@ static void wavefront_pixel(const Built& B, const Camera& cam, uint32_t W, uint3
   o.bounce_t = bh.t;
 }
 
+// ---- batched paths: closest hit, diffuse bounce, Russian roulette ----
+// The per-path loop of the reference's path tracer (feature/path_tracing/
+// ray_gen.rs:89-211 with the closest-hit BRDF sampling of ray_hit.rs:57-103),
+// reduced to a constant-albedo diffuse surface under a sky of radiance 1:
+// a miss at bounce k ends the path with radiance = throughput; a hit at
+// k == max_bounces ends it with 0; otherwise the sampler xxhash32(id, k, seed)
+// gives (s0, s1) for a cosine bounce around the facing geometric normal and s2
+// for Russian roulette from bounce rr_start on.
+static const uint32_t PATH_ESCAPED = 0x80000000u, PATH_ROULETTE = 0x40000000u;
+
+static void path_one(const Built& B, RayIn r, uint32_t id, uint32_t tlas, uint32_t max_bounces, uint32_t rr_start,
+                     float albedo, float rr_survive, uint32_t seed, float* out2, uint64_t* seg, Counters& cn) {
+  float throughput = 1.0f;
+  for (uint32_t k = 0;; k++) {
+    HitOut h;
+    uint32_t tri = 0;
+    traverse(B, r, tlas, 0, 0xFFu, 0, h, cn, nullptr, &tri);
+    seg[k]++;
+    uint32_t flags;
+    if (h.prim == INVALID_NEXT) {
+      out2[0] = throughput;
+      flags = k | PATH_ESCAPED;
+      memcpy(&out2[1], &flags, 4);
+      return;
+    }
+    if (k == max_bounces) {
+      out2[0] = 0.0f;
+      flags = k;
+      memcpy(&out2[1], &flags, 4);
+      return;
+    }
+    uint32_t st = xxhash32(id, k, seed);
+    float s0 = sample_next(st);
+    float s1 = sample_next(st);
+    float s2 = sample_next(st);
+    float t_next = throughput * albedo;
+    bool survive = true;
+    if (k + 1 >= rr_start) {
+      survive = s2 < rr_survive;
+      t_next = t_next / rr_survive;
+    }
+    if (!survive) {
+      out2[0] = 0.0f;
+      flags = k | PATH_ROULETTE;
+      memcpy(&out2[1], &flags, 4);
+      return;
+    }
+    V3 d = ld3(r.dir);
+    V3 hp = ld3(r.org) + d * h.t;
+    V3 n = world_normal(B, tri, h.instance);
+    V3 nf = dot(n, d) < 0.0f ? n : v3(-n.x, -n.y, -n.z);
+    V3 org = offset_ray_hit(hp, nf);
+    V3 dir = cosine_sample_in_dir(nf, s0, s1);
+    r = RayIn{{org.x, org.y, org.z}, F32_EPSILON, {dir.x, dir.y, dir.z}, F32_MAX};
+    throughput = t_next;
+  }
+}
+
 }  // namespace orc
 
 using namespace orc;
@@ -1192,6 +1250,48 @@ int orc_wavefront_shadow_bounce(void* cp, const float* cam, uint32_t W, uint32_t
       for (int k = 0; k < 3; k++) rays3[k] += rc[3 * (size_t)w + k];
   }
   (void)rows;
+  return 0;
+}
+
+
+// Batched paths over n rays (tlas_idx per ray, or tlas_uniform when NULL).
+// out = (radiance, depth|flags bits) per ray; seg receives rays traced per
+// bounce (max_bounces + 1 entries).
+int orc_trace_paths(void* cp, const RayIn* rays, uint32_t n, const uint32_t* tlas_idx, uint32_t tlas_uniform,
+                    uint32_t max_bounces, uint32_t rr_start, float albedo, float rr_survive, uint32_t seed,
+                    float* out, uint64_t* seg, int threads, double* seconds) {
+  Ctx& c = *(Ctx*)cp;
+  if (!c.built) {
+    int rc = build_all(c);
+    if (rc) return rc;
+  }
+  if (max_bounces > 16) return -1;
+  const Built& B = *c.built;
+  if (threads < 1) threads = 1;
+  std::vector<Counters> cn(threads);
+  std::vector<uint64_t> sg((size_t)threads * 17, 0);
+  std::atomic<uint32_t> next{0};
+  auto t0 = std::chrono::steady_clock::now();
+  auto work = [&](int w) {
+    for (;;) {
+      uint32_t s = next.fetch_add(256);
+      if (s >= n) break;
+      uint32_t e = s + 256 < n ? s + 256 : n;
+      for (uint32_t i = s; i < e; i++)
+        path_one(B, rays[i], i, tlas_idx ? tlas_idx[i] : tlas_uniform, max_bounces, rr_start, albedo, rr_survive,
+                 seed, out + 2 * (size_t)i, &sg[17 * (size_t)w], cn[w]);
+    }
+  };
+  std::vector<std::thread> th;
+  for (int w = 0; w < threads; w++) th.emplace_back(work, w);
+  for (auto& t : th) t.join();
+  auto t1 = std::chrono::steady_clock::now();
+  if (seconds) *seconds = std::chrono::duration<double>(t1 - t0).count();
+  if (seg)
+    for (uint32_t k = 0; k <= max_bounces; k++) {
+      seg[k] = 0;
+      for (int w = 0; w < threads; w++) seg[k] += sg[17 * (size_t)w + k];
+    }
   return 0;
 }
 

@@ -28,6 +28,7 @@ UNITS = {
     "trace.cu": ["-fmad=false"],
     "wavefront.cu": ["-fmad=false"],
     "wavefront_static.cu": [],
+    "paths.cu": ["-fmad=false"],
 }
 
 

@@ -1,0 +1,183 @@
+// Batched multi-scene path tracing, sm_103a.
+//
+// The reference's path tracer (scene/rendering/gpu-ray-tracing/src/feature/path_tracing/
+// ray_gen.rs:89-211, ray_hit.rs:12-103) loops up to max_path_depth bounces per
+// pixel through the task graph, one wavefront round per bounce. Here every ray
+// of every scene goes through one persistent launch per bounce:
+//
+//   path_kernel: warps fetch 32 queue entries at a time from a global work
+//   counter (load balance across scenes of very different size and across
+//   paths of different length); each entry is a 32 B ray plus a 16 B path
+//   state {output id, TLAS index, throughput, flags}. Closest hit in the
+//   entry's own scene (the reference's per-ray tlas_idx, traverse_cpu.rs:63),
+//   then one cosine-weighted diffuse bounce from an offset_ray_hit origin,
+//   Russian roulette from the configured bounce on, and a warp-ballot /
+//   one-atomic-per-warp append of the surviving path to the next queue.
+//
+// Path semantics (shared with the oracle): albedo a; a miss at bounce k
+// writes radiance = throughput (sky = 1) and depth k; a hit at k == max_bounces
+// or a path killed by roulette writes radiance 0. The sampler for bounce k of
+// path i is xxhash32(i, k, seed) -> next() x3 (direction, roulette).
+// Built with -fmad=false, like every traversal unit.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "paths.h"
+#include "shade.cuh"
+#include "traverse.cuh"
+
+namespace rdn {
+namespace {
+
+using namespace dev;
+
+template <bool ORDERED>
+__global__ void __launch_bounds__(128) path_kernel(TraceParams p, PathParams q, uint32_t bounce) {
+  extern __shared__ uint2 smem_stack[];
+  const uint32_t n = bounce == 0 ? q.count : *(volatile uint32_t*)(q.queue_count + bounce - 1);
+  const uint32_t lane = threadIdx.x & 31u;
+  const float4* in_rays = reinterpret_cast<const float4*>(bounce & 1 ? q.rays_b : q.rays_a);
+  const uint4* in_state = reinterpret_cast<const uint4*>(bounce & 1 ? q.state_b : q.state_a);
+  float4* out_rays = reinterpret_cast<float4*>(bounce & 1 ? q.rays_a : q.rays_b);
+  uint4* out_state = reinterpret_cast<uint4*>(bounce & 1 ? q.state_a : q.state_b);
+  uint32_t* work = q.work_counter + bounce;
+  for (;;) {
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(work, 32u);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= n) break;
+    const uint32_t j = base + lane;
+    bool keep = false;
+    float4 nr0 = make_float4(0.f, 0.f, 0.f, 0.f), nr1 = nr0;
+    uint4 ns = make_uint4(0u, 0u, 0u, 0u);
+    if (j < n) {
+      float4 r0, r1;
+      uint32_t id, tlas;
+      float throughput;
+      if (bounce == 0) {
+        const float4* rp = q.primary_rays + 2 * (size_t)j;
+        r0 = __ldg(rp);
+        r1 = __ldg(rp + 1);
+        id = j;
+        tlas = q.tlas_idx ? __ldg(q.tlas_idx + j) : q.tlas_uniform;
+        throughput = 1.0f;
+      } else {
+        r0 = in_rays[2 * (size_t)j];
+        r1 = in_rays[2 * (size_t)j + 1];
+        const uint4 s = in_state[j];
+        id = s.x;
+        tlas = s.y;
+        throughput = __uint_as_float(s.z);
+      }
+      RayCtx R;
+      R.o = make_float3(r0.x, r0.y, r0.z);
+      R.tmin = r0.w;
+      R.d = make_float3(r1.x, r1.y, r1.z);
+      R.tmax = r1.w;
+      R.cull_mask = 0xFFu;
+      R.ray_flags = 0u;
+      bool bad;
+      traverse_ray<ORDERED, false>(p, R, tlas, smem_stack + threadIdx.x, blockDim.x, bad);
+      if (!R.best.have) {
+        q.out[id] = make_float2(throughput, __uint_as_float(bounce | RDN_PATH_ESCAPED));
+      } else if (bounce == q.max_bounces) {
+        q.out[id] = make_float2(0.0f, __uint_as_float(bounce));
+      } else {
+        uint32_t st = xxhash32(id, bounce, q.seed);
+        const float s0 = sample_next(st);
+        const float s1 = sample_next(st);
+        const float s2 = sample_next(st);
+        float t_next = throughput * q.albedo;
+        bool survive = true;
+        if (bounce + 1 >= q.rr_start) {
+          survive = s2 < q.rr_survive;
+          t_next = t_next / q.rr_survive;
+        }
+        if (!survive) {
+          q.out[id] = make_float2(0.0f, __uint_as_float(bounce | RDN_PATH_ROULETTE));
+        } else {
+          const float3 hp = R.o + R.d * R.best.t;
+          const float3 nf = facing_normal(p, R.best.k, R.best.inst, R.d);
+          const float3 org = offset_ray_hit(hp, nf);
+          const float3 dir = cosine_sample_in_dir(nf, s0, s1);
+          nr0 = make_float4(org.x, org.y, org.z, 1.1920929e-7f);
+          nr1 = make_float4(dir.x, dir.y, dir.z, 3.40282347e+38f);
+          ns = make_uint4(id, tlas, __float_as_uint(t_next), 0u);
+          keep = true;
+        }
+      }
+    }
+    const uint32_t slot = warp_append(q.queue_count + bounce, keep);
+    if (keep) {
+      out_rays[2 * (size_t)slot] = nr0;
+      out_rays[2 * (size_t)slot + 1] = nr1;
+      out_state[slot] = ns;
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0 && q.segment_counts) q.segment_counts[bounce] = n;
+}
+
+}  // namespace
+
+size_t paths_scratch_bytes(uint32_t count, uint32_t max_bounces) {
+  auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  const size_t n = count;
+  return 256 + up(sizeof(uint32_t) * 2 * (max_bounces + 1)) + 2 * up(n * 32) + 2 * up(n * 16);
+}
+
+void paths_bind_scratch(PathParams& q, void* scratch) {
+  auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  const size_t n = q.count;
+  char* s = static_cast<char*>(scratch);
+  q.queue_count = reinterpret_cast<uint32_t*>(s + 256);
+  q.work_counter = q.queue_count + (q.max_bounces + 1);
+  size_t off = 256 + up(sizeof(uint32_t) * 2 * (q.max_bounces + 1));
+  q.rays_a = s + off;
+  off += up(n * 32);
+  q.rays_b = s + off;
+  off += up(n * 32);
+  q.state_a = s + off;
+  off += up(n * 16);
+  q.state_b = s + off;
+}
+
+cudaError_t prepare_paths(const TraceParams& p, const PathParams& q, bool ordered, uint32_t block, int sm_count,
+                          uint32_t* grid) {
+  if (block == 0) block = 128;
+  const size_t smem = ordered ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
+  static bool attr_done[2] = {false, false};
+  const void* fn = ordered ? (const void*)path_kernel<true> : (const void*)path_kernel<false>;
+  if (!attr_done[ordered ? 1 : 0]) {
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e != cudaSuccess) return e;
+    attr_done[ordered ? 1 : 0] = true;
+  }
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (int)block, smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) per_sm = 1;
+  // persistent grid, never larger than the primary queue needs
+  uint32_t g = (uint32_t)(sm_count * per_sm);
+  const uint32_t need = (q.count + block - 1) / block;
+  *grid = g > need ? need : g;
+  return cudaSuccess;
+}
+
+cudaError_t record_paths(const TraceParams& p, const PathParams& q, bool ordered, uint32_t block, uint32_t grid,
+                         cudaStream_t stream) {
+  if (block == 0) block = 128;
+  if (q.count == 0 || grid == 0) return cudaSuccess;
+  const size_t smem = ordered ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
+  cudaError_t e = cudaMemsetAsync(q.queue_count, 0, sizeof(uint32_t) * 2 * (q.max_bounces + 1), stream);
+  if (e != cudaSuccess) return e;
+  for (uint32_t b = 0; b <= q.max_bounces; b++) {
+    if (ordered) path_kernel<true><<<grid, block, smem, stream>>>(p, q, b);
+    else path_kernel<false><<<grid, block, smem, stream>>>(p, q, b);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+}  // namespace rdn

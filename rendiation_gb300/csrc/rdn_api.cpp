@@ -9,6 +9,7 @@
 
 #include "rdn_core.h"
 #include "trace_kernels.h"
+#include "paths.h"
 #include "wavefront.h"
 
 using rdn::DevBuf;
@@ -458,6 +459,134 @@ rdn_status rdn_wavefront_shadow_bounce(rdn_ctx* c, const rdn_wavefront_desc* d, 
     e = rdn::launch_wavefront(p, w, d->traversal == RDN_TRAVERSAL_ORDERED, d->block_size, c->sm_count,
                               d->phases, static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(c, e, "wavefront launch");
+  return RDN_OK;
+}
+
+}  // extern "C"
+
+struct rdn_graph {
+  cudaGraphExec_t exec = nullptr;
+  cudaGraph_t graph = nullptr;
+  int device = -1;
+};
+
+namespace {
+
+rdn_status prepare_path_launch(rdn_ctx* c, const rdn_path_desc* d, rdn::TraceParams& p, rdn::PathParams& q,
+                               uint32_t* grid) {
+  if (!c || !d) return fail(c, RDN_ERR_INVALID_ARG, "null context or descriptor");
+  if (c->device < 0) return fail(c, RDN_ERR_UNSUPPORTED, "host-only context cannot trace");
+  if (d->max_bounces > 16) return fail(c, RDN_ERR_INVALID_ARG, "max_bounces above 16");
+  if (d->count && (!d->rays || !d->out || !d->scratch)) return fail(c, RDN_ERR_INVALID_ARG, "null buffer");
+  if (d->scratch_bytes < rdn::paths_scratch_bytes(d->count, d->max_bounces))
+    return fail(c, RDN_ERR_INVALID_ARG, "scratch too small");
+  if ((reinterpret_cast<uintptr_t>(d->scratch) & 255) || (reinterpret_cast<uintptr_t>(d->rays) & 15) ||
+      (reinterpret_cast<uintptr_t>(d->out) & 7))
+    return fail(c, RDN_ERR_INVALID_ARG, "misaligned buffer");
+  if (d->traversal > RDN_TRAVERSAL_REFERENCE) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
+  if (d->block_size && (d->block_size % 32 || d->block_size > 128))
+    return fail(c, RDN_ERR_INVALID_ARG, "block_size must be a multiple of 32 up to 128");
+  if (!(d->rr_survive > 0.0f && d->rr_survive <= 1.0f)) return fail(c, RDN_ERR_INVALID_ARG, "rr_survive not in (0, 1]");
+  rdn_status st = ensure_built(c);
+  if (st != RDN_OK) return st;
+  rdn_trace_desc td;
+  std::memset(&td, 0, sizeof(td));
+  td.tlas_uniform = d->tlas_uniform;
+  td.cull_mask = 0xFF;
+  fill_params(c, &td, p);
+  std::memset(&q, 0, sizeof(q));
+  q.primary_rays = reinterpret_cast<const float4*>(d->rays);
+  q.tlas_idx = d->tlas_idx;
+  q.count = d->count;
+  q.tlas_uniform = d->tlas_uniform;
+  q.max_bounces = d->max_bounces;
+  q.rr_start = d->rr_start;
+  q.seed = d->seed;
+  q.albedo = d->albedo;
+  q.rr_survive = d->rr_survive;
+  q.out = reinterpret_cast<float2*>(d->out);
+  q.segment_counts = d->segment_counts;
+  if (d->count) rdn::paths_bind_scratch(q, d->scratch);
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e == cudaSuccess && d->count)
+    e = rdn::prepare_paths(p, q, d->traversal == RDN_TRAVERSAL_ORDERED, d->block_size, c->sm_count, grid);
+  if (e != cudaSuccess) return cuda_fail(c, e, "path launch preparation");
+  return RDN_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+rdn_status rdn_paths_scratch_size(uint32_t count, uint32_t max_bounces, size_t* bytes) {
+  if (!bytes || max_bounces > 16) return RDN_ERR_INVALID_ARG;
+  *bytes = rdn::paths_scratch_bytes(count, max_bounces);
+  return RDN_OK;
+}
+
+rdn_status rdn_trace_paths(rdn_ctx* c, const rdn_path_desc* d, void* stream) {
+  if (!c) return RDN_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(c->lock);
+  rdn::TraceParams p;
+  rdn::PathParams q;
+  uint32_t grid = 0;
+  rdn_status st = prepare_path_launch(c, d, p, q, &grid);
+  if (st != RDN_OK || d->count == 0) return st;
+  cudaError_t e = rdn::record_paths(p, q, d->traversal == RDN_TRAVERSAL_ORDERED, d->block_size, grid,
+                                    static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(c, e, "path launch");
+  return RDN_OK;
+}
+
+rdn_status rdn_trace_paths_graph(rdn_ctx* c, const rdn_path_desc* d, rdn_graph** out) {
+  if (!c || !out) return RDN_ERR_INVALID_ARG;
+  *out = nullptr;
+  std::lock_guard<std::mutex> lk(c->lock);
+  rdn::TraceParams p;
+  rdn::PathParams q;
+  uint32_t grid = 0;
+  rdn_status st = prepare_path_launch(c, d, p, q, &grid);
+  if (st != RDN_OK) return st;
+  cudaStream_t s = nullptr;
+  cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return cuda_fail(c, e, "capture stream");
+  auto* g = new (std::nothrow) rdn_graph();
+  if (!g) {
+    cudaStreamDestroy(s);
+    return fail(c, RDN_ERR_OOM, "host allocation failed");
+  }
+  g->device = c->device;
+  e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    cudaError_t rec = d->count ? rdn::record_paths(p, q, d->traversal == RDN_TRAVERSAL_ORDERED, d->block_size, grid, s)
+                               : cudaSuccess;
+    e = cudaStreamEndCapture(s, &g->graph);
+    if (rec != cudaSuccess) e = rec;
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&g->exec, g->graph, 0);
+  cudaStreamDestroy(s);
+  if (e != cudaSuccess) {
+    if (g->graph) cudaGraphDestroy(g->graph);
+    delete g;
+    return cuda_fail(c, e, "path graph capture");
+  }
+  *out = g;
+  return RDN_OK;
+}
+
+rdn_status rdn_graph_launch(rdn_graph* g, void* stream) {
+  if (!g || !g->exec) return RDN_ERR_INVALID_ARG;
+  cudaError_t e = cudaSetDevice(g->device);
+  if (e == cudaSuccess) e = cudaGraphLaunch(g->exec, static_cast<cudaStream_t>(stream));
+  return e == cudaSuccess ? RDN_OK : RDN_ERR_CUDA;
+}
+
+rdn_status rdn_graph_destroy(rdn_graph* g) {
+  if (!g) return RDN_ERR_INVALID_ARG;
+  cudaSetDevice(g->device);
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  delete g;
   return RDN_OK;
 }
 

@@ -24,7 +24,8 @@ EXPORTED_SYMBOLS = [
     "rdn_api_version", "rdn_create", "rdn_destroy", "rdn_last_error", "rdn_blas_create", "rdn_blas_delete",
     "rdn_tlas_create", "rdn_tlas_delete", "rdn_bind_tlas", "rdn_build", "rdn_get_build_stats", "rdn_get_built_array",
     "rdn_trace", "rdn_trace_counted", "rdn_wavefront_scratch_size", "rdn_wavefront_shadow_bounce",
-    "rdn_wavefront_shadow_bounce_static",
+    "rdn_wavefront_shadow_bounce_static", "rdn_paths_scratch_size", "rdn_trace_paths", "rdn_trace_paths_graph",
+    "rdn_graph_launch", "rdn_graph_destroy",
 ]
 
 
@@ -80,6 +81,14 @@ class WavefrontDesc(C.Structure):
                 ("ray_counts", C.c_void_p), ("phases", C.c_uint32), ("reserved", C.c_uint32)]
 
 
+class PathDesc(C.Structure):
+    _fields_ = [("rays", C.c_void_p), ("tlas_idx", C.c_void_p), ("count", C.c_uint32), ("tlas_uniform", C.c_uint32),
+                ("max_bounces", C.c_uint32), ("rr_start", C.c_uint32), ("albedo", C.c_float),
+                ("rr_survive", C.c_float), ("seed", C.c_uint32), ("traversal", C.c_uint32),
+                ("block_size", C.c_uint32), ("reserved", C.c_uint32), ("out", C.c_void_p), ("scratch", C.c_void_p),
+                ("scratch_bytes", C.c_size_t), ("segment_counts", C.c_void_p)]
+
+
 _lib = None
 
 
@@ -125,5 +134,15 @@ def lib() -> C.CDLL:
     L.rdn_wavefront_shadow_bounce.restype = i32
     L.rdn_wavefront_shadow_bounce_static.argtypes = [vp, C.POINTER(WavefrontDesc), vp]
     L.rdn_wavefront_shadow_bounce_static.restype = i32
+    L.rdn_paths_scratch_size.argtypes = [u32, u32, C.POINTER(C.c_size_t)]
+    L.rdn_paths_scratch_size.restype = i32
+    L.rdn_trace_paths.argtypes = [vp, C.POINTER(PathDesc), vp]
+    L.rdn_trace_paths.restype = i32
+    L.rdn_trace_paths_graph.argtypes = [vp, C.POINTER(PathDesc), C.POINTER(vp)]
+    L.rdn_trace_paths_graph.restype = i32
+    L.rdn_graph_launch.argtypes = [vp, vp]
+    L.rdn_graph_launch.restype = i32
+    L.rdn_graph_destroy.argtypes = [vp]
+    L.rdn_graph_destroy.restype = i32
     _lib = L
     return L

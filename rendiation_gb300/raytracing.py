@@ -269,6 +269,74 @@ class Wavefront:
         return int(c[0]), int(c[1]), int(c[2])
 
 
+PATH_DTYPE = np.dtype([("radiance", np.float32), ("depth_flags", np.uint32)])
+PATH_ESCAPED = 0x80000000
+PATH_ROULETTE = 0x40000000
+
+
+class Paths:
+    """Batched diffuse paths (rdn_trace_paths) over rays of many scenes; each ray
+    carries its index into the bound TLAS list. Buffers are torch CUDA tensors."""
+
+    def __init__(self, system: AccelerationStructureSystem, rays, tlas_idx=None, tlas_uniform=0, max_bounces=4,
+                 rr_start=2, albedo=0.5, rr_survive=0.5, seed=0, traversal=TRAVERSAL_ORDERED, block_size=0):
+        import torch
+
+        self.system = system
+        self.rays = rays
+        self.tlas_idx = tlas_idx
+        n = rays.shape[0]
+        self.n = n
+        self.max_bounces = max_bounces
+        size = C.c_size_t()
+        _check(None, system._L.rdn_paths_scratch_size(n, max_bounces, C.byref(size)))
+        self.scratch = torch.empty(size.value + 256, dtype=torch.uint8, device="cuda")
+        self.scratch_ptr = (self.scratch.data_ptr() + 255) & ~255
+        self.out = torch.empty((max(n, 1), 2), dtype=torch.float32, device="cuda")
+        self.segments_dev = torch.zeros(max_bounces + 1, dtype=torch.int32, device="cuda")
+        self.desc = native.PathDesc(rays.data_ptr(), 0 if tlas_idx is None else tlas_idx.data_ptr(), n, tlas_uniform,
+                                    max_bounces, rr_start, albedo, rr_survive, seed, traversal, block_size, 0,
+                                    self.out.data_ptr(), self.scratch_ptr, size.value, self.segments_dev.data_ptr())
+        self.graph = None
+
+    def run(self, stream=None):
+        import torch
+
+        s = (stream or torch.cuda.current_stream()).cuda_stream
+        _check(self.system._h, self.system._L.rdn_trace_paths(self.system._h, C.byref(self.desc), C.c_void_p(s)))
+
+    def capture(self):
+        """Captures the launches once into a CUDA graph (rdn_trace_paths_graph)."""
+        g = C.c_void_p()
+        _check(self.system._h, self.system._L.rdn_trace_paths_graph(self.system._h, C.byref(self.desc), C.byref(g)))
+        self.graph = g
+
+    def launch_graph(self, stream=None):
+        import torch
+
+        s = (stream or torch.cuda.current_stream()).cuda_stream
+        st = self.system._L.rdn_graph_launch(self.graph, C.c_void_p(s))
+        if st != native.RDN_OK:
+            raise native.RdnError(st, "rdn_graph_launch failed")
+
+    def close(self):
+        if self.graph:
+            self.system._L.rdn_graph_destroy(self.graph)
+            self.graph = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def results(self) -> np.ndarray:
+        return self.out.cpu().numpy()[: self.n].view(PATH_DTYPE).reshape(-1)
+
+    def segments(self) -> list[int]:
+        return [int(x) for x in self.segments_dev.cpu().numpy()]
+
+
 def hits_to_numpy(hits) -> np.ndarray:
     """(N,4) f32 CUDA tensor -> structured array (t, u, v, prim)."""
     h = hits.detach().cpu().numpy().astype(np.float32, copy=False)

@@ -217,3 +217,29 @@ def sphere_rays(n: int, box_min, box_max, seed: int, tmin: float = 0.0, tmax: fl
 def log_uniform_ints(n: int, lo: float, hi: float, seed: int) -> np.ndarray:
     rng = _rng(seed)
     return np.exp(rng.uniform(math.log(lo), math.log(hi), n)).astype(np.int64)
+
+
+@dataclass
+class BatchedScenes:
+    """Many independent triangle soups with rays of uneven count per scene."""
+
+    meshes: list
+    rays: np.ndarray       # all scenes' rays, grouped by scene
+    tlas_idx: np.ndarray   # scene index of every ray
+    ray_offsets: np.ndarray  # rays of scene s are rays[ray_offsets[s]:ray_offsets[s+1]]
+
+
+def batched_soups(n_scenes: int = 256, tri_range=(1_000, 200_000), ray_range=(4_096, 262_144), seed: int = 2,
+                  offset: float = 0.02) -> BatchedScenes:
+    """Batched workload: soups generated as triangle_soup with log-uniform
+    triangle counts, rays per scene log-uniform, origins uniform in the scene's
+    box [-offset, 1+offset]^3 and directions uniform on the sphere."""
+    tris = log_uniform_ints(n_scenes, tri_range[0], tri_range[1], seed)
+    nrays = log_uniform_ints(n_scenes, ray_range[0], ray_range[1], seed + 1)
+    meshes, rays, idx = [], [], []
+    for s in range(n_scenes):
+        meshes.append(triangle_soup(int(tris[s]), seed=1000 + s, offset=offset))
+        rays.append(sphere_rays(int(nrays[s]), (-offset,) * 3, (1 + offset,) * 3, seed=50_000 + s))
+        idx.append(np.full(int(nrays[s]), s, np.uint32))
+    offs = np.concatenate([[0], np.cumsum(nrays)]).astype(np.int64)
+    return BatchedScenes(meshes, np.concatenate(rays), np.concatenate(idx), offs)
