@@ -410,6 +410,83 @@ def bench_batched(args):
     }
 
 
+def bench_adjoint(args):
+    """Differentiable closest hit: heightfield 256^2 (130,050 tris) with a
+    per-vertex attribute uniform in [0,1], 512x512 primary rays, loss =
+    sum (interpolated attribute - target)^2 with the target rendered from a
+    copy whose heights are jittered by N(0, 0.005). Forward alone against
+    forward + adjoint (hits recomputed in the adjoint)."""
+    import ctypes as C
+
+    import torch
+
+    from rendiation_gb300 import native
+    from rendiation_gb300 import raytracing as rt
+    from rendiation_gb300 import scenes
+
+    n_grid, res = 256, 512
+    L = native.lib()
+    mesh = scenes.heightfield(n_grid, seed=1)
+    jit = scenes.heightfield(n_grid, seed=1, jitter_sigma=0.005, jitter_seed=4242)
+    rng = np.random.Generator(np.random.PCG64(17))
+    attr = torch.from_numpy(rng.random(mesh.positions.shape[0]).astype(np.float32)).cuda()
+    cam = scenes.PinholeCamera.look_at((0.5, -0.5, 0.8), (0.5, 0.5, 0.0), 20.0, res, res)
+    rays = torch.from_numpy(scenes.pinhole_rays(cam).view(np.float32).reshape(-1, 8).copy()).cuda()
+    n = res * res
+    traversal = rt.TRAVERSAL_REFERENCE if args.traversal == "reference" else rt.TRAVERSAL_ORDERED
+
+    def system(m):
+        P = rt.AccelerationStructureSystem(device=0)
+        b = P.create_bottom_level_acceleration_structure([rt.BottomLevelAccelerationStructureBuildSource(
+            m.positions, m.indices)])
+        P.bind_tlas([P.create_top_level_acceleration_structure([rt.TopLevelAccelerationStructureSourceInstance(b)])])
+        P.build(blas_bin_size=4)
+        return P
+
+    Pt = system(jit)
+    target = torch.zeros(n, device="cuda")
+    d = native.AttrLossDesc(rays.data_ptr(), n, 0, attr.data_ptr(), None, target.data_ptr(), None, None, None, None,
+                            None, 1.0, traversal, 0, 0)
+    assert L.rdn_attr_loss_forward(Pt._h, C.byref(d), None) == 0
+    torch.cuda.synchronize()
+    Pt.close()
+    P = system(mesh)
+    loss = torch.zeros(1, dtype=torch.float64, device="cuda")
+    grad = torch.zeros((mesh.positions.shape[0], 4), device="cuda")
+    fwd = native.AttrLossDesc(rays.data_ptr(), n, 0, attr.data_ptr(), target.data_ptr(), None, None,
+                              loss.data_ptr(), None, None, None, 1.0, traversal, 0, 0)
+    adj = native.AttrLossDesc(rays.data_ptr(), n, 0, attr.data_ptr(), target.data_ptr(), None, None, None,
+                              grad.data_ptr(), None, None, 1.0, traversal, 0, 0)
+    stream = torch.cuda.current_stream()
+    sp = C.c_void_p(stream.cuda_stream)
+
+    def run(with_adjoint):
+        loss.zero_()
+        assert L.rdn_attr_loss_forward(P._h, C.byref(fwd), sp) == 0
+        if with_adjoint:
+            grad.zero_()
+            assert L.rdn_attr_loss_adjoint(P._h, C.byref(adj), sp) == 0
+
+    out = {}
+    for name, w in (("forward", False), ("forward_adjoint", True)):
+        for _ in range(args.warmup):
+            run(w)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = 50
+        e0.record(stream)
+        for _ in range(reps):
+            run(w)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out[name + "_ms"] = round(e0.elapsed_time(e1) / reps, 4)
+        out[name + "_mrays"] = round(n / (e0.elapsed_time(e1) / reps / 1e3) / 1e6, 2)
+    out["fwd_adjoint_over_fwd"] = round(out["forward_adjoint_ms"] / out["forward_ms"], 3)
+    out["loss"] = float(loss.item())
+    out["workload"] = f"heightfield {n_grid}^2 ({mesh.triangle_count} tris), {res}x{res} rays, attribute loss"
+    P.close()
+    return out
+
+
 def cpu_baseline_wavefront(S, cam, threads: int, budget_s: float, steps: int = 1):
     """The oracle's pipeline on host cores over a bounded band of rows (BVH built beforehand)."""
     from oracle import orc
@@ -483,6 +560,7 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU work for the CPU baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--scenes", type=int, default=256)
     ap.add_argument("--batched-steps", type=int, default=5)
     args = ap.parse_args()
@@ -504,6 +582,8 @@ def main():
     if not args.no_batched:
         P.close()
         out["batched"] = bench_batched(args)
+    if not args.no_adjoint:
+        out["adjoint"] = bench_adjoint(args)
     if rank == 0:
         if not args.no_cpu_baseline:
             cb, _ = cpu_baseline_wavefront(oracle_heightfield(mesh), cam, os.cpu_count() or 1,

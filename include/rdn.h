@@ -350,6 +350,40 @@ rdn_status rdn_trace_paths_graph(rdn_ctx* ctx, const rdn_path_desc* desc, rdn_gr
 rdn_status rdn_graph_launch(rdn_graph* graph, void* stream);
 rdn_status rdn_graph_destroy(rdn_graph* graph);
 
+/* ---- differentiable closest hit (frozen visibility) ------------------ */
+
+/* Loss = sum over rays of (value - target)^2, value = the hit triangle's vertex
+ * attribute interpolated with the hit barycentrics (1-u-v, u, v); misses add
+ * nothing. Vertices are those of the built vertex array (all geometries'
+ * positions in creation order, rdn_get_built_array(..., 10, ...)). */
+typedef struct rdn_attr_loss_desc {
+  const rdn_ray* rays;          /* device */
+  uint32_t count;
+  uint32_t tlas_uniform;
+  const float* attributes;      /* device, one per built vertex */
+  const float* targets;         /* device, one per ray; NULL = 0 */
+  float* ray_value;             /* device, nullable: interpolated attribute per ray (forward) */
+  float* ray_loss;              /* device, nullable: per-ray loss (forward) */
+  double* loss_sum;             /* device, nullable: loss added here (forward; not reset) */
+  float* grad_vertices;         /* device, 4 per built vertex: dL/dx, dL/dy, dL/dz, dL/dattr;
+                                   accumulated (adjoint; the caller zeroes it) */
+  float* grad_ray_origin;       /* device, nullable: 3 per ray (adjoint) */
+  float* grad_ray_direction;    /* device, nullable: 3 per ray (adjoint) */
+  float grad_scale;             /* upstream gradient of the loss sum (adjoint), usually 1 */
+  uint32_t traversal;           /* RDN_TRAVERSAL_* */
+  uint32_t block_size;          /* 0 = 128 */
+  uint32_t reserved;
+} rdn_attr_loss_desc;
+
+/* Forward: trace, interpolate, loss. Extends the reference's closest-hit query
+ * (traverse_cpu.rs:52-245) with a differentiable attribute read-out. */
+rdn_status rdn_attr_loss_forward(rdn_ctx* ctx, const rdn_attr_loss_desc* desc, void* stream);
+/* Adjoint at frozen visibility: re-traces every ray (the hit is recomputed, not
+ * stored), then scatters gradients with respect to vertex positions and
+ * attributes and writes per-ray gradients with respect to origin and direction
+ * (object space of the hit instance). */
+rdn_status rdn_attr_loss_adjoint(rdn_ctx* ctx, const rdn_attr_loss_desc* desc, void* stream);
+
 /* Allocation-free variant of rdn_wavefront_shadow_bounce; it has no
  * counterpart in the reference. For callers that cannot allocate device
  * memory (a host that hands out all device memory from its own budget fixed at

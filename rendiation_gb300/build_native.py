@@ -29,6 +29,7 @@ UNITS = {
     "wavefront.cu": ["-fmad=false"],
     "wavefront_static.cu": [],
     "paths.cu": ["-fmad=false"],
+    "adjoint.cu": ["-fmad=false"],
 }
 
 

@@ -9,6 +9,7 @@
 
 #include "rdn_core.h"
 #include "trace_kernels.h"
+#include "adjoint.h"
 #include "paths.h"
 #include "wavefront.h"
 
@@ -39,6 +40,7 @@ void free_device(rdn::DeviceBuilt& d) {
   free_buf(d.indices_redirect);
   free_buf(d.leaf_ranges);
   free_buf(d.geom_root_code);
+  free_buf(d.indices);
   free_buf(d.tlas_bvh_forest);
   free_buf(d.tri_bvh_forest);
   free_buf(d.tlas_data);
@@ -105,8 +107,10 @@ rdn_status do_build(rdn_ctx* c) {
     UP(wide_nodes, wide_nodes)
     UP(leaf_ranges, leaf_ranges)
     UP(geom_root_code, geom_root_code)
+    UP(indices, indices)
 #undef UP
     d.max_blas_depth = hb->max_blas_depth;
+    d.vertex_count = hb->vertices.size() / 3;
     d.bytes = bytes;
     c->upload_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t1).count();
   }
@@ -587,6 +591,79 @@ rdn_status rdn_graph_destroy(rdn_graph* g) {
   if (g->exec) cudaGraphExecDestroy(g->exec);
   if (g->graph) cudaGraphDestroy(g->graph);
   delete g;
+  return RDN_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+rdn_status prepare_attr(rdn_ctx* c, const rdn_attr_loss_desc* d, bool adjoint, rdn::TraceParams& p,
+                        rdn::AdjointParams& a) {
+  if (!c || !d) return fail(c, RDN_ERR_INVALID_ARG, "null context or descriptor");
+  if (c->device < 0) return fail(c, RDN_ERR_UNSUPPORTED, "host-only context cannot trace");
+  if (d->count && (!d->rays || !d->attributes)) return fail(c, RDN_ERR_INVALID_ARG, "null rays or attributes");
+  if (adjoint && d->count && !d->grad_vertices) return fail(c, RDN_ERR_INVALID_ARG, "null gradient buffer");
+  if ((reinterpret_cast<uintptr_t>(d->rays) & 15) || (reinterpret_cast<uintptr_t>(d->grad_vertices) & 15))
+    return fail(c, RDN_ERR_INVALID_ARG, "rays and gradients must be 16-byte aligned");
+  if (d->traversal > RDN_TRAVERSAL_REFERENCE) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
+  if (d->block_size && (d->block_size % 32 || d->block_size > 128))
+    return fail(c, RDN_ERR_INVALID_ARG, "block_size must be a multiple of 32 up to 128");
+  rdn_status st = ensure_built(c);
+  if (st != RDN_OK) return st;
+  rdn_trace_desc td;
+  std::memset(&td, 0, sizeof(td));
+  td.tlas_uniform = d->tlas_uniform;
+  td.cull_mask = 0xFF;
+  fill_params(c, &td, p);
+  std::memset(&a, 0, sizeof(a));
+  a.rays = reinterpret_cast<const float4*>(d->rays);
+  a.count = d->count;
+  a.tlas_uniform = d->tlas_uniform;
+  a.indices = c->dev.indices.ptr;
+  a.attributes = d->attributes;
+  a.targets = d->targets;
+  a.ray_value = d->ray_value;
+  a.ray_loss = d->ray_loss;
+  a.loss_sum = d->loss_sum;
+  a.grad_vertices = d->grad_vertices;
+  a.grad_ray_origin = d->grad_ray_origin;
+  a.grad_ray_direction = d->grad_ray_direction;
+  a.grad_scale = d->grad_scale;
+  return RDN_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+rdn_status rdn_attr_loss_forward(rdn_ctx* c, const rdn_attr_loss_desc* d, void* stream) {
+  if (!c) return RDN_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(c->lock);
+  rdn::TraceParams p;
+  rdn::AdjointParams a;
+  rdn_status st = prepare_attr(c, d, false, p, a);
+  if (st != RDN_OK) return st;
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e == cudaSuccess)
+    e = rdn::launch_attr_forward(p, a, d->traversal == RDN_TRAVERSAL_ORDERED, d->block_size,
+                                 static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(c, e, "attribute loss forward");
+  return RDN_OK;
+}
+
+rdn_status rdn_attr_loss_adjoint(rdn_ctx* c, const rdn_attr_loss_desc* d, void* stream) {
+  if (!c) return RDN_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(c->lock);
+  rdn::TraceParams p;
+  rdn::AdjointParams a;
+  rdn_status st = prepare_attr(c, d, true, p, a);
+  if (st != RDN_OK) return st;
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e == cudaSuccess)
+    e = rdn::launch_attr_adjoint(p, a, d->traversal == RDN_TRAVERSAL_ORDERED, d->block_size,
+                                 static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(c, e, "attribute loss adjoint");
   return RDN_OK;
 }
 

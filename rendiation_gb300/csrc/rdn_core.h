@@ -120,7 +120,7 @@ struct DevBuf {
 };
 
 struct DeviceBuilt {
-  DevBuf<uint32_t> tlas_binding, tlas_bvh_root, indices_redirect, leaf_ranges, geom_root_code;
+  DevBuf<uint32_t> tlas_binding, tlas_bvh_root, indices_redirect, leaf_ranges, geom_root_code, indices;
   DevBuf<DeviceBVHNode> tlas_bvh_forest, tri_bvh_forest;
   DevBuf<DeviceInstance> tlas_data;
   DevBuf<TlasBounding> tlas_bounding;
@@ -129,6 +129,7 @@ struct DeviceBuilt {
   DevBuf<TriRecord> tri_records;
   DevBuf<WideNode> wide_nodes;
   uint32_t max_blas_depth = 0;
+  uint64_t vertex_count = 0;
   uint64_t bytes = 0;
 };
 

@@ -25,7 +25,7 @@ EXPORTED_SYMBOLS = [
     "rdn_tlas_create", "rdn_tlas_delete", "rdn_bind_tlas", "rdn_build", "rdn_get_build_stats", "rdn_get_built_array",
     "rdn_trace", "rdn_trace_counted", "rdn_wavefront_scratch_size", "rdn_wavefront_shadow_bounce",
     "rdn_wavefront_shadow_bounce_static", "rdn_paths_scratch_size", "rdn_trace_paths", "rdn_trace_paths_graph",
-    "rdn_graph_launch", "rdn_graph_destroy",
+    "rdn_graph_launch", "rdn_graph_destroy", "rdn_attr_loss_forward", "rdn_attr_loss_adjoint",
 ]
 
 
@@ -89,6 +89,14 @@ class PathDesc(C.Structure):
                 ("scratch_bytes", C.c_size_t), ("segment_counts", C.c_void_p)]
 
 
+class AttrLossDesc(C.Structure):
+    _fields_ = [("rays", C.c_void_p), ("count", C.c_uint32), ("tlas_uniform", C.c_uint32),
+                ("attributes", C.c_void_p), ("targets", C.c_void_p), ("ray_value", C.c_void_p),
+                ("ray_loss", C.c_void_p), ("loss_sum", C.c_void_p), ("grad_vertices", C.c_void_p),
+                ("grad_ray_origin", C.c_void_p), ("grad_ray_direction", C.c_void_p), ("grad_scale", C.c_float),
+                ("traversal", C.c_uint32), ("block_size", C.c_uint32), ("reserved", C.c_uint32)]
+
+
 _lib = None
 
 
@@ -144,5 +152,9 @@ def lib() -> C.CDLL:
     L.rdn_graph_launch.restype = i32
     L.rdn_graph_destroy.argtypes = [vp]
     L.rdn_graph_destroy.restype = i32
+    L.rdn_attr_loss_forward.argtypes = [vp, C.POINTER(AttrLossDesc), vp]
+    L.rdn_attr_loss_forward.restype = i32
+    L.rdn_attr_loss_adjoint.argtypes = [vp, C.POINTER(AttrLossDesc), vp]
+    L.rdn_attr_loss_adjoint.restype = i32
     _lib = L
     return L

@@ -12,7 +12,7 @@ pytestmark = pytest.mark.gpu
 
 @pytest.fixture(scope="module")
 def batched():
-    b = scenes.batched_soups(n_scenes=12, tri_range=(200, 3000), ray_range=(300, 3000), seed=7)
+    b = scenes.batched_soups(n_scenes=12, tri_range=(500, 3000), ray_range=(300, 3000), seed=7, offset=0.1)
     sc = Scene([[(m.positions, None, 1)] for m in b.meshes], [[{"blas": s}] for s in range(len(b.meshes))])
     return b, sc.build_oracle(), sc.build_product()
 
