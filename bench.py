@@ -176,7 +176,8 @@ def bench_wavefront(args, ws, rank):
     W, H = args.width, args.height
     mesh, P = build_heightfield_system(args.grid)
     cam = scenes.heightfield_camera(W, H)
-    traversal = rt.TRAVERSAL_REFERENCE if args.traversal == "reference" else rt.TRAVERSAL_ORDERED
+    traversal = {"reference": rt.TRAVERSAL_REFERENCE, "binary": rt.TRAVERSAL_ORDERED_BINARY}.get(
+        args.traversal, rt.TRAVERSAL_ORDERED)
     wf = rt.Wavefront(P, cam, LIGHT, traversal=traversal, block_size=args.block)
     stream = torch.cuda.current_stream()
 
@@ -342,7 +343,8 @@ def bench_batched(args):
     build_s = time.perf_counter() - t0
     rays = torch.from_numpy(b.rays.view(np.float32).reshape(-1, 8).copy()).cuda()
     tidx = torch.from_numpy(b.tlas_idx.astype(np.int32)).cuda()
-    traversal = rt.TRAVERSAL_REFERENCE if args.traversal == "reference" else rt.TRAVERSAL_ORDERED
+    traversal = {"reference": rt.TRAVERSAL_REFERENCE, "binary": rt.TRAVERSAL_ORDERED_BINARY}.get(
+        args.traversal, rt.TRAVERSAL_ORDERED)
     stream = torch.cuda.current_stream()
 
     batched = rt.Paths(P, rays, tidx, max_bounces=4, rr_start=2, seed=1, traversal=traversal)
@@ -433,7 +435,8 @@ def bench_adjoint(args):
     cam = scenes.PinholeCamera.look_at((0.5, -0.5, 0.8), (0.5, 0.5, 0.0), 20.0, res, res)
     rays = torch.from_numpy(scenes.pinhole_rays(cam).view(np.float32).reshape(-1, 8).copy()).cuda()
     n = res * res
-    traversal = rt.TRAVERSAL_REFERENCE if args.traversal == "reference" else rt.TRAVERSAL_ORDERED
+    traversal = {"reference": rt.TRAVERSAL_REFERENCE, "binary": rt.TRAVERSAL_ORDERED_BINARY}.get(
+        args.traversal, rt.TRAVERSAL_ORDERED)
 
     def system(m):
         P = rt.AccelerationStructureSystem(device=0)
@@ -555,7 +558,7 @@ def main():
     ap.add_argument("--grid", type=int, default=1024)
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
-    ap.add_argument("--traversal", default="ordered", choices=["ordered", "reference"])
+    ap.add_argument("--traversal", default="ordered", choices=["ordered", "binary", "reference"])
     ap.add_argument("--block", type=int, default=0)
     ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU work for the CPU baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")

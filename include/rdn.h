@@ -145,14 +145,17 @@ typedef struct rdn_hit_ext {
 } rdn_hit_ext;
 
 /* Traversal order.
- * RDN_TRAVERSAL_ORDERED: near-child-first stack traversal over 64 B two-child
- *   nodes. Closest hits equal the reference's except among hits at exactly
+ * RDN_TRAVERSAL_ORDERED: nearest-child-first stack traversal over 128 B
+ *   four-child nodes collapsed from the reference's tree (exact reference node
+ *   boxes). Closest hits equal the reference's except among hits at exactly
  *   equal distance; first-hit (shadow) queries agree on hit/miss.
  * RDN_TRAVERSAL_REFERENCE: the reference's stackless threaded hit/miss walk
  *   (traverse_cpu.rs:291-319) over its own 48 B node layout; bit-identical to
- *   the reference CPU traversal, including ties and which hit ends a search. */
+ *   the reference CPU traversal, including ties and which hit ends a search.
+ * RDN_TRAVERSAL_ORDERED_BINARY: as ORDERED over 64 B two-child nodes. */
 #define RDN_TRAVERSAL_ORDERED 0u
 #define RDN_TRAVERSAL_REFERENCE 1u
+#define RDN_TRAVERSAL_ORDERED_BINARY 2u
 
 /* Fixed any-hit policies for non-opaque geometry, standing in for a user
  * any-hit shader (RayAnyHitBehavior, api/ty.rs:134-136). */

@@ -51,7 +51,7 @@ __device__ __forceinline__ HitGeom hit_vertices(const TraceParams& p, const Adjo
   return h;
 }
 
-template <bool ORDERED>
+template <int MODE>
 __global__ void __launch_bounds__(128) attr_forward_kernel(TraceParams p, AdjointParams a) {
   extern __shared__ uint2 smem_stack[];
   __shared__ double block_sum[4];
@@ -68,7 +68,7 @@ __global__ void __launch_bounds__(128) attr_forward_kernel(TraceParams p, Adjoin
     R.cull_mask = 0xFFu;
     R.ray_flags = 0u;
     bool bad;
-    traverse_ray<ORDERED, false>(p, R, a.tlas_uniform, smem_stack + threadIdx.x, blockDim.x, bad);
+    traverse_ray<MODE, false>(p, R, a.tlas_uniform, smem_stack + threadIdx.x, blockDim.x, bad);
     float value = 0.0f;
     if (R.best.have) {
       const HitGeom h = hit_vertices(p, a, R);
@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(128) attr_forward_kernel(TraceParams p, Adjoin
   }
 }
 
-template <bool ORDERED>
+template <int MODE>
 __global__ void __launch_bounds__(128) attr_adjoint_kernel(TraceParams p, AdjointParams a) {
   extern __shared__ uint2 smem_stack[];
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -107,7 +107,7 @@ __global__ void __launch_bounds__(128) attr_adjoint_kernel(TraceParams p, Adjoin
   R.cull_mask = 0xFFu;
   R.ray_flags = 0u;
   bool bad;
-  traverse_ray<ORDERED, false>(p, R, a.tlas_uniform, smem_stack + threadIdx.x, blockDim.x, bad);
+  traverse_ray<MODE, false>(p, R, a.tlas_uniform, smem_stack + threadIdx.x, blockDim.x, bad);
   float3 go = make_float3(0.f, 0.f, 0.f), gd = go;
   if (R.best.have) {
     const HitGeom h = hit_vertices(p, a, R);
@@ -148,45 +148,44 @@ __global__ void __launch_bounds__(128) attr_adjoint_kernel(TraceParams p, Adjoin
   }
 }
 
-template <class K>
-cudaError_t setup(K kernel) {
-  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+template <int MODE>
+cudaError_t launch_attr_mode(const TraceParams& p, const AdjointParams& a, bool adjoint, uint32_t block,
+                             cudaStream_t stream) {
+  static bool done[2] = {false, false};
+  if (!done[adjoint]) {
+    cudaError_t e = adjoint ? cudaFuncSetAttribute(attr_adjoint_kernel<MODE>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024)
+                            : cudaFuncSetAttribute(attr_forward_kernel<MODE>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e != cudaSuccess) return e;
+    done[adjoint] = true;
+  }
+  const size_t smem = MODE != MODE_THREADED ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
+  const uint32_t grid = (a.count + block - 1) / block;
+  if (adjoint) attr_adjoint_kernel<MODE><<<grid, block, smem, stream>>>(p, a);
+  else attr_forward_kernel<MODE><<<grid, block, smem, stream>>>(p, a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_attr(const TraceParams& p, const AdjointParams& a, int mode, bool adjoint, uint32_t block,
+                        cudaStream_t stream) {
+  if (a.count == 0) return cudaSuccess;
+  if (block == 0) block = 128;
+  if (mode == MODE_WIDE4) return launch_attr_mode<MODE_WIDE4>(p, a, adjoint, block, stream);
+  if (mode == MODE_BINARY) return launch_attr_mode<MODE_BINARY>(p, a, adjoint, block, stream);
+  return launch_attr_mode<MODE_THREADED>(p, a, adjoint, block, stream);
 }
 
 }  // namespace
 
-cudaError_t launch_attr_forward(const TraceParams& p, const AdjointParams& a, bool ordered, uint32_t block,
+cudaError_t launch_attr_forward(const TraceParams& p, const AdjointParams& a, int mode, uint32_t block,
                                 cudaStream_t stream) {
-  if (a.count == 0) return cudaSuccess;
-  if (block == 0) block = 128;
-  static bool done[2] = {false, false};
-  if (!done[ordered]) {
-    cudaError_t e = ordered ? setup(attr_forward_kernel<true>) : setup(attr_forward_kernel<false>);
-    if (e != cudaSuccess) return e;
-    done[ordered] = true;
-  }
-  const size_t smem = ordered ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
-  const uint32_t grid = (a.count + block - 1) / block;
-  if (ordered) attr_forward_kernel<true><<<grid, block, smem, stream>>>(p, a);
-  else attr_forward_kernel<false><<<grid, block, smem, stream>>>(p, a);
-  return cudaGetLastError();
+  return launch_attr(p, a, mode, false, block, stream);
 }
 
-cudaError_t launch_attr_adjoint(const TraceParams& p, const AdjointParams& a, bool ordered, uint32_t block,
+cudaError_t launch_attr_adjoint(const TraceParams& p, const AdjointParams& a, int mode, uint32_t block,
                                 cudaStream_t stream) {
-  if (a.count == 0) return cudaSuccess;
-  if (block == 0) block = 128;
-  static bool done[2] = {false, false};
-  if (!done[ordered]) {
-    cudaError_t e = ordered ? setup(attr_adjoint_kernel<true>) : setup(attr_adjoint_kernel<false>);
-    if (e != cudaSuccess) return e;
-    done[ordered] = true;
-  }
-  const size_t smem = ordered ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
-  const uint32_t grid = (a.count + block - 1) / block;
-  if (ordered) attr_adjoint_kernel<true><<<grid, block, smem, stream>>>(p, a);
-  else attr_adjoint_kernel<false><<<grid, block, smem, stream>>>(p, a);
-  return cudaGetLastError();
+  return launch_attr(p, a, mode, true, block, stream);
 }
 
 }  // namespace rdn

@@ -23,9 +23,9 @@ struct AdjointParams {
   float grad_scale;           // upstream gradient of the loss sum
 };
 
-cudaError_t launch_attr_forward(const TraceParams& p, const AdjointParams& a, bool ordered, uint32_t block,
+cudaError_t launch_attr_forward(const TraceParams& p, const AdjointParams& a, int mode, uint32_t block,
                                 cudaStream_t stream);
-cudaError_t launch_attr_adjoint(const TraceParams& p, const AdjointParams& a, bool ordered, uint32_t block,
+cudaError_t launch_attr_adjoint(const TraceParams& p, const AdjointParams& a, int mode, uint32_t block,
                                 cudaStream_t stream);
 
 }  // namespace rdn

@@ -258,10 +258,11 @@ DeviceBVHNode to_device_node(const TreeNode& n, std::pair<uint32_t, uint32_t> li
   return d;
 }
 
-// Two-child nodes for one tree; returns the root's child code.
-uint32_t emit_wide(const Tree& t, uint32_t prim_offset, HostBuilt& hb) {
+// Two-child nodes for one tree; returns the root's child code and fills
+// `code` (per binary node: wide index or LEAF_BIT | leaf id).
+uint32_t emit_wide(const Tree& t, uint32_t prim_offset, HostBuilt& hb, std::vector<uint32_t>& code) {
   const uint32_t nn = (uint32_t)t.nodes.size();
-  std::vector<uint32_t> code(nn);
+  code.assign(nn, 0);
   uint32_t next_inner = (uint32_t)hb.wide_nodes.size();
   uint32_t next_leaf = (uint32_t)(hb.leaf_ranges.size() / 2);
   for (uint32_t i = 0; i < nn; i++) code[i] = t.nodes[i].left_count ? next_inner++ : (LEAF_BIT | next_leaf++);
@@ -287,6 +288,62 @@ uint32_t emit_wide(const Tree& t, uint32_t prim_offset, HostBuilt& hb) {
     w.code[3] = 0;
   }
   return nn ? code[0] : (LEAF_BIT | 0);
+}
+
+float node_area(const Box& b) {
+  const float w = b.hi.x - b.lo.x, h = b.hi.y - b.lo.y, d = b.hi.z - b.lo.z;
+  return w * h + w * d + h * d;
+}
+
+// Four-child node rooted at binary inner node `bi`; returns its index and
+// raises *depth to the deepest four-child level below.
+uint32_t emit_wide4(const Tree& t, uint32_t bi, const std::vector<uint32_t>& code2, HostBuilt& hb, uint32_t level,
+                    uint32_t* depth) {
+  uint32_t slot[4];
+  int n = 0;
+  slot[n++] = bi + 1;
+  slot[n++] = bi + t.nodes[bi].left_count + 1;
+  while (n < 4) {
+    int best = -1;
+    float best_area = -1.0f;
+    for (int k = 0; k < n; k++) {
+      const TreeNode& c = t.nodes[slot[k]];
+      if (!c.left_count) continue;
+      const float a = node_area(c.box);
+      if (best < 0 || a > best_area) {
+        best = k;
+        best_area = a;
+      }
+    }
+    if (best < 0) break;
+    const uint32_t open = slot[best];
+    for (int k = n; k > best + 1; k--) slot[k] = slot[k - 1];
+    slot[best] = open + 1;
+    slot[best + 1] = open + t.nodes[open].left_count + 1;
+    n++;
+  }
+  const uint32_t me = (uint32_t)hb.wide4_nodes.size();
+  hb.wide4_nodes.emplace_back();
+  if (level + 1 > *depth) *depth = level + 1;
+  uint32_t codes[4] = {EMPTY_SLOT, EMPTY_SLOT, EMPTY_SLOT, EMPTY_SLOT};
+  for (int k = 0; k < n; k++) {
+    const TreeNode& c = t.nodes[slot[k]];
+    codes[k] = c.left_count ? emit_wide4(t, slot[k], code2, hb, level + 1, depth) : code2[slot[k]];
+  }
+  Wide4Node& w = hb.wide4_nodes[me];
+  for (int k = 0; k < 4; k++) {
+    const bool used = k < n;
+    const Box b = used ? t.nodes[slot[k]].box : Box{{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+    w.lo_x[k] = b.lo.x;
+    w.lo_y[k] = b.lo.y;
+    w.lo_z[k] = b.lo.z;
+    w.hi_x[k] = b.hi.x;
+    w.hi_y[k] = b.hi.y;
+    w.hi_z[k] = b.hi.z;
+    w.code[k] = codes[k];
+    w.pad[k] = 0;
+  }
+  return me;
 }
 
 TriRecord make_tri(const f3& v0, const f3& v1, const f3& v2) {
@@ -441,7 +498,11 @@ std::string build_host(const std::vector<std::unique_ptr<std::vector<GeometrySou
     const auto links = threaded_links(pd.tree.nodes);
     for (size_t i = 0; i < pd.tree.nodes.size(); i++)
       hb.tri_bvh_forest.push_back(to_device_node(pd.tree.nodes[i], links[i], bvh_start, pd.primitive_start));
-    hb.geom_root_code.push_back(emit_wide(pd.tree, pd.primitive_start, hb));
+    std::vector<uint32_t> code2;
+    hb.geom_root_code.push_back(emit_wide(pd.tree, pd.primitive_start, hb, code2));
+    uint32_t d4 = 0;
+    hb.geom_root_code4.push_back(pd.tree.nodes[0].left_count ? emit_wide4(pd.tree, 0, code2, hb, 0, &d4) : code2[0]);
+    hb.max_wide4_depth = std::max(hb.max_wide4_depth, d4);
     const size_t cnt = pd.tree.order.size();
     for (size_t j = 0; j < cnt; j++) {
       const uint32_t tri = hb.indices_redirect[pd.primitive_start + j];

@@ -32,7 +32,7 @@ namespace {
 
 using namespace dev;
 
-template <bool ORDERED>
+template <int MODE>
 __global__ void __launch_bounds__(128) path_kernel(TraceParams p, PathParams q, uint32_t bounce) {
   extern __shared__ uint2 smem_stack[];
   const uint32_t n = bounce == 0 ? q.count : *(volatile uint32_t*)(q.queue_count + bounce - 1);
@@ -78,7 +78,7 @@ __global__ void __launch_bounds__(128) path_kernel(TraceParams p, PathParams q, 
       R.cull_mask = 0xFFu;
       R.ray_flags = 0u;
       bool bad;
-      traverse_ray<ORDERED, false>(p, R, tlas, smem_stack + threadIdx.x, blockDim.x, bad);
+      traverse_ray<MODE, false>(p, R, tlas, smem_stack + threadIdx.x, blockDim.x, bad);
       if (!R.best.have) {
         q.out[id] = make_float2(throughput, __uint_as_float(bounce | RDN_PATH_ESCAPED));
       } else if (bounce == q.max_bounces) {
@@ -142,16 +142,24 @@ void paths_bind_scratch(PathParams& q, void* scratch) {
   q.state_b = s + off;
 }
 
-cudaError_t prepare_paths(const TraceParams& p, const PathParams& q, bool ordered, uint32_t block, int sm_count,
+namespace {
+const void* path_fn(int mode) {
+  if (mode == MODE_WIDE4) return (const void*)path_kernel<MODE_WIDE4>;
+  if (mode == MODE_BINARY) return (const void*)path_kernel<MODE_BINARY>;
+  return (const void*)path_kernel<MODE_THREADED>;
+}
+}  // namespace
+
+cudaError_t prepare_paths(const TraceParams& p, const PathParams& q, int mode, uint32_t block, int sm_count,
                           uint32_t* grid) {
   if (block == 0) block = 128;
-  const size_t smem = ordered ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
-  static bool attr_done[2] = {false, false};
-  const void* fn = ordered ? (const void*)path_kernel<true> : (const void*)path_kernel<false>;
-  if (!attr_done[ordered ? 1 : 0]) {
+  const size_t smem = mode != MODE_THREADED ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
+  static bool attr_done[3] = {false, false, false};
+  const void* fn = path_fn(mode);
+  if (!attr_done[mode]) {
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     if (e != cudaSuccess) return e;
-    attr_done[ordered ? 1 : 0] = true;
+    attr_done[mode] = true;
   }
   int per_sm = 0;
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (int)block, smem);
@@ -164,16 +172,17 @@ cudaError_t prepare_paths(const TraceParams& p, const PathParams& q, bool ordere
   return cudaSuccess;
 }
 
-cudaError_t record_paths(const TraceParams& p, const PathParams& q, bool ordered, uint32_t block, uint32_t grid,
+cudaError_t record_paths(const TraceParams& p, const PathParams& q, int mode, uint32_t block, uint32_t grid,
                          cudaStream_t stream) {
   if (block == 0) block = 128;
   if (q.count == 0 || grid == 0) return cudaSuccess;
-  const size_t smem = ordered ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
+  const size_t smem = mode != MODE_THREADED ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
   cudaError_t e = cudaMemsetAsync(q.queue_count, 0, sizeof(uint32_t) * 2 * (q.max_bounces + 1), stream);
   if (e != cudaSuccess) return e;
   for (uint32_t b = 0; b <= q.max_bounces; b++) {
-    if (ordered) path_kernel<true><<<grid, block, smem, stream>>>(p, q, b);
-    else path_kernel<false><<<grid, block, smem, stream>>>(p, q, b);
+    if (mode == MODE_WIDE4) path_kernel<MODE_WIDE4><<<grid, block, smem, stream>>>(p, q, b);
+    else if (mode == MODE_BINARY) path_kernel<MODE_BINARY><<<grid, block, smem, stream>>>(p, q, b);
+    else path_kernel<MODE_THREADED><<<grid, block, smem, stream>>>(p, q, b);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }

@@ -28,10 +28,10 @@ size_t paths_scratch_bytes(uint32_t count, uint32_t max_bounces);
 void paths_bind_scratch(PathParams& q, void* scratch);
 // Sets the kernel attributes and returns the persistent grid (not stream-ordered:
 // call before any capture).
-cudaError_t prepare_paths(const TraceParams& p, const PathParams& q, bool ordered, uint32_t block, int sm_count,
+cudaError_t prepare_paths(const TraceParams& p, const PathParams& q, int mode, uint32_t block, int sm_count,
                           uint32_t* grid);
 // Records the counter reset and one launch per bounce on `stream`.
-cudaError_t record_paths(const TraceParams& p, const PathParams& q, bool ordered, uint32_t block, uint32_t grid,
+cudaError_t record_paths(const TraceParams& p, const PathParams& q, int mode, uint32_t block, uint32_t grid,
                          cudaStream_t stream);
 
 }  // namespace rdn

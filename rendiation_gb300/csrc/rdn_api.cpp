@@ -49,6 +49,8 @@ void free_device(rdn::DeviceBuilt& d) {
   free_buf(d.tri_bvh_root);
   free_buf(d.tri_records);
   free_buf(d.wide_nodes);
+  free_buf(d.wide4_nodes);
+  free_buf(d.geom_root_code4);
   d.bytes = 0;
 }
 
@@ -108,8 +110,11 @@ rdn_status do_build(rdn_ctx* c) {
     UP(leaf_ranges, leaf_ranges)
     UP(geom_root_code, geom_root_code)
     UP(indices, indices)
+    UP(wide4_nodes, wide4_nodes)
+    UP(geom_root_code4, geom_root_code4)
 #undef UP
     d.max_blas_depth = hb->max_blas_depth;
+    d.max_wide4_depth = hb->max_wide4_depth;
     d.vertex_count = hb->vertices.size() / 3;
     d.bytes = bytes;
     c->upload_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t1).count();
@@ -119,10 +124,10 @@ rdn_status do_build(rdn_ctx* c) {
   return RDN_OK;
 }
 
-uint32_t stack_depth_for(uint32_t max_depth) {
-  uint32_t d = max_depth + 1;
-  d = (d + 3) & ~3u;
-  return d < 8 ? 8 : d;
+int mode_of(uint32_t traversal) {
+  if (traversal == RDN_TRAVERSAL_REFERENCE) return rdn::MODE_THREADED;
+  if (traversal == RDN_TRAVERSAL_ORDERED_BINARY) return rdn::MODE_BINARY;
+  return rdn::MODE_WIDE4;
 }
 
 rdn_status fill_params(rdn_ctx* c, const rdn_trace_desc* desc, rdn::TraceParams& p) {
@@ -137,7 +142,7 @@ rdn_status fill_params(rdn_ctx* c, const rdn_trace_desc* desc, rdn::TraceParams&
   p.ray_flags = desc->ray_flags;
   p.cull_mask = desc->cull_mask;
   p.anyhit_mode = desc->anyhit_mode;
-  p.stack_depth = stack_depth_for(d.max_blas_depth);
+  p.stack_depth = rdn::stack_entries(mode_of(desc->traversal), d.max_blas_depth, d.max_wide4_depth);
   p.n_binding = (uint32_t)d.tlas_binding.count;
   p.n_tlas_root = (uint32_t)d.tlas_bvh_root.count;
   p.tlas_binding = d.tlas_binding.ptr;
@@ -153,6 +158,8 @@ rdn_status fill_params(rdn_ctx* c, const rdn_trace_desc* desc, rdn::TraceParams&
   p.wide = reinterpret_cast<const float4*>(d.wide_nodes.ptr);
   p.leaves = reinterpret_cast<const uint2*>(d.leaf_ranges.ptr);
   p.geom_root_code = d.geom_root_code.ptr;
+  p.wide4 = reinterpret_cast<const float4*>(d.wide4_nodes.ptr);
+  p.geom_root_code4 = d.geom_root_code4.ptr;
   p.counters = reinterpret_cast<unsigned long long*>(c->d_counters);
   p.error_word = c->d_counters + 8;
   return RDN_OK;
@@ -165,7 +172,7 @@ rdn_status validate_trace(rdn_ctx* c, const rdn_trace_desc* desc) {
   if ((reinterpret_cast<uintptr_t>(desc->rays) & 15) || (reinterpret_cast<uintptr_t>(desc->hits) & 15) ||
       (reinterpret_cast<uintptr_t>(desc->hits_ext) & 15))
     return fail(c, RDN_ERR_INVALID_ARG, "ray and hit buffers must be 16-byte aligned");
-  if (desc->traversal > RDN_TRAVERSAL_REFERENCE) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
+  if (desc->traversal > RDN_TRAVERSAL_ORDERED_BINARY) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
   if (desc->anyhit_mode > RDN_ANYHIT_ACCEPT_EVEN_PRIMS) return fail(c, RDN_ERR_INVALID_ARG, "unknown any-hit mode");
   if (desc->block_size && (desc->block_size % 32 || desc->block_size > 256))
     return fail(c, RDN_ERR_INVALID_ARG, "block_size must be a multiple of 32 up to 256");
@@ -383,8 +390,7 @@ rdn_status rdn_trace(rdn_ctx* c, const rdn_trace_desc* desc, void* stream) {
   fill_params(c, desc, p);
   cudaError_t e = cudaSetDevice(c->device);
   if (e == cudaSuccess)
-    e = rdn::launch_trace(p, desc->traversal == RDN_TRAVERSAL_ORDERED, false, desc->block_size,
-                          static_cast<cudaStream_t>(stream));
+    e = rdn::launch_trace(p, mode_of(desc->traversal), false, desc->block_size, static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(c, e, "trace launch");
   return RDN_OK;
 }
@@ -401,7 +407,7 @@ rdn_status rdn_trace_counted(rdn_ctx* c, const rdn_trace_desc* desc, void* strea
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   cudaError_t e = cudaSetDevice(c->device);
   if (e == cudaSuccess) e = cudaMemsetAsync(c->d_counters, 0, 64, s);
-  if (e == cudaSuccess) e = rdn::launch_trace(p, desc->traversal == RDN_TRAVERSAL_ORDERED, true, desc->block_size, s);
+  if (e == cudaSuccess) e = rdn::launch_trace(p, mode_of(desc->traversal), true, desc->block_size, s);
   uint64_t h[8];
   if (e == cudaSuccess) e = cudaMemcpyAsync(h, c->d_counters, 64, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
@@ -428,7 +434,7 @@ rdn_status rdn_wavefront_shadow_bounce(rdn_ctx* c, const rdn_wavefront_desc* d, 
   if (d->scratch_bytes < rdn::wavefront_scratch_bytes(W, H)) return fail(c, RDN_ERR_INVALID_ARG, "scratch too small");
   if ((reinterpret_cast<uintptr_t>(d->scratch) & 255) || (reinterpret_cast<uintptr_t>(d->out) & 15))
     return fail(c, RDN_ERR_INVALID_ARG, "scratch must be 256-byte and output 16-byte aligned");
-  if (d->traversal > RDN_TRAVERSAL_REFERENCE) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
+  if (d->traversal > RDN_TRAVERSAL_ORDERED_BINARY) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
   if (d->phases > 3) return fail(c, RDN_ERR_INVALID_ARG, "unknown phase mask");
   if (d->block_size && (d->block_size % 32 || d->block_size > 128))
     return fail(c, RDN_ERR_INVALID_ARG, "block_size must be a multiple of 32 up to 128");
@@ -439,6 +445,7 @@ rdn_status rdn_wavefront_shadow_bounce(rdn_ctx* c, const rdn_wavefront_desc* d, 
   std::memset(&td, 0, sizeof(td));
   td.tlas_uniform = d->tlas_uniform;
   td.cull_mask = 0xFF;
+  td.traversal = d->traversal;
   rdn::TraceParams p;
   fill_params(c, &td, p);
   rdn::WavefrontParams w;
@@ -460,8 +467,8 @@ rdn_status rdn_wavefront_shadow_bounce(rdn_ctx* c, const rdn_wavefront_desc* d, 
   rdn::wavefront_bind_scratch(w, d->scratch);
   cudaError_t e = cudaSetDevice(c->device);
   if (e == cudaSuccess)
-    e = rdn::launch_wavefront(p, w, d->traversal == RDN_TRAVERSAL_ORDERED, d->block_size, c->sm_count,
-                              d->phases, static_cast<cudaStream_t>(stream));
+    e = rdn::launch_wavefront(p, w, mode_of(d->traversal), d->block_size, c->sm_count, d->phases,
+                              static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(c, e, "wavefront launch");
   return RDN_OK;
 }
@@ -487,7 +494,7 @@ rdn_status prepare_path_launch(rdn_ctx* c, const rdn_path_desc* d, rdn::TracePar
   if ((reinterpret_cast<uintptr_t>(d->scratch) & 255) || (reinterpret_cast<uintptr_t>(d->rays) & 15) ||
       (reinterpret_cast<uintptr_t>(d->out) & 7))
     return fail(c, RDN_ERR_INVALID_ARG, "misaligned buffer");
-  if (d->traversal > RDN_TRAVERSAL_REFERENCE) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
+  if (d->traversal > RDN_TRAVERSAL_ORDERED_BINARY) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
   if (d->block_size && (d->block_size % 32 || d->block_size > 128))
     return fail(c, RDN_ERR_INVALID_ARG, "block_size must be a multiple of 32 up to 128");
   if (!(d->rr_survive > 0.0f && d->rr_survive <= 1.0f)) return fail(c, RDN_ERR_INVALID_ARG, "rr_survive not in (0, 1]");
@@ -497,6 +504,7 @@ rdn_status prepare_path_launch(rdn_ctx* c, const rdn_path_desc* d, rdn::TracePar
   std::memset(&td, 0, sizeof(td));
   td.tlas_uniform = d->tlas_uniform;
   td.cull_mask = 0xFF;
+  td.traversal = d->traversal;
   fill_params(c, &td, p);
   std::memset(&q, 0, sizeof(q));
   q.primary_rays = reinterpret_cast<const float4*>(d->rays);
@@ -513,7 +521,7 @@ rdn_status prepare_path_launch(rdn_ctx* c, const rdn_path_desc* d, rdn::TracePar
   if (d->count) rdn::paths_bind_scratch(q, d->scratch);
   cudaError_t e = cudaSetDevice(c->device);
   if (e == cudaSuccess && d->count)
-    e = rdn::prepare_paths(p, q, d->traversal == RDN_TRAVERSAL_ORDERED, d->block_size, c->sm_count, grid);
+    e = rdn::prepare_paths(p, q, mode_of(d->traversal), d->block_size, c->sm_count, grid);
   if (e != cudaSuccess) return cuda_fail(c, e, "path launch preparation");
   return RDN_OK;
 }
@@ -536,7 +544,7 @@ rdn_status rdn_trace_paths(rdn_ctx* c, const rdn_path_desc* d, void* stream) {
   uint32_t grid = 0;
   rdn_status st = prepare_path_launch(c, d, p, q, &grid);
   if (st != RDN_OK || d->count == 0) return st;
-  cudaError_t e = rdn::record_paths(p, q, d->traversal == RDN_TRAVERSAL_ORDERED, d->block_size, grid,
+  cudaError_t e = rdn::record_paths(p, q, mode_of(d->traversal), d->block_size, grid,
                                     static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(c, e, "path launch");
   return RDN_OK;
@@ -562,8 +570,7 @@ rdn_status rdn_trace_paths_graph(rdn_ctx* c, const rdn_path_desc* d, rdn_graph**
   g->device = c->device;
   e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
-    cudaError_t rec = d->count ? rdn::record_paths(p, q, d->traversal == RDN_TRAVERSAL_ORDERED, d->block_size, grid, s)
-                               : cudaSuccess;
+    cudaError_t rec = d->count ? rdn::record_paths(p, q, mode_of(d->traversal), d->block_size, grid, s) : cudaSuccess;
     e = cudaStreamEndCapture(s, &g->graph);
     if (rec != cudaSuccess) e = rec;
   }
@@ -606,7 +613,7 @@ rdn_status prepare_attr(rdn_ctx* c, const rdn_attr_loss_desc* d, bool adjoint, r
   if (adjoint && d->count && !d->grad_vertices) return fail(c, RDN_ERR_INVALID_ARG, "null gradient buffer");
   if ((reinterpret_cast<uintptr_t>(d->rays) & 15) || (reinterpret_cast<uintptr_t>(d->grad_vertices) & 15))
     return fail(c, RDN_ERR_INVALID_ARG, "rays and gradients must be 16-byte aligned");
-  if (d->traversal > RDN_TRAVERSAL_REFERENCE) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
+  if (d->traversal > RDN_TRAVERSAL_ORDERED_BINARY) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
   if (d->block_size && (d->block_size % 32 || d->block_size > 128))
     return fail(c, RDN_ERR_INVALID_ARG, "block_size must be a multiple of 32 up to 128");
   rdn_status st = ensure_built(c);
@@ -615,6 +622,7 @@ rdn_status prepare_attr(rdn_ctx* c, const rdn_attr_loss_desc* d, bool adjoint, r
   std::memset(&td, 0, sizeof(td));
   td.tlas_uniform = d->tlas_uniform;
   td.cull_mask = 0xFF;
+  td.traversal = d->traversal;
   fill_params(c, &td, p);
   std::memset(&a, 0, sizeof(a));
   a.rays = reinterpret_cast<const float4*>(d->rays);
@@ -646,8 +654,7 @@ rdn_status rdn_attr_loss_forward(rdn_ctx* c, const rdn_attr_loss_desc* d, void* 
   if (st != RDN_OK) return st;
   cudaError_t e = cudaSetDevice(c->device);
   if (e == cudaSuccess)
-    e = rdn::launch_attr_forward(p, a, d->traversal == RDN_TRAVERSAL_ORDERED, d->block_size,
-                                 static_cast<cudaStream_t>(stream));
+    e = rdn::launch_attr_forward(p, a, mode_of(d->traversal), d->block_size, static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(c, e, "attribute loss forward");
   return RDN_OK;
 }
@@ -661,8 +668,7 @@ rdn_status rdn_attr_loss_adjoint(rdn_ctx* c, const rdn_attr_loss_desc* d, void* 
   if (st != RDN_OK) return st;
   cudaError_t e = cudaSetDevice(c->device);
   if (e == cudaSuccess)
-    e = rdn::launch_attr_adjoint(p, a, d->traversal == RDN_TRAVERSAL_ORDERED, d->block_size,
-                                 static_cast<cudaStream_t>(stream));
+    e = rdn::launch_attr_adjoint(p, a, mode_of(d->traversal), d->block_size, static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(c, e, "attribute loss adjoint");
   return RDN_OK;
 }
@@ -684,7 +690,7 @@ rdn_status rdn_wavefront_shadow_bounce_static(rdn_ctx* c, const rdn_wavefront_de
                     std::to_string(RDN_WAVEFRONT_STATIC_SCRATCH_BYTES) + " (about 466,000 pixels)");
   if (W && H && !d->out) return fail(c, RDN_ERR_INVALID_ARG, "null output");
   if (reinterpret_cast<uintptr_t>(d->out) & 15) return fail(c, RDN_ERR_INVALID_ARG, "output must be 16-byte aligned");
-  if (d->traversal > RDN_TRAVERSAL_REFERENCE) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
+  if (d->traversal > RDN_TRAVERSAL_ORDERED_BINARY) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
   if (d->phases > 3) return fail(c, RDN_ERR_INVALID_ARG, "unknown phase mask");
   if (d->block_size && (d->block_size % 32 || d->block_size > 128))
     return fail(c, RDN_ERR_INVALID_ARG, "block_size must be a multiple of 32 up to 128");
@@ -695,6 +701,7 @@ rdn_status rdn_wavefront_shadow_bounce_static(rdn_ctx* c, const rdn_wavefront_de
   std::memset(&td, 0, sizeof(td));
   td.tlas_uniform = d->tlas_uniform;
   td.cull_mask = 0xFF;
+  td.traversal = d->traversal;
   rdn::TraceParams p;
   fill_params(c, &td, p);
   rdn::WavefrontParams w;
@@ -715,8 +722,8 @@ rdn_status rdn_wavefront_shadow_bounce_static(rdn_ctx* c, const rdn_wavefront_de
   w.ray_counts = d->ray_counts;
   cudaError_t e = cudaSetDevice(c->device);
   if (e == cudaSuccess)
-    e = rdn::launch_wavefront_static(p, w, d->traversal == RDN_TRAVERSAL_ORDERED, d->block_size, c->sm_count,
-                                     d->phases, c->device, static_cast<cudaStream_t>(stream));
+    e = rdn::launch_wavefront_static(p, w, mode_of(d->traversal), d->block_size, c->sm_count, d->phases,
+                                     c->device, static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(c, e, "static wavefront launch");
   return RDN_OK;
 }

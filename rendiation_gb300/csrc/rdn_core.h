@@ -77,6 +77,19 @@ struct WideNode {
 };
 static_assert(sizeof(WideNode) == 64, "64 B node");
 static const uint32_t LEAF_BIT = 0x80000000u;
+// Four-child node, 128 B, children's boxes as SoA rows:
+//   lo_x[4] lo_y[4] lo_z[4] hi_x[4] hi_y[4] hi_z[4] code[4] pad[4]
+// code: bit 31 clear = index of a child Wide4Node, set = index of a leaf range,
+// EMPTY_SLOT = unused slot. Children are binary-tree nodes collapsed from the
+// reference's SAH tree (the inner child with the largest surface area is opened
+// until four slots are used); every child box is an exact reference node box.
+struct Wide4Node {
+  float lo_x[4], lo_y[4], lo_z[4], hi_x[4], hi_y[4], hi_z[4];
+  uint32_t code[4];
+  uint32_t pad[4];
+};
+static_assert(sizeof(Wide4Node) == 128, "128 B node");
+static const uint32_t EMPTY_SLOT = 0xFFFFFFFFu;
 
 struct GeometrySource {
   uint32_t type;
@@ -109,7 +122,10 @@ struct HostBuilt {
   std::vector<WideNode> wide_nodes;
   std::vector<uint32_t> leaf_ranges;  // 2 per leaf: [start, end)
   std::vector<uint32_t> geom_root_code;  // per tri_bvh_root entry
+  std::vector<Wide4Node> wide4_nodes;
+  std::vector<uint32_t> geom_root_code4;  // per tri_bvh_root entry
   uint32_t max_blas_depth = 0;
+  uint32_t max_wide4_depth = 0;
   uint64_t sah_splits = 0, median_fallbacks = 0;
 };
 
@@ -128,7 +144,10 @@ struct DeviceBuilt {
   DevBuf<GeometryMetaInfo> tri_bvh_root;
   DevBuf<TriRecord> tri_records;
   DevBuf<WideNode> wide_nodes;
+  DevBuf<Wide4Node> wide4_nodes;
+  DevBuf<uint32_t> geom_root_code4;
   uint32_t max_blas_depth = 0;
+  uint32_t max_wide4_depth = 0;
   uint64_t vertex_count = 0;
   uint64_t bytes = 0;
 };

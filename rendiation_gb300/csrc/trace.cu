@@ -12,7 +12,7 @@ namespace {
 
 using namespace dev;
 
-template <bool ORDERED, bool COUNT>
+template <int MODE, bool COUNT>
 __global__ void __launch_bounds__(256) trace_kernel(TraceParams p) {
   extern __shared__ uint2 smem_stack[];
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -28,7 +28,7 @@ __global__ void __launch_bounds__(256) trace_kernel(TraceParams p) {
   R.ray_flags = p.ray_flags;
   const uint32_t tidx = p.tlas_idx ? __ldg(p.tlas_idx + i) : p.tlas_uniform;
   bool bad;
-  traverse_ray<ORDERED, COUNT>(p, R, tidx, smem_stack + threadIdx.x, blockDim.x, bad);
+  traverse_ray<MODE, COUNT>(p, R, tidx, smem_stack + threadIdx.x, blockDim.x, bad);
 
   float4 out;
   uint4 ext;
@@ -64,27 +64,34 @@ __global__ void __launch_bounds__(256) trace_kernel(TraceParams p) {
 
 }  // namespace
 
-cudaError_t launch_trace(const TraceParams& p, bool ordered, bool counted, uint32_t block, cudaStream_t stream) {
+uint32_t stack_entries(int mode, uint32_t max_binary_depth, uint32_t max_wide4_depth) {
+  uint32_t d = mode == MODE_WIDE4 ? 3 * max_wide4_depth + 1 : (mode == MODE_BINARY ? max_binary_depth + 1 : 0);
+  d = (d + 3) & ~3u;
+  return d < 8 ? 8 : d;
+}
+
+cudaError_t launch_trace(const TraceParams& p, int mode, bool counted, uint32_t block, cudaStream_t stream) {
   if (p.count == 0) return cudaSuccess;
   if (block == 0) block = 128;
   const uint32_t grid = (p.count + block - 1) / block;
-  const size_t smem = ordered ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
-  static bool attr_done[4] = {false, false, false, false};
-  const void* fn;
-  if (ordered) fn = counted ? (const void*)trace_kernel<true, true> : (const void*)trace_kernel<true, false>;
-  else fn = counted ? (const void*)trace_kernel<false, true> : (const void*)trace_kernel<false, false>;
-  const int slot = (ordered ? 2 : 0) + (counted ? 1 : 0);
+  const size_t smem = mode != MODE_THREADED ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
+  static bool attr_done[6] = {false, false, false, false, false, false};
+  const void* fns[6] = {(const void*)trace_kernel<0, false>, (const void*)trace_kernel<0, true>,
+                        (const void*)trace_kernel<1, false>, (const void*)trace_kernel<1, true>,
+                        (const void*)trace_kernel<2, false>, (const void*)trace_kernel<2, true>};
+  const int slot = 2 * mode + (counted ? 1 : 0);
   if (!attr_done[slot]) {
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaError_t e = cudaFuncSetAttribute(fns[slot], cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     if (e != cudaSuccess) return e;
     attr_done[slot] = true;
   }
-  if (ordered) {
-    if (counted) trace_kernel<true, true><<<grid, block, smem, stream>>>(p);
-    else trace_kernel<true, false><<<grid, block, smem, stream>>>(p);
-  } else {
-    if (counted) trace_kernel<false, true><<<grid, block, smem, stream>>>(p);
-    else trace_kernel<false, false><<<grid, block, smem, stream>>>(p);
+  switch (slot) {
+    case 0: trace_kernel<0, false><<<grid, block, smem, stream>>>(p); break;
+    case 1: trace_kernel<0, true><<<grid, block, smem, stream>>>(p); break;
+    case 2: trace_kernel<1, false><<<grid, block, smem, stream>>>(p); break;
+    case 3: trace_kernel<1, true><<<grid, block, smem, stream>>>(p); break;
+    case 4: trace_kernel<2, false><<<grid, block, smem, stream>>>(p); break;
+    default: trace_kernel<2, true><<<grid, block, smem, stream>>>(p); break;
   }
   return cudaGetLastError();
 }

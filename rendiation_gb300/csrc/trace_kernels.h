@@ -28,10 +28,18 @@ struct TraceParams {
   const float4* wide;   // 4 per node (WideNode)
   const uint2* leaves;
   const uint32_t* geom_root_code;
+  const float4* wide4;  // 8 per node (Wide4Node)
+  const uint32_t* geom_root_code4;
   unsigned long long* counters;  // 4 x u64, used by counted launches
   uint32_t* error_word;          // bit 0 stack overflow, bit 1 bad tlas index
 };
 
-cudaError_t launch_trace(const TraceParams& p, bool ordered, bool counted, uint32_t block, cudaStream_t stream);
+// Traversal modes (template argument of every traversal kernel).
+enum TraversalMode : int { MODE_THREADED = 0, MODE_BINARY = 1, MODE_WIDE4 = 2 };
+
+// stack entries the mode needs per thread
+uint32_t stack_entries(int mode, uint32_t max_binary_depth, uint32_t max_wide4_depth);
+
+cudaError_t launch_trace(const TraceParams& p, int mode, bool counted, uint32_t block, cudaStream_t stream);
 
 }  // namespace rdn

@@ -293,9 +293,111 @@ __device__ __forceinline__ bool blas_ordered(const TraceParams& p, RayCtx& R, co
   }
 }
 
+__device__ __forceinline__ void cswap(float& ta, uint32_t& ca, float& tb, uint32_t& cb) {
+  if (tb < ta) {
+    const float t = ta;
+    ta = tb;
+    tb = t;
+    const uint32_t c = ca;
+    ca = cb;
+    cb = c;
+  }
+}
+
+// BLAS of one geometry over 128 B four-child nodes, nearest child first. Each
+// child box is tested with the reference's slab test; the remaining hit
+// children are pushed farthest first and re-checked against the current far
+// (t_near_max < t_max) when popped.
+template <bool COUNT>
+__device__ __forceinline__ bool blas_wide4(const TraceParams& p, RayCtx& R, const InstanceRay& ir, uint32_t root_node,
+                                           uint32_t gslot, uint32_t inst_slot, bool is_opaque, bool cull_enable,
+                                           bool cull_back, uint32_t prim_start, uint2* stack, uint32_t stride,
+                                           uint32_t depth) {
+  {
+    if (COUNT) R.node_visits++;
+    const float4* nd = reinterpret_cast<const float4*>(p.tri_forest + root_node);
+    const float4 a = __ldg(nd), b = __ldg(nd + 1);
+    float tn;
+    if (!slab(ir.o, ir.inv_d, R.tmin * ir.scaling, R.far_world * ir.scaling, a.x, a.y, a.z, b.x, b.y, b.z, tn))
+      return false;
+  }
+  uint32_t code = __ldg(p.geom_root_code4 + gslot);
+  uint32_t sp = 0;
+  for (;;) {
+    bool have_node = true;
+    while (!(code & LEAF_BIT)) {
+      const float4* w = p.wide4 + 8 * (size_t)code;
+      const float4 lx = __ldg(w), ly = __ldg(w + 1), lz = __ldg(w + 2);
+      const float4 hx = __ldg(w + 3), hy = __ldg(w + 4), hz = __ldg(w + 5);
+      const uint4 cc = __ldg(reinterpret_cast<const uint4*>(w + 6));
+      const float near_ = R.tmin * ir.scaling, far_ = R.far_world * ir.scaling;
+      const float inf = __int_as_float(0x7f800000);
+      float t0 = inf, t1 = inf, t2 = inf, t3 = inf;
+      uint32_t c0 = EMPTY_SLOT, c1 = EMPTY_SLOT, c2 = EMPTY_SLOT, c3 = EMPTY_SLOT;
+      float tn;
+      if (cc.x != EMPTY_SLOT && slab(ir.o, ir.inv_d, near_, far_, lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, tn)) {
+        t0 = tn;
+        c0 = cc.x;
+      }
+      if (cc.y != EMPTY_SLOT && slab(ir.o, ir.inv_d, near_, far_, lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, tn)) {
+        t1 = tn;
+        c1 = cc.y;
+      }
+      if (cc.z != EMPTY_SLOT && slab(ir.o, ir.inv_d, near_, far_, lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, tn)) {
+        t2 = tn;
+        c2 = cc.z;
+      }
+      if (cc.w != EMPTY_SLOT && slab(ir.o, ir.inv_d, near_, far_, lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, tn)) {
+        t3 = tn;
+        c3 = cc.w;
+      }
+      if (COUNT) R.node_visits += (cc.x != EMPTY_SLOT) + (cc.y != EMPTY_SLOT) + (cc.z != EMPTY_SLOT) + (cc.w != EMPTY_SLOT);
+      // sort the four (t_near, code) pairs ascending; misses carry (+inf, EMPTY)
+      cswap(t0, c0, t1, c1);
+      cswap(t2, c2, t3, c3);
+      cswap(t0, c0, t2, c2);
+      cswap(t1, c1, t3, c3);
+      cswap(t1, c1, t2, c2);
+      if (c0 == EMPTY_SLOT) {
+        have_node = false;
+        break;
+      }
+      // push the farther hits, farthest first
+      if (c3 != EMPTY_SLOT) {
+        if (sp < depth) stack[(sp++) * stride] = make_uint2(c3, __float_as_uint(t3));
+        else atomicOr(p.error_word, 1u);
+      }
+      if (c2 != EMPTY_SLOT) {
+        if (sp < depth) stack[(sp++) * stride] = make_uint2(c2, __float_as_uint(t2));
+        else atomicOr(p.error_word, 1u);
+      }
+      if (c1 != EMPTY_SLOT) {
+        if (sp < depth) stack[(sp++) * stride] = make_uint2(c1, __float_as_uint(t1));
+        else atomicOr(p.error_word, 1u);
+      }
+      code = c0;
+    }
+    if (have_node) {
+      const uint2 lr = __ldg(p.leaves + (code & ~LEAF_BIT));
+      if (leaf_triangles<COUNT>(p, R, ir, lr.x, lr.y, gslot, inst_slot, is_opaque, cull_enable, cull_back,
+                                prim_start))
+        return true;
+    }
+    for (;;) {
+      if (sp == 0) return false;
+      sp--;
+      const uint2 e = stack[sp * stride];
+      if (__uint_as_float(e.y) < R.far_world * ir.scaling) {
+        code = e.x;
+        break;
+      }
+    }
+  }
+}
+
 // Full query of one ray (traverse_cpu.rs:52-245). R must hold the ray; on
 // return R.best holds the committed hit. `bad` reports an unbound TLAS index.
-template <bool ORDERED, bool COUNT>
+template <int MODE, bool COUNT>
 __device__ __forceinline__ void traverse_ray(const TraceParams& p, RayCtx& R, uint32_t tidx, uint2* stack,
                                              uint32_t stride, bool& bad) {
   R.inv_d = make_float3(1.0f / R.d.x, 1.0f / R.d.y, 1.0f / R.d.z);
@@ -343,7 +445,10 @@ __device__ __forceinline__ void traverse_ray(const TraceParams& p, RayCtx& R, ui
         geometry_cull(ir.flags, gm.w, pass, is_opaque, cull_enable, cull_back);
         if (!pass) continue;
         bool end;
-        if (ORDERED)
+        if (MODE == MODE_WIDE4)
+          end = blas_wide4<COUNT>(p, R, ir, gm.x, g, ti, is_opaque, cull_enable, cull_back, gm.z, stack, stride,
+                                  p.stack_depth);
+        else if (MODE == MODE_BINARY)
           end = blas_ordered<COUNT>(p, R, ir, gm.x, g, ti, is_opaque, cull_enable, cull_back, gm.z, stack, stride,
                                     p.stack_depth);
         else

@@ -36,7 +36,7 @@ namespace {
 
 using namespace dev;
 
-template <bool ORDERED>
+template <int MODE>
 __global__ void __launch_bounds__(128) primary_kernel(TraceParams p, WavefrontParams w) {
   extern __shared__ uint2 smem_stack[];
   const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -64,7 +64,7 @@ __global__ void __launch_bounds__(128) primary_kernel(TraceParams p, WavefrontPa
     R.cull_mask = 0xFFu;
     R.ray_flags = 0u;
     bool bad;
-    traverse_ray<ORDERED, false>(p, R, w.tlas, smem_stack + threadIdx.x, blockDim.x, bad);
+    traverse_ray<MODE, false>(p, R, w.tlas, smem_stack + threadIdx.x, blockDim.x, bad);
     PixelResult out;
     out.primary_prim = INVALID_NEXT;
     out.primary_t = R.tmax;
@@ -112,7 +112,7 @@ __global__ void __launch_bounds__(128) primary_kernel(TraceParams p, WavefrontPa
   }
 }
 
-template <bool ORDERED>
+template <int MODE>
 __global__ void __launch_bounds__(128) secondary_kernel(TraceParams p, WavefrontParams w) {
   extern __shared__ uint2 smem_stack[];
   const uint32_t n = *(volatile uint32_t*)w.queue_count;
@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(128) secondary_kernel(TraceParams p, Wavefront
       R.cull_mask = 0xFFu;
       R.ray_flags = shadow ? TF_END_SEARCH : 0u;
       bool bad;
-      traverse_ray<ORDERED, false>(p, R, w.tlas, smem_stack + threadIdx.x, blockDim.x, bad);
+      traverse_ray<MODE, false>(p, R, w.tlas, smem_stack + threadIdx.x, blockDim.x, bad);
       if (shadow) {
         PixelResult* o = w.out + w.shadow_pixel[q];
         o->light = R.best.have ? 2u : 1u;
@@ -183,23 +183,18 @@ void wavefront_bind_scratch(WavefrontParams& w, void* scratch) {
   w.bounce_pixel = reinterpret_cast<uint32_t*>(s + off);
 }
 
-cudaError_t launch_wavefront(const TraceParams& p, const WavefrontParams& w, bool ordered, uint32_t block,
-                             int sm_count, uint32_t phases, cudaStream_t stream) {
-  if (phases == 0) phases = 3;
-  if (block == 0) block = 128;
-  const size_t n = (size_t)w.width * w.height;
-  if (n == 0) return cudaSuccess;
-  const size_t smem = ordered ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
-  static bool attr_done[2] = {false, false};
-  const void* fns[4] = {(const void*)primary_kernel<false>, (const void*)secondary_kernel<false>,
-                        (const void*)primary_kernel<true>, (const void*)secondary_kernel<true>};
-  if (!attr_done[ordered ? 1 : 0]) {
-    for (int k = 0; k < 2; k++) {
-      cudaError_t e = cudaFuncSetAttribute(fns[(ordered ? 2 : 0) + k], cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           200 * 1024);
-      if (e != cudaSuccess) return e;
-    }
-    attr_done[ordered ? 1 : 0] = true;
+namespace {
+template <int MODE>
+cudaError_t launch_wavefront_mode(const TraceParams& p, const WavefrontParams& w, uint32_t block, int sm_count,
+                                  uint32_t phases, cudaStream_t stream) {
+  const size_t smem = MODE != MODE_THREADED ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
+  static bool attr_done = false;
+  if (!attr_done) {
+    cudaError_t e = cudaFuncSetAttribute(primary_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(secondary_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e != cudaSuccess) return e;
+    attr_done = true;
   }
   cudaError_t e;
   if (phases & 1u) {
@@ -209,8 +204,7 @@ cudaError_t launch_wavefront(const TraceParams& p, const WavefrontParams& w, boo
     const uint32_t tiles = ((w.width + 7) / 8) * ((w.height + 3) / 4);
     const uint32_t threads = tiles * 32;
     const uint32_t grid1 = (threads + block - 1) / block;
-    if (ordered) primary_kernel<true><<<grid1, block, smem, stream>>>(p, w);
-    else primary_kernel<false><<<grid1, block, smem, stream>>>(p, w);
+    primary_kernel<MODE><<<grid1, block, smem, stream>>>(p, w);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
@@ -219,13 +213,24 @@ cudaError_t launch_wavefront(const TraceParams& p, const WavefrontParams& w, boo
   if (e != cudaSuccess) return e;
   // persistent secondary grid: enough resident blocks to fill every SM
   int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fns[(ordered ? 2 : 0) + 1], (int)block, smem);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, secondary_kernel<MODE>, (int)block, smem);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
   const uint32_t grid2 = (uint32_t)(sm_count * per_sm);
-  if (ordered) secondary_kernel<true><<<grid2, block, smem, stream>>>(p, w);
-  else secondary_kernel<false><<<grid2, block, smem, stream>>>(p, w);
+  secondary_kernel<MODE><<<grid2, block, smem, stream>>>(p, w);
   return cudaGetLastError();
+}
+}  // namespace
+
+cudaError_t launch_wavefront(const TraceParams& p, const WavefrontParams& w, int mode, uint32_t block,
+                             int sm_count, uint32_t phases, cudaStream_t stream) {
+  if (phases == 0) phases = 3;
+  if (block == 0) block = 128;
+  const size_t n = (size_t)w.width * w.height;
+  if (n == 0) return cudaSuccess;
+  if (mode == MODE_WIDE4) return launch_wavefront_mode<MODE_WIDE4>(p, w, block, sm_count, phases, stream);
+  if (mode == MODE_BINARY) return launch_wavefront_mode<MODE_BINARY>(p, w, block, sm_count, phases, stream);
+  return launch_wavefront_mode<MODE_THREADED>(p, w, block, sm_count, phases, stream);
 }
 
 }  // namespace rdn

@@ -39,12 +39,12 @@ struct WavefrontParams {
 size_t wavefront_scratch_bytes(uint32_t width, uint32_t height);
 void wavefront_bind_scratch(WavefrontParams& w, void* scratch);
 // phases: bit 0 primary kernel, bit 1 secondary kernel (0 = both).
-cudaError_t launch_wavefront(const TraceParams& p, const WavefrontParams& w, bool ordered, uint32_t block,
+cudaError_t launch_wavefront(const TraceParams& p, const WavefrontParams& w, int mode, uint32_t block,
                              int sm_count, uint32_t phases, cudaStream_t stream);
 
 // Same launch with the queues in the library's static device array
 // (wavefront_static.cu); `device` must be current.
-cudaError_t launch_wavefront_static(const TraceParams& p, WavefrontParams w, bool ordered, uint32_t block,
+cudaError_t launch_wavefront_static(const TraceParams& p, WavefrontParams w, int mode, uint32_t block,
                                     int sm_count, uint32_t phases, int device, cudaStream_t stream);
 
 }  // namespace rdn

@@ -56,13 +56,13 @@ cudaError_t static_scratch_address(int device, void** out) {
 
 }  // namespace
 
-cudaError_t launch_wavefront_static(const TraceParams& p, WavefrontParams w, bool ordered, uint32_t block,
+cudaError_t launch_wavefront_static(const TraceParams& p, WavefrontParams w, int mode, uint32_t block,
                                     int sm_count, uint32_t phases, int device, cudaStream_t stream) {
   void* scratch = nullptr;
   cudaError_t e = static_scratch_address(device, &scratch);
   if (e != cudaSuccess) return e;
   wavefront_bind_scratch(w, scratch);
-  return launch_wavefront(p, w, ordered, block, sm_count, phases, stream);
+  return launch_wavefront(p, w, mode, block, sm_count, phases, stream);
 }
 
 }  // namespace rdn

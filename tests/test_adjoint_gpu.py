@@ -133,30 +133,53 @@ def test_gradients_vs_fp64(field, cuda):
     for k, wk in enumerate([1 - u - v, u, v]):
         np.add.at(ga, tv[:, k], r * wk)
         np.add.at(gp, tv[:, k], -wk[:, None] * lam)
-    scale_a = np.max(np.abs(ga))
-    scale_p = np.max(np.linalg.norm(gp, axis=1))
-    assert np.max(np.abs(g_attr - ga)) < 1e-4 * scale_a
-    assert np.max(np.linalg.norm(g_pos - gp, axis=1)) < 1e-3 * scale_p
+    # per vertex, against the FP64 analytic gradient
+    norm_p = np.linalg.norm(gp, axis=1)
+    floor_p = 1e-2 * np.median(norm_p[norm_p > 0])
+    floor_a = 1e-2 * np.median(np.abs(ga[ga != 0]))
+    rel_p = np.linalg.norm(g_pos - gp, axis=1) / np.maximum(norm_p, floor_p)
+    rel_a = np.abs(g_attr - ga) / np.maximum(np.abs(ga), floor_a)
+    assert rel_p.max() < 1e-3, rel_p.max()
+    assert rel_a.max() < 1e-3, rel_a.max()
 
-    # FP64 central differences (h = 1e-4) on 64 random vertices that some ray sees
+    # FP64 central differences on 64 random vertices that some ray sees, with
+    # h = 1e-4 and h/2 combined by Richardson extrapolation (error O(h^4)); the
+    # difference between the extrapolations at h and h/2 bounds the FD error
+    # itself (grazing rays make the barycentrics strongly nonlinear at h = 1e-4)
     seen = np.unique(tv.reshape(-1))
     pick = rng.choice(seen, size=min(64, seen.size), replace=False)
-    h = 1e-4
     pos64 = mesh.positions.astype(np.float64)
-    worst = 0.0
-    for vi in pick:
-        fd = np.zeros(4)
-        for c in range(3):
+
+    def sub_loss(pos, attrs, sel):
+        return fp64_loss(pos, mesh.indices, attrs, rh[sel], tri[sel], tg[sel])
+
+    def central(vi, c, hh, sel):
+        if c < 3:
             pp, pm = pos64.copy(), pos64.copy()
-            pp[vi, c] += h
-            pm[vi, c] -= h
-            fd[c] = (fp64_loss(pp, mesh.indices, a, rh, tri, tg) - fp64_loss(pm, mesh.indices, a, rh, tri, tg)) / (2 * h)
+            pp[vi, c] += hh
+            pm[vi, c] -= hh
+            return (sub_loss(pp, a, sel) - sub_loss(pm, a, sel)) / (2 * hh)
         ap, am = a.copy(), a.copy()
-        ap[vi] += h
-        am[vi] -= h
-        fd[3] = (fp64_loss(pos64, mesh.indices, ap, rh, tri, tg) - fp64_loss(pos64, mesh.indices, am, rh, tri, tg)) / (2 * h)
+        ap[vi] += hh
+        am[vi] -= hh
+        return (sub_loss(pos64, ap, sel) - sub_loss(pos64, am, sel)) / (2 * hh)
+
+    h = 1e-4
+    worst_plain, worst = 0.0, 0.0
+    for vi in pick:
+        sel = np.nonzero(np.any(tv == vi, axis=1))[0]
+        fd_h = np.array([central(vi, c, h, sel) for c in range(4)])
+        fd_h2 = np.array([central(vi, c, h / 2, sel) for c in range(4)])
+        fd_h4 = np.array([central(vi, c, h / 4, sel) for c in range(4)])
+        rich = (4 * fd_h2 - fd_h) / 3
+        rich2 = (4 * fd_h4 - fd_h2) / 3
+        fd_unc = np.linalg.norm(rich[:3] - rich2[:3])
         got = np.array([*g_pos[vi], g_attr[vi]])
-        denom = max(np.linalg.norm(fd[:3]), 1e-3 * scale_p)
-        worst = max(worst, np.linalg.norm(got[:3] - fd[:3]) / denom)
-        assert abs(got[3] - fd[3]) <= 1e-3 * max(abs(fd[3]), 1e-3 * scale_a)
-    assert worst < 1e-3, worst
+        den = max(np.linalg.norm(rich2[:3]), floor_p)
+        err = np.linalg.norm(got[:3] - rich2[:3])
+        assert err <= 1e-3 * den + 2 * fd_unc, (vi, err / den, fd_unc / den)
+        worst = max(worst, err / den)
+        worst_plain = max(worst_plain, np.linalg.norm(got[:3] - fd_h[:3]) / den)
+        assert abs(got[3] - rich2[3]) <= 1e-3 * max(abs(rich2[3]), floor_a)
+    print(f"position gradient vs FP64: analytic max {rel_p.max():.2e}, Richardson FD max {worst:.2e}, "
+          f"plain central difference (h=1e-4) max {worst_plain:.2e}")

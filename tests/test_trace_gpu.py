@@ -68,10 +68,11 @@ def test_soup_reference_order_bit_identical(soup, cuda):
     assert tot["far_assert"] == 0
 
 
-def test_soup_ordered_matches_except_ties(soup, cuda):
+@pytest.mark.parametrize("traversal", [rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_BINARY])
+def test_soup_ordered_matches_except_ties(soup, traversal, cuda):
     sc, S, P, rays = soup
     expect, _ = run_oracle(S, rays)
-    got, ext = run_product(P, rays, rt.TRAVERSAL_ORDERED)
+    got, ext = run_product(P, rays, traversal)
     c = classify(got, expect)
     assert c["other"] == 0, c
     assert c["hit_mismatch"] == 0, c
@@ -85,12 +86,13 @@ def test_counts_equal_reference_counters(soup, cuda):
     assert c["node_visits"] == tot["bvh_visit"]
     assert c["tri_tests"] == tot["tri_visit"]
     assert c["tri_hits"] == tot["tri_hit"]
-    c2 = P.trace_counted(to_dev(rays), hits, traversal=rt.TRAVERSAL_ORDERED)
-    # the ordered walk prunes with the nearest hit found so far: never more triangle tests
-    assert c2["tri_tests"] <= tot["tri_visit"]
+    for trav in (rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_BINARY):
+        c2 = P.trace_counted(to_dev(rays), hits, traversal=trav)
+        # the ordered walks prune with the nearest hit found so far: fewer triangle tests
+        assert c2["tri_tests"] <= tot["tri_visit"]
 
 
-@pytest.mark.parametrize("traversal", [rt.TRAVERSAL_REFERENCE, rt.TRAVERSAL_ORDERED])
+@pytest.mark.parametrize("traversal", [rt.TRAVERSAL_REFERENCE, rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_BINARY])
 def test_heightfield_random_rays(traversal, cuda):
     mesh = scenes.heightfield(128, seed=4)
     sc = single_mesh_scene(mesh, bins=2)
@@ -138,13 +140,14 @@ def test_flags_instances_reference_order(inst_scene, flags, anyhit, cuda):
         assert_bit_identical(got, ext, expect)
 
 
+@pytest.mark.parametrize("traversal", [rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_BINARY])
 @pytest.mark.parametrize("flags,anyhit", FLAG_CASES)
-def test_flags_instances_ordered(inst_scene, flags, anyhit, cuda):
+def test_flags_instances_ordered(inst_scene, flags, anyhit, traversal, cuda):
     sc, S, P, rays = inst_scene
     rng = np.random.default_rng(flags * 7 + anyhit)
     tidx = rng.integers(0, 2, rays.shape[0]).astype(np.uint32)
     expect, _ = run_oracle(S, rays, tlas_idx=tidx, ray_flags=flags, anyhit_mode=anyhit)
-    got, ext = run_product(P, rays, rt.TRAVERSAL_ORDERED, tlas_idx=tidx, ray_flags=flags, anyhit_mode=anyhit)
+    got, ext = run_product(P, rays, traversal, tlas_idx=tidx, ray_flags=flags, anyhit_mode=anyhit)
     first_hit = (flags & rt.RAY_FLAG_ACCEPT_FIRST_HIT_AND_END_SEARCH) or anyhit == 1
     if first_hit:
         # a first-hit query returns *a* hit: only hit/miss is order-independent
@@ -184,9 +187,10 @@ def test_edge_rays(cuda):
     expect, _ = run_oracle(S, rays)
     got, ext = run_product(P, rays, rt.TRAVERSAL_REFERENCE)
     assert_bit_identical(got, ext, expect)
-    got2, _ = run_product(P, rays, rt.TRAVERSAL_ORDERED)
-    c = classify(got2, expect)
-    assert c["other"] == 0, c
+    for trav in (rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_BINARY):
+        got2, _ = run_product(P, rays, trav)
+        c = classify(got2, expect)
+        assert c["other"] == 0, c
 
 
 def test_empty_batch_and_bad_tlas_index(cuda):

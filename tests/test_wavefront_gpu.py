@@ -36,10 +36,11 @@ def test_wavefront_reference_order_bit_identical(sample_index, cuda):
         assert np.array_equal(got[f].view(np.uint32), exp[f].view(np.uint32)), f
 
 
-def test_wavefront_ordered_matches_except_ties(cuda):
+@pytest.mark.parametrize("traversal", [rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_BINARY])
+def test_wavefront_ordered_matches_except_ties(traversal, cuda):
     mesh = scenes.heightfield(128, seed=1)
     cam = scenes.heightfield_camera(160, 96)
-    got, exp, rays, counts = run_both(mesh, cam, rt.TRAVERSAL_ORDERED)
+    got, exp, rays, counts = run_both(mesh, cam, traversal)
     assert counts == tuple(rays)
     same_primary = (got["primary_prim"] == exp["primary_prim"]) & (got["primary_t"] == exp["primary_t"])
     tie = (~same_primary) & (got["primary_t"] == exp["primary_t"])
