@@ -356,7 +356,9 @@ rdn_status rdn_graph_destroy(rdn_graph* graph);
 /* ---- differentiable closest hit (frozen visibility) ------------------ */
 
 /* Loss = sum over rays of (value - target)^2, value = the hit triangle's vertex
- * attribute interpolated with the hit barycentrics (1-u-v, u, v); misses add
+ * attribute interpolated with the barycentrics (1-u-v, u, v) of the hit, which
+ * the traversal finds with the reference's test and these kernels re-solve in
+ * float-float (f32 FMA) arithmetic for accuracy at grazing angles; misses add
  * nothing. Vertices are those of the built vertex array (all geometries'
  * positions in creation order, rdn_get_built_array(..., 10, ...)). */
 typedef struct rdn_attr_loss_desc {

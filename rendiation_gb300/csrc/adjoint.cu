@@ -21,6 +21,14 @@
 // Vertex gradients are accumulated as float4 (dx, dy, dz, dattr) per vertex
 // with one vector atomicAdd per triangle corner. All quantities are in the
 // instance's object space (world space for identity instances).
+//
+// Barycentrics of the loss: the traversal finds the hit with the reference's
+// f32 triangle test, whose projected barycentrics lose accuracy for rays that
+// graze the triangle (relative error ~ 1e-7 / cos). Both kernels therefore
+// re-solve (u, v) on the hit triangle with Cramer's rule in float-float
+// arithmetic (error-free TwoSum / TwoProduct built on f32 FMA), which keeps the
+// loss and its gradient accurate to ~1e-6 for rays down to a few degrees of
+// grazing, with f32 arithmetic only.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -34,20 +42,79 @@ namespace {
 
 using namespace dev;
 
+// float-float value hi + lo
+struct ff {
+  float hi, lo;
+};
+__device__ __forceinline__ ff two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  return ff{s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ ff two_prod(float a, float b) {
+  const float p = a * b;
+  return ff{p, fmaf(a, b, -p)};
+}
+__device__ __forceinline__ ff ff_add(ff a, ff b) {
+  ff s = two_sum(a.hi, b.hi);
+  const float lo = s.lo + (a.lo + b.lo);
+  return two_sum(s.hi, lo);
+}
+__device__ __forceinline__ ff ff_neg(ff a) { return ff{-a.hi, -a.lo}; }
+__device__ __forceinline__ ff ff_mul(ff a, ff b) {
+  ff p = two_prod(a.hi, b.hi);
+  const float lo = p.lo + (a.hi * b.lo + a.lo * b.hi);
+  return two_sum(p.hi, lo);
+}
+struct ff3 {
+  ff x, y, z;
+};
+__device__ __forceinline__ ff3 ff3_sub(float3 a, float3 b) {
+  return ff3{two_sum(a.x, -b.x), two_sum(a.y, -b.y), two_sum(a.z, -b.z)};
+}
+__device__ __forceinline__ ff3 ff3_of(float3 a) { return ff3{{a.x, 0.f}, {a.y, 0.f}, {a.z, 0.f}}; }
+__device__ __forceinline__ ff3 ff3_cross(ff3 a, ff3 b) {
+  return ff3{ff_add(ff_mul(a.y, b.z), ff_neg(ff_mul(a.z, b.y))),
+             ff_add(ff_mul(a.z, b.x), ff_neg(ff_mul(a.x, b.z))),
+             ff_add(ff_mul(a.x, b.y), ff_neg(ff_mul(a.y, b.x)))};
+}
+__device__ __forceinline__ ff ff3_dot(ff3 a, ff3 b) {
+  return ff_add(ff_add(ff_mul(a.x, b.x), ff_mul(a.y, b.y)), ff_mul(a.z, b.z));
+}
+__device__ __forceinline__ float ff_div(ff a, ff b) { return (a.hi + a.lo) / (b.hi + b.lo); }
+
 struct HitGeom {
   uint32_t i0, i1, i2;
   float w0, u, v;
+  float3 e1, e2;  // f32 edges (for the adjoint's lambda)
 };
 
-__device__ __forceinline__ HitGeom hit_vertices(const TraceParams& p, const AdjointParams& a, const RayCtx& R) {
+// Hit triangle's vertices and barycentrics re-solved in float-float: with
+// M = [-d | e1 | e2] and s = o - v0, u = det[-d, s, e2] / det M and
+// v = det[-d, e1, s] / det M (Cramer), e1, e2, s formed exactly.
+__device__ __forceinline__ HitGeom hit_vertices(const TraceParams& p, const AdjointParams& a, const RayCtx& R,
+                                                const InstanceRay& ir) {
   HitGeom h;
   const uint32_t tri = __ldg(p.redirect + R.best.k);
   h.i0 = __ldg(a.indices + 3 * (size_t)tri);
   h.i1 = __ldg(a.indices + 3 * (size_t)tri + 1);
   h.i2 = __ldg(a.indices + 3 * (size_t)tri + 2);
-  h.u = R.best.u;
-  h.v = R.best.v;
+  const float3 v0 = make_float3(__ldg(a.vertices + 3 * (size_t)h.i0), __ldg(a.vertices + 3 * (size_t)h.i0 + 1),
+                                __ldg(a.vertices + 3 * (size_t)h.i0 + 2));
+  const float3 v1 = make_float3(__ldg(a.vertices + 3 * (size_t)h.i1), __ldg(a.vertices + 3 * (size_t)h.i1 + 1),
+                                __ldg(a.vertices + 3 * (size_t)h.i1 + 2));
+  const float3 v2 = make_float3(__ldg(a.vertices + 3 * (size_t)h.i2), __ldg(a.vertices + 3 * (size_t)h.i2 + 1),
+                                __ldg(a.vertices + 3 * (size_t)h.i2 + 2));
+  const ff3 E1 = ff3_sub(v1, v0), E2 = ff3_sub(v2, v0), S = ff3_sub(ir.o, v0);
+  const ff3 ND = ff3_of(make_float3(-ir.d.x, -ir.d.y, -ir.d.z));
+  const ff det = ff3_dot(ND, ff3_cross(E1, E2));
+  const ff du = ff3_dot(ND, ff3_cross(S, E2));
+  const ff dv = ff3_dot(ND, ff3_cross(E1, S));
+  h.u = ff_div(du, det);
+  h.v = ff_div(dv, det);
   h.w0 = 1.0f - h.u - h.v;
+  h.e1 = make_float3(E1.x.hi, E1.y.hi, E1.z.hi);
+  h.e2 = make_float3(E2.x.hi, E2.y.hi, E2.z.hi);
   return h;
 }
 
@@ -71,7 +138,8 @@ __global__ void __launch_bounds__(128) attr_forward_kernel(TraceParams p, Adjoin
     traverse_ray<MODE, false>(p, R, a.tlas_uniform, smem_stack + threadIdx.x, blockDim.x, bad);
     float value = 0.0f;
     if (R.best.have) {
-      const HitGeom h = hit_vertices(p, a, R);
+      const InstanceRay ir = to_instance(p.tlas_data + R.best.inst, R.o, R.d, 0u);
+      const HitGeom h = hit_vertices(p, a, R, ir);
       value = h.w0 * __ldg(a.attributes + h.i0) + h.u * __ldg(a.attributes + h.i1) + h.v * __ldg(a.attributes + h.i2);
       const float diff = value - (a.targets ? __ldg(a.targets + i) : 0.0f);
       loss = diff * diff;
@@ -110,17 +178,14 @@ __global__ void __launch_bounds__(128) attr_adjoint_kernel(TraceParams p, Adjoin
   traverse_ray<MODE, false>(p, R, a.tlas_uniform, smem_stack + threadIdx.x, blockDim.x, bad);
   float3 go = make_float3(0.f, 0.f, 0.f), gd = go;
   if (R.best.have) {
-    const HitGeom h = hit_vertices(p, a, R);
+    const InstanceRay ir = to_instance(p.tlas_data + R.best.inst, R.o, R.d, 0u);
+    const HitGeom h = hit_vertices(p, a, R, ir);
     const float a0 = __ldg(a.attributes + h.i0), a1 = __ldg(a.attributes + h.i1), a2 = __ldg(a.attributes + h.i2);
     const float value = h.w0 * a0 + h.u * a1 + h.v * a2;
     const float target = a.targets ? __ldg(a.targets + i) : 0.0f;
     const float r = 2.0f * (value - target) * a.grad_scale;
     const float gu = r * (a1 - a0), gv = r * (a2 - a0);
-    // object-space ray of the hit instance and the triangle edges
-    const InstanceRay ir = to_instance(p.tlas_data + R.best.inst, R.o, R.d, 0u);
-    const float4* rec = p.tris + 4 * (size_t)R.best.k;
-    const float4 q1 = __ldg(rec + 1), q2 = __ldg(rec + 2);
-    const float3 e1 = make_float3(q1.x, q1.y, q1.z), e2 = make_float3(q2.x, q2.y, q2.z);
+    const float3 e1 = h.e1, e2 = h.e2;
     const float3 nd = make_float3(-ir.d.x, -ir.d.y, -ir.d.z);
     const float3 c12 = cross3(e1, e2);
     const float det = dot3(nd, c12);

@@ -12,6 +12,7 @@ struct AdjointParams {
   const float4* rays;         // 2 per ray
   uint32_t count, tlas_uniform;
   const uint32_t* indices;    // built vertex indices, 3 per triangle
+  const float* vertices;      // built vertex positions, 3 per vertex
   const float* attributes;    // per vertex of the built vertex array
   const float* targets;       // per ray, nullable (0)
   float* ray_value;           // per ray, nullable

@@ -41,6 +41,7 @@ void free_device(rdn::DeviceBuilt& d) {
   free_buf(d.leaf_ranges);
   free_buf(d.geom_root_code);
   free_buf(d.indices);
+  free_buf(d.vertices);
   free_buf(d.tlas_bvh_forest);
   free_buf(d.tri_bvh_forest);
   free_buf(d.tlas_data);
@@ -110,6 +111,7 @@ rdn_status do_build(rdn_ctx* c) {
     UP(leaf_ranges, leaf_ranges)
     UP(geom_root_code, geom_root_code)
     UP(indices, indices)
+    UP(vertices, vertices)
     UP(wide4_nodes, wide4_nodes)
     UP(geom_root_code4, geom_root_code4)
 #undef UP
@@ -629,6 +631,7 @@ rdn_status prepare_attr(rdn_ctx* c, const rdn_attr_loss_desc* d, bool adjoint, r
   a.count = d->count;
   a.tlas_uniform = d->tlas_uniform;
   a.indices = c->dev.indices.ptr;
+  a.vertices = c->dev.vertices.ptr;
   a.attributes = d->attributes;
   a.targets = d->targets;
   a.ray_value = d->ray_value;

@@ -137,6 +137,7 @@ struct DevBuf {
 
 struct DeviceBuilt {
   DevBuf<uint32_t> tlas_binding, tlas_bvh_root, indices_redirect, leaf_ranges, geom_root_code, indices;
+  DevBuf<float> vertices;
   DevBuf<DeviceBVHNode> tlas_bvh_forest, tri_bvh_forest;
   DevBuf<DeviceInstance> tlas_data;
   DevBuf<TlasBounding> tlas_bounding;

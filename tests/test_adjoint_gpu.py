@@ -95,10 +95,13 @@ def test_forward_matches_oracle_hits(field, cuda):
     hit = hits["prim"] != orc.MISS
     tri = hits["prim"][hit]
     tv = mesh.indices.reshape(-1, 3)[tri]
-    u, v = hits["u"][hit], hits["v"][hit]
-    expect = (np.float32(1) - u - v) * attr[tv[:, 0]] + u * attr[tv[:, 1]] + v * attr[tv[:, 2]]
+    # the loss kernels re-solve the barycentrics of the traversal's hit in float-float:
+    # the value must match the FP64 interpolation on the same triangle
+    t64, u64, v64, _ = fp64_hits(mesh.positions, mesh.indices, rays[hit], tri)
+    a64 = attr.astype(np.float64)
+    expect = (1 - u64 - v64) * a64[tv[:, 0]] + u64 * a64[tv[:, 1]] + v64 * a64[tv[:, 2]]
     got = value.cpu().numpy()
-    assert np.array_equal(got[hit], expect.astype(np.float32))
+    assert np.max(np.abs(got[hit] - expect)) < 2e-6
     assert np.all(got[~hit] == 0)
     assert abs(tot.item() - float(np.sum(loss.cpu().numpy().astype(np.float64)))) < 1e-6 * max(1.0, tot.item())
 
