@@ -91,7 +91,9 @@ struct HitGeom {
 
 // Hit triangle's vertices and barycentrics re-solved in float-float: with
 // M = [-d | e1 | e2] and s = o - v0, u = det[-d, s, e2] / det M and
-// v = det[-d, e1, s] / det M (Cramer), e1, e2, s formed exactly.
+// v = det[-d, e1, s] / det M (Cramer), e1, e2, s formed exactly. Cramer's rule
+// does not depend on the length of d, so d is the object-space direction before
+// normalisation (exact for an identity instance).
 __device__ __forceinline__ HitGeom hit_vertices(const TraceParams& p, const AdjointParams& a, const RayCtx& R,
                                                 const InstanceRay& ir) {
   HitGeom h;
@@ -106,7 +108,11 @@ __device__ __forceinline__ HitGeom hit_vertices(const TraceParams& p, const Adjo
   const float3 v2 = make_float3(__ldg(a.vertices + 3 * (size_t)h.i2), __ldg(a.vertices + 3 * (size_t)h.i2 + 1),
                                 __ldg(a.vertices + 3 * (size_t)h.i2 + 2));
   const ff3 E1 = ff3_sub(v1, v0), E2 = ff3_sub(v2, v0), S = ff3_sub(ir.o, v0);
-  const ff3 ND = ff3_of(make_float3(-ir.d.x, -ir.d.y, -ir.d.z));
+  const float* m = p.tlas_data[R.best.inst].transform_inv;
+  const float3 dobj = make_float3(R.d.x * __ldg(m + 0) + R.d.y * __ldg(m + 4) + R.d.z * __ldg(m + 8),
+                                  R.d.x * __ldg(m + 1) + R.d.y * __ldg(m + 5) + R.d.z * __ldg(m + 9),
+                                  R.d.x * __ldg(m + 2) + R.d.y * __ldg(m + 6) + R.d.z * __ldg(m + 10));
+  const ff3 ND = ff3_of(make_float3(-dobj.x, -dobj.y, -dobj.z));
   const ff det = ff3_dot(ND, ff3_cross(E1, E2));
   const ff du = ff3_dot(ND, ff3_cross(S, E2));
   const ff dv = ff3_dot(ND, ff3_cross(E1, S));
