@@ -389,6 +389,31 @@ rdn_status rdn_attr_loss_forward(rdn_ctx* ctx, const rdn_attr_loss_desc* desc, v
  * (object space of the hit instance). */
 rdn_status rdn_attr_loss_adjoint(rdn_ctx* ctx, const rdn_attr_loss_desc* desc, void* stream);
 
+/* ---- parallel primitives (shader/parallel-compute) ---------------------
+ * Stateless, on the calling thread's current device, stream-ordered. Scratch
+ * is caller-owned device memory of at least the queried size, 256-byte aligned. */
+
+rdn_status rdn_scan_scratch_size(uint32_t count, size_t* bytes);
+/* Prefix sum of u32 (wrapping). inclusive != 0 for an inclusive scan. segment:
+ * 0, or a power of two after which an inclusive scan restarts (the reference's
+ * workgroup-scoped scan, prefix_scan.rs:39-114; without segments it is the
+ * device-wide segmented scan of lib.rs:398-429, with no WG^2 length limit). */
+rdn_status rdn_scan_u32(const uint32_t* in, uint32_t* out, uint32_t count, int inclusive, uint32_t segment,
+                        void* scratch, size_t scratch_bytes, void* stream);
+
+rdn_status rdn_compact_scratch_size(uint32_t count, size_t* bytes);
+/* Stream compaction (stream_compaction.rs:3-45): out receives the values whose
+ * flag is non-zero, in order, and zeros after them; *out_count (device) the
+ * number kept. */
+rdn_status rdn_compact_u32(const uint32_t* values, const uint32_t* flags, uint32_t* out, uint32_t* out_count,
+                           uint32_t count, void* scratch, size_t scratch_bytes, void* stream);
+
+rdn_status rdn_radix_sort_scratch_size(uint32_t count, size_t* bytes);
+/* Stable LSD radix sort of u32 keys (radix_sort.rs:29-74) on their low
+ * key_bits bits (1..32), carrying optional u32 values; in place. */
+rdn_status rdn_radix_sort_u32(uint32_t* keys, uint32_t* values, uint32_t count, uint32_t key_bits, void* scratch,
+                              size_t scratch_bytes, void* stream);
+
 /* Allocation-free variant of rdn_wavefront_shadow_bounce; it has no
  * counterpart in the reference. For callers that cannot allocate device
  * memory (a host that hands out all device memory from its own budget fixed at

@@ -30,6 +30,7 @@ UNITS = {
     "wavefront_static.cu": [],
     "paths.cu": ["-fmad=false"],
     "adjoint.cu": ["-fmad=false"],
+    "parallel.cu": [],
 }
 
 

@@ -10,6 +10,7 @@
 #include "rdn_core.h"
 #include "trace_kernels.h"
 #include "adjoint.h"
+#include "parallel.h"
 #include "paths.h"
 #include "wavefront.h"
 
@@ -674,6 +675,53 @@ rdn_status rdn_attr_loss_adjoint(rdn_ctx* c, const rdn_attr_loss_desc* d, void* 
     e = rdn::launch_attr_adjoint(p, a, mode_of(d->traversal), d->block_size, static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(c, e, "attribute loss adjoint");
   return RDN_OK;
+}
+
+rdn_status rdn_scan_scratch_size(uint32_t count, size_t* bytes) {
+  if (!bytes) return RDN_ERR_INVALID_ARG;
+  *bytes = rdn::scan_scratch_bytes(count);
+  return RDN_OK;
+}
+
+rdn_status rdn_scan_u32(const uint32_t* in, uint32_t* out, uint32_t count, int inclusive, uint32_t segment,
+                        void* scratch, size_t scratch_bytes, void* stream) {
+  if (count && (!in || !out || !scratch)) return RDN_ERR_INVALID_ARG;
+  if (segment & (segment - 1)) return RDN_ERR_INVALID_ARG;
+  if (scratch_bytes < rdn::scan_scratch_bytes(count) || (reinterpret_cast<uintptr_t>(scratch) & 255))
+    return RDN_ERR_INVALID_ARG;
+  cudaError_t e = rdn::scan_u32(in, out, count, inclusive != 0, segment, scratch, static_cast<cudaStream_t>(stream));
+  return e == cudaSuccess ? RDN_OK : RDN_ERR_CUDA;
+}
+
+rdn_status rdn_compact_scratch_size(uint32_t count, size_t* bytes) {
+  if (!bytes) return RDN_ERR_INVALID_ARG;
+  *bytes = rdn::compact_scratch_bytes(count);
+  return RDN_OK;
+}
+
+rdn_status rdn_compact_u32(const uint32_t* values, const uint32_t* flags, uint32_t* out, uint32_t* out_count,
+                           uint32_t count, void* scratch, size_t scratch_bytes, void* stream) {
+  if (!out_count || (count && (!values || !flags || !out || !scratch))) return RDN_ERR_INVALID_ARG;
+  if (scratch_bytes < rdn::compact_scratch_bytes(count) || (reinterpret_cast<uintptr_t>(scratch) & 255))
+    return RDN_ERR_INVALID_ARG;
+  cudaError_t e = rdn::compact_u32(values, flags, out, out_count, count, scratch, static_cast<cudaStream_t>(stream));
+  return e == cudaSuccess ? RDN_OK : RDN_ERR_CUDA;
+}
+
+rdn_status rdn_radix_sort_scratch_size(uint32_t count, size_t* bytes) {
+  if (!bytes) return RDN_ERR_INVALID_ARG;
+  *bytes = rdn::sort_scratch_bytes(count);
+  return RDN_OK;
+}
+
+rdn_status rdn_radix_sort_u32(uint32_t* keys, uint32_t* values, uint32_t count, uint32_t key_bits, void* scratch,
+                              size_t scratch_bytes, void* stream) {
+  if (count > 1 && (!keys || !scratch)) return RDN_ERR_INVALID_ARG;
+  if (key_bits < 1 || key_bits > 32) return RDN_ERR_INVALID_ARG;
+  if (scratch_bytes < rdn::sort_scratch_bytes(count) || (reinterpret_cast<uintptr_t>(scratch) & 255))
+    return RDN_ERR_INVALID_ARG;
+  cudaError_t e = rdn::radix_sort_u32(keys, values, count, key_bits, scratch, static_cast<cudaStream_t>(stream));
+  return e == cudaSuccess ? RDN_OK : RDN_ERR_CUDA;
 }
 
 // Allocation-free wavefront: identical work to rdn_wavefront_shadow_bounce with

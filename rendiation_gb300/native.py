@@ -26,6 +26,8 @@ EXPORTED_SYMBOLS = [
     "rdn_trace", "rdn_trace_counted", "rdn_wavefront_scratch_size", "rdn_wavefront_shadow_bounce",
     "rdn_wavefront_shadow_bounce_static", "rdn_paths_scratch_size", "rdn_trace_paths", "rdn_trace_paths_graph",
     "rdn_graph_launch", "rdn_graph_destroy", "rdn_attr_loss_forward", "rdn_attr_loss_adjoint",
+    "rdn_scan_scratch_size", "rdn_scan_u32", "rdn_compact_scratch_size", "rdn_compact_u32",
+    "rdn_radix_sort_scratch_size", "rdn_radix_sort_u32",
 ]
 
 
@@ -156,5 +158,14 @@ def lib() -> C.CDLL:
     L.rdn_attr_loss_forward.restype = i32
     L.rdn_attr_loss_adjoint.argtypes = [vp, C.POINTER(AttrLossDesc), vp]
     L.rdn_attr_loss_adjoint.restype = i32
+    for name in ("rdn_scan_scratch_size", "rdn_compact_scratch_size", "rdn_radix_sort_scratch_size"):
+        getattr(L, name).argtypes = [u32, C.POINTER(C.c_size_t)]
+        getattr(L, name).restype = i32
+    L.rdn_scan_u32.argtypes = [vp, vp, u32, C.c_int, u32, vp, C.c_size_t, vp]
+    L.rdn_scan_u32.restype = i32
+    L.rdn_compact_u32.argtypes = [vp, vp, vp, vp, u32, vp, C.c_size_t, vp]
+    L.rdn_compact_u32.restype = i32
+    L.rdn_radix_sort_u32.argtypes = [vp, vp, u32, u32, vp, C.c_size_t, vp]
+    L.rdn_radix_sort_u32.restype = i32
     _lib = L
     return L
