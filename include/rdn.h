@@ -152,10 +152,15 @@ typedef struct rdn_hit_ext {
  * RDN_TRAVERSAL_REFERENCE: the reference's stackless threaded hit/miss walk
  *   (traverse_cpu.rs:291-319) over its own 48 B node layout; bit-identical to
  *   the reference CPU traversal, including ties and which hit ends a search.
- * RDN_TRAVERSAL_ORDERED_BINARY: as ORDERED over 64 B two-child nodes. */
+ * RDN_TRAVERSAL_ORDERED_BINARY: as ORDERED over 64 B two-child nodes.
+ * RDN_TRAVERSAL_SPECULATIVE(_BINARY): as ORDERED(_BINARY), and a lane that
+ *   reaches a leaf postpones it and keeps descending until every active lane of
+ *   its warp holds a leaf, so the warp tests triangles together. */
 #define RDN_TRAVERSAL_ORDERED 0u
 #define RDN_TRAVERSAL_REFERENCE 1u
 #define RDN_TRAVERSAL_ORDERED_BINARY 2u
+#define RDN_TRAVERSAL_SPECULATIVE 3u
+#define RDN_TRAVERSAL_SPECULATIVE_BINARY 4u
 
 /* Fixed any-hit policies for non-opaque geometry, standing in for a user
  * any-hit shader (RayAnyHitBehavior, api/ty.rs:134-136). */

@@ -144,6 +144,8 @@ void paths_bind_scratch(PathParams& q, void* scratch) {
 
 namespace {
 const void* path_fn(int mode) {
+  if (mode == MODE_WIDE4_SPEC) return (const void*)path_kernel<MODE_WIDE4_SPEC>;
+  if (mode == MODE_BINARY_SPEC) return (const void*)path_kernel<MODE_BINARY_SPEC>;
   if (mode == MODE_WIDE4) return (const void*)path_kernel<MODE_WIDE4>;
   if (mode == MODE_BINARY) return (const void*)path_kernel<MODE_BINARY>;
   return (const void*)path_kernel<MODE_THREADED>;
@@ -154,7 +156,7 @@ cudaError_t prepare_paths(const TraceParams& p, const PathParams& q, int mode, u
                           uint32_t* grid) {
   if (block == 0) block = 128;
   const size_t smem = mode != MODE_THREADED ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
-  static bool attr_done[3] = {false, false, false};
+  static bool attr_done[5] = {false, false, false, false, false};
   const void* fn = path_fn(mode);
   if (!attr_done[mode]) {
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
@@ -180,7 +182,9 @@ cudaError_t record_paths(const TraceParams& p, const PathParams& q, int mode, ui
   cudaError_t e = cudaMemsetAsync(q.queue_count, 0, sizeof(uint32_t) * 2 * (q.max_bounces + 1), stream);
   if (e != cudaSuccess) return e;
   for (uint32_t b = 0; b <= q.max_bounces; b++) {
-    if (mode == MODE_WIDE4) path_kernel<MODE_WIDE4><<<grid, block, smem, stream>>>(p, q, b);
+    if (mode == MODE_WIDE4_SPEC) path_kernel<MODE_WIDE4_SPEC><<<grid, block, smem, stream>>>(p, q, b);
+    else if (mode == MODE_BINARY_SPEC) path_kernel<MODE_BINARY_SPEC><<<grid, block, smem, stream>>>(p, q, b);
+    else if (mode == MODE_WIDE4) path_kernel<MODE_WIDE4><<<grid, block, smem, stream>>>(p, q, b);
     else if (mode == MODE_BINARY) path_kernel<MODE_BINARY><<<grid, block, smem, stream>>>(p, q, b);
     else path_kernel<MODE_THREADED><<<grid, block, smem, stream>>>(p, q, b);
     e = cudaGetLastError();

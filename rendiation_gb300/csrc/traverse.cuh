@@ -395,6 +395,147 @@ __device__ __forceinline__ bool blas_wide4(const TraceParams& p, RayCtx& R, cons
   }
 }
 
+// Pops the next pending child whose box still passes `t_near_max < t_max`
+// against the current far; EMPTY_SLOT when the stack is exhausted.
+__device__ __forceinline__ uint32_t pop_live(const uint2* stack, uint32_t stride, uint32_t& sp, float far_,
+                                             float& code_tn) {
+  while (sp) {
+    sp--;
+    const uint2 e = stack[sp * stride];
+    if (__uint_as_float(e.y) < far_) {
+      code_tn = __uint_as_float(e.y);
+      return e.x;
+    }
+  }
+  return EMPTY_SLOT;
+}
+
+__device__ __forceinline__ void push_entry(const TraceParams& p, uint2* stack, uint32_t stride, uint32_t& sp,
+                                           uint32_t depth, uint32_t code, float tn) {
+  if (sp < depth) stack[(sp++) * stride] = make_uint2(code, __float_as_uint(tn));
+  else atomicOr(p.error_word, 1u);  // the stack is sized from the tree depth: unreachable
+}
+
+// One interior-node step of the ordered walk: tests the children of node
+// `code`, pushes the farther hits and returns the nearest hit child (or the
+// next live stack entry when no child is hit).
+template <bool COUNT, int WIDTH>
+__device__ __forceinline__ uint32_t interior_step(const TraceParams& p, RayCtx& R, const InstanceRay& ir, uint32_t code,
+                                                  float& code_tn, uint2* stack, uint32_t stride, uint32_t& sp,
+                                                  uint32_t depth) {
+  const float near_ = R.tmin * ir.scaling, far_ = R.far_world * ir.scaling;
+  if (WIDTH == 2) {
+    const float4* w = p.wide + 4 * (size_t)code;
+    const float4 w0 = __ldg(w), w1 = __ldg(w + 1), w2 = __ldg(w + 2);
+    const uint2 cc = __ldg(reinterpret_cast<const uint2*>(w + 3));
+    if (COUNT) R.node_visits += 2;
+    float tn0, tn1;
+    const bool h0 = slab(ir.o, ir.inv_d, near_, far_, w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, tn0);
+    const bool h1 = slab(ir.o, ir.inv_d, near_, far_, w1.z, w1.w, w2.x, w2.y, w2.z, w2.w, tn1);
+    if (h0 && h1) {
+      const bool second_first = tn1 < tn0;
+      push_entry(p, stack, stride, sp, depth, second_first ? cc.x : cc.y, second_first ? tn0 : tn1);
+      code_tn = second_first ? tn1 : tn0;
+      return second_first ? cc.y : cc.x;
+    }
+    if (h0 || h1) {
+      code_tn = h0 ? tn0 : tn1;
+      return h0 ? cc.x : cc.y;
+    }
+    return pop_live(stack, stride, sp, far_, code_tn);
+  } else {
+    const float4* w = p.wide4 + 8 * (size_t)code;
+    const float4 lx = __ldg(w), ly = __ldg(w + 1), lz = __ldg(w + 2);
+    const float4 hx = __ldg(w + 3), hy = __ldg(w + 4), hz = __ldg(w + 5);
+    const uint4 cc = __ldg(reinterpret_cast<const uint4*>(w + 6));
+    const float inf = __int_as_float(0x7f800000);
+    float t0 = inf, t1 = inf, t2 = inf, t3 = inf;
+    uint32_t c0 = EMPTY_SLOT, c1 = EMPTY_SLOT, c2 = EMPTY_SLOT, c3 = EMPTY_SLOT;
+    float tn;
+    if (cc.x != EMPTY_SLOT && slab(ir.o, ir.inv_d, near_, far_, lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, tn)) {
+      t0 = tn;
+      c0 = cc.x;
+    }
+    if (cc.y != EMPTY_SLOT && slab(ir.o, ir.inv_d, near_, far_, lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, tn)) {
+      t1 = tn;
+      c1 = cc.y;
+    }
+    if (cc.z != EMPTY_SLOT && slab(ir.o, ir.inv_d, near_, far_, lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, tn)) {
+      t2 = tn;
+      c2 = cc.z;
+    }
+    if (cc.w != EMPTY_SLOT && slab(ir.o, ir.inv_d, near_, far_, lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, tn)) {
+      t3 = tn;
+      c3 = cc.w;
+    }
+    if (COUNT) R.node_visits += (cc.x != EMPTY_SLOT) + (cc.y != EMPTY_SLOT) + (cc.z != EMPTY_SLOT) + (cc.w != EMPTY_SLOT);
+    cswap(t0, c0, t1, c1);
+    cswap(t2, c2, t3, c3);
+    cswap(t0, c0, t2, c2);
+    cswap(t1, c1, t3, c3);
+    cswap(t1, c1, t2, c2);
+    if (c0 == EMPTY_SLOT) return pop_live(stack, stride, sp, far_, code_tn);
+    if (c3 != EMPTY_SLOT) push_entry(p, stack, stride, sp, depth, c3, t3);
+    if (c2 != EMPTY_SLOT) push_entry(p, stack, stride, sp, depth, c2, t2);
+    if (c1 != EMPTY_SLOT) push_entry(p, stack, stride, sp, depth, c1, t1);
+    code_tn = t0;
+    return c0;
+  }
+}
+
+// Ordered BLAS walk with speculative traversal: a lane that reaches a leaf
+// postpones it and keeps descending until every active lane of the warp holds
+// a leaf (or has finished), then the warp tests triangles together. Nodes are
+// visited in near-first order with the reference's box test; the speculation
+// only adds visits, never removes one, so the closest hit is unchanged.
+template <bool COUNT, int WIDTH>
+__device__ __forceinline__ bool blas_speculative(const TraceParams& p, RayCtx& R, const InstanceRay& ir,
+                                                 uint32_t root_node, uint32_t gslot, uint32_t inst_slot,
+                                                 bool is_opaque, bool cull_enable, bool cull_back, uint32_t prim_start,
+                                                 uint2* stack, uint32_t stride, uint32_t depth) {
+  {
+    if (COUNT) R.node_visits++;
+    const float4* nd = reinterpret_cast<const float4*>(p.tri_forest + root_node);
+    const float4 a = __ldg(nd), b = __ldg(nd + 1);
+    float tn;
+    if (!slab(ir.o, ir.inv_d, R.tmin * ir.scaling, R.far_world * ir.scaling, a.x, a.y, a.z, b.x, b.y, b.z, tn))
+      return false;
+  }
+  uint32_t code = __ldg((WIDTH == 2 ? p.geom_root_code : p.geom_root_code4) + gslot);
+  float code_tn = -__int_as_float(0x7f800000);
+  uint32_t leaf = EMPTY_SLOT;
+  uint32_t sp = 0;
+  if (code & LEAF_BIT) {
+    leaf = code;
+    code = EMPTY_SLOT;
+  }
+  while (code != EMPTY_SLOT || leaf != EMPTY_SLOT) {
+    while (code != EMPTY_SLOT && !(code & LEAF_BIT)) {
+      code = interior_step<COUNT, WIDTH>(p, R, ir, code, code_tn, stack, stride, sp, depth);
+      if (code != EMPTY_SLOT && (code & LEAF_BIT) && leaf == EMPTY_SLOT) {
+        leaf = code;
+        code = pop_live(stack, stride, sp, R.far_world * ir.scaling, code_tn);
+      }
+      if (!__any_sync(__activemask(), leaf == EMPTY_SLOT)) break;
+    }
+    while (leaf != EMPTY_SLOT) {
+      const uint2 lr = __ldg(p.leaves + (leaf & ~LEAF_BIT));
+      if (leaf_triangles<COUNT>(p, R, ir, lr.x, lr.y, gslot, inst_slot, is_opaque, cull_enable, cull_back,
+                                prim_start))
+        return true;
+      leaf = EMPTY_SLOT;
+      // the far may have shrunk: re-check the pending node before descending into it
+      if (code != EMPTY_SLOT && !(code_tn < R.far_world * ir.scaling))
+        code = pop_live(stack, stride, sp, R.far_world * ir.scaling, code_tn);
+      if (code != EMPTY_SLOT && (code & LEAF_BIT)) {
+        leaf = code;
+        code = pop_live(stack, stride, sp, R.far_world * ir.scaling, code_tn);
+      }
+    }
+  }
+  return false;
+}
+
 // Full query of one ray (traverse_cpu.rs:52-245). R must hold the ray; on
 // return R.best holds the committed hit. `bad` reports an unbound TLAS index.
 template <int MODE, bool COUNT>
@@ -445,7 +586,13 @@ __device__ __forceinline__ void traverse_ray(const TraceParams& p, RayCtx& R, ui
         geometry_cull(ir.flags, gm.w, pass, is_opaque, cull_enable, cull_back);
         if (!pass) continue;
         bool end;
-        if (MODE == MODE_WIDE4)
+        if (MODE == MODE_WIDE4_SPEC)
+          end = blas_speculative<COUNT, 4>(p, R, ir, gm.x, g, ti, is_opaque, cull_enable, cull_back, gm.z, stack,
+                                           stride, p.stack_depth);
+        else if (MODE == MODE_BINARY_SPEC)
+          end = blas_speculative<COUNT, 2>(p, R, ir, gm.x, g, ti, is_opaque, cull_enable, cull_back, gm.z, stack,
+                                           stride, p.stack_depth);
+        else if (MODE == MODE_WIDE4)
           end = blas_wide4<COUNT>(p, R, ir, gm.x, g, ti, is_opaque, cull_enable, cull_back, gm.z, stack, stride,
                                   p.stack_depth);
         else if (MODE == MODE_BINARY)

@@ -228,6 +228,8 @@ cudaError_t launch_wavefront(const TraceParams& p, const WavefrontParams& w, int
   if (block == 0) block = 128;
   const size_t n = (size_t)w.width * w.height;
   if (n == 0) return cudaSuccess;
+  if (mode == MODE_WIDE4_SPEC) return launch_wavefront_mode<MODE_WIDE4_SPEC>(p, w, block, sm_count, phases, stream);
+  if (mode == MODE_BINARY_SPEC) return launch_wavefront_mode<MODE_BINARY_SPEC>(p, w, block, sm_count, phases, stream);
   if (mode == MODE_WIDE4) return launch_wavefront_mode<MODE_WIDE4>(p, w, block, sm_count, phases, stream);
   if (mode == MODE_BINARY) return launch_wavefront_mode<MODE_BINARY>(p, w, block, sm_count, phases, stream);
   return launch_wavefront_mode<MODE_THREADED>(p, w, block, sm_count, phases, stream);

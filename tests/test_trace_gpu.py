@@ -15,6 +15,9 @@ from helpers import Scene, classify, instanced_scene, orc, rt, scenes, single_me
 
 pytestmark = pytest.mark.gpu
 
+ORDERED_MODES = [rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_BINARY, rt.TRAVERSAL_SPECULATIVE,
+                 rt.TRAVERSAL_SPECULATIVE_BINARY]
+
 
 def to_dev(rays: np.ndarray) -> torch.Tensor:
     return torch.from_numpy(np.ascontiguousarray(rays).view(np.float32).reshape(-1, 8).copy()).cuda()
@@ -68,7 +71,7 @@ def test_soup_reference_order_bit_identical(soup, cuda):
     assert tot["far_assert"] == 0
 
 
-@pytest.mark.parametrize("traversal", [rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_BINARY])
+@pytest.mark.parametrize("traversal", ORDERED_MODES)
 def test_soup_ordered_matches_except_ties(soup, traversal, cuda):
     sc, S, P, rays = soup
     expect, _ = run_oracle(S, rays)
@@ -86,13 +89,13 @@ def test_counts_equal_reference_counters(soup, cuda):
     assert c["node_visits"] == tot["bvh_visit"]
     assert c["tri_tests"] == tot["tri_visit"]
     assert c["tri_hits"] == tot["tri_hit"]
-    for trav in (rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_BINARY):
+    for trav in ORDERED_MODES:
         c2 = P.trace_counted(to_dev(rays), hits, traversal=trav)
         # the ordered walks prune with the nearest hit found so far: fewer triangle tests
         assert c2["tri_tests"] <= tot["tri_visit"]
 
 
-@pytest.mark.parametrize("traversal", [rt.TRAVERSAL_REFERENCE, rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_BINARY])
+@pytest.mark.parametrize("traversal", [rt.TRAVERSAL_REFERENCE] + ORDERED_MODES)
 def test_heightfield_random_rays(traversal, cuda):
     mesh = scenes.heightfield(128, seed=4)
     sc = single_mesh_scene(mesh, bins=2)
@@ -140,7 +143,7 @@ def test_flags_instances_reference_order(inst_scene, flags, anyhit, cuda):
         assert_bit_identical(got, ext, expect)
 
 
-@pytest.mark.parametrize("traversal", [rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_BINARY])
+@pytest.mark.parametrize("traversal", ORDERED_MODES)
 @pytest.mark.parametrize("flags,anyhit", FLAG_CASES)
 def test_flags_instances_ordered(inst_scene, flags, anyhit, traversal, cuda):
     sc, S, P, rays = inst_scene
@@ -187,7 +190,7 @@ def test_edge_rays(cuda):
     expect, _ = run_oracle(S, rays)
     got, ext = run_product(P, rays, rt.TRAVERSAL_REFERENCE)
     assert_bit_identical(got, ext, expect)
-    for trav in (rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_BINARY):
+    for trav in ORDERED_MODES:
         got2, _ = run_product(P, rays, trav)
         c = classify(got2, expect)
         assert c["other"] == 0, c
