@@ -176,9 +176,7 @@ def bench_wavefront(args, ws, rank):
     W, H = args.width, args.height
     mesh, P = build_heightfield_system(args.grid)
     cam = scenes.heightfield_camera(W, H)
-    traversal = {"reference": rt.TRAVERSAL_REFERENCE, "binary": rt.TRAVERSAL_ORDERED_BINARY,
-                  "speculative": rt.TRAVERSAL_SPECULATIVE,
-                  "speculative-binary": rt.TRAVERSAL_SPECULATIVE_BINARY}.get(
+    traversal = {"reference": rt.TRAVERSAL_REFERENCE, "wide": rt.TRAVERSAL_ORDERED_WIDE}.get(
         args.traversal, rt.TRAVERSAL_ORDERED)
     wf = rt.Wavefront(P, cam, LIGHT, traversal=traversal, block_size=args.block)
     stream = torch.cuda.current_stream()
@@ -345,9 +343,7 @@ def bench_batched(args):
     build_s = time.perf_counter() - t0
     rays = torch.from_numpy(b.rays.view(np.float32).reshape(-1, 8).copy()).cuda()
     tidx = torch.from_numpy(b.tlas_idx.astype(np.int32)).cuda()
-    traversal = {"reference": rt.TRAVERSAL_REFERENCE, "binary": rt.TRAVERSAL_ORDERED_BINARY,
-                  "speculative": rt.TRAVERSAL_SPECULATIVE,
-                  "speculative-binary": rt.TRAVERSAL_SPECULATIVE_BINARY}.get(
+    traversal = {"reference": rt.TRAVERSAL_REFERENCE, "wide": rt.TRAVERSAL_ORDERED_WIDE}.get(
         args.traversal, rt.TRAVERSAL_ORDERED)
     stream = torch.cuda.current_stream()
 
@@ -439,9 +435,7 @@ def bench_adjoint(args):
     cam = scenes.PinholeCamera.look_at((0.5, -0.5, 0.8), (0.5, 0.5, 0.0), 20.0, res, res)
     rays = torch.from_numpy(scenes.pinhole_rays(cam).view(np.float32).reshape(-1, 8).copy()).cuda()
     n = res * res
-    traversal = {"reference": rt.TRAVERSAL_REFERENCE, "binary": rt.TRAVERSAL_ORDERED_BINARY,
-                  "speculative": rt.TRAVERSAL_SPECULATIVE,
-                  "speculative-binary": rt.TRAVERSAL_SPECULATIVE_BINARY}.get(
+    traversal = {"reference": rt.TRAVERSAL_REFERENCE, "wide": rt.TRAVERSAL_ORDERED_WIDE}.get(
         args.traversal, rt.TRAVERSAL_ORDERED)
 
     def system(m):
@@ -564,8 +558,7 @@ def main():
     ap.add_argument("--grid", type=int, default=1024)
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
-    ap.add_argument("--traversal", default="ordered",
-                    choices=["ordered", "binary", "speculative", "speculative-binary", "reference"])
+    ap.add_argument("--traversal", default="ordered", choices=["ordered", "wide", "reference"])
     ap.add_argument("--block", type=int, default=0)
     ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU work for the CPU baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")

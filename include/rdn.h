@@ -145,22 +145,20 @@ typedef struct rdn_hit_ext {
 } rdn_hit_ext;
 
 /* Traversal order.
- * RDN_TRAVERSAL_ORDERED: nearest-child-first stack traversal over 128 B
- *   four-child nodes collapsed from the reference's tree (exact reference node
- *   boxes). Closest hits equal the reference's except among hits at exactly
- *   equal distance; first-hit (shadow) queries agree on hit/miss.
+ * RDN_TRAVERSAL_ORDERED (default): nearest-child-first stack traversal over
+ *   64 B two-child nodes holding the reference's exact node boxes, with
+ *   speculative leaf postponement (a lane that reaches a leaf keeps descending
+ *   until its whole warp holds leaves, so triangle tests run together). Closest
+ *   hits equal the reference's except among hits at exactly equal distance;
+ *   first-hit (shadow) queries agree on hit/miss.
  * RDN_TRAVERSAL_REFERENCE: the reference's stackless threaded hit/miss walk
  *   (traverse_cpu.rs:291-319) over its own 48 B node layout; bit-identical to
  *   the reference CPU traversal, including ties and which hit ends a search.
- * RDN_TRAVERSAL_ORDERED_BINARY: as ORDERED over 64 B two-child nodes.
- * RDN_TRAVERSAL_SPECULATIVE(_BINARY): as ORDERED(_BINARY), and a lane that
- *   reaches a leaf postpones it and keeps descending until every active lane of
- *   its warp holds a leaf, so the warp tests triangles together. */
+ * RDN_TRAVERSAL_ORDERED_WIDE: as ORDERED over 128 B four-child nodes collapsed
+ *   from the same tree (faster on coherent rays such as camera primaries). */
 #define RDN_TRAVERSAL_ORDERED 0u
 #define RDN_TRAVERSAL_REFERENCE 1u
-#define RDN_TRAVERSAL_ORDERED_BINARY 2u
-#define RDN_TRAVERSAL_SPECULATIVE 3u
-#define RDN_TRAVERSAL_SPECULATIVE_BINARY 4u
+#define RDN_TRAVERSAL_ORDERED_WIDE 2u
 
 /* Fixed any-hit policies for non-opaque geometry, standing in for a user
  * any-hit shader (RayAnyHitBehavior, api/ty.rs:134-136). */
@@ -179,7 +177,7 @@ typedef struct rdn_trace_desc {
   uint32_t cull_mask;       /* low 8 bits used */
   uint32_t traversal;       /* RDN_TRAVERSAL_* */
   uint32_t anyhit_mode;     /* RDN_ANYHIT_* */
-  uint32_t block_size;      /* 0 = tuned default */
+  uint32_t block_size;      /* 0 = 64 */
   uint32_t reserved;
 } rdn_trace_desc;
 
@@ -284,7 +282,7 @@ typedef struct rdn_wavefront_desc {
   uint32_t sample_index;     /* seeds the bounce sampler: xxhash32(px, py, 3*sample_index) */
   uint32_t tlas_uniform;
   uint32_t traversal;        /* RDN_TRAVERSAL_* */
-  uint32_t block_size;       /* 0 = 128 */
+  uint32_t block_size;       /* 0 = 64 */
   rdn_pixel_result* out;     /* device, width*height records */
   void* scratch;             /* device, >= rdn_wavefront_scratch_size() bytes, 256-byte aligned */
   size_t scratch_bytes;
@@ -335,7 +333,7 @@ typedef struct rdn_path_desc {
   float rr_survive;
   uint32_t seed;
   uint32_t traversal;           /* RDN_TRAVERSAL_* */
-  uint32_t block_size;          /* 0 = 128 */
+  uint32_t block_size;          /* 0 = 64 */
   uint32_t reserved;
   rdn_path_result* out;         /* device, count entries */
   void* scratch;                /* device, >= rdn_paths_scratch_size() bytes, 256-byte aligned */
@@ -381,7 +379,7 @@ typedef struct rdn_attr_loss_desc {
   float* grad_ray_direction;    /* device, nullable: 3 per ray (adjoint) */
   float grad_scale;             /* upstream gradient of the loss sum (adjoint), usually 1 */
   uint32_t traversal;           /* RDN_TRAVERSAL_* */
-  uint32_t block_size;          /* 0 = 128 */
+  uint32_t block_size;          /* 0 = 64 */
   uint32_t reserved;
 } rdn_attr_loss_desc;
 

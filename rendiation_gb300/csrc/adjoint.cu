@@ -241,9 +241,7 @@ cudaError_t launch_attr_mode(const TraceParams& p, const AdjointParams& a, bool 
 cudaError_t launch_attr(const TraceParams& p, const AdjointParams& a, int mode, bool adjoint, uint32_t block,
                         cudaStream_t stream) {
   if (a.count == 0) return cudaSuccess;
-  if (block == 0) block = 128;
-  if (mode == MODE_WIDE4_SPEC) return launch_attr_mode<MODE_WIDE4_SPEC>(p, a, adjoint, block, stream);
-  if (mode == MODE_BINARY_SPEC) return launch_attr_mode<MODE_BINARY_SPEC>(p, a, adjoint, block, stream);
+  if (block == 0) block = 64;
   if (mode == MODE_WIDE4) return launch_attr_mode<MODE_WIDE4>(p, a, adjoint, block, stream);
   if (mode == MODE_BINARY) return launch_attr_mode<MODE_BINARY>(p, a, adjoint, block, stream);
   return launch_attr_mode<MODE_THREADED>(p, a, adjoint, block, stream);

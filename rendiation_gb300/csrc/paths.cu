@@ -144,8 +144,6 @@ void paths_bind_scratch(PathParams& q, void* scratch) {
 
 namespace {
 const void* path_fn(int mode) {
-  if (mode == MODE_WIDE4_SPEC) return (const void*)path_kernel<MODE_WIDE4_SPEC>;
-  if (mode == MODE_BINARY_SPEC) return (const void*)path_kernel<MODE_BINARY_SPEC>;
   if (mode == MODE_WIDE4) return (const void*)path_kernel<MODE_WIDE4>;
   if (mode == MODE_BINARY) return (const void*)path_kernel<MODE_BINARY>;
   return (const void*)path_kernel<MODE_THREADED>;
@@ -154,9 +152,9 @@ const void* path_fn(int mode) {
 
 cudaError_t prepare_paths(const TraceParams& p, const PathParams& q, int mode, uint32_t block, int sm_count,
                           uint32_t* grid) {
-  if (block == 0) block = 128;
+  if (block == 0) block = 64;
   const size_t smem = mode != MODE_THREADED ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
-  static bool attr_done[5] = {false, false, false, false, false};
+  static bool attr_done[3] = {false, false, false};
   const void* fn = path_fn(mode);
   if (!attr_done[mode]) {
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
@@ -176,15 +174,13 @@ cudaError_t prepare_paths(const TraceParams& p, const PathParams& q, int mode, u
 
 cudaError_t record_paths(const TraceParams& p, const PathParams& q, int mode, uint32_t block, uint32_t grid,
                          cudaStream_t stream) {
-  if (block == 0) block = 128;
+  if (block == 0) block = 64;
   if (q.count == 0 || grid == 0) return cudaSuccess;
   const size_t smem = mode != MODE_THREADED ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
   cudaError_t e = cudaMemsetAsync(q.queue_count, 0, sizeof(uint32_t) * 2 * (q.max_bounces + 1), stream);
   if (e != cudaSuccess) return e;
   for (uint32_t b = 0; b <= q.max_bounces; b++) {
-    if (mode == MODE_WIDE4_SPEC) path_kernel<MODE_WIDE4_SPEC><<<grid, block, smem, stream>>>(p, q, b);
-    else if (mode == MODE_BINARY_SPEC) path_kernel<MODE_BINARY_SPEC><<<grid, block, smem, stream>>>(p, q, b);
-    else if (mode == MODE_WIDE4) path_kernel<MODE_WIDE4><<<grid, block, smem, stream>>>(p, q, b);
+    if (mode == MODE_WIDE4) path_kernel<MODE_WIDE4><<<grid, block, smem, stream>>>(p, q, b);
     else if (mode == MODE_BINARY) path_kernel<MODE_BINARY><<<grid, block, smem, stream>>>(p, q, b);
     else path_kernel<MODE_THREADED><<<grid, block, smem, stream>>>(p, q, b);
     e = cudaGetLastError();

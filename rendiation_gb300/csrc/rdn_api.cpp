@@ -129,10 +129,8 @@ rdn_status do_build(rdn_ctx* c) {
 
 int mode_of(uint32_t traversal) {
   if (traversal == RDN_TRAVERSAL_REFERENCE) return rdn::MODE_THREADED;
-  if (traversal == RDN_TRAVERSAL_ORDERED_BINARY) return rdn::MODE_BINARY;
-  if (traversal == RDN_TRAVERSAL_SPECULATIVE) return rdn::MODE_WIDE4_SPEC;
-  if (traversal == RDN_TRAVERSAL_SPECULATIVE_BINARY) return rdn::MODE_BINARY_SPEC;
-  return rdn::MODE_WIDE4;
+  if (traversal == RDN_TRAVERSAL_ORDERED_WIDE) return rdn::MODE_WIDE4;
+  return rdn::MODE_BINARY;
 }
 
 rdn_status fill_params(rdn_ctx* c, const rdn_trace_desc* desc, rdn::TraceParams& p) {
@@ -177,7 +175,7 @@ rdn_status validate_trace(rdn_ctx* c, const rdn_trace_desc* desc) {
   if ((reinterpret_cast<uintptr_t>(desc->rays) & 15) || (reinterpret_cast<uintptr_t>(desc->hits) & 15) ||
       (reinterpret_cast<uintptr_t>(desc->hits_ext) & 15))
     return fail(c, RDN_ERR_INVALID_ARG, "ray and hit buffers must be 16-byte aligned");
-  if (desc->traversal > RDN_TRAVERSAL_SPECULATIVE_BINARY) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
+  if (desc->traversal > RDN_TRAVERSAL_ORDERED_WIDE) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
   if (desc->anyhit_mode > RDN_ANYHIT_ACCEPT_EVEN_PRIMS) return fail(c, RDN_ERR_INVALID_ARG, "unknown any-hit mode");
   if (desc->block_size && (desc->block_size % 32 || desc->block_size > 256))
     return fail(c, RDN_ERR_INVALID_ARG, "block_size must be a multiple of 32 up to 256");
@@ -439,7 +437,7 @@ rdn_status rdn_wavefront_shadow_bounce(rdn_ctx* c, const rdn_wavefront_desc* d, 
   if (d->scratch_bytes < rdn::wavefront_scratch_bytes(W, H)) return fail(c, RDN_ERR_INVALID_ARG, "scratch too small");
   if ((reinterpret_cast<uintptr_t>(d->scratch) & 255) || (reinterpret_cast<uintptr_t>(d->out) & 15))
     return fail(c, RDN_ERR_INVALID_ARG, "scratch must be 256-byte and output 16-byte aligned");
-  if (d->traversal > RDN_TRAVERSAL_SPECULATIVE_BINARY) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
+  if (d->traversal > RDN_TRAVERSAL_ORDERED_WIDE) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
   if (d->phases > 3) return fail(c, RDN_ERR_INVALID_ARG, "unknown phase mask");
   if (d->block_size && (d->block_size % 32 || d->block_size > 128))
     return fail(c, RDN_ERR_INVALID_ARG, "block_size must be a multiple of 32 up to 128");
@@ -499,7 +497,7 @@ rdn_status prepare_path_launch(rdn_ctx* c, const rdn_path_desc* d, rdn::TracePar
   if ((reinterpret_cast<uintptr_t>(d->scratch) & 255) || (reinterpret_cast<uintptr_t>(d->rays) & 15) ||
       (reinterpret_cast<uintptr_t>(d->out) & 7))
     return fail(c, RDN_ERR_INVALID_ARG, "misaligned buffer");
-  if (d->traversal > RDN_TRAVERSAL_SPECULATIVE_BINARY) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
+  if (d->traversal > RDN_TRAVERSAL_ORDERED_WIDE) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
   if (d->block_size && (d->block_size % 32 || d->block_size > 128))
     return fail(c, RDN_ERR_INVALID_ARG, "block_size must be a multiple of 32 up to 128");
   if (!(d->rr_survive > 0.0f && d->rr_survive <= 1.0f)) return fail(c, RDN_ERR_INVALID_ARG, "rr_survive not in (0, 1]");
@@ -618,7 +616,7 @@ rdn_status prepare_attr(rdn_ctx* c, const rdn_attr_loss_desc* d, bool adjoint, r
   if (adjoint && d->count && !d->grad_vertices) return fail(c, RDN_ERR_INVALID_ARG, "null gradient buffer");
   if ((reinterpret_cast<uintptr_t>(d->rays) & 15) || (reinterpret_cast<uintptr_t>(d->grad_vertices) & 15))
     return fail(c, RDN_ERR_INVALID_ARG, "rays and gradients must be 16-byte aligned");
-  if (d->traversal > RDN_TRAVERSAL_SPECULATIVE_BINARY) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
+  if (d->traversal > RDN_TRAVERSAL_ORDERED_WIDE) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
   if (d->block_size && (d->block_size % 32 || d->block_size > 128))
     return fail(c, RDN_ERR_INVALID_ARG, "block_size must be a multiple of 32 up to 128");
   rdn_status st = ensure_built(c);
@@ -743,7 +741,7 @@ rdn_status rdn_wavefront_shadow_bounce_static(rdn_ctx* c, const rdn_wavefront_de
                     std::to_string(RDN_WAVEFRONT_STATIC_SCRATCH_BYTES) + " (about 466,000 pixels)");
   if (W && H && !d->out) return fail(c, RDN_ERR_INVALID_ARG, "null output");
   if (reinterpret_cast<uintptr_t>(d->out) & 15) return fail(c, RDN_ERR_INVALID_ARG, "output must be 16-byte aligned");
-  if (d->traversal > RDN_TRAVERSAL_SPECULATIVE_BINARY) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
+  if (d->traversal > RDN_TRAVERSAL_ORDERED_WIDE) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
   if (d->phases > 3) return fail(c, RDN_ERR_INVALID_ARG, "unknown phase mask");
   if (d->block_size && (d->block_size % 32 || d->block_size > 128))
     return fail(c, RDN_ERR_INVALID_ARG, "block_size must be a multiple of 32 up to 128");

@@ -65,24 +65,20 @@ __global__ void __launch_bounds__(256) trace_kernel(TraceParams p) {
 }  // namespace
 
 uint32_t stack_entries(int mode, uint32_t max_binary_depth, uint32_t max_wide4_depth) {
-  const bool wide4 = mode == MODE_WIDE4 || mode == MODE_WIDE4_SPEC;
-  const bool binary = mode == MODE_BINARY || mode == MODE_BINARY_SPEC;
-  uint32_t d = wide4 ? 3 * max_wide4_depth + 1 : (binary ? max_binary_depth + 1 : 0);
+  uint32_t d = mode == MODE_WIDE4 ? 3 * max_wide4_depth + 1 : (mode == MODE_BINARY ? max_binary_depth + 1 : 0);
   d = (d + 3) & ~3u;
   return d < 8 ? 8 : d;
 }
 
 cudaError_t launch_trace(const TraceParams& p, int mode, bool counted, uint32_t block, cudaStream_t stream) {
   if (p.count == 0) return cudaSuccess;
-  if (block == 0) block = 128;
+  if (block == 0) block = 64;
   const uint32_t grid = (p.count + block - 1) / block;
   const size_t smem = mode != MODE_THREADED ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
-  static bool attr_done[10] = {};
-  const void* fns[10] = {(const void*)trace_kernel<0, false>, (const void*)trace_kernel<0, true>,
-                         (const void*)trace_kernel<1, false>, (const void*)trace_kernel<1, true>,
-                         (const void*)trace_kernel<2, false>, (const void*)trace_kernel<2, true>,
-                         (const void*)trace_kernel<3, false>, (const void*)trace_kernel<3, true>,
-                         (const void*)trace_kernel<4, false>, (const void*)trace_kernel<4, true>};
+  static bool attr_done[6] = {};
+  const void* fns[6] = {(const void*)trace_kernel<0, false>, (const void*)trace_kernel<0, true>,
+                        (const void*)trace_kernel<1, false>, (const void*)trace_kernel<1, true>,
+                        (const void*)trace_kernel<2, false>, (const void*)trace_kernel<2, true>};
   const int slot = 2 * mode + (counted ? 1 : 0);
   if (!attr_done[slot]) {
     cudaError_t e = cudaFuncSetAttribute(fns[slot], cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
@@ -95,11 +91,7 @@ cudaError_t launch_trace(const TraceParams& p, int mode, bool counted, uint32_t 
     case 2: trace_kernel<1, false><<<grid, block, smem, stream>>>(p); break;
     case 3: trace_kernel<1, true><<<grid, block, smem, stream>>>(p); break;
     case 4: trace_kernel<2, false><<<grid, block, smem, stream>>>(p); break;
-    case 5: trace_kernel<2, true><<<grid, block, smem, stream>>>(p); break;
-    case 6: trace_kernel<3, false><<<grid, block, smem, stream>>>(p); break;
-    case 7: trace_kernel<3, true><<<grid, block, smem, stream>>>(p); break;
-    case 8: trace_kernel<4, false><<<grid, block, smem, stream>>>(p); break;
-    default: trace_kernel<4, true><<<grid, block, smem, stream>>>(p); break;
+    default: trace_kernel<2, true><<<grid, block, smem, stream>>>(p); break;
   }
   return cudaGetLastError();
 }

@@ -35,7 +35,7 @@ struct TraceParams {
 };
 
 // Traversal modes (template argument of every traversal kernel).
-enum TraversalMode : int { MODE_THREADED = 0, MODE_BINARY = 1, MODE_WIDE4 = 2, MODE_BINARY_SPEC = 3, MODE_WIDE4_SPEC = 4 };
+enum TraversalMode : int { MODE_THREADED = 0, MODE_BINARY = 1, MODE_WIDE4 = 2 };
 
 // stack entries the mode needs per thread
 uint32_t stack_entries(int mode, uint32_t max_binary_depth, uint32_t max_wide4_depth);

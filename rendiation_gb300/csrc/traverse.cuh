@@ -12,14 +12,16 @@
 // fminf/fmaxf (Rust f32::min/max), so every intersection value equals the
 // reference CPU's bit for bit.
 //
-// Two traversal orders over the same tree (the reference's SAH build):
+// Traversal orders over the same tree (the reference's SAH build):
 //   threaded: the reference's stackless hit/miss walk over its 48 B
 //     DeviceBVHNode forest (traverse_cpu.rs:291-319); identical results,
 //     including equal-distance ties and which hit ends a first-hit search.
-//   ordered: near-child-first traversal over 64 B two-child nodes with a
-//     per-thread stack in shared memory; each child box is tested with the
-//     reference's slab test, popped entries are re-checked against the current
-//     far with the reference's strict `t_near_max < t_max`.
+//   ordered (binary / wide4): nearest-child-first traversal over 64 B two-child
+//     or 128 B four-child nodes with a per-thread stack in shared memory, and
+//     speculative leaf postponement (a lane that reaches a leaf keeps
+//     descending until its whole warp holds leaves). Every child box is tested
+//     with the reference's slab test; popped entries are re-checked against the
+//     current far with the reference's strict `t_near_max < t_max`.
 // Both read triangles as 64 B precomputed records (v0, e1, e2, normal, uu, uv,
 // vv, 1/(uv^2-uu*vv)) — values the reference recomputes for every test.
 #pragma once
@@ -227,72 +229,6 @@ __device__ __forceinline__ bool blas_threaded(const TraceParams& p, RayCtx& R, c
   return false;
 }
 
-// BLAS of one geometry, near-child-first over two-child nodes.
-template <bool COUNT>
-__device__ __forceinline__ bool blas_ordered(const TraceParams& p, RayCtx& R, const InstanceRay& ir, uint32_t root_node,
-                                             uint32_t gslot, uint32_t inst_slot, bool is_opaque, bool cull_enable,
-                                             bool cull_back, uint32_t prim_start, uint2* stack, uint32_t stride,
-                                             uint32_t depth) {
-  // root box test with the reference node of this geometry
-  {
-    if (COUNT) R.node_visits++;
-    const float4* nd = reinterpret_cast<const float4*>(p.tri_forest + root_node);
-    const float4 a = __ldg(nd), b = __ldg(nd + 1);
-    float tn;
-    if (!slab(ir.o, ir.inv_d, R.tmin * ir.scaling, R.far_world * ir.scaling, a.x, a.y, a.z, b.x, b.y, b.z, tn))
-      return false;
-  }
-  uint32_t code = __ldg(p.geom_root_code + gslot);
-  uint32_t sp = 0;
-  for (;;) {
-    bool have_node = true;
-    // descend through interior nodes until a leaf is reached or no child is hit
-    while (!(code & LEAF_BIT)) {
-      const float4* w = p.wide + 4 * (size_t)code;
-      const float4 w0 = __ldg(w), w1 = __ldg(w + 1), w2 = __ldg(w + 2);
-      const uint2 cc = __ldg(reinterpret_cast<const uint2*>(w + 3));
-      if (COUNT) R.node_visits += 2;
-      const float near_ = R.tmin * ir.scaling, far_ = R.far_world * ir.scaling;
-      float tn0, tn1;
-      const bool h0 = slab(ir.o, ir.inv_d, near_, far_, w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, tn0);
-      const bool h1 = slab(ir.o, ir.inv_d, near_, far_, w1.z, w1.w, w2.x, w2.y, w2.z, w2.w, tn1);
-      if (h0 && h1) {
-        const bool second_first = tn1 < tn0;
-        const uint32_t later = second_first ? cc.x : cc.y;
-        const float later_tn = second_first ? tn0 : tn1;
-        if (sp < depth) {
-          stack[sp * stride] = make_uint2(later, __float_as_uint(later_tn));
-          sp++;
-        } else {
-          atomicOr(p.error_word, 1u);  // the stack is sized from the tree depth: unreachable
-        }
-        code = second_first ? cc.y : cc.x;
-      } else if (h0 || h1) {
-        code = h0 ? cc.x : cc.y;
-      } else {
-        have_node = false;
-        break;
-      }
-    }
-    if (have_node) {
-      const uint2 lr = __ldg(p.leaves + (code & ~LEAF_BIT));
-      if (leaf_triangles<COUNT>(p, R, ir, lr.x, lr.y, gslot, inst_slot, is_opaque, cull_enable, cull_back,
-                                prim_start))
-        return true;
-    }
-    // pop the next pending child whose box still passes `t_near_max < t_max`
-    for (;;) {
-      if (sp == 0) return false;
-      sp--;
-      const uint2 e = stack[sp * stride];
-      if (__uint_as_float(e.y) < R.far_world * ir.scaling) {
-        code = e.x;
-        break;
-      }
-    }
-  }
-}
-
 __device__ __forceinline__ void cswap(float& ta, uint32_t& ca, float& tb, uint32_t& cb) {
   if (tb < ta) {
     const float t = ta;
@@ -301,97 +237,6 @@ __device__ __forceinline__ void cswap(float& ta, uint32_t& ca, float& tb, uint32
     const uint32_t c = ca;
     ca = cb;
     cb = c;
-  }
-}
-
-// BLAS of one geometry over 128 B four-child nodes, nearest child first. Each
-// child box is tested with the reference's slab test; the remaining hit
-// children are pushed farthest first and re-checked against the current far
-// (t_near_max < t_max) when popped.
-template <bool COUNT>
-__device__ __forceinline__ bool blas_wide4(const TraceParams& p, RayCtx& R, const InstanceRay& ir, uint32_t root_node,
-                                           uint32_t gslot, uint32_t inst_slot, bool is_opaque, bool cull_enable,
-                                           bool cull_back, uint32_t prim_start, uint2* stack, uint32_t stride,
-                                           uint32_t depth) {
-  {
-    if (COUNT) R.node_visits++;
-    const float4* nd = reinterpret_cast<const float4*>(p.tri_forest + root_node);
-    const float4 a = __ldg(nd), b = __ldg(nd + 1);
-    float tn;
-    if (!slab(ir.o, ir.inv_d, R.tmin * ir.scaling, R.far_world * ir.scaling, a.x, a.y, a.z, b.x, b.y, b.z, tn))
-      return false;
-  }
-  uint32_t code = __ldg(p.geom_root_code4 + gslot);
-  uint32_t sp = 0;
-  for (;;) {
-    bool have_node = true;
-    while (!(code & LEAF_BIT)) {
-      const float4* w = p.wide4 + 8 * (size_t)code;
-      const float4 lx = __ldg(w), ly = __ldg(w + 1), lz = __ldg(w + 2);
-      const float4 hx = __ldg(w + 3), hy = __ldg(w + 4), hz = __ldg(w + 5);
-      const uint4 cc = __ldg(reinterpret_cast<const uint4*>(w + 6));
-      const float near_ = R.tmin * ir.scaling, far_ = R.far_world * ir.scaling;
-      const float inf = __int_as_float(0x7f800000);
-      float t0 = inf, t1 = inf, t2 = inf, t3 = inf;
-      uint32_t c0 = EMPTY_SLOT, c1 = EMPTY_SLOT, c2 = EMPTY_SLOT, c3 = EMPTY_SLOT;
-      float tn;
-      if (cc.x != EMPTY_SLOT && slab(ir.o, ir.inv_d, near_, far_, lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, tn)) {
-        t0 = tn;
-        c0 = cc.x;
-      }
-      if (cc.y != EMPTY_SLOT && slab(ir.o, ir.inv_d, near_, far_, lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, tn)) {
-        t1 = tn;
-        c1 = cc.y;
-      }
-      if (cc.z != EMPTY_SLOT && slab(ir.o, ir.inv_d, near_, far_, lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, tn)) {
-        t2 = tn;
-        c2 = cc.z;
-      }
-      if (cc.w != EMPTY_SLOT && slab(ir.o, ir.inv_d, near_, far_, lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, tn)) {
-        t3 = tn;
-        c3 = cc.w;
-      }
-      if (COUNT) R.node_visits += (cc.x != EMPTY_SLOT) + (cc.y != EMPTY_SLOT) + (cc.z != EMPTY_SLOT) + (cc.w != EMPTY_SLOT);
-      // sort the four (t_near, code) pairs ascending; misses carry (+inf, EMPTY)
-      cswap(t0, c0, t1, c1);
-      cswap(t2, c2, t3, c3);
-      cswap(t0, c0, t2, c2);
-      cswap(t1, c1, t3, c3);
-      cswap(t1, c1, t2, c2);
-      if (c0 == EMPTY_SLOT) {
-        have_node = false;
-        break;
-      }
-      // push the farther hits, farthest first
-      if (c3 != EMPTY_SLOT) {
-        if (sp < depth) stack[(sp++) * stride] = make_uint2(c3, __float_as_uint(t3));
-        else atomicOr(p.error_word, 1u);
-      }
-      if (c2 != EMPTY_SLOT) {
-        if (sp < depth) stack[(sp++) * stride] = make_uint2(c2, __float_as_uint(t2));
-        else atomicOr(p.error_word, 1u);
-      }
-      if (c1 != EMPTY_SLOT) {
-        if (sp < depth) stack[(sp++) * stride] = make_uint2(c1, __float_as_uint(t1));
-        else atomicOr(p.error_word, 1u);
-      }
-      code = c0;
-    }
-    if (have_node) {
-      const uint2 lr = __ldg(p.leaves + (code & ~LEAF_BIT));
-      if (leaf_triangles<COUNT>(p, R, ir, lr.x, lr.y, gslot, inst_slot, is_opaque, cull_enable, cull_back,
-                                prim_start))
-        return true;
-    }
-    for (;;) {
-      if (sp == 0) return false;
-      sp--;
-      const uint2 e = stack[sp * stride];
-      if (__uint_as_float(e.y) < R.far_world * ir.scaling) {
-        code = e.x;
-        break;
-      }
-    }
   }
 }
 
@@ -586,18 +431,12 @@ __device__ __forceinline__ void traverse_ray(const TraceParams& p, RayCtx& R, ui
         geometry_cull(ir.flags, gm.w, pass, is_opaque, cull_enable, cull_back);
         if (!pass) continue;
         bool end;
-        if (MODE == MODE_WIDE4_SPEC)
+        if (MODE == MODE_WIDE4)
           end = blas_speculative<COUNT, 4>(p, R, ir, gm.x, g, ti, is_opaque, cull_enable, cull_back, gm.z, stack,
                                            stride, p.stack_depth);
-        else if (MODE == MODE_BINARY_SPEC)
+        else if (MODE == MODE_BINARY)
           end = blas_speculative<COUNT, 2>(p, R, ir, gm.x, g, ti, is_opaque, cull_enable, cull_back, gm.z, stack,
                                            stride, p.stack_depth);
-        else if (MODE == MODE_WIDE4)
-          end = blas_wide4<COUNT>(p, R, ir, gm.x, g, ti, is_opaque, cull_enable, cull_back, gm.z, stack, stride,
-                                  p.stack_depth);
-        else if (MODE == MODE_BINARY)
-          end = blas_ordered<COUNT>(p, R, ir, gm.x, g, ti, is_opaque, cull_enable, cull_back, gm.z, stack, stride,
-                                    p.stack_depth);
         else
           end = blas_threaded<COUNT>(p, R, ir, gm.x, g, ti, is_opaque, cull_enable, cull_back, gm.z);
         if (end) {

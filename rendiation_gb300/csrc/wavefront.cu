@@ -225,11 +225,9 @@ cudaError_t launch_wavefront_mode(const TraceParams& p, const WavefrontParams& w
 cudaError_t launch_wavefront(const TraceParams& p, const WavefrontParams& w, int mode, uint32_t block,
                              int sm_count, uint32_t phases, cudaStream_t stream) {
   if (phases == 0) phases = 3;
-  if (block == 0) block = 128;
+  if (block == 0) block = 64;
   const size_t n = (size_t)w.width * w.height;
   if (n == 0) return cudaSuccess;
-  if (mode == MODE_WIDE4_SPEC) return launch_wavefront_mode<MODE_WIDE4_SPEC>(p, w, block, sm_count, phases, stream);
-  if (mode == MODE_BINARY_SPEC) return launch_wavefront_mode<MODE_BINARY_SPEC>(p, w, block, sm_count, phases, stream);
   if (mode == MODE_WIDE4) return launch_wavefront_mode<MODE_WIDE4>(p, w, block, sm_count, phases, stream);
   if (mode == MODE_BINARY) return launch_wavefront_mode<MODE_BINARY>(p, w, block, sm_count, phases, stream);
   return launch_wavefront_mode<MODE_THREADED>(p, w, block, sm_count, phases, stream);

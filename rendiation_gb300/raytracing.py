@@ -39,9 +39,7 @@ MISS = 0xFFFFFFFF
 
 TRAVERSAL_ORDERED = 0
 TRAVERSAL_REFERENCE = 1
-TRAVERSAL_ORDERED_BINARY = 2
-TRAVERSAL_SPECULATIVE = 3
-TRAVERSAL_SPECULATIVE_BINARY = 4
+TRAVERSAL_ORDERED_WIDE = 2
 ANYHIT_ACCEPT = 0
 ANYHIT_ACCEPT_AND_END = 1
 ANYHIT_ACCEPT_EVEN_PRIMS = 2

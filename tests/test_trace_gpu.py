@@ -15,8 +15,7 @@ from helpers import Scene, classify, instanced_scene, orc, rt, scenes, single_me
 
 pytestmark = pytest.mark.gpu
 
-ORDERED_MODES = [rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_BINARY, rt.TRAVERSAL_SPECULATIVE,
-                 rt.TRAVERSAL_SPECULATIVE_BINARY]
+ORDERED_MODES = [rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_WIDE]
 
 
 def to_dev(rays: np.ndarray) -> torch.Tensor:

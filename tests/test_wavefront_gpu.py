@@ -36,8 +36,7 @@ def test_wavefront_reference_order_bit_identical(sample_index, cuda):
         assert np.array_equal(got[f].view(np.uint32), exp[f].view(np.uint32)), f
 
 
-@pytest.mark.parametrize("traversal", [rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_BINARY, rt.TRAVERSAL_SPECULATIVE,
-                                       rt.TRAVERSAL_SPECULATIVE_BINARY])
+@pytest.mark.parametrize("traversal", [rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_WIDE])
 def test_wavefront_ordered_matches_except_ties(traversal, cuda):
     mesh = scenes.heightfield(128, seed=1)
     cam = scenes.heightfield_camera(160, 96)
