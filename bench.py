@@ -180,6 +180,25 @@ def bench_wavefront(args, ws, rank):
         args.traversal, rt.TRAVERSAL_ORDERED)
     wf = rt.Wavefront(P, cam, LIGHT, traversal=traversal, block_size=args.block)
     stream = torch.cuda.current_stream()
+    tuned = None
+    if args.tune and args.traversal == "ordered":
+        from rendiation_gb300.autotune import Autotuner, grid
+
+        tuner = Autotuner()
+        cands = grid(traversal=[rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_WIDE], block=[32, 64, 128])
+
+        def run_phase(ph):
+            def run(c):
+                wf.desc.traversal, wf.desc.block_size = c["traversal"], c["block"]
+                wf.run(7, phases=ph)
+            return run
+
+        wf.run(7)
+        torch.cuda.synchronize()
+        t1 = tuner.tune("wavefront-primary", cands, run_phase(1))
+        t2 = tuner.tune("wavefront-secondary", cands, run_phase(2))
+        wf.configure((t1.best["traversal"], t1.best["block"]), (t2.best["traversal"], t2.best["block"]))
+        tuned = {"primary": t1.best, "secondary": t2.best}
 
     # one frame to learn the ray counts, then the reference-order visit counts of those rays
     wf.run(0)
@@ -220,7 +239,7 @@ def bench_wavefront(args, ws, rank):
 
     k_prim, k_sec = [], []
     for s in range(max(3, min(args.steps, 10))):
-        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))  # noqa: B007
         e0.record(stream)
         wf.run(200 + s, phases=1)
         e1.record(stream)
@@ -280,6 +299,7 @@ def bench_wavefront(args, ws, rank):
             "rays_per_step": rays_per_step,
             "rays_primary": n_prim, "rays_shadow": n_sh, "rays_bounce": n_bo,
             "traversal": args.traversal,
+            "autotuned": tuned,
             "l2": f"no flush: acceleration structure {P.device_bytes() / 1e6:.0f} MB on device > 129 MB L2",
         },
         "e2e": {"value": round(e2e_value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": h2d,
@@ -348,6 +368,20 @@ def bench_batched(args):
     stream = torch.cuda.current_stream()
 
     batched = rt.Paths(P, rays, tidx, max_bounces=4, rr_start=2, seed=1, traversal=traversal)
+    tuned = None
+    if args.tune and args.traversal == "ordered":
+        from rendiation_gb300.autotune import Autotuner, grid
+
+        cands = grid(traversal=[rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_WIDE], block=[64, 128],
+                     sort_key=[rt.SORT_NONE, rt.SORT_SCENE_OCTANT, rt.SORT_SCENE_OCTANT_CELL])
+
+        def run(c):
+            batched.configure(c["traversal"], c["block"], c["sort_key"])
+            batched.run()
+
+        res = Autotuner().tune("batched-paths", cands, run, reps=2)
+        batched.configure(res.best["traversal"], res.best["block"], res.best["sort_key"])
+        tuned = {"best": res.best, "timings_ms": res.timings_ms}
     batched.capture()
     for _ in range(args.warmup):
         batched.launch_graph()
@@ -367,7 +401,7 @@ def bench_batched(args):
     L = native.lib()
     max_n = int(np.max(np.diff(b.ray_offsets)))
     size = C.c_size_t()
-    L.rdn_paths_scratch_size(max_n, 4, C.byref(size))
+    L.rdn_paths_scratch_size(max_n, 4, 0, C.byref(size))
     scratch = torch.empty(size.value + 256, dtype=torch.uint8, device="cuda")
     sptr = (scratch.data_ptr() + 255) & ~255
     out = torch.empty((b.rays.shape[0], 2), dtype=torch.float32, device="cuda")
@@ -409,6 +443,7 @@ def bench_batched(args):
         "speedup_vs_plain_loop": round(plain_ms / batched_ms, 3),
         "host_build_s": round(build_s, 2),
         "escaped_fraction": round(float(np.mean(res_batched["depth_flags"] >> 31)), 4),
+        "autotuned": tuned,
     }
 
 
@@ -564,6 +599,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-tune", dest="tune", action="store_false", help="skip the launch autotuner")
     ap.add_argument("--scenes", type=int, default=256)
     ap.add_argument("--batched-steps", type=int, default=5)
     args = ap.parse_args()

@@ -334,14 +334,19 @@ typedef struct rdn_path_desc {
   uint32_t seed;
   uint32_t traversal;           /* RDN_TRAVERSAL_* */
   uint32_t block_size;          /* 0 = 64 */
-  uint32_t reserved;
+  uint32_t sort_key;            /* RDN_SORT_*: regroup each bounce's rays before tracing */
   rdn_path_result* out;         /* device, count entries */
   void* scratch;                /* device, >= rdn_paths_scratch_size() bytes, 256-byte aligned */
   size_t scratch_bytes;
   uint32_t* segment_counts;     /* device, nullable: rays traced per bounce (max_bounces + 1) */
 } rdn_path_desc;
 
-rdn_status rdn_paths_scratch_size(uint32_t count, uint32_t max_bounces, size_t* bytes);
+/* Ray-sort keys (stable radix sort of each queue before its bounce). */
+#define RDN_SORT_NONE 0u
+#define RDN_SORT_SCENE_OCTANT 1u        /* (TLAS index, direction octant) */
+#define RDN_SORT_SCENE_OCTANT_CELL 2u   /* ... plus a 12-bit Morton cell of the origin in the scene box */
+
+rdn_status rdn_paths_scratch_size(uint32_t count, uint32_t max_bounces, uint32_t sort_key, size_t* bytes);
 
 /* Stream-ordered: one counter reset and max_bounces + 1 persistent launches;
  * queue sizes stay on the device (no host synchronisation). Replaces the

@@ -115,10 +115,18 @@ __global__ void zero_tail(uint32_t* __restrict__ out, uint32_t n, const uint32_t
 }
 
 // digit histogram of one tile, written digit-major: hist[d * tiles + tile]
-__global__ void __launch_bounds__(SORT_THREADS) sort_histogram(const uint32_t* __restrict__ keys, uint32_t n,
-                                                               uint32_t shift, uint32_t* __restrict__ hist,
-                                                               uint32_t tiles) {
+// n_dev (nullable): the element count lives on the device; n is the capacity
+__device__ __forceinline__ uint32_t live_count(uint32_t n, const uint32_t* n_dev) {
+  if (!n_dev) return n;
+  const uint32_t d = *n_dev;
+  return d < n ? d : n;
+}
+
+__global__ void __launch_bounds__(SORT_THREADS) sort_histogram(const uint32_t* __restrict__ keys, uint32_t n_cap,
+                                                               const uint32_t* __restrict__ n_dev, uint32_t shift,
+                                                               uint32_t* __restrict__ hist, uint32_t tiles) {
   __shared__ uint32_t h[256];
+  const uint32_t n = live_count(n_cap, n_dev);
   h[threadIdx.x] = 0u;
   __syncthreads();
   const size_t base = (size_t)blockIdx.x * SORT_TILE;
@@ -134,10 +142,11 @@ __global__ void __launch_bounds__(SORT_THREADS) sort_histogram(const uint32_t* _
 __global__ void __launch_bounds__(SORT_THREADS) sort_scatter(const uint32_t* __restrict__ keys_in,
                                                              const uint32_t* __restrict__ vals_in,
                                                              uint32_t* __restrict__ keys_out,
-                                                             uint32_t* __restrict__ vals_out, uint32_t n,
-                                                             uint32_t shift, const uint32_t* __restrict__ offsets,
-                                                             uint32_t tiles) {
+                                                             uint32_t* __restrict__ vals_out, uint32_t n_cap,
+                                                             const uint32_t* __restrict__ n_dev, uint32_t shift,
+                                                             const uint32_t* __restrict__ offsets, uint32_t tiles) {
   constexpr uint32_t WARPS = SORT_THREADS / 32;
+  const uint32_t n = live_count(n_cap, n_dev);
   __shared__ uint32_t run[256];          // running position of each digit in this tile
   __shared__ uint32_t wcount[WARPS][256];  // per-warp digit counts of the current round
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
@@ -245,7 +254,7 @@ size_t sort_scratch_bytes(uint32_t n) {
 }
 
 cudaError_t radix_sort_u32(uint32_t* keys, uint32_t* vals, uint32_t n, uint32_t key_bits, void* scratch,
-                           cudaStream_t stream) {
+                           cudaStream_t stream, const uint32_t* n_dev) {
   if (n <= 1) return cudaSuccess;
   const uint32_t tiles = (n + SORT_TILE - 1) / SORT_TILE;
   const uint32_t hist_n = tiles * 256;
@@ -265,12 +274,12 @@ cudaError_t radix_sort_u32(uint32_t* keys, uint32_t* vals, uint32_t n, uint32_t 
   const uint32_t passes = (key_bits + 7) / 8;
   for (uint32_t pass = 0; pass < passes; pass++) {
     const uint32_t shift = 8 * pass;
-    sort_histogram<<<tiles, SORT_THREADS, 0, stream>>>(k_src, n, shift, hist, tiles);
+    sort_histogram<<<tiles, SORT_THREADS, 0, stream>>>(k_src, n, n_dev, shift, hist, tiles);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     e = scan_u32(hist, offs, hist_n, false, 0, s, stream, false);
     if (e != cudaSuccess) return e;
-    sort_scatter<<<tiles, SORT_THREADS, 0, stream>>>(k_src, v_src, k_dst, v_dst, n, shift, offs, tiles);
+    sort_scatter<<<tiles, SORT_THREADS, 0, stream>>>(k_src, v_src, k_dst, v_dst, n, n_dev, shift, offs, tiles);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     uint32_t* t = k_src;
@@ -281,6 +290,7 @@ cudaError_t radix_sort_u32(uint32_t* keys, uint32_t* vals, uint32_t n, uint32_t 
     v_dst = vals ? t : nullptr;
   }
   if (k_src != keys) {
+    // with a device-side count the copy covers the capacity (entries past the count are don't-care)
     cudaError_t e = cudaMemcpyAsync(keys, k_src, (size_t)n * 4, cudaMemcpyDeviceToDevice, stream);
     if (e != cudaSuccess) return e;
     if (vals) e = cudaMemcpyAsync(vals, v_src, (size_t)n * 4, cudaMemcpyDeviceToDevice, stream);

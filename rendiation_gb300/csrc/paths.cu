@@ -23,6 +23,7 @@
 
 #include <cstdint>
 
+#include "parallel.h"
 #include "paths.h"
 #include "shade.cuh"
 #include "traverse.cuh"
@@ -32,15 +33,16 @@ namespace {
 
 using namespace dev;
 
+// Queue of bounce b: rays (2 float4) and states {id, tlas, throughput, 0}.
+// from_user: bounce 0 reads the caller's primary rays instead of a queue.
 template <int MODE>
-__global__ void __launch_bounds__(128) path_kernel(TraceParams p, PathParams q, uint32_t bounce) {
+__global__ void __launch_bounds__(128) path_kernel(TraceParams p, PathParams q, uint32_t bounce, bool from_user,
+                                                   const float4* __restrict__ in_rays,
+                                                   const uint4* __restrict__ in_state, float4* __restrict__ out_rays,
+                                                   uint4* __restrict__ out_state) {
   extern __shared__ uint2 smem_stack[];
   const uint32_t n = bounce == 0 ? q.count : *(volatile uint32_t*)(q.queue_count + bounce - 1);
   const uint32_t lane = threadIdx.x & 31u;
-  const float4* in_rays = reinterpret_cast<const float4*>(bounce & 1 ? q.rays_b : q.rays_a);
-  const uint4* in_state = reinterpret_cast<const uint4*>(bounce & 1 ? q.state_b : q.state_a);
-  float4* out_rays = reinterpret_cast<float4*>(bounce & 1 ? q.rays_a : q.rays_b);
-  uint4* out_state = reinterpret_cast<uint4*>(bounce & 1 ? q.state_a : q.state_b);
   uint32_t* work = q.work_counter + bounce;
   for (;;) {
     uint32_t base = 0;
@@ -55,7 +57,7 @@ __global__ void __launch_bounds__(128) path_kernel(TraceParams p, PathParams q, 
       float4 r0, r1;
       uint32_t id, tlas;
       float throughput;
-      if (bounce == 0) {
+      if (from_user) {
         const float4* rp = q.primary_rays + 2 * (size_t)j;
         r0 = __ldg(rp);
         r1 = __ldg(rp + 1);
@@ -118,12 +120,73 @@ __global__ void __launch_bounds__(128) path_kernel(TraceParams p, PathParams q, 
   if (blockIdx.x == 0 && threadIdx.x == 0 && q.segment_counts) q.segment_counts[bounce] = n;
 }
 
+// Primary rays into queue form (only when the executor sorts rays).
+__global__ void path_prime_kernel(PathParams q, float4* __restrict__ rays, uint4* __restrict__ state) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= q.count) return;
+  rays[2 * (size_t)i] = __ldg(q.primary_rays + 2 * (size_t)i);
+  rays[2 * (size_t)i + 1] = __ldg(q.primary_rays + 2 * (size_t)i + 1);
+  state[i] = make_uint4(i, q.tlas_idx ? __ldg(q.tlas_idx + i) : q.tlas_uniform, __float_as_uint(1.0f), 0u);
+}
+
+__device__ __forceinline__ uint32_t spread4(uint32_t v) {  // 4 bits -> every third bit
+  return (v & 1u) | ((v & 2u) << 2) | ((v & 4u) << 4) | ((v & 8u) << 6);
+}
+
+// Sort key of queue entry i (entries at or past the live count are skipped).
+__global__ void path_key_kernel(TraceParams p, PathParams q, const float4* __restrict__ rays,
+                                const uint4* __restrict__ state, const uint32_t* __restrict__ n_dev) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t n = n_dev ? *n_dev : q.count;
+  if (i >= n) return;
+  const float4 r0 = rays[2 * (size_t)i], r1 = rays[2 * (size_t)i + 1];
+  const uint32_t tlas = state[i].y;
+  const uint32_t oct = (r1.x < 0.0f ? 1u : 0u) | (r1.y < 0.0f ? 2u : 0u) | (r1.z < 0.0f ? 4u : 0u);
+  uint32_t key = (tlas << 3) | oct;
+  if (q.sort_key == 2) {
+    uint32_t cell = 0;
+    if (tlas < p.n_binding) {
+      const uint32_t h = __ldg(p.tlas_binding + tlas);
+      const uint32_t root = h < p.n_tlas_root ? __ldg(p.tlas_bvh_root + h) : INVALID_NEXT;
+      if (root != INVALID_NEXT) {
+        const float* b = reinterpret_cast<const float*>(p.tlas_forest + root);
+        const float lo[3] = {__ldg(b), __ldg(b + 1), __ldg(b + 2)}, hi[3] = {__ldg(b + 4), __ldg(b + 5), __ldg(b + 6)};
+        const float o[3] = {r0.x, r0.y, r0.z};
+        uint32_t c[3];
+        for (int a = 0; a < 3; a++) {
+          const float ext = hi[a] - lo[a];
+          const float f = ext > 0.0f ? (o[a] - lo[a]) / ext * 16.0f : 0.0f;
+          c[a] = f <= 0.0f ? 0u : (f >= 15.0f ? 15u : (uint32_t)f);
+        }
+        cell = spread4(c[0]) | (spread4(c[1]) << 1) | (spread4(c[2]) << 2);
+      }
+    }
+    key = (key << 12) | cell;
+  }
+  q.keys[i] = key;
+  q.idx[i] = i;
+}
+
+__global__ void path_gather_kernel(PathParams q, const float4* __restrict__ in_rays, const uint4* __restrict__ in_state,
+                                   float4* __restrict__ out_rays, uint4* __restrict__ out_state,
+                                   const uint32_t* __restrict__ n_dev) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t n = n_dev ? *n_dev : q.count;
+  if (i >= n) return;
+  const uint32_t j = q.idx[i];
+  out_rays[2 * (size_t)i] = in_rays[2 * (size_t)j];
+  out_rays[2 * (size_t)i + 1] = in_rays[2 * (size_t)j + 1];
+  out_state[i] = in_state[j];
+}
+
 }  // namespace
 
-size_t paths_scratch_bytes(uint32_t count, uint32_t max_bounces) {
+size_t paths_scratch_bytes(uint32_t count, uint32_t max_bounces, uint32_t sort_key) {
   auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
   const size_t n = count;
-  return 256 + up(sizeof(uint32_t) * 2 * (max_bounces + 1)) + 2 * up(n * 32) + 2 * up(n * 16);
+  size_t bytes = 256 + up(sizeof(uint32_t) * 2 * (max_bounces + 1)) + 2 * up(n * 32) + 2 * up(n * 16);
+  if (sort_key) bytes += 2 * up(n * 4) + sort_scratch_bytes(count);
+  return bytes;
 }
 
 void paths_bind_scratch(PathParams& q, void* scratch) {
@@ -140,6 +203,14 @@ void paths_bind_scratch(PathParams& q, void* scratch) {
   q.state_a = s + off;
   off += up(n * 16);
   q.state_b = s + off;
+  off += up(n * 16);
+  if (q.sort_key) {
+    q.keys = reinterpret_cast<uint32_t*>(s + off);
+    off += up(n * 4);
+    q.idx = reinterpret_cast<uint32_t*>(s + off);
+    off += up(n * 4);
+    q.sort_scratch = s + off;
+  }
 }
 
 namespace {
@@ -179,10 +250,46 @@ cudaError_t record_paths(const TraceParams& p, const PathParams& q, int mode, ui
   const size_t smem = mode != MODE_THREADED ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
   cudaError_t e = cudaMemsetAsync(q.queue_count, 0, sizeof(uint32_t) * 2 * (q.max_bounces + 1), stream);
   if (e != cudaSuccess) return e;
+  float4* ra = static_cast<float4*>(q.rays_a);
+  float4* rb = static_cast<float4*>(q.rays_b);
+  uint4* sa = static_cast<uint4*>(q.state_a);
+  uint4* sb = static_cast<uint4*>(q.state_b);
+  const uint32_t eg = (q.count + 255) / 256;
+  if (q.sort_key) {
+    path_prime_kernel<<<eg, 256, 0, stream>>>(q, ra, sa);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
   for (uint32_t b = 0; b <= q.max_bounces; b++) {
-    if (mode == MODE_WIDE4) path_kernel<MODE_WIDE4><<<grid, block, smem, stream>>>(p, q, b);
-    else if (mode == MODE_BINARY) path_kernel<MODE_BINARY><<<grid, block, smem, stream>>>(p, q, b);
-    else path_kernel<MODE_THREADED><<<grid, block, smem, stream>>>(p, q, b);
+    const float4* in_r;
+    const uint4* in_s;
+    float4* out_r;
+    uint4* out_s;
+    bool from_user = false;
+    if (q.sort_key) {
+      // regroup the queue in A by key into B, trace B, append to A
+      const uint32_t* n_dev = b == 0 ? nullptr : q.queue_count + b - 1;
+      path_key_kernel<<<eg, 256, 0, stream>>>(p, q, ra, sa, n_dev);
+      e = cudaGetLastError();
+      if (e == cudaSuccess) e = radix_sort_u32(q.keys, q.idx, q.count, q.key_bits, q.sort_scratch, stream, n_dev);
+      if (e != cudaSuccess) return e;
+      path_gather_kernel<<<eg, 256, 0, stream>>>(q, ra, sa, rb, sb, n_dev);
+      e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+      in_r = rb;
+      in_s = sb;
+      out_r = ra;
+      out_s = sa;
+    } else {
+      from_user = b == 0;
+      in_r = (b & 1) ? rb : ra;
+      in_s = (b & 1) ? sb : sa;
+      out_r = (b & 1) ? ra : rb;
+      out_s = (b & 1) ? sa : sb;
+    }
+    if (mode == MODE_WIDE4) path_kernel<MODE_WIDE4><<<grid, block, smem, stream>>>(p, q, b, from_user, in_r, in_s, out_r, out_s);
+    else if (mode == MODE_BINARY) path_kernel<MODE_BINARY><<<grid, block, smem, stream>>>(p, q, b, from_user, in_r, in_s, out_r, out_s);
+    else path_kernel<MODE_THREADED><<<grid, block, smem, stream>>>(p, q, b, from_user, in_r, in_s, out_r, out_s);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }

@@ -22,9 +22,17 @@ struct PathParams {
   void* rays_b;
   void* state_a;
   void* state_b;
+  // ray regrouping between bounces (sort_key != 0)
+  uint32_t sort_key, key_bits;
+  uint32_t* keys;
+  uint32_t* idx;
+  void* sort_scratch;
 };
 
-size_t paths_scratch_bytes(uint32_t count, uint32_t max_bounces);
+// Ray-sort keys: 0 none; 1 (scene, direction octant); 2 (scene, octant, 12-bit
+// Morton code of the origin inside the scene's root box).
+size_t paths_scratch_bytes(uint32_t count, uint32_t max_bounces, uint32_t sort_key);
+
 void paths_bind_scratch(PathParams& q, void* scratch);
 // Sets the kernel attributes and returns the persistent grid (not stream-ordered:
 // call before any capture).

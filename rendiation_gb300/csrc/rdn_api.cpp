@@ -2,6 +2,7 @@
 // (GPUAccelerationStructureSystemProvider, shader/ray-tracing/src/api/backend.rs:120-142,
 // implemented by NaiveSahBVHSystem, .../geometry/naive/mod.rs:496-609) and the
 // batch trace entry points.
+#include <algorithm>
 #include <chrono>
 #include <cstring>
 #include <exception>
@@ -492,7 +493,8 @@ rdn_status prepare_path_launch(rdn_ctx* c, const rdn_path_desc* d, rdn::TracePar
   if (c->device < 0) return fail(c, RDN_ERR_UNSUPPORTED, "host-only context cannot trace");
   if (d->max_bounces > 16) return fail(c, RDN_ERR_INVALID_ARG, "max_bounces above 16");
   if (d->count && (!d->rays || !d->out || !d->scratch)) return fail(c, RDN_ERR_INVALID_ARG, "null buffer");
-  if (d->scratch_bytes < rdn::paths_scratch_bytes(d->count, d->max_bounces))
+  if (d->sort_key > 2) return fail(c, RDN_ERR_INVALID_ARG, "unknown sort key");
+  if (d->scratch_bytes < rdn::paths_scratch_bytes(d->count, d->max_bounces, d->sort_key))
     return fail(c, RDN_ERR_INVALID_ARG, "scratch too small");
   if ((reinterpret_cast<uintptr_t>(d->scratch) & 255) || (reinterpret_cast<uintptr_t>(d->rays) & 15) ||
       (reinterpret_cast<uintptr_t>(d->out) & 7))
@@ -521,6 +523,14 @@ rdn_status prepare_path_launch(rdn_ctx* c, const rdn_path_desc* d, rdn::TracePar
   q.rr_survive = d->rr_survive;
   q.out = reinterpret_cast<float2*>(d->out);
   q.segment_counts = d->segment_counts;
+  q.sort_key = d->sort_key;
+  if (d->sort_key) {
+    uint32_t bits = 0;
+    while (bits < 32 && (1ull << bits) < (uint64_t)std::max<size_t>(1, c->dev.tlas_binding.count)) bits++;
+    bits += 3 + (d->sort_key == 2 ? 12 : 0);
+    if (bits > 32) return fail(c, RDN_ERR_INVALID_ARG, "too many bound TLASes for this sort key");
+    q.key_bits = bits;
+  }
   if (d->count) rdn::paths_bind_scratch(q, d->scratch);
   cudaError_t e = cudaSetDevice(c->device);
   if (e == cudaSuccess && d->count)
@@ -533,9 +543,9 @@ rdn_status prepare_path_launch(rdn_ctx* c, const rdn_path_desc* d, rdn::TracePar
 
 extern "C" {
 
-rdn_status rdn_paths_scratch_size(uint32_t count, uint32_t max_bounces, size_t* bytes) {
-  if (!bytes || max_bounces > 16) return RDN_ERR_INVALID_ARG;
-  *bytes = rdn::paths_scratch_bytes(count, max_bounces);
+rdn_status rdn_paths_scratch_size(uint32_t count, uint32_t max_bounces, uint32_t sort_key, size_t* bytes) {
+  if (!bytes || max_bounces > 16 || sort_key > 2) return RDN_ERR_INVALID_ARG;
+  *bytes = rdn::paths_scratch_bytes(count, max_bounces, sort_key);
   return RDN_OK;
 }
 

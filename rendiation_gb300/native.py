@@ -87,7 +87,7 @@ class PathDesc(C.Structure):
     _fields_ = [("rays", C.c_void_p), ("tlas_idx", C.c_void_p), ("count", C.c_uint32), ("tlas_uniform", C.c_uint32),
                 ("max_bounces", C.c_uint32), ("rr_start", C.c_uint32), ("albedo", C.c_float),
                 ("rr_survive", C.c_float), ("seed", C.c_uint32), ("traversal", C.c_uint32),
-                ("block_size", C.c_uint32), ("reserved", C.c_uint32), ("out", C.c_void_p), ("scratch", C.c_void_p),
+                ("block_size", C.c_uint32), ("sort_key", C.c_uint32), ("out", C.c_void_p), ("scratch", C.c_void_p),
                 ("scratch_bytes", C.c_size_t), ("segment_counts", C.c_void_p)]
 
 
@@ -144,7 +144,7 @@ def lib() -> C.CDLL:
     L.rdn_wavefront_shadow_bounce.restype = i32
     L.rdn_wavefront_shadow_bounce_static.argtypes = [vp, C.POINTER(WavefrontDesc), vp]
     L.rdn_wavefront_shadow_bounce_static.restype = i32
-    L.rdn_paths_scratch_size.argtypes = [u32, u32, C.POINTER(C.c_size_t)]
+    L.rdn_paths_scratch_size.argtypes = [u32, u32, u32, C.POINTER(C.c_size_t)]
     L.rdn_paths_scratch_size.restype = i32
     L.rdn_trace_paths.argtypes = [vp, C.POINTER(PathDesc), vp]
     L.rdn_trace_paths.restype = i32

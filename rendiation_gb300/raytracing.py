@@ -40,6 +40,9 @@ MISS = 0xFFFFFFFF
 TRAVERSAL_ORDERED = 0
 TRAVERSAL_REFERENCE = 1
 TRAVERSAL_ORDERED_WIDE = 2
+SORT_NONE = 0
+SORT_SCENE_OCTANT = 1
+SORT_SCENE_OCTANT_CELL = 2
 ANYHIT_ACCEPT = 0
 ANYHIT_ACCEPT_AND_END = 1
 ANYHIT_ACCEPT_EVEN_PRIMS = 2
@@ -251,16 +254,34 @@ class Wavefront:
         self.desc.scratch = self.scratch_ptr
         self.desc.scratch_bytes = size.value
         self.desc.ray_counts = self.ray_counts.data_ptr()
+        self.phase_config = None  # (primary, secondary) (traversal, block) when they differ
+
+    def configure(self, primary, secondary):
+        """Per-kernel (traversal, block_size); a frame then issues one call per kernel."""
+        if tuple(primary) == tuple(secondary):
+            self.desc.traversal, self.desc.block_size = primary
+            self.phase_config = None
+        else:
+            self.phase_config = (tuple(primary), tuple(secondary))
 
     def run(self, sample_index=0, stream=None, phases=0):
         """phases: 0 both kernels, 1 primary only, 2 secondary only (queues of the last primary run)."""
         import torch
 
         self.desc.sample_index = sample_index
-        self.desc.phases = phases
         s = (stream or torch.cuda.current_stream()).cuda_stream
-        _check(self.system._h, self.system._L.rdn_wavefront_shadow_bounce(self.system._h, C.byref(self.desc),
-                                                                          C.c_void_p(s)))
+        if self.phase_config is None:
+            self.desc.phases = phases
+            _check(self.system._h, self.system._L.rdn_wavefront_shadow_bounce(self.system._h, C.byref(self.desc),
+                                                                              C.c_void_p(s)))
+            return
+        for ph, (trav, block) in zip((1, 2), self.phase_config):
+            if phases and phases != ph:
+                continue
+            self.desc.phases = ph
+            self.desc.traversal, self.desc.block_size = trav, block
+            _check(self.system._h, self.system._L.rdn_wavefront_shadow_bounce(self.system._h, C.byref(self.desc),
+                                                                              C.c_void_p(s)))
 
     def results(self) -> np.ndarray:
         return self.out.cpu().numpy().view(PIXEL_DTYPE).reshape(-1)
@@ -280,7 +301,8 @@ class Paths:
     carries its index into the bound TLAS list. Buffers are torch CUDA tensors."""
 
     def __init__(self, system: AccelerationStructureSystem, rays, tlas_idx=None, tlas_uniform=0, max_bounces=4,
-                 rr_start=2, albedo=0.5, rr_survive=0.5, seed=0, traversal=TRAVERSAL_ORDERED, block_size=0):
+                 rr_start=2, albedo=0.5, rr_survive=0.5, seed=0, traversal=TRAVERSAL_ORDERED, block_size=0,
+                 sort_key=0):
         import torch
 
         self.system = system
@@ -290,15 +312,36 @@ class Paths:
         self.n = n
         self.max_bounces = max_bounces
         size = C.c_size_t()
-        _check(None, system._L.rdn_paths_scratch_size(n, max_bounces, C.byref(size)))
+        _check(None, system._L.rdn_paths_scratch_size(n, max_bounces, sort_key, C.byref(size)))
         self.scratch = torch.empty(size.value + 256, dtype=torch.uint8, device="cuda")
         self.scratch_ptr = (self.scratch.data_ptr() + 255) & ~255
         self.out = torch.empty((max(n, 1), 2), dtype=torch.float32, device="cuda")
         self.segments_dev = torch.zeros(max_bounces + 1, dtype=torch.int32, device="cuda")
         self.desc = native.PathDesc(rays.data_ptr(), 0 if tlas_idx is None else tlas_idx.data_ptr(), n, tlas_uniform,
-                                    max_bounces, rr_start, albedo, rr_survive, seed, traversal, block_size, 0,
+                                    max_bounces, rr_start, albedo, rr_survive, seed, traversal, block_size, sort_key,
                                     self.out.data_ptr(), self.scratch_ptr, size.value, self.segments_dev.data_ptr())
         self.graph = None
+        self.scratch_bytes = size.value
+
+    def configure(self, traversal=None, block_size=None, sort_key=None):
+        """Changes launch knobs (re-capture any graph afterwards)."""
+        import torch
+
+        if sort_key is not None and sort_key != self.desc.sort_key:
+            size = C.c_size_t()
+            _check(None, self.system._L.rdn_paths_scratch_size(self.n, self.max_bounces, sort_key, C.byref(size)))
+            if size.value > self.scratch_bytes:
+                self.scratch = torch.empty(size.value + 256, dtype=torch.uint8, device="cuda")
+                self.scratch_ptr = (self.scratch.data_ptr() + 255) & ~255
+                self.scratch_bytes = size.value
+                self.desc.scratch = self.scratch_ptr
+            self.desc.scratch_bytes = self.scratch_bytes
+            self.desc.sort_key = sort_key
+        if traversal is not None:
+            self.desc.traversal = traversal
+        if block_size is not None:
+            self.desc.block_size = block_size
+        self.close()
 
     def run(self, stream=None):
         import torch

@@ -65,6 +65,20 @@ def test_paths_ordered_matches_except_ties(batched, cuda):
     assert same.mean() > 0.999, same.mean()
 
 
+@pytest.mark.parametrize("sort_key", [rt.SORT_SCENE_OCTANT, rt.SORT_SCENE_OCTANT_CELL])
+def test_paths_sorted_queues_same_results(batched, sort_key, cuda):
+    """Regrouping the queues by key changes only the order rays are traced in."""
+    b, S, P = batched
+    exp, seg, _ = orc.trace_paths(S, b.rays, b.tlas_idx, max_bounces=4, rr_start=2, seed=11, threads=4)
+    got, gseg, _ = product_paths(P, b, rt.TRAVERSAL_REFERENCE, seed=11, sort_key=sort_key)
+    assert gseg == seg
+    assert np.array_equal(got["depth_flags"], exp["depth_flags"])
+    assert np.array_equal(got["radiance"].view(np.uint32), exp["radiance"].view(np.uint32))
+    got2, _, first = product_paths(P, b, rt.TRAVERSAL_REFERENCE, graph=True, seed=11, sort_key=sort_key)
+    assert np.array_equal(got2["depth_flags"], exp["depth_flags"])
+    assert np.array_equal(first["depth_flags"], exp["depth_flags"])
+
+
 def test_paths_no_roulette_no_bounce(batched, cuda):
     b, S, P = batched
     exp, seg, _ = orc.trace_paths(S, b.rays, b.tlas_idx, max_bounces=0, rr_start=99, seed=1, threads=4)
