@@ -397,6 +397,43 @@ rdn_status rdn_attr_loss_forward(rdn_ctx* ctx, const rdn_attr_loss_desc* desc, v
  * (object space of the hit instance). */
 rdn_status rdn_attr_loss_adjoint(rdn_ctx* ctx, const rdn_attr_loss_desc* desc, void* stream);
 
+/* Differentiable paths over many scenes: every path is a primary ray (with its
+ * own index into the bound TLAS list) followed by up to segments-1 cosine
+ * bounces generated like rdn_trace_paths's (facing normal, offset_ray_hit
+ * origin, sampler xxhash32(path, segment, seed), no roulette). Each segment's
+ * hit adds (value - target)^2 with the attribute interpolation above; a
+ * missed segment (and every later one) has value 0. The adjoint recomputes all
+ * hits by tracing each path again and treats each segment's ray as fixed:
+ * gradients flow to the vertices of every hit triangle, not through the bounce
+ * directions. */
+typedef struct rdn_attr_path_desc {
+  const rdn_ray* rays;          /* device, one primary ray per path */
+  const uint32_t* tlas_idx;     /* device, nullable: per-path TLAS index */
+  uint32_t count;
+  uint32_t tlas_uniform;
+  uint32_t segments;            /* 1..8: primary + bounces */
+  uint32_t seed;
+  const float* attributes;      /* device, one per built vertex */
+  const float* targets;         /* device, segments per path; NULL = 0 */
+  float* values;                /* device, nullable: segments per path (forward) */
+  double* loss_sum;             /* device, nullable: loss added here (forward) */
+  float* grad_vertices;         /* device, 4 per built vertex, accumulated (adjoint) */
+  uint32_t* seg_tri;            /* device, nullable: built triangle index of each segment's hit, RDN_MISS (forward) */
+  rdn_ray* seg_rays;            /* device, nullable: the ray of each segment (forward) */
+  float grad_scale;
+  uint32_t traversal;
+  uint32_t block_size;          /* 0 = 64 */
+  uint32_t reserved;
+} rdn_attr_path_desc;
+
+rdn_status rdn_attr_paths_forward(rdn_ctx* ctx, const rdn_attr_path_desc* desc, void* stream);
+rdn_status rdn_attr_paths_adjoint(rdn_ctx* ctx, const rdn_attr_path_desc* desc, void* stream);
+/* Forward and adjoint captured once into one executable CUDA graph; each
+ * launch zeroes *loss_sum and the gradient buffer (num_vertices entries of 4
+ * floats) first. */
+rdn_status rdn_attr_paths_graph(rdn_ctx* ctx, const rdn_attr_path_desc* desc, uint64_t num_vertices,
+                                rdn_graph** out);
+
 /* ---- parallel primitives (shader/parallel-compute) ---------------------
  * Stateless, on the calling thread's current device, stream-ordered. Scratch
  * is caller-owned device memory of at least the queried size, 256-byte aligned. */

@@ -72,6 +72,7 @@ def lib():
         L.orc_select_nth.argtypes = [vp, vp, C.c_size_t, C.c_size_t]
         L.orc_trace_paths.argtypes = [vp, vp, u32, vp, u32, u32, u32, C.c_float, C.c_float, u32, vp, vp, i32,
                                       C.POINTER(C.c_double)]
+        L.orc_path_segments.argtypes = [vp, vp, u32, vp, u32, u32, u32, vp, vp, i32]
         L.orc_wavefront_shadow_bounce.argtypes = [vp, vp, u32, u32, vp, u32, u32, u32, u32, vp, vp, i32,
                                                   C.POINTER(C.c_double)]
         _lib = L
@@ -226,6 +227,18 @@ def trace_paths(system: OracleSystem, rays, tlas_idx=None, tlas_uniform=0, max_b
     system._check(system._L.orc_trace_paths(system._h, _ptr(rays), n, _ptr(ti), tlas_uniform, max_bounces, rr_start,
                                             albedo, rr_survive, seed, _ptr(out), _ptr(seg), threads, C.byref(sec)))
     return out, [int(x) for x in seg], sec.value
+
+
+def path_segments(system: OracleSystem, rays, tlas_idx=None, tlas_uniform=0, segments=3, seed=0, threads=1):
+    """Per-segment rays and hit triangles of differentiable paths (seg_tri ~0 = miss)."""
+    rays = np.ascontiguousarray(rays)
+    n = rays.shape[0]
+    seg_rays = np.zeros(n * segments, rays.dtype)
+    seg_tri = np.zeros(n * segments, np.uint32)
+    ti = None if tlas_idx is None else np.ascontiguousarray(tlas_idx, np.uint32)
+    system._check(system._L.orc_path_segments(system._h, _ptr(rays), n, _ptr(ti), tlas_uniform, segments, seed,
+                                              _ptr(seg_rays), _ptr(seg_tri), threads))
+    return seg_rays, seg_tri
 
 
 def intersect_triangle(o, d, near, far, v0, v1, v2, cull_enable=False, cull_back=False):

@@ -1295,4 +1295,61 @@ int orc_trace_paths(void* cp, const RayIn* rays, uint32_t n, const uint32_t* tla
   return 0;
 }
 
+
+// Segment rays and hit triangles of differentiable paths: a primary ray per
+// path followed by up to segments-1 cosine bounces (no roulette), generated as
+// in path_one. seg_rays: 32 B per segment (untouched after a miss); seg_tri:
+// built triangle index per segment or ~0.
+int orc_path_segments(void* cp, const RayIn* rays, uint32_t n, const uint32_t* tlas_idx, uint32_t tlas_uniform,
+                      uint32_t segments, uint32_t seed, RayIn* seg_rays, uint32_t* seg_tri, int threads) {
+  Ctx& c = *(Ctx*)cp;
+  if (!c.built) {
+    int rc = build_all(c);
+    if (rc) return rc;
+  }
+  const Built& B = *c.built;
+  if (threads < 1) threads = 1;
+  std::vector<Counters> cn(threads);
+  std::atomic<uint32_t> next{0};
+  auto work = [&](int w) {
+    for (;;) {
+      uint32_t i = next.fetch_add(1);
+      if (i >= n) break;
+      RayIn r = rays[i];
+      uint32_t tlas = tlas_idx ? tlas_idx[i] : tlas_uniform;
+      bool alive = true;
+      for (uint32_t k = 0; k < segments; k++) {
+        size_t seg = (size_t)i * segments + k;
+        seg_tri[seg] = INVALID_NEXT;
+        if (!alive) continue;
+        seg_rays[seg] = r;
+        HitOut h;
+        uint32_t tri = 0;
+        traverse(B, r, tlas, 0, 0xFFu, 0, h, cn[w], nullptr, &tri);
+        if (h.prim == INVALID_NEXT) {
+          alive = false;
+          continue;
+        }
+        seg_tri[seg] = tri;
+        if (k + 1 < segments) {
+          uint32_t st = xxhash32(i, k, seed);
+          float s0 = sample_next(st);
+          float s1 = sample_next(st);
+          V3 d = ld3(r.dir);
+          V3 hp = ld3(r.org) + d * h.t;
+          V3 nn = world_normal(B, tri, h.instance);
+          V3 nf = dot(nn, d) < 0.0f ? nn : v3(-nn.x, -nn.y, -nn.z);
+          V3 org = offset_ray_hit(hp, nf);
+          V3 dir = cosine_sample_in_dir(nf, s0, s1);
+          r = RayIn{{org.x, org.y, org.z}, F32_EPSILON, {dir.x, dir.y, dir.z}, F32_MAX};
+        }
+      }
+    }
+  };
+  std::vector<std::thread> th;
+  for (int w = 0; w < threads; w++) th.emplace_back(work, w);
+  for (auto& t : th) t.join();
+  return 0;
+}
+
 }  // extern "C"

@@ -94,19 +94,20 @@ struct HitGeom {
 // v = det[-d, e1, s] / det M (Cramer), e1, e2, s formed exactly. Cramer's rule
 // does not depend on the length of d, so d is the object-space direction before
 // normalisation (exact for an identity instance).
-__device__ __forceinline__ HitGeom hit_vertices(const TraceParams& p, const AdjointParams& a, const RayCtx& R,
+__device__ __forceinline__ HitGeom hit_vertices(const TraceParams& p, const uint32_t* __restrict__ indices,
+                                                const float* __restrict__ vertices, const RayCtx& R,
                                                 const InstanceRay& ir) {
   HitGeom h;
   const uint32_t tri = __ldg(p.redirect + R.best.k);
-  h.i0 = __ldg(a.indices + 3 * (size_t)tri);
-  h.i1 = __ldg(a.indices + 3 * (size_t)tri + 1);
-  h.i2 = __ldg(a.indices + 3 * (size_t)tri + 2);
-  const float3 v0 = make_float3(__ldg(a.vertices + 3 * (size_t)h.i0), __ldg(a.vertices + 3 * (size_t)h.i0 + 1),
-                                __ldg(a.vertices + 3 * (size_t)h.i0 + 2));
-  const float3 v1 = make_float3(__ldg(a.vertices + 3 * (size_t)h.i1), __ldg(a.vertices + 3 * (size_t)h.i1 + 1),
-                                __ldg(a.vertices + 3 * (size_t)h.i1 + 2));
-  const float3 v2 = make_float3(__ldg(a.vertices + 3 * (size_t)h.i2), __ldg(a.vertices + 3 * (size_t)h.i2 + 1),
-                                __ldg(a.vertices + 3 * (size_t)h.i2 + 2));
+  h.i0 = __ldg(indices + 3 * (size_t)tri);
+  h.i1 = __ldg(indices + 3 * (size_t)tri + 1);
+  h.i2 = __ldg(indices + 3 * (size_t)tri + 2);
+  const float3 v0 = make_float3(__ldg(vertices + 3 * (size_t)h.i0), __ldg(vertices + 3 * (size_t)h.i0 + 1),
+                                __ldg(vertices + 3 * (size_t)h.i0 + 2));
+  const float3 v1 = make_float3(__ldg(vertices + 3 * (size_t)h.i1), __ldg(vertices + 3 * (size_t)h.i1 + 1),
+                                __ldg(vertices + 3 * (size_t)h.i1 + 2));
+  const float3 v2 = make_float3(__ldg(vertices + 3 * (size_t)h.i2), __ldg(vertices + 3 * (size_t)h.i2 + 1),
+                                __ldg(vertices + 3 * (size_t)h.i2 + 2));
   const ff3 E1 = ff3_sub(v1, v0), E2 = ff3_sub(v2, v0), S = ff3_sub(ir.o, v0);
   const float* m = p.tlas_data[R.best.inst].transform_inv;
   const float3 dobj = make_float3(R.d.x * __ldg(m + 0) + R.d.y * __ldg(m + 4) + R.d.z * __ldg(m + 8),
@@ -145,7 +146,7 @@ __global__ void __launch_bounds__(128) attr_forward_kernel(TraceParams p, Adjoin
     float value = 0.0f;
     if (R.best.have) {
       const InstanceRay ir = to_instance(p.tlas_data + R.best.inst, R.o, R.d, 0u);
-      const HitGeom h = hit_vertices(p, a, R, ir);
+      const HitGeom h = hit_vertices(p, a.indices, a.vertices, R, ir);
       value = h.w0 * __ldg(a.attributes + h.i0) + h.u * __ldg(a.attributes + h.i1) + h.v * __ldg(a.attributes + h.i2);
       const float diff = value - (a.targets ? __ldg(a.targets + i) : 0.0f);
       loss = diff * diff;
@@ -185,7 +186,7 @@ __global__ void __launch_bounds__(128) attr_adjoint_kernel(TraceParams p, Adjoin
   float3 go = make_float3(0.f, 0.f, 0.f), gd = go;
   if (R.best.have) {
     const InstanceRay ir = to_instance(p.tlas_data + R.best.inst, R.o, R.d, 0u);
-    const HitGeom h = hit_vertices(p, a, R, ir);
+    const HitGeom h = hit_vertices(p, a.indices, a.vertices, R, ir);
     const float a0 = __ldg(a.attributes + h.i0), a1 = __ldg(a.attributes + h.i1), a2 = __ldg(a.attributes + h.i2);
     const float value = h.w0 * a0 + h.u * a1 + h.v * a2;
     const float target = a.targets ? __ldg(a.targets + i) : 0.0f;
@@ -219,6 +220,136 @@ __global__ void __launch_bounds__(128) attr_adjoint_kernel(TraceParams p, Adjoin
   }
 }
 
+// lambda = M^{-T} (0, gu, gv) with M = [-d | e1 | e2] (d object space,
+// normalised), scattered to the three corners; returns lambda.
+__device__ __forceinline__ float3 scatter_vertex_grads(const HitGeom& h, const InstanceRay& ir, float r, float gu,
+                                                       float gv, float* grad_vertices) {
+  const float3 nd = make_float3(-ir.d.x, -ir.d.y, -ir.d.z);
+  const float3 c12 = cross3(h.e1, h.e2);
+  const float det = dot3(nd, c12);
+  const float3 b1 = cross3(h.e2, nd), b2 = cross3(nd, h.e1);
+  const float inv = 1.0f / det;
+  const float3 lam = make_float3((gu * b1.x + gv * b2.x) * inv, (gu * b1.y + gv * b2.y) * inv,
+                                 (gu * b1.z + gv * b2.z) * inv);
+  float4* g = reinterpret_cast<float4*>(grad_vertices);
+  atomicAdd(g + h.i0, make_float4(-h.w0 * lam.x, -h.w0 * lam.y, -h.w0 * lam.z, r * h.w0));
+  atomicAdd(g + h.i1, make_float4(-h.u * lam.x, -h.u * lam.y, -h.u * lam.z, r * h.u));
+  atomicAdd(g + h.i2, make_float4(-h.v * lam.x, -h.v * lam.y, -h.v * lam.z, r * h.v));
+  return lam;
+}
+
+// Persistent warps over paths; ADJOINT selects the gradient pass.
+template <int MODE, bool ADJOINT>
+__global__ void __launch_bounds__(128) attr_path_kernel(TraceParams p, PathAdjointParams a) {
+  extern __shared__ uint2 smem_stack[];
+  __shared__ double block_sum[4];
+  const uint32_t lane = threadIdx.x & 31u;
+  double loss_acc = 0.0;
+  for (;;) {
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(a.work_counter, 32u);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= a.count) break;
+    const uint32_t i = base + lane;
+    if (i >= a.count) continue;
+    const float4* rp = a.rays + 2 * (size_t)i;
+    float4 r0 = __ldg(rp), r1 = __ldg(rp + 1);
+    const uint32_t tlas = a.tlas_idx ? __ldg(a.tlas_idx + i) : a.tlas_uniform;
+    bool alive = true;
+    for (uint32_t k = 0; k < a.segments; k++) {
+      const size_t seg = (size_t)i * a.segments + k;
+      float value = 0.0f;
+      uint32_t tri_out = INVALID_NEXT;
+      if (alive) {
+        if (a.seg_rays) {
+          a.seg_rays[2 * seg] = r0;
+          a.seg_rays[2 * seg + 1] = r1;
+        }
+        RayCtx R;
+        R.o = make_float3(r0.x, r0.y, r0.z);
+        R.tmin = r0.w;
+        R.d = make_float3(r1.x, r1.y, r1.z);
+        R.tmax = r1.w;
+        R.cull_mask = 0xFFu;
+        R.ray_flags = 0u;
+        bool bad;
+        traverse_ray<MODE, false>(p, R, tlas, smem_stack + threadIdx.x, blockDim.x, bad);
+        if (!R.best.have) {
+          alive = false;
+        } else {
+          const InstanceRay ir = to_instance(p.tlas_data + R.best.inst, R.o, R.d, 0u);
+          const HitGeom h = hit_vertices(p, a.indices, a.vertices, R, ir);
+          tri_out = __ldg(p.redirect + R.best.k);
+          const float a0 = __ldg(a.attributes + h.i0), a1 = __ldg(a.attributes + h.i1),
+                      a2 = __ldg(a.attributes + h.i2);
+          value = h.w0 * a0 + h.u * a1 + h.v * a2;
+          const float target = a.targets ? __ldg(a.targets + seg) : 0.0f;
+          const float diff = value - target;
+          if (ADJOINT) {
+            const float r = 2.0f * diff * a.grad_scale;
+            scatter_vertex_grads(h, ir, r, r * (a1 - a0), r * (a2 - a0), a.grad_vertices);
+          } else {
+            loss_acc += (double)(diff * diff);
+          }
+          if (k + 1 < a.segments) {
+            uint32_t st = xxhash32(i, k, a.seed);
+            const float s0 = sample_next(st);
+            const float s1 = sample_next(st);
+            const float3 hp = R.o + R.d * R.best.t;
+            const float3 nf = facing_normal(p, R.best.k, R.best.inst, R.d);
+            const float3 org = offset_ray_hit(hp, nf);
+            const float3 dir = cosine_sample_in_dir(nf, s0, s1);
+            r0 = make_float4(org.x, org.y, org.z, 1.1920929e-7f);
+            r1 = make_float4(dir.x, dir.y, dir.z, 3.40282347e+38f);
+          }
+        }
+      } else if (!ADJOINT && a.targets) {
+        // a missed segment has value 0 against its target
+        const float t = __ldg(a.targets + seg);
+        loss_acc += (double)(t * t);
+      }
+      if (!ADJOINT && a.values) a.values[seg] = value;
+      if (!ADJOINT && a.seg_tri) a.seg_tri[seg] = tri_out;
+    }
+  }
+  if (!ADJOINT && a.loss_sum) {
+    double s = loss_acc;
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+    if ((threadIdx.x & 31) == 0) block_sum[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (uint32_t w = 0; w < (blockDim.x + 31) / 32; w++) t += block_sum[w];
+      atomicAdd(a.loss_sum, t);
+    }
+  }
+}
+
+template <int MODE>
+cudaError_t launch_attr_paths_mode(const TraceParams& p, const PathAdjointParams& a, bool adjoint, uint32_t block,
+                                   int sm_count, cudaStream_t stream) {
+  static bool done[2] = {false, false};
+  const void* fn = adjoint ? (const void*)attr_path_kernel<MODE, true> : (const void*)attr_path_kernel<MODE, false>;
+  if (!done[adjoint]) {
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e != cudaSuccess) return e;
+    done[adjoint] = true;
+  }
+  const size_t smem = MODE != MODE_THREADED ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (int)block, smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) per_sm = 1;
+  uint32_t grid = (uint32_t)(sm_count * per_sm);
+  const uint32_t need = (a.count + block - 1) / block;
+  if (grid > need) grid = need;
+  e = cudaMemsetAsync(a.work_counter, 0, 4, stream);
+  if (e != cudaSuccess) return e;
+  if (adjoint) attr_path_kernel<MODE, true><<<grid, block, smem, stream>>>(p, a);
+  else attr_path_kernel<MODE, false><<<grid, block, smem, stream>>>(p, a);
+  return cudaGetLastError();
+}
+
 template <int MODE>
 cudaError_t launch_attr_mode(const TraceParams& p, const AdjointParams& a, bool adjoint, uint32_t block,
                              cudaStream_t stream) {
@@ -248,6 +379,15 @@ cudaError_t launch_attr(const TraceParams& p, const AdjointParams& a, int mode, 
 }
 
 }  // namespace
+
+cudaError_t launch_attr_paths(const TraceParams& p, const PathAdjointParams& a, int mode, bool adjoint,
+                              uint32_t block, int sm_count, cudaStream_t stream) {
+  if (a.count == 0) return cudaSuccess;
+  if (block == 0) block = 64;
+  if (mode == MODE_WIDE4) return launch_attr_paths_mode<MODE_WIDE4>(p, a, adjoint, block, sm_count, stream);
+  if (mode == MODE_BINARY) return launch_attr_paths_mode<MODE_BINARY>(p, a, adjoint, block, sm_count, stream);
+  return launch_attr_paths_mode<MODE_THREADED>(p, a, adjoint, block, sm_count, stream);
+}
 
 cudaError_t launch_attr_forward(const TraceParams& p, const AdjointParams& a, int mode, uint32_t block,
                                 cudaStream_t stream) {

@@ -24,6 +24,32 @@ struct AdjointParams {
   float grad_scale;           // upstream gradient of the loss sum
 };
 
+// Multi-segment, multi-scene form: every path is a primary ray (its own TLAS
+// index) followed by up to segments-1 cosine bounces; each segment's hit adds
+// (value - target)^2. Bounce rays depend on the hit like the path executor's
+// (facing normal, offset origin, sampler xxhash32(id, k, seed)); the adjoint
+// treats each segment's ray as fixed (gradients do not flow through the bounce
+// directions) and recomputes every hit by tracing the path again.
+struct PathAdjointParams {
+  const float4* rays;         // 2 per path
+  const uint32_t* tlas_idx;   // per path, nullable
+  uint32_t count, tlas_uniform, segments, seed;
+  const uint32_t* indices;
+  const float* vertices;
+  const float* attributes;
+  const float* targets;       // segments per path, nullable (0)
+  float* values;              // segments per path, nullable
+  double* loss_sum;           // nullable
+  float* grad_vertices;       // 4 per vertex (adjoint)
+  uint32_t* seg_tri;          // segments per path, nullable: triangle index of each segment's hit (or ~0)
+  float4* seg_rays;           // 2 float4 per segment per path, nullable
+  float grad_scale;
+  uint32_t* work_counter;     // persistent work distribution (reset by the launcher)
+};
+
+cudaError_t launch_attr_paths(const TraceParams& p, const PathAdjointParams& a, int mode, bool adjoint,
+                              uint32_t block, int sm_count, cudaStream_t stream);
+
 cudaError_t launch_attr_forward(const TraceParams& p, const AdjointParams& a, int mode, uint32_t block,
                                 cudaStream_t stream);
 cudaError_t launch_attr_adjoint(const TraceParams& p, const AdjointParams& a, int mode, uint32_t block,

@@ -687,6 +687,137 @@ rdn_status rdn_attr_loss_adjoint(rdn_ctx* c, const rdn_attr_loss_desc* d, void* 
   return RDN_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+rdn_status prepare_attr_paths(rdn_ctx* c, const rdn_attr_path_desc* d, bool adjoint, rdn::TraceParams& p,
+                              rdn::PathAdjointParams& a) {
+  if (!c || !d) return fail(c, RDN_ERR_INVALID_ARG, "null context or descriptor");
+  if (c->device < 0) return fail(c, RDN_ERR_UNSUPPORTED, "host-only context cannot trace");
+  if (d->segments < 1 || d->segments > 8) return fail(c, RDN_ERR_INVALID_ARG, "segments must be 1..8");
+  if (d->count && (!d->rays || !d->attributes)) return fail(c, RDN_ERR_INVALID_ARG, "null rays or attributes");
+  if (adjoint && d->count && !d->grad_vertices) return fail(c, RDN_ERR_INVALID_ARG, "null gradient buffer");
+  if ((reinterpret_cast<uintptr_t>(d->rays) & 15) || (reinterpret_cast<uintptr_t>(d->grad_vertices) & 15) ||
+      (reinterpret_cast<uintptr_t>(d->seg_rays) & 15))
+    return fail(c, RDN_ERR_INVALID_ARG, "rays, segment rays and gradients must be 16-byte aligned");
+  if (d->traversal > RDN_TRAVERSAL_ORDERED_WIDE) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
+  if (d->block_size && (d->block_size % 32 || d->block_size > 128))
+    return fail(c, RDN_ERR_INVALID_ARG, "block_size must be a multiple of 32 up to 128");
+  rdn_status st = ensure_built(c);
+  if (st != RDN_OK) return st;
+  rdn_trace_desc td;
+  std::memset(&td, 0, sizeof(td));
+  td.tlas_uniform = d->tlas_uniform;
+  td.cull_mask = 0xFF;
+  td.traversal = d->traversal;
+  fill_params(c, &td, p);
+  std::memset(&a, 0, sizeof(a));
+  a.rays = reinterpret_cast<const float4*>(d->rays);
+  a.tlas_idx = d->tlas_idx;
+  a.count = d->count;
+  a.tlas_uniform = d->tlas_uniform;
+  a.segments = d->segments;
+  a.seed = d->seed;
+  a.indices = c->dev.indices.ptr;
+  a.vertices = c->dev.vertices.ptr;
+  a.attributes = d->attributes;
+  a.targets = d->targets;
+  a.values = d->values;
+  a.loss_sum = d->loss_sum;
+  a.grad_vertices = d->grad_vertices;
+  a.seg_tri = d->seg_tri;
+  a.seg_rays = reinterpret_cast<float4*>(d->seg_rays);
+  a.grad_scale = d->grad_scale;
+  a.work_counter = c->d_counters + 12;
+  return RDN_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+rdn_status rdn_attr_paths_forward(rdn_ctx* c, const rdn_attr_path_desc* d, void* stream) {
+  if (!c) return RDN_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(c->lock);
+  rdn::TraceParams p;
+  rdn::PathAdjointParams a;
+  rdn_status st = prepare_attr_paths(c, d, false, p, a);
+  if (st != RDN_OK) return st;
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e == cudaSuccess)
+    e = rdn::launch_attr_paths(p, a, mode_of(d->traversal), false, d->block_size, c->sm_count,
+                               static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(c, e, "attribute paths forward");
+  return RDN_OK;
+}
+
+rdn_status rdn_attr_paths_adjoint(rdn_ctx* c, const rdn_attr_path_desc* d, void* stream) {
+  if (!c) return RDN_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(c->lock);
+  rdn::TraceParams p;
+  rdn::PathAdjointParams a;
+  rdn_status st = prepare_attr_paths(c, d, true, p, a);
+  if (st != RDN_OK) return st;
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e == cudaSuccess)
+    e = rdn::launch_attr_paths(p, a, mode_of(d->traversal), true, d->block_size, c->sm_count,
+                               static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(c, e, "attribute paths adjoint");
+  return RDN_OK;
+}
+
+rdn_status rdn_attr_paths_graph(rdn_ctx* c, const rdn_attr_path_desc* d, uint64_t num_vertices, rdn_graph** out) {
+  if (!c || !out) return RDN_ERR_INVALID_ARG;
+  *out = nullptr;
+  std::lock_guard<std::mutex> lk(c->lock);
+  rdn::TraceParams p;
+  rdn::PathAdjointParams a;
+  rdn_status st = prepare_attr_paths(c, d, true, p, a);
+  if (st != RDN_OK) return st;
+  if (num_vertices > c->dev.vertex_count) return fail(c, RDN_ERR_INVALID_ARG, "more vertices than the structure has");
+  // warm launch outside the capture sets the kernel attributes
+  cudaStream_t s = nullptr;
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return cuda_fail(c, e, "capture stream");
+  const int mode = mode_of(d->traversal);
+  rdn::PathAdjointParams fwd = a;
+  fwd.grad_vertices = nullptr;
+  auto record = [&]() -> cudaError_t {
+    cudaError_t r = cudaSuccess;
+    if (d->loss_sum) r = cudaMemsetAsync(d->loss_sum, 0, sizeof(double), s);
+    if (r == cudaSuccess && d->grad_vertices) r = cudaMemsetAsync(d->grad_vertices, 0, num_vertices * 16, s);
+    if (r == cudaSuccess) r = rdn::launch_attr_paths(p, fwd, mode, false, d->block_size, c->sm_count, s);
+    if (r == cudaSuccess && d->grad_vertices)
+      r = rdn::launch_attr_paths(p, a, mode, true, d->block_size, c->sm_count, s);
+    return r;
+  };
+  e = record();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  auto* g = new (std::nothrow) rdn_graph();
+  if (!g) {
+    cudaStreamDestroy(s);
+    return fail(c, RDN_ERR_OOM, "host allocation failed");
+  }
+  g->device = c->device;
+  if (e == cudaSuccess) e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    cudaError_t rec = record();
+    e = cudaStreamEndCapture(s, &g->graph);
+    if (rec != cudaSuccess) e = rec;
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&g->exec, g->graph, 0);
+  cudaStreamDestroy(s);
+  if (e != cudaSuccess) {
+    if (g->graph) cudaGraphDestroy(g->graph);
+    delete g;
+    return cuda_fail(c, e, "attribute paths graph capture");
+  }
+  *out = g;
+  return RDN_OK;
+}
+
 rdn_status rdn_scan_scratch_size(uint32_t count, size_t* bytes) {
   if (!bytes) return RDN_ERR_INVALID_ARG;
   *bytes = rdn::scan_scratch_bytes(count);

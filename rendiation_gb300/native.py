@@ -27,7 +27,8 @@ EXPORTED_SYMBOLS = [
     "rdn_wavefront_shadow_bounce_static", "rdn_paths_scratch_size", "rdn_trace_paths", "rdn_trace_paths_graph",
     "rdn_graph_launch", "rdn_graph_destroy", "rdn_attr_loss_forward", "rdn_attr_loss_adjoint",
     "rdn_scan_scratch_size", "rdn_scan_u32", "rdn_compact_scratch_size", "rdn_compact_u32",
-    "rdn_radix_sort_scratch_size", "rdn_radix_sort_u32",
+    "rdn_radix_sort_scratch_size", "rdn_radix_sort_u32", "rdn_attr_paths_forward", "rdn_attr_paths_adjoint",
+    "rdn_attr_paths_graph",
 ]
 
 
@@ -99,6 +100,14 @@ class AttrLossDesc(C.Structure):
                 ("traversal", C.c_uint32), ("block_size", C.c_uint32), ("reserved", C.c_uint32)]
 
 
+class AttrPathDesc(C.Structure):
+    _fields_ = [("rays", C.c_void_p), ("tlas_idx", C.c_void_p), ("count", C.c_uint32), ("tlas_uniform", C.c_uint32),
+                ("segments", C.c_uint32), ("seed", C.c_uint32), ("attributes", C.c_void_p), ("targets", C.c_void_p),
+                ("values", C.c_void_p), ("loss_sum", C.c_void_p), ("grad_vertices", C.c_void_p),
+                ("seg_tri", C.c_void_p), ("seg_rays", C.c_void_p), ("grad_scale", C.c_float),
+                ("traversal", C.c_uint32), ("block_size", C.c_uint32), ("reserved", C.c_uint32)]
+
+
 _lib = None
 
 
@@ -167,5 +176,10 @@ def lib() -> C.CDLL:
     L.rdn_compact_u32.restype = i32
     L.rdn_radix_sort_u32.argtypes = [vp, vp, u32, u32, vp, C.c_size_t, vp]
     L.rdn_radix_sort_u32.restype = i32
+    for name in ("rdn_attr_paths_forward", "rdn_attr_paths_adjoint"):
+        getattr(L, name).argtypes = [vp, C.POINTER(AttrPathDesc), vp]
+        getattr(L, name).restype = i32
+    L.rdn_attr_paths_graph.argtypes = [vp, C.POINTER(AttrPathDesc), C.c_uint64, C.POINTER(vp)]
+    L.rdn_attr_paths_graph.restype = i32
     _lib = L
     return L
