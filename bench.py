@@ -525,6 +525,210 @@ def bench_adjoint(args):
     return out
 
 
+def bench_batched_adjoint(args):
+    """Batched differentiable paths: 64 heightfields with vertex grids
+    log-uniform in [64^2, 512^2] (octaves seeded per scene), each with a
+    per-vertex attribute and 64k..1M primary rays (log-uniform) plus 2 diffuse
+    bounces; targets are the same paths' values on copies with heights jittered
+    by N(0, 0.005). Forward + adjoint of all scenes in one captured CUDA graph,
+    hits recomputed in the adjoint. Gradient error per scene against FP64 on a
+    sample of 2048 paths per scene (analytic FP64 gradient over the sample, and
+    FP64 central differences, h = 1e-4 with Richardson extrapolation, on 2
+    vertices per scene)."""
+    import ctypes as C
+
+    import torch
+
+    from rendiation_gb300 import native
+    from rendiation_gb300 import raytracing as rt
+    from rendiation_gb300 import scenes
+
+    L = native.lib()
+    n_scenes, seg = args.diff_scenes, 3
+    grids = np.sqrt(scenes.log_uniform_ints(n_scenes, 64 * 64, 512 * 512, 31)).astype(np.int64)
+    nrays = scenes.log_uniform_ints(n_scenes, 64_000, 1_000_000, 32)
+    meshes = [scenes.heightfield(int(g), seed=100 + k) for k, g in enumerate(grids)]
+    jitter = [scenes.heightfield(int(g), seed=100 + k, jitter_sigma=0.005, jitter_seed=7000 + k)
+              for k, g in enumerate(grids)]
+
+    def system(ms):
+        P = rt.AccelerationStructureSystem(device=0)
+        for m in ms:
+            P.create_bottom_level_acceleration_structure([rt.BottomLevelAccelerationStructureBuildSource(
+                m.positions, m.indices)])
+        P.bind_tlas([P.create_top_level_acceleration_structure([rt.TopLevelAccelerationStructureSourceInstance(s)])
+                     for s in range(len(ms))])
+        P.build(blas_bin_size=4)
+        return P
+
+    rays, tidx = [], []
+    for k in range(n_scenes):
+        w = int(np.sqrt(nrays[k] * 16 / 9))
+        h = max(1, int(nrays[k]) // w)
+        cam = scenes.PinholeCamera.look_at((0.5, -0.5, 0.8), (0.5, 0.5, 0.0), 20.0, w, h)
+        r = scenes.pinhole_rays(cam)
+        rays.append(r)
+        tidx.append(np.full(r.shape[0], k, np.uint32))
+    rays = np.concatenate(rays)
+    tidx = np.concatenate(tidx)
+    n = rays.shape[0]
+    nv = sum(m.positions.shape[0] for m in meshes)
+    attr = torch.from_numpy(np.random.Generator(np.random.PCG64(33)).random(nv).astype(np.float32)).cuda()
+    d_rays = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).cuda()
+    d_tidx = torch.from_numpy(tidx.astype(np.int32)).cuda()
+    torch.cuda.reset_peak_memory_stats()
+
+    def desc(**kw):
+        d = native.AttrPathDesc()
+        d.rays, d.tlas_idx, d.count, d.segments, d.seed, d.grad_scale = d_rays.data_ptr(), d_tidx.data_ptr(), n, seg, 5, 1.0
+        d.attributes = attr.data_ptr()
+        for k, v in kw.items():
+            setattr(d, k, v)
+        return d
+
+    Pj = system(jitter)
+    targets = torch.zeros(n * seg, device="cuda")
+    assert L.rdn_attr_paths_forward(Pj._h, C.byref(desc(values=targets.data_ptr())), None) == 0
+    torch.cuda.synchronize()
+    Pj.close()
+    P = system(meshes)
+    as_bytes = P.device_bytes()
+    loss = torch.zeros(1, dtype=torch.float64, device="cuda")
+    grad = torch.zeros((nv, 4), device="cuda")
+    both = desc(targets=targets.data_ptr(), loss_sum=loss.data_ptr(), grad_vertices=grad.data_ptr())
+    fwd = desc(targets=targets.data_ptr(), loss_sum=loss.data_ptr())
+    g = C.c_void_p()
+    assert L.rdn_attr_paths_graph(P._h, C.byref(both), nv, C.byref(g)) == 0
+    gf = C.c_void_p()
+    assert L.rdn_attr_paths_graph(P._h, C.byref(fwd), nv, C.byref(gf)) == 0
+    stream = torch.cuda.current_stream()
+    sp = C.c_void_p(stream.cuda_stream)
+    out = {}
+    for name, handle in (("forward", gf), ("forward_adjoint", g)):
+        for _ in range(args.warmup):
+            L.rdn_graph_launch(handle, sp)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(5):
+            L.rdn_graph_launch(handle, sp)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out[name + "_ms"] = round(e0.elapsed_time(e1) / 5, 3)
+    L.rdn_graph_destroy(g)
+    L.rdn_graph_destroy(gf)
+    # segments traced per step (one forward pass records the segment triangles)
+    seg_tri = torch.zeros(n * seg, dtype=torch.int32, device="cuda")
+    assert L.rdn_attr_paths_forward(P._h, C.byref(desc(seg_tri=seg_tri.data_ptr())), None) == 0
+    torch.cuda.synchronize()
+    tri_all = seg_tri.cpu().numpy().view(np.uint32).reshape(-1, seg)
+    # a segment is traced when every earlier one hit
+    traced = int(n + np.sum(tri_all[:, 0] != 0xFFFFFFFF) + np.sum((tri_all[:, 0] != 0xFFFFFFFF) & (tri_all[:, 1] != 0xFFFFFFFF)))
+    out["segments_per_step"] = traced
+    out["forward_mrays"] = round(traced / (out["forward_ms"] / 1e3) / 1e6, 2)
+    out["forward_adjoint_mrays"] = round(traced / (out["forward_adjoint_ms"] / 1e3) / 1e6, 2)
+    out["fwd_adjoint_over_fwd"] = round(out["forward_adjoint_ms"] / out["forward_ms"], 3)
+    out["peak_hbm_bytes"] = int(torch.cuda.max_memory_allocated() + as_bytes)
+    out["workload"] = (f"{n_scenes} heightfields {int(grids.min())}^2..{int(grids.max())}^2 "
+                       f"({sum(m.triangle_count for m in meshes)} tris), {n} primaries, 2 bounces")
+    out["gradient_error"] = batched_gradient_error(P, meshes, rays, tidx, attr, targets, seg)
+    P.close()
+    return out
+
+
+def batched_gradient_error(P, meshes, rays, tidx, attr, targets, seg, sample=2048):
+    """Per scene: the kernel gradient of a loss over `sample` paths against FP64."""
+    import ctypes as C
+
+    import torch
+
+    from rendiation_gb300 import native
+
+    L = native.lib()
+    pos = np.concatenate([m.positions for m in meshes]).astype(np.float64)
+    offs = np.cumsum([0] + [m.positions.shape[0] for m in meshes])
+    idx = np.concatenate([m.indices + offs[k] for k, m in enumerate(meshes)]).astype(np.int64)
+    a = attr.cpu().numpy().astype(np.float64)
+    tg_all = targets.cpu().numpy().reshape(-1, seg)
+    worst_analytic, worst_fd, worst_fd_plain = [], [], []
+    rng = np.random.default_rng(8)
+    for s in range(len(meshes)):
+        sel = np.nonzero(tidx == s)[0]
+        sel = sel[rng.choice(sel.shape[0], min(sample, sel.shape[0]), replace=False)]
+        sr = np.ascontiguousarray(rays[sel])
+        m = sr.shape[0]
+        d_r = torch.from_numpy(sr.view(np.float32).reshape(-1, 8).copy()).cuda()
+        d_t = torch.from_numpy(tidx[sel].astype(np.int32)).cuda()
+        d_tg = torch.from_numpy(np.ascontiguousarray(tg_all[sel]).reshape(-1)).cuda()
+        seg_tri = torch.zeros(m * seg, dtype=torch.int32, device="cuda")
+        seg_rays = torch.zeros((m * seg, 8), device="cuda")
+        grad = torch.zeros((pos.shape[0], 4), device="cuda")
+        d = native.AttrPathDesc()
+        d.rays, d.tlas_idx, d.count, d.segments, d.seed, d.grad_scale = d_r.data_ptr(), d_t.data_ptr(), m, seg, 5, 1.0
+        d.attributes, d.targets = attr.data_ptr(), d_tg.data_ptr()
+        d.seg_tri, d.seg_rays = seg_tri.data_ptr(), seg_rays.data_ptr()
+        assert L.rdn_attr_paths_forward(P._h, C.byref(d), None) == 0
+        d.seg_tri, d.seg_rays, d.grad_vertices = None, None, grad.data_ptr()
+        assert L.rdn_attr_paths_adjoint(P._h, C.byref(d), None) == 0
+        torch.cuda.synchronize()
+        tri = seg_tri.cpu().numpy().view(np.uint32)
+        alive = tri != 0xFFFFFFFF
+        rr = seg_rays.cpu().numpy().reshape(-1, 8)[alive].astype(np.float64)
+        t_ = tri[alive].astype(np.int64)
+        tg = d_tg.cpu().numpy().astype(np.float64)[alive]
+        tv = idx.reshape(-1, 3)[t_]
+        dd = rr[:, 4:7] / np.linalg.norm(rr[:, 4:7], axis=1, keepdims=True)
+
+        def bary(P64):
+            v = P64[tv]
+            e1, e2 = v[:, 1] - v[:, 0], v[:, 2] - v[:, 0]
+            M = np.stack([-dd, e1, e2], axis=2)
+            x = np.linalg.solve(M, (rr[:, 0:3] - v[:, 0])[..., None])[..., 0]
+            return x[:, 1], x[:, 2], M
+
+        def loss_of(P64, sel_rows=None):
+            u, v, _ = bary(P64)
+            val = (1 - u - v) * a[tv[:, 0]] + u * a[tv[:, 1]] + v * a[tv[:, 2]]
+            return np.sum((val - tg) ** 2)
+
+        u, v, M = bary(pos)
+        val = (1 - u - v) * a[tv[:, 0]] + u * a[tv[:, 1]] + v * a[tv[:, 2]]
+        r = 2 * (val - tg)
+        gvec = np.stack([np.zeros_like(r), r * (a[tv[:, 1]] - a[tv[:, 0]]), r * (a[tv[:, 2]] - a[tv[:, 0]])], 1)
+        lam = np.linalg.solve(np.transpose(M, (0, 2, 1)), gvec[..., None])[..., 0]
+        gp = np.zeros((pos.shape[0], 3))
+        for k, wk in enumerate([1 - u - v, u, v]):
+            np.add.at(gp, tv[:, k], -wk[:, None] * lam)
+        gg = grad.cpu().numpy().astype(np.float64)[:, :3]
+        norm = np.linalg.norm(gp, axis=1)
+        live = norm > 0
+        floor = 1e-2 * np.median(norm[live]) if live.any() else 1.0
+        worst_analytic.append(float(np.max(np.linalg.norm(gg - gp, axis=1)[live] / np.maximum(norm[live], floor))))
+        # FP64 central differences on the 2 vertices with the largest gradient
+        fd_err, fd_plain = 0.0, 0.0
+        for vi in np.argsort(-norm)[:2]:
+            rows = np.any(tv == vi, axis=1)
+            fd = np.zeros(3)
+            fdp = np.zeros(3)
+            for c in range(3):
+                def cd(h):
+                    pp, pm = pos.copy(), pos.copy()
+                    pp[vi, c] += h
+                    pm[vi, c] -= h
+                    return (loss_of(pp) - loss_of(pm)) / (2 * h)
+                fdp[c] = cd(1e-4)
+                fd[c] = (4 * cd(5e-5) - fdp[c]) / 3
+            den = max(np.linalg.norm(fd), floor)
+            fd_err = max(fd_err, float(np.linalg.norm(gg[vi] - fd) / den))
+            fd_plain = max(fd_plain, float(np.linalg.norm(gg[vi] - fdp) / den))
+        worst_fd.append(fd_err)
+        worst_fd_plain.append(fd_plain)
+    return {"sample_paths_per_scene": sample,
+            "max_rel_vs_fp64_analytic": max(worst_analytic),
+            "max_rel_vs_fp64_fd_richardson": max(worst_fd),
+            "max_rel_vs_fp64_fd_h1e-4": max(worst_fd_plain),
+            "per_scene_rel_vs_fp64_fd_richardson": [round(x, 7) for x in worst_fd]}
+
+
 def cpu_baseline_wavefront(S, cam, threads: int, budget_s: float, steps: int = 1):
     """The oracle's pipeline on host cores over a bounded band of rows (BVH built beforehand)."""
     from oracle import orc
@@ -600,6 +804,8 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-tune", dest="tune", action="store_false", help="skip the launch autotuner")
+    ap.add_argument("--no-batched-adjoint", action="store_true")
+    ap.add_argument("--diff-scenes", type=int, default=64)
     ap.add_argument("--scenes", type=int, default=256)
     ap.add_argument("--batched-steps", type=int, default=5)
     args = ap.parse_args()
@@ -623,6 +829,8 @@ def main():
         out["batched"] = bench_batched(args)
     if not args.no_adjoint:
         out["adjoint"] = bench_adjoint(args)
+    if not args.no_batched_adjoint:
+        out["batched_adjoint"] = bench_batched_adjoint(args)
     if rank == 0:
         if not args.no_cpu_baseline:
             cb, _ = cpu_baseline_wavefront(oracle_heightfield(mesh), cam, os.cpu_count() or 1,
