@@ -430,7 +430,9 @@ rdn_status rdn_attr_paths_forward(rdn_ctx* ctx, const rdn_attr_path_desc* desc, 
 rdn_status rdn_attr_paths_adjoint(rdn_ctx* ctx, const rdn_attr_path_desc* desc, void* stream);
 /* Forward and adjoint captured once into one executable CUDA graph; each
  * launch zeroes *loss_sum and the gradient buffer (num_vertices entries of 4
- * floats) first. */
+ * floats) first. With grad_vertices NULL the graph holds the forward only.
+ * The differentiable-path calls of one context share a device work counter:
+ * order them on one stream. */
 rdn_status rdn_attr_paths_graph(rdn_ctx* ctx, const rdn_attr_path_desc* desc, uint64_t num_vertices,
                                 rdn_graph** out);
 

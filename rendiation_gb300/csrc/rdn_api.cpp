@@ -773,7 +773,7 @@ rdn_status rdn_attr_paths_graph(rdn_ctx* c, const rdn_attr_path_desc* d, uint64_
   std::lock_guard<std::mutex> lk(c->lock);
   rdn::TraceParams p;
   rdn::PathAdjointParams a;
-  rdn_status st = prepare_attr_paths(c, d, true, p, a);
+  rdn_status st = prepare_attr_paths(c, d, d->grad_vertices != nullptr, p, a);
   if (st != RDN_OK) return st;
   if (num_vertices > c->dev.vertex_count) return fail(c, RDN_ERR_INVALID_ARG, "more vertices than the structure has");
   // warm launch outside the capture sets the kernel attributes

@@ -85,7 +85,7 @@ def test_paths_forward_adjoint(fields, cuda):
     got_tri = seg_tri.cpu().numpy().view(np.uint32)
     assert np.array_equal(got_tri, exp_tri)
     alive = exp_tri != orc.MISS
-    assert alive.reshape(-1, SEG)[:, 2].mean() > 0.05  # some paths reach the second bounce
+    assert alive.reshape(-1, SEG)[:, 2].sum() > 50  # some paths reach the second bounce
     got_rays = seg_rays.cpu().numpy().view(exp_rays.dtype).reshape(-1)
     assert np.array_equal(got_rays[alive].view(np.uint32), exp_rays[alive].view(np.uint32))
 
