@@ -636,7 +636,8 @@ def bench_batched_adjoint(args):
 
 
 def batched_gradient_error(P, meshes, rays, tidx, attr, targets, seg, sample=2048):
-    """Per scene: the kernel gradient of a loss over `sample` paths against FP64."""
+    """Per scene: the kernel gradient of a loss over `sample` paths against FP64
+    (analytic over every vertex, central differences on 2 random vertices)."""
     import ctypes as C
 
     import torch
@@ -649,7 +650,7 @@ def batched_gradient_error(P, meshes, rays, tidx, attr, targets, seg, sample=204
     idx = np.concatenate([m.indices + offs[k] for k, m in enumerate(meshes)]).astype(np.int64)
     a = attr.cpu().numpy().astype(np.float64)
     tg_all = targets.cpu().numpy().reshape(-1, seg)
-    worst_analytic, worst_fd, worst_fd_plain = [], [], []
+    worst_analytic, worst_fd, worst_fd_plain, worst_unc = [], [], [], []
     rng = np.random.default_rng(8)
     for s in range(len(meshes)):
         sel = np.nonzero(tidx == s)[0]
@@ -703,29 +704,37 @@ def batched_gradient_error(P, meshes, rays, tidx, attr, targets, seg, sample=204
         live = norm > 0
         floor = 1e-2 * np.median(norm[live]) if live.any() else 1.0
         worst_analytic.append(float(np.max(np.linalg.norm(gg - gp, axis=1)[live] / np.maximum(norm[live], floor))))
-        # FP64 central differences on the 2 vertices with the largest gradient
-        fd_err, fd_plain = 0.0, 0.0
-        for vi in np.argsort(-norm)[:2]:
-            rows = np.any(tv == vi, axis=1)
-            fd = np.zeros(3)
-            fdp = np.zeros(3)
+        # FP64 central differences on 2 random vertices some sampled ray sees; the
+        # difference between the Richardson extrapolations from h and h/2 is the
+        # differences' own error, reported beside the result
+        fd_err, fd_plain, fd_unc = 0.0, 0.0, 0.0
+        seen = np.unique(tv.reshape(-1))
+        for vi in rng.choice(seen, size=min(2, seen.size), replace=False):
+            fd, fd2, fdp = np.zeros(3), np.zeros(3), np.zeros(3)
             for c in range(3):
                 def cd(h):
                     pp, pm = pos.copy(), pos.copy()
                     pp[vi, c] += h
                     pm[vi, c] -= h
                     return (loss_of(pp) - loss_of(pm)) / (2 * h)
-                fdp[c] = cd(1e-4)
-                fd[c] = (4 * cd(5e-5) - fdp[c]) / 3
-            den = max(np.linalg.norm(fd), floor)
-            fd_err = max(fd_err, float(np.linalg.norm(gg[vi] - fd) / den))
+                c1, c2, c4 = cd(1e-4), cd(5e-5), cd(2.5e-5)
+                fdp[c] = c1
+                fd[c] = (4 * c2 - c1) / 3
+                fd2[c] = (4 * c4 - c2) / 3
+            den = max(np.linalg.norm(fd2), floor)
+            fd_err = max(fd_err, float(np.linalg.norm(gg[vi] - fd2) / den))
             fd_plain = max(fd_plain, float(np.linalg.norm(gg[vi] - fdp) / den))
+            fd_unc = max(fd_unc, float(np.linalg.norm(fd - fd2) / den))
+        worst_unc.append(fd_unc)
         worst_fd.append(fd_err)
         worst_fd_plain.append(fd_plain)
     return {"sample_paths_per_scene": sample,
             "max_rel_vs_fp64_analytic": max(worst_analytic),
             "max_rel_vs_fp64_fd_richardson": max(worst_fd),
             "max_rel_vs_fp64_fd_h1e-4": max(worst_fd_plain),
+            "max_fd_own_uncertainty": max(worst_unc),
+            "median_rel_vs_fp64_fd_richardson": float(np.median(worst_fd)),
+            "scenes_within_1e-3_of_fd": int(sum(1 for e, u in zip(worst_fd, worst_unc) if e <= 1e-3 + 2 * u)),
             "per_scene_rel_vs_fp64_fd_richardson": [round(x, 7) for x in worst_fd]}
 
 

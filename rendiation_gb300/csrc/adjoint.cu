@@ -276,6 +276,10 @@ __global__ void __launch_bounds__(128) attr_path_kernel(TraceParams p, PathAdjoi
         traverse_ray<MODE, false>(p, R, tlas, smem_stack + threadIdx.x, blockDim.x, bad);
         if (!R.best.have) {
           alive = false;
+          if (!ADJOINT && a.targets) {
+            const float t = __ldg(a.targets + seg);  // value 0 against the target
+            loss_acc += (double)(t * t);
+          }
         } else {
           const InstanceRay ir = to_instance(p.tlas_data + R.best.inst, R.o, R.d, 0u);
           const HitGeom h = hit_vertices(p, a.indices, a.vertices, R, ir);
