@@ -184,7 +184,7 @@ def bench_wavefront(args, ws, rank):
     if args.tune and args.traversal == "ordered":
         from rendiation_gb300.autotune import Autotuner, grid
 
-        tuner = Autotuner()
+        tuner = Autotuner(args.tune_cache)
         cands = grid(traversal=[rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_WIDE], block=[32, 64, 128])
 
         def run_phase(ph):
@@ -651,6 +651,7 @@ def batched_gradient_error(P, meshes, rays, tidx, attr, targets, seg, sample=204
     a = attr.cpu().numpy().astype(np.float64)
     tg_all = targets.cpu().numpy().reshape(-1, seg)
     worst_analytic, worst_fd, worst_fd_plain, worst_unc = [], [], [], []
+    p99_analytic, worst_cond = [], []
     rng = np.random.default_rng(8)
     for s in range(len(meshes)):
         sel = np.nonzero(tidx == s)[0]
@@ -697,13 +698,18 @@ def batched_gradient_error(P, meshes, rays, tidx, attr, targets, seg, sample=204
         gvec = np.stack([np.zeros_like(r), r * (a[tv[:, 1]] - a[tv[:, 0]]), r * (a[tv[:, 2]] - a[tv[:, 0]])], 1)
         lam = np.linalg.solve(np.transpose(M, (0, 2, 1)), gvec[..., None])[..., 0]
         gp = np.zeros((pos.shape[0], 3))
+        gabs = np.zeros(pos.shape[0])  # sum of |per-ray contribution|: scale of the FP32 atomic sum's rounding
         for k, wk in enumerate([1 - u - v, u, v]):
             np.add.at(gp, tv[:, k], -wk[:, None] * lam)
+            np.add.at(gabs, tv[:, k], np.linalg.norm(wk[:, None] * lam, axis=1))
         gg = grad.cpu().numpy().astype(np.float64)[:, :3]
         norm = np.linalg.norm(gp, axis=1)
         live = norm > 0
         floor = 1e-2 * np.median(norm[live]) if live.any() else 1.0
-        worst_analytic.append(float(np.max(np.linalg.norm(gg - gp, axis=1)[live] / np.maximum(norm[live], floor))))
+        rel = np.linalg.norm(gg - gp, axis=1)[live] / np.maximum(norm[live], floor)
+        worst_analytic.append(float(np.max(rel)))
+        p99_analytic.append(float(np.percentile(rel, 99)))
+        worst_cond.append(float(np.max(np.linalg.norm(gg - gp, axis=1)[live] / gabs[live])))
         # FP64 central differences on 2 random vertices some sampled ray sees; the
         # difference between the Richardson extrapolations from h and h/2 is the
         # differences' own error, reported beside the result
@@ -730,6 +736,8 @@ def batched_gradient_error(P, meshes, rays, tidx, attr, targets, seg, sample=204
         worst_fd_plain.append(fd_plain)
     return {"sample_paths_per_scene": sample,
             "max_rel_vs_fp64_analytic": max(worst_analytic),
+            "p99_rel_vs_fp64_analytic": max(p99_analytic),
+            "max_err_over_contribution_abs_sum": max(worst_cond),
             "max_rel_vs_fp64_fd_richardson": max(worst_fd),
             "max_rel_vs_fp64_fd_h1e-4": max(worst_fd_plain),
             "max_fd_own_uncertainty": max(worst_unc),
@@ -813,6 +821,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-tune", dest="tune", action="store_false", help="skip the launch autotuner")
+    ap.add_argument("--tune-cache", default=None, help="JSON file that keeps the autotuner's choices between runs")
     ap.add_argument("--no-batched-adjoint", action="store_true")
     ap.add_argument("--diff-scenes", type=int, default=64)
     ap.add_argument("--scenes", type=int, default=256)
