@@ -7,8 +7,15 @@ one any-hit shadow ray to a point light at (0.2,0.2,2.0) and one
 cosine-weighted diffuse bounce ray. One step = one frame of the wavefront
 executor (rdn_wavefront_shadow_bounce). Metric: Mrays/s over all rays traced.
 
-Other workloads: "plain" (10k-triangle soup, 256x256 pinhole closest-hit rays,
-rdn_trace with host rays).
+Further legs, each a key of the same JSON line (skipped with --no-<leg>):
+  batched          256 triangle soups, up to 4 diffuse bounces with Russian
+                   roulette, one persistent launch per bounce in a CUDA graph,
+                   against the plain per-scene launch loop;
+  adjoint          256x256 heightfield, 512x512 rays, attribute loss: forward
+                   and forward + adjoint;
+  batched_adjoint  64 heightfields, primaries + 2 bounces, forward + adjoint in
+                   one graph, gradient error against FP64;
+  cpu_baseline     the oracle's pipeline on the host cores (rank 0 only).
 
 --impl reference times the reference's CPU path for the same workload: the
 oracle (a C++ restatement of the reference's CPU traversal, the Rust reference
@@ -104,6 +111,22 @@ def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return ws, rank, local
+
+
+def max_over_ranks(seconds: float, ws: int, device) -> float:
+    """The slowest rank's time: every replica's timed region must have ended."""
+    if ws == 1:
+        return seconds
+    import torch
+
+    t = torch.tensor([seconds], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replicas_value(rays_per_step: int, steps: int, ws: int, seconds: float) -> float:
+    """Whole-job Mrays/s of ws replicas that each traced steps x rays_per_step."""
+    return rays_per_step * steps * ws / seconds / 1e6
 
 
 def measured_peak_gbs():
@@ -251,11 +274,8 @@ def bench_wavefront(args, ws, rank):
     prim_ms, sec_ms = float(np.mean(k_prim)), float(np.mean(k_sec))
     frame_ms = total_ms / args.steps
     elapsed = total_ms / 1000.0
-    if ws > 1:
-        t = torch.tensor([elapsed], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        elapsed = float(t.item())
-    value = rays_per_step * args.steps * ws / elapsed / 1e6
+    elapsed = max_over_ranks(elapsed, ws, "cuda")
+    value = replicas_value(rays_per_step, args.steps, ws, elapsed)
 
     # e2e through the C ABI: each step launches the frame and reads the pixel
     # records back into pinned host memory
