@@ -110,7 +110,11 @@ typedef struct rdn_build_opts {
   uint32_t tlas_bin_size;
   uint32_t tlas_max_depth;
   uint32_t host_threads;
-  uint32_t reserved[3];
+  /* 1: build the triangle trees on the context's GPU (every flattened array
+   * byte-identical to the host build, which follows the reference's
+   * single-threaded builder); the TLAS stays on the host. 0: host build. */
+  uint32_t device_build;
+  uint32_t reserved[2];
 } rdn_build_opts;
 
 /* One ray, 32 B: ShaderRayTraceCallStoragePayload's origin, direction and
@@ -225,9 +229,10 @@ typedef struct rdn_build_stats {
   uint64_t sah_splits;
   uint64_t median_fallbacks;  /* degenerate binning -> BalanceTree median split */
   uint32_t max_blas_depth;
-  uint32_t reserved;
-  double build_seconds;       /* host SAH build + flattening */
+  uint32_t device_built;      /* 1 when the triangle trees were built on the GPU */
+  double build_seconds;       /* SAH build + flattening, wall clock */
   double upload_seconds;
+  double device_seconds;      /* device build only: span of its work on the GPU stream */
 } rdn_build_stats;
 rdn_status rdn_get_build_stats(const rdn_ctx* ctx, rdn_build_stats* out);
 

@@ -31,6 +31,7 @@ UNITS = {
     "paths.cu": ["-fmad=false"],
     "adjoint.cu": ["-fmad=false"],
     "parallel.cu": [],
+    "device_build.cu": ["-fmad=false"],
 }
 
 

@@ -23,6 +23,7 @@
 #include <future>
 #include <thread>
 
+#include "device_build.h"
 #include "rdn_core.h"
 #include "rust_select.h"
 
@@ -425,6 +426,67 @@ Box transform_box(const Box& b, const M4& m) {  // Box3::apply_matrix
   return r;
 }
 
+// TLAS forest (build_tlas, naive/mod.rs:262-320, and the loop at :435-454).
+// blas_box holds one entry per geometry, as naive/mod.rs:239 pushes it.
+std::string build_tlas_phase(const std::vector<std::unique_ptr<std::vector<InstanceSource>>>& tlas,
+                             const std::vector<Box>& blas_box, const std::vector<char>& blas_box_some,
+                             const BuildOptions& opt, HostBuilt& hb) {
+  for (const auto& tp : tlas) {
+    if (!tp) {
+      hb.tlas_bvh_root.push_back(INVALID_NEXT);
+      continue;
+    }
+    const uint32_t bvh_start = (uint32_t)hb.tlas_bvh_forest.size();
+    const uint32_t prim_start = (uint32_t)hb.tlas_data.size();
+    std::vector<Box> aabbs;
+    aabbs.reserve(tp->size());
+    for (const InstanceSource& s : *tp) {
+      if (s.blas_handle >= blas_box.size() || !blas_box_some[s.blas_handle])
+        return "instance references a deleted or missing BLAS";
+      M4 m;
+      std::memcpy(&m, s.transform, 64);
+      aabbs.push_back(transform_box(blas_box[s.blas_handle], m));
+    }
+    Tree t = build_tree(aabbs, opt.tlas_bin_size, opt.tlas_max_depth, 1);
+    for (uint32_t idx : t.order) {
+      const InstanceSource& s = (*tp)[idx];
+      M4 m;
+      std::memcpy(&m, s.transform, 64);
+      uint32_t flags = s.flags;
+      if (m3_det(m) < 0.0f) flags ^= RDN_INSTANCE_TRIANGLE_FLIP_FACING;
+      DeviceInstance di;
+      std::memset(&di, 0, sizeof(di));
+      std::memcpy(di.transform, s.transform, 64);
+      const M4 inv = m4_inverse_or_identity(m);
+      std::memcpy(di.transform_inv, &inv, 64);
+      di.instance_custom_index = s.custom_index;
+      di.sbt_offset = s.sbt_offset;
+      di.flags = flags;
+      di.acceleration_structure_handle = s.blas_handle;
+      TlasBounding tb;
+      std::memset(&tb, 0, sizeof(tb));
+      const Box& a = aabbs[idx];
+      tb.world_min[0] = a.lo.x;
+      tb.world_min[1] = a.lo.y;
+      tb.world_min[2] = a.lo.z;
+      tb.world_max[0] = a.hi.x;
+      tb.world_max[1] = a.hi.y;
+      tb.world_max[2] = a.hi.z;
+      tb.mask = s.mask;
+      tb.flags = flags;
+      hb.tlas_data.push_back(di);
+      hb.tlas_bounding.push_back(tb);
+    }
+    const auto links = threaded_links(t.nodes);
+    for (size_t i = 0; i < t.nodes.size(); i++)
+      hb.tlas_bvh_forest.push_back(to_device_node(t.nodes[i], links[i], bvh_start, prim_start));
+    hb.tlas_bvh_root.push_back(bvh_start);
+    hb.sah_splits += t.sah_splits;
+    hb.median_fallbacks += t.fallbacks;
+  }
+  return std::string();
+}
+
 }  // namespace
 
 std::string build_host(const std::vector<std::unique_ptr<std::vector<GeometrySource>>>& blas,
@@ -515,60 +577,92 @@ std::string build_host(const std::vector<std::unique_ptr<std::vector<GeometrySou
     }
   }
 
-  // TLAS forest (build_tlas, naive/mod.rs:262-320, and the loop at :435-454)
-  for (const auto& tp : tlas) {
-    if (!tp) {
-      hb.tlas_bvh_root.push_back(INVALID_NEXT);
+  std::string err = build_tlas_phase(tlas, blas_box, blas_box_some, opt, hb);
+  if (!err.empty()) return err;
+  hb.tlas_binding = binding;
+  hb.n_triangles = hb.indices_redirect.size();
+  hb.n_nodes = hb.tri_bvh_forest.size();
+  hb.n_indices = hb.indices.size();
+  hb.n_vertices = hb.vertices.size() / 3;
+  return std::string();
+}
+
+}  // namespace rdn
+
+namespace rdn {
+
+std::string build_with_device_blas(const std::vector<std::unique_ptr<std::vector<GeometrySource>>>& blas,
+                                   const std::vector<std::unique_ptr<std::vector<InstanceSource>>>& tlas,
+                                   const std::vector<uint32_t>& binding, const BuildOptions& opt, int sm_count,
+                                   HostBuilt& hb, DeviceBuilt& d, double* device_seconds) {
+  // the same geometry walk as build_host: one tree per triangle geometry in
+  // BLAS-slot order, one root-box entry per geometry (naive/mod.rs:239)
+  std::vector<DeviceGeometry> geoms;
+  struct TreeMeta {
+    uint32_t geometry_idx, flags;
+  };
+  std::vector<TreeMeta> meta;
+  std::vector<int64_t> box_entry;  // per geometry entry: tree index, -1 = non-triangle, -2 = deleted slot
+  for (const auto& bp : blas) {
+    if (!bp) {
+      hb.blas_meta_info.push_back(BlasMetaInfo{{0, 0}});
+      box_entry.push_back(-2);
       continue;
     }
-    const uint32_t bvh_start = (uint32_t)hb.tlas_bvh_forest.size();
-    const uint32_t prim_start = (uint32_t)hb.tlas_data.size();
-    std::vector<Box> aabbs;
-    aabbs.reserve(tp->size());
-    for (const InstanceSource& s : *tp) {
-      if (s.blas_handle >= blas_box.size() || !blas_box_some[s.blas_handle])
-        return "instance references a deleted or missing BLAS";
-      M4 m;
-      std::memcpy(&m, s.transform, 64);
-      aabbs.push_back(transform_box(blas_box[s.blas_handle], m));
+    const uint32_t first = (uint32_t)geoms.size();
+    uint32_t gidx = 0;
+    for (const GeometrySource& g : *bp) {
+      if (g.type == 0) {
+        const size_t vcount = g.positions.size() / 3;
+        const size_t ntri = (g.indexed ? g.indices.size() : vcount) / 3;
+        if (vcount >= (1ull << 32) || ntri >= (1ull << 32)) return "geometry too large";
+        box_entry.push_back((int64_t)geoms.size());
+        geoms.push_back(DeviceGeometry{g.positions.data(), (uint32_t)vcount, g.indexed ? g.indices.data() : nullptr,
+                                       (uint32_t)ntri});
+        meta.push_back(TreeMeta{gidx, g.flags});
+      } else {
+        box_entry.push_back(-1);
+      }
+      gidx++;
     }
-    Tree t = build_tree(aabbs, opt.tlas_bin_size, opt.tlas_max_depth, 1);
-    for (uint32_t idx : t.order) {
-      const InstanceSource& s = (*tp)[idx];
-      M4 m;
-      std::memcpy(&m, s.transform, 64);
-      uint32_t flags = s.flags;
-      if (m3_det(m) < 0.0f) flags ^= RDN_INSTANCE_TRIANGLE_FLIP_FACING;
-      DeviceInstance di;
-      std::memset(&di, 0, sizeof(di));
-      std::memcpy(di.transform, s.transform, 64);
-      const M4 inv = m4_inverse_or_identity(m);
-      std::memcpy(di.transform_inv, &inv, 64);
-      di.instance_custom_index = s.custom_index;
-      di.sbt_offset = s.sbt_offset;
-      di.flags = flags;
-      di.acceleration_structure_handle = s.blas_handle;
-      TlasBounding tb;
-      std::memset(&tb, 0, sizeof(tb));
-      const Box& a = aabbs[idx];
-      tb.world_min[0] = a.lo.x;
-      tb.world_min[1] = a.lo.y;
-      tb.world_min[2] = a.lo.z;
-      tb.world_max[0] = a.hi.x;
-      tb.world_max[1] = a.hi.y;
-      tb.world_max[2] = a.hi.z;
-      tb.mask = s.mask;
-      tb.flags = flags;
-      hb.tlas_data.push_back(di);
-      hb.tlas_bounding.push_back(tb);
-    }
-    const auto links = threaded_links(t.nodes);
-    for (size_t i = 0; i < t.nodes.size(); i++)
-      hb.tlas_bvh_forest.push_back(to_device_node(t.nodes[i], links[i], bvh_start, prim_start));
-    hb.tlas_bvh_root.push_back(bvh_start);
-    hb.sah_splits += t.sah_splits;
-    hb.median_fallbacks += t.fallbacks;
+    hb.blas_meta_info.push_back(BlasMetaInfo{{first, (uint32_t)geoms.size()}});
   }
+  DeviceBlasOut o;
+  std::string err = build_blas_device(geoms, opt.blas_bin_size, opt.blas_max_depth, sm_count, d, o);
+  if (!err.empty()) return err;
+  *device_seconds = o.kernel_seconds;
+  std::vector<Box> blas_box;
+  std::vector<char> blas_box_some;
+  for (int64_t e : box_entry) {
+    if (e >= 0) {
+      Box b = empty_box();
+      grow(b, o.root_box[(size_t)e]);
+      blas_box.push_back(b);
+    } else {
+      blas_box.push_back(empty_box());
+    }
+    blas_box_some.push_back(e == -2 ? 0 : 1);
+  }
+  uint32_t bvh_start = 0, prim_start = 0;
+  for (size_t t = 0; t < geoms.size(); t++) {
+    hb.tri_bvh_root.push_back(GeometryMetaInfo{bvh_start, meta[t].geometry_idx, prim_start, meta[t].flags});
+    bvh_start += o.tree_nodes[t];
+    prim_start += geoms[t].triangle_count;
+  }
+  hb.geom_root_code = o.root_code;
+  hb.geom_root_code4 = o.root_code4;
+  hb.max_blas_depth = o.max_depth;
+  hb.max_wide4_depth = o.max_wide4_depth;
+  hb.sah_splits = o.sah_splits;
+  hb.median_fallbacks = o.median_fallbacks;
+  hb.device_blas = true;
+  hb.device_bytes = o.bytes;
+  hb.n_triangles = o.triangles;
+  hb.n_nodes = o.nodes;
+  hb.n_indices = 3 * o.triangles;
+  hb.n_vertices = o.vertices;
+  err = build_tlas_phase(tlas, blas_box, blas_box_some, opt, hb);
+  if (!err.empty()) return err;
   hb.tlas_binding = binding;
   return std::string();
 }

@@ -74,25 +74,47 @@ rdn_status do_build(rdn_ctx* c) {
   auto t0 = std::chrono::steady_clock::now();
   auto hb = std::make_unique<rdn::HostBuilt>();
   std::string err;
+  const bool on_device = c->opts.device_build != 0;
+  c->device_seconds = 0.0;
+  if (on_device) {
+    if (c->device < 0) return fail(c, RDN_ERR_UNSUPPORTED, "host-only context cannot build on a device");
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaSetDevice");
+    e = cudaDeviceSynchronize();  // no trace may still read the buffers being replaced
+    if (e != cudaSuccess) return cuda_fail(c, e, "synchronize before build");
+    free_device(c->dev);
+  }
   try {
-    err = rdn::build_host(c->blas, c->tlas, c->binding, c->opts, *hb);
+    err = on_device ? rdn::build_with_device_blas(c->blas, c->tlas, c->binding, c->opts, c->sm_count, *hb, c->dev,
+                                                  &c->device_seconds)
+                    : rdn::build_host(c->blas, c->tlas, c->binding, c->opts, *hb);
   } catch (const std::bad_alloc&) {
+    if (on_device) free_device(c->dev);
     return fail(c, RDN_ERR_OOM, "host allocation failed during build");
   } catch (const std::exception& ex) {
+    if (on_device) free_device(c->dev);
     return fail(c, RDN_ERR_INVALID_ARG, ex.what());
   }
-  if (!err.empty()) return fail(c, RDN_ERR_INVALID_HANDLE, err);
+  if (!err.empty()) {
+    if (on_device) free_device(c->dev);
+    const rdn_status code = err.rfind("CUDA OOM ", 0) == 0 ? RDN_ERR_OOM
+                            : err.rfind("CUDA ", 0) == 0   ? RDN_ERR_CUDA
+                                                           : RDN_ERR_INVALID_HANDLE;
+    return fail(c, code, err);
+  }
   auto t1 = std::chrono::steady_clock::now();
   c->build_seconds = std::chrono::duration<double>(t1 - t0).count();
   c->upload_seconds = 0.0;
   if (c->device >= 0) {
     cudaError_t e = cudaSetDevice(c->device);
     if (e != cudaSuccess) return cuda_fail(c, e, "cudaSetDevice");
-    e = cudaDeviceSynchronize();  // no trace may still read the buffers being replaced
-    if (e != cudaSuccess) return cuda_fail(c, e, "synchronize before upload");
-    free_device(c->dev);
+    if (!on_device) {
+      e = cudaDeviceSynchronize();  // no trace may still read the buffers being replaced
+      if (e != cudaSuccess) return cuda_fail(c, e, "synchronize before upload");
+      free_device(c->dev);
+    }
     rdn::DeviceBuilt& d = c->dev;
-    uint64_t bytes = 0;
+    uint64_t bytes = hb->device_bytes;
 #define UP(field, src)                                      \
   e = upload(d.field, hb->src, bytes);                      \
   if (e != cudaSuccess) {                                   \
@@ -106,20 +128,22 @@ rdn_status do_build(rdn_ctx* c) {
     UP(tlas_bounding, tlas_bounding)
     UP(blas_meta_info, blas_meta_info)
     UP(tri_bvh_root, tri_bvh_root)
-    UP(tri_bvh_forest, tri_bvh_forest)
-    UP(indices_redirect, indices_redirect)
-    UP(tri_records, tri_records)
-    UP(wide_nodes, wide_nodes)
-    UP(leaf_ranges, leaf_ranges)
     UP(geom_root_code, geom_root_code)
-    UP(indices, indices)
-    UP(vertices, vertices)
-    UP(wide4_nodes, wide4_nodes)
     UP(geom_root_code4, geom_root_code4)
+    if (!hb->device_blas) {
+      UP(tri_bvh_forest, tri_bvh_forest)
+      UP(indices_redirect, indices_redirect)
+      UP(tri_records, tri_records)
+      UP(wide_nodes, wide_nodes)
+      UP(leaf_ranges, leaf_ranges)
+      UP(indices, indices)
+      UP(vertices, vertices)
+      UP(wide4_nodes, wide4_nodes)
+    }
 #undef UP
     d.max_blas_depth = hb->max_blas_depth;
     d.max_wide4_depth = hb->max_wide4_depth;
-    d.vertex_count = hb->vertices.size() / 3;
+    d.vertex_count = hb->n_vertices;
     d.bytes = bytes;
     c->upload_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t1).count();
   }
@@ -323,6 +347,8 @@ rdn_status rdn_build(rdn_ctx* c, const rdn_build_opts* o) {
     if (o->tlas_bin_size) opts.tlas_bin_size = o->tlas_bin_size;
     if (o->tlas_max_depth) opts.tlas_max_depth = o->tlas_max_depth;
     opts.host_threads = o->host_threads;
+    opts.device_build = o->device_build;
+    if (opts.device_build > 1) return fail(c, RDN_ERR_INVALID_ARG, "device_build must be 0 or 1");
     if (opts.blas_max_depth > 64 || opts.tlas_max_depth > 64)
       return fail(c, RDN_ERR_INVALID_ARG, "max tree depth above 64 is not supported");
   }
@@ -337,8 +363,10 @@ rdn_status rdn_get_build_stats(const rdn_ctx* cc, rdn_build_stats* out) {
   if (!c->host || c->dirty) return fail(c, RDN_ERR_NOT_BUILT, "structure not built");
   std::memset(out, 0, sizeof(*out));
   out->device_bytes = c->dev.bytes;
-  out->triangles = c->host->indices_redirect.size();
-  out->nodes = c->host->tri_bvh_forest.size();
+  out->triangles = c->host->n_triangles;
+  out->nodes = c->host->n_nodes;
+  out->device_built = c->host->device_blas ? 1u : 0u;
+  out->device_seconds = c->device_seconds;
   out->sah_splits = c->host->sah_splits;
   out->median_fallbacks = c->host->median_fallbacks;
   out->max_blas_depth = c->host->max_blas_depth;
@@ -376,10 +404,39 @@ rdn_status rdn_get_built_array(const rdn_ctx* cc, uint32_t which, void* dst, siz
       return fail(c, RDN_ERR_INVALID_ARG, "unknown array");
   }
 #undef CASE
+  const void* dev_src = nullptr;
+  if (B.device_blas) {  // these arrays were built on the device and live only there
+    switch (which) {
+      case 7:
+        dev_src = c->dev.tri_bvh_forest.ptr;
+        bytes = B.n_nodes * sizeof(rdn::DeviceBVHNode);
+        break;
+      case 8:
+        dev_src = c->dev.indices_redirect.ptr;
+        bytes = B.n_triangles * sizeof(uint32_t);
+        break;
+      case 9:
+        dev_src = c->dev.indices.ptr;
+        bytes = B.n_indices * sizeof(uint32_t);
+        break;
+      case 10:
+        dev_src = c->dev.vertices.ptr;
+        bytes = B.n_vertices * 3 * sizeof(float);
+        break;
+      default:
+        break;
+    }
+  }
   *size = bytes;
   if (dst) {
     if (capacity < bytes) return fail(c, RDN_ERR_INVALID_ARG, "destination too small");
-    if (bytes) std::memcpy(dst, src, bytes);
+    if (bytes && dev_src) {
+      cudaError_t e = cudaSetDevice(c->device);
+      if (e == cudaSuccess) e = cudaMemcpy(dst, dev_src, bytes, cudaMemcpyDeviceToHost);
+      if (e != cudaSuccess) return cuda_fail(c, e, "read back built array");
+    } else if (bytes) {
+      std::memcpy(dst, src, bytes);
+    }
   }
   return RDN_OK;
 }

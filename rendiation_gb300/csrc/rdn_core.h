@@ -127,6 +127,12 @@ struct HostBuilt {
   uint32_t max_blas_depth = 0;
   uint32_t max_wide4_depth = 0;
   uint64_t sah_splits = 0, median_fallbacks = 0;
+  // sizes of the reference-layout arrays (kept when they live on the device only)
+  uint64_t n_triangles = 0, n_nodes = 0, n_indices = 0, n_vertices = 0;
+  // true: the triangle forest, geometry arrays and GB300 node layouts were
+  // built on the device and exist only there
+  bool device_blas = false;
+  uint64_t device_bytes = 0;
 };
 
 template <class T>
@@ -155,6 +161,7 @@ struct DeviceBuilt {
 
 struct BuildOptions {
   uint32_t blas_bin_size = 2, blas_max_depth = 50, tlas_bin_size = 10, tlas_max_depth = 50, host_threads = 0;
+  uint32_t device_build = 0;
 };
 
 // Builds the whole structure from the sources (reference: NaiveSahBvhSource::build,
@@ -162,6 +169,14 @@ struct BuildOptions {
 std::string build_host(const std::vector<std::unique_ptr<std::vector<GeometrySource>>>& blas,
                        const std::vector<std::unique_ptr<std::vector<InstanceSource>>>& tlas,
                        const std::vector<uint32_t>& binding, const BuildOptions& opt, HostBuilt& out);
+
+// Same structure with the triangle trees built on the current device
+// (device_build.cu): the device arrays of the BLAS forest are written into
+// `d`, the small per-tree and TLAS arrays into `out`.
+std::string build_with_device_blas(const std::vector<std::unique_ptr<std::vector<GeometrySource>>>& blas,
+                                   const std::vector<std::unique_ptr<std::vector<InstanceSource>>>& tlas,
+                                   const std::vector<uint32_t>& binding, const BuildOptions& opt, int sm_count,
+                                   HostBuilt& out, DeviceBuilt& d, double* device_seconds);
 
 }  // namespace rdn
 
@@ -177,6 +192,6 @@ struct rdn_ctx {
   std::unique_ptr<rdn::HostBuilt> host;
   rdn::DeviceBuilt dev;
   uint32_t* d_counters = nullptr;  // 4 x u64 counters + error words
-  double build_seconds = 0.0, upload_seconds = 0.0;
+  double build_seconds = 0.0, upload_seconds = 0.0, device_seconds = 0.0;
   std::string err;
 };

@@ -50,13 +50,15 @@ class Instance(C.Structure):
 
 class BuildOpts(C.Structure):
     _fields_ = [("blas_bin_size", C.c_uint32), ("blas_max_depth", C.c_uint32), ("tlas_bin_size", C.c_uint32),
-                ("tlas_max_depth", C.c_uint32), ("host_threads", C.c_uint32), ("reserved", C.c_uint32 * 3)]
+                ("tlas_max_depth", C.c_uint32), ("host_threads", C.c_uint32), ("device_build", C.c_uint32),
+                ("reserved", C.c_uint32 * 2)]
 
 
 class BuildStats(C.Structure):
     _fields_ = [("device_bytes", C.c_uint64), ("triangles", C.c_uint64), ("nodes", C.c_uint64),
                 ("sah_splits", C.c_uint64), ("median_fallbacks", C.c_uint64), ("max_blas_depth", C.c_uint32),
-                ("reserved", C.c_uint32), ("build_seconds", C.c_double), ("upload_seconds", C.c_double)]
+                ("device_built", C.c_uint32), ("build_seconds", C.c_double), ("upload_seconds", C.c_double),
+                ("device_seconds", C.c_double)]
 
 
 class TraceDesc(C.Structure):

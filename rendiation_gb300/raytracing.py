@@ -151,8 +151,11 @@ class AccelerationStructureSystem:
         _check(self._h, self._L.rdn_bind_tlas(self._h, a.ctypes.data, a.shape[0]))
 
     # --- build / inspection ---
-    def build(self, blas_bin_size=0, blas_max_depth=0, tlas_bin_size=0, tlas_max_depth=0, host_threads=0):
-        o = native.BuildOpts(blas_bin_size, blas_max_depth, tlas_bin_size, tlas_max_depth, host_threads)
+    def build(self, blas_bin_size=0, blas_max_depth=0, tlas_bin_size=0, tlas_max_depth=0, host_threads=0,
+              device_build=False):
+        """device_build: build the triangle trees on the GPU (same arrays as the host build)."""
+        o = native.BuildOpts(blas_bin_size, blas_max_depth, tlas_bin_size, tlas_max_depth, host_threads,
+                             int(device_build))
         _check(self._h, self._L.rdn_build(self._h, C.byref(o)))
 
     def build_stats(self) -> dict:

@@ -51,7 +51,7 @@ class Scene:
         self.blas_bin_size = blas_bin_size
         self.tlas_bin_size = tlas_bin_size
 
-    def build_oracle(self) -> orc.OracleSystem:
+    def build_oracle(self, blas_max_depth=50) -> orc.OracleSystem:
         S = orc.OracleSystem()
         for geoms in self.blas:
             S.create_blas(geoms)
@@ -62,10 +62,10 @@ class Scene:
         for h in self.deleted_tlas:
             S.delete_tlas(h)
         S.bind_tlas(self.bind)
-        S.build(blas_bin_size=self.blas_bin_size, tlas_bin_size=self.tlas_bin_size)
+        S.build(blas_bin_size=self.blas_bin_size, tlas_bin_size=self.tlas_bin_size, blas_max_depth=blas_max_depth)
         return S
 
-    def build_product(self, device=0) -> rt.AccelerationStructureSystem:
+    def build_product(self, device=0, device_build=False, blas_max_depth=0) -> rt.AccelerationStructureSystem:
         P = rt.AccelerationStructureSystem(device=device)
         for geoms in self.blas:
             P.create_bottom_level_acceleration_structure(
@@ -80,7 +80,8 @@ class Scene:
         for h in self.deleted_tlas:
             P.delete_top_level_acceleration_structure(h)
         P.bind_tlas(self.bind)
-        P.build(blas_bin_size=self.blas_bin_size, tlas_bin_size=self.tlas_bin_size)
+        P.build(blas_bin_size=self.blas_bin_size, tlas_bin_size=self.tlas_bin_size, blas_max_depth=blas_max_depth,
+                device_build=device_build)
         return P
 
 

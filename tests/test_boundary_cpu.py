@@ -126,3 +126,11 @@ def test_handles_are_dense_and_deleted_slots_stay_empty():
     assert P.create_bottom_level_acceleration_structure(src) == 3
     with pytest.raises(native.RdnError):
         P.delete_bottom_level_acceleration_structure(1)
+
+
+def test_device_build_needs_a_device():
+    """A host-only context refuses the device build instead of building on the host."""
+    sc = single_mesh_scene(scenes.triangle_soup(100, seed=1))
+    with pytest.raises(native.RdnError) as ex:
+        sc.build_product(device=-1, device_build=True)
+    assert ex.value.status == -8  # RDN_ERR_UNSUPPORTED
