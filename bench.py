@@ -151,6 +151,8 @@ def traffic_from_profile(workload: str, kernel: str):
 # --------------------------------------------------------------------------- workloads
 
 def build_heightfield_system(n_grid: int):
+    """The heightfield scene, built on the host and on the GPU (kept); returns
+    (mesh, system, build comparison)."""
     from rendiation_gb300 import raytracing as rt
     from rendiation_gb300 import scenes
 
@@ -160,8 +162,7 @@ def build_heightfield_system(n_grid: int):
         mesh.positions, mesh.indices)])
     t = P.create_top_level_acceleration_structure([rt.TopLevelAccelerationStructureSourceInstance(b)])
     P.bind_tlas([t])
-    P.build(blas_bin_size=4)
-    return mesh, P
+    return mesh, P, compare_builds(P)
 
 
 def reference_counts_of_queues(P, wf, n_secondary):
@@ -197,7 +198,7 @@ def bench_wavefront(args, ws, rank):
     from rendiation_gb300 import scenes
 
     W, H = args.width, args.height
-    mesh, P = build_heightfield_system(args.grid)
+    mesh, P, build = build_heightfield_system(args.grid)
     cam = scenes.heightfield_camera(W, H)
     traversal = {"reference": rt.TRAVERSAL_REFERENCE, "wide": rt.TRAVERSAL_ORDERED_WIDE}.get(
         args.traversal, rt.TRAVERSAL_ORDERED)
@@ -342,8 +343,29 @@ def bench_wavefront(args, ws, rank):
             "peak_kind": peak_kind,
         },
         "clocks": clk.summary(),
+        "build": build,
     }
     return out, P, mesh, cam
+
+
+def compare_builds(P, bin_size=4) -> dict:
+    """Builds P's structure on the host, then on the GPU (the one kept), and
+    checks that the reference-layout arrays of both builds are identical."""
+    t0 = time.perf_counter()
+    P.build(blas_bin_size=bin_size)
+    host_s = time.perf_counter() - t0
+    host = {name: P.built_array(name) for name in ("tri_bvh_forest", "indices_redirect", "tri_bvh_root")}
+    P.build(blas_bin_size=bin_size, device_build=True)  # warm (context, allocator)
+    t0 = time.perf_counter()
+    P.build(blas_bin_size=bin_size, device_build=True)
+    dev_s = time.perf_counter() - t0
+    st = P.build_stats()
+    same = all(P.built_array(name) == data for name, data in host.items())
+    del host
+    return {"host_s": round(host_s, 4), "host_threads": os.cpu_count(), "device_s": round(dev_s, 4),
+            "device_gpu_span_s": round(st["device_seconds"], 5), "speedup": round(host_s / dev_s, 1),
+            "triangles": st["triangles"], "nodes": st["nodes"], "arrays_identical": bool(same),
+            "compared": "tri_bvh_forest, indices_redirect, tri_bvh_root (byte equality)"}
 
 
 def oracle_heightfield(mesh):
@@ -378,9 +400,8 @@ def bench_batched(args):
     handles = [P.create_top_level_acceleration_structure([rt.TopLevelAccelerationStructureSourceInstance(s)])
                for s in range(len(b.meshes))]
     P.bind_tlas(handles)
-    t0 = time.perf_counter()
-    P.build(blas_bin_size=4)
-    build_s = time.perf_counter() - t0
+    build = compare_builds(P)
+    build_s = build["host_s"]
     rays = torch.from_numpy(b.rays.view(np.float32).reshape(-1, 8).copy()).cuda()
     tidx = torch.from_numpy(b.tlas_idx.astype(np.int32)).cuda()
     traversal = {"reference": rt.TRAVERSAL_REFERENCE, "wide": rt.TRAVERSAL_ORDERED_WIDE}.get(
@@ -461,7 +482,7 @@ def bench_batched(args):
         "plain_loop_mrays": round(total / (plain_ms / 1e3) / 1e6, 2),
         "plain_loop_ms": round(plain_ms, 3),
         "speedup_vs_plain_loop": round(plain_ms / batched_ms, 3),
-        "host_build_s": round(build_s, 2),
+        "build": build,
         "escaped_fraction": round(float(np.mean(res_batched["depth_flags"] >> 31)), 4),
         "autotuned": tuned,
     }
@@ -498,7 +519,7 @@ def bench_adjoint(args):
         b = P.create_bottom_level_acceleration_structure([rt.BottomLevelAccelerationStructureBuildSource(
             m.positions, m.indices)])
         P.bind_tlas([P.create_top_level_acceleration_structure([rt.TopLevelAccelerationStructureSourceInstance(b)])])
-        P.build(blas_bin_size=4)
+        P.build(blas_bin_size=4, device_build=True)
         return P
 
     Pt = system(jit)
@@ -578,7 +599,7 @@ def bench_batched_adjoint(args):
                 m.positions, m.indices)])
         P.bind_tlas([P.create_top_level_acceleration_structure([rt.TopLevelAccelerationStructureSourceInstance(s)])
                      for s in range(len(ms))])
-        P.build(blas_bin_size=4)
+        P.build(blas_bin_size=4, device_build=True)
         return P
 
     rays, tidx = [], []
@@ -671,7 +692,7 @@ def batched_gradient_error(P, meshes, rays, tidx, attr, targets, seg, sample=204
     a = attr.cpu().numpy().astype(np.float64)
     tg_all = targets.cpu().numpy().reshape(-1, seg)
     worst_analytic, worst_fd, worst_fd_plain, worst_unc = [], [], [], []
-    p99_analytic, worst_cond = [], []
+    p99_analytic, worst_cond, worst_off_edge, edge_hits = [], [], [], []
     rng = np.random.default_rng(8)
     for s in range(len(meshes)):
         sel = np.nonzero(tidx == s)[0]
@@ -730,6 +751,17 @@ def batched_gradient_error(P, meshes, rays, tidx, attr, targets, seg, sample=204
         worst_analytic.append(float(np.max(rel)))
         p99_analytic.append(float(np.percentile(rel, 99)))
         worst_cond.append(float(np.max(np.linalg.norm(gg - gp, axis=1)[live] / gabs[live])))
+        # a segment that hits an edge shared by two triangles (a barycentric ~ 0)
+        # has two valid closest hits at the same distance; forward and adjoint
+        # may pick different ones (the ordered walks keep either), which moves
+        # that ray's contribution to another triangle's corners
+        edge = np.minimum(np.minimum(u, v), 1 - u - v) < 1e-6
+        near_edge = np.zeros(pos.shape[0], bool)
+        near_edge[tv[edge].reshape(-1)] = True
+        off = live & ~near_edge
+        edge_hits.append(int(edge.sum()))
+        if off.any():
+            worst_off_edge.append(float(np.max(np.linalg.norm(gg - gp, axis=1)[off] / np.maximum(norm[off], floor))))
         # FP64 central differences on 2 random vertices some sampled ray sees; the
         # difference between the Richardson extrapolations from h and h/2 is the
         # differences' own error, reported beside the result
@@ -758,6 +790,8 @@ def batched_gradient_error(P, meshes, rays, tidx, attr, targets, seg, sample=204
             "max_rel_vs_fp64_analytic": max(worst_analytic),
             "p99_rel_vs_fp64_analytic": max(p99_analytic),
             "max_err_over_contribution_abs_sum": max(worst_cond),
+            "max_rel_vs_fp64_analytic_off_edge_hits": max(worst_off_edge) if worst_off_edge else None,
+            "edge_hit_segments": int(sum(edge_hits)),
             "max_rel_vs_fp64_fd_richardson": max(worst_fd),
             "max_rel_vs_fp64_fd_h1e-4": max(worst_fd_plain),
             "max_fd_own_uncertainty": max(worst_unc),

@@ -86,7 +86,8 @@ __device__ __forceinline__ float ff_div(ff a, ff b) { return (a.hi + a.lo) / (b.
 struct HitGeom {
   uint32_t i0, i1, i2;
   float w0, u, v;
-  float3 e1, e2;  // f32 edges (for the adjoint's lambda)
+  ff3 b1, b2;  // e2 x (-d) and (-d) x e1 in float-float (the adjoint's lambda)
+  ff det;      // (-d) . (e1 x e2)
 };
 
 // Hit triangle's vertices and barycentrics re-solved in float-float: with
@@ -119,10 +120,24 @@ __device__ __forceinline__ HitGeom hit_vertices(const TraceParams& p, const uint
   const ff dv = ff3_dot(ND, ff3_cross(E1, S));
   h.u = ff_div(du, det);
   h.v = ff_div(dv, det);
-  h.w0 = 1.0f - h.u - h.v;
-  h.e1 = make_float3(E1.x.hi, E1.y.hi, E1.z.hi);
-  h.e2 = make_float3(E2.x.hi, E2.y.hi, E2.z.hi);
+  // w0 = 1 - u - v without the cancellation near the edge v1-v2 (w0 -> 0),
+  // where f32 would leave it with a large relative error
+  h.w0 = ff_div(ff_add(det, ff_neg(ff_add(du, dv))), det);
+  h.det = det;
+  h.b1 = ff3_cross(E2, ND);
+  h.b2 = ff3_cross(ND, E1);
   return h;
+}
+
+// lambda = M^{-T} (0, gu, gv) = (gu b1 + gv b2) / det, with the cofactors and
+// determinant of the float-float solve: a ray that grazes the triangle makes
+// det a small difference of large products, which f32 would lose. lambda does
+// not depend on the length of d (numerator and det scale alike).
+__device__ __forceinline__ float3 adjoint_lambda(const HitGeom& h, float gu, float gv) {
+  const ff GU{gu, 0.f}, GV{gv, 0.f};
+  return make_float3(ff_div(ff_add(ff_mul(GU, h.b1.x), ff_mul(GV, h.b2.x)), h.det),
+                     ff_div(ff_add(ff_mul(GU, h.b1.y), ff_mul(GV, h.b2.y)), h.det),
+                     ff_div(ff_add(ff_mul(GU, h.b1.z), ff_mul(GV, h.b2.z)), h.det));
 }
 
 template <int MODE>
@@ -192,14 +207,7 @@ __global__ void __launch_bounds__(128) attr_adjoint_kernel(TraceParams p, Adjoin
     const float target = a.targets ? __ldg(a.targets + i) : 0.0f;
     const float r = 2.0f * (value - target) * a.grad_scale;
     const float gu = r * (a1 - a0), gv = r * (a2 - a0);
-    const float3 e1 = h.e1, e2 = h.e2;
-    const float3 nd = make_float3(-ir.d.x, -ir.d.y, -ir.d.z);
-    const float3 c12 = cross3(e1, e2);
-    const float det = dot3(nd, c12);
-    const float3 b1 = cross3(e2, nd), b2 = cross3(nd, e1);
-    const float inv = 1.0f / det;
-    const float3 lam = make_float3((gu * b1.x + gv * b2.x) * inv, (gu * b1.y + gv * b2.y) * inv,
-                                   (gu * b1.z + gv * b2.z) * inv);
+    const float3 lam = adjoint_lambda(h, gu, gv);
     float4* g = reinterpret_cast<float4*>(a.grad_vertices);
     atomicAdd(g + h.i0, make_float4(-h.w0 * lam.x, -h.w0 * lam.y, -h.w0 * lam.z, r * h.w0));
     atomicAdd(g + h.i1, make_float4(-h.u * lam.x, -h.u * lam.y, -h.u * lam.z, r * h.u));
@@ -220,17 +228,11 @@ __global__ void __launch_bounds__(128) attr_adjoint_kernel(TraceParams p, Adjoin
   }
 }
 
-// lambda = M^{-T} (0, gu, gv) with M = [-d | e1 | e2] (d object space,
-// normalised), scattered to the three corners; returns lambda.
+// lambda = M^{-T} (0, gu, gv) with M = [-d | e1 | e2] (object space),
+// scattered to the three corners; returns lambda.
 __device__ __forceinline__ float3 scatter_vertex_grads(const HitGeom& h, const InstanceRay& ir, float r, float gu,
                                                        float gv, float* grad_vertices) {
-  const float3 nd = make_float3(-ir.d.x, -ir.d.y, -ir.d.z);
-  const float3 c12 = cross3(h.e1, h.e2);
-  const float det = dot3(nd, c12);
-  const float3 b1 = cross3(h.e2, nd), b2 = cross3(nd, h.e1);
-  const float inv = 1.0f / det;
-  const float3 lam = make_float3((gu * b1.x + gv * b2.x) * inv, (gu * b1.y + gv * b2.y) * inv,
-                                 (gu * b1.z + gv * b2.z) * inv);
+  const float3 lam = adjoint_lambda(h, gu, gv);
   float4* g = reinterpret_cast<float4*>(grad_vertices);
   atomicAdd(g + h.i0, make_float4(-h.w0 * lam.x, -h.w0 * lam.y, -h.w0 * lam.z, r * h.w0));
   atomicAdd(g + h.i1, make_float4(-h.u * lam.x, -h.u * lam.y, -h.u * lam.z, r * h.u));
