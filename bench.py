@@ -210,18 +210,23 @@ def bench_wavefront(args, ws, rank):
 
         tuner = Autotuner(args.tune_cache)
         cands = grid(traversal=[rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_WIDE], block=[32, 64, 128])
+        # secondary schedule: batches of 32 rays per warp (refill 0) or dynamic fetch
+        cands2 = grid(traversal=[rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_WIDE], block=[32, 64, 128],
+                      refill=[0, 4, 8, 16])
 
         def run_phase(ph):
             def run(c):
                 wf.desc.traversal, wf.desc.block_size = c["traversal"], c["block"]
+                wf.desc.refill = c.get("refill", 0)
                 wf.run(7, phases=ph)
             return run
 
         wf.run(7)
         torch.cuda.synchronize()
         t1 = tuner.tune("wavefront-primary", cands, run_phase(1))
-        t2 = tuner.tune("wavefront-secondary", cands, run_phase(2))
-        wf.configure((t1.best["traversal"], t1.best["block"]), (t2.best["traversal"], t2.best["block"]))
+        t2 = tuner.tune("wavefront-secondary", cands2, run_phase(2))
+        wf.configure((t1.best["traversal"], t1.best["block"]), (t2.best["traversal"], t2.best["block"]),
+                     refill=t2.best.get("refill", 0))
         tuned = {"primary": t1.best, "secondary": t2.best}
 
     # one frame to learn the ray counts, then the reference-order visit counts of those rays
@@ -493,7 +498,8 @@ def bench_adjoint(args):
     per-vertex attribute uniform in [0,1], 512x512 primary rays, loss =
     sum (interpolated attribute - target)^2 with the target rendered from a
     copy whose heights are jittered by N(0, 0.005). Forward alone against
-    forward + adjoint (hits recomputed in the adjoint)."""
+    forward + adjoint, the adjoint differentiating the hits the forward
+    recorded (and, for comparison, tracing them again)."""
     import ctypes as C
 
     import torch
@@ -532,22 +538,30 @@ def bench_adjoint(args):
     P = system(mesh)
     loss = torch.zeros(1, dtype=torch.float64, device="cuda")
     grad = torch.zeros((mesh.positions.shape[0], 4), device="cuda")
+    hit_tri = torch.zeros(n, dtype=torch.int32, device="cuda")
+    hit_inst = torch.zeros(n, dtype=torch.int32, device="cuda")
     fwd = native.AttrLossDesc(rays.data_ptr(), n, 0, attr.data_ptr(), target.data_ptr(), None, None,
                               loss.data_ptr(), None, None, None, 1.0, traversal, 0, 0)
+    fwd_rec = native.AttrLossDesc(rays.data_ptr(), n, 0, attr.data_ptr(), target.data_ptr(), None, None,
+                                  loss.data_ptr(), None, None, None, 1.0, traversal, 0, 0, hit_tri.data_ptr(),
+                                  hit_inst.data_ptr())
     adj = native.AttrLossDesc(rays.data_ptr(), n, 0, attr.data_ptr(), target.data_ptr(), None, None, None,
                               grad.data_ptr(), None, None, 1.0, traversal, 0, 0)
+    adj_rec = native.AttrLossDesc(rays.data_ptr(), n, 0, attr.data_ptr(), target.data_ptr(), None, None, None,
+                                  grad.data_ptr(), None, None, 1.0, traversal, 0, 1, hit_tri.data_ptr(),
+                                  hit_inst.data_ptr())
     stream = torch.cuda.current_stream()
     sp = C.c_void_p(stream.cuda_stream)
 
-    def run(with_adjoint):
+    def run(mode):
         loss.zero_()
-        assert L.rdn_attr_loss_forward(P._h, C.byref(fwd), sp) == 0
-        if with_adjoint:
+        assert L.rdn_attr_loss_forward(P._h, C.byref(fwd_rec if mode == "tape" else fwd), sp) == 0
+        if mode != "forward":
             grad.zero_()
-            assert L.rdn_attr_loss_adjoint(P._h, C.byref(adj), sp) == 0
+            assert L.rdn_attr_loss_adjoint(P._h, C.byref(adj_rec if mode == "tape" else adj), sp) == 0
 
     out = {}
-    for name, w in (("forward", False), ("forward_adjoint", True)):
+    for name, w in (("forward", "forward"), ("forward_adjoint", "tape"), ("forward_adjoint_retrace", "retrace")):
         for _ in range(args.warmup):
             run(w)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -560,6 +574,8 @@ def bench_adjoint(args):
         out[name + "_ms"] = round(e0.elapsed_time(e1) / reps, 4)
         out[name + "_mrays"] = round(n / (e0.elapsed_time(e1) / reps / 1e3) / 1e6, 2)
     out["fwd_adjoint_over_fwd"] = round(out["forward_adjoint_ms"] / out["forward_ms"], 3)
+    out["fwd_adjoint_retrace_over_fwd"] = round(out["forward_adjoint_retrace_ms"] / out["forward_ms"], 3)
+    out["adjoint"] = "from the forward's recorded hits (8 B per ray); _retrace: hits traced again"
     out["loss"] = float(loss.item())
     out["workload"] = f"heightfield {n_grid}^2 ({mesh.triangle_count} tris), {res}x{res} rays, attribute loss"
     P.close()
@@ -572,7 +588,8 @@ def bench_batched_adjoint(args):
     per-vertex attribute and 64k..1M primary rays (log-uniform) plus 2 diffuse
     bounces; targets are the same paths' values on copies with heights jittered
     by N(0, 0.005). Forward + adjoint of all scenes in one captured CUDA graph,
-    hits recomputed in the adjoint. Gradient error per scene against FP64 on a
+    the adjoint differentiating the segments the forward recorded (and, for
+    comparison, tracing the paths again). Gradient error per scene against FP64 on a
     sample of 2048 paths per scene (analytic FP64 gradient over the sample, and
     FP64 central differences, h = 1e-4 with Richardson extrapolation, on 2
     vertices per scene)."""
@@ -636,16 +653,25 @@ def bench_batched_adjoint(args):
     as_bytes = P.device_bytes()
     loss = torch.zeros(1, dtype=torch.float64, device="cuda")
     grad = torch.zeros((nv, 4), device="cuda")
-    both = desc(targets=targets.data_ptr(), loss_sum=loss.data_ptr(), grad_vertices=grad.data_ptr())
+    # the forward's record of every segment (triangle, instance, ray): 40 B per segment
+    tape_tri = torch.zeros(n * seg, dtype=torch.int32, device="cuda")
+    tape_inst = torch.zeros(n * seg, dtype=torch.int32, device="cuda")
+    tape_rays = torch.zeros((n * seg, 8), device="cuda")
+    tape = dict(seg_tri=tape_tri.data_ptr(), seg_inst=tape_inst.data_ptr(), seg_rays=tape_rays.data_ptr())
+    both = desc(targets=targets.data_ptr(), loss_sum=loss.data_ptr(), grad_vertices=grad.data_ptr(), from_record=1,
+                **tape)
+    retrace = desc(targets=targets.data_ptr(), loss_sum=loss.data_ptr(), grad_vertices=grad.data_ptr())
     fwd = desc(targets=targets.data_ptr(), loss_sum=loss.data_ptr())
     g = C.c_void_p()
     assert L.rdn_attr_paths_graph(P._h, C.byref(both), nv, C.byref(g)) == 0
+    gr = C.c_void_p()
+    assert L.rdn_attr_paths_graph(P._h, C.byref(retrace), nv, C.byref(gr)) == 0
     gf = C.c_void_p()
     assert L.rdn_attr_paths_graph(P._h, C.byref(fwd), nv, C.byref(gf)) == 0
     stream = torch.cuda.current_stream()
     sp = C.c_void_p(stream.cuda_stream)
     out = {}
-    for name, handle in (("forward", gf), ("forward_adjoint", g)):
+    for name, handle in (("forward", gf), ("forward_adjoint", g), ("forward_adjoint_retrace", gr)):
         for _ in range(args.warmup):
             L.rdn_graph_launch(handle, sp)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -656,7 +682,9 @@ def bench_batched_adjoint(args):
         torch.cuda.synchronize()
         out[name + "_ms"] = round(e0.elapsed_time(e1) / 5, 3)
     L.rdn_graph_destroy(g)
+    L.rdn_graph_destroy(gr)
     L.rdn_graph_destroy(gf)
+    del tape_tri, tape_inst, tape_rays
     # segments traced per step (one forward pass records the segment triangles)
     seg_tri = torch.zeros(n * seg, dtype=torch.int32, device="cuda")
     assert L.rdn_attr_paths_forward(P._h, C.byref(desc(seg_tri=seg_tri.data_ptr())), None) == 0
@@ -668,6 +696,10 @@ def bench_batched_adjoint(args):
     out["forward_mrays"] = round(traced / (out["forward_ms"] / 1e3) / 1e6, 2)
     out["forward_adjoint_mrays"] = round(traced / (out["forward_adjoint_ms"] / 1e3) / 1e6, 2)
     out["fwd_adjoint_over_fwd"] = round(out["forward_adjoint_ms"] / out["forward_ms"], 3)
+    out["forward_adjoint_retrace_mrays"] = round(traced / (out["forward_adjoint_retrace_ms"] / 1e3) / 1e6, 2)
+    out["fwd_adjoint_retrace_over_fwd"] = round(out["forward_adjoint_retrace_ms"] / out["forward_ms"], 3)
+    out["adjoint"] = ("from the forward's record of every segment (triangle, instance, ray; 40 B per segment), "
+                      "one graph for forward + adjoint; _retrace: the adjoint traces the paths again")
     out["peak_hbm_bytes"] = int(torch.cuda.max_memory_allocated() + as_bytes)
     out["workload"] = (f"{n_scenes} heightfields {int(grids.min())}^2..{int(grids.max())}^2 "
                        f"({sum(m.triangle_count for m in meshes)} tris), {n} primaries, 2 bounces")
@@ -693,6 +725,7 @@ def batched_gradient_error(P, meshes, rays, tidx, attr, targets, seg, sample=204
     tg_all = targets.cpu().numpy().reshape(-1, seg)
     worst_analytic, worst_fd, worst_fd_plain, worst_unc = [], [], [], []
     p99_analytic, worst_cond, worst_off_edge, edge_hits = [], [], [], []
+    worst_detail = {}
     rng = np.random.default_rng(8)
     for s in range(len(meshes)):
         sel = np.nonzero(tidx == s)[0]
@@ -709,12 +742,16 @@ def batched_gradient_error(P, meshes, rays, tidx, attr, targets, seg, sample=204
         d.rays, d.tlas_idx, d.count, d.segments, d.seed, d.grad_scale = d_r.data_ptr(), d_t.data_ptr(), m, seg, 5, 1.0
         d.attributes, d.targets = attr.data_ptr(), d_tg.data_ptr()
         d.seg_tri, d.seg_rays = seg_tri.data_ptr(), seg_rays.data_ptr()
+        seg_inst = torch.zeros(m * seg, dtype=torch.int32, device="cuda")
+        seg_val = torch.zeros(m * seg, device="cuda")
+        d.seg_inst, d.values = seg_inst.data_ptr(), seg_val.data_ptr()
         assert L.rdn_attr_paths_forward(P._h, C.byref(d), None) == 0
-        d.seg_tri, d.seg_rays, d.grad_vertices = None, None, grad.data_ptr()
+        d.grad_vertices, d.from_record = grad.data_ptr(), 1
         assert L.rdn_attr_paths_adjoint(P._h, C.byref(d), None) == 0
         torch.cuda.synchronize()
         tri = seg_tri.cpu().numpy().view(np.uint32)
         alive = tri != 0xFFFFFFFF
+        seg_vals = seg_val.cpu().numpy().astype(np.float64)
         rr = seg_rays.cpu().numpy().reshape(-1, 8)[alive].astype(np.float64)
         t_ = tri[alive].astype(np.int64)
         tg = d_tg.cpu().numpy().astype(np.float64)[alive]
@@ -748,6 +785,15 @@ def batched_gradient_error(P, meshes, rays, tidx, attr, targets, seg, sample=204
         live = norm > 0
         floor = 1e-2 * np.median(norm[live]) if live.any() else 1.0
         rel = np.linalg.norm(gg - gp, axis=1)[live] / np.maximum(norm[live], floor)
+        if float(np.max(rel)) > worst_detail.get("rel", -1.0):
+            wv = np.nonzero(live)[0][int(np.argmax(rel))]
+            contrib = np.sum(tv == wv)
+            vals = np.array(seg_vals)[alive] if seg_vals is not None else None
+            worst_detail.update({"rel": float(np.max(rel)), "scene": s, "segments_at_vertex": int(contrib),
+                                 "grad_norm_over_floor": float(norm[wv] / floor),
+                                 "abs_sum_over_grad_norm": float(gabs[wv] / max(norm[wv], 1e-300)),
+                                 "max_value_error_of_scene": (float(np.max(np.abs(vals - val)))
+                                                              if vals is not None else None)})
         worst_analytic.append(float(np.max(rel)))
         p99_analytic.append(float(np.percentile(rel, 99)))
         worst_cond.append(float(np.max(np.linalg.norm(gg - gp, axis=1)[live] / gabs[live])))
@@ -792,6 +838,7 @@ def batched_gradient_error(P, meshes, rays, tidx, attr, targets, seg, sample=204
             "max_err_over_contribution_abs_sum": max(worst_cond),
             "max_rel_vs_fp64_analytic_off_edge_hits": max(worst_off_edge) if worst_off_edge else None,
             "edge_hit_segments": int(sum(edge_hits)),
+            "worst_vertex": worst_detail,
             "max_rel_vs_fp64_fd_richardson": max(worst_fd),
             "max_rel_vs_fp64_fd_h1e-4": max(worst_fd_plain),
             "max_fd_own_uncertainty": max(worst_unc),

@@ -294,7 +294,9 @@ typedef struct rdn_wavefront_desc {
   uint32_t* ray_counts;      /* device, nullable: [primary, shadow, bounce] rays traced */
   uint32_t phases;           /* 0 = both; bit 0: primary kernel (raygen, trace, shade, enqueue),
                                 bit 1: secondary kernel (shadow + bounce queues of the last primary run) */
-  uint32_t reserved;
+  uint32_t refill;           /* secondary schedule of the ordered walks: 0 = each warp traces 32 queued
+                                rays together; k in 1..32 = each lane keeps its own traversal state and
+                                a warp takes new rays whenever k lanes are idle (dynamic fetch) */
 } rdn_wavefront_desc;
 
 /* Scratch size for the secondary-ray queues of a width x height launch. */
@@ -390,14 +392,18 @@ typedef struct rdn_attr_loss_desc {
   float grad_scale;             /* upstream gradient of the loss sum (adjoint), usually 1 */
   uint32_t traversal;           /* RDN_TRAVERSAL_* */
   uint32_t block_size;          /* 0 = 64 */
-  uint32_t reserved;
+  uint32_t from_record;         /* adjoint: 1 = differentiate the hits recorded by the forward in
+                                   hit_tri / hit_inst instead of tracing the rays again */
+  uint32_t* hit_tri;            /* device, nullable: built triangle of each ray's hit, RDN_MISS (forward) */
+  uint32_t* hit_inst;           /* device, nullable: TLAS instance slot of each ray's hit (forward) */
 } rdn_attr_loss_desc;
 
 /* Forward: trace, interpolate, loss. Extends the reference's closest-hit query
  * (traverse_cpu.rs:52-245) with a differentiable attribute read-out. */
 rdn_status rdn_attr_loss_forward(rdn_ctx* ctx, const rdn_attr_loss_desc* desc, void* stream);
 /* Adjoint at frozen visibility: re-traces every ray (the hit is recomputed, not
- * stored), then scatters gradients with respect to vertex positions and
+ * stored) or, with from_record, takes the hits the forward wrote to hit_tri /
+ * hit_inst; then scatters gradients with respect to vertex positions and
  * attributes and writes per-ray gradients with respect to origin and direction
  * (object space of the hit instance). */
 rdn_status rdn_attr_loss_adjoint(rdn_ctx* ctx, const rdn_attr_loss_desc* desc, void* stream);
@@ -428,7 +434,9 @@ typedef struct rdn_attr_path_desc {
   float grad_scale;
   uint32_t traversal;
   uint32_t block_size;          /* 0 = 64 */
-  uint32_t reserved;
+  uint32_t from_record;         /* adjoint: 1 = differentiate the segments recorded by the forward in
+                                   seg_tri / seg_inst / seg_rays (a tape) instead of tracing the paths again */
+  uint32_t* seg_inst;           /* device, nullable: TLAS instance slot of each segment's hit (forward) */
 } rdn_attr_path_desc;
 
 rdn_status rdn_attr_paths_forward(rdn_ctx* ctx, const rdn_attr_path_desc* desc, void* stream);

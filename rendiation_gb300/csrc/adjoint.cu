@@ -88,18 +88,19 @@ struct HitGeom {
   float w0, u, v;
   ff3 b1, b2;  // e2 x (-d) and (-d) x e1 in float-float (the adjoint's lambda)
   ff det;      // (-d) . (e1 x e2)
+  float t_unnorm;  // hit distance in units of the unnormalised object-space direction
 };
 
 // Hit triangle's vertices and barycentrics re-solved in float-float: with
 // M = [-d | e1 | e2] and s = o - v0, u = det[-d, s, e2] / det M and
 // v = det[-d, e1, s] / det M (Cramer), e1, e2, s formed exactly. Cramer's rule
 // does not depend on the length of d, so d is the object-space direction before
-// normalisation (exact for an identity instance).
-__device__ __forceinline__ HitGeom hit_vertices(const TraceParams& p, const uint32_t* __restrict__ indices,
-                                                const float* __restrict__ vertices, const RayCtx& R,
-                                                const InstanceRay& ir) {
+// normalisation (exact for an identity instance). `tri` is the built triangle
+// index, `inst` the TLAS instance slot of the hit, d_world the ray direction.
+__device__ __forceinline__ HitGeom hit_vertices_at(const TraceParams& p, const uint32_t* __restrict__ indices,
+                                                   const float* __restrict__ vertices, uint32_t tri, uint32_t inst,
+                                                   float3 d_world, const InstanceRay& ir) {
   HitGeom h;
-  const uint32_t tri = __ldg(p.redirect + R.best.k);
   h.i0 = __ldg(indices + 3 * (size_t)tri);
   h.i1 = __ldg(indices + 3 * (size_t)tri + 1);
   h.i2 = __ldg(indices + 3 * (size_t)tri + 2);
@@ -110,14 +111,17 @@ __device__ __forceinline__ HitGeom hit_vertices(const TraceParams& p, const uint
   const float3 v2 = make_float3(__ldg(vertices + 3 * (size_t)h.i2), __ldg(vertices + 3 * (size_t)h.i2 + 1),
                                 __ldg(vertices + 3 * (size_t)h.i2 + 2));
   const ff3 E1 = ff3_sub(v1, v0), E2 = ff3_sub(v2, v0), S = ff3_sub(ir.o, v0);
-  const float* m = p.tlas_data[R.best.inst].transform_inv;
-  const float3 dobj = make_float3(R.d.x * __ldg(m + 0) + R.d.y * __ldg(m + 4) + R.d.z * __ldg(m + 8),
-                                  R.d.x * __ldg(m + 1) + R.d.y * __ldg(m + 5) + R.d.z * __ldg(m + 9),
-                                  R.d.x * __ldg(m + 2) + R.d.y * __ldg(m + 6) + R.d.z * __ldg(m + 10));
+  const float* m = p.tlas_data[inst].transform_inv;
+  const float3 dobj = make_float3(d_world.x * __ldg(m + 0) + d_world.y * __ldg(m + 4) + d_world.z * __ldg(m + 8),
+                                  d_world.x * __ldg(m + 1) + d_world.y * __ldg(m + 5) + d_world.z * __ldg(m + 9),
+                                  d_world.x * __ldg(m + 2) + d_world.y * __ldg(m + 6) + d_world.z * __ldg(m + 10));
   const ff3 ND = ff3_of(make_float3(-dobj.x, -dobj.y, -dobj.z));
-  const ff det = ff3_dot(ND, ff3_cross(E1, E2));
+  const ff3 C12 = ff3_cross(E1, E2);
+  const ff det = ff3_dot(ND, C12);
   const ff du = ff3_dot(ND, ff3_cross(S, E2));
   const ff dv = ff3_dot(ND, ff3_cross(E1, S));
+  // distance along the unnormalised object-space direction (t = det[s, e1, e2] / det M)
+  h.t_unnorm = ff_div(ff3_dot(S, C12), det);
   h.u = ff_div(du, det);
   h.v = ff_div(dv, det);
   // w0 = 1 - u - v without the cancellation near the edge v1-v2 (w0 -> 0),
@@ -127,6 +131,12 @@ __device__ __forceinline__ HitGeom hit_vertices(const TraceParams& p, const uint
   h.b1 = ff3_cross(E2, ND);
   h.b2 = ff3_cross(ND, E1);
   return h;
+}
+
+__device__ __forceinline__ HitGeom hit_vertices(const TraceParams& p, const uint32_t* __restrict__ indices,
+                                                const float* __restrict__ vertices, const RayCtx& R,
+                                                const InstanceRay& ir) {
+  return hit_vertices_at(p, indices, vertices, __ldg(p.redirect + R.best.k), R.best.inst, R.d, ir);
 }
 
 // lambda = M^{-T} (0, gu, gv) = (gu b1 + gv b2) / det, with the cofactors and
@@ -166,6 +176,8 @@ __global__ void __launch_bounds__(128) attr_forward_kernel(TraceParams p, Adjoin
       const float diff = value - (a.targets ? __ldg(a.targets + i) : 0.0f);
       loss = diff * diff;
     }
+    if (a.hit_tri) a.hit_tri[i] = R.best.have ? __ldg(p.redirect + R.best.k) : INVALID_NEXT;
+    if (a.hit_inst) a.hit_inst[i] = R.best.have ? R.best.inst : INVALID_NEXT;
     if (a.ray_value) a.ray_value[i] = value;
     if (a.ray_loss) a.ray_loss[i] = loss;
   }
@@ -261,7 +273,7 @@ __global__ void __launch_bounds__(128) attr_path_kernel(TraceParams p, PathAdjoi
     for (uint32_t k = 0; k < a.segments; k++) {
       const size_t seg = (size_t)i * a.segments + k;
       float value = 0.0f;
-      uint32_t tri_out = INVALID_NEXT;
+      uint32_t tri_out = INVALID_NEXT, inst_out = INVALID_NEXT;
       if (alive) {
         if (a.seg_rays) {
           a.seg_rays[2 * seg] = r0;
@@ -286,6 +298,7 @@ __global__ void __launch_bounds__(128) attr_path_kernel(TraceParams p, PathAdjoi
           const InstanceRay ir = to_instance(p.tlas_data + R.best.inst, R.o, R.d, 0u);
           const HitGeom h = hit_vertices(p, a.indices, a.vertices, R, ir);
           tri_out = __ldg(p.redirect + R.best.k);
+          inst_out = R.best.inst;
           const float a0 = __ldg(a.attributes + h.i0), a1 = __ldg(a.attributes + h.i1),
                       a2 = __ldg(a.attributes + h.i2);
           value = h.w0 * a0 + h.u * a1 + h.v * a2;
@@ -316,6 +329,7 @@ __global__ void __launch_bounds__(128) attr_path_kernel(TraceParams p, PathAdjoi
       }
       if (!ADJOINT && a.values) a.values[seg] = value;
       if (!ADJOINT && a.seg_tri) a.seg_tri[seg] = tri_out;
+      if (!ADJOINT && a.seg_inst) a.seg_inst[seg] = inst_out;
     }
   }
   if (!ADJOINT && a.loss_sum) {
@@ -329,6 +343,68 @@ __global__ void __launch_bounds__(128) attr_path_kernel(TraceParams p, PathAdjoi
       atomicAdd(a.loss_sum, t);
     }
   }
+}
+
+// Adjoint from the forward's record (a tape): every recorded segment is
+// differentiated at the triangle and instance the forward hit, with no second
+// traversal. One thread per segment; misses were recorded as ~0 and add
+// nothing. The forward and the adjoint therefore always agree on visibility,
+// also where two triangles meet the ray at exactly the same distance.
+__global__ void __launch_bounds__(256) attr_path_recorded_kernel(TraceParams p, PathAdjointParams a) {
+  const size_t total = (size_t)a.count * a.segments;
+  for (size_t seg = blockIdx.x * (size_t)blockDim.x + threadIdx.x; seg < total; seg += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t tri = __ldg(a.seg_tri + seg);
+    if (tri == INVALID_NEXT) continue;
+    const uint32_t inst = __ldg(a.seg_inst + seg);
+    const float4 r0 = __ldg(a.seg_rays + 2 * seg), r1 = __ldg(a.seg_rays + 2 * seg + 1);
+    const float3 o = make_float3(r0.x, r0.y, r0.z), d = make_float3(r1.x, r1.y, r1.z);
+    const InstanceRay ir = to_instance(p.tlas_data + inst, o, d, 0u);
+    const HitGeom h = hit_vertices_at(p, a.indices, a.vertices, tri, inst, d, ir);
+    const float a0 = __ldg(a.attributes + h.i0), a1 = __ldg(a.attributes + h.i1), a2 = __ldg(a.attributes + h.i2);
+    const float value = h.w0 * a0 + h.u * a1 + h.v * a2;
+    const float target = a.targets ? __ldg(a.targets + seg) : 0.0f;
+    const float r = 2.0f * (value - target) * a.grad_scale;
+    scatter_vertex_grads(h, ir, r, r * (a1 - a0), r * (a2 - a0), a.grad_vertices);
+  }
+}
+
+__global__ void __launch_bounds__(256) attr_recorded_adjoint_kernel(TraceParams p, AdjointParams a) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.count; i += gridDim.x * blockDim.x) {
+    const uint32_t tri = __ldg(a.hit_tri + i);
+    float3 go = make_float3(0.f, 0.f, 0.f), gd = go;
+    if (tri != INVALID_NEXT) {
+      const uint32_t inst = __ldg(a.hit_inst + i);
+      const float4 r0 = __ldg(a.rays + 2 * (size_t)i), r1 = __ldg(a.rays + 2 * (size_t)i + 1);
+      const float3 o = make_float3(r0.x, r0.y, r0.z), d = make_float3(r1.x, r1.y, r1.z);
+      const InstanceRay ir = to_instance(p.tlas_data + inst, o, d, 0u);
+      const HitGeom h = hit_vertices_at(p, a.indices, a.vertices, tri, inst, d, ir);
+      const float a0 = __ldg(a.attributes + h.i0), a1 = __ldg(a.attributes + h.i1), a2 = __ldg(a.attributes + h.i2);
+      const float value = h.w0 * a0 + h.u * a1 + h.v * a2;
+      const float target = a.targets ? __ldg(a.targets + i) : 0.0f;
+      const float r = 2.0f * (value - target) * a.grad_scale;
+      const float3 lam = scatter_vertex_grads(h, ir, r, r * (a1 - a0), r * (a2 - a0), a.grad_vertices);
+      // object-space distance along the normalised direction: t_unnorm * |M3 d|
+      const float t_obj = h.t_unnorm * ir.scaling;
+      go = lam;
+      gd = make_float3(t_obj * lam.x, t_obj * lam.y, t_obj * lam.z);
+    }
+    if (a.grad_ray_origin) {
+      a.grad_ray_origin[3 * (size_t)i] = go.x;
+      a.grad_ray_origin[3 * (size_t)i + 1] = go.y;
+      a.grad_ray_origin[3 * (size_t)i + 2] = go.z;
+    }
+    if (a.grad_ray_direction) {
+      a.grad_ray_direction[3 * (size_t)i] = gd.x;
+      a.grad_ray_direction[3 * (size_t)i + 1] = gd.y;
+      a.grad_ray_direction[3 * (size_t)i + 2] = gd.z;
+    }
+  }
+}
+
+inline uint32_t recorded_grid(size_t items, int sm_count) {
+  const size_t need = (items + 255) / 256;
+  const size_t cap = (size_t)(sm_count > 0 ? sm_count : 1) * 16;
+  return (uint32_t)(need < cap ? (need ? need : 1) : cap);
 }
 
 template <int MODE>
@@ -389,6 +465,10 @@ cudaError_t launch_attr(const TraceParams& p, const AdjointParams& a, int mode, 
 cudaError_t launch_attr_paths(const TraceParams& p, const PathAdjointParams& a, int mode, bool adjoint,
                               uint32_t block, int sm_count, cudaStream_t stream) {
   if (a.count == 0) return cudaSuccess;
+  if (adjoint && a.from_record) {
+    attr_path_recorded_kernel<<<recorded_grid((size_t)a.count * a.segments, sm_count), 256, 0, stream>>>(p, a);
+    return cudaGetLastError();
+  }
   if (block == 0) block = 64;
   if (mode == MODE_WIDE4) return launch_attr_paths_mode<MODE_WIDE4>(p, a, adjoint, block, sm_count, stream);
   if (mode == MODE_BINARY) return launch_attr_paths_mode<MODE_BINARY>(p, a, adjoint, block, sm_count, stream);
@@ -401,7 +481,12 @@ cudaError_t launch_attr_forward(const TraceParams& p, const AdjointParams& a, in
 }
 
 cudaError_t launch_attr_adjoint(const TraceParams& p, const AdjointParams& a, int mode, uint32_t block,
-                                cudaStream_t stream) {
+                                int sm_count, cudaStream_t stream) {
+  if (a.from_record) {
+    if (a.count == 0) return cudaSuccess;
+    attr_recorded_adjoint_kernel<<<recorded_grid(a.count, sm_count), 256, 0, stream>>>(p, a);
+    return cudaGetLastError();
+  }
   return launch_attr(p, a, mode, true, block, stream);
 }
 

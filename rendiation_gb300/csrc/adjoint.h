@@ -22,6 +22,9 @@ struct AdjointParams {
   float* grad_ray_origin;     // 3 per ray, nullable
   float* grad_ray_direction;  // 3 per ray, nullable
   float grad_scale;           // upstream gradient of the loss sum
+  uint32_t* hit_tri;          // per ray, nullable: built triangle of the hit or ~0 (written by the forward)
+  uint32_t* hit_inst;         // per ray, nullable: instance slot of the hit (written by the forward)
+  bool from_record;           // adjoint: differentiate the recorded hits instead of tracing again
 };
 
 // Multi-segment, multi-scene form: every path is a primary ray (its own TLAS
@@ -29,7 +32,9 @@ struct AdjointParams {
 // (value - target)^2. Bounce rays depend on the hit like the path executor's
 // (facing normal, offset origin, sampler xxhash32(id, k, seed)); the adjoint
 // treats each segment's ray as fixed (gradients do not flow through the bounce
-// directions) and recomputes every hit by tracing the path again.
+// directions) and either recomputes every hit by tracing the path again or,
+// with from_record, differentiates the hits the forward recorded in seg_tri,
+// seg_inst and seg_rays.
 struct PathAdjointParams {
   const float4* rays;         // 2 per path
   const uint32_t* tlas_idx;   // per path, nullable
@@ -43,6 +48,8 @@ struct PathAdjointParams {
   float* grad_vertices;       // 4 per vertex (adjoint)
   uint32_t* seg_tri;          // segments per path, nullable: triangle index of each segment's hit (or ~0)
   float4* seg_rays;           // 2 float4 per segment per path, nullable
+  uint32_t* seg_inst;         // segments per path, nullable: instance slot of each segment's hit
+  bool from_record;           // adjoint: use seg_tri / seg_inst / seg_rays instead of tracing again
   float grad_scale;
   uint32_t* work_counter;     // persistent work distribution (reset by the launcher)
 };
@@ -53,6 +60,6 @@ cudaError_t launch_attr_paths(const TraceParams& p, const PathAdjointParams& a, 
 cudaError_t launch_attr_forward(const TraceParams& p, const AdjointParams& a, int mode, uint32_t block,
                                 cudaStream_t stream);
 cudaError_t launch_attr_adjoint(const TraceParams& p, const AdjointParams& a, int mode, uint32_t block,
-                                cudaStream_t stream);
+                                int sm_count, cudaStream_t stream);
 
 }  // namespace rdn

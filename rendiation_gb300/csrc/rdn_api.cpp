@@ -497,6 +497,7 @@ rdn_status rdn_wavefront_shadow_bounce(rdn_ctx* c, const rdn_wavefront_desc* d, 
     return fail(c, RDN_ERR_INVALID_ARG, "scratch must be 256-byte and output 16-byte aligned");
   if (d->traversal > RDN_TRAVERSAL_ORDERED_WIDE) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
   if (d->phases > 3) return fail(c, RDN_ERR_INVALID_ARG, "unknown phase mask");
+  if (d->refill > 32) return fail(c, RDN_ERR_INVALID_ARG, "refill must be 0..32");
   if (d->block_size && (d->block_size % 32 || d->block_size > 128))
     return fail(c, RDN_ERR_INVALID_ARG, "block_size must be a multiple of 32 up to 128");
   std::lock_guard<std::mutex> lk(c->lock);
@@ -525,6 +526,7 @@ rdn_status rdn_wavefront_shadow_bounce(rdn_ctx* c, const rdn_wavefront_desc* d, 
   w.tlas = d->tlas_uniform;
   w.out = reinterpret_cast<rdn::PixelResult*>(d->out);
   w.ray_counts = d->ray_counts;
+  w.refill = d->refill;
   rdn::wavefront_bind_scratch(w, d->scratch);
   cudaError_t e = cudaSetDevice(c->device);
   if (e == cudaSuccess)
@@ -683,6 +685,9 @@ rdn_status prepare_attr(rdn_ctx* c, const rdn_attr_loss_desc* d, bool adjoint, r
   if (adjoint && d->count && !d->grad_vertices) return fail(c, RDN_ERR_INVALID_ARG, "null gradient buffer");
   if ((reinterpret_cast<uintptr_t>(d->rays) & 15) || (reinterpret_cast<uintptr_t>(d->grad_vertices) & 15))
     return fail(c, RDN_ERR_INVALID_ARG, "rays and gradients must be 16-byte aligned");
+  if (d->from_record > 1) return fail(c, RDN_ERR_INVALID_ARG, "from_record must be 0 or 1");
+  if (adjoint && d->from_record && d->count && (!d->hit_tri || !d->hit_inst))
+    return fail(c, RDN_ERR_INVALID_ARG, "from_record needs the hit_tri and hit_inst records of the forward");
   if (d->traversal > RDN_TRAVERSAL_ORDERED_WIDE) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
   if (d->block_size && (d->block_size % 32 || d->block_size > 128))
     return fail(c, RDN_ERR_INVALID_ARG, "block_size must be a multiple of 32 up to 128");
@@ -709,6 +714,9 @@ rdn_status prepare_attr(rdn_ctx* c, const rdn_attr_loss_desc* d, bool adjoint, r
   a.grad_ray_origin = d->grad_ray_origin;
   a.grad_ray_direction = d->grad_ray_direction;
   a.grad_scale = d->grad_scale;
+  a.hit_tri = d->hit_tri;
+  a.hit_inst = d->hit_inst;
+  a.from_record = d->from_record != 0;
   return RDN_OK;
 }
 
@@ -739,7 +747,8 @@ rdn_status rdn_attr_loss_adjoint(rdn_ctx* c, const rdn_attr_loss_desc* d, void* 
   if (st != RDN_OK) return st;
   cudaError_t e = cudaSetDevice(c->device);
   if (e == cudaSuccess)
-    e = rdn::launch_attr_adjoint(p, a, mode_of(d->traversal), d->block_size, static_cast<cudaStream_t>(stream));
+    e = rdn::launch_attr_adjoint(p, a, mode_of(d->traversal), d->block_size, c->sm_count,
+                                 static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(c, e, "attribute loss adjoint");
   return RDN_OK;
 }
@@ -761,6 +770,9 @@ rdn_status prepare_attr_paths(rdn_ctx* c, const rdn_attr_path_desc* d, bool adjo
   if (d->traversal > RDN_TRAVERSAL_ORDERED_WIDE) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
   if (d->block_size && (d->block_size % 32 || d->block_size > 128))
     return fail(c, RDN_ERR_INVALID_ARG, "block_size must be a multiple of 32 up to 128");
+  if (d->from_record > 1) return fail(c, RDN_ERR_INVALID_ARG, "from_record must be 0 or 1");
+  if (adjoint && d->from_record && d->count && (!d->seg_tri || !d->seg_inst || !d->seg_rays))
+    return fail(c, RDN_ERR_INVALID_ARG, "from_record needs the seg_tri, seg_inst and seg_rays records of the forward");
   rdn_status st = ensure_built(c);
   if (st != RDN_OK) return st;
   rdn_trace_desc td;
@@ -785,6 +797,8 @@ rdn_status prepare_attr_paths(rdn_ctx* c, const rdn_attr_path_desc* d, bool adjo
   a.grad_vertices = d->grad_vertices;
   a.seg_tri = d->seg_tri;
   a.seg_rays = reinterpret_cast<float4*>(d->seg_rays);
+  a.seg_inst = d->seg_inst;
+  a.from_record = d->from_record != 0;
   a.grad_scale = d->grad_scale;
   a.work_counter = c->d_counters + 12;
   return RDN_OK;
@@ -941,6 +955,7 @@ rdn_status rdn_wavefront_shadow_bounce_static(rdn_ctx* c, const rdn_wavefront_de
   if (reinterpret_cast<uintptr_t>(d->out) & 15) return fail(c, RDN_ERR_INVALID_ARG, "output must be 16-byte aligned");
   if (d->traversal > RDN_TRAVERSAL_ORDERED_WIDE) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
   if (d->phases > 3) return fail(c, RDN_ERR_INVALID_ARG, "unknown phase mask");
+  if (d->refill > 32) return fail(c, RDN_ERR_INVALID_ARG, "refill must be 0..32");
   if (d->block_size && (d->block_size % 32 || d->block_size > 128))
     return fail(c, RDN_ERR_INVALID_ARG, "block_size must be a multiple of 32 up to 128");
   std::lock_guard<std::mutex> lk(c->lock);
@@ -969,6 +984,7 @@ rdn_status rdn_wavefront_shadow_bounce_static(rdn_ctx* c, const rdn_wavefront_de
   w.tlas = d->tlas_uniform;
   w.out = reinterpret_cast<rdn::PixelResult*>(d->out);
   w.ray_counts = d->ray_counts;
+  w.refill = d->refill;
   cudaError_t e = cudaSetDevice(c->device);
   if (e == cudaSuccess)
     e = rdn::launch_wavefront_static(p, w, mode_of(d->traversal), d->block_size, c->sm_count, d->phases,

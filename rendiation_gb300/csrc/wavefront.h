@@ -34,6 +34,9 @@ struct WavefrontParams {
   void* bounce_rays;
   uint32_t* shadow_pixel;
   uint32_t* bounce_pixel;
+  // secondary schedule: 0 = batches of 32 per warp; k = 1..32: a warp refills
+  // its idle lanes whenever at least k are idle (ordered walks only)
+  uint32_t refill;
 };
 
 size_t wavefront_scratch_bytes(uint32_t width, uint32_t height);

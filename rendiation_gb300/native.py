@@ -83,7 +83,7 @@ class WavefrontDesc(C.Structure):
     _fields_ = [("camera", Camera), ("light", C.c_float * 3), ("sample_index", C.c_uint32),
                 ("tlas_uniform", C.c_uint32), ("traversal", C.c_uint32), ("block_size", C.c_uint32),
                 ("out", C.c_void_p), ("scratch", C.c_void_p), ("scratch_bytes", C.c_size_t),
-                ("ray_counts", C.c_void_p), ("phases", C.c_uint32), ("reserved", C.c_uint32)]
+                ("ray_counts", C.c_void_p), ("phases", C.c_uint32), ("refill", C.c_uint32)]
 
 
 class PathDesc(C.Structure):
@@ -99,7 +99,8 @@ class AttrLossDesc(C.Structure):
                 ("attributes", C.c_void_p), ("targets", C.c_void_p), ("ray_value", C.c_void_p),
                 ("ray_loss", C.c_void_p), ("loss_sum", C.c_void_p), ("grad_vertices", C.c_void_p),
                 ("grad_ray_origin", C.c_void_p), ("grad_ray_direction", C.c_void_p), ("grad_scale", C.c_float),
-                ("traversal", C.c_uint32), ("block_size", C.c_uint32), ("reserved", C.c_uint32)]
+                ("traversal", C.c_uint32), ("block_size", C.c_uint32), ("from_record", C.c_uint32),
+                ("hit_tri", C.c_void_p), ("hit_inst", C.c_void_p)]
 
 
 class AttrPathDesc(C.Structure):
@@ -107,7 +108,8 @@ class AttrPathDesc(C.Structure):
                 ("segments", C.c_uint32), ("seed", C.c_uint32), ("attributes", C.c_void_p), ("targets", C.c_void_p),
                 ("values", C.c_void_p), ("loss_sum", C.c_void_p), ("grad_vertices", C.c_void_p),
                 ("seg_tri", C.c_void_p), ("seg_rays", C.c_void_p), ("grad_scale", C.c_float),
-                ("traversal", C.c_uint32), ("block_size", C.c_uint32), ("reserved", C.c_uint32)]
+                ("traversal", C.c_uint32), ("block_size", C.c_uint32), ("from_record", C.c_uint32),
+                ("seg_inst", C.c_void_p)]
 
 
 _lib = None

@@ -233,7 +233,7 @@ class Wavefront:
     torch CUDA tensors."""
 
     def __init__(self, system: AccelerationStructureSystem, camera, light, traversal=TRAVERSAL_ORDERED,
-                 tlas_uniform=0, block_size=0):
+                 tlas_uniform=0, block_size=0, refill=0):
         import torch
 
         self.system = system
@@ -257,10 +257,15 @@ class Wavefront:
         self.desc.scratch = self.scratch_ptr
         self.desc.scratch_bytes = size.value
         self.desc.ray_counts = self.ray_counts.data_ptr()
+        self.desc.refill = refill
         self.phase_config = None  # (primary, secondary) (traversal, block) when they differ
 
-    def configure(self, primary, secondary):
-        """Per-kernel (traversal, block_size); a frame then issues one call per kernel."""
+    def configure(self, primary, secondary, refill=None):
+        """Per-kernel (traversal, block_size); a frame then issues one call per kernel.
+        refill: secondary schedule (0 = batches of 32 rays per warp, k = dynamic
+        fetch whenever k lanes of a warp are idle); None keeps the current one."""
+        if refill is not None:
+            self.desc.refill = refill
         if tuple(primary) == tuple(secondary):
             self.desc.traversal, self.desc.block_size = primary
             self.phase_config = None

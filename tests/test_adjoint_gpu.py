@@ -21,29 +21,37 @@ class AttrLoss(torch.autograd.Function):
     returned but the forward ignores the tensor value."""
 
     @staticmethod
-    def forward(ctx, attributes, positions, system, rays, targets):
+    def forward(ctx, attributes, positions, system, rays, targets, record=False):
+        """record: the forward keeps each ray's hit (triangle, instance) and the
+        backward differentiates those hits instead of tracing again."""
         L = native.lib()
         n = rays.shape[0]
         loss = torch.zeros(1, dtype=torch.float64, device="cuda")
+        hit_tri = torch.zeros(n, dtype=torch.int32, device="cuda")
+        hit_inst = torch.zeros(n, dtype=torch.int32, device="cuda")
         d = native.AttrLossDesc(rays.data_ptr(), n, 0, attributes.data_ptr(), targets.data_ptr(), None, None,
-                                loss.data_ptr(), None, None, None, 1.0, rt.TRAVERSAL_ORDERED, 0, 0)
+                                loss.data_ptr(), None, None, None, 1.0, rt.TRAVERSAL_ORDERED, 0, 0,
+                                hit_tri.data_ptr() if record else None, hit_inst.data_ptr() if record else None)
         st = L.rdn_attr_loss_forward(system._h, C.byref(d), C.c_void_p(torch.cuda.current_stream().cuda_stream))
         assert st == 0, L.rdn_last_error(system._h).decode()
-        ctx.save_for_backward(attributes, rays, targets)
+        ctx.save_for_backward(attributes, rays, targets, hit_tri, hit_inst)
         ctx.system = system
         ctx.nv = positions.shape[0]
+        ctx.record = record
         return loss.to(torch.float32)
 
     @staticmethod
     def backward(ctx, g):
-        attributes, rays, targets = ctx.saved_tensors
+        attributes, rays, targets, hit_tri, hit_inst = ctx.saved_tensors
         L = native.lib()
         grad = torch.zeros((ctx.nv, 4), dtype=torch.float32, device="cuda")
+        rec = ctx.record
         d = native.AttrLossDesc(rays.data_ptr(), rays.shape[0], 0, attributes.data_ptr(), targets.data_ptr(), None,
-                                None, None, grad.data_ptr(), None, None, float(g.item()), rt.TRAVERSAL_ORDERED, 0, 0)
+                                None, None, grad.data_ptr(), None, None, float(g.item()), rt.TRAVERSAL_ORDERED, 0,
+                                int(rec), hit_tri.data_ptr() if rec else None, hit_inst.data_ptr() if rec else None)
         st = L.rdn_attr_loss_adjoint(ctx.system._h, C.byref(d), C.c_void_p(torch.cuda.current_stream().cuda_stream))
         assert st == 0, L.rdn_last_error(ctx.system._h).decode()
-        return grad[:, 3].contiguous(), grad[:, :3].contiguous(), None, None, None
+        return grad[:, 3].contiguous(), grad[:, :3].contiguous(), None, None, None, None
 
 
 def fp64_hits(pos, idx, rays, tri):
@@ -106,7 +114,9 @@ def test_forward_matches_oracle_hits(field, cuda):
     assert abs(tot.item() - float(np.sum(loss.cpu().numpy().astype(np.float64)))) < 1e-6 * max(1.0, tot.item())
 
 
-def test_gradients_vs_fp64(field, cuda):
+@pytest.mark.parametrize("record", [False, True])
+def test_gradients_vs_fp64(field, record, cuda):
+    """record: the adjoint differentiates the hits the forward recorded."""
     mesh, attr, rays, hits, S, P = field
     rng = np.random.default_rng(9)
     hit = hits["prim"] != orc.MISS
@@ -115,7 +125,7 @@ def test_gradients_vs_fp64(field, cuda):
     d_attr = torch.from_numpy(attr).cuda().requires_grad_(True)
     d_pos = torch.from_numpy(mesh.positions.copy()).cuda().requires_grad_(True)
     d_tgt = torch.from_numpy(targets).cuda()
-    loss = AttrLoss.apply(d_attr, d_pos, P, d_rays, d_tgt)
+    loss = AttrLoss.apply(d_attr, d_pos, P, d_rays, d_tgt, record)
     loss.backward()
     g_attr = d_attr.grad.cpu().numpy().astype(np.float64)
     g_pos = d_pos.grad.cpu().numpy().astype(np.float64)

@@ -13,10 +13,10 @@ pytestmark = pytest.mark.gpu
 LIGHT = (0.2, 0.2, 2.0)
 
 
-def run_both(mesh, cam, traversal, sample_index=0, bins=4):
+def run_both(mesh, cam, traversal, sample_index=0, bins=4, refill=0):
     sc = single_mesh_scene(mesh, bins=bins)
     S, P = sc.build_oracle(), sc.build_product()
-    wf = rt.Wavefront(P, cam, LIGHT, traversal=traversal)
+    wf = rt.Wavefront(P, cam, LIGHT, traversal=traversal, refill=refill)
     wf.run(sample_index)
     torch.cuda.synchronize()
     got = wf.results()
@@ -36,11 +36,13 @@ def test_wavefront_reference_order_bit_identical(sample_index, cuda):
         assert np.array_equal(got[f].view(np.uint32), exp[f].view(np.uint32)), f
 
 
+@pytest.mark.parametrize("refill", [0, 1, 8, 32])
 @pytest.mark.parametrize("traversal", [rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_WIDE])
-def test_wavefront_ordered_matches_except_ties(traversal, cuda):
+def test_wavefront_ordered_matches_except_ties(traversal, refill, cuda):
+    """refill > 0: the dynamic-fetch secondary schedule."""
     mesh = scenes.heightfield(128, seed=1)
     cam = scenes.heightfield_camera(160, 96)
-    got, exp, rays, counts = run_both(mesh, cam, traversal)
+    got, exp, rays, counts = run_both(mesh, cam, traversal, refill=refill)
     assert counts == tuple(rays)
     same_primary = (got["primary_prim"] == exp["primary_prim"]) & (got["primary_t"] == exp["primary_t"])
     tie = (~same_primary) & (got["primary_t"] == exp["primary_t"])
@@ -61,3 +63,26 @@ def test_wavefront_soup_camera(cuda):
     assert counts == tuple(rays)
     for f in exp.dtype.names:
         assert np.array_equal(got[f].view(np.uint32), exp[f].view(np.uint32)), f
+
+
+@pytest.mark.parametrize("refill", [1, 8])
+def test_wavefront_dynamic_fetch_instanced(refill, cuda):
+    """Dynamic fetch through a TLAS of several instances and geometries
+    (instance walk, geometry walk and BLAS walk all resumed per lane)."""
+    from helpers import instanced_scene
+
+    sc = instanced_scene(seed=0)
+    S, P = sc.build_oracle(), sc.build_product()
+    cam = scenes.PinholeCamera.look_at((0.5, -1.5, 1.2), (0.5, 0.5, 0.2), 50.0, 96, 64)
+    exp, rays, _ = orc.wavefront_shadow_bounce(S, cam.as_floats(), 96, 64, LIGHT, 3, tlas=1, threads=4)
+    for traversal in (rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_WIDE):
+        wf = rt.Wavefront(P, cam, LIGHT, traversal=traversal, tlas_uniform=1, refill=refill)
+        wf.run(3)
+        torch.cuda.synchronize()
+        got = wf.results()
+        assert wf.rays_traced() == tuple(rays)
+        ok = (got["primary_prim"] == exp["primary_prim"]) & (got["primary_t"] == exp["primary_t"])
+        assert ok.mean() > 0.99
+        assert np.array_equal(got["light"][ok], exp["light"][ok])
+        bsame = (got["bounce_prim"] == exp["bounce_prim"]) | (got["bounce_t"] == exp["bounce_t"])
+        assert np.all(bsame[ok])
