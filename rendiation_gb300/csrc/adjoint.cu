@@ -82,6 +82,14 @@ __device__ __forceinline__ ff ff3_dot(ff3 a, ff3 b) {
   return ff_add(ff_add(ff_mul(a.x, b.x), ff_mul(a.y, b.y)), ff_mul(a.z, b.z));
 }
 __device__ __forceinline__ float ff_div(ff a, ff b) { return (a.hi + a.lo) / (b.hi + b.lo); }
+// a / b as a float-float value: a first quotient, its remainder formed in
+// float-float, and a correction quotient.
+__device__ __forceinline__ ff ff_div_ff(ff a, ff b) {
+  const float q1 = a.hi / b.hi;
+  const ff rem = ff_add(a, ff_neg(ff_mul(ff{q1, 0.f}, b)));
+  const float q2 = (rem.hi + rem.lo) / b.hi;
+  return two_sum(q1, q2);
+}
 
 struct HitGeom {
   uint32_t i0, i1, i2;
@@ -89,6 +97,7 @@ struct HitGeom {
   ff3 b1, b2;  // e2 x (-d) and (-d) x e1 in float-float (the adjoint's lambda)
   ff det;      // (-d) . (e1 x e2)
   float t_unnorm;  // hit distance in units of the unnormalised object-space direction
+  ff wf, uf, vf;   // the three corner weights in float-float (w0, u, v round these)
 };
 
 // Hit triangle's vertices and barycentrics re-solved in float-float: with
@@ -122,11 +131,14 @@ __device__ __forceinline__ HitGeom hit_vertices_at(const TraceParams& p, const u
   const ff dv = ff3_dot(ND, ff3_cross(E1, S));
   // distance along the unnormalised object-space direction (t = det[s, e1, e2] / det M)
   h.t_unnorm = ff_div(ff3_dot(S, C12), det);
-  h.u = ff_div(du, det);
-  h.v = ff_div(dv, det);
+  h.uf = ff_div_ff(du, det);
+  h.vf = ff_div_ff(dv, det);
   // w0 = 1 - u - v without the cancellation near the edge v1-v2 (w0 -> 0),
   // where f32 would leave it with a large relative error
-  h.w0 = ff_div(ff_add(det, ff_neg(ff_add(du, dv))), det);
+  h.wf = ff_div_ff(ff_add(det, ff_neg(ff_add(du, dv))), det);
+  h.u = h.uf.hi + h.uf.lo;
+  h.v = h.vf.hi + h.vf.lo;
+  h.w0 = h.wf.hi + h.wf.lo;
   h.det = det;
   h.b1 = ff3_cross(E2, ND);
   h.b2 = ff3_cross(ND, E1);
@@ -148,6 +160,17 @@ __device__ __forceinline__ float3 adjoint_lambda(const HitGeom& h, float gu, flo
   return make_float3(ff_div(ff_add(ff_mul(GU, h.b1.x), ff_mul(GV, h.b2.x)), h.det),
                      ff_div(ff_add(ff_mul(GU, h.b1.y), ff_mul(GV, h.b2.y)), h.det),
                      ff_div(ff_add(ff_mul(GU, h.b1.z), ff_mul(GV, h.b2.z)), h.det));
+}
+
+// value - target with the interpolation (w0 a0 + u a1 + v a2) in float-float:
+// the residual, which scales every gradient of the ray, keeps its relative
+// accuracy when the interpolated value is close to the target. *value gets the
+// interpolated value rounded to f32.
+__device__ __forceinline__ float residual(const HitGeom& h, float a0, float a1, float a2, float target, float* value) {
+  const ff v = ff_add(ff_add(ff_mul(h.wf, ff{a0, 0.f}), ff_mul(h.uf, ff{a1, 0.f})), ff_mul(h.vf, ff{a2, 0.f}));
+  *value = v.hi + v.lo;
+  const ff d = ff_add(v, ff{-target, 0.f});
+  return d.hi + d.lo;
 }
 
 template <int MODE>
@@ -172,8 +195,8 @@ __global__ void __launch_bounds__(128) attr_forward_kernel(TraceParams p, Adjoin
     if (R.best.have) {
       const InstanceRay ir = to_instance(p.tlas_data + R.best.inst, R.o, R.d, 0u);
       const HitGeom h = hit_vertices(p, a.indices, a.vertices, R, ir);
-      value = h.w0 * __ldg(a.attributes + h.i0) + h.u * __ldg(a.attributes + h.i1) + h.v * __ldg(a.attributes + h.i2);
-      const float diff = value - (a.targets ? __ldg(a.targets + i) : 0.0f);
+      const float diff = residual(h, __ldg(a.attributes + h.i0), __ldg(a.attributes + h.i1),
+                                  __ldg(a.attributes + h.i2), a.targets ? __ldg(a.targets + i) : 0.0f, &value);
       loss = diff * diff;
     }
     if (a.hit_tri) a.hit_tri[i] = R.best.have ? __ldg(p.redirect + R.best.k) : INVALID_NEXT;
@@ -215,9 +238,9 @@ __global__ void __launch_bounds__(128) attr_adjoint_kernel(TraceParams p, Adjoin
     const InstanceRay ir = to_instance(p.tlas_data + R.best.inst, R.o, R.d, 0u);
     const HitGeom h = hit_vertices(p, a.indices, a.vertices, R, ir);
     const float a0 = __ldg(a.attributes + h.i0), a1 = __ldg(a.attributes + h.i1), a2 = __ldg(a.attributes + h.i2);
-    const float value = h.w0 * a0 + h.u * a1 + h.v * a2;
+    float value;
     const float target = a.targets ? __ldg(a.targets + i) : 0.0f;
-    const float r = 2.0f * (value - target) * a.grad_scale;
+    const float r = 2.0f * residual(h, a0, a1, a2, target, &value) * a.grad_scale;
     const float gu = r * (a1 - a0), gv = r * (a2 - a0);
     const float3 lam = adjoint_lambda(h, gu, gv);
     float4* g = reinterpret_cast<float4*>(a.grad_vertices);
@@ -301,9 +324,8 @@ __global__ void __launch_bounds__(128) attr_path_kernel(TraceParams p, PathAdjoi
           inst_out = R.best.inst;
           const float a0 = __ldg(a.attributes + h.i0), a1 = __ldg(a.attributes + h.i1),
                       a2 = __ldg(a.attributes + h.i2);
-          value = h.w0 * a0 + h.u * a1 + h.v * a2;
           const float target = a.targets ? __ldg(a.targets + seg) : 0.0f;
-          const float diff = value - target;
+          const float diff = residual(h, a0, a1, a2, target, &value);
           if (ADJOINT) {
             const float r = 2.0f * diff * a.grad_scale;
             scatter_vertex_grads(h, ir, r, r * (a1 - a0), r * (a2 - a0), a.grad_vertices);
@@ -350,22 +372,57 @@ __global__ void __launch_bounds__(128) attr_path_kernel(TraceParams p, PathAdjoi
 // traversal. One thread per segment; misses were recorded as ~0 and add
 // nothing. The forward and the adjoint therefore always agree on visibility,
 // also where two triangles meet the ray at exactly the same distance.
+__device__ __forceinline__ void recorded_segment(const TraceParams& p, const PathAdjointParams& a, size_t seg,
+                                                 uint32_t tri) {
+  const uint32_t inst = __ldg(a.seg_inst + seg);
+  const float4 r0 = __ldg(a.seg_rays + 2 * seg), r1 = __ldg(a.seg_rays + 2 * seg + 1);
+  const float3 o = make_float3(r0.x, r0.y, r0.z), d = make_float3(r1.x, r1.y, r1.z);
+  const InstanceRay ir = to_instance(p.tlas_data + inst, o, d, 0u);
+  const HitGeom h = hit_vertices_at(p, a.indices, a.vertices, tri, inst, d, ir);
+  const float a0 = __ldg(a.attributes + h.i0), a1 = __ldg(a.attributes + h.i1), a2 = __ldg(a.attributes + h.i2);
+  float value;
+  const float target = a.targets ? __ldg(a.targets + seg) : 0.0f;
+  const float r = 2.0f * residual(h, a0, a1, a2, target, &value) * a.grad_scale;
+  scatter_vertex_grads(h, ir, r, r * (a1 - a0), r * (a2 - a0), a.grad_vertices);
+}
+
+// One warp per 32-segment window of the record at a time; the live segments
+// (a hit was recorded) are gathered in a per-warp shared-memory queue and
+// differentiated 32 at a time, so that misses do not leave lanes idle.
 __global__ void __launch_bounds__(256) attr_path_recorded_kernel(TraceParams p, PathAdjointParams a) {
+  __shared__ uint32_t queue[8][64];
+  __shared__ uint32_t queue_tri[8][64];
+  const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
+  const uint32_t lanes_below = (1u << lane) - 1u;
   const size_t total = (size_t)a.count * a.segments;
-  for (size_t seg = blockIdx.x * (size_t)blockDim.x + threadIdx.x; seg < total; seg += (size_t)gridDim.x * blockDim.x) {
-    const uint32_t tri = __ldg(a.seg_tri + seg);
-    if (tri == INVALID_NEXT) continue;
-    const uint32_t inst = __ldg(a.seg_inst + seg);
-    const float4 r0 = __ldg(a.seg_rays + 2 * seg), r1 = __ldg(a.seg_rays + 2 * seg + 1);
-    const float3 o = make_float3(r0.x, r0.y, r0.z), d = make_float3(r1.x, r1.y, r1.z);
-    const InstanceRay ir = to_instance(p.tlas_data + inst, o, d, 0u);
-    const HitGeom h = hit_vertices_at(p, a.indices, a.vertices, tri, inst, d, ir);
-    const float a0 = __ldg(a.attributes + h.i0), a1 = __ldg(a.attributes + h.i1), a2 = __ldg(a.attributes + h.i2);
-    const float value = h.w0 * a0 + h.u * a1 + h.v * a2;
-    const float target = a.targets ? __ldg(a.targets + seg) : 0.0f;
-    const float r = 2.0f * (value - target) * a.grad_scale;
-    scatter_vertex_grads(h, ir, r, r * (a1 - a0), r * (a2 - a0), a.grad_vertices);
+  const size_t warps = ((size_t)gridDim.x * blockDim.x) >> 5;
+  const size_t first = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  // a queued entry is (window number << 5 | lane); segment = first*32 + window*warps*32 + lane
+  auto segment_of = [&](uint32_t e) { return first * 32 + (size_t)(e >> 5) * warps * 32 + (e & 31u); };
+  uint32_t held = 0, window = 0;
+  for (size_t w0 = first * 32; w0 < total; w0 += warps * 32, window++) {
+    const size_t seg = w0 + lane;
+    const uint32_t tri = seg < total ? __ldg(a.seg_tri + seg) : INVALID_NEXT;
+    const uint32_t live = __ballot_sync(0xffffffffu, tri != INVALID_NEXT);
+    if (tri != INVALID_NEXT) {
+      const uint32_t slot = held + __popc(live & lanes_below);
+      queue[wib][slot] = (window << 5) | lane;
+      queue_tri[wib][slot] = tri;
+    }
+    held += __popc(live);
+    __syncwarp();
+    if (held >= 32) {
+      recorded_segment(p, a, segment_of(queue[wib][lane]), queue_tri[wib][lane]);
+      __syncwarp();
+      held -= 32;
+      if (lane < held) {
+        queue[wib][lane] = queue[wib][32 + lane];
+        queue_tri[wib][lane] = queue_tri[wib][32 + lane];
+      }
+      __syncwarp();
+    }
   }
+  if (lane < held) recorded_segment(p, a, segment_of(queue[wib][lane]), queue_tri[wib][lane]);
 }
 
 __global__ void __launch_bounds__(256) attr_recorded_adjoint_kernel(TraceParams p, AdjointParams a) {
@@ -379,9 +436,9 @@ __global__ void __launch_bounds__(256) attr_recorded_adjoint_kernel(TraceParams 
       const InstanceRay ir = to_instance(p.tlas_data + inst, o, d, 0u);
       const HitGeom h = hit_vertices_at(p, a.indices, a.vertices, tri, inst, d, ir);
       const float a0 = __ldg(a.attributes + h.i0), a1 = __ldg(a.attributes + h.i1), a2 = __ldg(a.attributes + h.i2);
-      const float value = h.w0 * a0 + h.u * a1 + h.v * a2;
+      float value;
       const float target = a.targets ? __ldg(a.targets + i) : 0.0f;
-      const float r = 2.0f * (value - target) * a.grad_scale;
+      const float r = 2.0f * residual(h, a0, a1, a2, target, &value) * a.grad_scale;
       const float3 lam = scatter_vertex_grads(h, ir, r, r * (a1 - a0), r * (a2 - a0), a.grad_vertices);
       // object-space distance along the normalised direction: t_unnorm * |M3 d|
       const float t_obj = h.t_unnorm * ir.scaling;
