@@ -440,14 +440,14 @@ def bench_batched(args):
         from rendiation_gb300.autotune import Autotuner, grid
 
         cands = grid(traversal=[rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_WIDE], block=[64, 128],
-                     sort_key=[rt.SORT_NONE, rt.SORT_SCENE_OCTANT, rt.SORT_SCENE_OCTANT_CELL])
+                     sort_key=[rt.SORT_NONE, rt.SORT_SCENE_OCTANT], refill=[0, 8, 16])
 
         def run(c):
-            batched.configure(c["traversal"], c["block"], c["sort_key"])
+            batched.configure(c["traversal"], c["block"], c["sort_key"], c["refill"])
             batched.run()
 
         res = Autotuner().tune("batched-paths", cands, run, reps=2)
-        batched.configure(res.best["traversal"], res.best["block"], res.best["sort_key"])
+        batched.configure(res.best["traversal"], res.best["block"], res.best["sort_key"], res.best["refill"])
         tuned = {"best": res.best, "timings_ms": res.timings_ms}
     batched.capture()
     for _ in range(args.warmup):

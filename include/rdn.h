@@ -346,6 +346,9 @@ typedef struct rdn_path_desc {
   void* scratch;                /* device, >= rdn_paths_scratch_size() bytes, 256-byte aligned */
   size_t scratch_bytes;
   uint32_t* segment_counts;     /* device, nullable: rays traced per bounce (max_bounces + 1) */
+  uint32_t refill;              /* schedule of the ordered walks: 0 = each warp traces 32 queued rays
+                                   together; k in 1..32 = each lane keeps its own query and a warp takes
+                                   new rays whenever k lanes are idle (dynamic fetch) */
 } rdn_path_desc;
 
 /* Ray-sort keys (stable radix sort of each queue before its bounce). */

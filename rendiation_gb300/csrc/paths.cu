@@ -120,6 +120,114 @@ __global__ void __launch_bounds__(128) path_kernel(TraceParams p, PathParams q, 
   if (blockIdx.x == 0 && threadIdx.x == 0 && q.segment_counts) q.segment_counts[bounce] = n;
 }
 
+// The same bounce with dynamic fetch (ordered walks only, q.refill > 0): every
+// lane keeps its own resumable query (LaneWalk) and the warp claims new queue
+// entries for its idle lanes whenever at least q.refill of them are idle, so
+// that a few long paths do not hold a whole warp. Rays of different scenes and
+// directions are mixed anyway, so no coherence is lost by refilling. The
+// shading and the warp-aggregated append run for the lanes that finished in
+// the round; iterations are capped (error-word bit 2).
+template <int MODE>
+__global__ void __launch_bounds__(128, 8) path_dynamic_kernel(TraceParams p, PathParams q, uint32_t bounce,
+                                                              bool from_user, const float4* __restrict__ in_rays,
+                                                              const uint4* __restrict__ in_state,
+                                                              float4* __restrict__ out_rays,
+                                                              uint4* __restrict__ out_state) {
+  extern __shared__ uint2 smem_stack[];
+  constexpr int WIDTH = MODE == MODE_WIDE4 ? 4 : 2;
+  const uint32_t n = bounce == 0 ? q.count : *(volatile uint32_t*)(q.queue_count + bounce - 1);
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t lanes_below = (1u << lane) - 1u;
+  uint32_t* work = q.work_counter + bounce;
+  uint2* stack = smem_stack + threadIdx.x;
+  const uint32_t threshold = q.refill < 1u ? 1u : (q.refill > 32u ? 32u : q.refill);
+  LaneWalk<WIDTH> L;
+  L.reset();
+  uint32_t id = 0, tlas = 0;
+  float throughput = 0.0f;
+  bool exhausted = false;
+  for (uint32_t iter = 0;; iter++) {
+    if (iter >= kMaxWalkRounds) {
+      if (lane == 0) atomicOr(p.error_word, 4u);
+      break;
+    }
+    const uint32_t idle = __ballot_sync(0xffffffffu, L.phase == WALK_IDLE);
+    if (!exhausted && (__popc(idle) >= threshold || idle == 0xffffffffu)) {
+      const uint32_t cnt = __popc(idle);
+      uint32_t base = 0;
+      if (lane == 0) base = atomicAdd(work, cnt);
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (base + cnt >= n) exhausted = true;
+      if (L.phase == WALK_IDLE) {
+        const uint32_t j = base + __popc(idle & lanes_below);
+        if (j < n) {
+          float4 r0, r1;
+          if (from_user) {
+            const float4* rp = q.primary_rays + 2 * (size_t)j;
+            r0 = __ldg(rp);
+            r1 = __ldg(rp + 1);
+            id = j;
+            tlas = q.tlas_idx ? __ldg(q.tlas_idx + j) : q.tlas_uniform;
+            throughput = 1.0f;
+          } else {
+            r0 = in_rays[2 * (size_t)j];
+            r1 = in_rays[2 * (size_t)j + 1];
+            const uint4 st = in_state[j];
+            id = st.x;
+            tlas = st.y;
+            throughput = __uint_as_float(st.z);
+          }
+          L.start(p, r0, r1, tlas, 0u);
+        }
+      }
+    }
+    if (exhausted && __ballot_sync(0xffffffffu, L.phase != WALK_IDLE) == 0u) break;
+    if (L.phase != WALK_IDLE) L.advance(p, stack, blockDim.x, threshold);
+    bool keep = false;
+    float4 nr0 = make_float4(0.f, 0.f, 0.f, 0.f), nr1 = nr0;
+    uint4 ns = make_uint4(0u, 0u, 0u, 0u);
+    if (L.phase == WALK_DONE) {
+      const RayCtx& R = L.R;
+      if (!R.best.have) {
+        q.out[id] = make_float2(throughput, __uint_as_float(bounce | RDN_PATH_ESCAPED));
+      } else if (bounce == q.max_bounces) {
+        q.out[id] = make_float2(0.0f, __uint_as_float(bounce));
+      } else {
+        uint32_t st = xxhash32(id, bounce, q.seed);
+        const float s0 = sample_next(st);
+        const float s1 = sample_next(st);
+        const float s2 = sample_next(st);
+        float t_next = throughput * q.albedo;
+        bool survive = true;
+        if (bounce + 1 >= q.rr_start) {
+          survive = s2 < q.rr_survive;
+          t_next = t_next / q.rr_survive;
+        }
+        if (!survive) {
+          q.out[id] = make_float2(0.0f, __uint_as_float(bounce | RDN_PATH_ROULETTE));
+        } else {
+          const float3 hp = R.o + R.d * R.best.t;
+          const float3 nf = facing_normal(p, R.best.k, R.best.inst, R.d);
+          const float3 org = offset_ray_hit(hp, nf);
+          const float3 dir = cosine_sample_in_dir(nf, s0, s1);
+          nr0 = make_float4(org.x, org.y, org.z, 1.1920929e-7f);
+          nr1 = make_float4(dir.x, dir.y, dir.z, 3.40282347e+38f);
+          ns = make_uint4(id, tlas, __float_as_uint(t_next), 0u);
+          keep = true;
+        }
+      }
+      L.phase = WALK_IDLE;
+    }
+    const uint32_t slot = warp_append(q.queue_count + bounce, keep);
+    if (keep) {
+      out_rays[2 * (size_t)slot] = nr0;
+      out_rays[2 * (size_t)slot + 1] = nr1;
+      out_state[slot] = ns;
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0 && q.segment_counts) q.segment_counts[bounce] = n;
+}
+
 // Primary rays into queue form (only when the executor sorts rays).
 __global__ void path_prime_kernel(PathParams q, float4* __restrict__ rays, uint4* __restrict__ state) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -214,9 +322,10 @@ void paths_bind_scratch(PathParams& q, void* scratch) {
 }
 
 namespace {
-const void* path_fn(int mode) {
-  if (mode == MODE_WIDE4) return (const void*)path_kernel<MODE_WIDE4>;
-  if (mode == MODE_BINARY) return (const void*)path_kernel<MODE_BINARY>;
+const void* path_fn(int mode, bool dynamic) {
+  if (mode == MODE_WIDE4) return dynamic ? (const void*)path_dynamic_kernel<MODE_WIDE4> : (const void*)path_kernel<MODE_WIDE4>;
+  if (mode == MODE_BINARY)
+    return dynamic ? (const void*)path_dynamic_kernel<MODE_BINARY> : (const void*)path_kernel<MODE_BINARY>;
   return (const void*)path_kernel<MODE_THREADED>;
 }
 }  // namespace
@@ -225,12 +334,13 @@ cudaError_t prepare_paths(const TraceParams& p, const PathParams& q, int mode, u
                           uint32_t* grid) {
   if (block == 0) block = 64;
   const size_t smem = mode != MODE_THREADED ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
-  static bool attr_done[3] = {false, false, false};
-  const void* fn = path_fn(mode);
-  if (!attr_done[mode]) {
+  static bool attr_done[2][3] = {{false, false, false}, {false, false, false}};
+  const bool dynamic = mode != MODE_THREADED && q.refill != 0;
+  const void* fn = path_fn(mode, dynamic);
+  if (!attr_done[dynamic][mode]) {
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     if (e != cudaSuccess) return e;
-    attr_done[mode] = true;
+    attr_done[dynamic][mode] = true;
   }
   int per_sm = 0;
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (int)block, smem);
@@ -287,9 +397,17 @@ cudaError_t record_paths(const TraceParams& p, const PathParams& q, int mode, ui
       out_r = (b & 1) ? ra : rb;
       out_s = (b & 1) ? sa : sb;
     }
-    if (mode == MODE_WIDE4) path_kernel<MODE_WIDE4><<<grid, block, smem, stream>>>(p, q, b, from_user, in_r, in_s, out_r, out_s);
-    else if (mode == MODE_BINARY) path_kernel<MODE_BINARY><<<grid, block, smem, stream>>>(p, q, b, from_user, in_r, in_s, out_r, out_s);
-    else path_kernel<MODE_THREADED><<<grid, block, smem, stream>>>(p, q, b, from_user, in_r, in_s, out_r, out_s);
+    const bool dynamic = mode != MODE_THREADED && q.refill != 0;
+    if (mode == MODE_WIDE4 && dynamic)
+      path_dynamic_kernel<MODE_WIDE4><<<grid, block, smem, stream>>>(p, q, b, from_user, in_r, in_s, out_r, out_s);
+    else if (mode == MODE_WIDE4)
+      path_kernel<MODE_WIDE4><<<grid, block, smem, stream>>>(p, q, b, from_user, in_r, in_s, out_r, out_s);
+    else if (mode == MODE_BINARY && dynamic)
+      path_dynamic_kernel<MODE_BINARY><<<grid, block, smem, stream>>>(p, q, b, from_user, in_r, in_s, out_r, out_s);
+    else if (mode == MODE_BINARY)
+      path_kernel<MODE_BINARY><<<grid, block, smem, stream>>>(p, q, b, from_user, in_r, in_s, out_r, out_s);
+    else
+      path_kernel<MODE_THREADED><<<grid, block, smem, stream>>>(p, q, b, from_user, in_r, in_s, out_r, out_s);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }

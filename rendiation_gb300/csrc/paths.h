@@ -27,6 +27,9 @@ struct PathParams {
   uint32_t* keys;
   uint32_t* idx;
   void* sort_scratch;
+  // 0: warps trace 32 queued rays at a time; k > 0: dynamic fetch whenever k
+  // lanes of a warp are idle (ordered walks only)
+  uint32_t refill;
 };
 
 // Ray-sort keys: 0 none; 1 (scene, direction octant); 2 (scene, octant, 12-bit

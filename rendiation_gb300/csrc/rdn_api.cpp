@@ -553,6 +553,7 @@ rdn_status prepare_path_launch(rdn_ctx* c, const rdn_path_desc* d, rdn::TracePar
   if (d->max_bounces > 16) return fail(c, RDN_ERR_INVALID_ARG, "max_bounces above 16");
   if (d->count && (!d->rays || !d->out || !d->scratch)) return fail(c, RDN_ERR_INVALID_ARG, "null buffer");
   if (d->sort_key > 2) return fail(c, RDN_ERR_INVALID_ARG, "unknown sort key");
+  if (d->refill > 32) return fail(c, RDN_ERR_INVALID_ARG, "refill must be 0..32");
   if (d->scratch_bytes < rdn::paths_scratch_bytes(d->count, d->max_bounces, d->sort_key))
     return fail(c, RDN_ERR_INVALID_ARG, "scratch too small");
   if ((reinterpret_cast<uintptr_t>(d->scratch) & 255) || (reinterpret_cast<uintptr_t>(d->rays) & 15) ||
@@ -583,6 +584,7 @@ rdn_status prepare_path_launch(rdn_ctx* c, const rdn_path_desc* d, rdn::TracePar
   q.out = reinterpret_cast<float2*>(d->out);
   q.segment_counts = d->segment_counts;
   q.sort_key = d->sort_key;
+  q.refill = d->refill;
   if (d->sort_key) {
     uint32_t bits = 0;
     while (bits < 32 && (1ull << bits) < (uint64_t)std::max<size_t>(1, c->dev.tlas_binding.count)) bits++;

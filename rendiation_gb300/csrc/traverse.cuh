@@ -448,5 +448,180 @@ __device__ __forceinline__ void traverse_ray(const TraceParams& p, RayCtx& R, ui
   }
 }
 
+// Resumable per-lane query for dynamic-fetch schedules: the same TLAS walk,
+// instance and geometry loops and speculative ordered BLAS walk as
+// traverse_ray (WIDTH 2 or 4), with the state kept across calls so that a warp
+// can stop, hand new rays to its idle lanes, and continue.
+enum : uint32_t { WALK_IDLE = 0, WALK_TLAS = 1, WALK_INST = 2, WALK_GEOM = 3, WALK_BLAS = 4, WALK_DONE = 5 };
+constexpr uint32_t kMaxWalkRounds = 1u << 24;
+
+template <int WIDTH>
+struct LaneWalk {
+  RayCtx R;
+  InstanceRay ir;
+  uint32_t phase, tcur, ti, ti_end, inst_slot, g, g_end, gslot, prim_start;
+  bool is_opaque, cull_enable, cull_back;
+  uint32_t code, leaf, sp;
+  float code_tn;
+
+  __device__ __forceinline__ void reset() {
+    phase = WALK_IDLE;
+    R.cull_mask = 0xFFu;
+    R.best.have = false;
+    ir.o = ir.d = ir.inv_d = make_float3(0.f, 0.f, 0.f);
+    ir.scaling = 1.0f;
+    ir.flags = 0u;
+    tcur = INVALID_NEXT;
+    ti = ti_end = inst_slot = g = g_end = gslot = prim_start = 0;
+    is_opaque = true;
+    cull_enable = cull_back = false;
+    code = leaf = EMPTY_SLOT;
+    sp = 0;
+    code_tn = 0.0f;
+  }
+
+  __device__ __forceinline__ void start(const TraceParams& p, float4 r0, float4 r1, uint32_t tlas, uint32_t ray_flags) {
+    R.o = make_float3(r0.x, r0.y, r0.z);
+    R.tmin = r0.w;
+    R.d = make_float3(r1.x, r1.y, r1.z);
+    R.tmax = r1.w;
+    R.ray_flags = ray_flags;
+    R.cull_mask = 0xFFu;
+    R.inv_d = make_float3(1.0f / R.d.x, 1.0f / R.d.y, 1.0f / R.d.z);
+    R.far_world = R.tmax;
+    R.best.have = false;
+    tcur = INVALID_NEXT;
+    if (tlas < p.n_binding) {
+      const uint32_t handle = __ldg(p.tlas_binding + tlas);
+      if (handle < p.n_tlas_root) tcur = __ldg(p.tlas_bvh_root + handle);
+    }
+    code = leaf = EMPTY_SLOT;
+    phase = WALK_TLAS;
+  }
+
+  // TLAS / instance / geometry steps up to the next BLAS entry or the end.
+  __device__ __forceinline__ void to_blas(const TraceParams& p) {
+    const float inf = __int_as_float(0x7f800000);
+    while (phase == WALK_TLAS || phase == WALK_INST || phase == WALK_GEOM) {
+      if (phase == WALK_TLAS) {
+        bool found = false;
+        while (tcur != INVALID_NEXT) {
+          const float4* nd = reinterpret_cast<const float4*>(p.tlas_forest + tcur);
+          const float4 a = __ldg(nd), b = __ldg(nd + 1);
+          const uint32_t hit_next = __float_as_uint(a.w), miss_next = __float_as_uint(b.w);
+          float tn;
+          if (!slab(R.o, R.inv_d, R.tmin * 1.0f, R.far_world * 1.0f, a.x, a.y, a.z, b.x, b.y, b.z, tn)) {
+            tcur = miss_next;
+            continue;
+          }
+          tcur = hit_next;
+          if (hit_next != miss_next) continue;
+          const uint2 cr = __ldg(reinterpret_cast<const uint2*>(nd + 2));
+          ti = cr.x;
+          ti_end = cr.y;
+          found = true;
+          break;
+        }
+        phase = found ? WALK_INST : WALK_DONE;
+      } else if (phase == WALK_INST) {
+        bool entered = false;
+        while (ti < ti_end) {
+          const uint32_t cur = ti++;
+          const float4* tb = reinterpret_cast<const float4*>(p.tlas_bounding + cur);
+          const float4 ba = __ldg(tb), bb = __ldg(tb + 1);
+          float tn2;
+          if (!slab(R.o, R.inv_d, R.tmin, R.tmax, ba.x, ba.y, ba.z, bb.x, bb.y, bb.z, tn2)) continue;
+          if ((R.cull_mask & __float_as_uint(ba.w)) == 0) continue;
+          const DeviceInstance* inst = p.tlas_data + cur;
+          ir = to_instance(inst, R.o, R.d, R.ray_flags);
+          if (ir.flags & TF_SKIP_TRIANGLES) continue;
+          const uint32_t blas = __ldg(&inst->acceleration_structure_handle);
+          const uint2 range = __ldg(reinterpret_cast<const uint2*>(p.blas_meta + blas));
+          g = range.x;
+          g_end = range.y;
+          inst_slot = cur;
+          entered = true;
+          break;
+        }
+        phase = entered ? WALK_GEOM : WALK_TLAS;
+      } else {
+        bool entered = false;
+        while (g < g_end) {
+          const uint32_t cur = g++;
+          const uint4 gm = __ldg(reinterpret_cast<const uint4*>(p.tri_root + cur));
+          bool pass;
+          geometry_cull(ir.flags, gm.w, pass, is_opaque, cull_enable, cull_back);
+          if (!pass) continue;
+          const float4* nd = reinterpret_cast<const float4*>(p.tri_forest + gm.x);
+          const float4 a = __ldg(nd), b = __ldg(nd + 1);
+          float tn;
+          if (!slab(ir.o, ir.inv_d, R.tmin * ir.scaling, R.far_world * ir.scaling, a.x, a.y, a.z, b.x, b.y, b.z, tn))
+            continue;
+          code = __ldg((WIDTH == 2 ? p.geom_root_code : p.geom_root_code4) + cur);
+          code_tn = -inf;
+          leaf = EMPTY_SLOT;
+          sp = 0;
+          if (code & LEAF_BIT) {
+            leaf = code;
+            code = EMPTY_SLOT;
+          }
+          gslot = cur;
+          prim_start = gm.z;
+          entered = true;
+          break;
+        }
+        phase = entered ? WALK_BLAS : WALK_INST;
+      }
+    }
+  }
+
+  // Advances the query: to the next BLAS entry, then rounds of traverse_ray's
+  // speculative walk. Returns with phase WALK_DONE when the query ended, with
+  // WALK_GEOM when this BLAS is exhausted, or still WALK_BLAS after a round in
+  // which at least `threshold` lanes of the warp were outside the walk (the
+  // caller then refills its idle lanes).
+  __device__ __forceinline__ void advance(const TraceParams& p, uint2* stack, uint32_t stride, uint32_t threshold) {
+    to_blas(p);
+    if (phase != WALK_BLAS) return;
+    for (uint32_t round = 0;; round++) {
+      if (round >= kMaxWalkRounds) {
+        atomicOr(p.error_word, 4u);
+        phase = WALK_DONE;
+        return;
+      }
+      while (code != EMPTY_SLOT && !(code & LEAF_BIT)) {
+        code = interior_step<false, WIDTH>(p, R, ir, code, code_tn, stack, stride, sp, p.stack_depth);
+        if (code != EMPTY_SLOT && (code & LEAF_BIT) && leaf == EMPTY_SLOT) {
+          leaf = code;
+          code = pop_live(stack, stride, sp, R.far_world * ir.scaling, code_tn);
+        }
+        if (!__any_sync(__activemask(), leaf == EMPTY_SLOT)) break;
+      }
+      while (leaf != EMPTY_SLOT) {
+        const uint2 lr = __ldg(p.leaves + (leaf & ~LEAF_BIT));
+        if (leaf_triangles<false>(p, R, ir, lr.x, lr.y, gslot, inst_slot, is_opaque, cull_enable, cull_back,
+                                  prim_start)) {
+          code = leaf = EMPTY_SLOT;
+          phase = WALK_DONE;  // the search ends (first hit accepted)
+          return;
+        }
+        leaf = EMPTY_SLOT;
+        // the far may have shrunk: re-check the pending node before descending into it
+        if (code != EMPTY_SLOT && !(code_tn < R.far_world * ir.scaling))
+          code = pop_live(stack, stride, sp, R.far_world * ir.scaling, code_tn);
+        if (code != EMPTY_SLOT && (code & LEAF_BIT)) {
+          leaf = code;
+          code = pop_live(stack, stride, sp, R.far_world * ir.scaling, code_tn);
+        }
+      }
+      if (code == EMPTY_SLOT && leaf == EMPTY_SLOT) {
+        phase = WALK_GEOM;  // next geometry / instance on the next call
+        return;
+      }
+      if (32u - (uint32_t)__popc(__activemask()) >= threshold) return;  // let the warp refill
+    }
+  }
+};
+
 }  // namespace dev
 }  // namespace rdn

@@ -172,7 +172,6 @@ __global__ void __launch_bounds__(128) secondary_kernel(TraceParams p, Wavefront
 // schedule's up to the order in which exact-distance ties are met. Iterations
 // are capped far above any real traversal; a warp that reaches a cap sets bit
 // 2 of the error word and stops.
-enum : uint32_t { PH_IDLE = 0, PH_TLAS = 1, PH_INST = 2, PH_GEOM = 3, PH_BLAS = 4, PH_DONE = 5 };
 constexpr uint32_t kMaxWarpIterations = 1u << 24;
 
 template <int MODE>
@@ -191,182 +190,38 @@ __global__ void __launch_bounds__(128, 8) secondary_dynamic_kernel(TraceParams p
   uint2* stack = smem_stack + threadIdx.x;
   const uint32_t stride = blockDim.x;
   const uint32_t threshold = w.refill < 1u ? 1u : (w.refill > 32u ? 32u : w.refill);
-  const float inf = __int_as_float(0x7f800000);
-
-  RayCtx R;
-  R.cull_mask = 0xFFu;
-  InstanceRay ir;
-  ir.o = ir.d = ir.inv_d = make_float3(0.f, 0.f, 0.f);
-  ir.scaling = 1.0f;
-  ir.flags = 0u;
-  uint32_t phase = PH_IDLE, q = 0;
-  uint32_t tcur = INVALID_NEXT, ti = 0, ti_end = 0, inst_slot = 0, g = 0, g_end = 0;
-  uint32_t gslot = 0, prim_start = 0;
-  bool is_opaque = true, cull_enable = false, cull_back = false;
-  uint32_t code = EMPTY_SLOT, leaf = EMPTY_SLOT, sp = 0;
-  float code_tn = -inf;
+  LaneWalk<WIDTH> L;
+  L.reset();
+  uint32_t q = 0;
   bool exhausted = false;
-
   for (uint32_t iter = 0;; iter++) {
     if (iter >= kMaxWarpIterations) {
       if (lane == 0) atomicOr(p.error_word, 4u);
       break;
     }
     // refill idle lanes from the queue
-    const uint32_t idle = __ballot_sync(0xffffffffu, phase == PH_IDLE);
+    const uint32_t idle = __ballot_sync(0xffffffffu, L.phase == WALK_IDLE);
     if (!exhausted && (__popc(idle) >= threshold || idle == 0xffffffffu)) {
       const uint32_t cnt = __popc(idle);
       uint32_t base = 0;
       if (lane == 0) base = atomicAdd(w.work_counter, cnt);
       base = __shfl_sync(0xffffffffu, base, 0);
       if (base + cnt >= total) exhausted = true;
-      if (phase == PH_IDLE) {
+      if (L.phase == WALK_IDLE) {
         const uint32_t j = base + __popc(idle & lanes_below);
         if (j < total) {
           q = j;
           const bool shadow = j < n;
           const float4* rq =
               reinterpret_cast<const float4*>(shadow ? w.shadow_rays : w.bounce_rays) + 2 * (size_t)(shadow ? j : j - n);
-          const float4 r0 = rq[0], r1 = rq[1];
-          R.o = make_float3(r0.x, r0.y, r0.z);
-          R.tmin = r0.w;
-          R.d = make_float3(r1.x, r1.y, r1.z);
-          R.tmax = r1.w;
-          R.ray_flags = shadow ? TF_END_SEARCH : 0u;
-          R.inv_d = make_float3(1.0f / R.d.x, 1.0f / R.d.y, 1.0f / R.d.z);
-          R.far_world = R.tmax;
-          R.best.have = false;
-          tcur = INVALID_NEXT;
-          if (w.tlas < p.n_binding) {
-            const uint32_t handle = __ldg(p.tlas_binding + w.tlas);
-            if (handle < p.n_tlas_root) tcur = __ldg(p.tlas_bvh_root + handle);
-          }
-          phase = PH_TLAS;
+          L.start(p, rq[0], rq[1], w.tlas, shadow ? TF_END_SEARCH : 0u);
         }
       }
     }
-    if (exhausted && __ballot_sync(0xffffffffu, phase != PH_IDLE) == 0u) break;
-
-    // TLAS / instance / geometry walk up to the next BLAS entry (or the end)
-    while (phase == PH_TLAS || phase == PH_INST || phase == PH_GEOM) {
-      if (phase == PH_TLAS) {
-        bool found = false;
-        while (tcur != INVALID_NEXT) {
-          const float4* nd = reinterpret_cast<const float4*>(p.tlas_forest + tcur);
-          const float4 a = __ldg(nd), b = __ldg(nd + 1);
-          const uint32_t hit_next = __float_as_uint(a.w), miss_next = __float_as_uint(b.w);
-          float tn;
-          if (!slab(R.o, R.inv_d, R.tmin * 1.0f, R.far_world * 1.0f, a.x, a.y, a.z, b.x, b.y, b.z, tn)) {
-            tcur = miss_next;
-            continue;
-          }
-          tcur = hit_next;
-          if (hit_next != miss_next) continue;
-          const uint2 cr = __ldg(reinterpret_cast<const uint2*>(nd + 2));
-          ti = cr.x;
-          ti_end = cr.y;
-          found = true;
-          break;
-        }
-        phase = found ? PH_INST : PH_DONE;
-      } else if (phase == PH_INST) {
-        bool entered = false;
-        while (ti < ti_end) {
-          const uint32_t cur = ti++;
-          const float4* tb = reinterpret_cast<const float4*>(p.tlas_bounding + cur);
-          const float4 ba = __ldg(tb), bb = __ldg(tb + 1);
-          float tn2;
-          if (!slab(R.o, R.inv_d, R.tmin, R.tmax, ba.x, ba.y, ba.z, bb.x, bb.y, bb.z, tn2)) continue;
-          if ((R.cull_mask & __float_as_uint(ba.w)) == 0) continue;
-          const DeviceInstance* inst = p.tlas_data + cur;
-          ir = to_instance(inst, R.o, R.d, R.ray_flags);
-          if (ir.flags & TF_SKIP_TRIANGLES) continue;
-          const uint32_t blas = __ldg(&inst->acceleration_structure_handle);
-          const uint2 range = __ldg(reinterpret_cast<const uint2*>(p.blas_meta + blas));
-          g = range.x;
-          g_end = range.y;
-          inst_slot = cur;
-          entered = true;
-          break;
-        }
-        phase = entered ? PH_GEOM : PH_TLAS;
-      } else {
-        bool entered = false;
-        while (g < g_end) {
-          const uint32_t cur = g++;
-          const uint4 gm = __ldg(reinterpret_cast<const uint4*>(p.tri_root + cur));
-          bool pass;
-          geometry_cull(ir.flags, gm.w, pass, is_opaque, cull_enable, cull_back);
-          if (!pass) continue;
-          const float4* nd = reinterpret_cast<const float4*>(p.tri_forest + gm.x);
-          const float4 a = __ldg(nd), b = __ldg(nd + 1);
-          float tn;
-          if (!slab(ir.o, ir.inv_d, R.tmin * ir.scaling, R.far_world * ir.scaling, a.x, a.y, a.z, b.x, b.y, b.z, tn))
-            continue;
-          code = __ldg((WIDTH == 2 ? p.geom_root_code : p.geom_root_code4) + cur);
-          code_tn = -inf;
-          leaf = EMPTY_SLOT;
-          sp = 0;
-          if (code & LEAF_BIT) {
-            leaf = code;
-            code = EMPTY_SLOT;
-          }
-          gslot = cur;
-          prim_start = gm.z;
-          entered = true;
-          break;
-        }
-        phase = entered ? PH_BLAS : PH_INST;
-      }
-    }
-
-    // BLAS walk: traverse_ray's speculative near-first loop, left for a refill
-    if (phase == PH_BLAS) {
-      for (uint32_t round = 0;; round++) {
-        if (round >= kMaxWarpIterations) {
-          atomicOr(p.error_word, 4u);
-          phase = PH_DONE;
-          break;
-        }
-        while (code != EMPTY_SLOT && !(code & LEAF_BIT)) {
-          code = interior_step<false, WIDTH>(p, R, ir, code, code_tn, stack, stride, sp, p.stack_depth);
-          if (code != EMPTY_SLOT && (code & LEAF_BIT) && leaf == EMPTY_SLOT) {
-            leaf = code;
-            code = pop_live(stack, stride, sp, R.far_world * ir.scaling, code_tn);
-          }
-          if (!__any_sync(__activemask(), leaf == EMPTY_SLOT)) break;
-        }
-        bool ended = false;
-        while (leaf != EMPTY_SLOT) {
-          const uint2 lr = __ldg(p.leaves + (leaf & ~LEAF_BIT));
-          if (leaf_triangles<false>(p, R, ir, lr.x, lr.y, gslot, inst_slot, is_opaque, cull_enable, cull_back,
-                                    prim_start)) {
-            ended = true;  // the search ends (first hit accepted)
-            break;
-          }
-          leaf = EMPTY_SLOT;
-          // the far may have shrunk: re-check the pending node before descending into it
-          if (code != EMPTY_SLOT && !(code_tn < R.far_world * ir.scaling))
-            code = pop_live(stack, stride, sp, R.far_world * ir.scaling, code_tn);
-          if (code != EMPTY_SLOT && (code & LEAF_BIT)) {
-            leaf = code;
-            code = pop_live(stack, stride, sp, R.far_world * ir.scaling, code_tn);
-          }
-        }
-        if (ended) {
-          code = leaf = EMPTY_SLOT;
-          phase = PH_DONE;
-          break;
-        }
-        if (code == EMPTY_SLOT && leaf == EMPTY_SLOT) {
-          phase = PH_GEOM;  // next geometry / instance, in the next outer round
-          break;
-        }
-        if (32u - (uint32_t)__popc(__activemask()) >= threshold) break;  // let the warp refill
-      }
-    }
-
-    if (phase == PH_DONE) {
+    if (exhausted && __ballot_sync(0xffffffffu, L.phase != WALK_IDLE) == 0u) break;
+    if (L.phase != WALK_IDLE) L.advance(p, stack, stride, threshold);
+    if (L.phase == WALK_DONE) {
+      const RayCtx& R = L.R;
       if (q < n) {
         PixelResult* o = w.out + w.shadow_pixel[q];
         o->light = R.best.have ? 2u : 1u;
@@ -377,7 +232,7 @@ __global__ void __launch_bounds__(128, 8) secondary_dynamic_kernel(TraceParams p
         o->bounce_prim = __ldg(p.redirect + R.best.k) - gm.z;
         o->bounce_t = R.best.t;
       }
-      phase = PH_IDLE;
+      L.phase = WALK_IDLE;
     }
   }
 }

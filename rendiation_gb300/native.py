@@ -91,7 +91,7 @@ class PathDesc(C.Structure):
                 ("max_bounces", C.c_uint32), ("rr_start", C.c_uint32), ("albedo", C.c_float),
                 ("rr_survive", C.c_float), ("seed", C.c_uint32), ("traversal", C.c_uint32),
                 ("block_size", C.c_uint32), ("sort_key", C.c_uint32), ("out", C.c_void_p), ("scratch", C.c_void_p),
-                ("scratch_bytes", C.c_size_t), ("segment_counts", C.c_void_p)]
+                ("scratch_bytes", C.c_size_t), ("segment_counts", C.c_void_p), ("refill", C.c_uint32)]
 
 
 class AttrLossDesc(C.Structure):

@@ -310,7 +310,7 @@ class Paths:
 
     def __init__(self, system: AccelerationStructureSystem, rays, tlas_idx=None, tlas_uniform=0, max_bounces=4,
                  rr_start=2, albedo=0.5, rr_survive=0.5, seed=0, traversal=TRAVERSAL_ORDERED, block_size=0,
-                 sort_key=0):
+                 sort_key=0, refill=0):
         import torch
 
         self.system = system
@@ -327,12 +327,15 @@ class Paths:
         self.segments_dev = torch.zeros(max_bounces + 1, dtype=torch.int32, device="cuda")
         self.desc = native.PathDesc(rays.data_ptr(), 0 if tlas_idx is None else tlas_idx.data_ptr(), n, tlas_uniform,
                                     max_bounces, rr_start, albedo, rr_survive, seed, traversal, block_size, sort_key,
-                                    self.out.data_ptr(), self.scratch_ptr, size.value, self.segments_dev.data_ptr())
+                                    self.out.data_ptr(), self.scratch_ptr, size.value, self.segments_dev.data_ptr(),
+                                    refill)
         self.graph = None
         self.scratch_bytes = size.value
 
-    def configure(self, traversal=None, block_size=None, sort_key=None):
-        """Changes launch knobs (re-capture any graph afterwards)."""
+    def configure(self, traversal=None, block_size=None, sort_key=None, refill=None):
+        """Changes launch knobs (re-capture any graph afterwards). refill: 0 =
+        warps trace 32 queued rays together, k = dynamic fetch whenever k lanes
+        of a warp are idle."""
         import torch
 
         if sort_key is not None and sort_key != self.desc.sort_key:
@@ -349,6 +352,8 @@ class Paths:
             self.desc.traversal = traversal
         if block_size is not None:
             self.desc.block_size = block_size
+        if refill is not None:
+            self.desc.refill = refill
         self.close()
 
     def run(self, stream=None):

@@ -56,10 +56,15 @@ def test_paths_graph_replays_identically(batched, cuda):
     assert np.array_equal(got["radiance"].view(np.uint32), exp["radiance"].view(np.uint32))
 
 
-def test_paths_ordered_matches_except_ties(batched, cuda):
+@pytest.mark.parametrize("refill", [0, 1, 8])
+@pytest.mark.parametrize("traversal", [rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_WIDE])
+def test_paths_ordered_matches_except_ties(batched, traversal, refill, cuda):
+    """refill > 0: the dynamic-fetch schedule (also replayed from a graph)."""
     b, S, P = batched
     exp, seg, _ = orc.trace_paths(S, b.rays, b.tlas_idx, max_bounces=4, rr_start=2, seed=5, threads=4)
-    got, gseg, _ = product_paths(P, b, rt.TRAVERSAL_ORDERED, seed=5)
+    got, gseg, first = product_paths(P, b, traversal, graph=refill == 8, seed=5, refill=refill)
+    if first is not None:
+        assert (first["depth_flags"] == got["depth_flags"]).mean() > 0.999
     # a path diverges from the oracle only after an exact-distance tie picks another triangle
     same = (got["depth_flags"] == exp["depth_flags"]) & (got["radiance"] == exp["radiance"])
     assert same.mean() > 0.999, same.mean()
