@@ -209,15 +209,18 @@ def bench_wavefront(args, ws, rank):
         from rendiation_gb300.autotune import Autotuner, grid
 
         tuner = Autotuner(args.tune_cache)
-        cands = grid(traversal=[rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_WIDE], block=[32, 64, 128])
+        # traversal stack in shared memory (local 0) or in local memory (1)
+        cands = grid(traversal=[rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_WIDE], block=[32, 64, 128], local=[0, 1])
         # secondary schedule: batches of 32 rays per warp (refill 0) or dynamic fetch
-        cands2 = grid(traversal=[rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_WIDE], block=[32, 64, 128],
-                      refill=[0, 4, 8, 16])
+        cands2 = (grid(traversal=[rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_WIDE], block=[32, 64, 128],
+                       refill=[0], local=[0, 1])
+                  + grid(traversal=[rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_WIDE], block=[64], refill=[8, 16],
+                         local=[0]))
 
         def run_phase(ph):
             def run(c):
                 wf.desc.traversal, wf.desc.block_size = c["traversal"], c["block"]
-                wf.desc.refill = c.get("refill", 0)
+                wf.desc.refill, wf.desc.local_stack = c.get("refill", 0), c.get("local", 0)
                 wf.run(7, phases=ph)
             return run
 
@@ -225,7 +228,8 @@ def bench_wavefront(args, ws, rank):
         torch.cuda.synchronize()
         t1 = tuner.tune("wavefront-primary", cands, run_phase(1))
         t2 = tuner.tune("wavefront-secondary", cands2, run_phase(2))
-        wf.configure((t1.best["traversal"], t1.best["block"]), (t2.best["traversal"], t2.best["block"]),
+        wf.configure((t1.best["traversal"], t1.best["block"], t1.best.get("local", 0)),
+                     (t2.best["traversal"], t2.best["block"], t2.best.get("local", 0)),
                      refill=t2.best.get("refill", 0))
         tuned = {"primary": t1.best, "secondary": t2.best}
 

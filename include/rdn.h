@@ -297,6 +297,8 @@ typedef struct rdn_wavefront_desc {
   uint32_t refill;           /* secondary schedule of the ordered walks: 0 = each warp traces 32 queued
                                 rays together; k in 1..32 = each lane keeps its own traversal state and
                                 a warp takes new rays whenever k lanes are idle (dynamic fetch) */
+  uint32_t local_stack;      /* ordered walks: 1 = traversal stacks in the threads' local memory (L1)
+                                instead of shared memory, for trees whose stack fits 64 entries */
 } rdn_wavefront_desc;
 
 /* Scratch size for the secondary-ray queues of a width x height launch. */

@@ -36,9 +36,16 @@ namespace {
 
 using namespace dev;
 
-template <int MODE>
+// LOCAL: the traversal stack lives in the thread's local memory (L1-cached)
+// instead of shared memory, so that the stack no longer limits occupancy.
+constexpr uint32_t kLocalStackEntries = 64;
+
+template <int MODE, bool LOCAL>
 __global__ void __launch_bounds__(128) primary_kernel(TraceParams p, WavefrontParams w) {
   extern __shared__ uint2 smem_stack[];
+  uint2 local_stack[LOCAL ? kLocalStackEntries : 1];
+  uint2* const stack = LOCAL ? local_stack : smem_stack + threadIdx.x;
+  const uint32_t stride = LOCAL ? 1u : blockDim.x;
   const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t warp = gtid >> 5, lane = gtid & 31u;
   const uint32_t tiles_x = (w.width + 7u) / 8u;
@@ -64,7 +71,7 @@ __global__ void __launch_bounds__(128) primary_kernel(TraceParams p, WavefrontPa
     R.cull_mask = 0xFFu;
     R.ray_flags = 0u;
     bool bad;
-    traverse_ray<MODE, false>(p, R, w.tlas, smem_stack + threadIdx.x, blockDim.x, bad);
+    traverse_ray<MODE, false>(p, R, w.tlas, stack, stride, bad);
     PixelResult out;
     out.primary_prim = INVALID_NEXT;
     out.primary_t = R.tmax;
@@ -112,9 +119,12 @@ __global__ void __launch_bounds__(128) primary_kernel(TraceParams p, WavefrontPa
   }
 }
 
-template <int MODE>
+template <int MODE, bool LOCAL>
 __global__ void __launch_bounds__(128) secondary_kernel(TraceParams p, WavefrontParams w) {
   extern __shared__ uint2 smem_stack[];
+  uint2 local_stack[LOCAL ? kLocalStackEntries : 1];
+  uint2* const stack = LOCAL ? local_stack : smem_stack + threadIdx.x;
+  const uint32_t stride = LOCAL ? 1u : blockDim.x;
   const uint32_t n = *(volatile uint32_t*)w.queue_count;
   const uint32_t total = 2u * n;
   const uint32_t lane = threadIdx.x & 31u;
@@ -142,7 +152,7 @@ __global__ void __launch_bounds__(128) secondary_kernel(TraceParams p, Wavefront
       R.cull_mask = 0xFFu;
       R.ray_flags = shadow ? TF_END_SEARCH : 0u;
       bool bad;
-      traverse_ray<MODE, false>(p, R, w.tlas, smem_stack + threadIdx.x, blockDim.x, bad);
+      traverse_ray<MODE, false>(p, R, w.tlas, stack, stride, bad);
       if (shadow) {
         PixelResult* o = w.out + w.shadow_pixel[q];
         o->light = R.best.have ? 2u : 1u;
@@ -262,15 +272,16 @@ void wavefront_bind_scratch(WavefrontParams& w, void* scratch) {
 }
 
 namespace {
-template <int MODE>
+template <int MODE, bool LOCAL>
 cudaError_t launch_wavefront_mode(const TraceParams& p, const WavefrontParams& w, uint32_t block, int sm_count,
                                   uint32_t phases, cudaStream_t stream) {
-  const size_t smem = MODE != MODE_THREADED ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
+  const size_t smem = MODE != MODE_THREADED && !LOCAL ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
   static bool attr_done = false;
   if (!attr_done) {
-    cudaError_t e = cudaFuncSetAttribute(primary_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaError_t e =
+        cudaFuncSetAttribute(primary_kernel<MODE, LOCAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(secondary_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+      e = cudaFuncSetAttribute(secondary_kernel<MODE, LOCAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     if (e == cudaSuccess && MODE != MODE_THREADED)
       e = cudaFuncSetAttribute(secondary_dynamic_kernel<MODE == MODE_THREADED ? MODE_BINARY : MODE>,
                                cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
@@ -285,7 +296,7 @@ cudaError_t launch_wavefront_mode(const TraceParams& p, const WavefrontParams& w
     const uint32_t tiles = ((w.width + 7) / 8) * ((w.height + 3) / 4);
     const uint32_t threads = tiles * 32;
     const uint32_t grid1 = (threads + block - 1) / block;
-    primary_kernel<MODE><<<grid1, block, smem, stream>>>(p, w);
+    primary_kernel<MODE, LOCAL><<<grid1, block, smem, stream>>>(p, w);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
@@ -293,18 +304,18 @@ cudaError_t launch_wavefront_mode(const TraceParams& p, const WavefrontParams& w
   e = cudaMemsetAsync(w.work_counter, 0, 64, stream);
   if (e != cudaSuccess) return e;
   // persistent secondary grid: enough resident blocks to fill every SM
-  const bool dynamic = MODE != MODE_THREADED && w.refill != 0u;
+  const bool dynamic = MODE != MODE_THREADED && w.refill != 0u && !LOCAL;
   int per_sm = 0;
   constexpr int DMODE = MODE == MODE_THREADED ? MODE_BINARY : MODE;  // the threaded walk has no dynamic form
   if (dynamic)
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, secondary_dynamic_kernel<DMODE>, (int)block, smem);
   else
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, secondary_kernel<MODE>, (int)block, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, secondary_kernel<MODE, LOCAL>, (int)block, smem);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
   const uint32_t grid2 = (uint32_t)(sm_count * per_sm);
   if (dynamic) secondary_dynamic_kernel<DMODE><<<grid2, block, smem, stream>>>(p, w);
-  else secondary_kernel<MODE><<<grid2, block, smem, stream>>>(p, w);
+  else secondary_kernel<MODE, LOCAL><<<grid2, block, smem, stream>>>(p, w);
   return cudaGetLastError();
 }
 }  // namespace
@@ -315,9 +326,15 @@ cudaError_t launch_wavefront(const TraceParams& p, const WavefrontParams& w, int
   if (block == 0) block = 64;
   const size_t n = (size_t)w.width * w.height;
   if (n == 0) return cudaSuccess;
-  if (mode == MODE_WIDE4) return launch_wavefront_mode<MODE_WIDE4>(p, w, block, sm_count, phases, stream);
-  if (mode == MODE_BINARY) return launch_wavefront_mode<MODE_BINARY>(p, w, block, sm_count, phases, stream);
-  return launch_wavefront_mode<MODE_THREADED>(p, w, block, sm_count, phases, stream);
+  // the local-memory stack holds kLocalStackEntries entries; deeper trees keep the shared-memory stack
+  const bool local = w.local_stack && mode != MODE_THREADED && p.stack_depth <= kLocalStackEntries;
+  if (mode == MODE_WIDE4)
+    return local ? launch_wavefront_mode<MODE_WIDE4, true>(p, w, block, sm_count, phases, stream)
+                 : launch_wavefront_mode<MODE_WIDE4, false>(p, w, block, sm_count, phases, stream);
+  if (mode == MODE_BINARY)
+    return local ? launch_wavefront_mode<MODE_BINARY, true>(p, w, block, sm_count, phases, stream)
+                 : launch_wavefront_mode<MODE_BINARY, false>(p, w, block, sm_count, phases, stream);
+  return launch_wavefront_mode<MODE_THREADED, false>(p, w, block, sm_count, phases, stream);
 }
 
 }  // namespace rdn

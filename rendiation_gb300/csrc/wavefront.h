@@ -37,6 +37,9 @@ struct WavefrontParams {
   // secondary schedule: 0 = batches of 32 per warp; k = 1..32: a warp refills
   // its idle lanes whenever at least k are idle (ordered walks only)
   uint32_t refill;
+  // 1: traversal stacks in local memory (ordered walks, trees up to the
+  // local stack's depth); 0: in shared memory
+  uint32_t local_stack;
 };
 
 size_t wavefront_scratch_bytes(uint32_t width, uint32_t height);

@@ -261,16 +261,19 @@ class Wavefront:
         self.phase_config = None  # (primary, secondary) (traversal, block) when they differ
 
     def configure(self, primary, secondary, refill=None):
-        """Per-kernel (traversal, block_size); a frame then issues one call per kernel.
-        refill: secondary schedule (0 = batches of 32 rays per warp, k = dynamic
-        fetch whenever k lanes of a warp are idle); None keeps the current one."""
+        """Per-kernel (traversal, block_size[, local_stack]); a frame then issues
+        one call per kernel. refill: secondary schedule (0 = batches of 32 rays
+        per warp, k = dynamic fetch whenever k lanes of a warp are idle); None
+        keeps the current one."""
         if refill is not None:
             self.desc.refill = refill
-        if tuple(primary) == tuple(secondary):
-            self.desc.traversal, self.desc.block_size = primary
+        primary = tuple(primary) + (0,) * (3 - len(primary))
+        secondary = tuple(secondary) + (0,) * (3 - len(secondary))
+        if primary == secondary:
+            self.desc.traversal, self.desc.block_size, self.desc.local_stack = primary
             self.phase_config = None
         else:
-            self.phase_config = (tuple(primary), tuple(secondary))
+            self.phase_config = (primary, secondary)
 
     def run(self, sample_index=0, stream=None, phases=0):
         """phases: 0 both kernels, 1 primary only, 2 secondary only (queues of the last primary run)."""
@@ -283,11 +286,11 @@ class Wavefront:
             _check(self.system._h, self.system._L.rdn_wavefront_shadow_bounce(self.system._h, C.byref(self.desc),
                                                                               C.c_void_p(s)))
             return
-        for ph, (trav, block) in zip((1, 2), self.phase_config):
+        for ph, (trav, block, local) in zip((1, 2), self.phase_config):
             if phases and phases != ph:
                 continue
             self.desc.phases = ph
-            self.desc.traversal, self.desc.block_size = trav, block
+            self.desc.traversal, self.desc.block_size, self.desc.local_stack = trav, block, local
             _check(self.system._h, self.system._L.rdn_wavefront_shadow_bounce(self.system._h, C.byref(self.desc),
                                                                               C.c_void_p(s)))
 

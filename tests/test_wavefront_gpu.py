@@ -86,3 +86,23 @@ def test_wavefront_dynamic_fetch_instanced(refill, cuda):
         assert np.array_equal(got["light"][ok], exp["light"][ok])
         bsame = (got["bounce_prim"] == exp["bounce_prim"]) | (got["bounce_t"] == exp["bounce_t"])
         assert np.all(bsame[ok])
+
+
+@pytest.mark.parametrize("traversal", [rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_WIDE])
+def test_wavefront_local_memory_stack(traversal, cuda):
+    """Traversal stacks in local memory instead of shared memory: same results."""
+    mesh = scenes.heightfield(128, seed=1)
+    cam = scenes.heightfield_camera(160, 96)
+    sc = single_mesh_scene(mesh)
+    P = sc.build_product()
+    a = rt.Wavefront(P, cam, LIGHT, traversal=traversal)
+    b = rt.Wavefront(P, cam, LIGHT, traversal=traversal)
+    b.desc.local_stack = 1
+    a.run(2)
+    b.run(2)
+    torch.cuda.synchronize()
+    ra, rb = a.results(), b.results()
+    assert a.rays_traced() == b.rays_traced()
+    same = ra["primary_prim"] == rb["primary_prim"]
+    assert same.mean() > 0.999 and np.array_equal(ra["primary_t"].view(np.uint32), rb["primary_t"].view(np.uint32))
+    assert np.array_equal(ra["light"][same], rb["light"][same])
