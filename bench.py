@@ -443,15 +443,18 @@ def bench_batched(args):
     if args.tune and args.traversal == "ordered":
         from rendiation_gb300.autotune import Autotuner, grid
 
-        cands = grid(traversal=[rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_WIDE], block=[64, 128],
-                     sort_key=[rt.SORT_NONE, rt.SORT_SCENE_OCTANT], refill=[0, 8, 16])
+        orders = [rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_WIDE]
+        cands = (grid(traversal=orders, block=[64, 128], sort_key=[rt.SORT_NONE], refill=[0], local=[0, 1])
+                 + grid(traversal=orders, block=[64], sort_key=[rt.SORT_SCENE_OCTANT], refill=[0], local=[0, 1])
+                 + grid(traversal=orders, block=[64], sort_key=[rt.SORT_NONE], refill=[8, 16], local=[0]))
 
         def run(c):
-            batched.configure(c["traversal"], c["block"], c["sort_key"], c["refill"])
+            batched.configure(c["traversal"], c["block"], c["sort_key"], c["refill"], c["local"])
             batched.run()
 
         res = Autotuner().tune("batched-paths", cands, run, reps=2)
-        batched.configure(res.best["traversal"], res.best["block"], res.best["sort_key"], res.best["refill"])
+        batched.configure(res.best["traversal"], res.best["block"], res.best["sort_key"], res.best["refill"],
+                          res.best["local"])
         tuned = {"best": res.best, "timings_ms": res.timings_ms}
     batched.capture()
     for _ in range(args.warmup):
@@ -578,6 +581,24 @@ def bench_adjoint(args):
     stream = torch.cuda.current_stream()
     sp = C.c_void_p(stream.cuda_stream)
 
+    # traversal stacks in shared or local memory: the faster forward decides
+    def fwd_ms(ls, reps=20):
+        fwd.local_stack = ls
+        for _ in range(3):
+            assert L.rdn_attr_loss_forward(P._h, C.byref(fwd), sp) == 0
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            assert L.rdn_attr_loss_forward(P._h, C.byref(fwd), sp) == 0
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    stack_ms = {ls: fwd_ms(ls) for ls in (0, 1)}
+    local = min(stack_ms, key=stack_ms.get)
+    for dsc in (fwd, fwd_rec, adj, adj_rec):
+        dsc.local_stack = local
+
     def run(mode):
         loss.zero_()
         assert L.rdn_attr_loss_forward(P._h, C.byref(fwd_rec if mode == "tape" else fwd), sp) == 0
@@ -601,6 +622,7 @@ def bench_adjoint(args):
     out["fwd_adjoint_over_fwd"] = round(out["forward_adjoint_ms"] / out["forward_ms"], 3)
     out["fwd_adjoint_retrace_over_fwd"] = round(out["forward_adjoint_retrace_ms"] / out["forward_ms"], 3)
     out["adjoint"] = "from the forward's recorded hits (8 B per ray); _retrace: hits traced again"
+    out["local_stack"] = local
     out["loss"] = float(loss.item())
     out["workload"] = f"heightfield {n_grid}^2 ({mesh.triangle_count} tris), {res}x{res} rays, attribute loss"
     P.close()
@@ -683,19 +705,39 @@ def bench_batched_adjoint(args):
     tape_inst = torch.zeros(n * seg, dtype=torch.int32, device="cuda")
     tape_rays = torch.zeros((n * seg, 8), device="cuda")
     tape = dict(seg_tri=tape_tri.data_ptr(), seg_inst=tape_inst.data_ptr(), seg_rays=tape_rays.data_ptr())
+    stream = torch.cuda.current_stream()
+    sp = C.c_void_p(stream.cuda_stream)
+
+    def graph_ms(dsc, reps=3):
+        h = C.c_void_p()
+        assert L.rdn_attr_paths_graph(P._h, C.byref(dsc), nv, C.byref(h)) == 0
+        L.rdn_graph_launch(h, sp)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            L.rdn_graph_launch(h, sp)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        L.rdn_graph_destroy(h)
+        return e0.elapsed_time(e1) / reps
+
+    # traversal stacks in shared or local memory: the faster forward decides
+    stack_ms = {ls: graph_ms(desc(targets=targets.data_ptr(), loss_sum=loss.data_ptr(), local_stack=ls))
+                for ls in (0, 1)}
+    local = min(stack_ms, key=stack_ms.get)
     both = desc(targets=targets.data_ptr(), loss_sum=loss.data_ptr(), grad_vertices=grad.data_ptr(), from_record=1,
-                **tape)
-    retrace = desc(targets=targets.data_ptr(), loss_sum=loss.data_ptr(), grad_vertices=grad.data_ptr())
-    fwd = desc(targets=targets.data_ptr(), loss_sum=loss.data_ptr())
+                local_stack=local, **tape)
+    retrace = desc(targets=targets.data_ptr(), loss_sum=loss.data_ptr(), grad_vertices=grad.data_ptr(),
+                   local_stack=local)
+    fwd = desc(targets=targets.data_ptr(), loss_sum=loss.data_ptr(), local_stack=local)
     g = C.c_void_p()
     assert L.rdn_attr_paths_graph(P._h, C.byref(both), nv, C.byref(g)) == 0
     gr = C.c_void_p()
     assert L.rdn_attr_paths_graph(P._h, C.byref(retrace), nv, C.byref(gr)) == 0
     gf = C.c_void_p()
     assert L.rdn_attr_paths_graph(P._h, C.byref(fwd), nv, C.byref(gf)) == 0
-    stream = torch.cuda.current_stream()
-    sp = C.c_void_p(stream.cuda_stream)
-    out = {}
+    out = {"local_stack": local, "forward_ms_by_stack": {("local" if k else "shared"): round(v, 3)
+                                                          for k, v in stack_ms.items()}}
     for name, handle in (("forward", gf), ("forward_adjoint", g), ("forward_adjoint_retrace", gr)):
         for _ in range(args.warmup):
             L.rdn_graph_launch(handle, sp)

@@ -182,7 +182,8 @@ typedef struct rdn_trace_desc {
   uint32_t traversal;       /* RDN_TRAVERSAL_* */
   uint32_t anyhit_mode;     /* RDN_ANYHIT_* */
   uint32_t block_size;      /* 0 = 64 */
-  uint32_t reserved;
+  uint32_t local_stack;      /* ordered walks: 1 = per-thread traversal stacks in local memory (L1)
+                                instead of shared memory, for trees whose stack fits 64 entries */
 } rdn_trace_desc;
 
 /* Counters of node visits and triangle tests, the reference's
@@ -351,6 +352,7 @@ typedef struct rdn_path_desc {
   uint32_t refill;              /* schedule of the ordered walks: 0 = each warp traces 32 queued rays
                                    together; k in 1..32 = each lane keeps its own query and a warp takes
                                    new rays whenever k lanes are idle (dynamic fetch) */
+  uint32_t local_stack;         /* ordered walks, batch schedule: 1 = traversal stacks in local memory */
 } rdn_path_desc;
 
 /* Ray-sort keys (stable radix sort of each queue before its bounce). */
@@ -401,6 +403,7 @@ typedef struct rdn_attr_loss_desc {
                                    hit_tri / hit_inst instead of tracing the rays again */
   uint32_t* hit_tri;            /* device, nullable: built triangle of each ray's hit, RDN_MISS (forward) */
   uint32_t* hit_inst;           /* device, nullable: TLAS instance slot of each ray's hit (forward) */
+  uint32_t local_stack;         /* ordered walks: 1 = traversal stacks in local memory */
 } rdn_attr_loss_desc;
 
 /* Forward: trace, interpolate, loss. Extends the reference's closest-hit query
@@ -442,6 +445,7 @@ typedef struct rdn_attr_path_desc {
   uint32_t from_record;         /* adjoint: 1 = differentiate the segments recorded by the forward in
                                    seg_tri / seg_inst / seg_rays (a tape) instead of tracing the paths again */
   uint32_t* seg_inst;           /* device, nullable: TLAS instance slot of each segment's hit (forward) */
+  uint32_t local_stack;         /* ordered walks: 1 = traversal stacks in local memory */
 } rdn_attr_path_desc;
 
 rdn_status rdn_attr_paths_forward(rdn_ctx* ctx, const rdn_attr_path_desc* desc, void* stream);

@@ -173,9 +173,9 @@ __device__ __forceinline__ float residual(const HitGeom& h, float a0, float a1, 
   return d.hi + d.lo;
 }
 
-template <int MODE>
+template <int MODE, bool LOCAL>
 __global__ void __launch_bounds__(128) attr_forward_kernel(TraceParams p, AdjointParams a) {
-  extern __shared__ uint2 smem_stack[];
+  RDN_TRAVERSAL_STACK(LOCAL);
   __shared__ double block_sum[4];
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   float loss = 0.0f;
@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(128) attr_forward_kernel(TraceParams p, Adjoin
     R.cull_mask = 0xFFu;
     R.ray_flags = 0u;
     bool bad;
-    traverse_ray<MODE, false>(p, R, a.tlas_uniform, smem_stack + threadIdx.x, blockDim.x, bad);
+    traverse_ray<MODE, false>(p, R, a.tlas_uniform, stack_ptr, stack_stride, bad);
     float value = 0.0f;
     if (R.best.have) {
       const InstanceRay ir = to_instance(p.tlas_data + R.best.inst, R.o, R.d, 0u);
@@ -217,9 +217,9 @@ __global__ void __launch_bounds__(128) attr_forward_kernel(TraceParams p, Adjoin
   }
 }
 
-template <int MODE>
+template <int MODE, bool LOCAL>
 __global__ void __launch_bounds__(128) attr_adjoint_kernel(TraceParams p, AdjointParams a) {
-  extern __shared__ uint2 smem_stack[];
+  RDN_TRAVERSAL_STACK(LOCAL);
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.count) return;
   const float4* rp = a.rays + 2 * (size_t)i;
@@ -232,7 +232,7 @@ __global__ void __launch_bounds__(128) attr_adjoint_kernel(TraceParams p, Adjoin
   R.cull_mask = 0xFFu;
   R.ray_flags = 0u;
   bool bad;
-  traverse_ray<MODE, false>(p, R, a.tlas_uniform, smem_stack + threadIdx.x, blockDim.x, bad);
+  traverse_ray<MODE, false>(p, R, a.tlas_uniform, stack_ptr, stack_stride, bad);
   float3 go = make_float3(0.f, 0.f, 0.f), gd = go;
   if (R.best.have) {
     const InstanceRay ir = to_instance(p.tlas_data + R.best.inst, R.o, R.d, 0u);
@@ -276,9 +276,9 @@ __device__ __forceinline__ float3 scatter_vertex_grads(const HitGeom& h, const I
 }
 
 // Persistent warps over paths; ADJOINT selects the gradient pass.
-template <int MODE, bool ADJOINT>
+template <int MODE, bool ADJOINT, bool LOCAL>
 __global__ void __launch_bounds__(128) attr_path_kernel(TraceParams p, PathAdjointParams a) {
-  extern __shared__ uint2 smem_stack[];
+  RDN_TRAVERSAL_STACK(LOCAL);
   __shared__ double block_sum[4];
   const uint32_t lane = threadIdx.x & 31u;
   double loss_acc = 0.0;
@@ -310,7 +310,7 @@ __global__ void __launch_bounds__(128) attr_path_kernel(TraceParams p, PathAdjoi
         R.cull_mask = 0xFFu;
         R.ray_flags = 0u;
         bool bad;
-        traverse_ray<MODE, false>(p, R, tlas, smem_stack + threadIdx.x, blockDim.x, bad);
+        traverse_ray<MODE, false>(p, R, tlas, stack_ptr, stack_stride, bad);
         if (!R.best.have) {
           alive = false;
           if (!ADJOINT && a.targets) {
@@ -464,17 +464,18 @@ inline uint32_t recorded_grid(size_t items, int sm_count) {
   return (uint32_t)(need < cap ? (need ? need : 1) : cap);
 }
 
-template <int MODE>
-cudaError_t launch_attr_paths_mode(const TraceParams& p, const PathAdjointParams& a, bool adjoint, uint32_t block,
-                                   int sm_count, cudaStream_t stream) {
+template <int MODE, bool LOCAL>
+cudaError_t launch_attr_paths_variant(const TraceParams& p, const PathAdjointParams& a, bool adjoint, uint32_t block,
+                                      int sm_count, cudaStream_t stream) {
   static bool done[2] = {false, false};
-  const void* fn = adjoint ? (const void*)attr_path_kernel<MODE, true> : (const void*)attr_path_kernel<MODE, false>;
+  const void* fn = adjoint ? (const void*)attr_path_kernel<MODE, true, LOCAL>
+                           : (const void*)attr_path_kernel<MODE, false, LOCAL>;
   if (!done[adjoint]) {
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     if (e != cudaSuccess) return e;
     done[adjoint] = true;
   }
-  const size_t smem = MODE != MODE_THREADED ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
+  const size_t smem = MODE != MODE_THREADED && !LOCAL ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
   int per_sm = 0;
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (int)block, smem);
   if (e != cudaSuccess) return e;
@@ -484,28 +485,44 @@ cudaError_t launch_attr_paths_mode(const TraceParams& p, const PathAdjointParams
   if (grid > need) grid = need;
   e = cudaMemsetAsync(a.work_counter, 0, 4, stream);
   if (e != cudaSuccess) return e;
-  if (adjoint) attr_path_kernel<MODE, true><<<grid, block, smem, stream>>>(p, a);
-  else attr_path_kernel<MODE, false><<<grid, block, smem, stream>>>(p, a);
+  if (adjoint) attr_path_kernel<MODE, true, LOCAL><<<grid, block, smem, stream>>>(p, a);
+  else attr_path_kernel<MODE, false, LOCAL><<<grid, block, smem, stream>>>(p, a);
+  return cudaGetLastError();
+}
+
+template <int MODE>
+cudaError_t launch_attr_paths_mode(const TraceParams& p, const PathAdjointParams& a, bool adjoint, uint32_t block,
+                                   int sm_count, cudaStream_t stream) {
+  if (MODE != MODE_THREADED && p.local_stack)
+    return launch_attr_paths_variant<MODE, MODE != MODE_THREADED>(p, a, adjoint, block, sm_count, stream);
+  return launch_attr_paths_variant<MODE, false>(p, a, adjoint, block, sm_count, stream);
+}
+
+template <int MODE, bool LOCAL>
+cudaError_t launch_attr_variant(const TraceParams& p, const AdjointParams& a, bool adjoint, uint32_t block,
+                                cudaStream_t stream) {
+  static bool done[2] = {false, false};
+  if (!done[adjoint]) {
+    cudaError_t e = adjoint ? cudaFuncSetAttribute(attr_adjoint_kernel<MODE, LOCAL>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024)
+                            : cudaFuncSetAttribute(attr_forward_kernel<MODE, LOCAL>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e != cudaSuccess) return e;
+    done[adjoint] = true;
+  }
+  const size_t smem = MODE != MODE_THREADED && !LOCAL ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
+  const uint32_t grid = (a.count + block - 1) / block;
+  if (adjoint) attr_adjoint_kernel<MODE, LOCAL><<<grid, block, smem, stream>>>(p, a);
+  else attr_forward_kernel<MODE, LOCAL><<<grid, block, smem, stream>>>(p, a);
   return cudaGetLastError();
 }
 
 template <int MODE>
 cudaError_t launch_attr_mode(const TraceParams& p, const AdjointParams& a, bool adjoint, uint32_t block,
                              cudaStream_t stream) {
-  static bool done[2] = {false, false};
-  if (!done[adjoint]) {
-    cudaError_t e = adjoint ? cudaFuncSetAttribute(attr_adjoint_kernel<MODE>,
-                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024)
-                            : cudaFuncSetAttribute(attr_forward_kernel<MODE>,
-                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    if (e != cudaSuccess) return e;
-    done[adjoint] = true;
-  }
-  const size_t smem = MODE != MODE_THREADED ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
-  const uint32_t grid = (a.count + block - 1) / block;
-  if (adjoint) attr_adjoint_kernel<MODE><<<grid, block, smem, stream>>>(p, a);
-  else attr_forward_kernel<MODE><<<grid, block, smem, stream>>>(p, a);
-  return cudaGetLastError();
+  if (MODE != MODE_THREADED && p.local_stack)
+    return launch_attr_variant<MODE, MODE != MODE_THREADED>(p, a, adjoint, block, stream);
+  return launch_attr_variant<MODE, false>(p, a, adjoint, block, stream);
 }
 
 cudaError_t launch_attr(const TraceParams& p, const AdjointParams& a, int mode, bool adjoint, uint32_t block,

@@ -35,12 +35,12 @@ using namespace dev;
 
 // Queue of bounce b: rays (2 float4) and states {id, tlas, throughput, 0}.
 // from_user: bounce 0 reads the caller's primary rays instead of a queue.
-template <int MODE>
+template <int MODE, bool LOCAL>
 __global__ void __launch_bounds__(128) path_kernel(TraceParams p, PathParams q, uint32_t bounce, bool from_user,
                                                    const float4* __restrict__ in_rays,
                                                    const uint4* __restrict__ in_state, float4* __restrict__ out_rays,
                                                    uint4* __restrict__ out_state) {
-  extern __shared__ uint2 smem_stack[];
+  RDN_TRAVERSAL_STACK(LOCAL);
   const uint32_t n = bounce == 0 ? q.count : *(volatile uint32_t*)(q.queue_count + bounce - 1);
   const uint32_t lane = threadIdx.x & 31u;
   uint32_t* work = q.work_counter + bounce;
@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(128) path_kernel(TraceParams p, PathParams q, 
       R.cull_mask = 0xFFu;
       R.ray_flags = 0u;
       bool bad;
-      traverse_ray<MODE, false>(p, R, tlas, smem_stack + threadIdx.x, blockDim.x, bad);
+      traverse_ray<MODE, false>(p, R, tlas, stack_ptr, stack_stride, bad);
       if (!R.best.have) {
         q.out[id] = make_float2(throughput, __uint_as_float(bounce | RDN_PATH_ESCAPED));
       } else if (bounce == q.max_bounces) {
@@ -322,25 +322,34 @@ void paths_bind_scratch(PathParams& q, void* scratch) {
 }
 
 namespace {
-const void* path_fn(int mode, bool dynamic) {
-  if (mode == MODE_WIDE4) return dynamic ? (const void*)path_dynamic_kernel<MODE_WIDE4> : (const void*)path_kernel<MODE_WIDE4>;
+// kernel variant: 0 batch, 1 dynamic fetch, 2 batch with local-memory stacks
+int path_variant(int mode, const TraceParams& p, const PathParams& q) {
+  if (mode == MODE_THREADED) return 0;
+  if (q.refill != 0) return 1;
+  return p.local_stack ? 2 : 0;
+}
+const void* path_fn(int mode, int variant) {
+  if (mode == MODE_WIDE4)
+    return variant == 1 ? (const void*)path_dynamic_kernel<MODE_WIDE4>
+                        : (variant == 2 ? (const void*)path_kernel<MODE_WIDE4, true> : (const void*)path_kernel<MODE_WIDE4, false>);
   if (mode == MODE_BINARY)
-    return dynamic ? (const void*)path_dynamic_kernel<MODE_BINARY> : (const void*)path_kernel<MODE_BINARY>;
-  return (const void*)path_kernel<MODE_THREADED>;
+    return variant == 1 ? (const void*)path_dynamic_kernel<MODE_BINARY>
+                        : (variant == 2 ? (const void*)path_kernel<MODE_BINARY, true> : (const void*)path_kernel<MODE_BINARY, false>);
+  return (const void*)path_kernel<MODE_THREADED, false>;
 }
 }  // namespace
 
 cudaError_t prepare_paths(const TraceParams& p, const PathParams& q, int mode, uint32_t block, int sm_count,
                           uint32_t* grid) {
   if (block == 0) block = 64;
-  const size_t smem = mode != MODE_THREADED ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
-  static bool attr_done[2][3] = {{false, false, false}, {false, false, false}};
-  const bool dynamic = mode != MODE_THREADED && q.refill != 0;
-  const void* fn = path_fn(mode, dynamic);
-  if (!attr_done[dynamic][mode]) {
+  const int variant = path_variant(mode, p, q);
+  const size_t smem = mode != MODE_THREADED && variant != 2 ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
+  static bool attr_done[3][3] = {};
+  const void* fn = path_fn(mode, variant);
+  if (!attr_done[variant][mode]) {
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     if (e != cudaSuccess) return e;
-    attr_done[dynamic][mode] = true;
+    attr_done[variant][mode] = true;
   }
   int per_sm = 0;
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (int)block, smem);
@@ -357,7 +366,8 @@ cudaError_t record_paths(const TraceParams& p, const PathParams& q, int mode, ui
                          cudaStream_t stream) {
   if (block == 0) block = 64;
   if (q.count == 0 || grid == 0) return cudaSuccess;
-  const size_t smem = mode != MODE_THREADED ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
+  const int variant = path_variant(mode, p, q);
+  const size_t smem = mode != MODE_THREADED && variant != 2 ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
   cudaError_t e = cudaMemsetAsync(q.queue_count, 0, sizeof(uint32_t) * 2 * (q.max_bounces + 1), stream);
   if (e != cudaSuccess) return e;
   float4* ra = static_cast<float4*>(q.rays_a);
@@ -397,17 +407,20 @@ cudaError_t record_paths(const TraceParams& p, const PathParams& q, int mode, ui
       out_r = (b & 1) ? ra : rb;
       out_s = (b & 1) ? sa : sb;
     }
-    const bool dynamic = mode != MODE_THREADED && q.refill != 0;
-    if (mode == MODE_WIDE4 && dynamic)
+    if (mode == MODE_WIDE4 && variant == 1)
       path_dynamic_kernel<MODE_WIDE4><<<grid, block, smem, stream>>>(p, q, b, from_user, in_r, in_s, out_r, out_s);
+    else if (mode == MODE_WIDE4 && variant == 2)
+      path_kernel<MODE_WIDE4, true><<<grid, block, smem, stream>>>(p, q, b, from_user, in_r, in_s, out_r, out_s);
     else if (mode == MODE_WIDE4)
-      path_kernel<MODE_WIDE4><<<grid, block, smem, stream>>>(p, q, b, from_user, in_r, in_s, out_r, out_s);
-    else if (mode == MODE_BINARY && dynamic)
+      path_kernel<MODE_WIDE4, false><<<grid, block, smem, stream>>>(p, q, b, from_user, in_r, in_s, out_r, out_s);
+    else if (mode == MODE_BINARY && variant == 1)
       path_dynamic_kernel<MODE_BINARY><<<grid, block, smem, stream>>>(p, q, b, from_user, in_r, in_s, out_r, out_s);
+    else if (mode == MODE_BINARY && variant == 2)
+      path_kernel<MODE_BINARY, true><<<grid, block, smem, stream>>>(p, q, b, from_user, in_r, in_s, out_r, out_s);
     else if (mode == MODE_BINARY)
-      path_kernel<MODE_BINARY><<<grid, block, smem, stream>>>(p, q, b, from_user, in_r, in_s, out_r, out_s);
+      path_kernel<MODE_BINARY, false><<<grid, block, smem, stream>>>(p, q, b, from_user, in_r, in_s, out_r, out_s);
     else
-      path_kernel<MODE_THREADED><<<grid, block, smem, stream>>>(p, q, b, from_user, in_r, in_s, out_r, out_s);
+      path_kernel<MODE_THREADED, false><<<grid, block, smem, stream>>>(p, q, b, from_user, in_r, in_s, out_r, out_s);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }

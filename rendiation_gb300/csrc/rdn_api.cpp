@@ -190,6 +190,8 @@ rdn_status fill_params(rdn_ctx* c, const rdn_trace_desc* desc, rdn::TraceParams&
   p.geom_root_code4 = d.geom_root_code4.ptr;
   p.counters = reinterpret_cast<unsigned long long*>(c->d_counters);
   p.error_word = c->d_counters + 8;
+  p.local_stack = desc->local_stack && desc->traversal != RDN_TRAVERSAL_REFERENCE &&
+                  p.stack_depth <= rdn::kLocalStackEntries;
   return RDN_OK;
 }
 
@@ -204,6 +206,7 @@ rdn_status validate_trace(rdn_ctx* c, const rdn_trace_desc* desc) {
   if (desc->anyhit_mode > RDN_ANYHIT_ACCEPT_EVEN_PRIMS) return fail(c, RDN_ERR_INVALID_ARG, "unknown any-hit mode");
   if (desc->block_size && (desc->block_size % 32 || desc->block_size > 256))
     return fail(c, RDN_ERR_INVALID_ARG, "block_size must be a multiple of 32 up to 256");
+  if (desc->local_stack > 1) return fail(c, RDN_ERR_INVALID_ARG, "local_stack must be 0 or 1");
   return RDN_OK;
 }
 
@@ -572,6 +575,7 @@ rdn_status prepare_path_launch(rdn_ctx* c, const rdn_path_desc* d, rdn::TracePar
   td.tlas_uniform = d->tlas_uniform;
   td.cull_mask = 0xFF;
   td.traversal = d->traversal;
+  td.local_stack = d->local_stack;
   fill_params(c, &td, p);
   std::memset(&q, 0, sizeof(q));
   q.primary_rays = reinterpret_cast<const float4*>(d->rays);
@@ -702,6 +706,7 @@ rdn_status prepare_attr(rdn_ctx* c, const rdn_attr_loss_desc* d, bool adjoint, r
   td.tlas_uniform = d->tlas_uniform;
   td.cull_mask = 0xFF;
   td.traversal = d->traversal;
+  td.local_stack = d->local_stack;
   fill_params(c, &td, p);
   std::memset(&a, 0, sizeof(a));
   a.rays = reinterpret_cast<const float4*>(d->rays);
@@ -784,6 +789,7 @@ rdn_status prepare_attr_paths(rdn_ctx* c, const rdn_attr_path_desc* d, bool adjo
   td.tlas_uniform = d->tlas_uniform;
   td.cull_mask = 0xFF;
   td.traversal = d->traversal;
+  td.local_stack = d->local_stack;
   fill_params(c, &td, p);
   std::memset(&a, 0, sizeof(a));
   a.rays = reinterpret_cast<const float4*>(d->rays);

@@ -12,9 +12,9 @@ namespace {
 
 using namespace dev;
 
-template <int MODE, bool COUNT>
+template <int MODE, bool COUNT, bool LOCAL>
 __global__ void __launch_bounds__(256) trace_kernel(TraceParams p) {
-  extern __shared__ uint2 smem_stack[];
+  RDN_TRAVERSAL_STACK(LOCAL);
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= p.count) return;
   const float4* rp = p.rays + 2 * (size_t)i;
@@ -28,7 +28,7 @@ __global__ void __launch_bounds__(256) trace_kernel(TraceParams p) {
   R.ray_flags = p.ray_flags;
   const uint32_t tidx = p.tlas_idx ? __ldg(p.tlas_idx + i) : p.tlas_uniform;
   bool bad;
-  traverse_ray<MODE, COUNT>(p, R, tidx, smem_stack + threadIdx.x, blockDim.x, bad);
+  traverse_ray<MODE, COUNT>(p, R, tidx, stack_ptr, stack_stride, bad);
 
   float4 out;
   uint4 ext;
@@ -70,30 +70,39 @@ uint32_t stack_entries(int mode, uint32_t max_binary_depth, uint32_t max_wide4_d
   return d < 8 ? 8 : d;
 }
 
+namespace {
+template <int MODE, bool COUNT, bool LOCAL>
+cudaError_t launch_trace_variant(const TraceParams& p, uint32_t block, uint32_t grid, cudaStream_t stream) {
+  const size_t smem = MODE != MODE_THREADED && !LOCAL ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
+  static bool attr_done = false;
+  if (!attr_done) {
+    cudaError_t e = cudaFuncSetAttribute(trace_kernel<MODE, COUNT, LOCAL>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e != cudaSuccess) return e;
+    attr_done = true;
+  }
+  trace_kernel<MODE, COUNT, LOCAL><<<grid, block, smem, stream>>>(p);
+  return cudaGetLastError();
+}
+}  // namespace
+
 cudaError_t launch_trace(const TraceParams& p, int mode, bool counted, uint32_t block, cudaStream_t stream) {
   if (p.count == 0) return cudaSuccess;
   if (block == 0) block = 64;
   const uint32_t grid = (p.count + block - 1) / block;
-  const size_t smem = mode != MODE_THREADED ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
-  static bool attr_done[6] = {};
-  const void* fns[6] = {(const void*)trace_kernel<0, false>, (const void*)trace_kernel<0, true>,
-                        (const void*)trace_kernel<1, false>, (const void*)trace_kernel<1, true>,
-                        (const void*)trace_kernel<2, false>, (const void*)trace_kernel<2, true>};
-  const int slot = 2 * mode + (counted ? 1 : 0);
-  if (!attr_done[slot]) {
-    cudaError_t e = cudaFuncSetAttribute(fns[slot], cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    if (e != cudaSuccess) return e;
-    attr_done[slot] = true;
+  const bool local = p.local_stack != 0;
+  if (mode == MODE_WIDE4) {
+    if (counted) return launch_trace_variant<MODE_WIDE4, true, false>(p, block, grid, stream);
+    return local ? launch_trace_variant<MODE_WIDE4, false, true>(p, block, grid, stream)
+                 : launch_trace_variant<MODE_WIDE4, false, false>(p, block, grid, stream);
   }
-  switch (slot) {
-    case 0: trace_kernel<0, false><<<grid, block, smem, stream>>>(p); break;
-    case 1: trace_kernel<0, true><<<grid, block, smem, stream>>>(p); break;
-    case 2: trace_kernel<1, false><<<grid, block, smem, stream>>>(p); break;
-    case 3: trace_kernel<1, true><<<grid, block, smem, stream>>>(p); break;
-    case 4: trace_kernel<2, false><<<grid, block, smem, stream>>>(p); break;
-    default: trace_kernel<2, true><<<grid, block, smem, stream>>>(p); break;
+  if (mode == MODE_BINARY) {
+    if (counted) return launch_trace_variant<MODE_BINARY, true, false>(p, block, grid, stream);
+    return local ? launch_trace_variant<MODE_BINARY, false, true>(p, block, grid, stream)
+                 : launch_trace_variant<MODE_BINARY, false, false>(p, block, grid, stream);
   }
-  return cudaGetLastError();
+  return counted ? launch_trace_variant<MODE_THREADED, true, false>(p, block, grid, stream)
+                 : launch_trace_variant<MODE_THREADED, false, false>(p, block, grid, stream);
 }
 
 }  // namespace rdn

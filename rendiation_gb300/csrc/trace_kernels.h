@@ -31,8 +31,14 @@ struct TraceParams {
   const float4* wide4;  // 8 per node (Wide4Node)
   const uint32_t* geom_root_code4;
   unsigned long long* counters;  // 4 x u64, used by counted launches
-  uint32_t* error_word;          // bit 0 stack overflow, bit 1 bad tlas index
+  uint32_t* error_word;          // bit 0 stack overflow, bit 1 bad tlas index, bit 2 iteration cap
+  // 1: per-thread traversal stacks in local memory (ordered walks whose stack
+  // fits kLocalStackEntries), 0: in shared memory
+  uint32_t local_stack;
 };
+
+// entries of a local-memory traversal stack
+constexpr uint32_t kLocalStackEntries = 64;
 
 // Traversal modes (template argument of every traversal kernel).
 enum TraversalMode : int { MODE_THREADED = 0, MODE_BINARY = 1, MODE_WIDE4 = 2 };

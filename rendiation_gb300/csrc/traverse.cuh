@@ -32,6 +32,15 @@
 #include "rdn_core.h"
 #include "trace_kernels.h"
 
+// Per-thread traversal stack of a kernel: with LOCAL in the thread's local
+// memory (kLocalStackEntries entries, L1-cached), else a column of the
+// dynamic shared-memory block (stride blockDim.x).
+#define RDN_TRAVERSAL_STACK(LOCAL)                                                   \
+  extern __shared__ uint2 smem_stack[];                                              \
+  uint2 local_stack_[(LOCAL) ? ::rdn::kLocalStackEntries : 1];                       \
+  uint2* const stack_ptr = (LOCAL) ? local_stack_ : smem_stack + threadIdx.x;        \
+  const uint32_t stack_stride = (LOCAL) ? 1u : blockDim.x
+
 namespace rdn {
 namespace dev {
 

@@ -38,7 +38,6 @@ using namespace dev;
 
 // LOCAL: the traversal stack lives in the thread's local memory (L1-cached)
 // instead of shared memory, so that the stack no longer limits occupancy.
-constexpr uint32_t kLocalStackEntries = 64;
 
 template <int MODE, bool LOCAL>
 __global__ void __launch_bounds__(128) primary_kernel(TraceParams p, WavefrontParams w) {

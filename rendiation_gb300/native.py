@@ -65,7 +65,7 @@ class TraceDesc(C.Structure):
     _fields_ = [("rays", C.c_void_p), ("hits", C.c_void_p), ("hits_ext", C.c_void_p), ("tlas_idx", C.c_void_p),
                 ("count", C.c_uint32), ("tlas_uniform", C.c_uint32), ("ray_flags", C.c_uint32),
                 ("cull_mask", C.c_uint32), ("traversal", C.c_uint32), ("anyhit_mode", C.c_uint32),
-                ("block_size", C.c_uint32), ("reserved", C.c_uint32)]
+                ("block_size", C.c_uint32), ("local_stack", C.c_uint32)]
 
 
 class Counters(C.Structure):
@@ -92,7 +92,8 @@ class PathDesc(C.Structure):
                 ("max_bounces", C.c_uint32), ("rr_start", C.c_uint32), ("albedo", C.c_float),
                 ("rr_survive", C.c_float), ("seed", C.c_uint32), ("traversal", C.c_uint32),
                 ("block_size", C.c_uint32), ("sort_key", C.c_uint32), ("out", C.c_void_p), ("scratch", C.c_void_p),
-                ("scratch_bytes", C.c_size_t), ("segment_counts", C.c_void_p), ("refill", C.c_uint32)]
+                ("scratch_bytes", C.c_size_t), ("segment_counts", C.c_void_p), ("refill", C.c_uint32),
+                ("local_stack", C.c_uint32)]
 
 
 class AttrLossDesc(C.Structure):
@@ -101,7 +102,7 @@ class AttrLossDesc(C.Structure):
                 ("ray_loss", C.c_void_p), ("loss_sum", C.c_void_p), ("grad_vertices", C.c_void_p),
                 ("grad_ray_origin", C.c_void_p), ("grad_ray_direction", C.c_void_p), ("grad_scale", C.c_float),
                 ("traversal", C.c_uint32), ("block_size", C.c_uint32), ("from_record", C.c_uint32),
-                ("hit_tri", C.c_void_p), ("hit_inst", C.c_void_p)]
+                ("hit_tri", C.c_void_p), ("hit_inst", C.c_void_p), ("local_stack", C.c_uint32)]
 
 
 class AttrPathDesc(C.Structure):
@@ -110,7 +111,7 @@ class AttrPathDesc(C.Structure):
                 ("values", C.c_void_p), ("loss_sum", C.c_void_p), ("grad_vertices", C.c_void_p),
                 ("seg_tri", C.c_void_p), ("seg_rays", C.c_void_p), ("grad_scale", C.c_float),
                 ("traversal", C.c_uint32), ("block_size", C.c_uint32), ("from_record", C.c_uint32),
-                ("seg_inst", C.c_void_p)]
+                ("seg_inst", C.c_void_p), ("local_stack", C.c_uint32)]
 
 
 _lib = None

@@ -176,21 +176,23 @@ class AccelerationStructureSystem:
 
     # --- queries ---
     def _desc(self, rays, hits, hits_ext, tlas_idx, ray_flags, cull_mask, tlas_uniform, traversal, anyhit_mode,
-              block_size, count=None):
+              block_size, count=None, local_stack=0):
         n = rays.shape[0] if count is None else count
         return native.TraceDesc(rays.data_ptr(), hits.data_ptr(), 0 if hits_ext is None else hits_ext.data_ptr(),
                                 0 if tlas_idx is None else tlas_idx.data_ptr(), n, tlas_uniform, ray_flags,
-                                cull_mask, traversal, anyhit_mode, block_size, 0)
+                                cull_mask, traversal, anyhit_mode, block_size, local_stack)
 
     def trace(self, rays, hits, hits_ext=None, tlas_idx=None, ray_flags=0, cull_mask=0xFF, tlas_uniform=0,
-              traversal=TRAVERSAL_ORDERED, anyhit_mode=ANYHIT_ACCEPT, block_size=0, stream=None, count=None):
+              traversal=TRAVERSAL_ORDERED, anyhit_mode=ANYHIT_ACCEPT, block_size=0, stream=None, count=None,
+              local_stack=0):
         """rays: CUDA f32 tensor (N, 8); hits: CUDA f32 tensor (N, 4) (prim id stored as u32 bits);
         hits_ext: optional CUDA int32 tensor (N, 4); tlas_idx: optional CUDA int32 tensor (N,).
-        count overrides N (e.g. 0 for an empty batch)."""
+        count overrides N (e.g. 0 for an empty batch). local_stack: traversal stacks in
+        local memory instead of shared memory (ordered walks)."""
         import torch
 
         d = self._desc(rays, hits, hits_ext, tlas_idx, ray_flags, cull_mask, tlas_uniform, traversal, anyhit_mode,
-                       block_size, count)
+                       block_size, count, local_stack)
         s = (stream or torch.cuda.current_stream()).cuda_stream
         _check(self._h, self._L.rdn_trace(self._h, C.byref(d), C.c_void_p(s)))
 
@@ -335,7 +337,7 @@ class Paths:
         self.graph = None
         self.scratch_bytes = size.value
 
-    def configure(self, traversal=None, block_size=None, sort_key=None, refill=None):
+    def configure(self, traversal=None, block_size=None, sort_key=None, refill=None, local_stack=None):
         """Changes launch knobs (re-capture any graph afterwards). refill: 0 =
         warps trace 32 queued rays together, k = dynamic fetch whenever k lanes
         of a warp are idle."""
@@ -357,6 +359,8 @@ class Paths:
             self.desc.block_size = block_size
         if refill is not None:
             self.desc.refill = refill
+        if local_stack is not None:
+            self.desc.local_stack = local_stack
         self.close()
 
     def run(self, stream=None):

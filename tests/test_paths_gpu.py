@@ -20,7 +20,10 @@ def batched():
 def product_paths(P, b, traversal, graph=False, **kw):
     rays = torch.from_numpy(b.rays.view(np.float32).reshape(-1, 8).copy()).cuda()
     tidx = torch.from_numpy(b.tlas_idx.astype(np.int32)).cuda()
+    local = kw.pop("local", False)
     paths = rt.Paths(P, rays, tidx, traversal=traversal, **kw)
+    if local:
+        paths.configure(local_stack=1)
     if graph:
         paths.capture()
         paths.launch_graph()
@@ -56,13 +59,16 @@ def test_paths_graph_replays_identically(batched, cuda):
     assert np.array_equal(got["radiance"].view(np.uint32), exp["radiance"].view(np.uint32))
 
 
-@pytest.mark.parametrize("refill", [0, 1, 8])
+@pytest.mark.parametrize("refill,local", [(0, 0), (0, 1), (1, 0), (8, 0)])
 @pytest.mark.parametrize("traversal", [rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_WIDE])
-def test_paths_ordered_matches_except_ties(batched, traversal, refill, cuda):
-    """refill > 0: the dynamic-fetch schedule (also replayed from a graph)."""
+def test_paths_ordered_matches_except_ties(batched, traversal, refill, local, cuda):
+    """refill > 0: the dynamic-fetch schedule (also replayed from a graph);
+    local: traversal stacks in local memory."""
     b, S, P = batched
     exp, seg, _ = orc.trace_paths(S, b.rays, b.tlas_idx, max_bounces=4, rr_start=2, seed=5, threads=4)
     got, gseg, first = product_paths(P, b, traversal, graph=refill == 8, seed=5, refill=refill)
+    if local:
+        got, gseg, first = product_paths(P, b, traversal, graph=True, seed=5, local=True)
     if first is not None:
         assert (first["depth_flags"] == got["depth_flags"]).mean() > 0.999
     # a path diverges from the oracle only after an exact-distance tie picks another triangle

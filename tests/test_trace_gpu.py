@@ -221,3 +221,13 @@ def test_rebuild_after_delete(cuda):
     expect, _ = run_oracle(sc2.build_oracle(), rays)
     assert np.array_equal(b["prim"], expect["prim"])
     assert not np.array_equal(a["prim"], b["prim"])
+
+
+@pytest.mark.parametrize("traversal", ORDERED_MODES)
+def test_local_memory_stack_same_hits(soup, traversal, cuda):
+    """Traversal stacks in local memory instead of shared memory: the same hits."""
+    sc, S, P, rays = soup
+    expect, _ = run_oracle(S, rays)
+    got, ext = run_product(P, rays, traversal, local_stack=1)
+    c = classify(got, expect)
+    assert c["other"] == 0 and c["hit_mismatch"] == 0, c
