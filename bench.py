@@ -210,17 +210,20 @@ def bench_wavefront(args, ws, rank):
 
         tuner = Autotuner(args.tune_cache)
         # traversal stack in shared memory (local 0) or in local memory (1)
-        cands = grid(traversal=[rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_WIDE], block=[32, 64, 128], local=[0, 1])
+        orders = [rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_WIDE]
+        # register tier (regs) applies to the local-stack kernels
+        cands = (grid(traversal=orders, block=[32, 64, 128], local=[0])
+                 + grid(traversal=orders, block=[32, 64, 128], local=[1], regs=[0, 1, 2]))
         # secondary schedule: batches of 32 rays per warp (refill 0) or dynamic fetch
-        cands2 = (grid(traversal=[rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_WIDE], block=[32, 64, 128],
-                       refill=[0], local=[0, 1])
-                  + grid(traversal=[rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_WIDE], block=[64], refill=[8, 16],
-                         local=[0]))
+        cands2 = (grid(traversal=orders, block=[32, 64, 128], refill=[0], local=[0])
+                  + grid(traversal=orders, block=[32, 64, 128], refill=[0], local=[1], regs=[0, 1, 2])
+                  + grid(traversal=orders, block=[64], refill=[8, 16], local=[0]))
 
         def run_phase(ph):
             def run(c):
                 wf.desc.traversal, wf.desc.block_size = c["traversal"], c["block"]
                 wf.desc.refill, wf.desc.local_stack = c.get("refill", 0), c.get("local", 0)
+                wf.desc.register_tier = c.get("regs", 0)
                 wf.run(7, phases=ph)
             return run
 
@@ -228,8 +231,8 @@ def bench_wavefront(args, ws, rank):
         torch.cuda.synchronize()
         t1 = tuner.tune("wavefront-primary", cands, run_phase(1))
         t2 = tuner.tune("wavefront-secondary", cands2, run_phase(2))
-        wf.configure((t1.best["traversal"], t1.best["block"], t1.best.get("local", 0)),
-                     (t2.best["traversal"], t2.best["block"], t2.best.get("local", 0)),
+        wf.configure((t1.best["traversal"], t1.best["block"], t1.best.get("local", 0), t1.best.get("regs", 0)),
+                     (t2.best["traversal"], t2.best["block"], t2.best.get("local", 0), t2.best.get("regs", 0)),
                      refill=t2.best.get("refill", 0))
         tuned = {"primary": t1.best, "secondary": t2.best}
 
@@ -295,8 +298,8 @@ def bench_wavefront(args, ws, rank):
     if wf.phase_config is not None:
         wf2.configure(*wf.phase_config, refill=wf.desc.refill)
     else:
-        wf2.configure((wf.desc.traversal, wf.desc.block_size), (wf.desc.traversal, wf.desc.block_size),
-                      refill=wf.desc.refill)
+        same = (wf.desc.traversal, wf.desc.block_size, wf.desc.local_stack, wf.desc.register_tier)
+        wf2.configure(same, same, refill=wf.desc.refill)
     frames = (wf, wf2)
     host_out = [torch.empty(wf.out.shape, dtype=wf.out.dtype, pin_memory=True) for _ in range(2)]
     copy_stream = torch.cuda.Stream()

@@ -300,6 +300,8 @@ typedef struct rdn_wavefront_desc {
                                 a warp takes new rays whenever k lanes are idle (dynamic fetch) */
   uint32_t local_stack;      /* ordered walks: 1 = traversal stacks in the threads' local memory (L1)
                                 instead of shared memory, for trees whose stack fits 64 entries */
+  uint32_t register_tier;    /* local-stack kernels: 0 = 64 registers per thread, 1 = about 80 (no
+                                spills, fewer resident warps), 2 = 51 (more warps, more spills) */
 } rdn_wavefront_desc;
 
 /* Scratch size for the secondary-ray queues of a width x height launch. */

@@ -502,6 +502,7 @@ rdn_status rdn_wavefront_shadow_bounce(rdn_ctx* c, const rdn_wavefront_desc* d, 
   if (d->phases > 3) return fail(c, RDN_ERR_INVALID_ARG, "unknown phase mask");
   if (d->refill > 32) return fail(c, RDN_ERR_INVALID_ARG, "refill must be 0..32");
   if (d->local_stack > 1) return fail(c, RDN_ERR_INVALID_ARG, "local_stack must be 0 or 1");
+  if (d->register_tier > 2) return fail(c, RDN_ERR_INVALID_ARG, "register_tier must be 0, 1 or 2");
   if (d->block_size && (d->block_size % 32 || d->block_size > 128))
     return fail(c, RDN_ERR_INVALID_ARG, "block_size must be a multiple of 32 up to 128");
   std::lock_guard<std::mutex> lk(c->lock);
@@ -532,6 +533,7 @@ rdn_status rdn_wavefront_shadow_bounce(rdn_ctx* c, const rdn_wavefront_desc* d, 
   w.ray_counts = d->ray_counts;
   w.refill = d->refill;
   w.local_stack = d->local_stack;
+  w.register_tier = d->register_tier;
   rdn::wavefront_bind_scratch(w, d->scratch);
   cudaError_t e = cudaSetDevice(c->device);
   if (e == cudaSuccess)
@@ -967,6 +969,7 @@ rdn_status rdn_wavefront_shadow_bounce_static(rdn_ctx* c, const rdn_wavefront_de
   if (d->phases > 3) return fail(c, RDN_ERR_INVALID_ARG, "unknown phase mask");
   if (d->refill > 32) return fail(c, RDN_ERR_INVALID_ARG, "refill must be 0..32");
   if (d->local_stack > 1) return fail(c, RDN_ERR_INVALID_ARG, "local_stack must be 0 or 1");
+  if (d->register_tier > 2) return fail(c, RDN_ERR_INVALID_ARG, "register_tier must be 0, 1 or 2");
   if (d->block_size && (d->block_size % 32 || d->block_size > 128))
     return fail(c, RDN_ERR_INVALID_ARG, "block_size must be a multiple of 32 up to 128");
   std::lock_guard<std::mutex> lk(c->lock);
@@ -997,6 +1000,7 @@ rdn_status rdn_wavefront_shadow_bounce_static(rdn_ctx* c, const rdn_wavefront_de
   w.ray_counts = d->ray_counts;
   w.refill = d->refill;
   w.local_stack = d->local_stack;
+  w.register_tier = d->register_tier;
   cudaError_t e = cudaSetDevice(c->device);
   if (e == cudaSuccess)
     e = rdn::launch_wavefront_static(p, w, mode_of(d->traversal), d->block_size, c->sm_count, d->phases,

@@ -38,9 +38,14 @@ using namespace dev;
 
 // LOCAL: the traversal stack lives in the thread's local memory (L1-cached)
 // instead of shared memory, so that the stack no longer limits occupancy.
+// TIER picks the register budget through the launch bounds: 0 = the
+// compiler's default for 128-thread blocks (64 registers, some spills),
+// 1 = at least 4 blocks of 128 per SM (about 80 registers, no spills, fewer
+// warps), 2 = at least 10 blocks (51 registers, more warps, more spills).
+constexpr int min_blocks(int tier) { return tier == 1 ? 4 : (tier == 2 ? 10 : 0); }
 
-template <int MODE, bool LOCAL>
-__global__ void __launch_bounds__(128) primary_kernel(TraceParams p, WavefrontParams w) {
+template <int MODE, bool LOCAL, int TIER>
+__global__ void __launch_bounds__(128, min_blocks(TIER)) primary_kernel(TraceParams p, WavefrontParams w) {
   extern __shared__ uint2 smem_stack[];
   uint2 local_stack[LOCAL ? kLocalStackEntries : 1];
   uint2* const stack = LOCAL ? local_stack : smem_stack + threadIdx.x;
@@ -118,8 +123,8 @@ __global__ void __launch_bounds__(128) primary_kernel(TraceParams p, WavefrontPa
   }
 }
 
-template <int MODE, bool LOCAL>
-__global__ void __launch_bounds__(128) secondary_kernel(TraceParams p, WavefrontParams w) {
+template <int MODE, bool LOCAL, int TIER>
+__global__ void __launch_bounds__(128, min_blocks(TIER)) secondary_kernel(TraceParams p, WavefrontParams w) {
   extern __shared__ uint2 smem_stack[];
   uint2 local_stack[LOCAL ? kLocalStackEntries : 1];
   uint2* const stack = LOCAL ? local_stack : smem_stack + threadIdx.x;
@@ -271,16 +276,17 @@ void wavefront_bind_scratch(WavefrontParams& w, void* scratch) {
 }
 
 namespace {
-template <int MODE, bool LOCAL>
+template <int MODE, bool LOCAL, int TIER>
 cudaError_t launch_wavefront_mode(const TraceParams& p, const WavefrontParams& w, uint32_t block, int sm_count,
                                   uint32_t phases, cudaStream_t stream) {
   const size_t smem = MODE != MODE_THREADED && !LOCAL ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
   static bool attr_done = false;
   if (!attr_done) {
     cudaError_t e =
-        cudaFuncSetAttribute(primary_kernel<MODE, LOCAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(primary_kernel<MODE, LOCAL, TIER>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(secondary_kernel<MODE, LOCAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+      e = cudaFuncSetAttribute(secondary_kernel<MODE, LOCAL, TIER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               200 * 1024);
     if (e == cudaSuccess && MODE != MODE_THREADED)
       e = cudaFuncSetAttribute(secondary_dynamic_kernel<MODE == MODE_THREADED ? MODE_BINARY : MODE>,
                                cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
@@ -295,7 +301,7 @@ cudaError_t launch_wavefront_mode(const TraceParams& p, const WavefrontParams& w
     const uint32_t tiles = ((w.width + 7) / 8) * ((w.height + 3) / 4);
     const uint32_t threads = tiles * 32;
     const uint32_t grid1 = (threads + block - 1) / block;
-    primary_kernel<MODE, LOCAL><<<grid1, block, smem, stream>>>(p, w);
+    primary_kernel<MODE, LOCAL, TIER><<<grid1, block, smem, stream>>>(p, w);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
@@ -309,12 +315,12 @@ cudaError_t launch_wavefront_mode(const TraceParams& p, const WavefrontParams& w
   if (dynamic)
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, secondary_dynamic_kernel<DMODE>, (int)block, smem);
   else
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, secondary_kernel<MODE, LOCAL>, (int)block, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, secondary_kernel<MODE, LOCAL, TIER>, (int)block, smem);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
   const uint32_t grid2 = (uint32_t)(sm_count * per_sm);
   if (dynamic) secondary_dynamic_kernel<DMODE><<<grid2, block, smem, stream>>>(p, w);
-  else secondary_kernel<MODE, LOCAL><<<grid2, block, smem, stream>>>(p, w);
+  else secondary_kernel<MODE, LOCAL, TIER><<<grid2, block, smem, stream>>>(p, w);
   return cudaGetLastError();
 }
 }  // namespace
@@ -327,13 +333,23 @@ cudaError_t launch_wavefront(const TraceParams& p, const WavefrontParams& w, int
   if (n == 0) return cudaSuccess;
   // the local-memory stack holds kLocalStackEntries entries; deeper trees keep the shared-memory stack
   const bool local = w.local_stack && mode != MODE_THREADED && p.stack_depth <= kLocalStackEntries;
-  if (mode == MODE_WIDE4)
-    return local ? launch_wavefront_mode<MODE_WIDE4, true>(p, w, block, sm_count, phases, stream)
-                 : launch_wavefront_mode<MODE_WIDE4, false>(p, w, block, sm_count, phases, stream);
-  if (mode == MODE_BINARY)
-    return local ? launch_wavefront_mode<MODE_BINARY, true>(p, w, block, sm_count, phases, stream)
-                 : launch_wavefront_mode<MODE_BINARY, false>(p, w, block, sm_count, phases, stream);
-  return launch_wavefront_mode<MODE_THREADED, false>(p, w, block, sm_count, phases, stream);
+  // register tiers apply to the local-stack kernels
+  const uint32_t tier = local ? w.register_tier : 0u;
+#define RDN_WF(M, L, T) return launch_wavefront_mode<M, L, T>(p, w, block, sm_count, phases, stream)
+  if (mode == MODE_WIDE4) {
+    if (!local) RDN_WF(MODE_WIDE4, false, 0);
+    if (tier == 1) RDN_WF(MODE_WIDE4, true, 1);
+    if (tier == 2) RDN_WF(MODE_WIDE4, true, 2);
+    RDN_WF(MODE_WIDE4, true, 0);
+  }
+  if (mode == MODE_BINARY) {
+    if (!local) RDN_WF(MODE_BINARY, false, 0);
+    if (tier == 1) RDN_WF(MODE_BINARY, true, 1);
+    if (tier == 2) RDN_WF(MODE_BINARY, true, 2);
+    RDN_WF(MODE_BINARY, true, 0);
+  }
+  RDN_WF(MODE_THREADED, false, 0);
+#undef RDN_WF
 }
 
 }  // namespace rdn

@@ -40,6 +40,8 @@ struct WavefrontParams {
   // 1: traversal stacks in local memory (ordered walks, trees up to the
   // local stack's depth); 0: in shared memory
   uint32_t local_stack;
+  // register budget of the local-stack kernels: 0 default (64), 1 about 80, 2 51
+  uint32_t register_tier;
 };
 
 size_t wavefront_scratch_bytes(uint32_t width, uint32_t height);

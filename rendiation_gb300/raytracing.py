@@ -263,16 +263,17 @@ class Wavefront:
         self.phase_config = None  # (primary, secondary) (traversal, block) when they differ
 
     def configure(self, primary, secondary, refill=None):
-        """Per-kernel (traversal, block_size[, local_stack]); a frame then issues
-        one call per kernel. refill: secondary schedule (0 = batches of 32 rays
+        """Per-kernel (traversal, block_size[, local_stack[, register_tier]]); a
+        frame then issues one call per kernel. refill: secondary schedule (0 = batches of 32 rays
         per warp, k = dynamic fetch whenever k lanes of a warp are idle); None
         keeps the current one."""
         if refill is not None:
             self.desc.refill = refill
-        primary = tuple(primary) + (0,) * (3 - len(primary))
-        secondary = tuple(secondary) + (0,) * (3 - len(secondary))
+        primary = tuple(primary) + (0,) * (4 - len(primary))
+        secondary = tuple(secondary) + (0,) * (4 - len(secondary))
         if primary == secondary:
-            self.desc.traversal, self.desc.block_size, self.desc.local_stack = primary
+            (self.desc.traversal, self.desc.block_size, self.desc.local_stack,
+             self.desc.register_tier) = primary
             self.phase_config = None
         else:
             self.phase_config = (primary, secondary)
@@ -288,11 +289,12 @@ class Wavefront:
             _check(self.system._h, self.system._L.rdn_wavefront_shadow_bounce(self.system._h, C.byref(self.desc),
                                                                               C.c_void_p(s)))
             return
-        for ph, (trav, block, local) in zip((1, 2), self.phase_config):
+        for ph, (trav, block, local, tier) in zip((1, 2), self.phase_config):
             if phases and phases != ph:
                 continue
             self.desc.phases = ph
-            self.desc.traversal, self.desc.block_size, self.desc.local_stack = trav, block, local
+            (self.desc.traversal, self.desc.block_size, self.desc.local_stack,
+             self.desc.register_tier) = trav, block, local, tier
             _check(self.system._h, self.system._L.rdn_wavefront_shadow_bounce(self.system._h, C.byref(self.desc),
                                                                               C.c_void_p(s)))
 

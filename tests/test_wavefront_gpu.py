@@ -96,13 +96,17 @@ def test_wavefront_local_memory_stack(traversal, cuda):
     sc = single_mesh_scene(mesh)
     P = sc.build_product()
     a = rt.Wavefront(P, cam, LIGHT, traversal=traversal)
-    b = rt.Wavefront(P, cam, LIGHT, traversal=traversal)
-    b.desc.local_stack = 1
     a.run(2)
-    b.run(2)
     torch.cuda.synchronize()
-    ra, rb = a.results(), b.results()
-    assert a.rays_traced() == b.rays_traced()
-    same = ra["primary_prim"] == rb["primary_prim"]
-    assert same.mean() > 0.999 and np.array_equal(ra["primary_t"].view(np.uint32), rb["primary_t"].view(np.uint32))
-    assert np.array_equal(ra["light"][same], rb["light"][same])
+    ra = a.results()
+    for tier in (0, 1, 2):  # register budgets of the local-stack kernels
+        b = rt.Wavefront(P, cam, LIGHT, traversal=traversal)
+        b.desc.local_stack, b.desc.register_tier = 1, tier
+        b.run(2)
+        torch.cuda.synchronize()
+        rb = b.results()
+        assert a.rays_traced() == b.rays_traced()
+        same = ra["primary_prim"] == rb["primary_prim"]
+        assert same.mean() > 0.999
+        assert np.array_equal(ra["primary_t"].view(np.uint32), rb["primary_t"].view(np.uint32))
+        assert np.array_equal(ra["light"][same], rb["light"][same])
