@@ -223,7 +223,7 @@ def bench_wavefront(args, ws, rank):
             def run(c):
                 wf.desc.traversal, wf.desc.block_size = c["traversal"], c["block"]
                 wf.desc.refill, wf.desc.local_stack = c.get("refill", 0), c.get("local", 0)
-                wf.desc.register_tier = c.get("regs", 0)
+                wf.desc.register_tier, wf.desc.speculation = c.get("regs", 0), c.get("spec", 0)
                 wf.run(7, phases=ph)
             return run
 
@@ -231,10 +231,17 @@ def bench_wavefront(args, ws, rank):
         torch.cuda.synchronize()
         t1 = tuner.tune("wavefront-primary", cands, run_phase(1))
         t2 = tuner.tune("wavefront-secondary", cands2, run_phase(2))
-        wf.configure((t1.best["traversal"], t1.best["block"], t1.best.get("local", 0), t1.best.get("regs", 0)),
-                     (t2.best["traversal"], t2.best["block"], t2.best.get("local", 0), t2.best.get("regs", 0)),
-                     refill=t2.best.get("refill", 0))
-        tuned = {"primary": t1.best, "secondary": t2.best}
+        # second stage: leaf-postponement threshold of the speculative walk
+        b1, b2 = dict(t1.best), dict(t2.best)
+        s1 = tuner.tune("wavefront-primary-speculation", [dict(b1, spec=k) for k in (0, 2, 4, 8, 16)],
+                        run_phase(1))
+        s2 = tuner.tune("wavefront-secondary-speculation", [dict(b2, spec=k) for k in (0, 2, 4, 8, 16)],
+                        run_phase(2))
+        b1, b2 = s1.best, s2.best
+        wf.configure((b1["traversal"], b1["block"], b1.get("local", 0), b1.get("regs", 0), b1.get("spec", 0)),
+                     (b2["traversal"], b2["block"], b2.get("local", 0), b2.get("regs", 0), b2.get("spec", 0)),
+                     refill=b2.get("refill", 0))
+        tuned = {"primary": b1, "secondary": b2}
 
     # one frame to learn the ray counts, then the reference-order visit counts of those rays
     wf.run(0)
@@ -298,7 +305,8 @@ def bench_wavefront(args, ws, rank):
     if wf.phase_config is not None:
         wf2.configure(*wf.phase_config, refill=wf.desc.refill)
     else:
-        same = (wf.desc.traversal, wf.desc.block_size, wf.desc.local_stack, wf.desc.register_tier)
+        same = (wf.desc.traversal, wf.desc.block_size, wf.desc.local_stack, wf.desc.register_tier,
+                wf.desc.speculation)
         wf2.configure(same, same, refill=wf.desc.refill)
     frames = (wf, wf2)
     host_out = [torch.empty(wf.out.shape, dtype=wf.out.dtype, pin_memory=True) for _ in range(2)]
@@ -456,8 +464,17 @@ def bench_batched(args):
             batched.run()
 
         res = Autotuner().tune("batched-paths", cands, run, reps=2)
-        batched.configure(res.best["traversal"], res.best["block"], res.best["sort_key"], res.best["refill"],
-                          res.best["local"])
+        best = dict(res.best)
+
+        def run_spec(c):
+            batched.configure(speculation=c["spec"])
+            batched.run()
+
+        batched.configure(best["traversal"], best["block"], best["sort_key"], best["refill"], best["local"])
+        res2 = Autotuner().tune("batched-paths-speculation", [dict(best, spec=k) for k in (0, 2, 4, 8)], run_spec,
+                                reps=2)
+        batched.configure(speculation=res2.best["spec"])
+        res.best, res.timings_ms = res2.best, res.timings_ms + res2.timings_ms
         tuned = {"best": res.best, "timings_ms": res.timings_ms}
     batched.capture()
     for _ in range(args.warmup):

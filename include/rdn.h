@@ -302,6 +302,8 @@ typedef struct rdn_wavefront_desc {
                                 instead of shared memory, for trees whose stack fits 64 entries */
   uint32_t register_tier;    /* local-stack kernels: 0 = 64 registers per thread, 1 = about 80 (no
                                 spills, fewer resident warps), 2 = 51 (more warps, more spills) */
+  uint32_t speculation;      /* ordered walks: a lane holding a leaf keeps descending while more than
+                                this many lanes of its warp still look for one (0 = until all have one) */
 } rdn_wavefront_desc;
 
 /* Scratch size for the secondary-ray queues of a width x height launch. */
@@ -355,6 +357,7 @@ typedef struct rdn_path_desc {
                                    together; k in 1..32 = each lane keeps its own query and a warp takes
                                    new rays whenever k lanes are idle (dynamic fetch) */
   uint32_t local_stack;         /* ordered walks, batch schedule: 1 = traversal stacks in local memory */
+  uint32_t speculation;         /* ordered walks: leaf postponement threshold, as in rdn_wavefront_desc */
 } rdn_path_desc;
 
 /* Ray-sort keys (stable radix sort of each queue before its bounce). */

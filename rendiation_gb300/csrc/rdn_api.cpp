@@ -503,6 +503,7 @@ rdn_status rdn_wavefront_shadow_bounce(rdn_ctx* c, const rdn_wavefront_desc* d, 
   if (d->refill > 32) return fail(c, RDN_ERR_INVALID_ARG, "refill must be 0..32");
   if (d->local_stack > 1) return fail(c, RDN_ERR_INVALID_ARG, "local_stack must be 0 or 1");
   if (d->register_tier > 2) return fail(c, RDN_ERR_INVALID_ARG, "register_tier must be 0, 1 or 2");
+  if (d->speculation > 31) return fail(c, RDN_ERR_INVALID_ARG, "speculation must be 0..31");
   if (d->block_size && (d->block_size % 32 || d->block_size > 128))
     return fail(c, RDN_ERR_INVALID_ARG, "block_size must be a multiple of 32 up to 128");
   std::lock_guard<std::mutex> lk(c->lock);
@@ -534,6 +535,7 @@ rdn_status rdn_wavefront_shadow_bounce(rdn_ctx* c, const rdn_wavefront_desc* d, 
   w.refill = d->refill;
   w.local_stack = d->local_stack;
   w.register_tier = d->register_tier;
+  p.spec_threshold = d->speculation;
   rdn::wavefront_bind_scratch(w, d->scratch);
   cudaError_t e = cudaSetDevice(c->device);
   if (e == cudaSuccess)
@@ -561,6 +563,7 @@ rdn_status prepare_path_launch(rdn_ctx* c, const rdn_path_desc* d, rdn::TracePar
   if (d->count && (!d->rays || !d->out || !d->scratch)) return fail(c, RDN_ERR_INVALID_ARG, "null buffer");
   if (d->sort_key > 2) return fail(c, RDN_ERR_INVALID_ARG, "unknown sort key");
   if (d->refill > 32) return fail(c, RDN_ERR_INVALID_ARG, "refill must be 0..32");
+  if (d->speculation > 31) return fail(c, RDN_ERR_INVALID_ARG, "speculation must be 0..31");
   if (d->scratch_bytes < rdn::paths_scratch_bytes(d->count, d->max_bounces, d->sort_key))
     return fail(c, RDN_ERR_INVALID_ARG, "scratch too small");
   if ((reinterpret_cast<uintptr_t>(d->scratch) & 255) || (reinterpret_cast<uintptr_t>(d->rays) & 15) ||
@@ -593,6 +596,7 @@ rdn_status prepare_path_launch(rdn_ctx* c, const rdn_path_desc* d, rdn::TracePar
   q.segment_counts = d->segment_counts;
   q.sort_key = d->sort_key;
   q.refill = d->refill;
+  p.spec_threshold = d->speculation;
   if (d->sort_key) {
     uint32_t bits = 0;
     while (bits < 32 && (1ull << bits) < (uint64_t)std::max<size_t>(1, c->dev.tlas_binding.count)) bits++;
@@ -970,6 +974,7 @@ rdn_status rdn_wavefront_shadow_bounce_static(rdn_ctx* c, const rdn_wavefront_de
   if (d->refill > 32) return fail(c, RDN_ERR_INVALID_ARG, "refill must be 0..32");
   if (d->local_stack > 1) return fail(c, RDN_ERR_INVALID_ARG, "local_stack must be 0 or 1");
   if (d->register_tier > 2) return fail(c, RDN_ERR_INVALID_ARG, "register_tier must be 0, 1 or 2");
+  if (d->speculation > 31) return fail(c, RDN_ERR_INVALID_ARG, "speculation must be 0..31");
   if (d->block_size && (d->block_size % 32 || d->block_size > 128))
     return fail(c, RDN_ERR_INVALID_ARG, "block_size must be a multiple of 32 up to 128");
   std::lock_guard<std::mutex> lk(c->lock);
@@ -1001,6 +1006,7 @@ rdn_status rdn_wavefront_shadow_bounce_static(rdn_ctx* c, const rdn_wavefront_de
   w.refill = d->refill;
   w.local_stack = d->local_stack;
   w.register_tier = d->register_tier;
+  p.spec_threshold = d->speculation;
   cudaError_t e = cudaSetDevice(c->device);
   if (e == cudaSuccess)
     e = rdn::launch_wavefront_static(p, w, mode_of(d->traversal), d->block_size, c->sm_count, d->phases,

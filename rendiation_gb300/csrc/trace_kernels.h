@@ -35,6 +35,10 @@ struct TraceParams {
   // 1: per-thread traversal stacks in local memory (ordered walks whose stack
   // fits kLocalStackEntries), 0: in shared memory
   uint32_t local_stack;
+  // speculative ordered walk: lanes holding a leaf keep descending while more
+  // than this many lanes of the warp are still looking for one (0 = until all
+  // have one)
+  uint32_t spec_threshold;
 };
 
 // entries of a local-memory traversal stack

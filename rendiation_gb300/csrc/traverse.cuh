@@ -370,7 +370,8 @@ __device__ __forceinline__ bool blas_speculative(const TraceParams& p, RayCtx& R
         leaf = code;
         code = pop_live(stack, stride, sp, R.far_world * ir.scaling, code_tn);
       }
-      if (!__any_sync(__activemask(), leaf == EMPTY_SLOT)) break;
+      // keep descending while more than spec_threshold lanes still look for a leaf
+      if ((uint32_t)__popc(__ballot_sync(__activemask(), leaf == EMPTY_SLOT)) <= p.spec_threshold) break;
     }
     while (leaf != EMPTY_SLOT) {
       const uint2 lr = __ldg(p.leaves + (leaf & ~LEAF_BIT));
@@ -604,7 +605,7 @@ struct LaneWalk {
           leaf = code;
           code = pop_live(stack, stride, sp, R.far_world * ir.scaling, code_tn);
         }
-        if (!__any_sync(__activemask(), leaf == EMPTY_SLOT)) break;
+        if ((uint32_t)__popc(__ballot_sync(__activemask(), leaf == EMPTY_SLOT)) <= p.spec_threshold) break;
       }
       while (leaf != EMPTY_SLOT) {
         const uint2 lr = __ldg(p.leaves + (leaf & ~LEAF_BIT));

@@ -84,7 +84,7 @@ class WavefrontDesc(C.Structure):
                 ("tlas_uniform", C.c_uint32), ("traversal", C.c_uint32), ("block_size", C.c_uint32),
                 ("out", C.c_void_p), ("scratch", C.c_void_p), ("scratch_bytes", C.c_size_t),
                 ("ray_counts", C.c_void_p), ("phases", C.c_uint32), ("refill", C.c_uint32),
-                ("local_stack", C.c_uint32), ("register_tier", C.c_uint32)]
+                ("local_stack", C.c_uint32), ("register_tier", C.c_uint32), ("speculation", C.c_uint32)]
 
 
 class PathDesc(C.Structure):
@@ -93,7 +93,7 @@ class PathDesc(C.Structure):
                 ("rr_survive", C.c_float), ("seed", C.c_uint32), ("traversal", C.c_uint32),
                 ("block_size", C.c_uint32), ("sort_key", C.c_uint32), ("out", C.c_void_p), ("scratch", C.c_void_p),
                 ("scratch_bytes", C.c_size_t), ("segment_counts", C.c_void_p), ("refill", C.c_uint32),
-                ("local_stack", C.c_uint32)]
+                ("local_stack", C.c_uint32), ("speculation", C.c_uint32)]
 
 
 class AttrLossDesc(C.Structure):

@@ -263,17 +263,17 @@ class Wavefront:
         self.phase_config = None  # (primary, secondary) (traversal, block) when they differ
 
     def configure(self, primary, secondary, refill=None):
-        """Per-kernel (traversal, block_size[, local_stack[, register_tier]]); a
-        frame then issues one call per kernel. refill: secondary schedule (0 = batches of 32 rays
+        """Per-kernel (traversal, block_size[, local_stack[, register_tier[,
+        speculation]]]); a frame then issues one call per kernel. refill: secondary schedule (0 = batches of 32 rays
         per warp, k = dynamic fetch whenever k lanes of a warp are idle); None
         keeps the current one."""
         if refill is not None:
             self.desc.refill = refill
-        primary = tuple(primary) + (0,) * (4 - len(primary))
-        secondary = tuple(secondary) + (0,) * (4 - len(secondary))
+        primary = tuple(primary) + (0,) * (5 - len(primary))
+        secondary = tuple(secondary) + (0,) * (5 - len(secondary))
         if primary == secondary:
-            (self.desc.traversal, self.desc.block_size, self.desc.local_stack,
-             self.desc.register_tier) = primary
+            (self.desc.traversal, self.desc.block_size, self.desc.local_stack, self.desc.register_tier,
+             self.desc.speculation) = primary
             self.phase_config = None
         else:
             self.phase_config = (primary, secondary)
@@ -289,12 +289,12 @@ class Wavefront:
             _check(self.system._h, self.system._L.rdn_wavefront_shadow_bounce(self.system._h, C.byref(self.desc),
                                                                               C.c_void_p(s)))
             return
-        for ph, (trav, block, local, tier) in zip((1, 2), self.phase_config):
+        for ph, (trav, block, local, tier, spec) in zip((1, 2), self.phase_config):
             if phases and phases != ph:
                 continue
             self.desc.phases = ph
-            (self.desc.traversal, self.desc.block_size, self.desc.local_stack,
-             self.desc.register_tier) = trav, block, local, tier
+            (self.desc.traversal, self.desc.block_size, self.desc.local_stack, self.desc.register_tier,
+             self.desc.speculation) = trav, block, local, tier, spec
             _check(self.system._h, self.system._L.rdn_wavefront_shadow_bounce(self.system._h, C.byref(self.desc),
                                                                               C.c_void_p(s)))
 
@@ -339,7 +339,8 @@ class Paths:
         self.graph = None
         self.scratch_bytes = size.value
 
-    def configure(self, traversal=None, block_size=None, sort_key=None, refill=None, local_stack=None):
+    def configure(self, traversal=None, block_size=None, sort_key=None, refill=None, local_stack=None,
+                  speculation=None):
         """Changes launch knobs (re-capture any graph afterwards). refill: 0 =
         warps trace 32 queued rays together, k = dynamic fetch whenever k lanes
         of a warp are idle."""
@@ -363,6 +364,8 @@ class Paths:
             self.desc.refill = refill
         if local_stack is not None:
             self.desc.local_stack = local_stack
+        if speculation is not None:
+            self.desc.speculation = speculation
         self.close()
 
     def run(self, stream=None):

@@ -21,9 +21,12 @@ def product_paths(P, b, traversal, graph=False, **kw):
     rays = torch.from_numpy(b.rays.view(np.float32).reshape(-1, 8).copy()).cuda()
     tidx = torch.from_numpy(b.tlas_idx.astype(np.int32)).cuda()
     local = kw.pop("local", False)
+    speculation = kw.pop("speculation", None)
     paths = rt.Paths(P, rays, tidx, traversal=traversal, **kw)
     if local:
         paths.configure(local_stack=1)
+    if speculation is not None:
+        paths.configure(speculation=speculation)
     if graph:
         paths.capture()
         paths.launch_graph()
@@ -59,7 +62,7 @@ def test_paths_graph_replays_identically(batched, cuda):
     assert np.array_equal(got["radiance"].view(np.uint32), exp["radiance"].view(np.uint32))
 
 
-@pytest.mark.parametrize("refill,local", [(0, 0), (0, 1), (1, 0), (8, 0)])
+@pytest.mark.parametrize("refill,local", [(0, 0), (0, 1), (1, 0), (8, 0), (0, 4)])
 @pytest.mark.parametrize("traversal", [rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_WIDE])
 def test_paths_ordered_matches_except_ties(batched, traversal, refill, local, cuda):
     """refill > 0: the dynamic-fetch schedule (also replayed from a graph);
@@ -67,8 +70,10 @@ def test_paths_ordered_matches_except_ties(batched, traversal, refill, local, cu
     b, S, P = batched
     exp, seg, _ = orc.trace_paths(S, b.rays, b.tlas_idx, max_bounces=4, rr_start=2, seed=5, threads=4)
     got, gseg, first = product_paths(P, b, traversal, graph=refill == 8, seed=5, refill=refill)
-    if local:
+    if local == 1:
         got, gseg, first = product_paths(P, b, traversal, graph=True, seed=5, local=True)
+    elif local:  # the leaf-postponement threshold instead
+        got, gseg, first = product_paths(P, b, traversal, seed=5, speculation=local)
     if first is not None:
         assert (first["depth_flags"] == got["depth_flags"]).mean() > 0.999
     # a path diverges from the oracle only after an exact-distance tie picks another triangle

@@ -99,9 +99,9 @@ def test_wavefront_local_memory_stack(traversal, cuda):
     a.run(2)
     torch.cuda.synchronize()
     ra = a.results()
-    for tier in (0, 1, 2):  # register budgets of the local-stack kernels
+    for tier, spec in ((0, 0), (1, 4), (2, 16)):  # register budgets; leaf-postponement thresholds
         b = rt.Wavefront(P, cam, LIGHT, traversal=traversal)
-        b.desc.local_stack, b.desc.register_tier = 1, tier
+        b.desc.local_stack, b.desc.register_tier, b.desc.speculation = 1, tier, spec
         b.run(2)
         torch.cuda.synchronize()
         rb = b.results()
