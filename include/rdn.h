@@ -169,6 +169,8 @@ typedef struct rdn_hit_ext {
 #define RDN_ANYHIT_ACCEPT 0u
 #define RDN_ANYHIT_ACCEPT_AND_END 1u
 #define RDN_ANYHIT_ACCEPT_EVEN_PRIMS 2u
+#define RDN_ANYHIT_PRIMITIVE_MASK 3u   /* accept a non-opaque hit when bit t of anyhit_mask is set, t the
+                                          built triangle index (creation order); a data-driven alpha test */
 
 typedef struct rdn_trace_desc {
   const rdn_ray* rays;      /* device, count entries */
@@ -184,6 +186,7 @@ typedef struct rdn_trace_desc {
   uint32_t block_size;      /* 0 = 64 */
   uint32_t local_stack;      /* ordered walks: 1 = per-thread traversal stacks in local memory (L1)
                                 instead of shared memory, for trees whose stack fits 64 entries */
+  const uint32_t* anyhit_mask; /* device, RDN_ANYHIT_PRIMITIVE_MASK: one bit per built triangle */
 } rdn_trace_desc;
 
 /* Counters of node visits and triangle tests, the reference's

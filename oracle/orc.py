@@ -64,7 +64,7 @@ def lib():
         L.orc_build_stats.argtypes = [vp, vp]
         L.orc_get_buffer.restype = C.c_size_t
         L.orc_get_buffer.argtypes = [vp, i32, vp, C.c_size_t]
-        L.orc_trace.argtypes = [vp, vp, u32, vp, u32, u32, u32, u32, vp, vp, vp, i32, C.POINTER(C.c_double)]
+        L.orc_trace.argtypes = [vp, vp, u32, vp, u32, u32, u32, u32, vp, vp, vp, vp, i32, C.POINTER(C.c_double)]
         L.orc_eval_fp64.argtypes = [vp, vp, u32, vp, vp]
         L.orc_bruteforce_fp64.argtypes = [vp, vp, u32, u32, vp, i32]
         L.orc_intersect_triangle.argtypes = [vp, vp, C.c_float, C.c_float, vp, vp, vp, i32, i32, vp]
@@ -161,7 +161,8 @@ class OracleSystem:
         return b.tobytes()
 
     def trace(self, rays: np.ndarray, tlas_idx=None, tlas_uniform=0, ray_flags=0, cull_mask=0xFF, anyhit_mode=0,
-              threads=1, counts=False):
+              threads=1, counts=False, anyhit_mask=None):
+        """anyhit_mask: uint32 bit array over built triangles (anyhit_mode 3)."""
         rays = np.ascontiguousarray(rays)
         n = rays.shape[0]
         out = np.zeros(n, HIT_DTYPE)
@@ -169,8 +170,10 @@ class OracleSystem:
         tot = np.zeros(6, np.uint64)
         ti = None if tlas_idx is None else np.ascontiguousarray(tlas_idx, np.uint32)
         sec = C.c_double()
+        mask = None if anyhit_mask is None else np.ascontiguousarray(anyhit_mask, np.uint32)
         self._check(self._L.orc_trace(self._h, _ptr(rays), n, _ptr(ti), tlas_uniform, ray_flags, cull_mask,
-                                      anyhit_mode, _ptr(out), _ptr(rc), _ptr(tot), threads, C.byref(sec)))
+                                      anyhit_mode, _ptr(mask), _ptr(out), _ptr(rc), _ptr(tot), threads,
+                                      C.byref(sec)))
         totals = dict(zip(["tri_visit", "tri_hit", "bvh_visit", "bvh_hit", "far_assert", "bad_tlas"],
                           (int(x) for x in tot)))
         totals["seconds"] = sec.value

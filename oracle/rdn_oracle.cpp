@@ -606,18 +606,20 @@ struct BvhIter {
   }
 };
 
-// anyhit_mode: the fixed any-hit policies offered at the C ABI in place of a
-// user EDSL any-hit shader. 0 = accept; 1 = accept and end search;
-// 2 = accept only even primitive ids (an alpha-test stand-in).
-static inline uint32_t any_hit_policy(uint32_t mode, uint32_t primitive_idx) {
+// anyhit_mode: the any-hit policies offered at the C ABI in place of a user
+// EDSL any-hit shader. 0 = accept; 1 = accept and end search; 2 = accept only
+// even primitive ids; 3 = accept when bit `tri_idx` (the built triangle index)
+// of `mask` is set (a data-driven alpha test).
+static inline uint32_t any_hit_policy(uint32_t mode, uint32_t primitive_idx, uint32_t tri_idx, const uint32_t* mask) {
   if (mode == 1) return ANYHIT_ACCEPT | ANYHIT_END_SEARCH;
   if (mode == 2) return (primitive_idx & 1u) ? 0u : ANYHIT_ACCEPT;
+  if (mode == 3) return (mask[tri_idx >> 5] >> (tri_idx & 31u)) & 1u ? ANYHIT_ACCEPT : 0u;
   return ANYHIT_ACCEPT;
 }
 
 static void traverse(const Built& B, const RayIn& ray, uint32_t tlas_idx, uint32_t ray_flags, uint32_t cull_mask,
                      uint32_t anyhit_mode, HitOut& out, Counters& cn, uint32_t* ray_counts,
-                     uint32_t* tri_out = nullptr) {
+                     uint32_t* tri_out = nullptr, const uint32_t* anyhit_mask = nullptr) {
   out = HitOut{ray.tmax, 0.0f, 0.0f, INVALID_NEXT, INVALID_NEXT, INVALID_NEXT, INVALID_NEXT, 0};
   uint32_t node_visits = 0, tri_tests = 0;
   bool have = false;
@@ -677,7 +679,8 @@ static void traverse(const Built& B, const RayIn& ray, uint32_t tlas_idx, uint32
                 float distance = r.t / distance_scaling;
                 uint32_t primitive_idx = tri_idx - g.primitive_start;
                 cn.tri_hit++;
-                uint32_t behavior = is_opaque ? ANYHIT_ACCEPT : any_hit_policy(anyhit_mode, primitive_idx);
+                uint32_t behavior =
+                    is_opaque ? ANYHIT_ACCEPT : any_hit_policy(anyhit_mode, primitive_idx, tri_idx, anyhit_mask);
                 if (behavior & ANYHIT_ACCEPT) {
                   // RayRange::update_far asserts near <= far <= current far (traverse_cpu.rs:272-276);
                   // the reference aborts when they fail, the oracle counts it and goes on.
@@ -1044,8 +1047,9 @@ size_t orc_get_buffer(void* cp, int which, void* dst, size_t cap) {
 // bvh_visit, bvh_hit, far_assert, bad_tlas. Returns elapsed seconds of the
 // traversal loop in *seconds (nullable).
 int orc_trace(void* cp, const RayIn* rays, uint32_t n, const uint32_t* tlas_idx, uint32_t tlas_uniform,
-              uint32_t ray_flags, uint32_t cull_mask, uint32_t anyhit_mode, HitOut* out, uint32_t* ray_counts,
-              uint64_t* totals, int threads, double* seconds) {
+              uint32_t ray_flags, uint32_t cull_mask, uint32_t anyhit_mode, const uint32_t* anyhit_mask, HitOut* out,
+              uint32_t* ray_counts, uint64_t* totals, int threads, double* seconds) {
+  if (anyhit_mode == 3 && !anyhit_mask) return -1;
   Ctx& c = *(Ctx*)cp;
   if (!c.built) {
     int rc = build_all(c);
@@ -1059,7 +1063,7 @@ int orc_trace(void* cp, const RayIn* rays, uint32_t n, const uint32_t* tlas_idx,
     uint32_t s = (uint32_t)((uint64_t)n * w / threads), e = (uint32_t)((uint64_t)n * (w + 1) / threads);
     for (uint32_t i = s; i < e; i++)
       traverse(B, rays[i], tlas_idx ? tlas_idx[i] : tlas_uniform, ray_flags, cull_mask, anyhit_mode, out[i], cn[w],
-               ray_counts ? ray_counts + 2 * (size_t)i : nullptr);
+               ray_counts ? ray_counts + 2 * (size_t)i : nullptr, nullptr, anyhit_mask);
   };
   if (threads == 1) {
     work(0);

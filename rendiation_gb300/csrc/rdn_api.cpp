@@ -170,6 +170,7 @@ rdn_status fill_params(rdn_ctx* c, const rdn_trace_desc* desc, rdn::TraceParams&
   p.ray_flags = desc->ray_flags;
   p.cull_mask = desc->cull_mask;
   p.anyhit_mode = desc->anyhit_mode;
+  p.anyhit_mask = desc->anyhit_mask;
   p.stack_depth = rdn::stack_entries(mode_of(desc->traversal), d.max_blas_depth, d.max_wide4_depth);
   p.n_binding = (uint32_t)d.tlas_binding.count;
   p.n_tlas_root = (uint32_t)d.tlas_bvh_root.count;
@@ -203,7 +204,9 @@ rdn_status validate_trace(rdn_ctx* c, const rdn_trace_desc* desc) {
       (reinterpret_cast<uintptr_t>(desc->hits_ext) & 15))
     return fail(c, RDN_ERR_INVALID_ARG, "ray and hit buffers must be 16-byte aligned");
   if (desc->traversal > RDN_TRAVERSAL_ORDERED_WIDE) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
-  if (desc->anyhit_mode > RDN_ANYHIT_ACCEPT_EVEN_PRIMS) return fail(c, RDN_ERR_INVALID_ARG, "unknown any-hit mode");
+  if (desc->anyhit_mode > RDN_ANYHIT_PRIMITIVE_MASK) return fail(c, RDN_ERR_INVALID_ARG, "unknown any-hit mode");
+  if (desc->anyhit_mode == RDN_ANYHIT_PRIMITIVE_MASK && !desc->anyhit_mask)
+    return fail(c, RDN_ERR_INVALID_ARG, "RDN_ANYHIT_PRIMITIVE_MASK needs anyhit_mask");
   if (desc->block_size && (desc->block_size % 32 || desc->block_size > 256))
     return fail(c, RDN_ERR_INVALID_ARG, "block_size must be a multiple of 32 up to 256");
   if (desc->local_stack > 1) return fail(c, RDN_ERR_INVALID_ARG, "local_stack must be 0 or 1");

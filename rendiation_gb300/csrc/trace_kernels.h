@@ -39,6 +39,7 @@ struct TraceParams {
   // than this many lanes of the warp are still looking for one (0 = until all
   // have one)
   uint32_t spec_threshold;
+  const uint32_t* anyhit_mask;  // RDN_ANYHIT_PRIMITIVE_MASK: one bit per built triangle
 };
 
 // entries of a local-memory traversal stack

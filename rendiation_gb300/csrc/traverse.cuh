@@ -161,9 +161,14 @@ __device__ __forceinline__ void geometry_cull(uint32_t f, uint32_t gf, bool& pas
   cull_back = (flip && cb) || (!flip && cf);
 }
 
-__device__ __forceinline__ uint32_t anyhit_policy(uint32_t mode, uint32_t primitive_idx) {
+// Policies in place of a user any-hit shader: 0 accept, 1 accept and end the
+// search, 2 accept even primitive ids, 3 accept when bit `tri` (built
+// triangle index) of the mask is set.
+__device__ __forceinline__ uint32_t anyhit_policy(uint32_t mode, uint32_t primitive_idx, uint32_t tri,
+                                                  const uint32_t* __restrict__ mask) {
   if (mode == 1) return ANYHIT_ACCEPT | ANYHIT_END;
   if (mode == 2) return (primitive_idx & 1u) ? 0u : ANYHIT_ACCEPT;
+  if (mode == 3) return (__ldg(mask + (tri >> 5)) >> (tri & 31u)) & 1u ? ANYHIT_ACCEPT : 0u;
   return ANYHIT_ACCEPT;
 }
 
@@ -191,7 +196,10 @@ __device__ __forceinline__ bool leaf_triangles(const TraceParams& p, RayCtx& R, 
     if (COUNT) R.tri_hits++;
     const float distance = h.t / ir.scaling;
     uint32_t behavior = ANYHIT_ACCEPT;
-    if (!is_opaque) behavior = anyhit_policy(p.anyhit_mode, __ldg(p.redirect + k) - prim_start);
+    if (!is_opaque) {
+      const uint32_t tri = __ldg(p.redirect + k);
+      behavior = anyhit_policy(p.anyhit_mode, tri - prim_start, tri, p.anyhit_mask);
+    }
     if (behavior & ANYHIT_ACCEPT) {
       R.far_world = distance;
       R.best.t = distance;

@@ -65,7 +65,7 @@ class TraceDesc(C.Structure):
     _fields_ = [("rays", C.c_void_p), ("hits", C.c_void_p), ("hits_ext", C.c_void_p), ("tlas_idx", C.c_void_p),
                 ("count", C.c_uint32), ("tlas_uniform", C.c_uint32), ("ray_flags", C.c_uint32),
                 ("cull_mask", C.c_uint32), ("traversal", C.c_uint32), ("anyhit_mode", C.c_uint32),
-                ("block_size", C.c_uint32), ("local_stack", C.c_uint32)]
+                ("block_size", C.c_uint32), ("local_stack", C.c_uint32), ("anyhit_mask", C.c_void_p)]
 
 
 class Counters(C.Structure):

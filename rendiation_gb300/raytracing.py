@@ -46,6 +46,7 @@ SORT_SCENE_OCTANT_CELL = 2
 ANYHIT_ACCEPT = 0
 ANYHIT_ACCEPT_AND_END = 1
 ANYHIT_ACCEPT_EVEN_PRIMS = 2
+ANYHIT_PRIMITIVE_MASK = 3
 
 # built-array ids of rdn_get_built_array
 BUILT_ARRAYS = ["tlas_binding", "tlas_bvh_root", "tlas_bvh_forest", "tlas_data", "tlas_bounding",
@@ -176,23 +177,25 @@ class AccelerationStructureSystem:
 
     # --- queries ---
     def _desc(self, rays, hits, hits_ext, tlas_idx, ray_flags, cull_mask, tlas_uniform, traversal, anyhit_mode,
-              block_size, count=None, local_stack=0):
+              block_size, count=None, local_stack=0, anyhit_mask=None):
         n = rays.shape[0] if count is None else count
         return native.TraceDesc(rays.data_ptr(), hits.data_ptr(), 0 if hits_ext is None else hits_ext.data_ptr(),
                                 0 if tlas_idx is None else tlas_idx.data_ptr(), n, tlas_uniform, ray_flags,
-                                cull_mask, traversal, anyhit_mode, block_size, local_stack)
+                                cull_mask, traversal, anyhit_mode, block_size, local_stack,
+                                None if anyhit_mask is None else anyhit_mask.data_ptr())
 
     def trace(self, rays, hits, hits_ext=None, tlas_idx=None, ray_flags=0, cull_mask=0xFF, tlas_uniform=0,
               traversal=TRAVERSAL_ORDERED, anyhit_mode=ANYHIT_ACCEPT, block_size=0, stream=None, count=None,
-              local_stack=0):
+              local_stack=0, anyhit_mask=None):
         """rays: CUDA f32 tensor (N, 8); hits: CUDA f32 tensor (N, 4) (prim id stored as u32 bits);
         hits_ext: optional CUDA int32 tensor (N, 4); tlas_idx: optional CUDA int32 tensor (N,).
         count overrides N (e.g. 0 for an empty batch). local_stack: traversal stacks in
-        local memory instead of shared memory (ordered walks)."""
+        local memory instead of shared memory (ordered walks). anyhit_mask: CUDA int32
+        bit array over built triangles (ANYHIT_PRIMITIVE_MASK)."""
         import torch
 
         d = self._desc(rays, hits, hits_ext, tlas_idx, ray_flags, cull_mask, tlas_uniform, traversal, anyhit_mode,
-                       block_size, count, local_stack)
+                       block_size, count, local_stack, anyhit_mask)
         s = (stream or torch.cuda.current_stream()).cuda_stream
         _check(self._h, self._L.rdn_trace(self._h, C.byref(d), C.c_void_p(s)))
 

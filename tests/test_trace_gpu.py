@@ -231,3 +231,34 @@ def test_local_memory_stack_same_hits(soup, traversal, cuda):
     got, ext = run_product(P, rays, traversal, local_stack=1)
     c = classify(got, expect)
     assert c["other"] == 0 and c["hit_mismatch"] == 0, c
+
+
+@pytest.mark.parametrize("flags", [0, rt.RAY_FLAG_FORCE_NON_OPAQUE,
+                                   rt.RAY_FLAG_FORCE_NON_OPAQUE | rt.RAY_FLAG_ACCEPT_FIRST_HIT_AND_END_SEARCH])
+@pytest.mark.parametrize("traversal", [rt.TRAVERSAL_REFERENCE] + ORDERED_MODES)
+def test_anyhit_primitive_mask(inst_scene, flags, traversal, cuda):
+    """Data-driven any-hit (RDN_ANYHIT_PRIMITIVE_MASK): a non-opaque hit is
+    accepted when the triangle's bit is set in a mask over built triangles."""
+    sc, S, P, rays = inst_scene
+    ntri = len(P.built_array("indices")) // 12
+    rng = np.random.default_rng(31 + flags)
+    mask = np.packbits(rng.random(ntri + 31) < 0.6, bitorder="little").view(np.uint8)
+    mask = np.frombuffer(np.pad(mask, (0, (-len(mask)) % 4)).tobytes(), np.uint32)
+    tidx = rng.integers(0, 2, rays.shape[0]).astype(np.uint32)
+    expect, _ = S.trace(rays, tlas_idx=tidx, ray_flags=flags, anyhit_mode=rt.ANYHIT_PRIMITIVE_MASK,
+                        anyhit_mask=mask, threads=4)
+    d_mask = torch.from_numpy(mask.view(np.int32).copy()).cuda()
+    got, ext = run_product(P, rays, traversal, tlas_idx=tidx, ray_flags=flags,
+                           anyhit_mode=rt.ANYHIT_PRIMITIVE_MASK, anyhit_mask=d_mask)
+    if traversal == rt.TRAVERSAL_REFERENCE:
+        assert_bit_identical(got, ext, expect)
+    elif flags & rt.RAY_FLAG_ACCEPT_FIRST_HIT_AND_END_SEARCH:
+        assert np.array_equal(got["prim"] == orc.MISS, expect["prim"] == orc.MISS)
+    else:
+        c = classify(got, expect)
+        assert c["other"] == 0, c
+    # the mask changes results: with every bit clear non-opaque geometry is never hit
+    none, _ = S.trace(rays, tlas_idx=tidx, ray_flags=flags, anyhit_mode=rt.ANYHIT_PRIMITIVE_MASK,
+                      anyhit_mask=np.zeros_like(mask), threads=4)
+    if flags & rt.RAY_FLAG_FORCE_NON_OPAQUE:
+        assert np.all(none["prim"] == orc.MISS)
