@@ -602,8 +602,8 @@ def bench_adjoint(args):
     sp = C.c_void_p(stream.cuda_stream)
 
     # traversal stacks in shared or local memory: the faster forward decides
-    def fwd_ms(ls, reps=20):
-        fwd.local_stack = ls
+    def fwd_ms(ls, sp_, reps=20):
+        fwd.local_stack, fwd.speculation = ls, sp_
         for _ in range(3):
             assert L.rdn_attr_loss_forward(P._h, C.byref(fwd), sp) == 0
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -614,10 +614,10 @@ def bench_adjoint(args):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / reps
 
-    stack_ms = {ls: fwd_ms(ls) for ls in (0, 1)}
-    local = min(stack_ms, key=stack_ms.get)
+    stack_ms = {(ls, sp_): fwd_ms(ls, sp_) for ls in (0, 1) for sp_ in (0, 4)}
+    local, spec = min(stack_ms, key=stack_ms.get)
     for dsc in (fwd, fwd_rec, adj, adj_rec):
-        dsc.local_stack = local
+        dsc.local_stack, dsc.speculation = local, spec
 
     def run(mode):
         loss.zero_()
@@ -642,7 +642,7 @@ def bench_adjoint(args):
     out["fwd_adjoint_over_fwd"] = round(out["forward_adjoint_ms"] / out["forward_ms"], 3)
     out["fwd_adjoint_retrace_over_fwd"] = round(out["forward_adjoint_retrace_ms"] / out["forward_ms"], 3)
     out["adjoint"] = "from the forward's recorded hits (8 B per ray); _retrace: hits traced again"
-    out["local_stack"] = local
+    out["local_stack"], out["speculation"] = local, spec
     out["loss"] = float(loss.item())
     out["workload"] = f"heightfield {n_grid}^2 ({mesh.triangle_count} tris), {res}x{res} rays, attribute loss"
     P.close()
@@ -741,23 +741,26 @@ def bench_batched_adjoint(args):
         L.rdn_graph_destroy(h)
         return e0.elapsed_time(e1) / reps
 
-    # traversal stacks in shared or local memory: the faster forward decides
-    stack_ms = {ls: graph_ms(desc(targets=targets.data_ptr(), loss_sum=loss.data_ptr(), local_stack=ls))
-                for ls in (0, 1)}
-    local = min(stack_ms, key=stack_ms.get)
+    # traversal stacks in shared or local memory and the leaf-postponement
+    # threshold: the faster forward decides
+    stack_ms = {(ls, sp_): graph_ms(desc(targets=targets.data_ptr(), loss_sum=loss.data_ptr(), local_stack=ls,
+                                         speculation=sp_))
+                for ls in (0, 1) for sp_ in (0, 4)}
+    local, spec = min(stack_ms, key=stack_ms.get)
+    knobs = dict(local_stack=local, speculation=spec)
     both = desc(targets=targets.data_ptr(), loss_sum=loss.data_ptr(), grad_vertices=grad.data_ptr(), from_record=1,
-                local_stack=local, **tape)
-    retrace = desc(targets=targets.data_ptr(), loss_sum=loss.data_ptr(), grad_vertices=grad.data_ptr(),
-                   local_stack=local)
-    fwd = desc(targets=targets.data_ptr(), loss_sum=loss.data_ptr(), local_stack=local)
+                **knobs, **tape)
+    retrace = desc(targets=targets.data_ptr(), loss_sum=loss.data_ptr(), grad_vertices=grad.data_ptr(), **knobs)
+    fwd = desc(targets=targets.data_ptr(), loss_sum=loss.data_ptr(), **knobs)
     g = C.c_void_p()
     assert L.rdn_attr_paths_graph(P._h, C.byref(both), nv, C.byref(g)) == 0
     gr = C.c_void_p()
     assert L.rdn_attr_paths_graph(P._h, C.byref(retrace), nv, C.byref(gr)) == 0
     gf = C.c_void_p()
     assert L.rdn_attr_paths_graph(P._h, C.byref(fwd), nv, C.byref(gf)) == 0
-    out = {"local_stack": local, "forward_ms_by_stack": {("local" if k else "shared"): round(v, 3)
-                                                          for k, v in stack_ms.items()}}
+    out = {"local_stack": local, "speculation": spec,
+           "forward_ms_by_knobs": {f"{'local' if k[0] else 'shared'}/spec{k[1]}": round(v, 3)
+                                   for k, v in stack_ms.items()}}
     for name, handle in (("forward", gf), ("forward_adjoint", g), ("forward_adjoint_retrace", gr)):
         for _ in range(args.warmup):
             L.rdn_graph_launch(handle, sp)

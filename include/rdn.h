@@ -412,6 +412,7 @@ typedef struct rdn_attr_loss_desc {
   uint32_t* hit_tri;            /* device, nullable: built triangle of each ray's hit, RDN_MISS (forward) */
   uint32_t* hit_inst;           /* device, nullable: TLAS instance slot of each ray's hit (forward) */
   uint32_t local_stack;         /* ordered walks: 1 = traversal stacks in local memory */
+  uint32_t speculation;         /* ordered walks: leaf postponement threshold, as in rdn_wavefront_desc */
 } rdn_attr_loss_desc;
 
 /* Forward: trace, interpolate, loss. Extends the reference's closest-hit query
@@ -454,6 +455,7 @@ typedef struct rdn_attr_path_desc {
                                    seg_tri / seg_inst / seg_rays (a tape) instead of tracing the paths again */
   uint32_t* seg_inst;           /* device, nullable: TLAS instance slot of each segment's hit (forward) */
   uint32_t local_stack;         /* ordered walks: 1 = traversal stacks in local memory */
+  uint32_t speculation;         /* ordered walks: leaf postponement threshold, as in rdn_wavefront_desc */
 } rdn_attr_path_desc;
 
 rdn_status rdn_attr_paths_forward(rdn_ctx* ctx, const rdn_attr_path_desc* desc, void* stream);

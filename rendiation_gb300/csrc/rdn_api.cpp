@@ -717,6 +717,8 @@ rdn_status prepare_attr(rdn_ctx* c, const rdn_attr_loss_desc* d, bool adjoint, r
   td.traversal = d->traversal;
   td.local_stack = d->local_stack;
   fill_params(c, &td, p);
+  if (d->speculation > 31) return fail(c, RDN_ERR_INVALID_ARG, "speculation must be 0..31");
+  p.spec_threshold = d->speculation;
   std::memset(&a, 0, sizeof(a));
   a.rays = reinterpret_cast<const float4*>(d->rays);
   a.count = d->count;
@@ -800,6 +802,8 @@ rdn_status prepare_attr_paths(rdn_ctx* c, const rdn_attr_path_desc* d, bool adjo
   td.traversal = d->traversal;
   td.local_stack = d->local_stack;
   fill_params(c, &td, p);
+  if (d->speculation > 31) return fail(c, RDN_ERR_INVALID_ARG, "speculation must be 0..31");
+  p.spec_threshold = d->speculation;
   std::memset(&a, 0, sizeof(a));
   a.rays = reinterpret_cast<const float4*>(d->rays);
   a.tlas_idx = d->tlas_idx;

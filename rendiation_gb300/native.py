@@ -102,7 +102,8 @@ class AttrLossDesc(C.Structure):
                 ("ray_loss", C.c_void_p), ("loss_sum", C.c_void_p), ("grad_vertices", C.c_void_p),
                 ("grad_ray_origin", C.c_void_p), ("grad_ray_direction", C.c_void_p), ("grad_scale", C.c_float),
                 ("traversal", C.c_uint32), ("block_size", C.c_uint32), ("from_record", C.c_uint32),
-                ("hit_tri", C.c_void_p), ("hit_inst", C.c_void_p), ("local_stack", C.c_uint32)]
+                ("hit_tri", C.c_void_p), ("hit_inst", C.c_void_p), ("local_stack", C.c_uint32),
+                ("speculation", C.c_uint32)]
 
 
 class AttrPathDesc(C.Structure):
@@ -111,7 +112,7 @@ class AttrPathDesc(C.Structure):
                 ("values", C.c_void_p), ("loss_sum", C.c_void_p), ("grad_vertices", C.c_void_p),
                 ("seg_tri", C.c_void_p), ("seg_rays", C.c_void_p), ("grad_scale", C.c_float),
                 ("traversal", C.c_uint32), ("block_size", C.c_uint32), ("from_record", C.c_uint32),
-                ("seg_inst", C.c_void_p), ("local_stack", C.c_uint32)]
+                ("seg_inst", C.c_void_p), ("local_stack", C.c_uint32), ("speculation", C.c_uint32)]
 
 
 _lib = None
