@@ -409,6 +409,73 @@ def compare_builds(P, bin_size=4) -> dict:
             "compared": "tri_bvh_forest, indices_redirect, tri_bvh_root (byte equality)"}
 
 
+def accuracy_vs_fp64(P, S, cam, sample=65536):
+    """Errors of the product's FP32 closest hits against FP64, the figure the
+    metric is stated at: (1) a sample of the frame's primary rays, each hit
+    re-evaluated in FP64 on the same triangle (the oracle's evaluator); (2) a
+    10,000-triangle soup with 64x64 pinhole rays against an FP64 brute-force
+    closest hit over every triangle (no BVH)."""
+    import torch
+
+    from oracle import orc
+    from rendiation_gb300 import raytracing as rt
+    from rendiation_gb300 import scenes
+
+    def product_hits(system, rays):
+        d = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).cuda()
+        hits = torch.empty((rays.shape[0], 4), device="cuda")
+        ext = torch.empty((rays.shape[0], 4), dtype=torch.int32, device="cuda")
+        system.trace(d, hits, ext, traversal=rt.TRAVERSAL_ORDERED_WIDE, local_stack=1)
+        torch.cuda.synchronize()
+        h = rt.hits_to_numpy(hits)
+        out = np.zeros(rays.shape[0], orc.HIT_DTYPE)
+        for k in ("t", "u", "v", "prim"):
+            out[k] = h[k]
+        e = ext.cpu().numpy().view(np.uint32)
+        out["geometry"], out["instance"] = e[:, 0], e[:, 1]
+        return out
+
+    rays = scenes.pinhole_rays(cam)
+    pick = np.random.default_rng(5).choice(rays.shape[0], min(sample, rays.shape[0]), replace=False)
+    r = np.ascontiguousarray(rays[pick])
+    got = product_hits(P, r)
+    f64 = S.eval_fp64(r, got)
+    hit = got["prim"] != orc.MISS
+    rel_t = np.abs(got["t"][hit] - f64[hit, 0]) / np.maximum(np.abs(f64[hit, 0]), 1e-30)
+    bary = np.maximum(np.abs(got["u"][hit] - f64[hit, 1]), np.abs(got["v"][hit] - f64[hit, 2]))
+
+    soup = scenes.triangle_soup(10_000, seed=0)
+    Ps = rt.AccelerationStructureSystem(device=0)
+    b = Ps.create_bottom_level_acceleration_structure([rt.BottomLevelAccelerationStructureBuildSource(soup.positions)])
+    Ps.bind_tlas([Ps.create_top_level_acceleration_structure([rt.TopLevelAccelerationStructureSourceInstance(b)])])
+    Ps.build(blas_bin_size=4, device_build=True)
+    Ss = orc.OracleSystem()
+    sb = Ss.create_blas([(soup.positions, None, 1)])
+    Ss.bind_tlas([Ss.create_tlas([{"blas": sb}])])
+    Ss.build(blas_bin_size=4)
+    srays = scenes.pinhole_rays(scenes.soup_camera(64, 64))
+    sg = product_hits(Ps, srays)
+    truth = Ss.bruteforce_fp64(srays, threads=os.cpu_count() or 1)
+    t_hit = np.isfinite(truth[:, 0])
+    g_hit = sg["prim"] != orc.MISS
+    both = t_hit & g_hit
+    Ps.close()
+    return {
+        "heightfield_primary_rays_sampled": int(r.shape[0]),
+        "max_rel_t_error_vs_fp64_same_triangle": float(rel_t.max()) if rel_t.size else 0.0,
+        "max_abs_barycentric_error_vs_fp64": float(bary.max()) if bary.size else 0.0,
+        "soup10k_rays": int(srays.shape[0]),
+        "soup_hit_miss_disagreements_vs_fp64_bruteforce": int(np.sum(t_hit != g_hit)),
+        "soup_closest_triangle_disagreements_vs_fp64_bruteforce": int(np.sum(sg["prim"][both]
+                                                                            != truth[both, 3].astype(np.uint32))),
+        "soup_max_rel_t_error_vs_fp64_bruteforce": float(np.max(np.abs(sg["t"][both] - truth[both, 0])
+                                                                / truth[both, 0])) if both.any() else 0.0,
+        "note": ("u, v follow the reference's projected-barycentric formula bit for bit; its error grows as "
+                 "1/cos of the angle between the ray and the triangle plane (the differentiable kernels "
+                 "re-solve u, v in float-float)"),
+    }
+
+
 def oracle_heightfield(mesh):
     from oracle import orc
 
@@ -1014,6 +1081,7 @@ def main():
     ap.add_argument("--no-tune", dest="tune", action="store_false", help="skip the launch autotuner")
     ap.add_argument("--tune-cache", default=None, help="JSON file that keeps the autotuner's choices between runs")
     ap.add_argument("--no-batched-adjoint", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the FP32-vs-FP64 accuracy check")
     ap.add_argument("--diff-scenes", type=int, default=64)
     ap.add_argument("--scenes", type=int, default=256)
     ap.add_argument("--batched-steps", type=int, default=5)
@@ -1033,6 +1101,10 @@ def main():
     if ws > 1:
         torch.distributed.init_process_group("nccl")
     out, P, mesh, cam = bench_wavefront(args, ws, rank)
+    # the oracle's copy of the heightfield (CPU), for the accuracy check and the CPU baseline
+    S_field = oracle_heightfield(mesh) if rank == 0 and not (args.no_accuracy and args.no_cpu_baseline) else None
+    if S_field is not None and not args.no_accuracy:
+        out["accuracy_vs_fp64"] = accuracy_vs_fp64(P, S_field, cam)
     if not args.no_batched:
         P.close()
         out["batched"] = bench_batched(args)
@@ -1042,8 +1114,7 @@ def main():
         out["batched_adjoint"] = bench_batched_adjoint(args)
     if rank == 0:
         if not args.no_cpu_baseline:
-            cb, _ = cpu_baseline_wavefront(oracle_heightfield(mesh), cam, os.cpu_count() or 1,
-                                           budget_s=args.cpu_budget)
+            cb, _ = cpu_baseline_wavefront(S_field, cam, os.cpu_count() or 1, budget_s=args.cpu_budget)
             out["cpu_baseline"] = cb
         print(json.dumps(out), flush=True)
     if ws > 1:
