@@ -189,6 +189,25 @@ typedef struct rdn_trace_desc {
   const uint32_t* anyhit_mask; /* device, RDN_ANYHIT_PRIMITIVE_MASK: one bit per built triangle */
 } rdn_trace_desc;
 
+/* ---- device status ----------------------------------------------------- */
+
+/* Bits of the device error word the kernels set instead of faulting. */
+#define RDN_ERROR_STACK_OVERFLOW 0x1u   /* a traversal stack push past its depth (unreachable by construction) */
+#define RDN_ERROR_BAD_TLAS_INDEX 0x2u   /* a ray named a TLAS index that is not bound (the ray misses) */
+#define RDN_ERROR_ITERATION_LIMIT 0x4u  /* a dynamic-fetch warp reached its iteration limit and stopped */
+
+/* Waits for `stream`, reads and clears the context's device error word
+ * (*flags, nullable) and returns RDN_ERR_TIMEOUT when a warp hit its iteration
+ * limit, RDN_ERR_QUEUE_OVERFLOW on a stack overflow, else RDN_OK. The
+ * reference aborts instead (panic = "abort"); kernels here record and return. */
+rdn_status rdn_check_errors(rdn_ctx* ctx, void* stream, uint32_t* flags);
+
+/* Iteration cap of the dynamic-fetch loops (refill > 0) of every later launch;
+ * 0 restores the built-in cap (2^24, far above any real traversal). A lower cap
+ * lets a caller (or a test) bound the work of one launch: warps that reach it
+ * stop, and rdn_check_errors reports RDN_ERR_TIMEOUT. */
+rdn_status rdn_set_iteration_limit(rdn_ctx* ctx, uint32_t limit);
+
 /* Counters of node visits and triangle tests, the reference's
  * BVH_VISIT_COUNT / TRI_VISIT_COUNT (traverse_cpu.rs:38-41). */
 typedef struct rdn_counters {

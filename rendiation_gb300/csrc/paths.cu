@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(128, 8) path_dynamic_kernel(TraceParams p, Pat
   float throughput = 0.0f;
   bool exhausted = false;
   for (uint32_t iter = 0;; iter++) {
-    if (iter >= kMaxWalkRounds) {
+    if (iter >= walk_round_cap(p)) {
       if (lane == 0) atomicOr(p.error_word, 4u);
       break;
     }

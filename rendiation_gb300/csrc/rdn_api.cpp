@@ -8,6 +8,8 @@
 #include <exception>
 #include <new>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "rdn_core.h"
 #include "trace_kernels.h"
 #include "adjoint.h"
@@ -18,6 +20,13 @@
 using rdn::DevBuf;
 
 namespace {
+
+// NVTX range around an entry point (a no-op unless a profiler is attached):
+// the timeline shows build / trace / frame / paths / differentiable phases.
+struct Range {
+  explicit Range(const char* name) { nvtxRangePushA(name); }
+  ~Range() { nvtxRangePop(); }
+};
 
 rdn_status fail(rdn_ctx* c, rdn_status code, const std::string& msg) {
   if (c) c->err = msg;
@@ -193,6 +202,7 @@ rdn_status fill_params(rdn_ctx* c, const rdn_trace_desc* desc, rdn::TraceParams&
   p.error_word = c->d_counters + 8;
   p.local_stack = desc->local_stack && desc->traversal != RDN_TRAVERSAL_REFERENCE &&
                   p.stack_depth <= rdn::kLocalStackEntries;
+  p.iteration_limit = c->iteration_limit;
   return RDN_OK;
 }
 
@@ -260,6 +270,32 @@ rdn_status rdn_destroy(rdn_ctx* c) {
 }
 
 const char* rdn_last_error(const rdn_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+rdn_status rdn_set_iteration_limit(rdn_ctx* c, uint32_t limit) {
+  if (!c) return RDN_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(c->lock);
+  c->iteration_limit = limit;
+  return RDN_OK;
+}
+
+rdn_status rdn_check_errors(rdn_ctx* c, void* stream, uint32_t* flags) {
+  if (!c) return RDN_ERR_INVALID_ARG;
+  if (flags) *flags = 0;
+  if (c->device < 0) return RDN_OK;
+  std::lock_guard<std::mutex> lk(c->lock);
+  uint32_t word = 0;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&word, c->d_counters + 8, 4, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(c->d_counters + 8, 0, 4, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(c, e, "read the error word");
+  if (flags) *flags = word;
+  if (word & RDN_ERROR_ITERATION_LIMIT)
+    return fail(c, RDN_ERR_TIMEOUT, "a dynamic-fetch warp reached its iteration limit; its rays are incomplete");
+  if (word & RDN_ERROR_STACK_OVERFLOW) return fail(c, RDN_ERR_QUEUE_OVERFLOW, "traversal stack overflow");
+  return RDN_OK;
+}
 
 rdn_status rdn_blas_create(rdn_ctx* c, const rdn_geometry* g, uint32_t count, uint32_t* out_handle) {
   if (!c || !out_handle || (count && !g)) return fail(c, RDN_ERR_INVALID_ARG, "null argument");
@@ -344,6 +380,7 @@ rdn_status rdn_bind_tlas(rdn_ctx* c, const uint32_t* handles, uint32_t count) {
 }
 
 rdn_status rdn_build(rdn_ctx* c, const rdn_build_opts* o) {
+  Range range_("rdn_build");
   if (!c) return RDN_ERR_INVALID_ARG;
   std::lock_guard<std::mutex> lk(c->lock);
   rdn::BuildOptions opts;
@@ -448,6 +485,7 @@ rdn_status rdn_get_built_array(const rdn_ctx* cc, uint32_t which, void* dst, siz
 }
 
 rdn_status rdn_trace(rdn_ctx* c, const rdn_trace_desc* desc, void* stream) {
+  Range range_("rdn_trace");
   rdn_status st = validate_trace(c, desc);
   if (st != RDN_OK) return st;
   std::lock_guard<std::mutex> lk(c->lock);
@@ -463,6 +501,7 @@ rdn_status rdn_trace(rdn_ctx* c, const rdn_trace_desc* desc, void* stream) {
 }
 
 rdn_status rdn_trace_counted(rdn_ctx* c, const rdn_trace_desc* desc, void* stream, rdn_counters* out) {
+  Range range_("rdn_trace_counted");
   rdn_status st = validate_trace(c, desc);
   if (st != RDN_OK) return st;
   if (!out) return fail(c, RDN_ERR_INVALID_ARG, "null counters");
@@ -493,6 +532,7 @@ rdn_status rdn_wavefront_scratch_size(uint32_t width, uint32_t height, size_t* b
 }
 
 rdn_status rdn_wavefront_shadow_bounce(rdn_ctx* c, const rdn_wavefront_desc* d, void* stream) {
+  Range range_("rdn_wavefront_shadow_bounce");
   if (!c || !d) return fail(c, RDN_ERR_INVALID_ARG, "null context or descriptor");
   if (c->device < 0) return fail(c, RDN_ERR_UNSUPPORTED, "host-only context cannot trace");
   const uint32_t W = d->camera.width, H = d->camera.height;
@@ -626,6 +666,7 @@ rdn_status rdn_paths_scratch_size(uint32_t count, uint32_t max_bounces, uint32_t
 }
 
 rdn_status rdn_trace_paths(rdn_ctx* c, const rdn_path_desc* d, void* stream) {
+  Range range_("rdn_trace_paths");
   if (!c) return RDN_ERR_INVALID_ARG;
   std::lock_guard<std::mutex> lk(c->lock);
   rdn::TraceParams p;
@@ -640,6 +681,7 @@ rdn_status rdn_trace_paths(rdn_ctx* c, const rdn_path_desc* d, void* stream) {
 }
 
 rdn_status rdn_trace_paths_graph(rdn_ctx* c, const rdn_path_desc* d, rdn_graph** out) {
+  Range range_("rdn_trace_paths_graph");
   if (!c || !out) return RDN_ERR_INVALID_ARG;
   *out = nullptr;
   std::lock_guard<std::mutex> lk(c->lock);
@@ -675,6 +717,7 @@ rdn_status rdn_trace_paths_graph(rdn_ctx* c, const rdn_path_desc* d, rdn_graph**
 }
 
 rdn_status rdn_graph_launch(rdn_graph* g, void* stream) {
+  Range range_("rdn_graph_launch");
   if (!g || !g->exec) return RDN_ERR_INVALID_ARG;
   cudaError_t e = cudaSetDevice(g->device);
   if (e == cudaSuccess) e = cudaGraphLaunch(g->exec, static_cast<cudaStream_t>(stream));
@@ -745,6 +788,7 @@ rdn_status prepare_attr(rdn_ctx* c, const rdn_attr_loss_desc* d, bool adjoint, r
 extern "C" {
 
 rdn_status rdn_attr_loss_forward(rdn_ctx* c, const rdn_attr_loss_desc* d, void* stream) {
+  Range range_("rdn_attr_loss_forward");
   if (!c) return RDN_ERR_INVALID_ARG;
   std::lock_guard<std::mutex> lk(c->lock);
   rdn::TraceParams p;
@@ -759,6 +803,7 @@ rdn_status rdn_attr_loss_forward(rdn_ctx* c, const rdn_attr_loss_desc* d, void* 
 }
 
 rdn_status rdn_attr_loss_adjoint(rdn_ctx* c, const rdn_attr_loss_desc* d, void* stream) {
+  Range range_("rdn_attr_loss_adjoint");
   if (!c) return RDN_ERR_INVALID_ARG;
   std::lock_guard<std::mutex> lk(c->lock);
   rdn::TraceParams p;
@@ -832,6 +877,7 @@ rdn_status prepare_attr_paths(rdn_ctx* c, const rdn_attr_path_desc* d, bool adjo
 extern "C" {
 
 rdn_status rdn_attr_paths_forward(rdn_ctx* c, const rdn_attr_path_desc* d, void* stream) {
+  Range range_("rdn_attr_paths_forward");
   if (!c) return RDN_ERR_INVALID_ARG;
   std::lock_guard<std::mutex> lk(c->lock);
   rdn::TraceParams p;
@@ -847,6 +893,7 @@ rdn_status rdn_attr_paths_forward(rdn_ctx* c, const rdn_attr_path_desc* d, void*
 }
 
 rdn_status rdn_attr_paths_adjoint(rdn_ctx* c, const rdn_attr_path_desc* d, void* stream) {
+  Range range_("rdn_attr_paths_adjoint");
   if (!c) return RDN_ERR_INVALID_ARG;
   std::lock_guard<std::mutex> lk(c->lock);
   rdn::TraceParams p;
@@ -862,6 +909,7 @@ rdn_status rdn_attr_paths_adjoint(rdn_ctx* c, const rdn_attr_path_desc* d, void*
 }
 
 rdn_status rdn_attr_paths_graph(rdn_ctx* c, const rdn_attr_path_desc* d, uint64_t num_vertices, rdn_graph** out) {
+  Range range_("rdn_attr_paths_graph");
   if (!c || !out) return RDN_ERR_INVALID_ARG;
   *out = nullptr;
   std::lock_guard<std::mutex> lk(c->lock);
@@ -920,6 +968,7 @@ rdn_status rdn_scan_scratch_size(uint32_t count, size_t* bytes) {
 
 rdn_status rdn_scan_u32(const uint32_t* in, uint32_t* out, uint32_t count, int inclusive, uint32_t segment,
                         void* scratch, size_t scratch_bytes, void* stream) {
+  Range range_("rdn_scan_u32");
   if (count && (!in || !out || !scratch)) return RDN_ERR_INVALID_ARG;
   if (segment & (segment - 1)) return RDN_ERR_INVALID_ARG;
   if (scratch_bytes < rdn::scan_scratch_bytes(count) || (reinterpret_cast<uintptr_t>(scratch) & 255))
@@ -936,6 +985,7 @@ rdn_status rdn_compact_scratch_size(uint32_t count, size_t* bytes) {
 
 rdn_status rdn_compact_u32(const uint32_t* values, const uint32_t* flags, uint32_t* out, uint32_t* out_count,
                            uint32_t count, void* scratch, size_t scratch_bytes, void* stream) {
+  Range range_("rdn_compact_u32");
   if (!out_count || (count && (!values || !flags || !out || !scratch))) return RDN_ERR_INVALID_ARG;
   if (scratch_bytes < rdn::compact_scratch_bytes(count) || (reinterpret_cast<uintptr_t>(scratch) & 255))
     return RDN_ERR_INVALID_ARG;
@@ -951,6 +1001,7 @@ rdn_status rdn_radix_sort_scratch_size(uint32_t count, size_t* bytes) {
 
 rdn_status rdn_radix_sort_u32(uint32_t* keys, uint32_t* values, uint32_t count, uint32_t key_bits, void* scratch,
                               size_t scratch_bytes, void* stream) {
+  Range range_("rdn_radix_sort_u32");
   if (count > 1 && (!keys || !scratch)) return RDN_ERR_INVALID_ARG;
   if (key_bits < 1 || key_bits > 32) return RDN_ERR_INVALID_ARG;
   if (scratch_bytes < rdn::sort_scratch_bytes(count) || (reinterpret_cast<uintptr_t>(scratch) & 255))
@@ -962,6 +1013,7 @@ rdn_status rdn_radix_sort_u32(uint32_t* keys, uint32_t* values, uint32_t count, 
 // Allocation-free wavefront: identical work to rdn_wavefront_shadow_bounce with
 // the queues in the library's static device array (see wavefront_static.cu).
 rdn_status rdn_wavefront_shadow_bounce_static(rdn_ctx* c, const rdn_wavefront_desc* d, void* stream) {
+  Range range_("rdn_wavefront_shadow_bounce_static");
   if (!c || !d) return fail(c, RDN_ERR_INVALID_ARG, "null context or descriptor");
   if (c->device < 0) return fail(c, RDN_ERR_UNSUPPORTED, "host-only context cannot trace");
   if (d->scratch || d->scratch_bytes)

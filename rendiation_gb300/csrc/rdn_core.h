@@ -192,6 +192,7 @@ struct rdn_ctx {
   std::unique_ptr<rdn::HostBuilt> host;
   rdn::DeviceBuilt dev;
   uint32_t* d_counters = nullptr;  // 4 x u64 counters + error words
+  uint32_t iteration_limit = 0;     // cap of the dynamic-fetch loops (0 = built-in)
   double build_seconds = 0.0, upload_seconds = 0.0, device_seconds = 0.0;
   std::string err;
 };

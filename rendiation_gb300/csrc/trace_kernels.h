@@ -40,6 +40,9 @@ struct TraceParams {
   // have one)
   uint32_t spec_threshold;
   const uint32_t* anyhit_mask;  // RDN_ANYHIT_PRIMITIVE_MASK: one bit per built triangle
+  // iteration cap of the dynamic-fetch loops (0 = the built-in cap); on
+  // reaching it a warp sets bit 2 of the error word and stops
+  uint32_t iteration_limit;
 };
 
 // entries of a local-memory traversal stack

@@ -472,6 +472,9 @@ __device__ __forceinline__ void traverse_ray(const TraceParams& p, RayCtx& R, ui
 // can stop, hand new rays to its idle lanes, and continue.
 enum : uint32_t { WALK_IDLE = 0, WALK_TLAS = 1, WALK_INST = 2, WALK_GEOM = 3, WALK_BLAS = 4, WALK_DONE = 5 };
 constexpr uint32_t kMaxWalkRounds = 1u << 24;
+__device__ __forceinline__ uint32_t walk_round_cap(const TraceParams& p) {
+  return p.iteration_limit ? p.iteration_limit : kMaxWalkRounds;
+}
 
 template <int WIDTH>
 struct LaneWalk {
@@ -602,7 +605,7 @@ struct LaneWalk {
     to_blas(p);
     if (phase != WALK_BLAS) return;
     for (uint32_t round = 0;; round++) {
-      if (round >= kMaxWalkRounds) {
+      if (round >= walk_round_cap(p)) {
         atomicOr(p.error_word, 4u);
         phase = WALK_DONE;
         return;

@@ -209,7 +209,7 @@ __global__ void __launch_bounds__(128, 8) secondary_dynamic_kernel(TraceParams p
   uint32_t q = 0;
   bool exhausted = false;
   for (uint32_t iter = 0;; iter++) {
-    if (iter >= kMaxWarpIterations) {
+    if (iter >= (p.iteration_limit ? p.iteration_limit : kMaxWarpIterations)) {
       if (lane == 0) atomicOr(p.error_word, 4u);
       break;
     }

@@ -28,8 +28,12 @@ EXPORTED_SYMBOLS = [
     "rdn_graph_launch", "rdn_graph_destroy", "rdn_attr_loss_forward", "rdn_attr_loss_adjoint",
     "rdn_scan_scratch_size", "rdn_scan_u32", "rdn_compact_scratch_size", "rdn_compact_u32",
     "rdn_radix_sort_scratch_size", "rdn_radix_sort_u32", "rdn_attr_paths_forward", "rdn_attr_paths_adjoint",
-    "rdn_attr_paths_graph",
+    "rdn_attr_paths_graph", "rdn_check_errors", "rdn_set_iteration_limit",
 ]
+
+
+# device error-word bits (rdn_check_errors)
+ERROR_STACK_OVERFLOW, ERROR_BAD_TLAS_INDEX, ERROR_ITERATION_LIMIT = 0x1, 0x2, 0x4
 
 
 class RdnError(RuntimeError):
@@ -154,6 +158,10 @@ def lib() -> C.CDLL:
     L.rdn_trace.restype = i32
     L.rdn_trace_counted.argtypes = [vp, C.POINTER(TraceDesc), vp, C.POINTER(Counters)]
     L.rdn_trace_counted.restype = i32
+    L.rdn_check_errors.argtypes = [vp, vp, C.POINTER(u32)]
+    L.rdn_check_errors.restype = i32
+    L.rdn_set_iteration_limit.argtypes = [vp, u32]
+    L.rdn_set_iteration_limit.restype = i32
     L.rdn_wavefront_scratch_size.argtypes = [u32, u32, C.POINTER(C.c_size_t)]
     L.rdn_wavefront_scratch_size.restype = i32
     L.rdn_wavefront_shadow_bounce.argtypes = [vp, C.POINTER(WavefrontDesc), vp]

@@ -164,6 +164,20 @@ class AccelerationStructureSystem:
         _check(self._h, self._L.rdn_get_build_stats(self._h, C.byref(st)))
         return {name: getattr(st, name) for name, _ in native.BuildStats._fields_ if name != "reserved"}
 
+    def check_errors(self, stream=None) -> tuple[int, int]:
+        """Waits for the stream and returns (status, error-word bits) of the
+        kernels launched since the last check (the word is cleared)."""
+        import torch
+
+        s = (stream or torch.cuda.current_stream()).cuda_stream
+        flags = C.c_uint32()
+        st = self._L.rdn_check_errors(self._h, C.c_void_p(s), C.byref(flags))
+        return st, flags.value
+
+    def set_iteration_limit(self, limit: int):
+        """Cap of the dynamic-fetch loops of later launches (0 = built-in)."""
+        _check(self._h, self._L.rdn_set_iteration_limit(self._h, limit))
+
     def device_bytes(self) -> int:
         return int(self.build_stats()["device_bytes"])
 

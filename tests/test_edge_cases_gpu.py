@@ -102,3 +102,37 @@ def test_empty_launches(field, cuda):
     assert c["node_visits"] == 0
     torch.cuda.synchronize()
     assert torch.all(sentinel == -3.0)
+
+
+def test_error_word_reports_and_recovers(cuda):
+    """Failure detection without a GPU fault: kernels record conditions in the
+    context's error word and return; rdn_check_errors maps them to a status,
+    clears the word, and the context keeps working."""
+    mesh = scenes.heightfield(64, seed=1)
+    sc = single_mesh_scene(mesh)
+    S, P = sc.build_oracle(), sc.build_product()
+    cam = scenes.heightfield_camera(96, 64)
+    wf = rt.Wavefront(P, cam, (0.2, 0.2, 2.0), traversal=rt.TRAVERSAL_ORDERED, refill=8)
+    wf.run(1)
+    assert P.check_errors() == (0, 0)
+    # a ray naming an unbound TLAS misses and is flagged, status stays OK
+    rays = scenes.pinhole_rays(cam)[:64]
+    got, _ = run_product(P, rays, rt.TRAVERSAL_ORDERED, tlas_idx=np.full(64, 7, np.int32))
+    assert np.all(got["prim"] == orc.MISS)
+    st, flags = P.check_errors()
+    assert st == 0 and flags == native.ERROR_BAD_TLAS_INDEX
+    assert P.check_errors() == (0, 0)  # cleared
+    # a tiny iteration cap stops the dynamic-fetch warps: RDN_ERR_TIMEOUT, no hang, no fault
+    P.set_iteration_limit(2)
+    wf.run(1)
+    st, flags = P.check_errors()
+    assert st == -6 and flags & native.ERROR_ITERATION_LIMIT  # RDN_ERR_TIMEOUT
+    # back to the built-in cap: the same frame completes and matches the oracle
+    P.set_iteration_limit(0)
+    wf.run(1)
+    assert P.check_errors() == (0, 0)
+    exp, _, _ = orc.wavefront_shadow_bounce(S, cam.as_floats(), 96, 64, (0.2, 0.2, 2.0), 1, threads=4)
+    got = wf.results()
+    same = got["primary_prim"] == exp["primary_prim"]
+    assert same.mean() > 0.999
+    assert np.array_equal(got["light"][same], exp["light"][same])
