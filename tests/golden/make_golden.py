@@ -17,8 +17,14 @@ Cases:
             scene, both TLAS, five ray-flag / cull-mask combinations.
   wavefront 32x32 heightfield, 48x32 frame of the primary + shadow + bounce
             pipeline (pixel records).
+  naive_fixture
+            the reference's own BVH test scene (naive/test.rs:9-225: sphere, torus
+            and cube BLAS, five TLAS) with its 256x256 back-face-culled camera:
+            the generated vertex arrays and instance transforms, per TLAS the
+            primitive-id image of test.rs:266-270 and the full hit records of
+            every fourth pixel in both directions, and the build digests.
 
-Run:  python tests/golden/make_golden.py
+Run:  python tests/golden/make_golden.py [case ...]   (all cases when none is named)
 """
 
 from __future__ import annotations
@@ -34,6 +40,7 @@ TESTS = os.path.dirname(HERE)
 sys.path.insert(0, TESTS)
 
 from helpers import instanced_scene, orc, rt, scenes, single_mesh_scene  # noqa: E402
+import naive_fixture as nf  # noqa: E402
 
 LIGHT = np.array([0.2, 0.2, 2.0], np.float32)
 FLAG_CASES = [
@@ -80,8 +87,27 @@ def wavefront_case():
                 sample_index=np.uint32(4), pixels=pix, ray_counts=np.array(nrays, np.uint64))
 
 
+def naive_fixture_case():
+    ms = nf.meshes()
+    S = nf.make_scene(ms).build_oracle()
+    rays = nf.camera_rays(*nf.CPU_TEST_RANGE)
+    out = {"digests": digests(S), "transforms": nf.all_transforms()}
+    for name, m in zip(("sphere", "torus", "cube"), ms):
+        out[f"{name}_positions"], out[f"{name}_indices"] = m.positions, m.indices
+    for k in range(5):
+        h, _ = S.trace(rays, tlas_uniform=k, ray_flags=rt.RAY_FLAG_CULL_BACK_FACING_TRIANGLES)
+        out[f"image{k}"] = nf.id_image(h["prim"], orc.MISS)
+        out[f"hits{k}"] = h.reshape(nf.H, nf.W)[::4, ::4].reshape(-1)
+    return out
+
+
+CASES = {"soup1k": soup_case, "instanced": instanced_case, "wavefront": wavefront_case,
+         "naive_fixture": naive_fixture_case}
+
+
 def main():
-    for name, fn in [("soup1k", soup_case), ("instanced", instanced_case), ("wavefront", wavefront_case)]:
+    names = sys.argv[1:] or list(CASES)
+    for name, fn in ((n, CASES[n]) for n in names):
         path = os.path.join(HERE, f"{name}.npz")
         np.savez_compressed(path, **fn())
         print(path, os.path.getsize(path))
