@@ -230,11 +230,9 @@ __device__ __forceinline__ bool blas_threaded(const TraceParams& p, RayCtx& R, c
     float tn;
     const uint32_t hit_next = __float_as_uint(a.w), miss_next = __float_as_uint(b.w);
     if (slab(ir.o, ir.inv_d, R.tmin * ir.scaling, R.far_world * ir.scaling, a.x, a.y, a.z, b.x, b.y, b.z, tn)) {
-      const uint32_t leaf = curr;
       curr = hit_next;
-      if (hit_next == miss_next) {
+      if (hit_next == miss_next) {  // a leaf: hit and miss links are the same node
         const uint2 cr = __ldg(reinterpret_cast<const uint2*>(nd + 2));
-        (void)leaf;
         if (leaf_triangles<COUNT>(p, R, ir, cr.x, cr.y, gslot, inst_slot, is_opaque, cull_enable, cull_back,
                                   prim_start))
           return true;
