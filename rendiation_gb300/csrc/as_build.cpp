@@ -594,7 +594,7 @@ namespace rdn {
 std::string build_with_device_blas(const std::vector<std::unique_ptr<std::vector<GeometrySource>>>& blas,
                                    const std::vector<std::unique_ptr<std::vector<InstanceSource>>>& tlas,
                                    const std::vector<uint32_t>& binding, const BuildOptions& opt, int sm_count,
-                                   HostBuilt& hb, DeviceBuilt& d, double* device_seconds) {
+                                   cudaMemPool_t pool, HostBuilt& hb, DeviceBuilt& d, double* device_seconds) {
   // the same geometry walk as build_host: one tree per triangle geometry in
   // BLAS-slot order, one root-box entry per geometry (naive/mod.rs:239)
   std::vector<DeviceGeometry> geoms;
@@ -628,7 +628,7 @@ std::string build_with_device_blas(const std::vector<std::unique_ptr<std::vector
     hb.blas_meta_info.push_back(BlasMetaInfo{{first, (uint32_t)geoms.size()}});
   }
   DeviceBlasOut o;
-  std::string err = build_blas_device(geoms, opt.blas_bin_size, opt.blas_max_depth, sm_count, d, o);
+  std::string err = build_blas_device(geoms, opt.blas_bin_size, opt.blas_max_depth, sm_count, pool, d, o);
   if (!err.empty()) return err;
   *device_seconds = o.kernel_seconds;
   std::vector<Box> blas_box;

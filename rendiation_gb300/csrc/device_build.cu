@@ -82,8 +82,8 @@ struct BNode {  // 64 B, one per tree node during the build
 };
 static_assert(sizeof(BNode) == 64, "64 B build node");
 
-struct LevelCounters {
-  uint32_t chunks, children;
+struct LevelCounters {  // one per tree level, zeroed before the first level
+  uint32_t chunks, children, big, pad;
 };
 struct BuildCounters {
   unsigned long long sah, fallback;
@@ -190,33 +190,73 @@ __global__ void prepare_primitives_kernel(uint32_t N, uint32_t G, const uint32_t
 
 // ---- one tree level -----------------------------------------------------
 
-__global__ void level_prepare_kernel(uint32_t lb, uint32_t W, uint32_t bin_size, uint32_t max_depth,
-                                     BNode* __restrict__ pool, uint32_t* __restrict__ acc_cnt,
-                                     int* __restrict__ acc_box, uint32_t* __restrict__ chunk_node,
-                                     LevelCounters* lc) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= W) return;
-  BNode& n = pool[lb + i];
-  const uint32_t count = n.end - n.start;
-  const bool active = n.depth < max_depth && count > bin_size;
-  const bool need = active || (n.flags & F_BOX_PENDING);
-  const uint32_t nch = need ? (count + kChunk - 1) / kChunk : 0;
-  n.flags = (n.flags & ~(F_ACTIVE | F_FALLBACK)) | (active ? F_ACTIVE : 0u);
-  n.left = NONE;
-  n.nchunks = nch;
-  n.cbase = 0;
-  if (nch) {
-    const uint32_t base = atomicAdd(&lc->chunks, nch);
-    n.cbase = base;
-    for (uint32_t j = 0; j < nch; j++) chunk_node[base + j] = lb + i;
+__device__ __forceinline__ uint32_t warp_inclusive_u32(uint32_t v, uint32_t lane) {
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= (uint32_t)o) v += t;
   }
-  if (active) {
-    for (int b = 0; b < 4; b++) acc_cnt[4 * (size_t)i + b] = 0;
-    for (int b = 0; b < 4; b++)
-      for (int k = 0; k < 3; k++) {
-        acc_box[24 * (size_t)i + 6 * b + k] = key_of(INFINITY);
-        acc_box[24 * (size_t)i + 6 * b + 3 + k] = key_of(-INFINITY);
-      }
+  return v;
+}
+
+// Warp-aggregated claim on a counter: all 32 lanes call, each with its own
+// amount (0 allowed); one atomic per warp instead of one per lane (a level
+// of 250 k nodes would otherwise serialise on the counter's address).
+__device__ __forceinline__ uint32_t warp_claim(uint32_t* ctr, uint32_t amount, uint32_t lane) {
+  const uint32_t inc = warp_inclusive_u32(amount, lane);
+  const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
+  uint32_t base = 0;
+  if (lane == 31 && total) base = atomicAdd(ctr, total);
+  base = __shfl_sync(0xffffffffu, base, 31);
+  return base + inc - amount;
+}
+
+// Level L holds nodes [lvl[L], lvl[L+1]) of the pool. The bounds live on the
+// device: level L's last kernel writes lvl[L+2], so that the host can queue
+// several levels without reading anything back. Kernels of an empty level
+// (past the last one) find no node and return. Node loops step a whole warp
+// at a time (warp-uniform bounds) so that the lanes can aggregate atomics.
+__global__ void level_prepare_kernel(const uint32_t* __restrict__ lvl, uint32_t L, uint32_t bin_size,
+                                     uint32_t max_depth, BNode* __restrict__ pool, uint32_t* __restrict__ acc_cnt,
+                                     int* __restrict__ acc_box, uint32_t* __restrict__ chunk_node,
+                                     LevelCounters* lcs) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t lb = lvl[L], W = lvl[L + 1] - lb;
+  LevelCounters* lc = lcs + L;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t i0 = blockIdx.x * blockDim.x + threadIdx.x - lane; i0 < W; i0 += stride) {
+    const uint32_t i = i0 + lane;
+    uint32_t nch = 0;
+    bool active = false;
+    if (i < W) {
+      BNode& n = pool[lb + i];
+      const uint32_t count = n.end - n.start;
+      active = n.depth < max_depth && count > bin_size;
+      const bool need = active || (n.flags & F_BOX_PENDING);
+      nch = need ? (count + kChunk - 1) / kChunk : 0;
+      n.flags = (n.flags & ~(F_ACTIVE | F_FALLBACK)) | (active ? F_ACTIVE : 0u);
+      n.left = NONE;
+      n.nchunks = nch;
+    }
+    const uint32_t base = warp_claim(&lc->chunks, nch, lane);
+    if (i < W) pool[lb + i].cbase = nch ? base : 0u;
+    // chunk -> node map: small ranges by their own lane, long ones by the whole warp
+    if (nch && nch <= 32)
+      for (uint32_t j = 0; j < nch; j++) chunk_node[base + j] = lb + i;
+    uint32_t wide = __ballot_sync(0xffffffffu, nch > 32);
+    while (wide) {
+      const uint32_t src = __ffs(wide) - 1;
+      wide &= wide - 1;
+      const uint32_t b = __shfl_sync(0xffffffffu, base, src), c = __shfl_sync(0xffffffffu, nch, src);
+      for (uint32_t j = lane; j < c; j += 32) chunk_node[b + j] = lb + i0 + src;
+    }
+    if (active) {
+      for (int b = 0; b < 4; b++) acc_cnt[4 * (size_t)i + b] = 0;
+      for (int b = 0; b < 4; b++)
+        for (int k = 0; k < 3; k++) {
+          acc_box[24 * (size_t)i + 6 * b + k] = key_of(INFINITY);
+          acc_box[24 * (size_t)i + 6 * b + 3 + k] = key_of(-INFINITY);
+        }
+    }
   }
 }
 
@@ -226,10 +266,11 @@ __device__ __forceinline__ void chunk_range(const BNode& n, uint32_t c, uint32_t
 }
 
 // Boxes of nodes whose box is still unknown: min/max of the primitive boxes.
-__global__ void level_box_kernel(const LevelCounters* lc, BNode* __restrict__ pool, const uint32_t* __restrict__ chunk_node,
-                                 const uint32_t* __restrict__ order, const float4* __restrict__ pbox) {
+__global__ void level_box_kernel(const LevelCounters* lcs, uint32_t L, BNode* __restrict__ pool,
+                                 const uint32_t* __restrict__ chunk_node, const uint32_t* __restrict__ order,
+                                 const float4* __restrict__ pbox) {
   const uint32_t lane = threadIdx.x & 31u;
-  const uint32_t total = lc->chunks;
+  const uint32_t total = lcs[L].chunks;
   for (uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < total; c += (gridDim.x * blockDim.x) >> 5) {
     const uint32_t id = chunk_node[c];
     const BNode n = pool[id];
@@ -274,13 +315,15 @@ __device__ __forceinline__ SplitPlane plane_of(const BNode& n) {
 }
 
 // Bucket counts and boxes of each chunk, merged into the node.
-__global__ void level_stats_kernel(uint32_t lb, uint32_t N, const LevelCounters* lc, const BNode* __restrict__ pool,
+__global__ void level_stats_kernel(const uint32_t* __restrict__ lvl, uint32_t L, uint32_t N,
+                                   const LevelCounters* lcs, const BNode* __restrict__ pool,
                                    const uint32_t* __restrict__ chunk_node, const uint32_t* __restrict__ order,
                                    const float4* __restrict__ pbox, const float* __restrict__ cen,
                                    uint32_t* __restrict__ chunk_cnt, uint32_t* __restrict__ acc_cnt,
                                    int* __restrict__ acc_box) {
   const uint32_t lane = threadIdx.x & 31u;
-  const uint32_t total = lc->chunks;
+  const uint32_t lb = lvl[L];
+  const uint32_t total = lcs[L].chunks;
   for (uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < total; c += (gridDim.x * blockDim.x) >> 5) {
     const uint32_t id = chunk_node[c];
     const BNode n = pool[id];
@@ -334,133 +377,221 @@ __global__ void level_stats_kernel(uint32_t lb, uint32_t N, const LevelCounters*
   }
 }
 
-__device__ __forceinline__ uint32_t warp_inclusive_u32(uint32_t v, uint32_t lane) {
-  for (int o = 1; o < 32; o <<= 1) {
-    const uint32_t t = __shfl_up_sync(0xffffffffu, v, o);
-    if (lane >= (uint32_t)o) v += t;
+// Nodes with more chunks than this leave their chunk prefix to
+// level_big_prefix_kernel (a block per node); smaller ones are scanned by
+// their own thread.
+constexpr uint32_t kBigChunks = 8;
+
+// The reference's split decision for one active node (strategy.rs:202-284):
+// the 4 buckets' counts and boxes, then either BalanceTree's median split
+// (3 empty buckets, strategy.rs:67-87) or the first strictly cheaper of the 3
+// SAH candidates. Fills the two children; returns true for the median split.
+__device__ __forceinline__ bool decide_split(const BNode& n, uint32_t i, const uint32_t* __restrict__ acc_cnt,
+                                             const int* __restrict__ acc_box, BNode& l, BNode& r) {
+  uint32_t cnt[4];
+  NodeBox bb[4];
+  for (int q = 0; q < 4; q++) {
+    cnt[q] = acc_cnt[4 * (size_t)i + q];
+    const int* k = acc_box + 24 * (size_t)i + 6 * q;
+    bb[q] = NodeBox{{val_of(k[0]), val_of(k[1]), val_of(k[2])}, {val_of(k[3]), val_of(k[4]), val_of(k[5])}};
   }
-  return v;
+  const int empties = (cnt[0] == 0) + (cnt[1] == 0) + (cnt[2] == 0) + (cnt[3] == 0);
+  bool fallback = false;
+  if (empties == 3) {
+    // BalanceTree: median by centre on the same axis; child boxes come from
+    // the next level's box pass
+    fallback = true;
+    const uint32_t mid = (n.end + n.start) / 2;
+    l.start = n.start;
+    l.end = mid;
+    r.start = mid;
+    r.end = n.end;
+    l.flags = r.flags = F_BOX_PENDING;
+    set_box(l, empty_box());
+    set_box(r, empty_box());
+  } else {
+    // candidate j puts buckets 0..=j left; the first strictly cheaper
+    // candidate wins, candidate 0 when no cost is below +inf
+    float best_cost = INFINITY;
+    NodeBox best_l = empty_box(), best_r = empty_box();
+    uint32_t best_lc = 0;
+    for (int j = 0; j < 3; j++) {
+      NodeBox lb_ = empty_box(), rb_ = empty_box();
+      uint32_t lc_ = 0, rc_ = 0;
+      for (int p = 0; p <= j; p++) {
+        grow(lb_, bb[p]);
+        lc_ += cnt[p];
+      }
+      for (int p = j + 1; p < 4; p++) {
+        grow(rb_, bb[p]);
+        rc_ += cnt[p];
+      }
+      const float cost = sah_area(lb_) * (float)lc_ + sah_area(rb_) * (float)rc_;
+      if (j == 0 || cost < best_cost) {
+        best_l = lb_;
+        best_r = rb_;
+        best_lc = lc_;
+      }
+      if (cost < best_cost) best_cost = cost;
+    }
+    l.start = n.start;
+    l.end = n.start + best_lc;
+    r.start = n.start + best_lc;
+    r.end = n.end;
+    l.flags = r.flags = 0;
+    set_box(l, best_l);
+    set_box(r, best_r);
+  }
+  l.depth = r.depth = n.depth + 1;
+  l.tree = r.tree = n.tree;
+  l.left = r.left = NONE;
+  return fallback;
 }
 
-// One warp per node of the level: the split decision, the children, and the
-// per-bucket offsets of the node's chunks.
-__global__ void level_decide_kernel(uint32_t lb, uint32_t W, uint32_t next_base, BNode* __restrict__ pool,
+// One thread per node of the level: the split decision, the two children
+// (slots claimed per warp), and the exclusive per-bucket prefix of the node's
+// chunk counts (big nodes: appended to big_list for the block-wide scan).
+__global__ void level_decide_kernel(const uint32_t* __restrict__ lvl, uint32_t L, BNode* __restrict__ pool,
                                     const uint32_t* __restrict__ acc_cnt, const int* __restrict__ acc_box,
-                                    const uint32_t* __restrict__ chunk_cnt, uint32_t* __restrict__ chunk_prefix,
-                                    LevelCounters* lc, BuildCounters* bc) {
+                                    const uint4* __restrict__ chunk_cnt, uint4* __restrict__ chunk_prefix,
+                                    LevelCounters* lcs, BuildCounters* bc, uint32_t* __restrict__ big_list,
+                                    uint32_t big_cap) {
   const uint32_t lane = threadIdx.x & 31u;
-  const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (i >= W) return;
-  const uint32_t id = lb + i;
-  const BNode n = pool[id];
-  if (!(n.flags & F_ACTIVE)) return;
-  uint32_t fallback = 0;
-  if (lane == 0) {
-    uint32_t cnt[4];
-    NodeBox bb[4];
-    for (int q = 0; q < 4; q++) {
-      cnt[q] = acc_cnt[4 * (size_t)i + q];
-      const int* k = acc_box + 24 * (size_t)i + 6 * q;
-      bb[q] = NodeBox{{val_of(k[0]), val_of(k[1]), val_of(k[2])}, {val_of(k[3]), val_of(k[4]), val_of(k[5])}};
-    }
-    const int empties = (cnt[0] == 0) + (cnt[1] == 0) + (cnt[2] == 0) + (cnt[3] == 0);
+  const uint32_t lb = lvl[L], next_base = lvl[L + 1], W = next_base - lb;
+  LevelCounters* lc = lcs + L;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t i0 = blockIdx.x * blockDim.x + threadIdx.x - lane; i0 < W; i0 += stride) {
+    const uint32_t i = i0 + lane;
+    BNode n;
+    bool active = false, fallback = false;
     BNode l{}, r{};
-    if (empties == 3) {
-      // BalanceTree: median by centre on the same axis; child boxes come from
-      // the next level's box pass
-      fallback = 1;
-      const uint32_t mid = (n.end + n.start) / 2;
-      l.start = n.start;
-      l.end = mid;
-      r.start = mid;
-      r.end = n.end;
-      l.flags = r.flags = F_BOX_PENDING;
-      set_box(l, empty_box());
-      set_box(r, empty_box());
-      atomicAdd(&bc->fallback, 1ull);
-    } else {
-      // candidate j puts buckets 0..=j left; the first strictly cheaper
-      // candidate wins, candidate 0 when no cost is below +inf
-      float best_cost = INFINITY;
-      NodeBox best_l = empty_box(), best_r = empty_box();
-      uint32_t best_lc = 0;
-      for (int j = 0; j < 3; j++) {
-        NodeBox lb_ = empty_box(), rb_ = empty_box();
-        uint32_t lc_ = 0, rc_ = 0;
-        for (int p = 0; p <= j; p++) {
-          grow(lb_, bb[p]);
-          lc_ += cnt[p];
-        }
-        for (int p = j + 1; p < 4; p++) {
-          grow(rb_, bb[p]);
-          rc_ += cnt[p];
-        }
-        const float cost = sah_area(lb_) * (float)lc_ + sah_area(rb_) * (float)rc_;
-        if (j == 0 || cost < best_cost) {
-          best_l = lb_;
-          best_r = rb_;
-          best_lc = lc_;
-        }
-        if (cost < best_cost) best_cost = cost;
-      }
-      l.start = n.start;
-      l.end = n.start + best_lc;
-      r.start = n.start + best_lc;
-      r.end = n.end;
-      l.flags = r.flags = 0;
-      set_box(l, best_l);
-      set_box(r, best_r);
-      atomicAdd(&bc->sah, 1ull);
+    if (i < W) {
+      n = pool[lb + i];
+      active = (n.flags & F_ACTIVE) != 0;
+      if (active) fallback = decide_split(n, i, acc_cnt, acc_box, l, r);
     }
-    l.depth = r.depth = n.depth + 1;
-    l.tree = r.tree = n.tree;
-    l.left = r.left = NONE;
-    const uint32_t base = next_base + atomicAdd(&lc->children, 2u);
+    const uint32_t base = next_base + warp_claim(&lc->children, active ? 2u : 0u, lane);
+    const uint32_t n_sah = __popc(__ballot_sync(0xffffffffu, active && !fallback));
+    const uint32_t n_med = __popc(__ballot_sync(0xffffffffu, active && fallback));
+    if (lane == 0 && n_sah) atomicAdd(&bc->sah, (unsigned long long)n_sah);
+    if (lane == 0 && n_med) atomicAdd(&bc->fallback, (unsigned long long)n_med);
+    const bool big = active && !fallback && n.nchunks > kBigChunks;
+    const uint32_t slot = warp_claim(&lc->big, big ? 1u : 0u, lane);
+    if (!active) continue;
     pool[base] = l;
     pool[base + 1] = r;
-    pool[id].left = base;
-    if (fallback) pool[id].flags = n.flags | F_FALLBACK;
+    pool[lb + i].left = base;
+    if (fallback) pool[lb + i].flags = n.flags | F_FALLBACK;
+    if (fallback || n.nchunks == 0) continue;
+    if (big && slot < big_cap) {
+      big_list[slot] = lb + i;
+      continue;
+    }
+    uint4 run = make_uint4(0u, 0u, 0u, 0u);
+    for (uint32_t j = 0; j < n.nchunks; j++) {
+      const uint4 v = chunk_cnt[n.cbase + j];
+      chunk_prefix[n.cbase + j] = run;
+      run.x += v.x;
+      run.y += v.y;
+      run.z += v.z;
+      run.w += v.w;
+    }
   }
-  fallback = __shfl_sync(0xffffffffu, fallback, 0);
-  if (fallback || n.nchunks == 0) return;
-  // exclusive per-bucket prefix of the chunk counts inside the node
-  uint32_t carry[4] = {0, 0, 0, 0};
-  for (uint32_t b0 = 0; b0 < n.nchunks; b0 += 32) {
-    const uint32_t j = b0 + lane;
-    const bool valid = j < n.nchunks;
-    const uint32_t c = n.cbase + j;
+}
+
+// Exclusive per-bucket prefix of the chunk counts of the big nodes, one block
+// per node: each thread takes kPerThread consecutive chunks of a tile, the
+// block scans the thread totals (warp shuffles, then the warp totals).
+constexpr uint32_t kPerThread = 4;
+__global__ void __launch_bounds__(kBlock) level_big_prefix_kernel(const LevelCounters* lcs, uint32_t L,
+                                                                  const BNode* __restrict__ pool,
+                                                                  const uint32_t* __restrict__ big_list,
+                                                                  uint32_t big_cap, const uint4* __restrict__ chunk_cnt,
+                                                                  uint4* __restrict__ chunk_prefix) {
+  __shared__ uint4 warp_total[kWarps];
+  __shared__ uint4 carry_s;
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const uint32_t nbig = min(lcs[L].big, big_cap);
+  for (uint32_t b = blockIdx.x; b < nbig; b += gridDim.x) {
+    const BNode n = pool[big_list[b]];
+    uint4 carry = make_uint4(0u, 0u, 0u, 0u);
+    for (uint32_t t0 = 0; t0 < n.nchunks; t0 += kBlock * kPerThread) {
+      const uint32_t j0 = t0 + threadIdx.x * kPerThread;
+      uint4 v[kPerThread];
+      uint4 sum = make_uint4(0u, 0u, 0u, 0u);
 #pragma unroll
-    for (int q = 0; q < 4; q++) {
-      const uint32_t v = valid ? chunk_cnt[4 * (size_t)c + q] : 0u;
-      const uint32_t inc = warp_inclusive_u32(v, lane);
-      if (valid) chunk_prefix[4 * (size_t)c + q] = carry[q] + inc - v;
-      carry[q] += __shfl_sync(0xffffffffu, inc, 31);
+      for (uint32_t k = 0; k < kPerThread; k++) {
+        v[k] = j0 + k < n.nchunks ? chunk_cnt[n.cbase + j0 + k] : make_uint4(0u, 0u, 0u, 0u);
+        sum.x += v[k].x;
+        sum.y += v[k].y;
+        sum.z += v[k].z;
+        sum.w += v[k].w;
+      }
+      uint4 inc = sum;  // inclusive scan of the thread totals inside the warp
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t x = __shfl_up_sync(0xffffffffu, inc.x, o), y = __shfl_up_sync(0xffffffffu, inc.y, o);
+        const uint32_t z = __shfl_up_sync(0xffffffffu, inc.z, o), w = __shfl_up_sync(0xffffffffu, inc.w, o);
+        if (lane >= (uint32_t)o) {
+          inc.x += x;
+          inc.y += y;
+          inc.z += z;
+          inc.w += w;
+        }
+      }
+      if (lane == 31) warp_total[warp] = inc;
+      __syncthreads();
+      uint4 before = carry;  // carry + earlier warps of the tile
+      for (uint32_t q = 0; q < warp; q++) {
+        const uint4 t = warp_total[q];
+        before.x += t.x;
+        before.y += t.y;
+        before.z += t.z;
+        before.w += t.w;
+      }
+      uint4 run = make_uint4(before.x + inc.x - sum.x, before.y + inc.y - sum.y, before.z + inc.z - sum.z,
+                             before.w + inc.w - sum.w);
+#pragma unroll
+      for (uint32_t k = 0; k < kPerThread; k++) {
+        if (j0 + k < n.nchunks) chunk_prefix[n.cbase + j0 + k] = run;
+        run.x += v[k].x;
+        run.y += v[k].y;
+        run.z += v[k].z;
+        run.w += v[k].w;
+      }
+      if (threadIdx.x == kBlock - 1) carry_s = run;  // the last thread's running total ends the tile
+      __syncthreads();
+      carry = carry_s;
+      __syncthreads();
     }
   }
 }
 
 // Median split: Rust's select_nth_unstable_by on the node's range, one thread per node.
-__global__ void level_select_kernel(uint32_t lb, uint32_t W, uint32_t N, const BNode* __restrict__ pool,
-                                    const float* __restrict__ cen, uint32_t* __restrict__ order) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= W) return;
-  const BNode n = pool[lb + i];
-  if (!(n.flags & F_FALLBACK)) return;
-  const uint32_t count = n.end - n.start;
-  if (count / 2 == 0) return;
-  const int axis = split_axis(box_of(n));
-  RustSelectNth<uint32_t, CentreLess> sel(CentreLess{cen + (size_t)axis * N});
-  sel.run(order + n.start, count, count / 2);
+__global__ void level_select_kernel(const uint32_t* __restrict__ lvl, uint32_t L, uint32_t N,
+                                    const BNode* __restrict__ pool, const float* __restrict__ cen,
+                                    uint32_t* __restrict__ order) {
+  const uint32_t lb = lvl[L], W = lvl[L + 1] - lb;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < W; i += gridDim.x * blockDim.x) {
+    const BNode n = pool[lb + i];
+    if (!(n.flags & F_FALLBACK)) continue;
+    const uint32_t count = n.end - n.start;
+    if (count / 2 == 0) continue;
+    const int axis = split_axis(box_of(n));
+    RustSelectNth<uint32_t, CentreLess> sel(CentreLess{cen + (size_t)axis * N});
+    sel.run(order + n.start, count, count / 2);
+  }
 }
 
 // SAH nodes: each chunk writes its primitives to their bucket-ordered slots.
-__global__ void level_scatter_kernel(uint32_t lb, uint32_t N, const LevelCounters* lc, const BNode* __restrict__ pool,
+__global__ void level_scatter_kernel(const uint32_t* __restrict__ lvl, uint32_t L, uint32_t N,
+                                     const LevelCounters* lcs, const BNode* __restrict__ pool,
                                      const uint32_t* __restrict__ chunk_node, const uint32_t* __restrict__ order,
                                      const float* __restrict__ cen, const uint32_t* __restrict__ acc_cnt,
                                      const uint32_t* __restrict__ chunk_prefix, uint32_t* __restrict__ scratch) {
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t lt_mask = (1u << lane) - 1u;
-  const uint32_t total = lc->chunks;
+  const uint32_t lb = lvl[L];
+  const uint32_t total = lcs[L].chunks;
   for (uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < total; c += (gridDim.x * blockDim.x) >> 5) {
     const uint32_t id = chunk_node[c];
     const BNode n = pool[id];
@@ -494,11 +625,14 @@ __global__ void level_scatter_kernel(uint32_t lb, uint32_t N, const LevelCounter
   }
 }
 
-__global__ void level_copyback_kernel(const LevelCounters* lc, const BNode* __restrict__ pool,
-                                      const uint32_t* __restrict__ chunk_node, const uint32_t* __restrict__ scratch,
-                                      uint32_t* __restrict__ order) {
+// Also closes the level: the next level's end is its start plus the children
+// that level_decide_kernel created (decide ran before this launch).
+__global__ void level_copyback_kernel(uint32_t* __restrict__ lvl, uint32_t L, const LevelCounters* lcs,
+                                      const BNode* __restrict__ pool, const uint32_t* __restrict__ chunk_node,
+                                      const uint32_t* __restrict__ scratch, uint32_t* __restrict__ order) {
   const uint32_t lane = threadIdx.x & 31u;
-  const uint32_t total = lc->chunks;
+  const uint32_t total = lcs[L].chunks;
+  if (blockIdx.x == 0 && threadIdx.x == 0) lvl[L + 2] = lvl[L + 1] + lcs[L].children;
   for (uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < total; c += (gridDim.x * blockDim.x) >> 5) {
     const BNode n = pool[chunk_node[c]];
     if ((n.flags & (F_ACTIVE | F_FALLBACK)) != F_ACTIVE) continue;
@@ -694,25 +828,24 @@ __global__ void wide4_emit_kernel(uint32_t a, uint32_t W, uint32_t next_base, ui
 
 // ---- host side -------------------------------------------------------------
 
+// Stream-ordered scratch: allocated from the context's pool on the build
+// stream and returned to it (also stream-ordered) when the build returns, so
+// that a rebuild takes no driver allocation and no implicit synchronisation.
 struct Scratch {
+  cudaMemPool_t pool;
+  cudaStream_t st;
   std::vector<void*> ptrs;
   ~Scratch() {
-    for (void* p : ptrs) cudaFree(p);
+    for (void* p : ptrs) cudaFreeAsync(p, st);
   }
   template <class T>
   cudaError_t alloc(T** out, size_t count) {
     void* p = nullptr;
-    cudaError_t e = cudaMalloc(&p, (count ? count : 1) * sizeof(T));
+    const size_t bytes = (count ? count : 1) * sizeof(T);
+    cudaError_t e = pool ? cudaMallocFromPoolAsync(&p, bytes, pool, st) : cudaMallocAsync(&p, bytes, st);
     if (e == cudaSuccess) ptrs.push_back(p);
     *out = static_cast<T*>(p);
     return e;
-  }
-  void release(void* p) {
-    for (auto& q : ptrs)
-      if (q == p) {
-        cudaFree(q);
-        q = nullptr;
-      }
   }
 };
 
@@ -737,7 +870,7 @@ inline uint32_t blocks_for(uint64_t n, uint32_t per = kBlock) {
 }  // namespace
 
 std::string build_blas_device(const std::vector<DeviceGeometry>& geoms, uint32_t bin_size, uint32_t max_depth,
-                              int sm_count, DeviceBuilt& d, DeviceBlasOut& out) {
+                              int sm_count, cudaMemPool_t mem_pool, DeviceBuilt& d, DeviceBlasOut& out) {
   const uint32_t G = (uint32_t)geoms.size();
   uint64_t N64 = 0, V64 = 0;
   for (const auto& g : geoms) {
@@ -757,7 +890,7 @@ std::string build_blas_device(const std::vector<DeviceGeometry>& geoms, uint32_t
     cudaStream_t s;
     ~StreamGuard() { cudaStreamDestroy(s); }
   } guard{st};
-  Scratch S;
+  Scratch S{mem_pool, st, {}};
   uint64_t& bytes = out.bytes;
 #define CK(x)                                                                                  \
   do {                                                                                         \
@@ -807,13 +940,11 @@ std::string build_blas_device(const std::vector<DeviceGeometry>& geoms, uint32_t
   float* cen;
   uint32_t *order, *scratch;
   BuildCounters* bc;
-  LevelCounters* lc;
   CK(S.alloc(&pbox, 2 * (size_t)N));
   CK(S.alloc(&cen, 3 * (size_t)N));
   CK(S.alloc(&order, N));
   CK(S.alloc(&scratch, N));
   CK(S.alloc(&bc, 1));
-  CK(S.alloc(&lc, 1));
   CK(cudaMemsetAsync(bc, 0, sizeof(BuildCounters), st));
   const uint32_t persistent = (uint32_t)(sm_count > 0 ? sm_count : 1) * 8;
   cudaEvent_t ev0, ev1;
@@ -861,73 +992,69 @@ std::string build_blas_device(const std::vector<DeviceGeometry>& geoms, uint32_t
     if (G) CK(cudaMemcpyAsync(pool, roots.data(), sizeof(BNode) * G, cudaMemcpyHostToDevice, st));
   }
 
-  // level rounds
-  std::vector<uint32_t> level_begin = {0};
-  uint32_t lb = 0, le = G;
-  size_t acc_cap = 0, chunk_cap = 0;
-  uint32_t *acc_cnt = nullptr, *chunk_node = nullptr, *chunk_cnt = nullptr, *chunk_prefix = nullptr;
-  int* acc_box = nullptr;
-  uint32_t* h_children = nullptr;
-  CK(cudaMallocHost(&h_children, sizeof(uint32_t)));
-  struct HostGuard {
-    void* p;
-    ~HostGuard() { cudaFreeHost(p); }
-  } hg{h_children};
-  while (le > lb) {
-    const uint32_t W = le - lb;
-    if ((size_t)le + 2 * (size_t)W > cap) {  // room for this level's children
-      size_t ncap = std::max(cap * 2, (size_t)le + 2 * (size_t)W);
-      BNode* np;
-      CK(S.alloc(&np, ncap));
-      CK(cudaMemcpyAsync(np, pool, sizeof(BNode) * (size_t)le, cudaMemcpyDeviceToDevice, st));
-      CK(cudaStreamSynchronize(st));
-      S.release(pool);
-      pool = np;
-      cap = ncap;
+  // level rounds. Every buffer is sized for the largest possible level (a
+  // level holds at most N + G nodes: ranges are disjoint and only empty roots
+  // are empty), so that no level waits for the host. The host queues a batch
+  // of levels, then reads the level bounds back once to see whether an empty
+  // level has been reached; levels queued past it do nothing.
+  const uint32_t level_cap = (uint32_t)std::min<uint64_t>(max_depth, N) + 2;  // possible levels + one empty
+  const size_t node_cap = (size_t)N + G + 1;
+  const size_t chunk_cap = (size_t)N / kChunk + node_cap + 1;
+  const uint32_t big_cap = N / (kBigChunks * kChunk) + 2;  // a big node holds > kBigChunks * kChunk primitives
+  uint32_t *lvl, *acc_cnt, *chunk_node, *chunk_cnt, *chunk_prefix, *big_list;
+  LevelCounters* lcs;
+  int* acc_box;
+  CK(S.alloc(&lvl, (size_t)level_cap + 2));
+  CK(S.alloc(&lcs, level_cap));
+  CK(S.alloc(&acc_cnt, 4 * node_cap));
+  CK(S.alloc(&acc_box, 24 * node_cap));
+  CK(S.alloc(&chunk_node, chunk_cap));
+  CK(S.alloc(&chunk_cnt, 4 * chunk_cap));
+  CK(S.alloc(&chunk_prefix, 4 * chunk_cap));
+  CK(S.alloc(&big_list, big_cap));
+  CK(cudaMemsetAsync(lcs, 0, sizeof(LevelCounters) * level_cap, st));
+  const uint32_t lvl0[2] = {0, G};
+  CK(cudaMemcpyAsync(lvl, lvl0, sizeof(lvl0), cudaMemcpyHostToDevice, st));
+  std::vector<uint32_t> h_lvl((size_t)level_cap + 2);
+  uint32_t queued = 0, levels = 0;
+  bool closed = false;
+  // first batch: about the depth of a balanced tree, then a few levels at a time
+  uint32_t batch = 2;
+  for (uint64_t m = std::max<uint32_t>(bin_size, 1); m < N; m *= 2) batch++;
+  while (!closed) {
+    const uint32_t stop = std::min(queued + batch, level_cap);
+    batch = 4;
+    for (; queued < stop; queued++) {
+      const uint32_t L = queued;
+      level_prepare_kernel<<<persistent, kBlock, 0, st>>>(lvl, L, bin_size, max_depth, pool, acc_cnt, acc_box,
+                                                          chunk_node, lcs);
+      level_box_kernel<<<persistent, kBlock, 0, st>>>(lcs, L, pool, chunk_node, order, pbox);
+      level_stats_kernel<<<persistent, kBlock, 0, st>>>(lvl, L, N, lcs, pool, chunk_node, order, pbox, cen,
+                                                        chunk_cnt, acc_cnt, acc_box);
+      level_decide_kernel<<<persistent, kBlock, 0, st>>>(lvl, L, pool, acc_cnt, acc_box,
+                                                         reinterpret_cast<const uint4*>(chunk_cnt),
+                                                         reinterpret_cast<uint4*>(chunk_prefix), lcs, bc, big_list,
+                                                         big_cap);
+      level_big_prefix_kernel<<<persistent, kBlock, 0, st>>>(lcs, L, pool, big_list, big_cap,
+                                                             reinterpret_cast<const uint4*>(chunk_cnt),
+                                                             reinterpret_cast<uint4*>(chunk_prefix));
+      level_select_kernel<<<persistent, kBlock, 0, st>>>(lvl, L, N, pool, cen, order);
+      level_scatter_kernel<<<persistent, kBlock, 0, st>>>(lvl, L, N, lcs, pool, chunk_node, order, cen, acc_cnt,
+                                                          chunk_prefix, scratch);
+      level_copyback_kernel<<<persistent, kBlock, 0, st>>>(lvl, L, lcs, pool, chunk_node, scratch, order);
     }
-    if (W > acc_cap) {
-      if (acc_cnt) {
-        CK(cudaStreamSynchronize(st));
-        S.release(acc_cnt);
-        S.release(acc_box);
-      }
-      acc_cap = std::max((size_t)W, acc_cap * 2);
-      CK(S.alloc(&acc_cnt, 4 * acc_cap));
-      CK(S.alloc(&acc_box, 24 * acc_cap));
-    }
-    const size_t need_chunks = N / kChunk + (size_t)W + 1;
-    if (need_chunks > chunk_cap) {
-      if (chunk_node) {
-        CK(cudaStreamSynchronize(st));
-        S.release(chunk_node);
-        S.release(chunk_cnt);
-        S.release(chunk_prefix);
-      }
-      chunk_cap = std::max(need_chunks, chunk_cap * 2);
-      CK(S.alloc(&chunk_node, chunk_cap));
-      CK(S.alloc(&chunk_cnt, 4 * chunk_cap));
-      CK(S.alloc(&chunk_prefix, 4 * chunk_cap));
-    }
-    CK(cudaMemsetAsync(lc, 0, sizeof(LevelCounters), st));
-    level_prepare_kernel<<<blocks_for(W), kBlock, 0, st>>>(lb, W, bin_size, max_depth, pool, acc_cnt, acc_box,
-                                                           chunk_node, lc);
-    level_box_kernel<<<persistent, kBlock, 0, st>>>(lc, pool, chunk_node, order, pbox);
-    level_stats_kernel<<<persistent, kBlock, 0, st>>>(lb, N, lc, pool, chunk_node, order, pbox, cen, chunk_cnt,
-                                                      acc_cnt, acc_box);
-    level_decide_kernel<<<blocks_for(W, kWarps), kBlock, 0, st>>>(lb, W, le, pool, acc_cnt, acc_box, chunk_cnt,
-                                                                  chunk_prefix, lc, bc);
-    level_select_kernel<<<blocks_for(W), kBlock, 0, st>>>(lb, W, N, pool, cen, order);
-    level_scatter_kernel<<<persistent, kBlock, 0, st>>>(lb, N, lc, pool, chunk_node, order, cen, acc_cnt,
-                                                        chunk_prefix, scratch);
-    level_copyback_kernel<<<persistent, kBlock, 0, st>>>(lc, pool, chunk_node, scratch, order);
     CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(h_children, &lc->children, 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(h_lvl.data(), lvl, 4 * ((size_t)queued + 2), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    lb = le;
-    le = le + *h_children;
-    level_begin.push_back(lb);
+    for (uint32_t k = 0; k <= queued && !closed; k++)
+      if (h_lvl[k + 1] == h_lvl[k]) {  // level k is empty: the tree has k levels
+        levels = k;
+        closed = true;
+      }
+    if (!closed && queued >= level_cap) return "device build: tree deeper than its level bound";
   }
-  const uint32_t T = le;
+  std::vector<uint32_t> level_begin(h_lvl.begin(), h_lvl.begin() + levels + 1);
+  const uint32_t T = h_lvl[levels];
   level_begin.push_back(T);  // level l = [level_begin[l], level_begin[l+1]); the last entry repeats T
   const uint32_t L = (uint32_t)level_begin.size() - 2;  // number of levels (0 when G == 0)
   out.max_depth = L ? L - 1 : 0;
@@ -1001,19 +1128,16 @@ std::string build_blas_device(const std::vector<DeviceGeometry>& geoms, uint32_t
   // four-child layout, one collapse level per round
   out.root_code.resize(G);
   out.root_code4.resize(G);
-  if (G) {
-    CK(cudaMemcpyAsync(out.root_code.data(), root_code, 4 * (size_t)G, cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-  }
   CK(alloc_out(d.wide4_nodes, inner_total, bytes, st));
   uint32_t *src4, *nin4, *off4;
   CK(S.alloc(&src4, inner_total));
   CK(S.alloc(&nin4, inner_total));
   CK(S.alloc(&off4, inner_total));
   std::vector<uint32_t> first;
+  std::vector<char> leaf_root(G, 0);  // their four-child code is the two-child one, read back at the end
   for (uint32_t g = 0; g < G; g++) {
     if (roots[g].left == NONE && out.tree_nodes[g] == 1) {
-      out.root_code4[g] = out.root_code[g];
+      leaf_root[g] = 1;
     } else {
       out.root_code4[g] = (uint32_t)first.size();
       first.push_back(g);
@@ -1044,8 +1168,11 @@ std::string build_blas_device(const std::vector<DeviceGeometry>& geoms, uint32_t
   CK(cudaEventRecord(ev1, st));
 
   BuildCounters hbc;
+  if (G) CK(cudaMemcpyAsync(out.root_code.data(), root_code, 4 * (size_t)G, cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(&hbc, bc, sizeof(hbc), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
+  for (uint32_t g = 0; g < G; g++)
+    if (leaf_root[g]) out.root_code4[g] = out.root_code[g];
   float ms = 0.0f;
   CK(cudaEventElapsedTime(&ms, ev0, ev1));
   out.kernel_seconds = ms / 1000.0;

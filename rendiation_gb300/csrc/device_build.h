@@ -35,8 +35,9 @@ struct DeviceBlasOut {
 // geometry order exactly as the host build concatenates them. Returns "" or
 // the error ("CUDA ..." for a failed CUDA call, "CUDA OOM ..." when device
 // memory ran out); on error the arrays already written stay in `d` for the
-// caller to free.
+// caller to free. Scratch memory comes from `pool` (stream-ordered; nullptr =
+// the device's default pool) and goes back to it when the build returns.
 std::string build_blas_device(const std::vector<DeviceGeometry>& geoms, uint32_t bin_size, uint32_t max_depth,
-                              int sm_count, DeviceBuilt& d, DeviceBlasOut& out);
+                              int sm_count, cudaMemPool_t pool, DeviceBuilt& d, DeviceBlasOut& out);
 
 }  // namespace rdn

@@ -92,10 +92,26 @@ rdn_status do_build(rdn_ctx* c) {
     e = cudaDeviceSynchronize();  // no trace may still read the buffers being replaced
     if (e != cudaSuccess) return cuda_fail(c, e, "synchronize before build");
     free_device(c->dev);
+    if (!c->build_pool) {
+      // the build's scratch (about 200 B per triangle) stays in this pool
+      // between builds, so that a rebuild allocates nothing from the driver
+      cudaMemPoolProps props = {};
+      props.allocType = cudaMemAllocationTypePinned;
+      props.location.type = cudaMemLocationTypeDevice;
+      props.location.id = c->device;
+      e = cudaMemPoolCreate(&c->build_pool, &props);
+      if (e != cudaSuccess) {
+        c->build_pool = nullptr;
+        return cuda_fail(c, e, "cudaMemPoolCreate");
+      }
+      uint64_t keep = ~0ull;
+      e = cudaMemPoolSetAttribute(c->build_pool, cudaMemPoolAttrReleaseThreshold, &keep);
+      if (e != cudaSuccess) return cuda_fail(c, e, "cudaMemPoolSetAttribute");
+    }
   }
   try {
-    err = on_device ? rdn::build_with_device_blas(c->blas, c->tlas, c->binding, c->opts, c->sm_count, *hb, c->dev,
-                                                  &c->device_seconds)
+    err = on_device ? rdn::build_with_device_blas(c->blas, c->tlas, c->binding, c->opts, c->sm_count, c->build_pool,
+                                                  *hb, c->dev, &c->device_seconds)
                     : rdn::build_host(c->blas, c->tlas, c->binding, c->opts, *hb);
   } catch (const std::bad_alloc&) {
     if (on_device) free_device(c->dev);
@@ -264,6 +280,7 @@ rdn_status rdn_destroy(rdn_ctx* c) {
     cudaDeviceSynchronize();
     free_device(c->dev);
     if (c->d_counters) cudaFree(c->d_counters);
+    if (c->build_pool) cudaMemPoolDestroy(c->build_pool);
   }
   delete c;
   return RDN_OK;

@@ -176,7 +176,7 @@ std::string build_host(const std::vector<std::unique_ptr<std::vector<GeometrySou
 std::string build_with_device_blas(const std::vector<std::unique_ptr<std::vector<GeometrySource>>>& blas,
                                    const std::vector<std::unique_ptr<std::vector<InstanceSource>>>& tlas,
                                    const std::vector<uint32_t>& binding, const BuildOptions& opt, int sm_count,
-                                   HostBuilt& out, DeviceBuilt& d, double* device_seconds);
+                                   cudaMemPool_t pool, HostBuilt& out, DeviceBuilt& d, double* device_seconds);
 
 }  // namespace rdn
 
@@ -193,6 +193,7 @@ struct rdn_ctx {
   rdn::DeviceBuilt dev;
   uint32_t* d_counters = nullptr;  // 4 x u64 counters + error words
   uint32_t iteration_limit = 0;     // cap of the dynamic-fetch loops (0 = built-in)
+  cudaMemPool_t build_pool = nullptr;  // stream-ordered scratch of device builds, kept for the next build
   double build_seconds = 0.0, upload_seconds = 0.0, device_seconds = 0.0;
   std::string err;
 };
