@@ -322,8 +322,8 @@ typedef struct rdn_wavefront_desc {
                                 a warp takes new rays whenever k lanes are idle (dynamic fetch) */
   uint32_t local_stack;      /* ordered walks: 1 = traversal stacks in the threads' local memory (L1)
                                 instead of shared memory, for trees whose stack fits 64 entries */
-  uint32_t register_tier;    /* local-stack kernels: 0 = 64 registers per thread, 1 = about 80 (no
-                                spills, fewer resident warps), 2 = 51 (more warps, more spills) */
+  uint32_t register_tier;    /* local-stack kernels: 0 = 64 registers per thread, 1 = 72 (no spills,
+                                fewer resident warps), 2 = 56 (more warps, more spills) */
   uint32_t speculation;      /* ordered walks: a lane holding a leaf keeps descending while more than
                                 this many lanes of its warp still look for one (0 = until all have one) */
 } rdn_wavefront_desc;

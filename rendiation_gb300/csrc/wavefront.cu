@@ -40,9 +40,9 @@ using namespace dev;
 // instead of shared memory, so that the stack no longer limits occupancy.
 // TIER picks the register budget through the launch bounds: 0 = the
 // compiler's default for 128-thread blocks (64 registers, some spills),
-// 1 = at least 4 blocks of 128 per SM (about 80 registers, no spills, fewer
-// warps), 2 = at least 10 blocks (51 registers, more warps, more spills).
-constexpr int min_blocks(int tier) { return tier == 1 ? 4 : (tier == 2 ? 10 : 0); }
+// 1 = at least 7 blocks of 128 per SM (72 registers, no spills, 28 warps),
+// 2 = at least 9 blocks (56 registers, 36 warps, more spills).
+constexpr int min_blocks(int tier) { return tier == 1 ? 7 : (tier == 2 ? 9 : 0); }
 
 template <int MODE, bool LOCAL, int TIER>
 __global__ void __launch_bounds__(128, min_blocks(TIER)) primary_kernel(TraceParams p, WavefrontParams w) {
