@@ -10,8 +10,8 @@
 // (scene/rendering/gpu-ray-tracing/src/feature/path_tracing/{ray_gen.rs,ray_hit.rs})
 // is two kernels:
 //
-//   primary_kernel: one thread per pixel, warps mapped to 8x4 pixel tiles.
-//     Pinhole ray -> closest hit -> geometric normal facing the ray ->
+//   primary_kernel: one thread per pixel, persistent warps that claim 8x4
+//     pixel tiles from a counter. Pinhole ray -> closest hit -> geometric normal facing the ray ->
 //     offset_ray_hit origin -> one shadow ray to the point light and one
 //     cosine-weighted bounce ray, appended to two queues that share one
 //     counter: a warp ballot and one atomicAdd per warp reserve the slots, so
@@ -25,6 +25,7 @@
 // order as the oracle, so secondary rays are bit-identical.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 
 #include "shade.cuh"
@@ -50,76 +51,84 @@ __global__ void __launch_bounds__(128, min_blocks(TIER)) primary_kernel(TracePar
   uint2 local_stack[LOCAL ? kLocalStackEntries : 1];
   uint2* const stack = LOCAL ? local_stack : smem_stack + threadIdx.x;
   const uint32_t stride = LOCAL ? 1u : blockDim.x;
-  const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t warp = gtid >> 5, lane = gtid & 31u;
+  const uint32_t lane = threadIdx.x & 31u;
   const uint32_t tiles_x = (w.width + 7u) / 8u;
-  const uint32_t px = (warp % tiles_x) * 8u + (lane & 7u);
-  const uint32_t py = (warp / tiles_x) * 4u + (lane >> 3);
-  const bool valid = px < w.width && py < w.height;
+  const uint32_t tiles = tiles_x * ((w.height + 3u) / 4u);
+  // persistent: each warp claims 8x4 pixel tiles from a counter until none is
+  // left, so that a warp that finishes early does not wait for its block
+  for (;;) {
+    uint32_t tile = 0;
+    if (lane == 0) tile = atomicAdd(w.tile_counter, 1u);
+    tile = __shfl_sync(0xffffffffu, tile, 0);
+    if (tile >= tiles) break;
+    const uint32_t px = (tile % tiles_x) * 8u + (lane & 7u);
+    const uint32_t py = (tile / tiles_x) * 4u + (lane >> 3);
+    const bool valid = px < w.width && py < w.height;
 
-  bool want = false;
-  float3 org = make_float3(0.f, 0.f, 0.f), ldir = org, bdir = org;
-  float dist = 0.0f;
-  if (valid) {
-    // camera ray (pixel centre), the same f32 steps as the host generator
-    const float sx = (((float)px + 0.5f) / (float)w.width * 2.0f - 1.0f) * w.tan_half * w.aspect;
-    const float sy = (1.0f - ((float)py + 0.5f) / (float)w.height * 2.0f) * w.tan_half;
-    const float3 d = normalize3(make_float3((w.forward.x + sx * w.right.x) + sy * w.up.x,
-                                            (w.forward.y + sx * w.right.y) + sy * w.up.y,
-                                            (w.forward.z + sx * w.right.z) + sy * w.up.z));
-    RayCtx R;
-    R.o = w.origin;
-    R.d = d;
-    R.tmin = 0.0f;
-    R.tmax = __int_as_float(0x7f800000);
-    R.cull_mask = 0xFFu;
-    R.ray_flags = 0u;
-    bool bad;
-    traverse_ray<MODE, false>(p, R, w.tlas, stack, stride, bad);
-    PixelResult out;
-    out.primary_prim = INVALID_NEXT;
-    out.primary_t = R.tmax;
-    out.bounce_prim = INVALID_NEXT;
-    out.bounce_t = F32_MAX;
-    out.primary_flags = 0u;
-    out.light = 0u;
-    out.direct = 0.0f;
-    out.primary_instance = INVALID_NEXT;
-    if (R.best.have) {
-      const uint4 gm = __ldg(reinterpret_cast<const uint4*>(p.tri_root + R.best.geom_slot));
-      out.primary_prim = __ldg(p.redirect + R.best.k) - gm.z;
-      out.primary_t = R.best.t;
-      out.primary_flags = 1u;
-      out.primary_instance = R.best.inst;
-      // hit point and world geometric normal facing the incoming ray
-      const float3 hp = R.o + d * R.best.t;
-      const float3 nf = facing_normal(p, R.best.k, R.best.inst, d);
-      org = offset_ray_hit(hp, nf);
-      const float3 L = w.light - org;
-      const float dist2 = dot3(L, L);
-      dist = sqrtf(dist2);
-      ldir = normalize3(L);
-      out.direct = fmaxf(0.0f, dot3(nf, ldir)) / dist2;  // kept only if the light is visible
-      uint32_t state = xxhash32(px, py, w.sample_index * 3u);
-      const float s0 = sample_next(state);
-      const float s1 = sample_next(state);
-      bdir = cosine_sample_in_dir(nf, s0, s1);
-      want = true;
+    bool want = false;
+    float3 org = make_float3(0.f, 0.f, 0.f), ldir = org, bdir = org;
+    float dist = 0.0f;
+    if (valid) {
+      // camera ray (pixel centre), the same f32 steps as the host generator
+      const float sx = (((float)px + 0.5f) / (float)w.width * 2.0f - 1.0f) * w.tan_half * w.aspect;
+      const float sy = (1.0f - ((float)py + 0.5f) / (float)w.height * 2.0f) * w.tan_half;
+      const float3 d = normalize3(make_float3((w.forward.x + sx * w.right.x) + sy * w.up.x,
+                                              (w.forward.y + sx * w.right.y) + sy * w.up.y,
+                                              (w.forward.z + sx * w.right.z) + sy * w.up.z));
+      RayCtx R;
+      R.o = w.origin;
+      R.d = d;
+      R.tmin = 0.0f;
+      R.tmax = __int_as_float(0x7f800000);
+      R.cull_mask = 0xFFu;
+      R.ray_flags = 0u;
+      bool bad;
+      traverse_ray<MODE, false>(p, R, w.tlas, stack, stride, bad);
+      PixelResult out;
+      out.primary_prim = INVALID_NEXT;
+      out.primary_t = R.tmax;
+      out.bounce_prim = INVALID_NEXT;
+      out.bounce_t = F32_MAX;
+      out.primary_flags = 0u;
+      out.light = 0u;
+      out.direct = 0.0f;
+      out.primary_instance = INVALID_NEXT;
+      if (R.best.have) {
+        const uint4 gm = __ldg(reinterpret_cast<const uint4*>(p.tri_root + R.best.geom_slot));
+        out.primary_prim = __ldg(p.redirect + R.best.k) - gm.z;
+        out.primary_t = R.best.t;
+        out.primary_flags = 1u;
+        out.primary_instance = R.best.inst;
+        // hit point and world geometric normal facing the incoming ray
+        const float3 hp = R.o + d * R.best.t;
+        const float3 nf = facing_normal(p, R.best.k, R.best.inst, d);
+        org = offset_ray_hit(hp, nf);
+        const float3 L = w.light - org;
+        const float dist2 = dot3(L, L);
+        dist = sqrtf(dist2);
+        ldir = normalize3(L);
+        out.direct = fmaxf(0.0f, dot3(nf, ldir)) / dist2;  // kept only if the light is visible
+        uint32_t state = xxhash32(px, py, w.sample_index * 3u);
+        const float s0 = sample_next(state);
+        const float s1 = sample_next(state);
+        bdir = cosine_sample_in_dir(nf, s0, s1);
+        want = true;
+      }
+      w.out[(size_t)py * w.width + px] = out;
     }
-    w.out[(size_t)py * w.width + px] = out;
-  }
-  // compacted append of both secondary rays (one counter for the pair)
-  const uint32_t slot = warp_append(w.queue_count, want);
-  if (want) {
-    const uint32_t pix = py * w.width + px;
-    float4* sq = reinterpret_cast<float4*>(w.shadow_rays) + 2 * (size_t)slot;
-    sq[0] = make_float4(org.x, org.y, org.z, F32_EPSILON);
-    sq[1] = make_float4(ldir.x, ldir.y, ldir.z, dist);
-    float4* bq = reinterpret_cast<float4*>(w.bounce_rays) + 2 * (size_t)slot;
-    bq[0] = make_float4(org.x, org.y, org.z, F32_EPSILON);
-    bq[1] = make_float4(bdir.x, bdir.y, bdir.z, F32_MAX);
-    w.shadow_pixel[slot] = pix;
-    w.bounce_pixel[slot] = pix;
+    // compacted append of both secondary rays (one counter for the pair)
+    const uint32_t slot = warp_append(w.queue_count, want);
+    if (want) {
+      const uint32_t pix = py * w.width + px;
+      float4* sq = reinterpret_cast<float4*>(w.shadow_rays) + 2 * (size_t)slot;
+      sq[0] = make_float4(org.x, org.y, org.z, F32_EPSILON);
+      sq[1] = make_float4(ldir.x, ldir.y, ldir.z, dist);
+      float4* bq = reinterpret_cast<float4*>(w.bounce_rays) + 2 * (size_t)slot;
+      bq[0] = make_float4(org.x, org.y, org.z, F32_EPSILON);
+      bq[1] = make_float4(bdir.x, bdir.y, bdir.z, F32_MAX);
+      w.shadow_pixel[slot] = pix;
+      w.bounce_pixel[slot] = pix;
+    }
   }
 }
 
@@ -264,6 +273,7 @@ void wavefront_bind_scratch(WavefrontParams& w, void* scratch) {
   auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
   char* s = static_cast<char*>(scratch);
   w.queue_count = reinterpret_cast<uint32_t*>(s);
+  w.tile_counter = reinterpret_cast<uint32_t*>(s + 16);
   w.work_counter = reinterpret_cast<uint32_t*>(s + 64);
   size_t off = 256;
   w.shadow_rays = s + off;
@@ -297,10 +307,15 @@ cudaError_t launch_wavefront_mode(const TraceParams& p, const WavefrontParams& w
   if (phases & 1u) {
     e = cudaMemsetAsync(w.queue_count, 0, 64, stream);
     if (e != cudaSuccess) return e;
-    // primary grid: whole 8x4 tiles, one warp each
-    const uint32_t tiles = ((w.width + 7) / 8) * ((w.height + 3) / 4);
-    const uint32_t threads = tiles * 32;
-    const uint32_t grid1 = (threads + block - 1) / block;
+    // persistent primary grid: as many resident blocks as fill every SM, or
+    // fewer when the frame has fewer 8x4 tiles than resident warps
+    int per_sm1 = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm1, primary_kernel<MODE, LOCAL, TIER>, (int)block, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm1 < 1) per_sm1 = 1;
+    const uint64_t tiles = (uint64_t)((w.width + 7) / 8) * ((w.height + 3) / 4);
+    const uint64_t need = (tiles * 32 + block - 1) / block;
+    const uint32_t grid1 = (uint32_t)std::min<uint64_t>((uint64_t)sm_count * per_sm1, need);
     primary_kernel<MODE, LOCAL, TIER><<<grid1, block, smem, stream>>>(p, w);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;

@@ -29,6 +29,7 @@ struct WavefrontParams {
   uint32_t* ray_counts;  // nullable: [primary, shadow, bounce]
   // scratch (wavefront_bind_scratch)
   uint32_t* queue_count;
+  uint32_t* tile_counter;  // primary tiles claimed (inside the 64 B the launch zeroes at queue_count)
   uint32_t* work_counter;
   void* shadow_rays;
   void* bounce_rays;
@@ -40,7 +41,7 @@ struct WavefrontParams {
   // 1: traversal stacks in local memory (ordered walks, trees up to the
   // local stack's depth); 0: in shared memory
   uint32_t local_stack;
-  // register budget of the local-stack kernels: 0 default (64), 1 about 80, 2 51
+  // register budget of the local-stack kernels: 0 default (64), 1 = 72, 2 = 56
   uint32_t register_tier;
 };
 
