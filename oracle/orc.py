@@ -65,6 +65,7 @@ def lib():
         L.orc_get_buffer.restype = C.c_size_t
         L.orc_get_buffer.argtypes = [vp, i32, vp, C.c_size_t]
         L.orc_trace.argtypes = [vp, vp, u32, vp, u32, u32, u32, u32, vp, vp, vp, vp, i32, C.POINTER(C.c_double)]
+        L.orc_nan_exposure.argtypes = [vp, vp, u32, vp, u32, u32, u32, vp, i32]
         L.orc_eval_fp64.argtypes = [vp, vp, u32, vp, vp]
         L.orc_bruteforce_fp64.argtypes = [vp, vp, u32, u32, vp, i32]
         L.orc_intersect_triangle.argtypes = [vp, vp, C.c_float, C.c_float, vp, vp, vp, i32, i32, vp]
@@ -180,6 +181,17 @@ class OracleSystem:
         if counts:
             return out, totals, rc
         return out, totals
+
+    def nan_exposure(self, rays: np.ndarray, tlas_idx=None, tlas_uniform=0, ray_flags=0, cull_mask=0xFF,
+                     threads=4) -> np.ndarray:
+        """Per ray: True when some triangle its boxes admit (far held at tmax) gives a NaN
+        distance, so that the result depends on the order of the walk."""
+        rays = np.ascontiguousarray(rays)
+        out = np.zeros(rays.shape[0], np.uint8)
+        ti = None if tlas_idx is None else np.ascontiguousarray(tlas_idx, np.uint32)
+        self._check(self._L.orc_nan_exposure(self._h, _ptr(rays), rays.shape[0], _ptr(ti), tlas_uniform, ray_flags,
+                                             cull_mask, _ptr(out), threads))
+        return out.astype(bool)
 
     def eval_fp64(self, rays: np.ndarray, hits: np.ndarray) -> np.ndarray:
         out = np.zeros((rays.shape[0], 3), np.float64)

@@ -714,6 +714,67 @@ done:
   }
 }
 
+// Test infrastructure: does the ray meet a NaN distance anywhere its boxes let
+// it reach? The same walk as traverse() with the far held at the ray's tmax
+// (every node any walk order could visit) and nothing committed; true when a
+// triangle that passes the culling tests gives t = NaN (a zero-area triangle,
+// or a ray lying in the triangle's plane). Once such a NaN is committed, every
+// later range test of the ray passes, so the reference's own result depends on
+// the order in which it meets the triangles.
+static bool nan_exposure(const Built& B, const RayIn& ray, uint32_t tlas_idx, uint32_t ray_flags,
+                         uint32_t cull_mask) {
+  if (tlas_idx >= B.tlas_binding.size() || B.tlas_binding[tlas_idx] >= B.tlas_bvh_root.size()) return false;
+  Counters cn;
+  uint32_t visits = 0;
+  float far_cell = ray.tmax;
+  RayRange ray_range{ray.tmin, &far_cell, 1.0f};
+  V3 ro = ld3(ray.org), rd = ld3(ray.dir);
+  BvhIter tlas_iter{B.tlas_bvh_forest.data(), ro, rd, ray_range, B.tlas_bvh_root[B.tlas_binding[tlas_idx]]};
+  for (;;) {
+    uint32_t hit_idx = tlas_iter.next(cn, &visits);
+    if (hit_idx == INVALID_NEXT) break;
+    const DeviceBVHNode& node = B.tlas_bvh_forest[hit_idx];
+    for (uint32_t ti = node.content_range[0]; ti < node.content_range[1]; ti++) {
+      const TlasBounding& tb = B.tlas_bounding[ti];
+      if (!intersect_ray_aabb(ro, rd, ray.tmin, ray.tmax, ld3(tb.world_min), ld3(tb.world_max))) continue;
+      if ((cull_mask & tb.mask) == 0) continue;
+      const DeviceInstance& inst = B.tlas_data[ti];
+      uint32_t iflags = merge_geometry_instance_flag(ray_flags, inst.flags);
+      if (iflags & TF_SKIP_TRIANGLES) continue;
+      M4 inv;
+      memcpy(inv.m, inst.transform_inv, 64);
+      V4 o4 = m4_mul_v4(inv, V4{ro.x, ro.y, ro.z, 1.0f});
+      V3 bo = v3(o4.x, o4.y, o4.z) / o4.w;
+      V3 bd = m3_mul_v3(inv, rd);
+      RayRange blas_range{ray_range.near_, &far_cell, length(bd)};
+      bd = normalize(bd);
+      const BlasMetaInfo& bm = B.blas_meta_info[inst.acceleration_structure_handle];
+      for (uint32_t gi = bm.tri_root_range[0]; gi < bm.tri_root_range[1]; gi++) {
+        const GeometryMetaInfo& g = B.tri_bvh_root[gi];
+        bool pass, is_opaque, cull_enable, cull_back;
+        cull_geometry(iflags, g.geometry_flags, &pass, &is_opaque);
+        if (!pass) continue;
+        cull_triangle(iflags, &cull_enable, &cull_back);
+        BvhIter it{B.tri_bvh_forest.data(), bo, bd, blas_range, g.bvh_root_idx};
+        for (;;) {
+          uint32_t leaf = it.next(cn, &visits);
+          if (leaf == INVALID_NEXT) break;
+          const DeviceBVHNode& ln = B.tri_bvh_forest[leaf];
+          for (uint32_t k = ln.content_range[0]; k < ln.content_range[1]; k++) {
+            uint32_t tri_idx = B.indices_redirect[k];
+            uint32_t i0 = B.indices[tri_idx * 3], i1 = B.indices[tri_idx * 3 + 1], i2 = B.indices[tri_idx * 3 + 2];
+            TriResult r = intersect_ray_triangle(bo, bd, blas_range.get_near(), blas_range.get_far(),
+                                                 ld3(&B.vertices[i0 * 3]), ld3(&B.vertices[i1 * 3]),
+                                                 ld3(&B.vertices[i2 * 3]), cull_enable, cull_back);
+            if (r.s != 0.0f && std::isnan(r.t)) return true;
+          }
+        }
+      }
+    }
+  }
+  return false;
+}
+
 // FP64 re-evaluation of a reported hit: the same formula in double on the same
 // (object-space) triangle, to state the FP32 result's error.
 static void eval_fp64(const Built& B, const RayIn& ray, const HitOut& h, double* out3) {
@@ -1085,6 +1146,27 @@ int orc_trace(void* cp, const RayIn* rays, uint32_t n, const uint32_t* tlas_idx,
       totals[5] += x.bad_tlas;
     }
   }
+  return 0;
+}
+
+// out[i] = 1 when ray i can meet a NaN distance (nan_exposure).
+int orc_nan_exposure(void* cp, const RayIn* rays, uint32_t n, const uint32_t* tlas_idx, uint32_t tlas_uniform,
+                     uint32_t ray_flags, uint32_t cull_mask, uint8_t* out, int threads) {
+  Ctx& c = *(Ctx*)cp;
+  if (!c.built) {
+    int rc = build_all(c);
+    if (rc) return rc;
+  }
+  const Built& B = *c.built;
+  if (threads < 1) threads = 1;
+  auto work = [&](int w) {
+    uint32_t s = (uint32_t)((uint64_t)n * w / threads), e = (uint32_t)((uint64_t)n * (w + 1) / threads);
+    for (uint32_t i = s; i < e; i++)
+      out[i] = nan_exposure(B, rays[i], tlas_idx ? tlas_idx[i] : tlas_uniform, ray_flags, cull_mask) ? 1 : 0;
+  };
+  std::vector<std::thread> th;
+  for (int w = 0; w < threads; w++) th.emplace_back(work, w);
+  for (auto& t : th) t.join();
   return 0;
 }
 

@@ -122,6 +122,18 @@ def test_oracle_culling_and_degenerate_pole_triangles(oracle):
             assert nan.sum() > 0 and set(plain["prim"][nan].tolist()) <= degenerate
 
 
+def test_oracle_nan_exposure(oracle):
+    """The oracle's NaN-exposure flag covers every ray whose result is NaN; back-face culling
+    (which rejects b = 0) leaves no ray exposed on the sphere."""
+    rays = nf.camera_rays(*nf.CPU_TEST_RANGE)
+    plain, _ = oracle.trace(rays, tlas_uniform=4, threads=4)
+    exposed = oracle.nan_exposure(rays, tlas_uniform=4)
+    assert exposed[np.isnan(plain["t"])].all()
+    assert exposed.sum() < 0.05 * rays.shape[0]
+    assert not oracle.nan_exposure(rays, tlas_uniform=4, ray_flags=CULL).any()
+    assert not oracle.nan_exposure(rays, tlas_uniform=0).any()  # cubes seen from outside, no in-plane rays
+
+
 def test_oracle_reproduces_golden(golden, oracle):
     assert gc.digests_of_oracle(oracle) == golden["digests"].tolist()
     rays = nf.camera_rays(*nf.CPU_TEST_RANGE)

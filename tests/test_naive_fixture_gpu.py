@@ -93,6 +93,27 @@ def test_unculled_nan_hits_reference_order(fixture, cuda):
     assert np.array_equal(ext[:, 1], expect["instance"])
 
 
+@pytest.mark.parametrize("traversal", ORDERED_MODES)
+def test_unculled_nan_hits_ordered(fixture, traversal, cuda):
+    """Without culling, a NaN distance from a zero-area pole triangle also disables every later
+    range test of the ray (comparisons with NaN are false), so which triangle a ray ends with
+    depends on the order the walk meets them. The ordered walks may therefore differ from the
+    reference on rays that can meet such a triangle (the oracle's nan_exposure); every other ray
+    is identical except ties."""
+    g, sc, S, P = fixture
+    rays = nf.camera_rays(*nf.CPU_TEST_RANGE)
+    expect, _ = S.trace(rays, tlas_uniform=4, threads=8)
+    got, _ = run_product(P, rays, traversal, tlas_uniform=4)
+    nan = S.nan_exposure(rays, tlas_uniform=4)
+    assert nan.sum() >= np.isnan(expect["t"]).sum()
+    same_t = (got["t"] == expect["t"]) | (np.isnan(got["t"]) & np.isnan(expect["t"]))
+    identical = (got["prim"] == expect["prim"]) & same_t
+    tie = ~identical & (got["t"] == expect["t"]) & (got["prim"] != orc.MISS)
+    assert (~identical & ~nan & ~tie).sum() == 0
+    assert np.array_equal(got["prim"] != orc.MISS, expect["prim"] != orc.MISS)
+    assert identical.mean() > 0.98
+
+
 def test_device_build_matches_host_build(fixture, cuda):
     g, sc, S, P = fixture
     D = sc.build_product(device_build=True)
