@@ -1,0 +1,134 @@
+/* A host program that uses the library through its C ABI only (include/rdn.h
+ * plus the CUDA runtime for device buffers), the way a Rust, Go or C++ host
+ * binds it: one triangle geometry, one identity instance, a build, one batch
+ * trace, results written to a file.
+ *
+ *   c_client <input> <output> <traversal> <device_build>
+ *
+ * input:  u32 vertex_count, u32 index_count (0 = non-indexed), u32 ray_count,
+ *         f32 positions[3 * vertex_count], u32 indices[index_count],
+ *         f32 rays[8 * ray_count] (org, tmin, dir, tmax)
+ * output: rdn_hit[ray_count], rdn_hit_ext[ray_count], u32 error_flags
+ *
+ * Exit codes: 0 ok, 1 usage or file error, 2 an rdn_* call failed (its status
+ * and rdn_last_error are printed), 3 a CUDA runtime call failed. */
+#include <cuda_runtime_api.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "rdn.h"
+
+static rdn_ctx* ctx = NULL;
+
+#define CHECK(x)                                                                                 \
+  do {                                                                                           \
+    rdn_status s_ = (x);                                                                         \
+    if (s_ != RDN_OK) {                                                                          \
+      fprintf(stderr, "%s failed: status %d: %s\n", #x, (int)s_, ctx ? rdn_last_error(ctx) : ""); \
+      return 2;                                                                                  \
+    }                                                                                            \
+  } while (0)
+#define CUCHECK(x)                                                      \
+  do {                                                                  \
+    cudaError_t e_ = (x);                                               \
+    if (e_ != cudaSuccess) {                                            \
+      fprintf(stderr, "%s failed: %s\n", #x, cudaGetErrorString(e_));   \
+      return 3;                                                         \
+    }                                                                   \
+  } while (0)
+
+static int read_all(FILE* f, void* dst, size_t bytes) { return bytes == 0 || fread(dst, 1, bytes, f) == bytes; }
+
+int main(int argc, char** argv) {
+  if (argc != 5) {
+    fprintf(stderr, "usage: %s <input> <output> <traversal> <device_build>\n", argv[0]);
+    return 1;
+  }
+  const uint32_t traversal = (uint32_t)atoi(argv[3]);
+  const uint32_t device_build = (uint32_t)atoi(argv[4]);
+  FILE* in = fopen(argv[1], "rb");
+  if (!in) return 1;
+  uint32_t head[3];
+  if (!read_all(in, head, sizeof head)) return 1;
+  const uint32_t nv = head[0], ni = head[1], nr = head[2];
+  float* pos = (float*)malloc(12 * (size_t)nv + 4);
+  uint32_t* idx = (uint32_t*)malloc(4 * (size_t)ni + 4);
+  rdn_ray* rays = (rdn_ray*)malloc(sizeof(rdn_ray) * (size_t)nr + 4);
+  if (!pos || !idx || !rays) return 1;
+  if (!read_all(in, pos, 12 * (size_t)nv) || !read_all(in, idx, 4 * (size_t)ni) ||
+      !read_all(in, rays, sizeof(rdn_ray) * (size_t)nr))
+    return 1;
+  fclose(in);
+  if (rdn_api_version() != RDN_API_VERSION) {
+    fprintf(stderr, "header and library disagree on the API version\n");
+    return 1;
+  }
+
+  CHECK(rdn_create(&ctx, 0));
+  rdn_geometry g;
+  memset(&g, 0, sizeof g);
+  g.type = 0; /* triangles */
+  g.flags = RDN_GEOMETRY_OPAQUE;
+  g.positions = pos;
+  g.vertex_count = nv;
+  g.index_count = ni;
+  g.indices = ni ? idx : NULL;
+  uint32_t blas = 0, tlas = 0;
+  CHECK(rdn_blas_create(ctx, &g, 1, &blas));
+  rdn_instance inst;
+  memset(&inst, 0, sizeof inst);
+  inst.transform[0] = inst.transform[5] = inst.transform[10] = inst.transform[15] = 1.0f;
+  inst.mask = 0xFFu;
+  inst.blas_handle = blas;
+  CHECK(rdn_tlas_create(ctx, &inst, 1, &tlas));
+  CHECK(rdn_bind_tlas(ctx, &tlas, 1));
+  rdn_build_opts opts;
+  memset(&opts, 0, sizeof opts);
+  opts.blas_bin_size = 4;
+  opts.device_build = device_build;
+  CHECK(rdn_build(ctx, &opts));
+
+  rdn_ray* d_rays = NULL;
+  rdn_hit* d_hits = NULL;
+  rdn_hit_ext* d_ext = NULL;
+  CUCHECK(cudaMalloc((void**)&d_rays, sizeof(rdn_ray) * (size_t)nr + 32));
+  CUCHECK(cudaMalloc((void**)&d_hits, sizeof(rdn_hit) * (size_t)nr + 16));
+  CUCHECK(cudaMalloc((void**)&d_ext, sizeof(rdn_hit_ext) * (size_t)nr + 16));
+  CUCHECK(cudaMemcpy(d_rays, rays, sizeof(rdn_ray) * (size_t)nr, cudaMemcpyHostToDevice));
+  rdn_trace_desc d;
+  memset(&d, 0, sizeof d);
+  d.rays = d_rays;
+  d.hits = d_hits;
+  d.hits_ext = d_ext;
+  d.count = nr;
+  d.cull_mask = 0xFFu;
+  d.traversal = traversal;
+  CHECK(rdn_trace(ctx, &d, NULL));
+  uint32_t flags = 0;
+  CHECK(rdn_check_errors(ctx, NULL, &flags));
+
+  rdn_hit* hits = (rdn_hit*)malloc(sizeof(rdn_hit) * (size_t)nr + 16);
+  rdn_hit_ext* ext = (rdn_hit_ext*)malloc(sizeof(rdn_hit_ext) * (size_t)nr + 16);
+  if (!hits || !ext) return 1;
+  CUCHECK(cudaMemcpy(hits, d_hits, sizeof(rdn_hit) * (size_t)nr, cudaMemcpyDeviceToHost));
+  CUCHECK(cudaMemcpy(ext, d_ext, sizeof(rdn_hit_ext) * (size_t)nr, cudaMemcpyDeviceToHost));
+  FILE* out = fopen(argv[2], "wb");
+  if (!out) return 1;
+  fwrite(hits, sizeof(rdn_hit), nr, out);
+  fwrite(ext, sizeof(rdn_hit_ext), nr, out);
+  fwrite(&flags, 4, 1, out);
+  fclose(out);
+
+  cudaFree(d_rays);
+  cudaFree(d_hits);
+  cudaFree(d_ext);
+  CHECK(rdn_destroy(ctx));
+  ctx = NULL;
+  free(pos);
+  free(idx);
+  free(rays);
+  free(hits);
+  free(ext);
+  return 0;
+}
