@@ -291,6 +291,35 @@ uint32_t emit_wide(const Tree& t, uint32_t prim_offset, HostBuilt& hb, std::vect
   return nn ? code[0] : (LEAF_BIT | 0);
 }
 
+// True when box s is flat on some axis and lies on a face plane of box a,
+// which is not flat there. The four-child walk tests a node's slots but not
+// the two-child nodes it opened to reach them, which is exact only while the
+// slab test is monotone (a box inside another never passes when the outer one
+// fails). A ray with a zero direction component breaks that exactly here: with
+// its origin in that plane it fails a's slab test (0 * inf = NaN beside
+// +-inf) but passes the flat box's (NaN on both planes, dropped by fmin/fmax).
+// The collapse therefore never opens a node whose children are flat on its
+// faces or on the faces of the nodes opened above it.
+bool flat_on_boundary(const Box& s, const Box& a) {
+  const float sl[3] = {s.lo.x, s.lo.y, s.lo.z}, sh[3] = {s.hi.x, s.hi.y, s.hi.z};
+  const float al[3] = {a.lo.x, a.lo.y, a.lo.z}, ah[3] = {a.hi.x, a.hi.y, a.hi.z};
+  for (int k = 0; k < 3; k++)
+    if (sl[k] == sh[k] && al[k] != ah[k] && (al[k] == sl[k] || ah[k] == sl[k])) return true;
+  return false;
+}
+
+// Whether binary node x (opened ancestors anc, EMPTY_SLOT when absent) may be
+// opened in a four-child node: no child of x is flat on a face of x or of anc.
+bool openable(const Tree& t, uint32_t x, const uint32_t anc[2]) {
+  const uint32_t kids[2] = {x + 1, x + t.nodes[x].left_count + 1};
+  for (uint32_t c : kids) {
+    if (flat_on_boundary(t.nodes[c].box, t.nodes[x].box)) return false;
+    for (int a = 0; a < 2; a++)
+      if (anc[a] != EMPTY_SLOT && flat_on_boundary(t.nodes[c].box, t.nodes[anc[a]].box)) return false;
+  }
+  return true;
+}
+
 float node_area(const Box& b) {
   const float w = b.hi.x - b.lo.x, h = b.hi.y - b.lo.y, d = b.hi.z - b.lo.z;
   return w * h + w * d + h * d;
@@ -301,15 +330,17 @@ float node_area(const Box& b) {
 uint32_t emit_wide4(const Tree& t, uint32_t bi, const std::vector<uint32_t>& code2, HostBuilt& hb, uint32_t level,
                     uint32_t* depth) {
   uint32_t slot[4];
+  uint32_t anc[4][2];  // per slot, the binary nodes opened above it in this node (never tested by the walk)
   int n = 0;
   slot[n++] = bi + 1;
   slot[n++] = bi + t.nodes[bi].left_count + 1;
+  for (auto& a : anc) a[0] = a[1] = EMPTY_SLOT;
   while (n < 4) {
     int best = -1;
     float best_area = -1.0f;
     for (int k = 0; k < n; k++) {
       const TreeNode& c = t.nodes[slot[k]];
-      if (!c.left_count) continue;
+      if (!c.left_count || !openable(t, slot[k], anc[k])) continue;
       const float a = node_area(c.box);
       if (best < 0 || a > best_area) {
         best = k;
@@ -318,9 +349,18 @@ uint32_t emit_wide4(const Tree& t, uint32_t bi, const std::vector<uint32_t>& cod
     }
     if (best < 0) break;
     const uint32_t open = slot[best];
-    for (int k = n; k > best + 1; k--) slot[k] = slot[k - 1];
+    const uint32_t up[2] = {open, anc[best][0]};
+    for (int k = n; k > best + 1; k--) {
+      slot[k] = slot[k - 1];
+      anc[k][0] = anc[k - 1][0];
+      anc[k][1] = anc[k - 1][1];
+    }
     slot[best] = open + 1;
     slot[best + 1] = open + t.nodes[open].left_count + 1;
+    for (int k = best; k <= best + 1; k++) {
+      anc[k][0] = up[0];
+      anc[k][1] = up[1];
+    }
     n++;
   }
   const uint32_t me = (uint32_t)hb.wide4_nodes.size();

@@ -755,17 +755,44 @@ __global__ void emit_primitives_kernel(uint32_t N, const uint32_t* __restrict__ 
   }
 }
 
+// True when box s is flat on some axis and lies on a face plane of box a,
+// which is not flat there (the host build's flat_on_boundary: a ray with a
+// zero direction component and its origin in that plane fails a's slab test
+// but passes s's, so the four-child walk, which skips the boxes of opened
+// nodes, must not open a node above such a child).
+__device__ __forceinline__ bool flat_on_boundary(const NodeBox& s, const NodeBox& a) {
+  const float sl[3] = {s.lo.x, s.lo.y, s.lo.z}, sh[3] = {s.hi.x, s.hi.y, s.hi.z};
+  const float al[3] = {a.lo.x, a.lo.y, a.lo.z}, ah[3] = {a.hi.x, a.hi.y, a.hi.z};
+  for (int k = 0; k < 3; k++)
+    if (sl[k] == sh[k] && al[k] != ah[k] && (al[k] == sl[k] || ah[k] == sl[k])) return true;
+  return false;
+}
+
+__device__ __forceinline__ bool openable(uint32_t x, const uint32_t anc[2], const BNode* pool) {
+  const NodeBox bx = box_of(pool[x]);
+  for (uint32_t c = pool[x].left; c <= pool[x].left + 1; c++) {
+    const NodeBox bc = box_of(pool[c]);
+    if (flat_on_boundary(bc, bx)) return false;
+    for (int a = 0; a < 2; a++)
+      if (anc[a] != NONE && flat_on_boundary(bc, box_of(pool[anc[a]]))) return false;
+  }
+  return true;
+}
+
 // Four-child collapse of binary inner node b: open the inner slot with the
-// largest surface area (first of equals) until 4 slots are used.
+// largest surface area (first of equals) until 4 slots are used, skipping
+// nodes that openable() refuses (the host build's emit_wide4).
 __device__ __forceinline__ int collapse_slots(uint32_t b, const BNode* pool, uint32_t slot[4]) {
+  uint32_t anc[4][2];
   int n = 0;
   slot[n++] = pool[b].left;
   slot[n++] = pool[b].left + 1;
+  for (int k = 0; k < 4; k++) anc[k][0] = anc[k][1] = NONE;
   while (n < 4) {
     int best = -1;
     float best_area = -1.0f;
     for (int k = 0; k < n; k++) {
-      if (pool[slot[k]].left == NONE) continue;
+      if (pool[slot[k]].left == NONE || !openable(slot[k], anc[k], pool)) continue;
       const float a = half_area(box_of(pool[slot[k]]));
       if (best < 0 || a > best_area) {
         best = k;
@@ -774,9 +801,18 @@ __device__ __forceinline__ int collapse_slots(uint32_t b, const BNode* pool, uin
     }
     if (best < 0) break;
     const uint32_t open = slot[best];
-    for (int k = n; k > best + 1; k--) slot[k] = slot[k - 1];
+    const uint32_t up0 = open, up1 = anc[best][0];
+    for (int k = n; k > best + 1; k--) {
+      slot[k] = slot[k - 1];
+      anc[k][0] = anc[k - 1][0];
+      anc[k][1] = anc[k - 1][1];
+    }
     slot[best] = pool[open].left;
     slot[best + 1] = pool[open].left + 1;
+    for (int k = best; k <= best + 1; k++) {
+      anc[k][0] = up0;
+      anc[k][1] = up1;
+    }
     n++;
   }
   return n;

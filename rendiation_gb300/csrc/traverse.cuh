@@ -397,17 +397,6 @@ __device__ __forceinline__ bool blas_speculative(const TraceParams& p, RayCtx& R
   return false;
 }
 
-// The four-child layout skips the boxes of the two-child nodes it collapses.
-// That is exact only while the slab test is monotone (a box inside another
-// never passes when the outer one fails). A direction component of 0 (or one
-// whose reciprocal overflows) breaks it: 0 * inf = NaN when the origin lies on
-// a box plane, and fmin/fmax drop the NaN, so a flat inner box can pass where
-// its parent failed. Such rays take the two-child walk, which tests every box
-// the reference tests.
-__device__ __forceinline__ bool axis_parallel(const InstanceRay& ir) {
-  return isinf(ir.inv_d.x) || isinf(ir.inv_d.y) || isinf(ir.inv_d.z);
-}
-
 // Full query of one ray (traverse_cpu.rs:52-245). R must hold the ray; on
 // return R.best holds the committed hit. `bad` reports an unbound TLAS index.
 template <int MODE, bool COUNT>
@@ -458,10 +447,7 @@ __device__ __forceinline__ void traverse_ray(const TraceParams& p, RayCtx& R, ui
         geometry_cull(ir.flags, gm.w, pass, is_opaque, cull_enable, cull_back);
         if (!pass) continue;
         bool end;
-        if (MODE == MODE_WIDE4 && axis_parallel(ir))
-          end = blas_speculative<COUNT, 2>(p, R, ir, gm.x, g, ti, is_opaque, cull_enable, cull_back, gm.z, stack,
-                                           stride, p.stack_depth);
-        else if (MODE == MODE_WIDE4)
+        if (MODE == MODE_WIDE4)
           end = blas_speculative<COUNT, 4>(p, R, ir, gm.x, g, ti, is_opaque, cull_enable, cull_back, gm.z, stack,
                                            stride, p.stack_depth);
         else if (MODE == MODE_BINARY)
@@ -494,7 +480,6 @@ struct LaneWalk {
   InstanceRay ir;
   uint32_t phase, tcur, ti, ti_end, inst_slot, g, g_end, gslot, prim_start;
   bool is_opaque, cull_enable, cull_back;
-  bool narrow;  // four-child walk: this instance's ray takes the two-child nodes (axis_parallel)
   uint32_t code, leaf, sp;
   float code_tn;
 
@@ -509,7 +494,6 @@ struct LaneWalk {
     ti = ti_end = inst_slot = g = g_end = gslot = prim_start = 0;
     is_opaque = true;
     cull_enable = cull_back = false;
-    narrow = false;
     code = leaf = EMPTY_SLOT;
     sp = 0;
     code_tn = 0.0f;
@@ -592,8 +576,7 @@ struct LaneWalk {
           float tn;
           if (!slab(ir.o, ir.inv_d, R.tmin * ir.scaling, R.far_world * ir.scaling, a.x, a.y, a.z, b.x, b.y, b.z, tn))
             continue;
-          narrow = WIDTH == 4 && axis_parallel(ir);
-          code = __ldg((WIDTH == 2 || narrow ? p.geom_root_code : p.geom_root_code4) + cur);
+          code = __ldg((WIDTH == 2 ? p.geom_root_code : p.geom_root_code4) + cur);
           code_tn = -inf;
           leaf = EMPTY_SLOT;
           sp = 0;
@@ -626,9 +609,7 @@ struct LaneWalk {
         return;
       }
       while (code != EMPTY_SLOT && !(code & LEAF_BIT)) {
-        code = WIDTH == 4 && narrow
-                   ? interior_step<false, 2>(p, R, ir, code, code_tn, stack, stride, sp, p.stack_depth)
-                   : interior_step<false, WIDTH>(p, R, ir, code, code_tn, stack, stride, sp, p.stack_depth);
+        code = interior_step<false, WIDTH>(p, R, ir, code, code_tn, stack, stride, sp, p.stack_depth);
         if (code != EMPTY_SLOT && (code & LEAF_BIT) && leaf == EMPTY_SLOT) {
           leaf = code;
           code = pop_live(stack, stride, sp, R.far_world * ir.scaling, code_tn);
