@@ -818,27 +818,44 @@ __device__ __forceinline__ int collapse_slots(uint32_t b, const BNode* pool, uin
   return n;
 }
 
-__global__ void wide4_count_kernel(uint32_t a, uint32_t W, const uint32_t* __restrict__ src, const BNode* __restrict__ pool,
-                                   uint32_t* __restrict__ inner_slots) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= W) return;
-  uint32_t slot[4];
-  const int n = collapse_slots(src[a + i], pool, slot);
-  uint32_t k = 0;
-  for (int s = 0; s < n; s++) k += pool[slot[s]].left != NONE;
-  inner_slots[i] = k;
+// Four-child layout without a host round trip per level: the binary nodes
+// that root a four-child node ("collapse roots") are marked top-down, one
+// binary level per launch (a root's slots lie one to three levels below it,
+// so they are marked before their level runs); one scan numbers the roots in
+// pool order and one launch emits every node.
+__global__ void wide4_roots_kernel(uint32_t G, const BNode* __restrict__ pool, uint32_t* __restrict__ croot,
+                                   uint32_t* __restrict__ level4, uint32_t* __restrict__ max_level4) {
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= G || pool[g].left == NONE) return;
+  croot[g] = 1u;
+  level4[g] = 1u;
+  atomicMax(max_level4, 1u);
 }
 
-__global__ void wide4_emit_kernel(uint32_t a, uint32_t W, uint32_t next_base, uint32_t* __restrict__ src,
-                                  const BNode* __restrict__ pool, const uint32_t* __restrict__ offs,
-                                  const uint32_t* __restrict__ pre, const uint32_t* __restrict__ rank,
-                                  Wide4Node* __restrict__ out) {
+__global__ void wide4_mark_kernel(uint32_t lb, uint32_t W, const BNode* __restrict__ pool,
+                                  uint32_t* __restrict__ croot, uint32_t* __restrict__ level4,
+                                  uint32_t* __restrict__ max_level4) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= W) return;
+  if (i >= W || !croot[lb + i]) return;
   uint32_t slot[4];
-  const int n = collapse_slots(src[a + i], pool, slot);
+  const int n = collapse_slots(lb + i, pool, slot);
+  const uint32_t lv = level4[lb + i] + 1u;
+  for (int k = 0; k < n; k++)
+    if (pool[slot[k]].left != NONE) {
+      croot[slot[k]] = 1u;
+      level4[slot[k]] = lv;
+      atomicMax(max_level4, lv);
+    }
+}
+
+__global__ void wide4_emit_kernel(uint32_t T, const BNode* __restrict__ pool, const uint32_t* __restrict__ croot,
+                                  const uint32_t* __restrict__ index4, const uint32_t* __restrict__ pre,
+                                  const uint32_t* __restrict__ rank, Wide4Node* __restrict__ out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= T || !croot[i]) return;
+  uint32_t slot[4];
+  const int n = collapse_slots(i, pool, slot);
   Wide4Node w;
-  uint32_t child = next_base + offs[i];
   for (int k = 0; k < 4; k++) {
     const bool used = k < n;
     const NodeBox b = used ? box_of(pool[slot[k]]) : NodeBox{{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
@@ -852,14 +869,13 @@ __global__ void wide4_emit_kernel(uint32_t a, uint32_t W, uint32_t next_base, ui
     if (!used) {
       w.code[k] = EMPTY_SLOT;
     } else if (pool[slot[k]].left != NONE) {
-      src[child] = slot[k];
-      w.code[k] = child++;
+      w.code[k] = index4[slot[k]];
     } else {
       const uint32_t g = pre[slot[k]];
       w.code[k] = LEAF_BIT | (g - rank[g]);
     }
   }
-  out[a + i] = w;
+  out[index4[i]] = w;
 }
 
 // ---- host side -------------------------------------------------------------
@@ -1161,52 +1177,51 @@ std::string build_blas_device(const std::vector<DeviceGeometry>& geoms, uint32_t
         N, order, d.indices.ptr, d.vertices.ptr, d.indices_redirect.ptr, d.tri_records.ptr);
   CK(cudaGetLastError());
 
-  // four-child layout, one collapse level per round
+  // four-child layout: collapse roots marked level by level, numbered by one
+  // scan in pool order (inner geometry roots first, in geometry order), one emit
   out.root_code.resize(G);
   out.root_code4.resize(G);
   CK(alloc_out(d.wide4_nodes, inner_total, bytes, st));
-  uint32_t *src4, *nin4, *off4;
-  CK(S.alloc(&src4, inner_total));
-  CK(S.alloc(&nin4, inner_total));
-  CK(S.alloc(&off4, inner_total));
-  std::vector<uint32_t> first;
   std::vector<char> leaf_root(G, 0);  // their four-child code is the two-child one, read back at the end
-  for (uint32_t g = 0; g < G; g++) {
-    if (roots[g].left == NONE && out.tree_nodes[g] == 1) {
-      leaf_root[g] = 1;
-    } else {
-      out.root_code4[g] = (uint32_t)first.size();
-      first.push_back(g);
+  {
+    uint32_t inner_roots = 0;
+    for (uint32_t g = 0; g < G; g++) {
+      if (roots[g].left == NONE) leaf_root[g] = 1;
+      else out.root_code4[g] = inner_roots++;
     }
   }
-  uint32_t a4 = 0, b4 = (uint32_t)first.size(), levels4 = 0;
-  void* scan4 = nullptr;
-  if (b4) {
-    CK(cudaMemcpyAsync(src4, first.data(), 4 * (size_t)b4, cudaMemcpyHostToDevice, st));
-    CK(S.alloc(reinterpret_cast<char**>(&scan4), scan_scratch_bytes(inner_total) + 256));
-  }
-  while (b4 > a4) {
-    const uint32_t W = b4 - a4;
-    levels4++;
-    wide4_count_kernel<<<blocks_for(W), kBlock, 0, st>>>(a4, W, src4, pool, nin4);
-    CK(scan_u32(nin4, off4, W, false, 0, scan4, st));
-    wide4_emit_kernel<<<blocks_for(W), kBlock, 0, st>>>(a4, W, b4, src4, pool, off4, pre, rank, d.wide4_nodes.ptr);
+  uint32_t *croot, *level4, *index4, *max_level4;
+  CK(S.alloc(&croot, T));
+  CK(S.alloc(&level4, T));
+  CK(S.alloc(&index4, T));
+  CK(S.alloc(&max_level4, 1));
+  CK(cudaMemsetAsync(croot, 0, 4 * (size_t)(T ? T : 1), st));
+  CK(cudaMemsetAsync(level4, 0, 4 * (size_t)(T ? T : 1), st));
+  CK(cudaMemsetAsync(max_level4, 0, 4, st));
+  uint32_t tail4[3] = {0, 0, 0};  // index4[T-1], croot[T-1], deepest level
+  if (T) {
+    wide4_roots_kernel<<<blocks_for(G), kBlock, 0, st>>>(G, pool, croot, level4, max_level4);
+    for (uint32_t l = 0; l < L; l++) {
+      const uint32_t a = level_begin[l], W = level_begin[l + 1] - a;
+      wide4_mark_kernel<<<blocks_for(W), kBlock, 0, st>>>(a, W, pool, croot, level4, max_level4);
+    }
+    void* scan4;
+    CK(S.alloc(reinterpret_cast<char**>(&scan4), scan_scratch_bytes(T) + 256));
+    CK(scan_u32(croot, index4, T, false, 0, scan4, st));
+    wide4_emit_kernel<<<blocks_for(T), kBlock, 0, st>>>(T, pool, croot, index4, pre, rank, d.wide4_nodes.ptr);
     CK(cudaGetLastError());
-    uint32_t last[2];
-    CK(cudaMemcpyAsync(&last[0], off4 + (W - 1), 4, cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(&last[1], nin4 + (W - 1), 4, cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    a4 = b4;
-    b4 += last[0] + last[1];
+    CK(cudaMemcpyAsync(&tail4[0], index4 + (T - 1), 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&tail4[1], croot + (T - 1), 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&tail4[2], max_level4, 4, cudaMemcpyDeviceToHost, st));
   }
-  d.wide4_nodes.count = b4;
-  out.max_wide4_depth = levels4;
   CK(cudaEventRecord(ev1, st));
 
   BuildCounters hbc;
   if (G) CK(cudaMemcpyAsync(out.root_code.data(), root_code, 4 * (size_t)G, cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(&hbc, bc, sizeof(hbc), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
+  d.wide4_nodes.count = tail4[0] + tail4[1];
+  out.max_wide4_depth = tail4[2];
   for (uint32_t g = 0; g < G; g++)
     if (leaf_root[g]) out.root_code4[g] = out.root_code[g];
   float ms = 0.0f;
