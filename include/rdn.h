@@ -527,6 +527,116 @@ rdn_status rdn_radix_sort_u32(uint32_t* keys, uint32_t* values, uint32_t count, 
 #define RDN_WAVEFRONT_STATIC_SCRATCH_BYTES (32u * 1024u * 1024u)
 rdn_status rdn_wavefront_shadow_bounce_static(rdn_ctx* ctx, const rdn_wavefront_desc* desc, void* stream);
 
+/* ---- device task graph (shader/task-graph) ----------------------------
+ * DeviceTaskGraphBuildSource / DeviceTaskGraphExecutor (runtime/mod.rs:54-397)
+ * on the GPU: each task group has a pool of max_in_flight * capacity task
+ * records plus the fallback record 0, an active list, an empty-index pool and
+ * a removed list. The reference's shader futures are EDSL code; here a task's
+ * future is one of two built-in programs:
+ *   RDN_TASK_PROGRAM_CHAIN  BaseShaderFuture, then n_spawn stages of
+ *       .then(spawn a task of spawn_type[k] with self as parent, payload made
+ *       by spawn_op[k]), then .map(map_op) (future/mod.rs, then.rs, task.rs,
+ *       map.rs). The base future resolves on the task's first poll; a stage
+ *       resolves in the poll that reads its finished child.
+ *   RDN_TASK_PROGRAM_TRACE  the ray-trace task (trace_task.rs:150-360): its
+ *       first poll traverses the trace call in its payload and spawns the
+ *       closest-hit or miss task the call names; it resolves when that child
+ *       has finished, taking back the child's user payload.
+ * All calls are stream-ordered on the given stream except the read-backs,
+ * which wait for it. Counts are those of the reference's
+ * TaskGraphExecutionStates. */
+#define RDN_TASK_MAX_GROUPS 16u
+#define RDN_TASK_PROGRAM_CHAIN 0u
+#define RDN_TASK_PROGRAM_TRACE 1u
+#define RDN_TASK_SPAWN_ZERO 0u          /* zeroed child payload */
+#define RDN_TASK_SPAWN_AO_PRIMARY 1u    /* AO ray generation: payload word 0 = pixel -> camera trace call */
+#define RDN_TASK_SPAWN_AO_OCCLUSION 2u  /* AO primary closest hit -> occlusion-ray trace call */
+#define RDN_TASK_MAP_NONE 0u
+#define RDN_TASK_MAP_AO_ACCUMULATE 1u   /* running average of the child's occlusion into the AO image */
+#define RDN_TASK_MAP_STORE_CHILD 2u     /* own user payload <- the child's */
+#define RDN_TASK_MAP_STORE_ZERO 3u      /* own user payload <- 0.0 */
+#define RDN_TASK_MAP_STORE_ONE 4u       /* own user payload <- 1.0 */
+#define RDN_TASK_INIT_ZERO 0u           /* dispatch_init payload: zero */
+#define RDN_TASK_INIT_INDEX 1u          /* dispatch_init payload: word 0 = dispatch index */
+/* error flags of rdn_task_graph_check_errors */
+#define RDN_TASK_ERROR_NO_FREE_SLOT 0x1u  /* a spawn found the group's pool full (the task stays pending) */
+#define RDN_TASK_ERROR_ACTIVE_FULL 0x2u   /* an active-list push past capacity was dropped */
+#define RDN_TASK_ERROR_REMOVED_FULL 0x4u  /* a removed-list push past capacity was dropped */
+
+/* Trace-call payload words of TRACE tasks and of the closest-hit / miss tasks
+ * they spawn: [0..7] origin xyz, tmin, direction xyz, tmax; [8] ray flags;
+ * [9] cull mask; [10] TLAS index; [11] closest-hit group; [12] miss group
+ * (0xFFFFFFFF none); [13..15] user payload. Closest-hit payloads add [16]
+ * built triangle, [17] instance slot, [18] t, [19] u, [20] v, [21] hit kind,
+ * [22] geometry index, [23] primitive index. */
+typedef struct rdn_task_group_desc {
+  uint32_t program;        /* RDN_TASK_PROGRAM_* */
+  uint32_t max_in_flight;  /* >= 1 */
+  uint32_t payload_words;  /* 1..32 u32 words (TRACE: >= 16) */
+  uint32_t n_spawn;        /* CHAIN: 0..4 spawn stages */
+  uint32_t spawn_type[4];  /* task group of each stage's child */
+  uint32_t spawn_op[4];    /* RDN_TASK_SPAWN_* */
+  uint32_t map_op;         /* RDN_TASK_MAP_* */
+} rdn_task_group_desc;
+
+/* Environment of the trace and AO programs, and the descriptor of an AO
+ * frame: the reference's ray-traced AO renderer (feature/ao.rs). Camera ray
+ * of pixel (x, y): uv = (x, y) / size + jitter / size with the jitter drawn
+ * from xxhash32(x, y, sample_count), target = view_projection_inv applied to
+ * ndc (2u-1, 1-2v, 1, 1), direction = normalize(target - camera_position);
+ * CULL_BACK_FACING over [f32::EPSILON, f32::MAX]. A hit spawns one
+ * ACCEPT_FIRST_HIT_AND_END_SEARCH occlusion ray over [0.01, 100] from the hit
+ * point along tbn(shading normal) * cosine_hemisphere(hammersley(sample_count,
+ * 256)); the pixel's payload is 0 when it hits and 1 otherwise (1 too when the
+ * camera ray misses). The RGBA8 texel becomes
+ * (old * sample_count + payload) / (sample_count + 1) while sample_count < 256. */
+typedef struct rdn_ao_desc {
+  float view_projection_inv[16];  /* Mat4 in the reference's memory order */
+  float camera_position[3];
+  uint32_t width, height;
+  uint32_t sample_count;          /* samples already averaged into image */
+  uint32_t tlas_uniform;
+  uint32_t traversal;             /* RDN_TRAVERSAL_* */
+  const float* normals;           /* device, nullable: 3 per built vertex (shading normals) */
+  uint8_t* image;                 /* device, RGBA8 unorm, width * height texels, 4-byte aligned */
+  uint32_t sbt_closest[2];        /* task graphs: closest-hit group of the camera and the occlusion ray */
+  uint32_t sbt_miss;              /* task graphs: miss group of both rays */
+  uint32_t pad;
+} rdn_ao_desc;
+
+typedef struct rdn_task_graph rdn_task_graph;
+rdn_status rdn_task_graph_create(rdn_ctx* ctx, const rdn_task_group_desc* groups, uint32_t count, uint32_t capacity,
+                                 void* stream, rdn_task_graph** out);
+rdn_status rdn_task_graph_destroy(rdn_task_graph* graph);
+/* dispatch_allocate_init_task (runtime/mod.rs:199-260): count root tasks, no parent. */
+rdn_status rdn_task_graph_dispatch_init(rdn_task_graph* graph, uint32_t group, uint32_t count, uint32_t init_op,
+                                        void* stream);
+/* execute (runtime/mod.rs:357-397): rounds x (every group in order: prepare,
+ * poll, compact). env: NULL when no group runs a TRACE program or an AO
+ * operation. */
+rdn_status rdn_task_graph_execute(rdn_task_graph* graph, uint32_t rounds, const rdn_ao_desc* env, void* stream);
+/* read_back_execution_states: wake, sleep_or_finished and empty counts per
+ * group (arrays of the graph's group count); waits for the stream. */
+rdn_status rdn_task_graph_states(rdn_task_graph* graph, uint32_t* wake, uint32_t* sleep_or_finished,
+                                 uint32_t* empty, void* stream);
+/* debug_execution for one group: active list, empty pool (each up to the
+ * group's max_in_flight * capacity entries) and the state of every record
+ * (capacity + 1 entries; host arrays); waits for the stream. */
+rdn_status rdn_task_graph_debug(rdn_task_graph* graph, uint32_t group, uint32_t* active, uint32_t* n_active,
+                                uint32_t* empty, uint32_t* n_empty, uint32_t* task_states, void* stream);
+rdn_status rdn_task_graph_check_errors(rdn_task_graph* graph, void* stream, uint32_t* flags);
+
+/* The reference's AO pipeline as a task graph (feature/ao.rs:162-313 on
+ * trace_ray): group 0 ray-trace task (max_in_flight 2), 1 ray generation,
+ * 2 primary closest hit, 3 occlusion closest hit, 4 miss; capacity =
+ * width * height. rdn_ao_render_graph dispatches one ray-generation task per
+ * pixel and runs 8 rounds (the reference's execution_round_hint). */
+rdn_status rdn_ao_pipeline_create(rdn_ctx* ctx, uint32_t width, uint32_t height, void* stream,
+                                  rdn_task_graph** out);
+rdn_status rdn_ao_render_graph(rdn_task_graph* graph, const rdn_ao_desc* desc, void* stream);
+/* The same frame as one fused kernel, one thread per pixel. */
+rdn_status rdn_ao_render(rdn_ctx* ctx, const rdn_ao_desc* desc, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

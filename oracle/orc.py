@@ -74,6 +74,8 @@ def lib():
         L.orc_trace_paths.argtypes = [vp, vp, u32, vp, u32, u32, u32, C.c_float, C.c_float, u32, vp, vp, i32,
                                       C.POINTER(C.c_double)]
         L.orc_path_segments.argtypes = [vp, vp, u32, vp, u32, u32, u32, vp, vp, i32]
+        L.orc_ao_render.argtypes = [vp, vp, vp, u32, u32, u32, u32, vp, vp, u32, u32, i32, vp,
+                                    C.POINTER(C.c_double)]
         L.orc_wavefront_shadow_bounce.argtypes = [vp, vp, u32, u32, vp, u32, u32, u32, u32, vp, vp, i32,
                                                   C.POINTER(C.c_double)]
         _lib = L
@@ -276,3 +278,20 @@ def select_nth(keys: np.ndarray, index: int) -> np.ndarray:
     idx = np.arange(keys.shape[0], dtype=np.uint64)
     lib().orc_select_nth(_ptr(keys), _ptr(idx), keys.shape[0], index)
     return idx
+
+
+def ao_render(system: OracleSystem, vp_inv, cam, width, height, image: np.ndarray, sample_count=0, tlas=0,
+              normals=None, rows=None, threads=4):
+    """One AO sample into image (uint32 RGBA8 texels, width*height, updated in
+    place) for rows [r0, r1). Returns (rays traced [camera, occlusion], seconds)."""
+    vp = np.ascontiguousarray(vp_inv, np.float32)
+    cm = np.ascontiguousarray(cam, np.float32)
+    assert image.dtype == np.uint32 and image.size == width * height and image.flags.c_contiguous
+    nrm = None if normals is None else np.ascontiguousarray(normals, np.float32)
+    r0, r1 = rows if rows is not None else (0, height)
+    rays = np.zeros(2, np.uint64)
+    sec = C.c_double()
+    rc = lib().orc_ao_render(system._h, _ptr(vp), _ptr(cm), width, height, sample_count, tlas, _ptr(nrm), _ptr(image),
+                             r0, r1, threads, _ptr(rays), C.byref(sec))
+    system._check(rc)
+    return (int(rays[0]), int(rays[1])), sec.value

@@ -49,6 +49,7 @@
 #include "orc_math.h"
 #include "orc_select.h"
 #include "orc_shade.h"
+#include "orc_ao.h"
 
 namespace orc {
 
@@ -1339,6 +1340,75 @@ int orc_wavefront_shadow_bounce(void* cp, const float* cam, uint32_t W, uint32_t
   return 0;
 }
 
+
+// One AO sample for rows [row0, row1) of a width x height frame (see
+// orc_ao.h); image: width * height RGBA8 texels, updated in place. rays2
+// receives the camera and occlusion rays traced.
+int orc_ao_render(void* cp, const float* vp_inv, const float* cam, uint32_t W, uint32_t H, uint32_t sample_count,
+                  uint32_t tlas, const float* normals, uint32_t* image, uint32_t row0, uint32_t row1, int threads,
+                  uint64_t* rays2, double* seconds) {
+  Ctx& c = *(Ctx*)cp;
+  if (!c.built) {
+    int rc = build_all(c);
+    if (rc) return rc;
+  }
+  const Built& B = *c.built;
+  AoView A;
+  memcpy(A.vp_inv, vp_inv, sizeof(A.vp_inv));
+  memcpy(A.cam, cam, sizeof(A.cam));
+  A.width = W;
+  A.height = H;
+  A.sample_count = sample_count;
+  if (row1 > H) row1 = H;
+  if (row0 > row1) row0 = row1;
+  if (threads < 1) threads = 1;
+  std::vector<Counters> cn(threads);
+  std::vector<uint64_t> rc(2 * (size_t)threads, 0);
+  std::atomic<uint32_t> next_row{row0};
+  auto t0 = std::chrono::steady_clock::now();
+  auto work = [&](int w) {
+    for (;;) {
+      const uint32_t y = next_row.fetch_add(1);
+      if (y >= row1) break;
+      for (uint32_t x = 0; x < W; x++) {
+        V3 o, d;
+        ao_camera_ray(A, x, y, &o, &d);
+        RayIn r{{o.x, o.y, o.z}, F32_EPSILON, {d.x, d.y, d.z}, F32_MAX};
+        HitOut h;
+        uint32_t tri = 0;
+        traverse(B, r, tlas, 0x10u, 0xFFFFFFFFu, 0, h, cn[w], nullptr, &tri);
+        rc[2 * (size_t)w]++;
+        float payload = 1.0f;
+        if (h.prim != INVALID_NEXT) {
+          const V3 hit = o + d * h.t;
+          const V3 n = ao_shading_normal(B.indices.data(), B.vertices.data(), normals,
+                                         B.tlas_data[h.instance].transform_inv, tri, h.u, h.v, o, hit);
+          const V3 dir = ao_direction(n, sample_count);
+          RayIn sr{{hit.x, hit.y, hit.z}, 0.01f, {dir.x, dir.y, dir.z}, 100.0f};
+          HitOut sh;
+          traverse(B, sr, tlas, RAY_FLAG_END_SEARCH, 0xFFFFFFFFu, 0, sh, cn[w], nullptr);
+          rc[2 * (size_t)w + 1]++;
+          payload = sh.prim != INVALID_NEXT ? 0.0f : 1.0f;
+        }
+        uint32_t& texel = image[(size_t)y * W + x];
+        texel = ao_accumulate(texel, sample_count, payload);
+      }
+    }
+  };
+  std::vector<std::thread> th;
+  for (int w = 0; w < threads; w++) th.emplace_back(work, w);
+  for (auto& t : th) t.join();
+  auto t1 = std::chrono::steady_clock::now();
+  if (seconds) *seconds = std::chrono::duration<double>(t1 - t0).count();
+  if (rays2) {
+    rays2[0] = rays2[1] = 0;
+    for (int w = 0; w < threads; w++) {
+      rays2[0] += rc[2 * (size_t)w];
+      rays2[1] += rc[2 * (size_t)w + 1];
+    }
+  }
+  return 0;
+}
 
 // Batched paths over n rays (tlas_idx per ray, or tlas_uniform when NULL).
 // out = (radiance, depth|flags bits) per ray; seg receives rays traced per

@@ -32,6 +32,8 @@ UNITS = {
     "adjoint.cu": ["-fmad=false"],
     "parallel.cu": [],
     "device_build.cu": ["-fmad=false"],
+    "task_graph.cu": ["-fmad=false"],
+    "ao.cu": ["-fmad=false"],
 }
 
 

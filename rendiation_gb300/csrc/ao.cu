@@ -1,0 +1,85 @@
+// Fused ambient-occlusion frame for sm_103a: the reference AO renderer's ray
+// generation, primary closest hit, occlusion ray and miss shaders
+// (feature/ao.rs:193-296) as one kernel, one thread per pixel, warps over 8x4
+// pixel tiles. It computes what the task-graph form of the same pipeline
+// computes, without the task pools. Built with -fmad=false: see ao.cuh.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "ao.cuh"
+#include "traverse.cuh"
+
+namespace rdn {
+namespace {
+
+using namespace dev;
+
+template <int MODE, bool LOCAL>
+__global__ void __launch_bounds__(128) ao_kernel(TraceParams P, AoEnv A) {
+  RDN_TRAVERSAL_STACK(LOCAL);
+  const uint32_t tiles_x = (A.width + 7) / 8;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
+  const uint32_t x = (warp % tiles_x) * 8 + (lane & 7u), y = (warp / tiles_x) * 4 + (lane >> 3);
+  if (x >= A.width || y >= A.height) return;
+  float3 o, d;
+  ao_camera_ray(A, x, y, o, d);
+  RayCtx R;
+  R.o = o;
+  R.d = d;
+  R.tmin = F32_EPSILON;
+  R.tmax = F32_MAX;
+  R.ray_flags = RAY_FLAG_CULL_BACK;
+  R.cull_mask = 0xFFFFFFFFu;
+  bool bad;
+  traverse_ray<MODE, false>(P, R, A.tlas, stack_ptr, stack_stride, bad);
+  float payload = 1.0f;  // miss shader
+  if (R.best.have) {
+    const float3 hit = o + d * R.best.t;
+    const float3 n =
+        ao_shading_normal(A, P.tlas_data + R.best.inst, __ldg(P.redirect + R.best.k), R.best.u, R.best.v, o, hit);
+    RayCtx S;
+    S.o = hit;
+    S.d = ao_direction(n, A.sample_count);
+    S.tmin = AO_TEST_MIN;
+    S.tmax = AO_TEST_MAX;
+    S.ray_flags = RAY_FLAG_END_SEARCH;
+    S.cull_mask = 0xFFFFFFFFu;
+    bool bad2;
+    traverse_ray<MODE, false>(P, S, A.tlas, stack_ptr, stack_stride, bad2);
+    bad |= bad2;
+    payload = S.best.have ? 0.0f : 1.0f;  // secondary closest hit: occluded
+  }
+  if (bad) atomicOr(P.error_word, 2u);
+  ao_accumulate(A, y * A.width + x, payload);
+}
+
+template <int MODE, bool LOCAL>
+cudaError_t launch_variant(const TraceParams& p, const AoEnv& a, cudaStream_t st) {
+  const uint32_t warps = ((a.width + 7) / 8) * ((a.height + 3) / 4);
+  const uint32_t grid = (warps * 32 + 127) / 128;
+  const size_t smem = MODE != MODE_THREADED && !LOCAL ? (size_t)p.stack_depth * 128 * sizeof(uint2) : 0;
+  static bool attr_done = false;
+  if (!attr_done) {
+    cudaError_t e =
+        cudaFuncSetAttribute(ao_kernel<MODE, LOCAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e != cudaSuccess) return e;
+    attr_done = true;
+  }
+  ao_kernel<MODE, LOCAL><<<grid, 128, smem, st>>>(p, a);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_ao(const TraceParams& p, const AoEnv& a, int mode, cudaStream_t st) {
+  if (a.width == 0 || a.height == 0) return cudaSuccess;
+  if (mode == MODE_WIDE4)
+    return p.local_stack ? launch_variant<MODE_WIDE4, true>(p, a, st) : launch_variant<MODE_WIDE4, false>(p, a, st);
+  if (mode == MODE_BINARY)
+    return p.local_stack ? launch_variant<MODE_BINARY, true>(p, a, st)
+                         : launch_variant<MODE_BINARY, false>(p, a, st);
+  return launch_variant<MODE_THREADED, false>(p, a, st);
+}
+
+}  // namespace rdn

@@ -15,6 +15,7 @@
 #include "adjoint.h"
 #include "parallel.h"
 #include "paths.h"
+#include "task_graph.h"
 #include "wavefront.h"
 
 using rdn::DevBuf;
@@ -1088,6 +1089,244 @@ rdn_status rdn_wavefront_shadow_bounce_static(rdn_ctx* c, const rdn_wavefront_de
     e = rdn::launch_wavefront_static(p, w, mode_of(d->traversal), d->block_size, c->sm_count, d->phases,
                                      c->device, static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(c, e, "static wavefront launch");
+  return RDN_OK;
+}
+
+}  // extern "C"
+
+// ---- device task graph and AO -------------------------------------------
+
+struct rdn_task_graph {
+  rdn_ctx* ctx = nullptr;
+  rdn::TaskGraph graph;
+  bool needs_env = false;    // a TRACE program or an AO operation
+  bool ao_pipeline = false;  // made by rdn_ao_pipeline_create
+  uint32_t width = 0, height = 0;
+};
+
+namespace {
+
+rdn_status ao_env(rdn_ctx* c, const rdn_ao_desc* d, rdn::TraceParams& p, rdn::AoEnv& a) {
+  if (!d->image) return fail(c, RDN_ERR_INVALID_ARG, "null AO image");
+  if (reinterpret_cast<uintptr_t>(d->image) & 3) return fail(c, RDN_ERR_INVALID_ARG, "AO image must be 4-byte aligned");
+  if (d->width == 0 || d->height == 0 || (uint64_t)d->width * d->height > 0x7FFFFFFFull)
+    return fail(c, RDN_ERR_INVALID_ARG, "AO frame size must be 1..2^31 pixels");
+  if (d->traversal > RDN_TRAVERSAL_ORDERED_WIDE) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
+  rdn_status st = ensure_built(c);
+  if (st != RDN_OK) return st;
+  rdn_trace_desc td;
+  std::memset(&td, 0, sizeof(td));
+  td.tlas_uniform = d->tlas_uniform;
+  td.cull_mask = 0xFFFFFFFFu;
+  td.traversal = d->traversal;
+  td.local_stack = 1;
+  fill_params(c, &td, p);
+  std::memset(&a, 0, sizeof(a));
+  std::memcpy(a.vp_inv, d->view_projection_inv, sizeof(a.vp_inv));
+  std::memcpy(a.cam, d->camera_position, sizeof(a.cam));
+  a.width = d->width;
+  a.height = d->height;
+  a.sample_count = d->sample_count;
+  a.tlas = d->tlas_uniform;
+  a.sbt_closest[0] = d->sbt_closest[0];
+  a.sbt_closest[1] = d->sbt_closest[1];
+  a.sbt_miss = d->sbt_miss;
+  a.image = d->image;
+  a.normals = d->normals;
+  a.indices = c->dev.indices.ptr;
+  a.vertices = c->dev.vertices.ptr;
+  a.n_instances = (uint32_t)c->dev.tlas_data.count;
+  a.n_triangles = (uint32_t)(c->dev.indices.count / 3);
+  return RDN_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+rdn_status rdn_task_graph_create(rdn_ctx* c, const rdn_task_group_desc* groups, uint32_t count, uint32_t capacity,
+                                 void* stream, rdn_task_graph** out) {
+  if (!c || !groups || !out) return fail(c, RDN_ERR_INVALID_ARG, "null context, groups or output");
+  if (c->device < 0) return fail(c, RDN_ERR_UNSUPPORTED, "host-only context has no device");
+  *out = nullptr;
+  std::vector<rdn::TaskGroupDesc> desc(count);
+  bool needs_env = false;
+  for (uint32_t g = 0; g < count; g++) {
+    rdn::TaskGroupDesc& d = desc[g];
+    d.program = groups[g].program;
+    d.max_in_flight = groups[g].max_in_flight;
+    d.payload_words = groups[g].payload_words;
+    d.n_spawn = groups[g].n_spawn;
+    d.map_op = groups[g].map_op;
+    for (uint32_t k = 0; k < 4; k++) {
+      d.spawn_type[k] = groups[g].spawn_type[k];
+      d.spawn_op[k] = k < d.n_spawn ? groups[g].spawn_op[k] : 0u;
+      if (k < d.n_spawn && d.spawn_op[k] != RDN_TASK_SPAWN_ZERO) needs_env = true;
+    }
+    if (d.program == RDN_TASK_PROGRAM_TRACE || d.map_op == RDN_TASK_MAP_AO_ACCUMULATE) needs_env = true;
+  }
+  std::unique_ptr<rdn_task_graph> tg(new (std::nothrow) rdn_task_graph());
+  if (!tg) return fail(c, RDN_ERR_OOM, "out of host memory");
+  tg->ctx = c;
+  tg->needs_env = needs_env;
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e != cudaSuccess) return cuda_fail(c, e, "cudaSetDevice");
+  const std::string err = tg->graph.create(desc, capacity, c->sm_count, static_cast<cudaStream_t>(stream));
+  if (!err.empty()) {
+    const bool oom = err.find("cudaMalloc") != std::string::npos;
+    return fail(c, oom ? RDN_ERR_OOM : RDN_ERR_INVALID_ARG, err);
+  }
+  *out = tg.release();
+  return RDN_OK;
+}
+
+rdn_status rdn_task_graph_destroy(rdn_task_graph* g) {
+  if (!g) return RDN_OK;
+  if (g->ctx && g->ctx->device >= 0) cudaSetDevice(g->ctx->device);
+  delete g;
+  return RDN_OK;
+}
+
+rdn_status rdn_task_graph_dispatch_init(rdn_task_graph* g, uint32_t group, uint32_t count, uint32_t init_op,
+                                        void* stream) {
+  if (!g) return RDN_ERR_INVALID_ARG;
+  rdn_ctx* c = g->ctx;
+  if (group >= g->graph.group_count()) return fail(c, RDN_ERR_INVALID_ARG, "no such task group");
+  if (init_op > RDN_TASK_INIT_INDEX) return fail(c, RDN_ERR_INVALID_ARG, "unknown init payload");
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e == cudaSuccess) e = g->graph.dispatch_init(group, count, init_op, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(c, e, "task graph dispatch");
+  return RDN_OK;
+}
+
+rdn_status rdn_task_graph_execute(rdn_task_graph* g, uint32_t rounds, const rdn_ao_desc* env, void* stream) {
+  if (!g) return RDN_ERR_INVALID_ARG;
+  rdn_ctx* c = g->ctx;
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e != cudaSuccess) return cuda_fail(c, e, "cudaSetDevice");
+  if (!g->needs_env) {
+    e = g->graph.execute(rounds, nullptr, rdn::MODE_THREADED, nullptr, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(c, e, "task graph execute");
+    return RDN_OK;
+  }
+  if (!env) return fail(c, RDN_ERR_INVALID_ARG, "this graph traces or shades: pass an rdn_ao_desc environment");
+  std::lock_guard<std::mutex> lk(c->lock);
+  rdn::TraceParams p;
+  rdn::AoEnv a;
+  rdn_status st = ao_env(c, env, p, a);
+  if (st != RDN_OK) return st;
+  e = g->graph.execute(rounds, &p, mode_of(env->traversal), &a, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(c, e, "task graph execute");
+  return RDN_OK;
+}
+
+rdn_status rdn_task_graph_states(rdn_task_graph* g, uint32_t* wake, uint32_t* sleep_or_finished, uint32_t* empty,
+                                 void* stream) {
+  if (!g) return RDN_ERR_INVALID_ARG;
+  rdn_ctx* c = g->ctx;
+  if (!wake || !sleep_or_finished || !empty) return fail(c, RDN_ERR_INVALID_ARG, "null output array");
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e == cudaSuccess) e = g->graph.states(wake, empty, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(c, e, "task graph states");
+  for (uint32_t i = 0; i < g->graph.group_count(); i++)
+    sleep_or_finished[i] = g->graph.group_cap(i) - empty[i] - wake[i];
+  return RDN_OK;
+}
+
+rdn_status rdn_task_graph_debug(rdn_task_graph* g, uint32_t group, uint32_t* active, uint32_t* n_active,
+                                uint32_t* empty, uint32_t* n_empty, uint32_t* task_states, void* stream) {
+  if (!g) return RDN_ERR_INVALID_ARG;
+  rdn_ctx* c = g->ctx;
+  if (group >= g->graph.group_count()) return fail(c, RDN_ERR_INVALID_ARG, "no such task group");
+  if (!active || !n_active || !empty || !n_empty || !task_states)
+    return fail(c, RDN_ERR_INVALID_ARG, "null output array");
+  std::vector<uint32_t> a, em, s;
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e == cudaSuccess) e = g->graph.debug(group, a, em, s, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(c, e, "task graph debug");
+  std::copy(a.begin(), a.end(), active);
+  std::copy(em.begin(), em.end(), empty);
+  std::copy(s.begin(), s.end(), task_states);
+  *n_active = (uint32_t)a.size();
+  *n_empty = (uint32_t)em.size();
+  return RDN_OK;
+}
+
+rdn_status rdn_task_graph_check_errors(rdn_task_graph* g, void* stream, uint32_t* flags) {
+  if (!g || !flags) return RDN_ERR_INVALID_ARG;
+  cudaError_t e = cudaSetDevice(g->ctx->device);
+  if (e == cudaSuccess) e = g->graph.read_error(flags, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(g->ctx, e, "task graph error word");
+  return RDN_OK;
+}
+
+rdn_status rdn_ao_pipeline_create(rdn_ctx* c, uint32_t width, uint32_t height, void* stream, rdn_task_graph** out) {
+  if (!c || !out) return fail(c, RDN_ERR_INVALID_ARG, "null context or output");
+  if (width == 0 || height == 0 || (uint64_t)width * height * 2 >= (1ull << 28))
+    return fail(c, RDN_ERR_INVALID_ARG, "AO pipeline frame must have 1..2^27 pixels");
+  rdn_task_group_desc g[5];
+  std::memset(g, 0, sizeof(g));
+  // 0: ray-trace task (max_in_flight_trace_ray(2))
+  g[0].program = RDN_TASK_PROGRAM_TRACE;
+  g[0].max_in_flight = 2;
+  g[0].payload_words = 16;
+  // 1: ray generation: then_trace(camera ray).map(accumulate)
+  g[1].max_in_flight = 1;
+  g[1].payload_words = 1;
+  g[1].n_spawn = 1;
+  g[1].spawn_type[0] = 0;
+  g[1].spawn_op[0] = RDN_TASK_SPAWN_AO_PRIMARY;
+  g[1].map_op = RDN_TASK_MAP_AO_ACCUMULATE;
+  // 2: primary closest hit: then_trace(occlusion ray).map(store the result)
+  g[2].max_in_flight = 1;
+  g[2].payload_words = 24;
+  g[2].n_spawn = 1;
+  g[2].spawn_type[0] = 0;
+  g[2].spawn_op[0] = RDN_TASK_SPAWN_AO_OCCLUSION;
+  g[2].map_op = RDN_TASK_MAP_STORE_CHILD;
+  // 3: occlusion closest hit: payload 0
+  g[3].max_in_flight = 1;
+  g[3].payload_words = 24;
+  g[3].map_op = RDN_TASK_MAP_STORE_ZERO;
+  // 4: miss: payload 1
+  g[4].max_in_flight = 1;
+  g[4].payload_words = 16;
+  g[4].map_op = RDN_TASK_MAP_STORE_ONE;
+  rdn_status st = rdn_task_graph_create(c, g, 5, width * height, stream, out);
+  if (st != RDN_OK) return st;
+  (*out)->ao_pipeline = true;
+  (*out)->width = width;
+  (*out)->height = height;
+  return RDN_OK;
+}
+
+rdn_status rdn_ao_render_graph(rdn_task_graph* g, const rdn_ao_desc* d, void* stream) {
+  if (!g || !d) return RDN_ERR_INVALID_ARG;
+  rdn_ctx* c = g->ctx;
+  if (!g->ao_pipeline) return fail(c, RDN_ERR_INVALID_ARG, "not an AO pipeline graph");
+  if (d->width != g->width || d->height != g->height)
+    return fail(c, RDN_ERR_INVALID_ARG, "frame size differs from the pipeline's");
+  rdn_ao_desc env = *d;
+  env.sbt_closest[0] = 2;
+  env.sbt_closest[1] = 3;
+  env.sbt_miss = 4;
+  rdn_status st = rdn_task_graph_dispatch_init(g, 1, d->width * d->height, RDN_TASK_INIT_INDEX, stream);
+  if (st != RDN_OK) return st;
+  return rdn_task_graph_execute(g, 8, &env, stream);
+}
+
+rdn_status rdn_ao_render(rdn_ctx* c, const rdn_ao_desc* d, void* stream) {
+  Range range_("rdn_ao_render");
+  if (!c || !d) return fail(c, RDN_ERR_INVALID_ARG, "null context or descriptor");
+  if (c->device < 0) return fail(c, RDN_ERR_UNSUPPORTED, "host-only context cannot trace");
+  std::lock_guard<std::mutex> lk(c->lock);
+  rdn::TraceParams p;
+  rdn::AoEnv a;
+  rdn_status st = ao_env(c, d, p, a);
+  if (st != RDN_OK) return st;
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e == cudaSuccess) e = rdn::launch_ao(p, a, mode_of(d->traversal), static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(c, e, "AO launch");
   return RDN_OK;
 }
 

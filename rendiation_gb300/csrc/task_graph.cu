@@ -1,0 +1,728 @@
+// Device task graph for sm_103a (see task_graph.h for the reference map).
+//
+// One execute round runs, for each group in order, four launches:
+//   drain    commit the active / empty / removed bump counters and move the
+//            removed indices to the end of the empty pool (prepare_execution)
+//   poll     one thread per active task: run its program, then finish it
+//            (wake the parent or clean up) or put it to sleep
+//   count    commit the active list, count the tasks still NOT_FINISHED_WAKEN
+//            per 1024-entry tile (GO_TO_SLEEP becomes SLEEP), and in the last
+//            block to finish, scan the tile counts
+//   scatter  write the kept indices, in order, to the other active buffer
+// The committed sizes live in a 64 B control block per group in device memory:
+// no host round trip inside a round, and a sequence of rounds can be captured
+// into a CUDA graph. The last-block pattern (a ticket counter) lets the first
+// blocks read the old sizes while only the last one writes the new ones.
+//
+// Deviations from the reference, both at exhaustion only: a bump list or the
+// empty pool that is full rejects the push or pop and sets an error bit,
+// where the reference's bound check admits one access past the end
+// (bump_allocator.rs:254-258, 296-300).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+
+#include "ao.cuh"
+#include "task_graph.h"
+#include "traverse.cuh"
+
+namespace rdn {
+namespace {
+
+using namespace dev;
+
+constexpr uint32_t kTile = 1024;
+constexpr uint32_t kCompactThreads = 256;
+constexpr uint32_t kPollThreads = 128;
+
+__device__ __forceinline__ uint32_t* task_locals(const TaskGroupDev& T, uint32_t i) {
+  return T.locals + (size_t)i * kTaskLocalWords;
+}
+__device__ __forceinline__ uint32_t* task_payload(const TaskGroupDev& T, uint32_t i) {
+  return T.payload + (size_t)i * T.payload_words;
+}
+
+// DeviceBumpAllocationInvocationInstance::bump_allocate into the active list.
+__device__ __forceinline__ void push_active(const TaskGraphDev& G, const TaskGroupDev& T, uint32_t idx) {
+  GroupCtl* c = T.ctl;
+  const uint32_t size = c->active.size;
+  const uint32_t b = atomicAdd(&c->active.bump, 1u);
+  if (b < T.cap - size)
+    T.active[c->sel][size + b] = idx;
+  else
+    atomicOr(G.error, TASK_ERR_ACTIVE_FULL);
+}
+
+// TaskGroupDeviceInvocationInstance::spawn_new_task_dyn: pop a free index,
+// write the record (state, parent, payload, initial future state), push the
+// index to the active list. Returns TASK_HANDLE_UNINIT when the pool is empty.
+__device__ uint32_t spawn_task(const TaskGraphDev& G, uint32_t g, const uint32_t* src, uint32_t src_words,
+                               uint32_t parent_type, uint32_t parent_index) {
+  const TaskGroupDev& T = G.g[g];
+  GroupCtl* c = T.ctl;
+  const uint32_t esize = c->empty.size;
+  const uint32_t b = atomicAdd(&c->empty.bump, 1u);
+  if (b >= esize) {
+    atomicOr(G.error, TASK_ERR_NO_FREE_SLOT);
+    return TASK_HANDLE_UNINIT;
+  }
+  const uint32_t idx = T.empty[esize - b - 1];
+  T.state[idx] = TASK_NOT_FINISHED_WAKEN;
+  T.parent_index[idx] = parent_index;
+  T.parent_type[idx] = parent_type;
+  uint32_t* pl = task_payload(T, idx);
+  for (uint32_t w = 0; w < T.payload_words; w++) pl[w] = w < src_words ? src[w] : 0u;
+  uint32_t* L = task_locals(T, idx);
+  L[0] = 0u;
+  for (uint32_t k = 0; k < kTaskMaxSpawns; k++) L[1 + k] = TASK_HANDLE_UNINIT;
+  L[5] = TRACE_SUB_NOT_SPAWNED;
+  L[6] = TRACE_SUB_NOT_SPAWNED;
+  L[7] = 0u;
+  push_active(G, T, idx);
+  return idx;
+}
+
+// wake_task_dyn: a task still in the active list (GO_TO_SLEEP) is only
+// re-flagged; a sleeping one is pushed again.
+__device__ __forceinline__ void wake_task(const TaskGraphDev& G, uint32_t g, uint32_t idx) {
+  const TaskGroupDev& T = G.g[g];
+  const bool in_active = T.state[idx] == TASK_GO_TO_SLEEP;
+  T.state[idx] = TASK_NOT_FINISHED_WAKEN;
+  if (!in_active) push_active(G, T, idx);
+}
+
+// cleanup_finished_task_state_and_payload
+__device__ __forceinline__ void cleanup_task(const TaskGraphDev& G, uint32_t g, uint32_t idx) {
+  const TaskGroupDev& T = G.g[g];
+  GroupCtl* c = T.ctl;
+  const uint32_t size = c->removed.size;
+  const uint32_t b = atomicAdd(&c->removed.bump, 1u);
+  if (b < T.cap - size)
+    T.removed[size + b] = idx;
+  else
+    atomicOr(G.error, TASK_ERR_REMOVED_FULL);
+  T.state[idx] = TASK_NOT_EXIST;
+}
+
+// poll_task_dyn: a finished child is cleaned up; its payload stays readable
+// until the removed list is drained at the child group's next round.
+__device__ __forceinline__ bool poll_child(const TaskGraphDev& G, uint32_t g, uint32_t idx) {
+  if (G.g[g].state[idx] != TASK_FINISHED) return false;
+  cleanup_task(G, g, idx);
+  return true;
+}
+
+// Poll finalisation of the polling pipeline (task_group.rs:130-165).
+__device__ __forceinline__ void finalize(const TaskGraphDev& G, uint32_t g, uint32_t idx, bool resolved) {
+  const TaskGroupDev& T = G.g[g];
+  if (!resolved) {
+    T.state[idx] = TASK_GO_TO_SLEEP;
+    return;
+  }
+  T.state[idx] = TASK_FINISHED;
+  const uint32_t pi = T.parent_index[idx], pt = T.parent_type[idx];
+  if (pi == TASK_NO_PARENT)
+    cleanup_task(G, g, idx);
+  else if (pt < G.n_groups)
+    wake_task(G, pt, pi);
+}
+
+__device__ __forceinline__ void put_ray(uint32_t* b, float3 o, float tmin, float3 d, float tmax) {
+  b[0] = __float_as_uint(o.x);
+  b[1] = __float_as_uint(o.y);
+  b[2] = __float_as_uint(o.z);
+  b[3] = __float_as_uint(tmin);
+  b[4] = __float_as_uint(d.x);
+  b[5] = __float_as_uint(d.y);
+  b[6] = __float_as_uint(d.z);
+  b[7] = __float_as_uint(tmax);
+}
+
+// Payload of a chain's child (the closure of a .then stage).
+__device__ uint32_t child_payload(uint32_t op, const uint32_t* self, const TraceParams& P, const AoEnv& A,
+                                  uint32_t* b) {
+  if (op == TASK_SPAWN_AO_PRIMARY) {
+    const uint32_t pixel = self[0];
+    float3 o, d;
+    ao_camera_ray(A, pixel % A.width, pixel / A.width, o, d);
+    put_ray(b, o, F32_EPSILON, d, F32_MAX);
+    b[8] = RAY_FLAG_CULL_BACK;
+    b[9] = 0xFFFFFFFFu;
+    b[10] = A.tlas;
+    b[11] = A.sbt_closest[0];
+    b[12] = A.sbt_miss;
+    b[13] = __float_as_uint(0.0f);
+    b[14] = b[15] = 0u;
+    return kTraceCallWords;
+  }
+  if (op == TASK_SPAWN_AO_OCCLUSION) {
+    if (self[17] >= A.n_instances || self[16] >= A.n_triangles) {
+      // not a closest-hit payload: an empty trace call that resolves at once
+      put_ray(b, make_float3(0.0f, 0.0f, 0.0f), 1.0f, make_float3(0.0f, 0.0f, 1.0f), 0.0f);
+      b[8] = 0u;
+      b[9] = 0u;
+      b[10] = 0u;
+      b[11] = b[12] = 0xFFFFFFFFu;
+      b[13] = __float_as_uint(1.0f);
+      b[14] = b[15] = 0u;
+      return kTraceCallWords;
+    }
+    const float3 ro = make_float3(__uint_as_float(self[0]), __uint_as_float(self[1]), __uint_as_float(self[2]));
+    const float3 rd = make_float3(__uint_as_float(self[4]), __uint_as_float(self[5]), __uint_as_float(self[6]));
+    const float t = __uint_as_float(self[18]);
+    const float3 hit = ro + rd * t;
+    const float3 n = ao_shading_normal(A, P.tlas_data + self[17], self[16], __uint_as_float(self[19]),
+                                       __uint_as_float(self[20]), ro, hit);
+    const float3 dir = ao_direction(n, A.sample_count);
+    put_ray(b, hit, AO_TEST_MIN, dir, AO_TEST_MAX);
+    b[8] = RAY_FLAG_END_SEARCH;
+    b[9] = 0xFFFFFFFFu;
+    b[10] = self[10];
+    b[11] = A.sbt_closest[1];
+    b[12] = A.sbt_miss;
+    b[13] = __float_as_uint(1.0f);
+    b[14] = b[15] = 0u;
+    return kTraceCallWords;
+  }
+  return 0u;
+}
+
+__device__ __forceinline__ void apply_map(uint32_t op, uint32_t* self, const uint32_t* child, const AoEnv& A) {
+  if (op == TASK_MAP_AO_ACCUMULATE) {
+    if (self[0] < A.width * A.height) ao_accumulate(A, self[0], __uint_as_float(child[kTraceUser]));
+  } else if (op == TASK_MAP_STORE_CHILD) {
+    for (uint32_t w = 0; w < 3; w++) self[kTraceUser + w] = child[kTraceUser + w];
+  } else if (op == TASK_MAP_STORE_ZERO) {
+    self[kTraceUser] = __float_as_uint(0.0f);
+  } else if (op == TASK_MAP_STORE_ONE) {
+    self[kTraceUser] = __float_as_uint(1.0f);
+  }
+}
+
+// BaseShaderFuture.then(spawn).then(spawn)...map: the base future resolves on
+// its first poll only; a stage whose upstream resolved spawns its child and
+// polls it at once; a stage resolves in the poll that reads its finished child.
+__device__ bool poll_chain(const TaskGraphDev& G, uint32_t g, uint32_t idx, const TraceParams& P, const AoEnv& A) {
+  const TaskGroupDev& T = G.g[g];
+  uint32_t* L = task_locals(T, idx);
+  uint32_t* self = task_payload(T, idx);
+  bool r = L[0] == 0u;
+  L[0] = 1u;
+  const uint32_t* child = nullptr;
+  for (uint32_t k = 0; k < T.n_spawn; k++) {
+    const uint32_t cg = T.spawn_type[k];
+    if (r) {
+      uint32_t b[kTaskMaxPayloadWords];
+      const uint32_t words = child_payload(T.spawn_op[k], self, P, A, b);
+      L[1 + k] = spawn_task(G, cg, b, words, g, idx);
+    }
+    r = false;
+    const uint32_t h = L[1 + k];
+    if (h != TASK_HANDLE_UNINIT && h != TASK_HANDLE_RESOLVED && poll_child(G, cg, h)) {
+      child = task_payload(G.g[cg], h);
+      L[1 + k] = TASK_HANDLE_RESOLVED;
+      r = true;
+    }
+  }
+  if (r) apply_map(T.map_op, self, child, A);
+  return r;
+}
+
+// The ray-trace task (trace_task.rs:150-360): the first poll traverses and
+// spawns the closest-hit or miss task of its trace call (resolving at once
+// when there is none to spawn); the task resolves in the poll that finds that
+// child finished, taking back the child's user payload.
+template <int MODE>
+__device__ bool poll_trace(const TaskGraphDev& G, uint32_t g, uint32_t idx, const TraceParams& P, uint2* stack,
+                           uint32_t stride) {
+  const TaskGroupDev& T = G.g[g];
+  uint32_t* L = task_locals(T, idx);
+  uint32_t* self = task_payload(T, idx);
+  if (L[6] == TRACE_SUB_NOT_SPAWNED) {
+    RayCtx R;
+    R.o = make_float3(__uint_as_float(self[0]), __uint_as_float(self[1]), __uint_as_float(self[2]));
+    R.tmin = __uint_as_float(self[3]);
+    R.d = make_float3(__uint_as_float(self[4]), __uint_as_float(self[5]), __uint_as_float(self[6]));
+    R.tmax = __uint_as_float(self[7]);
+    R.ray_flags = self[8];
+    R.cull_mask = self[9];
+    bool bad;
+    traverse_ray<MODE, false>(P, R, self[10], stack, stride, bad);
+    if (bad) atomicOr(P.error_word, 2u);
+    uint32_t b[kClosestWords];
+    for (uint32_t w = 0; w < kTraceCallWords; w++) b[w] = self[w];
+    uint32_t target = TRACE_SUB_NOT_SPAWNED, words = kTraceCallWords;
+    if (R.best.have) {
+      if (!(R.ray_flags & RAY_FLAG_SKIP_CLOSEST) && self[11] < G.n_groups &&
+          G.g[self[11]].payload_words >= kTraceCallWords) {
+        const uint4 gm = __ldg(reinterpret_cast<const uint4*>(P.tri_root + R.best.geom_slot));
+        const uint32_t tri = __ldg(P.redirect + R.best.k);
+        b[16] = tri;
+        b[17] = R.best.inst;
+        b[18] = __float_as_uint(R.best.t);
+        b[19] = __float_as_uint(R.best.u);
+        b[20] = __float_as_uint(R.best.v);
+        b[21] = R.best.s < 0.0f ? 0xFFu : 0xFEu;
+        b[22] = gm.y;
+        b[23] = tri - gm.z;
+        target = self[11];
+        words = kClosestWords;
+      }
+    } else if (self[12] < G.n_groups && G.g[self[12]].payload_words >= kTraceCallWords) {
+      target = self[12];
+    }
+    if (target != TRACE_SUB_NOT_SPAWNED) {
+      const uint32_t h = spawn_task(G, target, b, words, g, idx);
+      L[5] = target;
+      L[6] = h == TASK_HANDLE_UNINIT ? TRACE_SUB_SPAWN_FAILED : h;
+    }
+  }
+  bool resolved = false;
+  if (L[6] == TRACE_SUB_SPAWN_FAILED || L[6] == TRACE_SUB_NOT_SPAWNED) {
+    if (!L[7]) {
+      L[7] = 1u;
+      resolved = true;
+    }
+  }
+  if (!L[7]) {
+    const uint32_t cg = L[5], h = L[6];
+    if (poll_child(G, cg, h)) {
+      const uint32_t* cp = task_payload(G.g[cg], h);
+      for (uint32_t w = 0; w < 3; w++) self[kTraceUser + w] = cp[kTraceUser + w];
+      L[7] = 1u;
+      resolved = true;
+    }
+  }
+  return resolved;
+}
+
+template <int MODE, bool LOCAL>
+__global__ void __launch_bounds__(kPollThreads) poll_kernel(TaskGraphDev G, uint32_t g, TraceParams P, AoEnv A) {
+  RDN_TRAVERSAL_STACK(LOCAL);
+  const TaskGroupDev& T = G.g[g];
+  const GroupCtl* c = T.ctl;
+  const uint32_t n = c->active.size;
+  const uint32_t* list = T.active[c->sel];
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint32_t idx = list[i];
+    bool r;
+    if (T.program == TASK_PROGRAM_TRACE)
+      r = poll_trace<MODE>(G, g, idx, P, stack_ptr, stack_stride);
+    else
+      r = poll_chain(G, g, idx, P, A);
+    finalize(G, g, idx, r);
+  }
+}
+
+__device__ __forceinline__ uint32_t commit_alloc(uint32_t size, uint32_t bump, uint32_t cap) {
+  return bump > cap - size ? cap : size + bump;
+}
+__device__ __forceinline__ uint32_t commit_dealloc(uint32_t size, uint32_t bump) {
+  return bump > size ? 0u : size - bump;
+}
+
+// prepare_execution: commit the three bump lists, drain removed -> empty.
+__global__ void __launch_bounds__(256) drain_kernel(TaskGroupDev T, uint32_t* ticket) {
+  GroupCtl* c = T.ctl;
+  __shared__ uint32_t s_removed, s_empty, s_last;
+  if (threadIdx.x == 0) {
+    s_removed = commit_alloc(c->removed.size, c->removed.bump, T.cap);
+    s_empty = commit_dealloc(c->empty.size, c->empty.bump);
+  }
+  __syncthreads();
+  const uint32_t n = s_removed, off = s_empty;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    if (off + i < T.cap) T.empty[off + i] = T.removed[i];
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (s_last && threadIdx.x == 0) {
+    __threadfence();
+    c->active.size = commit_alloc(c->active.size, c->active.bump, T.cap);
+    c->active.bump = 0u;
+    c->empty.size = min(T.cap, off + n);
+    c->empty.bump = 0u;
+    c->removed.size = 0u;
+    c->removed.bump = 0u;
+    c->drain_n = n;
+    c->drain_off = off;
+    *ticket = 0u;
+  }
+}
+
+// dispatch_allocate_init_task's commits (active: allocate, empty: deallocate).
+__global__ void commit_spawn_kernel(TaskGroupDev T) {
+  GroupCtl* c = T.ctl;
+  c->active.size = commit_alloc(c->active.size, c->active.bump, T.cap);
+  c->active.bump = 0u;
+  c->empty.size = commit_dealloc(c->empty.size, c->empty.bump);
+  c->empty.bump = 0u;
+}
+
+__device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t* warp_sums) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+  if (lane == 0) warp_sums[warp] = v;
+  __syncthreads();
+  uint32_t t = 0;
+  for (uint32_t w = 0; w < blockDim.x / 32; w++) t += warp_sums[w];
+  __syncthreads();
+  return t;
+}
+
+// Commit of the active list and first half of the compaction
+// (ActiveTaskCompact); the last block scans the tile counts and writes the
+// new size.
+__global__ void __launch_bounds__(kCompactThreads) compact_count_kernel(TaskGroupDev T, uint32_t ntiles,
+                                                                        uint32_t* ticket) {
+  GroupCtl* c = T.ctl;
+  __shared__ uint32_t s_n, s_sel, s_last, warp_sums[kCompactThreads / 32];
+  if (threadIdx.x == 0) {
+    s_n = commit_alloc(c->active.size, c->active.bump, T.cap);
+    s_sel = c->sel;
+  }
+  __syncthreads();
+  const uint32_t n = s_n;
+  const uint32_t* list = T.active[s_sel];
+  uint32_t kept = 0;
+  const uint32_t base = blockIdx.x * kTile;
+  for (uint32_t j = 0; j < kTile / kCompactThreads; j++) {
+    const uint32_t i = base + j * kCompactThreads + threadIdx.x;
+    if (i < n) {
+      const uint32_t idx = list[i];
+      const uint32_t st = T.state[idx];
+      if (st == TASK_GO_TO_SLEEP) T.state[idx] = TASK_NOT_FINISHED_SLEEP;
+      kept += st == TASK_NOT_FINISHED_WAKEN;
+    }
+  }
+  const uint32_t total = block_sum(kept, warp_sums);
+  if (threadIdx.x == 0) T.tile_offsets[blockIdx.x] = total;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  // exclusive scan of the tile counts, kCompactThreads at a time
+  __shared__ uint32_t s_carry;
+  if (threadIdx.x == 0) s_carry = 0;
+  __syncthreads();
+  for (uint32_t b0 = 0; b0 < ntiles; b0 += kCompactThreads) {
+    const uint32_t t = b0 + threadIdx.x;
+    const uint32_t v = t < ntiles ? *((volatile uint32_t*)(T.tile_offsets + t)) : 0u;
+    uint32_t x = v;
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+      if (lane >= (uint32_t)o) x += y;
+    }
+    if (lane == 31) warp_sums[warp] = x;
+    __syncthreads();
+    uint32_t before = s_carry;
+    for (uint32_t w = 0; w < warp; w++) before += warp_sums[w];
+    if (t < ntiles) T.tile_offsets[t] = before + x - v;
+    __syncthreads();
+    if (threadIdx.x == kCompactThreads - 1) s_carry = before + x;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    c->compact_n = n;
+    c->src_sel = s_sel;
+    c->sel = s_sel ^ 1u;
+    c->active.size = s_carry;
+    c->active.bump = 0u;
+    *ticket = 0u;
+  }
+}
+
+// Second half of the compaction: kept indices, in order, to the other buffer.
+__global__ void __launch_bounds__(kCompactThreads) compact_scatter_kernel(TaskGroupDev T) {
+  const GroupCtl* c = T.ctl;
+  const uint32_t n = c->compact_n;
+  const uint32_t base = blockIdx.x * kTile;
+  if (base >= n) return;
+  const uint32_t* src = T.active[c->src_sel];
+  uint32_t* dst = T.active[c->src_sel ^ 1u];
+  __shared__ uint32_t warp_counts[kCompactThreads / 32];
+  uint32_t offset = T.tile_offsets[blockIdx.x];
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  for (uint32_t j = 0; j < kTile / kCompactThreads; j++) {
+    const uint32_t i = base + j * kCompactThreads + threadIdx.x;
+    uint32_t idx = 0;
+    bool keep = false;
+    if (i < n) {
+      idx = src[i];
+      keep = T.state[idx] == TASK_NOT_FINISHED_WAKEN;
+    }
+    const uint32_t ballot = __ballot_sync(0xFFFFFFFFu, keep);
+    if (lane == 0) warp_counts[warp] = __popc(ballot);
+    __syncthreads();
+    uint32_t before = offset;
+    for (uint32_t w = 0; w < warp; w++) before += warp_counts[w];
+    if (keep) dst[before + __popc(ballot & ((1u << lane) - 1u))] = idx;
+    uint32_t round = 0;
+    for (uint32_t w = 0; w < kCompactThreads / 32; w++) round += warp_counts[w];
+    __syncthreads();
+    offset += round;
+  }
+}
+
+// TaskGroupExecutorResource::init: empty pool = 1..cap, fallback task 0.
+__global__ void init_kernel(TaskGroupDev T) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < T.cap; i += gridDim.x * blockDim.x)
+    T.empty[i] = i + 1;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    GroupCtl* c = T.ctl;
+    c->empty.size = T.cap;
+    T.state[0] = TASK_NOT_FINISHED_WAKEN;
+    T.parent_index[0] = TASK_NO_PARENT;
+    T.parent_type[0] = TASK_NO_PARENT;
+    uint32_t* L = T.locals;
+    for (uint32_t k = 0; k < kTaskMaxSpawns; k++) L[1 + k] = TASK_HANDLE_UNINIT;
+    L[5] = L[6] = TRACE_SUB_NOT_SPAWNED;
+  }
+}
+
+__global__ void spawn_init_kernel(TaskGraphDev G, uint32_t g, uint32_t count, uint32_t init_op) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+    const uint32_t v = i;
+    spawn_task(G, g, &v, init_op == TASK_INIT_INDEX ? 1u : 0u, TASK_NO_PARENT, TASK_NO_PARENT);
+  }
+}
+
+uint32_t tiles_of(uint32_t cap) { return (cap + kTile - 1) / kTile; }
+
+template <int MODE, bool LOCAL>
+cudaError_t launch_poll(const TaskGraphDev& G, uint32_t g, const TraceParams& P, const AoEnv& A, uint32_t grid,
+                        cudaStream_t st) {
+  const size_t smem = MODE != MODE_THREADED && !LOCAL ? (size_t)P.stack_depth * kPollThreads * sizeof(uint2) : 0;
+  static bool attr_done = false;
+  if (!attr_done) {
+    cudaError_t e =
+        cudaFuncSetAttribute(poll_kernel<MODE, LOCAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e != cudaSuccess) return e;
+    attr_done = true;
+  }
+  poll_kernel<MODE, LOCAL><<<grid, kPollThreads, smem, st>>>(G, g, P, A);
+  return cudaGetLastError();
+}
+
+bool op_reads_trace_payload(uint32_t op) {
+  return op == TASK_MAP_AO_ACCUMULATE || op == TASK_MAP_STORE_CHILD;
+}
+
+}  // namespace
+
+TaskGraph::~TaskGraph() {
+  for (void* p : allocs_) cudaFree(p);
+}
+
+std::string TaskGraph::create(const std::vector<TaskGroupDesc>& groups, uint32_t capacity, int sm_count,
+                              cudaStream_t st) {
+  const uint32_t n = (uint32_t)groups.size();
+  if (n == 0 || n > kTaskMaxGroups) return "a task graph holds 1 to 16 task groups";
+  if (capacity == 0) return "capacity must be at least 1";
+  for (uint32_t g = 0; g < n; g++) {
+    const TaskGroupDesc& d = groups[g];
+    if (d.program > TASK_PROGRAM_TRACE) return "unknown task program";
+    if (d.max_in_flight == 0) return "max_in_flight must be at least 1";
+    if ((uint64_t)d.max_in_flight * capacity >= (1ull << 28)) return "max_in_flight * capacity too large";
+    if (d.payload_words == 0 || d.payload_words > kTaskMaxPayloadWords) return "payload_words must be 1..32";
+    if (d.program == TASK_PROGRAM_TRACE && d.payload_words < kTraceCallWords)
+      return "a trace task needs a payload of at least 16 words";
+    if (d.n_spawn > kTaskMaxSpawns) return "a chain has at most 4 spawn stages";
+    if (d.map_op > TASK_MAP_STORE_ONE) return "unknown map operation";
+    const uint32_t* last_child = nullptr;
+    for (uint32_t k = 0; k < d.n_spawn; k++) {
+      if (d.spawn_type[k] >= n) return "spawn stage names a task group that does not exist";
+      if (d.spawn_op[k] > TASK_SPAWN_AO_OCCLUSION) return "unknown spawn payload operation";
+      const TaskGroupDesc& cd = groups[d.spawn_type[k]];
+      if (d.spawn_op[k] != TASK_SPAWN_ZERO && cd.program != TASK_PROGRAM_TRACE)
+        return "a trace-call payload must go to a trace task group";
+      if (d.spawn_op[k] == TASK_SPAWN_AO_OCCLUSION && d.payload_words < kClosestWords)
+        return "the occlusion-ray stage reads a closest-hit payload of 24 words";
+      last_child = &d.spawn_type[k];
+    }
+    if (op_reads_trace_payload(d.map_op)) {
+      if (!last_child || groups[*last_child].payload_words < kTraceCallWords)
+        return "the map operation reads the user payload of a trace-call child";
+    }
+    if ((d.map_op == TASK_MAP_STORE_CHILD || d.map_op == TASK_MAP_STORE_ZERO || d.map_op == TASK_MAP_STORE_ONE) &&
+        d.payload_words < kTraceCallWords)
+      return "the map operation writes a trace-call user payload (16 words)";
+  }
+  desc_ = groups;
+  sm_count_ = sm_count > 0 ? sm_count : 1;
+  std::memset(&dev_, 0, sizeof(dev_));
+  dev_.n_groups = n;
+  // control blocks + error word + per-group tickets (2 per group)
+  void* ctl = nullptr;
+  cudaError_t e = cudaMalloc(&ctl, sizeof(GroupCtl) * n + 256);
+  if (e != cudaSuccess) return std::string("cudaMalloc: ") + cudaGetErrorString(e);
+  allocs_.push_back(ctl);
+  e = cudaMemsetAsync(ctl, 0, sizeof(GroupCtl) * n + 256, st);
+  if (e != cudaSuccess) return std::string("cudaMemsetAsync: ") + cudaGetErrorString(e);
+  GroupCtl* ctls = static_cast<GroupCtl*>(ctl);
+  dev_.error = reinterpret_cast<uint32_t*>(ctls + n);
+  for (uint32_t g = 0; g < n; g++) {
+    const TaskGroupDesc& d = groups[g];
+    TaskGroupDev& T = dev_.g[g];
+    T.cap = d.max_in_flight * capacity;
+    T.payload_words = d.payload_words;
+    T.program = d.program;
+    T.n_spawn = d.n_spawn;
+    T.map_op = d.map_op;
+    for (uint32_t k = 0; k < kTaskMaxSpawns; k++) {
+      T.spawn_type[k] = d.spawn_type[k];
+      T.spawn_op[k] = d.spawn_op[k];
+    }
+    const size_t rec = (size_t)T.cap + 1;
+    const size_t words = rec * 3 + rec * d.payload_words + rec * kTaskLocalWords + (size_t)T.cap * 4 +
+                         tiles_of(T.cap) + 64;
+    void* mem = nullptr;
+    e = cudaMalloc(&mem, words * 4);
+    if (e != cudaSuccess) return std::string("cudaMalloc: ") + cudaGetErrorString(e);
+    allocs_.push_back(mem);
+    e = cudaMemsetAsync(mem, 0, words * 4, st);
+    if (e != cudaSuccess) return std::string("cudaMemsetAsync: ") + cudaGetErrorString(e);
+    uint32_t* w = static_cast<uint32_t*>(mem);
+    T.state = w;
+    w += rec;
+    T.parent_type = w;
+    w += rec;
+    T.parent_index = w;
+    w += rec;
+    T.payload = w;
+    w += rec * d.payload_words;
+    T.locals = w;
+    w += rec * kTaskLocalWords;
+    T.active[0] = w;
+    w += T.cap;
+    T.active[1] = w;
+    w += T.cap;
+    T.removed = w;
+    w += T.cap;
+    T.empty = w;
+    w += T.cap;
+    T.tile_offsets = w;
+    T.ctl = ctls + g;
+    const uint32_t grid = std::min<uint32_t>((T.cap + 255) / 256, (uint32_t)sm_count_ * 8);
+    init_kernel<<<grid, 256, 0, st>>>(T);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return std::string("init launch: ") + cudaGetErrorString(e);
+  }
+  return "";
+}
+
+cudaError_t TaskGraph::prepare(uint32_t g, cudaStream_t st) {
+  const TaskGroupDev& T = dev_.g[g];
+  const uint32_t grid = std::max<uint32_t>(1, std::min<uint32_t>((T.cap + 255) / 256, (uint32_t)sm_count_ * 4));
+  drain_kernel<<<grid, 256, 0, st>>>(T, dev_.error + 2 + 2 * g);
+  return cudaGetLastError();
+}
+
+cudaError_t TaskGraph::compact(uint32_t g, cudaStream_t st) {
+  const TaskGroupDev& T = dev_.g[g];
+  const uint32_t nt = tiles_of(T.cap);
+  compact_count_kernel<<<nt, kCompactThreads, 0, st>>>(T, nt, dev_.error + 3 + 2 * g);
+  compact_scatter_kernel<<<nt, kCompactThreads, 0, st>>>(T);
+  return cudaGetLastError();
+}
+
+cudaError_t TaskGraph::poll(uint32_t g, const TraceParams* p, int mode, const AoEnv* ao, cudaStream_t st) {
+  const TaskGroupDev& T = dev_.g[g];
+  const uint32_t grid =
+      std::max<uint32_t>(1, std::min<uint32_t>((T.cap + kPollThreads - 1) / kPollThreads, (uint32_t)sm_count_ * 8));
+  TraceParams P;
+  AoEnv A;
+  if (p)
+    P = *p;
+  else
+    std::memset(&P, 0, sizeof(P));
+  if (ao)
+    A = *ao;
+  else
+    std::memset(&A, 0, sizeof(A));
+  if (T.program != TASK_PROGRAM_TRACE || !p) return launch_poll<MODE_THREADED, false>(dev_, g, P, A, grid, st);
+  if (mode == MODE_WIDE4)
+    return P.local_stack ? launch_poll<MODE_WIDE4, true>(dev_, g, P, A, grid, st)
+                         : launch_poll<MODE_WIDE4, false>(dev_, g, P, A, grid, st);
+  if (mode == MODE_BINARY)
+    return P.local_stack ? launch_poll<MODE_BINARY, true>(dev_, g, P, A, grid, st)
+                         : launch_poll<MODE_BINARY, false>(dev_, g, P, A, grid, st);
+  return launch_poll<MODE_THREADED, false>(dev_, g, P, A, grid, st);
+}
+
+cudaError_t TaskGraph::dispatch_init(uint32_t group, uint32_t count, uint32_t init_op, cudaStream_t st) {
+  cudaError_t e = prepare(group, st);
+  if (e != cudaSuccess || count == 0) return e;
+  const uint32_t grid = std::min<uint32_t>((count + 255) / 256, (uint32_t)sm_count_ * 8);
+  spawn_init_kernel<<<grid, 256, 0, st>>>(dev_, group, count, init_op);
+  commit_spawn_kernel<<<1, 1, 0, st>>>(dev_.g[group]);
+  return cudaGetLastError();
+}
+
+cudaError_t TaskGraph::execute(uint32_t rounds, const TraceParams* p, int mode, const AoEnv* ao, cudaStream_t st) {
+  for (uint32_t r = 0; r < rounds; r++) {
+    for (uint32_t g = 0; g < dev_.n_groups; g++) {
+      cudaError_t e = prepare(g, st);
+      if (e == cudaSuccess) e = poll(g, p, mode, ao, st);
+      if (e == cudaSuccess) e = compact(g, st);
+      if (e != cudaSuccess) return e;
+    }
+  }
+  return cudaSuccess;
+}
+
+cudaError_t TaskGraph::states(uint32_t* wake, uint32_t* empty, cudaStream_t st) {
+  for (uint32_t g = 0; g < dev_.n_groups; g++) {
+    cudaError_t e = prepare(g, st);
+    if (e == cudaSuccess) e = compact(g, st);
+    if (e != cudaSuccess) return e;
+  }
+  std::vector<GroupCtl> h(dev_.n_groups);
+  cudaError_t e =
+      cudaMemcpyAsync(h.data(), dev_.g[0].ctl, sizeof(GroupCtl) * dev_.n_groups, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return e;
+  for (uint32_t g = 0; g < dev_.n_groups; g++) {
+    wake[g] = h[g].active.size;
+    empty[g] = h[g].empty.size;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t TaskGraph::debug(uint32_t group, std::vector<uint32_t>& active, std::vector<uint32_t>& empty,
+                             std::vector<uint32_t>& task_states, cudaStream_t st) {
+  for (uint32_t g = 0; g < dev_.n_groups; g++) {
+    cudaError_t e = prepare(g, st);
+    if (e == cudaSuccess) e = compact(g, st);
+    if (e != cudaSuccess) return e;
+  }
+  const TaskGroupDev& T = dev_.g[group];
+  GroupCtl h;
+  cudaError_t e = cudaMemcpyAsync(&h, T.ctl, sizeof(h), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return e;
+  active.assign(h.active.size, 0);
+  empty.assign(h.empty.size, 0);
+  task_states.assign((size_t)T.cap + 1, 0);
+  if (h.active.size)
+    e = cudaMemcpyAsync(active.data(), T.active[h.sel], 4 * (size_t)h.active.size, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess && h.empty.size)
+    e = cudaMemcpyAsync(empty.data(), T.empty, 4 * (size_t)h.empty.size, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(task_states.data(), T.state, 4 * ((size_t)T.cap + 1), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  return e;
+}
+
+cudaError_t TaskGraph::read_error(uint32_t* flags, cudaStream_t st) {
+  cudaError_t e = cudaMemcpyAsync(flags, dev_.error, 4, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  return e;
+}
+
+}  // namespace rdn

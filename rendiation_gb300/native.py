@@ -28,7 +28,10 @@ EXPORTED_SYMBOLS = [
     "rdn_graph_launch", "rdn_graph_destroy", "rdn_attr_loss_forward", "rdn_attr_loss_adjoint",
     "rdn_scan_scratch_size", "rdn_scan_u32", "rdn_compact_scratch_size", "rdn_compact_u32",
     "rdn_radix_sort_scratch_size", "rdn_radix_sort_u32", "rdn_attr_paths_forward", "rdn_attr_paths_adjoint",
-    "rdn_attr_paths_graph", "rdn_check_errors", "rdn_set_iteration_limit",
+    "rdn_attr_paths_graph", "rdn_check_errors", "rdn_set_iteration_limit", "rdn_task_graph_create",
+    "rdn_task_graph_destroy", "rdn_task_graph_dispatch_init", "rdn_task_graph_execute", "rdn_task_graph_states",
+    "rdn_task_graph_debug", "rdn_task_graph_check_errors", "rdn_ao_pipeline_create", "rdn_ao_render_graph",
+    "rdn_ao_render",
 ]
 
 
@@ -119,6 +122,19 @@ class AttrPathDesc(C.Structure):
                 ("seg_inst", C.c_void_p), ("local_stack", C.c_uint32), ("speculation", C.c_uint32)]
 
 
+class TaskGroupDesc(C.Structure):
+    _fields_ = [("program", C.c_uint32), ("max_in_flight", C.c_uint32), ("payload_words", C.c_uint32),
+                ("n_spawn", C.c_uint32), ("spawn_type", C.c_uint32 * 4), ("spawn_op", C.c_uint32 * 4),
+                ("map_op", C.c_uint32)]
+
+
+class AoDesc(C.Structure):
+    _fields_ = [("view_projection_inv", C.c_float * 16), ("camera_position", C.c_float * 3), ("width", C.c_uint32),
+                ("height", C.c_uint32), ("sample_count", C.c_uint32), ("tlas_uniform", C.c_uint32),
+                ("traversal", C.c_uint32), ("normals", C.c_void_p), ("image", C.c_void_p),
+                ("sbt_closest", C.c_uint32 * 2), ("sbt_miss", C.c_uint32), ("pad", C.c_uint32)]
+
+
 _lib = None
 
 
@@ -196,5 +212,25 @@ def lib() -> C.CDLL:
         getattr(L, name).restype = i32
     L.rdn_attr_paths_graph.argtypes = [vp, C.POINTER(AttrPathDesc), C.c_uint64, C.POINTER(vp)]
     L.rdn_attr_paths_graph.restype = i32
+    L.rdn_task_graph_create.argtypes = [vp, C.POINTER(TaskGroupDesc), u32, u32, vp, C.POINTER(vp)]
+    L.rdn_task_graph_create.restype = i32
+    L.rdn_task_graph_destroy.argtypes = [vp]
+    L.rdn_task_graph_destroy.restype = i32
+    L.rdn_task_graph_dispatch_init.argtypes = [vp, u32, u32, u32, vp]
+    L.rdn_task_graph_dispatch_init.restype = i32
+    L.rdn_task_graph_execute.argtypes = [vp, u32, C.POINTER(AoDesc), vp]
+    L.rdn_task_graph_execute.restype = i32
+    L.rdn_task_graph_states.argtypes = [vp, vp, vp, vp, vp]
+    L.rdn_task_graph_states.restype = i32
+    L.rdn_task_graph_debug.argtypes = [vp, u32, vp, C.POINTER(u32), vp, C.POINTER(u32), vp, vp]
+    L.rdn_task_graph_debug.restype = i32
+    L.rdn_task_graph_check_errors.argtypes = [vp, vp, C.POINTER(u32)]
+    L.rdn_task_graph_check_errors.restype = i32
+    L.rdn_ao_pipeline_create.argtypes = [vp, u32, u32, vp, C.POINTER(vp)]
+    L.rdn_ao_pipeline_create.restype = i32
+    L.rdn_ao_render_graph.argtypes = [vp, C.POINTER(AoDesc), vp]
+    L.rdn_ao_render_graph.restype = i32
+    L.rdn_ao_render.argtypes = [vp, C.POINTER(AoDesc), vp]
+    L.rdn_ao_render.restype = i32
     _lib = L
     return L

@@ -1,0 +1,135 @@
+"""Ray-traced ambient occlusion (the reference's feature/ao.rs pipeline):
+the fused kernel and the five-group task-graph pipeline against the AO oracle
+over several progressive samples. Reference traversal order: every texel
+bit-identical; the four-child walk: identical except texels where an
+exact-distance tie picks another triangle of the camera ray."""
+
+import numpy as np
+import pytest
+
+from helpers import Scene, mat4_cols, orc, rot_z, single_mesh_scene
+from rendiation_gb300 import raytracing as rt
+from rendiation_gb300 import scenes
+from rendiation_gb300 import task_graph as tg
+
+pytestmark = pytest.mark.gpu
+
+W, H = 96, 72
+# hammersley(sample, 256) points along the normal for the first samples; later
+# ones reach grazing directions, where the rough field occludes
+SAMPLES = (150, 200, 250)
+
+
+def camera():
+    eye = (0.5, -0.45, 0.75)
+    vp = tg.look_at_view_projection_inv(eye, (0.5, 0.5, 0.0), (0, 0, 1), 45.0, W / H, 0.01, 100.0)
+    return vp, np.asarray(eye, np.float32)
+
+
+def vertex_normals(mesh):
+    p = mesh.positions.astype(np.float64)
+    t = mesh.indices.reshape(-1, 3)
+    fn = np.cross(p[t[:, 1]] - p[t[:, 0]], p[t[:, 2]] - p[t[:, 0]])
+    n = np.zeros_like(p)
+    for k in range(3):
+        np.add.at(n, t[:, k], fn)
+    n /= np.linalg.norm(n, axis=1, keepdims=True)
+    return n.astype(np.float32)
+
+
+def run_oracle(scene, samples, normals=None):
+    S = scene.build_oracle()
+    vp, eye = camera()
+    img = np.zeros(W * H, np.uint32)
+    for s in samples:
+        orc.ao_render(S, vp, eye, W, H, img, sample_count=s, normals=normals, threads=8)
+    return img
+
+
+def run_gpu(scene, samples, traversal, mode, normals=None):
+    import torch
+
+    P = scene.build_product()
+    vp, eye = camera()
+    nt = None if normals is None else torch.from_numpy(normals.reshape(-1)).cuda()
+    ao = tg.AmbientOcclusion(P, W, H, vp, eye, traversal=traversal, normals=nt, mode=mode)
+    for s in samples:
+        ao.sample_count = s
+        ao.render()
+    torch.cuda.synchronize()
+    flags = P.check_errors()
+    img = ao.result().reshape(-1, 4)
+    packed = (img[:, 0].astype(np.uint32) | (img[:, 1].astype(np.uint32) << 8) | (img[:, 2].astype(np.uint32) << 16)
+              | (img[:, 3].astype(np.uint32) << 24))
+    return packed, ao, flags
+
+
+def field_mesh():
+    return scenes.heightfield(48, seed=3, jitter_sigma=0.02)
+
+
+def field_scene():
+    return single_mesh_scene(field_mesh())
+
+
+@pytest.mark.parametrize("mode", ["fused", "graph"])
+@pytest.mark.parametrize("with_normals", [False, True])
+def test_reference_order_is_bit_identical_to_the_oracle(cuda, mode, with_normals):
+    mesh = field_mesh()
+    normals = vertex_normals(mesh) if with_normals else None
+    scene = single_mesh_scene(mesh)
+    want = run_oracle(scene, SAMPLES, normals)
+    got, ao, flags = run_gpu(scene, SAMPLES, rt.TRAVERSAL_REFERENCE, mode, normals)
+    assert flags == (0, 0)
+    assert np.array_equal(got, want)
+    # starting from 0 at sample 150 the bytes encode each pixel's three payloads
+    v = want & 0xFF
+    assert len(np.unique(v)) >= 3 and 0.005 < (v == 0).mean() < 0.5
+    if mode == "graph":
+        assert ao.graph.read_back_execution_states().is_empty()
+        assert ao.graph.check_errors() == 0
+
+
+@pytest.mark.parametrize("mode", ["fused", "graph"])
+def test_four_child_walk_matches_except_ties(cuda, mode):
+    scene = field_scene()
+    want = run_oracle(scene, SAMPLES)
+    got, _, flags = run_gpu(scene, SAMPLES, rt.TRAVERSAL_ORDERED_WIDE, mode)
+    assert flags == (0, 0)
+    assert (got == want).mean() > 0.995
+
+
+def test_graph_equals_fused(cuda):
+    scene = field_scene()
+    for traversal in (rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_WIDE):
+        a, _, _ = run_gpu(scene, SAMPLES, traversal, "fused")
+        b, _, _ = run_gpu(scene, SAMPLES, traversal, "graph")
+        assert np.array_equal(a, b)
+
+
+def test_instanced_scene_with_transforms(cuda):
+    a = scenes.heightfield(32, seed=5)
+    b = scenes.heightfield(24, seed=6)
+    t0 = mat4_cols(rot_z(0.3), (0.6, 0.6, 0.6), (0.1, 0.0, 0.0))
+    t1 = mat4_cols(rot_z(-0.2), (-0.5, 0.5, 0.7), (0.9, 0.3, 0.02))  # mirrored
+    scene = Scene([[(a.positions, a.indices, 1)], [(b.positions, b.indices, 1)]],
+                  [[{"blas": 0, "transform": t0}, {"blas": 1, "transform": t1}]])
+    want = run_oracle(scene, SAMPLES)
+    got, _, _ = run_gpu(scene, SAMPLES, rt.TRAVERSAL_REFERENCE, "fused")
+    assert np.array_equal(got, want)
+
+
+def test_frozen_after_256_samples(cuda):
+    import torch
+
+    scene = field_scene()
+    P = scene.build_product()
+    vp, eye = camera()
+    ao = tg.AmbientOcclusion(P, W, H, vp, eye, traversal=rt.TRAVERSAL_ORDERED_WIDE)
+    ao.image.fill_(200)
+    ao.sample_count = 256
+    before = ao.result().copy()
+    ao.render()
+    torch.cuda.synchronize()
+    assert np.array_equal(ao.result()[..., :3], before[..., :3])
+    assert np.all(ao.result()[..., 3] == 255)
