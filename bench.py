@@ -487,6 +487,98 @@ def oracle_heightfield(mesh):
     return S
 
 
+def bench_ao(args, P, S_field):
+    """Ray-traced ambient occlusion of the reference (feature/ao.rs) on the
+    1024^2 heightfield: a 512x512 frame (the reference clamps AO frames to
+    512^2 pixels), one jittered camera ray per pixel and one occlusion ray per
+    hit, progressive average into RGBA8. The fused kernel against the
+    reference's pipeline as a device task graph (5 task groups, 8 rounds),
+    issued as plain launches and replayed from a captured CUDA graph. The
+    sample index advances every frame."""
+    import ctypes as C
+
+    import torch
+
+    from rendiation_gb300 import native
+    from rendiation_gb300 import raytracing as rt
+    from rendiation_gb300 import task_graph as tg
+
+    L = native.lib()
+    W = H = 512
+    eye = (0.5, -0.5, 0.8)
+    vp = tg.look_at_view_projection_inv(eye, (0.5, 0.5, 0.0), (0, 0, 1), 20.0, 1.0, 0.01, 100.0)
+    # coherent camera rays: the four-child walk unless the reference order is asked for
+    traversal = rt.TRAVERSAL_REFERENCE if args.traversal == "reference" else rt.TRAVERSAL_ORDERED_WIDE
+    stream = torch.cuda.current_stream()
+    sp = C.c_void_p(stream.cuda_stream)
+    counts = torch.zeros(2, dtype=torch.int32, device="cuda")
+    images = {m: torch.zeros(W * H * 4, dtype=torch.uint8, device="cuda") for m in ("fused", "graph")}
+    descs = {m: tg.ao_desc(W, H, vp, eye, images[m], 0, 0, traversal) for m in images}
+    for d in descs.values():
+        d.ray_counts = counts.data_ptr()
+    h = C.c_void_p()
+    assert L.rdn_ao_pipeline_create(P._h, W, H, sp, C.byref(h)) == 0
+
+    def frame(mode, s):
+        d = descs[mode]
+        d.sample_count = s % 256
+        if mode == "fused":
+            assert L.rdn_ao_render(P._h, C.byref(d), sp) == 0
+        else:
+            assert L.rdn_ao_render_graph(h, C.byref(d), sp) == 0
+
+    # one frame each from a zero image: the two forms must write the same bytes
+    frame("fused", 0)
+    frame("graph", 0)
+    torch.cuda.synchronize()
+    out = {"images_equal": bool(torch.equal(images["fused"], images["graph"]))}
+    reps = 20
+
+    def timed(fn):
+        for k in range(args.warmup):
+            fn(k)
+        counts.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for k in range(reps):
+            fn(args.warmup + k)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        c = counts.cpu().numpy()
+        return e0.elapsed_time(e1) / reps, (int(c[0]) + int(c[1])) / reps
+
+    ms, rays = timed(lambda k: frame("fused", k))
+    out["rays_per_frame"] = rays
+    out["fused_ms"], out["fused_mrays"] = round(ms, 4), round(rays / ms / 1e3, 1)
+    ms, rays_g = timed(lambda k: frame("graph", k))
+    out["graph_ms"], out["graph_mrays"] = round(ms, 4), round(rays_g / ms / 1e3, 1)
+    # the task-graph frame captured once, replayed
+    g = torch.cuda.CUDAGraph()
+    descs["graph"].sample_count = 7
+    with torch.cuda.graph(g):
+        assert L.rdn_ao_render_graph(h, C.byref(descs["graph"]), C.c_void_p(torch.cuda.current_stream().cuda_stream)) == 0
+    ms, rays_c = timed(lambda k: g.replay())
+    out["graph_captured_ms"], out["graph_captured_mrays"] = round(ms, 4), round(rays_c / ms / 1e3, 1)
+    out["graph_over_fused"] = round(out["graph_ms"] / out["fused_ms"], 2)
+    out["graph_launches_per_frame"] = 3 + 8 * 5 * 4
+    st, flags = P.check_errors()
+    assert st == 0 and flags == 0
+    L.rdn_task_graph_destroy(h)
+    if S_field is not None:
+        from oracle import orc
+
+        img = np.zeros(W * H, np.uint32)
+        rows = (0, 64)
+        n, sec = orc.ao_render(S_field, vp, eye, W, H, img, sample_count=0, rows=rows, threads=os.cpu_count() or 1)
+        out["cpu_mrays"] = round((n[0] + n[1]) / sec / 1e6, 2)
+        out["cpu_threads"] = os.cpu_count() or 1
+        out["cpu_sample"] = f"rows {rows[0]}..{rows[1]} of the frame"
+    out["traversal"] = {rt.TRAVERSAL_REFERENCE: "reference", rt.TRAVERSAL_ORDERED_WIDE: "wide"}.get(traversal, "ordered")
+    out["workload"] = (f"heightfield 1024^2 (2093058 tris), AO {W}x{H}: camera ray + occlusion ray per hit "
+                       "(ACCEPT_FIRST_HIT_AND_END_SEARCH, [0.01, 100])")
+    return out
+
+
 def bench_batched(args):
     """Batched multi-scene paths: 256 soups (log-uniform 1k..200k triangles),
     log-uniform 4k..256k rays per scene, <= 4 diffuse bounces with Russian
@@ -1081,6 +1173,7 @@ def main():
     ap.add_argument("--no-tune", dest="tune", action="store_false", help="skip the launch autotuner")
     ap.add_argument("--tune-cache", default=None, help="JSON file that keeps the autotuner's choices between runs")
     ap.add_argument("--no-batched-adjoint", action="store_true")
+    ap.add_argument("--no-ao", action="store_true", help="skip the ambient-occlusion leg")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP32-vs-FP64 accuracy check")
     ap.add_argument("--diff-scenes", type=int, default=64)
     ap.add_argument("--scenes", type=int, default=256)
@@ -1105,6 +1198,8 @@ def main():
     S_field = oracle_heightfield(mesh) if rank == 0 and not (args.no_accuracy and args.no_cpu_baseline) else None
     if S_field is not None and not args.no_accuracy:
         out["accuracy_vs_fp64"] = accuracy_vs_fp64(P, S_field, cam)
+    if not args.no_ao:
+        out["ao"] = bench_ao(args, P, S_field if not args.no_cpu_baseline else None)
     if not args.no_batched:
         P.close()
         out["batched"] = bench_batched(args)

@@ -602,6 +602,7 @@ typedef struct rdn_ao_desc {
   uint32_t sbt_closest[2];        /* task graphs: closest-hit group of the camera and the occlusion ray */
   uint32_t sbt_miss;              /* task graphs: miss group of both rays */
   uint32_t pad;
+  uint32_t* ray_counts;           /* device, nullable: [camera, occlusion] rays traced, added to */
 } rdn_ao_desc;
 
 typedef struct rdn_task_graph rdn_task_graph;
@@ -628,9 +629,12 @@ rdn_status rdn_task_graph_check_errors(rdn_task_graph* graph, void* stream, uint
 
 /* The reference's AO pipeline as a task graph (feature/ao.rs:162-313 on
  * trace_ray): group 0 ray-trace task (max_in_flight 2), 1 ray generation,
- * 2 primary closest hit, 3 occlusion closest hit, 4 miss; capacity =
- * width * height. rdn_ao_render_graph dispatches one ray-generation task per
- * pixel and runs 8 rounds (the reference's execution_round_hint). */
+ * 2 primary closest hit, 3 occlusion closest hit, 4 miss; capacity = the
+ * frame rounded up to whole 8x4 pixel tiles. rdn_ao_render_graph dispatches
+ * one ray-generation task per pixel of those tiles (32 consecutive tasks per
+ * tile, so that a warp traces neighbouring pixels; tasks past the frame
+ * resolve without tracing) and runs 8 rounds (the reference's
+ * execution_round_hint). */
 rdn_status rdn_ao_pipeline_create(rdn_ctx* ctx, uint32_t width, uint32_t height, void* stream,
                                   rdn_task_graph** out);
 rdn_status rdn_ao_render_graph(rdn_task_graph* graph, const rdn_ao_desc* desc, void* stream);

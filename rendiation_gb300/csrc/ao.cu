@@ -18,10 +18,8 @@ using namespace dev;
 template <int MODE, bool LOCAL>
 __global__ void __launch_bounds__(128) ao_kernel(TraceParams P, AoEnv A) {
   RDN_TRAVERSAL_STACK(LOCAL);
-  const uint32_t tiles_x = (A.width + 7) / 8;
-  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
-  const uint32_t x = (warp % tiles_x) * 8 + (lane & 7u), y = (warp / tiles_x) * 4 + (lane >> 3);
-  if (x >= A.width || y >= A.height) return;
+  uint32_t x, y;
+  if (!ao_pixel(A, blockIdx.x * blockDim.x + threadIdx.x, x, y)) return;
   float3 o, d;
   ao_camera_ray(A, x, y, o, d);
   RayCtx R;
@@ -51,13 +49,14 @@ __global__ void __launch_bounds__(128) ao_kernel(TraceParams P, AoEnv A) {
     payload = S.best.have ? 0.0f : 1.0f;  // secondary closest hit: occluded
   }
   if (bad) atomicOr(P.error_word, 2u);
+  ao_count(A, 0, true);
+  ao_count(A, 1, R.best.have);
   ao_accumulate(A, y * A.width + x, payload);
 }
 
 template <int MODE, bool LOCAL>
 cudaError_t launch_variant(const TraceParams& p, const AoEnv& a, cudaStream_t st) {
-  const uint32_t warps = ((a.width + 7) / 8) * ((a.height + 3) / 4);
-  const uint32_t grid = (warps * 32 + 127) / 128;
+  const uint32_t grid = (ao_dispatch_count(a.width, a.height) + 127) / 128;
   const size_t smem = MODE != MODE_THREADED && !LOCAL ? (size_t)p.stack_depth * 128 * sizeof(uint2) : 0;
   static bool attr_done = false;
   if (!attr_done) {

@@ -47,6 +47,16 @@ __device__ __forceinline__ void sincos_reduced(float phi, float& s, float& c) {
   }
 }
 
+// Pixel of dispatch index i: each run of 32 indices covers an 8x4 tile, tiles
+// in row order (a warp traces one tile). Indices of the tiles' overhang past
+// the frame return false.
+__device__ __forceinline__ bool ao_pixel(const AoEnv& A, uint32_t i, uint32_t& x, uint32_t& y) {
+  const uint32_t tiles_x = (A.width + 7) / 8, t = i >> 5, lane = i & 31u;
+  x = (t % tiles_x) * 8 + (lane & 7u);
+  y = (t / tiles_x) * 4 + (lane >> 3);
+  return x < A.width && y < A.height;
+}
+
 // Mat4 * (x, y, z, w), Mat4 in the reference's column order.
 __device__ __forceinline__ float4 mat4_mul(const float* m, float x, float y, float z, float w) {
   return make_float4(x * m[0] + y * m[4] + z * m[8] + w * m[12], x * m[1] + y * m[5] + z * m[9] + w * m[13],
@@ -129,6 +139,14 @@ __device__ __forceinline__ float3 ao_direction(float3 n, uint32_t sample) {
   const float3 bt = normalize3(make_float3(b, sign + n.y * n.y * a, -n.y));
   return make_float3(t.x * lx + bt.x * ly + n.x * lz, t.y * lx + bt.y * ly + n.y * lz,
                      t.z * lx + bt.z * ly + n.z * lz);
+}
+
+// Adds the lanes that want it to counter k of the AO ray counts, one atomic per warp.
+__device__ __forceinline__ void ao_count(const AoEnv& A, uint32_t k, bool want) {
+  if (!A.ray_counts) return;
+  const uint32_t active = __activemask();
+  const uint32_t mask = __ballot_sync(active, want);
+  if ((threadIdx.x & 31u) == (uint32_t)(__ffs(active) - 1) && mask) atomicAdd(A.ray_counts + k, __popc(mask));
 }
 
 __device__ __forceinline__ uint32_t to_unorm8(float x) {

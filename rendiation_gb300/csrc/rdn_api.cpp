@@ -1137,6 +1137,7 @@ rdn_status ao_env(rdn_ctx* c, const rdn_ao_desc* d, rdn::TraceParams& p, rdn::Ao
   a.vertices = c->dev.vertices.ptr;
   a.n_instances = (uint32_t)c->dev.tlas_data.count;
   a.n_triangles = (uint32_t)(c->dev.indices.count / 3);
+  a.ray_counts = d->ray_counts;
   return RDN_OK;
 }
 
@@ -1292,7 +1293,8 @@ rdn_status rdn_ao_pipeline_create(rdn_ctx* c, uint32_t width, uint32_t height, v
   g[4].max_in_flight = 1;
   g[4].payload_words = 16;
   g[4].map_op = RDN_TASK_MAP_STORE_ONE;
-  rdn_status st = rdn_task_graph_create(c, g, 5, width * height, stream, out);
+  // one ray-generation task per dispatch index, 8x4 pixel tiles (ao_pixel)
+  rdn_status st = rdn_task_graph_create(c, g, 5, rdn::ao_dispatch_count(width, height), stream, out);
   if (st != RDN_OK) return st;
   (*out)->ao_pipeline = true;
   (*out)->width = width;
@@ -1310,7 +1312,8 @@ rdn_status rdn_ao_render_graph(rdn_task_graph* g, const rdn_ao_desc* d, void* st
   env.sbt_closest[0] = 2;
   env.sbt_closest[1] = 3;
   env.sbt_miss = 4;
-  rdn_status st = rdn_task_graph_dispatch_init(g, 1, d->width * d->height, RDN_TASK_INIT_INDEX, stream);
+  rdn_status st =
+      rdn_task_graph_dispatch_init(g, 1, rdn::ao_dispatch_count(d->width, d->height), RDN_TASK_INIT_INDEX, stream);
   if (st != RDN_OK) return st;
   return rdn_task_graph_execute(g, 8, &env, stream);
 }

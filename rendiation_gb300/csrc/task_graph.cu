@@ -36,18 +36,40 @@ constexpr uint32_t kTile = 1024;
 constexpr uint32_t kCompactThreads = 256;
 constexpr uint32_t kPollThreads = 128;
 
-__device__ __forceinline__ uint32_t* task_locals(const TaskGroupDev& T, uint32_t i) {
-  return T.locals + (size_t)i * kTaskLocalWords;
+// Payload and local words are stored word-major (structure of arrays): word w
+// of record i at [w * (cap + 1) + i]. Neighbouring lanes mostly hold
+// neighbouring records (indices leave and return to the empty pool in warp
+// order), so a warp's accesses to one word coalesce.
+struct Rec {
+  uint32_t* base;
+  uint32_t stride;
+  __device__ __forceinline__ uint32_t& operator[](uint32_t w) const { return base[(size_t)w * stride]; }
+};
+__device__ __forceinline__ Rec task_locals(const TaskGroupDev& T, uint32_t i) { return Rec{T.locals + i, T.cap + 1}; }
+__device__ __forceinline__ Rec task_payload(const TaskGroupDev& T, uint32_t i) {
+  return Rec{T.payload + i, T.cap + 1};
 }
-__device__ __forceinline__ uint32_t* task_payload(const TaskGroupDev& T, uint32_t i) {
-  return T.payload + (size_t)i * T.payload_words;
+
+// Fetch-and-increment of a bump counter, aggregated over the converged lanes
+// that name the same counter: one atomic per (warp, counter), each lane gets a
+// distinct old value. Tens of thousands of tasks push to the same few counters
+// in one launch; per-lane atomics on one address serialise.
+__device__ __forceinline__ uint32_t agg_inc(uint32_t* ctr) {
+  const uint32_t active = __activemask();
+  const uint32_t peers = __match_any_sync(active, reinterpret_cast<unsigned long long>(ctr));
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t leader = __ffs(peers) - 1;
+  uint32_t base = 0;
+  if (lane == leader) base = atomicAdd(ctr, (uint32_t)__popc(peers));
+  base = __shfl_sync(peers, base, leader);
+  return base + __popc(peers & ((1u << lane) - 1u));
 }
 
 // DeviceBumpAllocationInvocationInstance::bump_allocate into the active list.
 __device__ __forceinline__ void push_active(const TaskGraphDev& G, const TaskGroupDev& T, uint32_t idx) {
   GroupCtl* c = T.ctl;
   const uint32_t size = c->active.size;
-  const uint32_t b = atomicAdd(&c->active.bump, 1u);
+  const uint32_t b = agg_inc(&c->active.bump);
   if (b < T.cap - size)
     T.active[c->sel][size + b] = idx;
   else
@@ -55,14 +77,15 @@ __device__ __forceinline__ void push_active(const TaskGraphDev& G, const TaskGro
 }
 
 // TaskGroupDeviceInvocationInstance::spawn_new_task_dyn: pop a free index,
-// write the record (state, parent, payload, initial future state), push the
-// index to the active list. Returns TASK_HANDLE_UNINIT when the pool is empty.
-__device__ uint32_t spawn_task(const TaskGraphDev& G, uint32_t g, const uint32_t* src, uint32_t src_words,
-                               uint32_t parent_type, uint32_t parent_index) {
+// write the record (state, parent, initial future state), push the index to
+// the active list. Returns TASK_HANDLE_UNINIT when the pool is empty. The
+// caller writes the payload (task_payload) in the same launch: the pushed
+// index is polled only after the next commit.
+__device__ uint32_t spawn_task(const TaskGraphDev& G, uint32_t g, uint32_t parent_type, uint32_t parent_index) {
   const TaskGroupDev& T = G.g[g];
   GroupCtl* c = T.ctl;
   const uint32_t esize = c->empty.size;
-  const uint32_t b = atomicAdd(&c->empty.bump, 1u);
+  const uint32_t b = agg_inc(&c->empty.bump);
   if (b >= esize) {
     atomicOr(G.error, TASK_ERR_NO_FREE_SLOT);
     return TASK_HANDLE_UNINIT;
@@ -71,9 +94,7 @@ __device__ uint32_t spawn_task(const TaskGraphDev& G, uint32_t g, const uint32_t
   T.state[idx] = TASK_NOT_FINISHED_WAKEN;
   T.parent_index[idx] = parent_index;
   T.parent_type[idx] = parent_type;
-  uint32_t* pl = task_payload(T, idx);
-  for (uint32_t w = 0; w < T.payload_words; w++) pl[w] = w < src_words ? src[w] : 0u;
-  uint32_t* L = task_locals(T, idx);
+  const Rec L = task_locals(T, idx);
   L[0] = 0u;
   for (uint32_t k = 0; k < kTaskMaxSpawns; k++) L[1 + k] = TASK_HANDLE_UNINIT;
   L[5] = TRACE_SUB_NOT_SPAWNED;
@@ -97,7 +118,7 @@ __device__ __forceinline__ void cleanup_task(const TaskGraphDev& G, uint32_t g, 
   const TaskGroupDev& T = G.g[g];
   GroupCtl* c = T.ctl;
   const uint32_t size = c->removed.size;
-  const uint32_t b = atomicAdd(&c->removed.bump, 1u);
+  const uint32_t b = agg_inc(&c->removed.bump);
   if (b < T.cap - size)
     T.removed[size + b] = idx;
   else
@@ -114,21 +135,21 @@ __device__ __forceinline__ bool poll_child(const TaskGraphDev& G, uint32_t g, ui
 }
 
 // Poll finalisation of the polling pipeline (task_group.rs:130-165).
-__device__ __forceinline__ void finalize(const TaskGraphDev& G, uint32_t g, uint32_t idx, bool resolved) {
+__device__ __forceinline__ void finalize(const TaskGraphDev& G, uint32_t g, uint32_t idx, bool resolved, uint32_t pi,
+                                         uint32_t pt) {
   const TaskGroupDev& T = G.g[g];
   if (!resolved) {
     T.state[idx] = TASK_GO_TO_SLEEP;
     return;
   }
   T.state[idx] = TASK_FINISHED;
-  const uint32_t pi = T.parent_index[idx], pt = T.parent_type[idx];
   if (pi == TASK_NO_PARENT)
     cleanup_task(G, g, idx);
   else if (pt < G.n_groups)
     wake_task(G, pt, pi);
 }
 
-__device__ __forceinline__ void put_ray(uint32_t* b, float3 o, float tmin, float3 d, float tmax) {
+__device__ __forceinline__ void put_ray(const Rec& b, float3 o, float tmin, float3 d, float tmax) {
   b[0] = __float_as_uint(o.x);
   b[1] = __float_as_uint(o.y);
   b[2] = __float_as_uint(o.z);
@@ -139,34 +160,37 @@ __device__ __forceinline__ void put_ray(uint32_t* b, float3 o, float tmin, float
   b[7] = __float_as_uint(tmax);
 }
 
-// Payload of a chain's child (the closure of a .then stage).
-__device__ uint32_t child_payload(uint32_t op, const uint32_t* self, const TraceParams& P, const AoEnv& A,
-                                  uint32_t* b) {
-  if (op == TASK_SPAWN_AO_PRIMARY) {
-    const uint32_t pixel = self[0];
+// Payload of a chain's child (the closure of a .then stage), written to the
+// child's record b of `words` words (validated: >= 16 for the AO operations).
+__device__ void child_payload(uint32_t op, const Rec& self, const TraceParams& P, const AoEnv& A, const Rec& b,
+                              uint32_t words) {
+  uint32_t px, py;
+  if (op == TASK_SPAWN_AO_PRIMARY && ao_pixel(A, self[0], px, py)) {
     float3 o, d;
-    ao_camera_ray(A, pixel % A.width, pixel / A.width, o, d);
+    ao_camera_ray(A, px, py, o, d);
     put_ray(b, o, F32_EPSILON, d, F32_MAX);
+    ao_count(A, 0, true);
     b[8] = RAY_FLAG_CULL_BACK;
     b[9] = 0xFFFFFFFFu;
     b[10] = A.tlas;
     b[11] = A.sbt_closest[0];
     b[12] = A.sbt_miss;
     b[13] = __float_as_uint(0.0f);
-    b[14] = b[15] = 0u;
-    return kTraceCallWords;
+    for (uint32_t w = 14; w < words; w++) b[w] = 0u;
+    return;
   }
-  if (op == TASK_SPAWN_AO_OCCLUSION) {
-    if (self[17] >= A.n_instances || self[16] >= A.n_triangles) {
-      // not a closest-hit payload: an empty trace call that resolves at once
+  if (op == TASK_SPAWN_AO_PRIMARY || op == TASK_SPAWN_AO_OCCLUSION) {
+    if (op == TASK_SPAWN_AO_PRIMARY || self[17] >= A.n_instances || self[16] >= A.n_triangles) {
+      // past the frame, or not a closest-hit payload: an empty trace call
+      // that resolves at once
       put_ray(b, make_float3(0.0f, 0.0f, 0.0f), 1.0f, make_float3(0.0f, 0.0f, 1.0f), 0.0f);
       b[8] = 0u;
       b[9] = 0u;
       b[10] = 0u;
       b[11] = b[12] = 0xFFFFFFFFu;
       b[13] = __float_as_uint(1.0f);
-      b[14] = b[15] = 0u;
-      return kTraceCallWords;
+      for (uint32_t w = 14; w < words; w++) b[w] = 0u;
+      return;
     }
     const float3 ro = make_float3(__uint_as_float(self[0]), __uint_as_float(self[1]), __uint_as_float(self[2]));
     const float3 rd = make_float3(__uint_as_float(self[4]), __uint_as_float(self[5]), __uint_as_float(self[6]));
@@ -176,21 +200,23 @@ __device__ uint32_t child_payload(uint32_t op, const uint32_t* self, const Trace
                                        __uint_as_float(self[20]), ro, hit);
     const float3 dir = ao_direction(n, A.sample_count);
     put_ray(b, hit, AO_TEST_MIN, dir, AO_TEST_MAX);
+    ao_count(A, 1, true);
     b[8] = RAY_FLAG_END_SEARCH;
     b[9] = 0xFFFFFFFFu;
     b[10] = self[10];
     b[11] = A.sbt_closest[1];
     b[12] = A.sbt_miss;
     b[13] = __float_as_uint(1.0f);
-    b[14] = b[15] = 0u;
-    return kTraceCallWords;
+    for (uint32_t w = 14; w < words; w++) b[w] = 0u;
+    return;
   }
-  return 0u;
+  for (uint32_t w = 0; w < words; w++) b[w] = 0u;
 }
 
-__device__ __forceinline__ void apply_map(uint32_t op, uint32_t* self, const uint32_t* child, const AoEnv& A) {
+__device__ __forceinline__ void apply_map(uint32_t op, const Rec& self, const Rec& child, const AoEnv& A) {
   if (op == TASK_MAP_AO_ACCUMULATE) {
-    if (self[0] < A.width * A.height) ao_accumulate(A, self[0], __uint_as_float(child[kTraceUser]));
+    uint32_t x, y;
+    if (ao_pixel(A, self[0], x, y)) ao_accumulate(A, y * A.width + x, __uint_as_float(child[kTraceUser]));
   } else if (op == TASK_MAP_STORE_CHILD) {
     for (uint32_t w = 0; w < 3; w++) self[kTraceUser + w] = child[kTraceUser + w];
   } else if (op == TASK_MAP_STORE_ZERO) {
@@ -205,20 +231,31 @@ __device__ __forceinline__ void apply_map(uint32_t op, uint32_t* self, const uin
 // polls it at once; a stage resolves in the poll that reads its finished child.
 __device__ bool poll_chain(const TaskGraphDev& G, uint32_t g, uint32_t idx, const TraceParams& P, const AoEnv& A) {
   const TaskGroupDev& T = G.g[g];
-  uint32_t* L = task_locals(T, idx);
-  uint32_t* self = task_payload(T, idx);
-  bool r = L[0] == 0u;
-  L[0] = 1u;
-  const uint32_t* child = nullptr;
-  for (uint32_t k = 0; k < T.n_spawn; k++) {
+  const Rec L = task_locals(T, idx);
+  const Rec self = task_payload(T, idx);
+  const uint32_t n_spawn = T.n_spawn;
+  // the future's words are independent loads: issue them together
+  uint32_t l[1 + kTaskMaxSpawns];
+#pragma unroll
+  for (uint32_t k = 0; k <= kTaskMaxSpawns; k++) l[k] = k <= n_spawn ? L[k] : 0u;
+  bool r = l[0] == 0u;
+  if (r) L[0] = 1u;
+  Rec child{nullptr, 0};
+#pragma unroll
+  for (uint32_t k = 0; k < kTaskMaxSpawns; k++) {
+    if (k >= n_spawn) break;
     const uint32_t cg = T.spawn_type[k];
     if (r) {
-      uint32_t b[kTaskMaxPayloadWords];
-      const uint32_t words = child_payload(T.spawn_op[k], self, P, A, b);
-      L[1 + k] = spawn_task(G, cg, b, words, g, idx);
+      const uint32_t h = spawn_task(G, cg, g, idx);
+      if (h != TASK_HANDLE_UNINIT) {
+        const TaskGroupDev& C = G.g[cg];
+        child_payload(T.spawn_op[k], self, P, A, task_payload(C, h), C.payload_words);
+      }
+      L[1 + k] = h;
+      l[1 + k] = h;
     }
     r = false;
-    const uint32_t h = L[1 + k];
+    const uint32_t h = l[1 + k];
     if (h != TASK_HANDLE_UNINIT && h != TASK_HANDLE_RESOLVED && poll_child(G, cg, h)) {
       child = task_payload(G.g[cg], h);
       L[1 + k] = TASK_HANDLE_RESOLVED;
@@ -237,9 +274,10 @@ template <int MODE>
 __device__ bool poll_trace(const TaskGraphDev& G, uint32_t g, uint32_t idx, const TraceParams& P, uint2* stack,
                            uint32_t stride) {
   const TaskGroupDev& T = G.g[g];
-  uint32_t* L = task_locals(T, idx);
-  uint32_t* self = task_payload(T, idx);
-  if (L[6] == TRACE_SUB_NOT_SPAWNED) {
+  const Rec L = task_locals(T, idx);
+  const Rec self = task_payload(T, idx);
+  uint32_t sub_group = L[5], sub_id = L[6], terminated = L[7];
+  if (sub_id == TRACE_SUB_NOT_SPAWNED) {
     RayCtx R;
     R.o = make_float3(__uint_as_float(self[0]), __uint_as_float(self[1]), __uint_as_float(self[2]));
     R.tmin = __uint_as_float(self[3]);
@@ -250,46 +288,57 @@ __device__ bool poll_trace(const TaskGraphDev& G, uint32_t g, uint32_t idx, cons
     bool bad;
     traverse_ray<MODE, false>(P, R, self[10], stack, stride, bad);
     if (bad) atomicOr(P.error_word, 2u);
-    uint32_t b[kClosestWords];
-    for (uint32_t w = 0; w < kTraceCallWords; w++) b[w] = self[w];
-    uint32_t target = TRACE_SUB_NOT_SPAWNED, words = kTraceCallWords;
+    uint32_t target = TRACE_SUB_NOT_SPAWNED;
     if (R.best.have) {
       if (!(R.ray_flags & RAY_FLAG_SKIP_CLOSEST) && self[11] < G.n_groups &&
-          G.g[self[11]].payload_words >= kTraceCallWords) {
-        const uint4 gm = __ldg(reinterpret_cast<const uint4*>(P.tri_root + R.best.geom_slot));
-        const uint32_t tri = __ldg(P.redirect + R.best.k);
-        b[16] = tri;
-        b[17] = R.best.inst;
-        b[18] = __float_as_uint(R.best.t);
-        b[19] = __float_as_uint(R.best.u);
-        b[20] = __float_as_uint(R.best.v);
-        b[21] = R.best.s < 0.0f ? 0xFFu : 0xFEu;
-        b[22] = gm.y;
-        b[23] = tri - gm.z;
+          G.g[self[11]].payload_words >= kClosestWords)
         target = self[11];
-        words = kClosestWords;
-      }
     } else if (self[12] < G.n_groups && G.g[self[12]].payload_words >= kTraceCallWords) {
       target = self[12];
     }
     if (target != TRACE_SUB_NOT_SPAWNED) {
-      const uint32_t h = spawn_task(G, target, b, words, g, idx);
-      L[5] = target;
-      L[6] = h == TASK_HANDLE_UNINIT ? TRACE_SUB_SPAWN_FAILED : h;
+      const uint32_t h = spawn_task(G, target, g, idx);
+      sub_group = target;
+      sub_id = h == TASK_HANDLE_UNINIT ? TRACE_SUB_SPAWN_FAILED : h;
+      L[5] = sub_group;
+      L[6] = sub_id;
+      if (h != TASK_HANDLE_UNINIT) {
+        const TaskGroupDev& C = G.g[target];
+        const Rec b = task_payload(C, h);
+        for (uint32_t w = 0; w < kTraceCallWords; w++) b[w] = self[w];
+        uint32_t w = kTraceCallWords;
+        if (R.best.have) {
+          const uint4 gm = __ldg(reinterpret_cast<const uint4*>(P.tri_root + R.best.geom_slot));
+          const uint32_t tri = __ldg(P.redirect + R.best.k);
+          b[16] = tri;
+          b[17] = R.best.inst;
+          b[18] = __float_as_uint(R.best.t);
+          b[19] = __float_as_uint(R.best.u);
+          b[20] = __float_as_uint(R.best.v);
+          b[21] = R.best.s < 0.0f ? 0xFFu : 0xFEu;
+          b[22] = gm.y;
+          b[23] = tri - gm.z;
+          w = kClosestWords;
+        }
+        for (; w < C.payload_words; w++) b[w] = 0u;
+      }
     }
   }
   bool resolved = false;
-  if (L[6] == TRACE_SUB_SPAWN_FAILED || L[6] == TRACE_SUB_NOT_SPAWNED) {
-    if (!L[7]) {
+  if (sub_id == TRACE_SUB_SPAWN_FAILED || sub_id == TRACE_SUB_NOT_SPAWNED) {
+    if (!terminated) {
       L[7] = 1u;
+      terminated = 1u;
       resolved = true;
     }
   }
-  if (!L[7]) {
-    const uint32_t cg = L[5], h = L[6];
-    if (poll_child(G, cg, h)) {
-      const uint32_t* cp = task_payload(G.g[cg], h);
-      for (uint32_t w = 0; w < 3; w++) self[kTraceUser + w] = cp[kTraceUser + w];
+  if (!terminated) {
+    if (poll_child(G, sub_group, sub_id)) {
+      const Rec cp = task_payload(G.g[sub_group], sub_id);
+      const uint32_t u0 = cp[kTraceUser], u1 = cp[kTraceUser + 1], u2 = cp[kTraceUser + 2];
+      self[kTraceUser] = u0;
+      self[kTraceUser + 1] = u1;
+      self[kTraceUser + 2] = u2;
       L[7] = 1u;
       resolved = true;
     }
@@ -298,20 +347,27 @@ __device__ bool poll_trace(const TaskGraphDev& G, uint32_t g, uint32_t idx, cons
 }
 
 template <int MODE, bool LOCAL>
-__global__ void __launch_bounds__(kPollThreads) poll_kernel(TaskGraphDev G, uint32_t g, TraceParams P, AoEnv A) {
+__global__ void __launch_bounds__(kPollThreads, 8) poll_kernel(const TaskGraphDev* __restrict__ Gp, uint32_t g,
+                                                            TraceParams P, AoEnv A) {
   RDN_TRAVERSAL_STACK(LOCAL);
+  const TaskGraphDev& G = *Gp;
   const TaskGroupDev& T = G.g[g];
   const GroupCtl* c = T.ctl;
   const uint32_t n = c->active.size;
   const uint32_t* list = T.active[c->sel];
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const uint32_t idx = list[i];
+    // the parent is read now, and its state line fetched into L2, so that a
+    // resolving task does not wait for them at the end
+    const uint32_t pi = T.parent_index[idx], pt = T.parent_type[idx];
+    if (pi != TASK_NO_PARENT && pt < G.n_groups)
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(G.g[pt].state + pi));
     bool r;
     if (T.program == TASK_PROGRAM_TRACE)
       r = poll_trace<MODE>(G, g, idx, P, stack_ptr, stack_stride);
     else
       r = poll_chain(G, g, idx, P, A);
-    finalize(G, g, idx, r);
+    finalize(G, g, idx, r, pi, pt);
   }
 }
 
@@ -479,23 +535,30 @@ __global__ void init_kernel(TaskGroupDev T) {
     T.state[0] = TASK_NOT_FINISHED_WAKEN;
     T.parent_index[0] = TASK_NO_PARENT;
     T.parent_type[0] = TASK_NO_PARENT;
-    uint32_t* L = T.locals;
+    const Rec L = task_locals(T, 0);
     for (uint32_t k = 0; k < kTaskMaxSpawns; k++) L[1 + k] = TASK_HANDLE_UNINIT;
     L[5] = L[6] = TRACE_SUB_NOT_SPAWNED;
   }
 }
 
-__global__ void spawn_init_kernel(TaskGraphDev G, uint32_t g, uint32_t count, uint32_t init_op) {
+__global__ void spawn_init_kernel(const TaskGraphDev* __restrict__ Gp, uint32_t g, uint32_t count,
+                                  uint32_t init_op) {
+  const TaskGraphDev& G = *Gp;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
-    const uint32_t v = i;
-    spawn_task(G, g, &v, init_op == TASK_INIT_INDEX ? 1u : 0u, TASK_NO_PARENT, TASK_NO_PARENT);
+    const uint32_t h = spawn_task(G, g, TASK_NO_PARENT, TASK_NO_PARENT);
+    if (h != TASK_HANDLE_UNINIT) {
+      const TaskGroupDev& T = G.g[g];
+      const Rec b = task_payload(T, h);
+      b[0] = init_op == TASK_INIT_INDEX ? i : 0u;
+      for (uint32_t w = 1; w < T.payload_words; w++) b[w] = 0u;
+    }
   }
 }
 
 uint32_t tiles_of(uint32_t cap) { return (cap + kTile - 1) / kTile; }
 
 template <int MODE, bool LOCAL>
-cudaError_t launch_poll(const TaskGraphDev& G, uint32_t g, const TraceParams& P, const AoEnv& A, uint32_t grid,
+cudaError_t launch_poll(const TaskGraphDev* G, uint32_t g, const TraceParams& P, const AoEnv& A, uint32_t grid,
                         cudaStream_t st) {
   const size_t smem = MODE != MODE_THREADED && !LOCAL ? (size_t)P.stack_depth * kPollThreads * sizeof(uint2) : 0;
   static bool attr_done = false;
@@ -613,6 +676,15 @@ std::string TaskGraph::create(const std::vector<TaskGroupDesc>& groups, uint32_t
     e = cudaGetLastError();
     if (e != cudaSuccess) return std::string("init launch: ") + cudaGetErrorString(e);
   }
+  // the kernels read the group table from device memory (indexed by group at
+  // run time, which kernel parameters do not support without a local copy)
+  void* table = nullptr;
+  e = cudaMalloc(&table, sizeof(TaskGraphDev));
+  if (e != cudaSuccess) return std::string("cudaMalloc: ") + cudaGetErrorString(e);
+  allocs_.push_back(table);
+  dev_ptr_ = static_cast<TaskGraphDev*>(table);
+  e = cudaMemcpyAsync(dev_ptr_, &dev_, sizeof(TaskGraphDev), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return std::string("cudaMemcpyAsync: ") + cudaGetErrorString(e);
   return "";
 }
 
@@ -633,8 +705,10 @@ cudaError_t TaskGraph::compact(uint32_t g, cudaStream_t st) {
 
 cudaError_t TaskGraph::poll(uint32_t g, const TraceParams* p, int mode, const AoEnv* ao, cudaStream_t st) {
   const TaskGroupDev& T = dev_.g[g];
-  const uint32_t grid =
-      std::max<uint32_t>(1, std::min<uint32_t>((T.cap + kPollThreads - 1) / kPollThreads, (uint32_t)sm_count_ * 8));
+  // one thread per possible active entry: blocks past the committed size exit
+  // at once, and a block's traversals do not queue behind one another as in
+  // a grid-stride loop (divergent trace polls finish when their slowest ray does)
+  const uint32_t grid = std::max<uint32_t>(1, (T.cap + kPollThreads - 1) / kPollThreads);
   TraceParams P;
   AoEnv A;
   if (p)
@@ -645,21 +719,22 @@ cudaError_t TaskGraph::poll(uint32_t g, const TraceParams* p, int mode, const Ao
     A = *ao;
   else
     std::memset(&A, 0, sizeof(A));
-  if (T.program != TASK_PROGRAM_TRACE || !p) return launch_poll<MODE_THREADED, false>(dev_, g, P, A, grid, st);
+  const TaskGraphDev* G = dev_ptr_;
+  if (T.program != TASK_PROGRAM_TRACE || !p) return launch_poll<MODE_THREADED, false>(G, g, P, A, grid, st);
   if (mode == MODE_WIDE4)
-    return P.local_stack ? launch_poll<MODE_WIDE4, true>(dev_, g, P, A, grid, st)
-                         : launch_poll<MODE_WIDE4, false>(dev_, g, P, A, grid, st);
+    return P.local_stack ? launch_poll<MODE_WIDE4, true>(G, g, P, A, grid, st)
+                         : launch_poll<MODE_WIDE4, false>(G, g, P, A, grid, st);
   if (mode == MODE_BINARY)
-    return P.local_stack ? launch_poll<MODE_BINARY, true>(dev_, g, P, A, grid, st)
-                         : launch_poll<MODE_BINARY, false>(dev_, g, P, A, grid, st);
-  return launch_poll<MODE_THREADED, false>(dev_, g, P, A, grid, st);
+    return P.local_stack ? launch_poll<MODE_BINARY, true>(G, g, P, A, grid, st)
+                         : launch_poll<MODE_BINARY, false>(G, g, P, A, grid, st);
+  return launch_poll<MODE_THREADED, false>(G, g, P, A, grid, st);
 }
 
 cudaError_t TaskGraph::dispatch_init(uint32_t group, uint32_t count, uint32_t init_op, cudaStream_t st) {
   cudaError_t e = prepare(group, st);
   if (e != cudaSuccess || count == 0) return e;
   const uint32_t grid = std::min<uint32_t>((count + 255) / 256, (uint32_t)sm_count_ * 8);
-  spawn_init_kernel<<<grid, 256, 0, st>>>(dev_, group, count, init_op);
+  spawn_init_kernel<<<grid, 256, 0, st>>>(dev_ptr_, group, count, init_op);
   commit_spawn_kernel<<<1, 1, 0, st>>>(dev_.g[group]);
   return cudaGetLastError();
 }

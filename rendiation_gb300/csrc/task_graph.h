@@ -110,8 +110,8 @@ struct TaskGroupDev {
   uint32_t* state;
   uint32_t* parent_type;
   uint32_t* parent_index;
-  uint32_t* payload;  // (cap + 1) * payload_words
-  uint32_t* locals;   // (cap + 1) * kTaskLocalWords
+  uint32_t* payload;  // payload_words x (cap + 1), word-major
+  uint32_t* locals;   // kTaskLocalWords x (cap + 1), word-major
   uint32_t* active[2];
   uint32_t* removed;
   uint32_t* empty;
@@ -143,7 +143,13 @@ struct AoEnv {
   const float* vertices;    // built vertex positions
   uint32_t n_instances;     // TLAS instance slots
   uint32_t n_triangles;     // built triangles
+  uint32_t* ray_counts;     // nullable: [camera, occlusion] rays traced
 };
+
+// Ray-generation tasks of a w x h AO frame: whole 8x4 pixel tiles, 32 per tile.
+__host__ __device__ inline uint32_t ao_dispatch_count(uint32_t w, uint32_t h) {
+  return ((w + 7) / 8) * ((h + 3) / 4) * 32;
+}
 
 struct TaskGroupDesc {
   uint32_t program = TASK_PROGRAM_CHAIN;
@@ -185,6 +191,7 @@ class TaskGraph {
   cudaError_t poll(uint32_t g, const TraceParams* p, int mode, const AoEnv* ao, cudaStream_t st);
 
   TaskGraphDev dev_{};
+  TaskGraphDev* dev_ptr_ = nullptr;  // device copy of dev_
   std::vector<TaskGroupDesc> desc_;
   std::vector<void*> allocs_;
   int sm_count_ = 1;
