@@ -1148,8 +1148,8 @@ extern "C" {
 rdn_status rdn_task_graph_create(rdn_ctx* c, const rdn_task_group_desc* groups, uint32_t count, uint32_t capacity,
                                  void* stream, rdn_task_graph** out) {
   if (!c || !groups || !out) return fail(c, RDN_ERR_INVALID_ARG, "null context, groups or output");
-  if (c->device < 0) return fail(c, RDN_ERR_UNSUPPORTED, "host-only context has no device");
   *out = nullptr;
+  if (count > RDN_TASK_MAX_GROUPS) return fail(c, RDN_ERR_INVALID_ARG, "a task graph holds 1 to 16 task groups");
   std::vector<rdn::TaskGroupDesc> desc(count);
   bool needs_env = false;
   for (uint32_t g = 0; g < count; g++) {
@@ -1166,6 +1166,9 @@ rdn_status rdn_task_graph_create(rdn_ctx* c, const rdn_task_group_desc* groups, 
     }
     if (d.program == RDN_TASK_PROGRAM_TRACE || d.map_op == RDN_TASK_MAP_AO_ACCUMULATE) needs_env = true;
   }
+  const std::string bad = rdn::TaskGraph::validate(desc, capacity);
+  if (!bad.empty()) return fail(c, RDN_ERR_INVALID_ARG, bad);
+  if (c->device < 0) return fail(c, RDN_ERR_UNSUPPORTED, "host-only context has no device");
   std::unique_ptr<rdn_task_graph> tg(new (std::nothrow) rdn_task_graph());
   if (!tg) return fail(c, RDN_ERR_OOM, "out of host memory");
   tg->ctx = c;

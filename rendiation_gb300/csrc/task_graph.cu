@@ -582,8 +582,7 @@ TaskGraph::~TaskGraph() {
   for (void* p : allocs_) cudaFree(p);
 }
 
-std::string TaskGraph::create(const std::vector<TaskGroupDesc>& groups, uint32_t capacity, int sm_count,
-                              cudaStream_t st) {
+std::string TaskGraph::validate(const std::vector<TaskGroupDesc>& groups, uint32_t capacity) {
   const uint32_t n = (uint32_t)groups.size();
   if (n == 0 || n > kTaskMaxGroups) return "a task graph holds 1 to 16 task groups";
   if (capacity == 0) return "capacity must be at least 1";
@@ -616,6 +615,14 @@ std::string TaskGraph::create(const std::vector<TaskGroupDesc>& groups, uint32_t
         d.payload_words < kTraceCallWords)
       return "the map operation writes a trace-call user payload (16 words)";
   }
+  return "";
+}
+
+std::string TaskGraph::create(const std::vector<TaskGroupDesc>& groups, uint32_t capacity, int sm_count,
+                              cudaStream_t st) {
+  const std::string bad = validate(groups, capacity);
+  if (!bad.empty()) return bad;
+  const uint32_t n = (uint32_t)groups.size();
   desc_ = groups;
   sm_count_ = sm_count > 0 ? sm_count : 1;
   std::memset(&dev_, 0, sizeof(dev_));

@@ -166,6 +166,8 @@ struct TaskGroupDesc {
 class TaskGraph {
  public:
   ~TaskGraph();
+  // The descriptor checks of create(), without a device: "" when valid.
+  static std::string validate(const std::vector<TaskGroupDesc>& groups, uint32_t capacity);
   // Validates, allocates and initialises (TaskGroupExecutorResource::init).
   std::string create(const std::vector<TaskGroupDesc>& groups, uint32_t capacity, int sm_count, cudaStream_t st);
   // dispatch_allocate_init_task (runtime/mod.rs:217-260)

@@ -172,3 +172,69 @@ def test_ao_camera_miss_writes_one():
     p, i = quad(0.0, 0.01)  # tiny floor: almost every camera ray misses
     img = ao_oracle(Scene([[(p, i, 1)]], [[{"blas": 0}]]), 2.0)
     assert np.all(img == 0xFFFFFFFF)
+
+
+# ---- C ABI host logic (no device needed) ----
+
+def _create(system, descs, capacity=8):
+    import ctypes as C
+
+    from rendiation_gb300 import native
+
+    arr = (native.TaskGroupDesc * max(1, len(descs)))()
+    for i, d in enumerate(descs):
+        for k, v in d.items():
+            if k in ("spawn_type", "spawn_op"):
+                for j, x in enumerate(v):
+                    getattr(arr[i], k)[j] = x
+            else:
+                setattr(arr[i], k, v)
+    h = C.c_void_p()
+    st = system._L.rdn_task_graph_create(system._h, arr, len(descs), capacity, None, C.byref(h))
+    msg = system._L.rdn_last_error(system._h).decode()
+    return st, msg, h
+
+
+def test_task_graph_descriptors_are_validated_on_the_host():
+    from rendiation_gb300 import native
+    from rendiation_gb300 import raytracing as rt
+
+    S = rt.AccelerationStructureSystem(device=-1)
+    chain = {"program": 0, "max_in_flight": 1, "payload_words": 1}
+    cases = [
+        ([], "1 to 16"),
+        ([dict(chain)] * 17, "1 to 16"),
+        ([dict(chain, max_in_flight=0)], "max_in_flight"),
+        ([dict(chain, payload_words=33)], "payload_words"),
+        ([dict(chain, n_spawn=1, spawn_type=[3])], "does not exist"),
+        ([dict(chain, n_spawn=5)], "at most 4"),
+        ([dict(chain, map_op=9)], "unknown map"),
+        ([{"program": 1, "max_in_flight": 1, "payload_words": 8}], "at least 16"),
+        ([dict(chain, n_spawn=1, spawn_type=[0], spawn_op=[1])], "trace task group"),
+        ([dict(chain, map_op=2)], "user payload"),
+    ]
+    for descs, text in cases:
+        st, msg, _ = _create(S, descs)
+        assert st == -1 and text in msg, (descs, st, msg)
+    # a valid graph on a host-only context: unsupported, not invalid
+    st, msg, _ = _create(S, [dict(chain), dict(chain, n_spawn=1, spawn_type=[0])])
+    assert st == -8 and "host-only" in msg
+    st, msg, _ = _create(S, [dict(chain)], capacity=0)
+    assert st == -1 and "capacity" in msg
+    assert native.STATUS_NAMES[st] == "RDN_ERR_INVALID_ARG"
+
+
+def test_ao_entry_points_need_a_device():
+    import ctypes as C
+
+    from rendiation_gb300 import native
+    from rendiation_gb300 import raytracing as rt
+
+    S = rt.AccelerationStructureSystem(device=-1)
+    d = native.AoDesc()
+    d.width = d.height = 4
+    assert S._L.rdn_ao_render(S._h, C.byref(d), None) == -8
+    h = C.c_void_p()
+    assert S._L.rdn_ao_pipeline_create(S._h, 4, 4, None, C.byref(h)) == -8
+    assert S._L.rdn_ao_pipeline_create(S._h, 0, 4, None, C.byref(h)) == -1
+    assert S._L.rdn_task_graph_destroy(None) == 0
