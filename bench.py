@@ -552,15 +552,21 @@ def bench_ao(args, P, S_field):
     out["fused_ms"], out["fused_mrays"] = round(ms, 4), round(rays / ms / 1e3, 1)
     ms, rays_g = timed(lambda k: frame("graph", k))
     out["graph_ms"], out["graph_mrays"] = round(ms, 4), round(rays_g / ms / 1e3, 1)
-    # the task-graph frame captured once, replayed
-    g = torch.cuda.CUDAGraph()
-    descs["graph"].sample_count = 7
-    with torch.cuda.graph(g):
-        assert L.rdn_ao_render_graph(h, C.byref(descs["graph"]), C.c_void_p(torch.cuda.current_stream().cuda_stream)) == 0
-    ms, rays_c = timed(lambda k: g.replay())
-    out["graph_captured_ms"], out["graph_captured_mrays"] = round(ms, 4), round(rays_c / ms / 1e3, 1)
+    # each form captured once (rdn_ao_capture) and replayed; the frame reads and
+    # advances a device sample counter, so every replay draws the next sample
+    counter = torch.zeros(1, dtype=torch.int32, device="cuda")
+    for mode, pipe in (("fused", None), ("graph", h)):
+        d = descs[mode]
+        d.sample_counter = counter.data_ptr()
+        ge = C.c_void_p()
+        assert L.rdn_ao_capture(P._h, pipe, C.byref(d), C.byref(ge)) == 0
+        ms, rays_c = timed(lambda k: L.rdn_graph_launch(ge, sp))
+        L.rdn_graph_destroy(ge)
+        d.sample_counter = None
+        out[mode + "_captured_ms"], out[mode + "_captured_mrays"] = round(ms, 4), round(rays_c / ms / 1e3, 1)
     out["graph_over_fused"] = round(out["graph_ms"] / out["fused_ms"], 2)
     out["graph_launches_per_frame"] = 3 + 8 * 5 * 4
+    out["captured"] = "rdn_ao_capture: one CUDA graph per frame, sample index read from a device counter"
     st, flags = P.check_errors()
     assert st == 0 and flags == 0
     L.rdn_task_graph_destroy(h)

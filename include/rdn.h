@@ -603,6 +603,9 @@ typedef struct rdn_ao_desc {
   uint32_t sbt_miss;              /* task graphs: miss group of both rays */
   uint32_t pad;
   uint32_t* ray_counts;           /* device, nullable: [camera, occlusion] rays traced, added to */
+  uint32_t* sample_counter;       /* device, nullable: when set, the frame reads its sample index from
+                                     here instead of sample_count and adds one to it at its end, so
+                                     that a captured frame (rdn_ao_capture) advances by itself */
 } rdn_ao_desc;
 
 typedef struct rdn_task_graph rdn_task_graph;
@@ -640,6 +643,12 @@ rdn_status rdn_ao_pipeline_create(rdn_ctx* ctx, uint32_t width, uint32_t height,
 rdn_status rdn_ao_render_graph(rdn_task_graph* graph, const rdn_ao_desc* desc, void* stream);
 /* The same frame as one fused kernel, one thread per pixel. */
 rdn_status rdn_ao_render(rdn_ctx* ctx, const rdn_ao_desc* desc, void* stream);
+/* One AO frame captured into an executable CUDA graph: the fused kernel
+ * (pipeline NULL) or the task-graph pipeline's dispatch and 8 rounds. The
+ * descriptor is baked in; with desc->sample_counter set, each rdn_graph_launch
+ * draws the next sample. The context's structure must stay built and the
+ * buffers alive while the graph is in use. */
+rdn_status rdn_ao_capture(rdn_ctx* ctx, rdn_task_graph* pipeline, const rdn_ao_desc* desc, rdn_graph** out);
 
 #ifdef __cplusplus
 }

@@ -38,7 +38,7 @@ __global__ void __launch_bounds__(128) ao_kernel(TraceParams P, AoEnv A) {
         ao_shading_normal(A, P.tlas_data + R.best.inst, __ldg(P.redirect + R.best.k), R.best.u, R.best.v, o, hit);
     RayCtx S;
     S.o = hit;
-    S.d = ao_direction(n, A.sample_count);
+    S.d = ao_direction(n, ao_sample(A));
     S.tmin = AO_TEST_MIN;
     S.tmax = AO_TEST_MAX;
     S.ray_flags = RAY_FLAG_END_SEARCH;
@@ -69,7 +69,14 @@ cudaError_t launch_variant(const TraceParams& p, const AoEnv& a, cudaStream_t st
   return cudaGetLastError();
 }
 
+__global__ void ao_advance_kernel(uint32_t* counter) { *counter += 1u; }
+
 }  // namespace
+
+cudaError_t launch_ao_advance(uint32_t* counter, cudaStream_t st) {
+  ao_advance_kernel<<<1, 1, 0, st>>>(counter);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_ao(const TraceParams& p, const AoEnv& a, int mode, cudaStream_t st) {
   if (a.width == 0 || a.height == 0) return cudaSuccess;

@@ -63,10 +63,13 @@ __device__ __forceinline__ float4 mat4_mul(const float* m, float x, float y, flo
                      x * m[2] + y * m[6] + z * m[10] + w * m[14], x * m[3] + y * m[7] + z * m[11] + w * m[15]);
 }
 
+// Sample index of the frame: the device counter when the frame reads one.
+__device__ __forceinline__ uint32_t ao_sample(const AoEnv& A) { return A.sample_dev ? *A.sample_dev : A.sample_count; }
+
 // DefaultRtxCameraInvocation::generate_ray with PCGRandomSampler seeded by
 // xxhash32(x, y, sample index); next_2d = (next(), next()).
 __device__ __forceinline__ void ao_camera_ray(const AoEnv& A, uint32_t x, uint32_t y, float3& o, float3& d) {
-  uint32_t state = xxhash32(x, y, A.sample_count);
+  uint32_t state = xxhash32(x, y, ao_sample(A));
   const float j0 = sample_next(state);
   const float j1 = sample_next(state);
   const float fw = (float)A.width, fh = (float)A.height;
@@ -159,10 +162,11 @@ __device__ __forceinline__ void ao_accumulate(const AoEnv& A, uint32_t pixel, fl
   uint32_t* texel = reinterpret_cast<uint32_t*>(A.image) + pixel;
   const uint32_t old = *texel;
   const float prev = (float)(old & 0xFFu) / 255.0f;
-  const float prev_count = (float)A.sample_count;
+  const uint32_t count = ao_sample(A);
+  const float prev_count = (float)count;
   const float all = prev_count + 1.0f;
   const float next = (prev * prev_count + payload) / all;
-  const float w = A.sample_count < AO_MAX_SAMPLE ? next : prev;
+  const float w = count < AO_MAX_SAMPLE ? next : prev;
   const uint32_t q = to_unorm8(w);
   *texel = q | (q << 8) | (q << 16) | (255u << 24);
 }

@@ -1138,6 +1138,7 @@ rdn_status ao_env(rdn_ctx* c, const rdn_ao_desc* d, rdn::TraceParams& p, rdn::Ao
   a.n_instances = (uint32_t)c->dev.tlas_data.count;
   a.n_triangles = (uint32_t)(c->dev.indices.count / 3);
   a.ray_counts = d->ray_counts;
+  a.sample_dev = d->sample_counter;
   return RDN_OK;
 }
 
@@ -1317,8 +1318,10 @@ rdn_status rdn_ao_render_graph(rdn_task_graph* g, const rdn_ao_desc* d, void* st
   env.sbt_miss = 4;
   rdn_status st =
       rdn_task_graph_dispatch_init(g, 1, rdn::ao_dispatch_count(d->width, d->height), RDN_TASK_INIT_INDEX, stream);
-  if (st != RDN_OK) return st;
-  return rdn_task_graph_execute(g, 8, &env, stream);
+  if (st == RDN_OK) st = rdn_task_graph_execute(g, 8, &env, stream);
+  if (st != RDN_OK || !d->sample_counter) return st;
+  cudaError_t e = rdn::launch_ao_advance(d->sample_counter, static_cast<cudaStream_t>(stream));
+  return e == cudaSuccess ? RDN_OK : cuda_fail(c, e, "AO sample counter");
 }
 
 rdn_status rdn_ao_render(rdn_ctx* c, const rdn_ao_desc* d, void* stream) {
@@ -1332,7 +1335,47 @@ rdn_status rdn_ao_render(rdn_ctx* c, const rdn_ao_desc* d, void* stream) {
   if (st != RDN_OK) return st;
   cudaError_t e = cudaSetDevice(c->device);
   if (e == cudaSuccess) e = rdn::launch_ao(p, a, mode_of(d->traversal), static_cast<cudaStream_t>(stream));
+  if (e == cudaSuccess && d->sample_counter) e = rdn::launch_ao_advance(d->sample_counter, static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(c, e, "AO launch");
+  return RDN_OK;
+}
+
+rdn_status rdn_ao_capture(rdn_ctx* c, rdn_task_graph* pipeline, const rdn_ao_desc* d, rdn_graph** out) {
+  Range range_("rdn_ao_capture");
+  if (!c || !d || !out) return fail(c, RDN_ERR_INVALID_ARG, "null context, descriptor or output");
+  *out = nullptr;
+  if (c->device < 0) return fail(c, RDN_ERR_UNSUPPORTED, "host-only context cannot trace");
+  if (pipeline && pipeline->ctx != c) return fail(c, RDN_ERR_INVALID_ARG, "the pipeline belongs to another context");
+  {
+    std::lock_guard<std::mutex> lk(c->lock);
+    // a build allocates and synchronises, which a capture cannot hold
+    if (c->dirty || !c->host) return fail(c, RDN_ERR_NOT_BUILT, "build the structure before capturing a frame");
+  }
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e != cudaSuccess) return cuda_fail(c, e, "cudaSetDevice");
+  cudaStream_t s = nullptr;
+  e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return cuda_fail(c, e, "capture stream");
+  auto* g = new (std::nothrow) rdn_graph();
+  if (!g) {
+    cudaStreamDestroy(s);
+    return fail(c, RDN_ERR_OOM, "host allocation failed");
+  }
+  g->device = c->device;
+  rdn_status st = RDN_OK;
+  e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    st = pipeline ? rdn_ao_render_graph(pipeline, d, s) : rdn_ao_render(c, d, s);
+    e = cudaStreamEndCapture(s, &g->graph);
+  }
+  if (e == cudaSuccess && st == RDN_OK) e = cudaGraphInstantiate(&g->exec, g->graph, 0);
+  cudaStreamDestroy(s);
+  if (e != cudaSuccess || st != RDN_OK) {
+    if (g->graph) cudaGraphDestroy(g->graph);
+    delete g;
+    return st != RDN_OK ? st : cuda_fail(c, e, "AO frame capture");
+  }
+  *out = g;
   return RDN_OK;
 }
 

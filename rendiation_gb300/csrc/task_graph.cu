@@ -198,7 +198,7 @@ __device__ void child_payload(uint32_t op, const Rec& self, const TraceParams& P
     const float3 hit = ro + rd * t;
     const float3 n = ao_shading_normal(A, P.tlas_data + self[17], self[16], __uint_as_float(self[19]),
                                        __uint_as_float(self[20]), ro, hit);
-    const float3 dir = ao_direction(n, A.sample_count);
+    const float3 dir = ao_direction(n, ao_sample(A));
     put_ray(b, hit, AO_TEST_MIN, dir, AO_TEST_MAX);
     ao_count(A, 1, true);
     b[8] = RAY_FLAG_END_SEARCH;

@@ -144,6 +144,7 @@ struct AoEnv {
   uint32_t n_instances;     // TLAS instance slots
   uint32_t n_triangles;     // built triangles
   uint32_t* ray_counts;     // nullable: [camera, occlusion] rays traced
+  const uint32_t* sample_dev;  // nullable: the sample index, read at run time instead of sample_count
 };
 
 // Ray-generation tasks of a w x h AO frame: whole 8x4 pixel tiles, 32 per tile.
@@ -201,5 +202,7 @@ class TaskGraph {
 
 // Fused AO frame (ao.cu): every pixel of a.width x a.height, one launch.
 cudaError_t launch_ao(const TraceParams& p, const AoEnv& a, int mode, cudaStream_t st);
+// Adds one to a device sample counter (the end of a frame that reads it).
+cudaError_t launch_ao_advance(uint32_t* counter, cudaStream_t st);
 
 }  // namespace rdn

@@ -31,7 +31,7 @@ EXPORTED_SYMBOLS = [
     "rdn_attr_paths_graph", "rdn_check_errors", "rdn_set_iteration_limit", "rdn_task_graph_create",
     "rdn_task_graph_destroy", "rdn_task_graph_dispatch_init", "rdn_task_graph_execute", "rdn_task_graph_states",
     "rdn_task_graph_debug", "rdn_task_graph_check_errors", "rdn_ao_pipeline_create", "rdn_ao_render_graph",
-    "rdn_ao_render",
+    "rdn_ao_render", "rdn_ao_capture",
 ]
 
 
@@ -133,7 +133,7 @@ class AoDesc(C.Structure):
                 ("height", C.c_uint32), ("sample_count", C.c_uint32), ("tlas_uniform", C.c_uint32),
                 ("traversal", C.c_uint32), ("normals", C.c_void_p), ("image", C.c_void_p),
                 ("sbt_closest", C.c_uint32 * 2), ("sbt_miss", C.c_uint32), ("pad", C.c_uint32),
-                ("ray_counts", C.c_void_p)]
+                ("ray_counts", C.c_void_p), ("sample_counter", C.c_void_p)]
 
 
 _lib = None
@@ -233,5 +233,7 @@ def lib() -> C.CDLL:
     L.rdn_ao_render_graph.restype = i32
     L.rdn_ao_render.argtypes = [vp, C.POINTER(AoDesc), vp]
     L.rdn_ao_render.restype = i32
+    L.rdn_ao_capture.argtypes = [vp, vp, C.POINTER(AoDesc), C.POINTER(vp)]
+    L.rdn_ao_capture.restype = i32
     _lib = L
     return L

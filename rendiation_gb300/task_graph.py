@@ -255,9 +255,33 @@ class AmbientOcclusion:
         elif mode != "fused":
             raise ValueError("mode is 'fused' or 'graph'")
 
-    def desc(self):
-        return ao_desc(self.width, self.height, self.vp_inv, self.cam, self.image, self.sample_count,
-                       self.tlas_uniform, self.traversal, self.normals)
+    def desc(self, counter=None):
+        d = ao_desc(self.width, self.height, self.vp_inv, self.cam, self.image, self.sample_count,
+                    self.tlas_uniform, self.traversal, self.normals)
+        if counter is not None:
+            d.sample_counter = counter.data_ptr()
+        return d
+
+    def capture(self, counter):
+        """One frame captured into a CUDA graph (rdn_ao_capture) that reads its
+        sample index from `counter` (a CUDA int32 tensor of one element) and
+        advances it; returns a callable that replays the frame."""
+        d = self.desc(counter)
+        g = C.c_void_p()
+        pipe = self.graph._h if self.graph is not None else None
+        _check(self.system._h, self.system._L.rdn_ao_capture(self.system._h, pipe, C.byref(d), C.byref(g)))
+        L = self.system._L
+
+        class Frame:
+            def __call__(self_inner, stream=None):
+                st = L.rdn_graph_launch(g, _stream(stream))
+                if st != native.RDN_OK:
+                    raise native.RdnError(st, "rdn_graph_launch")
+
+            def __del__(self_inner):
+                L.rdn_graph_destroy(g)
+
+        return Frame()
 
     def render(self, stream=None):
         d = self.desc()

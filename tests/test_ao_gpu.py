@@ -133,3 +133,32 @@ def test_frozen_after_256_samples(cuda):
     torch.cuda.synchronize()
     assert np.array_equal(ao.result()[..., :3], before[..., :3])
     assert np.all(ao.result()[..., 3] == 255)
+
+
+@pytest.mark.parametrize("mode", ["fused", "graph"])
+def test_captured_frame_advances_its_sample(cuda, mode):
+    """rdn_ao_capture: a frame that reads its sample index from a device counter
+    and advances it; three replays equal three frames with host-side counts."""
+    import torch
+
+    scene = field_scene()
+    P = scene.build_product()
+    vp, eye = camera()
+    ref = tg.AmbientOcclusion(P, W, H, vp, eye, traversal=rt.TRAVERSAL_ORDERED_WIDE, mode=mode)
+    for s in SAMPLES:
+        ref.sample_count = s
+        ref.render()
+    cap = tg.AmbientOcclusion(P, W, H, vp, eye, traversal=rt.TRAVERSAL_ORDERED_WIDE, mode=mode)
+    counter = torch.tensor([150], dtype=torch.int32, device="cuda")
+    frame = cap.capture(counter)
+    # the captured frame draws samples 150, 151, 152: compare with those host counts
+    ref2 = tg.AmbientOcclusion(P, W, H, vp, eye, traversal=rt.TRAVERSAL_ORDERED_WIDE, mode=mode)
+    for s in (150, 151, 152):
+        ref2.sample_count = s
+        ref2.render()
+        frame()
+    torch.cuda.synchronize()
+    assert int(counter.item()) == 153
+    assert np.array_equal(cap.result(), ref2.result())
+    assert not np.array_equal(ref2.result(), ref.result())  # the sample indices matter
+    assert P.check_errors() == (0, 0)
