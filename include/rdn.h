@@ -629,6 +629,15 @@ rdn_status rdn_task_graph_states(rdn_task_graph* graph, uint32_t* wake, uint32_t
 rdn_status rdn_task_graph_debug(rdn_task_graph* graph, uint32_t group, uint32_t* active, uint32_t* n_active,
                                 uint32_t* empty, uint32_t* n_empty, uint32_t* task_states, void* stream);
 rdn_status rdn_task_graph_check_errors(rdn_task_graph* graph, void* stream, uint32_t* flags);
+/* dispatch_init of `count` root tasks in `group`, then rounds until no group
+ * holds an active task, at most max_rounds, captured into an executable CUDA
+ * graph (rdn_graph_launch / rdn_graph_destroy). The loop is a conditional node
+ * that the device ends after the first round that leaves no task active: no
+ * host round trip and no idle rounds. The graph is then empty, unless a spawn
+ * found a pool full and its parent waits for ever (as in the reference). env is baked in, as for
+ * rdn_task_graph_execute; a graph that traces needs the structure built. */
+rdn_status rdn_task_graph_capture(rdn_task_graph* graph, uint32_t group, uint32_t count, uint32_t init_op,
+                                  uint32_t max_rounds, const rdn_ao_desc* env, rdn_graph** out);
 
 /* The reference's AO pipeline as a task graph (feature/ao.rs:162-313 on
  * trace_ray): group 0 ray-trace task (max_in_flight 2), 1 ray generation,
@@ -644,7 +653,8 @@ rdn_status rdn_ao_render_graph(rdn_task_graph* graph, const rdn_ao_desc* desc, v
 /* The same frame as one fused kernel, one thread per pixel. */
 rdn_status rdn_ao_render(rdn_ctx* ctx, const rdn_ao_desc* desc, void* stream);
 /* One AO frame captured into an executable CUDA graph: the fused kernel
- * (pipeline NULL) or the task-graph pipeline's dispatch and 8 rounds. The
+ * (pipeline NULL) or the task-graph pipeline's dispatch and rounds until the
+ * pipeline is empty (at most 8, ended on the device). The
  * descriptor is baked in; with desc->sample_counter set, each rdn_graph_launch
  * draws the next sample. The context's structure must stay built and the
  * buffers alive while the graph is in use. */

@@ -1204,25 +1204,103 @@ rdn_status rdn_task_graph_dispatch_init(rdn_task_graph* g, uint32_t group, uint3
   return RDN_OK;
 }
 
-rdn_status rdn_task_graph_execute(rdn_task_graph* g, uint32_t rounds, const rdn_ao_desc* env, void* stream) {
-  if (!g) return RDN_ERR_INVALID_ARG;
+}  // extern "C"
+
+namespace {
+
+// `rounds` rounds of every group; with until_empty (inside a stream capture
+// only) a device-ended loop of at most `rounds` rounds instead.
+rdn_status run_rounds(rdn_task_graph* g, uint32_t rounds, const rdn_ao_desc* env, cudaStream_t s, bool until_empty) {
   rdn_ctx* c = g->ctx;
   cudaError_t e = cudaSetDevice(c->device);
   if (e != cudaSuccess) return cuda_fail(c, e, "cudaSetDevice");
-  if (!g->needs_env) {
-    e = g->graph.execute(rounds, nullptr, rdn::MODE_THREADED, nullptr, static_cast<cudaStream_t>(stream));
-    if (e != cudaSuccess) return cuda_fail(c, e, "task graph execute");
-    return RDN_OK;
-  }
-  if (!env) return fail(c, RDN_ERR_INVALID_ARG, "this graph traces or shades: pass an rdn_ao_desc environment");
-  std::lock_guard<std::mutex> lk(c->lock);
   rdn::TraceParams p;
   rdn::AoEnv a;
-  rdn_status st = ao_env(c, env, p, a);
-  if (st != RDN_OK) return st;
-  e = g->graph.execute(rounds, &p, mode_of(env->traversal), &a, static_cast<cudaStream_t>(stream));
-  if (e != cudaSuccess) return cuda_fail(c, e, "task graph execute");
+  const rdn::TraceParams* pp = nullptr;
+  const rdn::AoEnv* ap = nullptr;
+  int mode = rdn::MODE_THREADED;
+  std::unique_lock<std::mutex> lk(c->lock, std::defer_lock);
+  if (g->needs_env) {
+    if (!env) return fail(c, RDN_ERR_INVALID_ARG, "this graph traces or shades: pass an rdn_ao_desc environment");
+    lk.lock();
+    rdn_status st = ao_env(c, env, p, a);
+    if (st != RDN_OK) return st;
+    pp = &p;
+    ap = &a;
+    mode = mode_of(env->traversal);
+  }
+  e = until_empty ? g->graph.record_until_empty(rounds, pp, mode, ap, s) : g->graph.execute(rounds, pp, mode, ap, s);
+  if (e != cudaSuccess) return cuda_fail(c, e, until_empty ? "task graph drain loop" : "task graph execute");
   return RDN_OK;
+}
+
+// Captures record(stream) into an executable graph.
+template <class F>
+rdn_status capture_graph(rdn_ctx* c, const char* what, F record, rdn_graph** out) {
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e != cudaSuccess) return cuda_fail(c, e, "cudaSetDevice");
+  cudaStream_t s = nullptr;
+  e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return cuda_fail(c, e, "capture stream");
+  auto* g = new (std::nothrow) rdn_graph();
+  if (!g) {
+    cudaStreamDestroy(s);
+    return fail(c, RDN_ERR_OOM, "host allocation failed");
+  }
+  g->device = c->device;
+  rdn_status st = RDN_OK;
+  e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    st = record(s);
+    e = cudaStreamEndCapture(s, &g->graph);
+  }
+  if (e == cudaSuccess && st == RDN_OK) e = cudaGraphInstantiate(&g->exec, g->graph, 0);
+  cudaStreamDestroy(s);
+  if (e != cudaSuccess || st != RDN_OK) {
+    if (g->graph) cudaGraphDestroy(g->graph);
+    delete g;
+    return st != RDN_OK ? st : cuda_fail(c, e, what);
+  }
+  *out = g;
+  return RDN_OK;
+}
+
+rdn_status require_built(rdn_ctx* c) {
+  std::lock_guard<std::mutex> lk(c->lock);
+  // a build allocates and synchronises, which a capture cannot hold
+  if (c->dirty || !c->host) return fail(c, RDN_ERR_NOT_BUILT, "build the structure before capturing");
+  return RDN_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+rdn_status rdn_task_graph_execute(rdn_task_graph* g, uint32_t rounds, const rdn_ao_desc* env, void* stream) {
+  if (!g) return RDN_ERR_INVALID_ARG;
+  return run_rounds(g, rounds, env, static_cast<cudaStream_t>(stream), false);
+}
+
+rdn_status rdn_task_graph_capture(rdn_task_graph* g, uint32_t group, uint32_t count, uint32_t init_op,
+                                  uint32_t max_rounds, const rdn_ao_desc* env, rdn_graph** out) {
+  if (!g || !out) return RDN_ERR_INVALID_ARG;
+  *out = nullptr;
+  rdn_ctx* c = g->ctx;
+  if (group >= g->graph.group_count()) return fail(c, RDN_ERR_INVALID_ARG, "no such task group");
+  if (init_op > RDN_TASK_INIT_INDEX) return fail(c, RDN_ERR_INVALID_ARG, "unknown init payload");
+  if (max_rounds == 0) return fail(c, RDN_ERR_INVALID_ARG, "max_rounds must be at least 1");
+  if (g->needs_env) {
+    rdn_status st = require_built(c);
+    if (st != RDN_OK) return st;
+  }
+  return capture_graph(
+      c, "task graph capture",
+      [&](cudaStream_t s) {
+        cudaError_t e = g->graph.dispatch_init(group, count, init_op, s);
+        if (e != cudaSuccess) return cuda_fail(c, e, "task graph dispatch");
+        return run_rounds(g, max_rounds, env, s, true);
+      },
+      out);
 }
 
 rdn_status rdn_task_graph_states(rdn_task_graph* g, uint32_t* wake, uint32_t* sleep_or_finished, uint32_t* empty,
@@ -1306,8 +1384,13 @@ rdn_status rdn_ao_pipeline_create(rdn_ctx* c, uint32_t width, uint32_t height, v
   return RDN_OK;
 }
 
-rdn_status rdn_ao_render_graph(rdn_task_graph* g, const rdn_ao_desc* d, void* stream) {
-  if (!g || !d) return RDN_ERR_INVALID_ARG;
+}  // extern "C"
+
+namespace {
+
+// One AO frame on the pipeline graph: dispatch, then the reference's 8 rounds,
+// or (inside a capture) a device-ended loop of at most 8 rounds.
+rdn_status ao_graph_frame(rdn_task_graph* g, const rdn_ao_desc* d, cudaStream_t s, bool until_empty) {
   rdn_ctx* c = g->ctx;
   if (!g->ao_pipeline) return fail(c, RDN_ERR_INVALID_ARG, "not an AO pipeline graph");
   if (d->width != g->width || d->height != g->height)
@@ -1316,12 +1399,23 @@ rdn_status rdn_ao_render_graph(rdn_task_graph* g, const rdn_ao_desc* d, void* st
   env.sbt_closest[0] = 2;
   env.sbt_closest[1] = 3;
   env.sbt_miss = 4;
-  rdn_status st =
-      rdn_task_graph_dispatch_init(g, 1, rdn::ao_dispatch_count(d->width, d->height), RDN_TASK_INIT_INDEX, stream);
-  if (st == RDN_OK) st = rdn_task_graph_execute(g, 8, &env, stream);
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e == cudaSuccess)
+    e = g->graph.dispatch_init(1, rdn::ao_dispatch_count(d->width, d->height), RDN_TASK_INIT_INDEX, s);
+  if (e != cudaSuccess) return cuda_fail(c, e, "task graph dispatch");
+  rdn_status st = run_rounds(g, 8, &env, s, until_empty);
   if (st != RDN_OK || !d->sample_counter) return st;
-  cudaError_t e = rdn::launch_ao_advance(d->sample_counter, static_cast<cudaStream_t>(stream));
+  e = rdn::launch_ao_advance(d->sample_counter, s);
   return e == cudaSuccess ? RDN_OK : cuda_fail(c, e, "AO sample counter");
+}
+
+}  // namespace
+
+extern "C" {
+
+rdn_status rdn_ao_render_graph(rdn_task_graph* g, const rdn_ao_desc* d, void* stream) {
+  if (!g || !d) return RDN_ERR_INVALID_ARG;
+  return ao_graph_frame(g, d, static_cast<cudaStream_t>(stream), false);
 }
 
 rdn_status rdn_ao_render(rdn_ctx* c, const rdn_ao_desc* d, void* stream) {
@@ -1346,37 +1440,12 @@ rdn_status rdn_ao_capture(rdn_ctx* c, rdn_task_graph* pipeline, const rdn_ao_des
   *out = nullptr;
   if (c->device < 0) return fail(c, RDN_ERR_UNSUPPORTED, "host-only context cannot trace");
   if (pipeline && pipeline->ctx != c) return fail(c, RDN_ERR_INVALID_ARG, "the pipeline belongs to another context");
-  {
-    std::lock_guard<std::mutex> lk(c->lock);
-    // a build allocates and synchronises, which a capture cannot hold
-    if (c->dirty || !c->host) return fail(c, RDN_ERR_NOT_BUILT, "build the structure before capturing a frame");
-  }
-  cudaError_t e = cudaSetDevice(c->device);
-  if (e != cudaSuccess) return cuda_fail(c, e, "cudaSetDevice");
-  cudaStream_t s = nullptr;
-  e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
-  if (e != cudaSuccess) return cuda_fail(c, e, "capture stream");
-  auto* g = new (std::nothrow) rdn_graph();
-  if (!g) {
-    cudaStreamDestroy(s);
-    return fail(c, RDN_ERR_OOM, "host allocation failed");
-  }
-  g->device = c->device;
-  rdn_status st = RDN_OK;
-  e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
-  if (e == cudaSuccess) {
-    st = pipeline ? rdn_ao_render_graph(pipeline, d, s) : rdn_ao_render(c, d, s);
-    e = cudaStreamEndCapture(s, &g->graph);
-  }
-  if (e == cudaSuccess && st == RDN_OK) e = cudaGraphInstantiate(&g->exec, g->graph, 0);
-  cudaStreamDestroy(s);
-  if (e != cudaSuccess || st != RDN_OK) {
-    if (g->graph) cudaGraphDestroy(g->graph);
-    delete g;
-    return st != RDN_OK ? st : cuda_fail(c, e, "AO frame capture");
-  }
-  *out = g;
-  return RDN_OK;
+  rdn_status st = require_built(c);
+  if (st != RDN_OK) return st;
+  return capture_graph(
+      c, "AO frame capture",
+      [&](cudaStream_t s) { return pipeline ? ao_graph_frame(pipeline, d, s, true) : rdn_ao_render(c, d, s); },
+      out);
 }
 
 }  // extern "C"

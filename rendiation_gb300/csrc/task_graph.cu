@@ -555,6 +555,30 @@ __global__ void spawn_init_kernel(const TaskGraphDev* __restrict__ Gp, uint32_t 
   }
 }
 
+// Drain loop of a captured graph (a WHILE conditional node): the round counter
+// is reset before the loop; after each round one warp looks for an active
+// entry in any group (committed or pushed since), and the loop ends when there
+// is none or after max_rounds rounds. Without an active task no later round
+// can change anything: only a polled task spawns or wakes another, so the
+// graph is then either empty or holds tasks that wait for children whose
+// spawn failed (RDN_TASK_ERROR_NO_FREE_SLOT).
+__global__ void loop_reset_kernel(uint32_t* rounds) { *rounds = 0u; }
+
+__global__ void loop_check_kernel(const TaskGraphDev* __restrict__ G, uint32_t* rounds, uint32_t max_rounds,
+                                  cudaGraphConditionalHandle handle) {
+  bool busy = false;
+  for (uint32_t g = threadIdx.x; g < G->n_groups; g += 32) {
+    const GroupCtl* c = G->g[g].ctl;
+    busy |= c->active.size + c->active.bump != 0u;
+  }
+  busy = __any_sync(0xFFFFFFFFu, busy);
+  if (threadIdx.x == 0) {
+    const uint32_t r = *rounds + 1u;
+    *rounds = r;
+    cudaGraphSetConditional(handle, busy && r < max_rounds ? 1u : 0u);
+  }
+}
+
 uint32_t tiles_of(uint32_t cap) { return (cap + kTile - 1) / kTile; }
 
 template <int MODE, bool LOCAL>
@@ -798,6 +822,49 @@ cudaError_t TaskGraph::debug(uint32_t group, std::vector<uint32_t>& active, std:
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(task_states.data(), T.state, 4 * ((size_t)T.cap + 1), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  return e;
+}
+
+cudaError_t TaskGraph::record_until_empty(uint32_t max_rounds, const TraceParams* p, int mode, const AoEnv* ao,
+                                          cudaStream_t cap) {
+  uint32_t* rounds = dev_.error + 40;
+  loop_reset_kernel<<<1, 1, 0, cap>>>(rounds);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  cudaStreamCaptureStatus status;
+  cudaGraph_t graph = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t n_deps = 0;
+  e = cudaStreamGetCaptureInfo(cap, &status, nullptr, &graph, &deps, nullptr, &n_deps);
+  if (e != cudaSuccess) return e;
+  if (status != cudaStreamCaptureStatusActive) return cudaErrorStreamCaptureImplicit;
+  cudaGraphConditionalHandle handle;
+  e = cudaGraphConditionalHandleCreate(&handle, graph, 1u, cudaGraphCondAssignDefault);
+  if (e != cudaSuccess) return e;
+  cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};  // the remaining members zero
+  cp.conditional.handle = handle;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t node;
+  e = cudaGraphAddNode(&node, graph, deps, nullptr, n_deps, &cp);
+  if (e != cudaSuccess) return e;
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  e = cudaStreamUpdateCaptureDependencies(cap, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+  if (e != cudaSuccess) return e;
+  cudaStream_t bs = nullptr;
+  e = cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return e;
+  e = cudaStreamBeginCaptureToGraph(bs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    cudaError_t rec = execute(1, p, mode, ao, bs);
+    if (rec == cudaSuccess) {
+      loop_check_kernel<<<1, 32, 0, bs>>>(dev_ptr_, rounds, max_rounds, handle);
+      rec = cudaGetLastError();
+    }
+    e = cudaStreamEndCapture(bs, &body);
+    if (rec != cudaSuccess) e = rec;
+  }
+  cudaStreamDestroy(bs);
   return e;
 }
 

@@ -183,6 +183,11 @@ class TaskGraph {
   cudaError_t debug(uint32_t group, std::vector<uint32_t>& active, std::vector<uint32_t>& empty,
                     std::vector<uint32_t>& task_states, cudaStream_t st);
   cudaError_t read_error(uint32_t* flags, cudaStream_t st);
+  // Into the stream being captured: rounds until no group holds a task, at
+  // most max_rounds, as a WHILE conditional node (the device decides after
+  // each round; the host issues nothing per round).
+  cudaError_t record_until_empty(uint32_t max_rounds, const TraceParams* p, int mode, const AoEnv* ao,
+                                 cudaStream_t capturing);
 
   uint32_t group_count() const { return dev_.n_groups; }
   uint32_t group_cap(uint32_t g) const { return dev_.g[g].cap; }

@@ -172,6 +172,28 @@ class DeviceTaskGraphExecutor:
             out.append(TaskExecutionDebugInfo(active[:na.value].tolist(), empty[:ne.value].tolist(), states.tolist()))
         return out
 
+    def capture_until_empty(self, task_count: int, task_id: int, init: int = INIT_ZERO, max_rounds: int = 1024,
+                            env: "native.AoDesc | None" = None):
+        """dispatch_allocate_init_task then rounds until every group is empty (at
+        most max_rounds) as one CUDA graph whose loop the device ends
+        (rdn_task_graph_capture). Returns a callable that launches it."""
+        g = C.c_void_p()
+        _check(self.system._h, self._L.rdn_task_graph_capture(self._h, task_id, task_count, init, max_rounds,
+                                                              C.byref(env) if env is not None else None,
+                                                              C.byref(g)))
+        L = self._L
+
+        class Launch:
+            def __call__(self_inner, stream=None):
+                st = L.rdn_graph_launch(g, _stream(stream))
+                if st != native.RDN_OK:
+                    raise native.RdnError(st, "rdn_graph_launch")
+
+            def __del__(self_inner):
+                L.rdn_graph_destroy(g)
+
+        return Launch()
+
     def check_errors(self, stream=None) -> int:
         f = C.c_uint32()
         _check(self.system._h, self._L.rdn_task_graph_check_errors(self._h, _stream(stream), C.byref(f)))

@@ -196,3 +196,44 @@ def test_invalid_graphs_are_rejected(system):
     exe = src.build(system)
     with pytest.raises(native.RdnError, match="environment"):
         exe.execute(1)
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_captured_drain_loop_empties_the_graph(system, seed):
+    """rdn_task_graph_capture: dispatch + a device-ended loop of rounds; one
+    launch leaves the graph where the oracle's rounds leave it once no task is
+    active: empty, or (where a small pool overflowed) with the same waiting tasks."""
+    rnd = random.Random(2000 + seed)
+    n = rnd.randint(2, 6)
+    groups = []
+    for gi in range(n):
+        k = rnd.randint(1, 4) if gi < n - 1 else 0
+        groups.append((tuple(rnd.randrange(gi + 1, n) for _ in range(k)), rnd.randint(1, 3)))
+    exe = build(system, groups, 64)
+    ora = OracleTaskGraph(groups, 64)
+    cnt = rnd.randint(1, 40)
+    ora.dispatch_allocate_init_task(cnt, 0)
+    launch = exe.capture_until_empty(cnt, 0, max_rounds=4096)
+    launch()
+    for _ in range(2000):
+        ora.execute(1)
+        if not any(ora.read_back_execution_states()[0]):
+            break
+    got = exe.read_back_execution_states()
+    assert (got.wake_counts, got.sleep_or_finished_counts, got.empty_counts) == ora.read_back_execution_states()
+    assert bool(exe.check_errors()) == bool(ora.error)
+    if not ora.error:
+        assert got.is_empty()
+        launch()  # a second launch dispatches and drains again
+        assert exe.read_back_execution_states().is_empty()
+
+
+def test_captured_drain_loop_stops_at_max_rounds(system):
+    # self-spawning chain (test.rs:142-198): never empties; the loop must stop
+    src = tg.DeviceTaskGraphBuildSource(capacity=8)
+    t = src.define_task(tg.BaseShaderFuture().then_spawn_task(0).map(), 4)
+    exe = src.build(system)
+    launch = exe.capture_until_empty(3, t, max_rounds=3)
+    launch()
+    info = exe.read_back_execution_states()
+    assert info.wake_counts[t] == 3 and info.sleep_or_finished_counts[t] == 9
