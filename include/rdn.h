@@ -548,6 +548,8 @@ rdn_status rdn_wavefront_shadow_bounce_static(rdn_ctx* ctx, const rdn_wavefront_
 #define RDN_TASK_MAX_GROUPS 16u
 #define RDN_TASK_PROGRAM_CHAIN 0u
 #define RDN_TASK_PROGRAM_TRACE 1u
+#define RDN_TASK_PROGRAM_EXTERNAL 2u    /* polled by a kernel of the caller's (include/rdn_task.cuh), launched by
+                                           the callback given to rdn_task_graph_set_poll */
 #define RDN_TASK_SPAWN_ZERO 0u          /* zeroed child payload */
 #define RDN_TASK_SPAWN_AO_PRIMARY 1u    /* AO ray generation: payload word 0 = pixel -> camera trace call */
 #define RDN_TASK_SPAWN_AO_OCCLUSION 2u  /* AO primary closest hit -> occlusion-ray trace call */
@@ -629,6 +631,14 @@ rdn_status rdn_task_graph_states(rdn_task_graph* graph, uint32_t* wake, uint32_t
 rdn_status rdn_task_graph_debug(rdn_task_graph* graph, uint32_t group, uint32_t* active, uint32_t* n_active,
                                 uint32_t* empty, uint32_t* n_empty, uint32_t* task_states, void* stream);
 rdn_status rdn_task_graph_check_errors(rdn_task_graph* graph, void* stream, uint32_t* flags);
+/* Poll of an RDN_TASK_PROGRAM_EXTERNAL group: the executor calls fn once per
+ * round where it would launch a built-in poll, with the device graph table,
+ * the group, its max_in_flight * capacity and the stream (captures included);
+ * fn launches the caller's poll kernel (rdn_task::launch in rdn_task.cuh) and
+ * returns RDN_OK. */
+typedef rdn_status (*rdn_task_poll_fn)(const void* graph_device, uint32_t group, uint32_t group_capacity,
+                                       void* stream, void* user);
+rdn_status rdn_task_graph_set_poll(rdn_task_graph* graph, uint32_t group, rdn_task_poll_fn fn, void* user);
 /* dispatch_init of `count` root tasks in `group`, then rounds until no group
  * holds an active task, at most max_rounds, captured into an executable CUDA
  * graph (rdn_graph_launch / rdn_graph_destroy). The loop is a conditional node

@@ -1212,6 +1212,8 @@ namespace {
 // only) a device-ended loop of at most `rounds` rounds instead.
 rdn_status run_rounds(rdn_task_graph* g, uint32_t rounds, const rdn_ao_desc* env, cudaStream_t s, bool until_empty) {
   rdn_ctx* c = g->ctx;
+  const std::string missing = g->graph.check_external();
+  if (!missing.empty()) return fail(c, RDN_ERR_INVALID_ARG, missing);
   cudaError_t e = cudaSetDevice(c->device);
   if (e != cudaSuccess) return cuda_fail(c, e, "cudaSetDevice");
   rdn::TraceParams p;
@@ -1279,6 +1281,16 @@ extern "C" {
 rdn_status rdn_task_graph_execute(rdn_task_graph* g, uint32_t rounds, const rdn_ao_desc* env, void* stream) {
   if (!g) return RDN_ERR_INVALID_ARG;
   return run_rounds(g, rounds, env, static_cast<cudaStream_t>(stream), false);
+}
+
+rdn_status rdn_task_graph_set_poll(rdn_task_graph* g, uint32_t group, rdn_task_poll_fn fn, void* user) {
+  if (!g) return RDN_ERR_INVALID_ARG;
+  rdn_ctx* c = g->ctx;
+  if (group >= g->graph.group_count()) return fail(c, RDN_ERR_INVALID_ARG, "no such task group");
+  if (g->graph.groups()[group].program != RDN_TASK_PROGRAM_EXTERNAL)
+    return fail(c, RDN_ERR_INVALID_ARG, "the group runs a built-in program");
+  g->graph.set_external(group, reinterpret_cast<rdn::ExternalPoll>(fn), user);
+  return RDN_OK;
 }
 
 rdn_status rdn_task_graph_capture(rdn_task_graph* g, uint32_t group, uint32_t count, uint32_t init_op,

@@ -61,7 +61,13 @@ constexpr uint32_t TASK_ERR_REMOVED_FULL = 0x4;  // a removed-list push past its
 // polled once, [1..4] child handles of the chain's spawn stages, [5] trace
 // sub-task group, [6] trace sub-task id, [7] trace has_terminated.
 // Programs
-enum : uint32_t { TASK_PROGRAM_CHAIN = 0, TASK_PROGRAM_TRACE = 1 };
+// EXTERNAL: polled by a kernel compiled outside librdn (include/rdn_task.cuh)
+// that a host callback launches.
+enum : uint32_t { TASK_PROGRAM_CHAIN = 0, TASK_PROGRAM_TRACE = 1, TASK_PROGRAM_EXTERNAL = 2 };
+// Host callback that launches an external program's poll kernel on `stream`
+// for group `group` of the device graph table `graph_device` (returns 0 on success).
+using ExternalPoll = int32_t (*)(const void* graph_device, uint32_t group, uint32_t group_capacity, void* stream,
+                                 void* user);
 // payload of a spawned child
 enum : uint32_t {
   TASK_SPAWN_ZERO = 0,          // zeroed payload
@@ -183,6 +189,12 @@ class TaskGraph {
   cudaError_t debug(uint32_t group, std::vector<uint32_t>& active, std::vector<uint32_t>& empty,
                     std::vector<uint32_t>& task_states, cudaStream_t st);
   cudaError_t read_error(uint32_t* flags, cudaStream_t st);
+  void set_external(uint32_t g, ExternalPoll fn, void* user) {
+    ext_fn_[g] = fn;
+    ext_user_[g] = user;
+  }
+  // "" when every EXTERNAL group has a poll callback
+  std::string check_external() const;
   // Into the stream being captured: rounds until no group holds a task, at
   // most max_rounds, as a WHILE conditional node (the device decides after
   // each round; the host issues nothing per round).
@@ -200,6 +212,8 @@ class TaskGraph {
 
   TaskGraphDev dev_{};
   TaskGraphDev* dev_ptr_ = nullptr;  // device copy of dev_
+  std::vector<ExternalPoll> ext_fn_;
+  std::vector<void*> ext_user_;
   std::vector<TaskGroupDesc> desc_;
   std::vector<void*> allocs_;
   int sm_count_ = 1;

@@ -31,7 +31,7 @@ EXPORTED_SYMBOLS = [
     "rdn_attr_paths_graph", "rdn_check_errors", "rdn_set_iteration_limit", "rdn_task_graph_create",
     "rdn_task_graph_destroy", "rdn_task_graph_dispatch_init", "rdn_task_graph_execute", "rdn_task_graph_states",
     "rdn_task_graph_debug", "rdn_task_graph_check_errors", "rdn_ao_pipeline_create", "rdn_ao_render_graph",
-    "rdn_ao_render", "rdn_ao_capture", "rdn_task_graph_capture",
+    "rdn_ao_render", "rdn_ao_capture", "rdn_task_graph_capture", "rdn_task_graph_set_poll",
 ]
 
 
@@ -237,5 +237,7 @@ def lib() -> C.CDLL:
     L.rdn_ao_capture.restype = i32
     L.rdn_task_graph_capture.argtypes = [vp, u32, u32, u32, u32, C.POINTER(AoDesc), C.POINTER(vp)]
     L.rdn_task_graph_capture.restype = i32
+    L.rdn_task_graph_set_poll.argtypes = [vp, u32, vp, vp]
+    L.rdn_task_graph_set_poll.restype = i32
     _lib = L
     return L

@@ -24,7 +24,7 @@ import numpy as np
 from . import native
 from .raytracing import TRAVERSAL_ORDERED_WIDE, _check
 
-PROGRAM_CHAIN, PROGRAM_TRACE = 0, 1
+PROGRAM_CHAIN, PROGRAM_TRACE, PROGRAM_EXTERNAL = 0, 1, 2
 SPAWN_ZERO, SPAWN_AO_PRIMARY, SPAWN_AO_OCCLUSION = 0, 1, 2
 MAP_NONE, MAP_AO_ACCUMULATE, MAP_STORE_CHILD, MAP_STORE_ZERO, MAP_STORE_ONE = 0, 1, 2, 3, 4
 INIT_ZERO, INIT_INDEX = 0, 1
@@ -59,6 +59,12 @@ def BaseShaderFuture() -> ShaderFuture:  # noqa: N802 - the reference's name
 
 def TraceTaskFuture() -> ShaderFuture:  # noqa: N802
     return ShaderFuture(program=PROGRAM_TRACE)
+
+
+def ExternalFuture() -> ShaderFuture:  # noqa: N802
+    """A task polled by a CUDA C++ program of the caller's (include/rdn_task.cuh);
+    register its launcher with DeviceTaskGraphExecutor.set_poll."""
+    return ShaderFuture(program=PROGRAM_EXTERNAL)
 
 
 @dataclass
@@ -193,6 +199,11 @@ class DeviceTaskGraphExecutor:
                 L.rdn_graph_destroy(g)
 
         return Launch()
+
+    def set_poll(self, task_id: int, fn_ptr: int, user: int | None = None):
+        """Registers the launcher (an rdn_task_poll_fn address) of an external program."""
+        _check(self.system._h, self._L.rdn_task_graph_set_poll(self._h, task_id, C.c_void_p(fn_ptr),
+                                                               C.c_void_p(user) if user else None))
 
     def check_errors(self, stream=None) -> int:
         f = C.c_uint32()

@@ -16,6 +16,7 @@ from rendiation_gb300 import native
 def header_functions():
     txt = open(os.path.join(ROOT, "include", "rdn.h")).read()
     txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    txt = re.sub(r"typedef\s+rdn_status\s*\(\*[^;]*;", "", txt)  # function-pointer types
     return sorted(set(re.findall(r"\b(rdn_[a-z0-9_]+)\s*\(", txt)))
 
 
