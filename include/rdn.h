@@ -619,7 +619,8 @@ rdn_status rdn_task_graph_dispatch_init(rdn_task_graph* graph, uint32_t group, u
                                         void* stream);
 /* execute (runtime/mod.rs:357-397): rounds x (every group in order: prepare,
  * poll, compact). env: NULL when no group runs a TRACE program or an AO
- * operation. */
+ * operation; without AO operations only its traversal and tlas_uniform
+ * fields are read. */
 rdn_status rdn_task_graph_execute(rdn_task_graph* graph, uint32_t rounds, const rdn_ao_desc* env, void* stream);
 /* read_back_execution_states: wake, sleep_or_finished and empty counts per
  * group (arrays of the graph's group count); waits for the stream. */

@@ -1100,17 +1100,23 @@ struct rdn_task_graph {
   rdn_ctx* ctx = nullptr;
   rdn::TaskGraph graph;
   bool needs_env = false;    // a TRACE program or an AO operation
+  bool uses_ao = false;      // an AO operation (reads the camera and writes the image)
   bool ao_pipeline = false;  // made by rdn_ao_pipeline_create
   uint32_t width = 0, height = 0;
 };
 
 namespace {
 
-rdn_status ao_env(rdn_ctx* c, const rdn_ao_desc* d, rdn::TraceParams& p, rdn::AoEnv& a) {
-  if (!d->image) return fail(c, RDN_ERR_INVALID_ARG, "null AO image");
-  if (reinterpret_cast<uintptr_t>(d->image) & 3) return fail(c, RDN_ERR_INVALID_ARG, "AO image must be 4-byte aligned");
-  if (d->width == 0 || d->height == 0 || (uint64_t)d->width * d->height > 0x7FFFFFFFull)
-    return fail(c, RDN_ERR_INVALID_ARG, "AO frame size must be 1..2^31 pixels");
+// need_image: the launch runs AO operations (a trace-only task graph reads the
+// traversal fields alone).
+rdn_status ao_env(rdn_ctx* c, const rdn_ao_desc* d, rdn::TraceParams& p, rdn::AoEnv& a, bool need_image = true) {
+  if (need_image) {
+    if (!d->image) return fail(c, RDN_ERR_INVALID_ARG, "null AO image");
+    if (reinterpret_cast<uintptr_t>(d->image) & 3)
+      return fail(c, RDN_ERR_INVALID_ARG, "AO image must be 4-byte aligned");
+    if (d->width == 0 || d->height == 0 || (uint64_t)d->width * d->height > 0x7FFFFFFFull)
+      return fail(c, RDN_ERR_INVALID_ARG, "AO frame size must be 1..2^31 pixels");
+  }
   if (d->traversal > RDN_TRAVERSAL_ORDERED_WIDE) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
   rdn_status st = ensure_built(c);
   if (st != RDN_OK) return st;
@@ -1152,7 +1158,7 @@ rdn_status rdn_task_graph_create(rdn_ctx* c, const rdn_task_group_desc* groups, 
   *out = nullptr;
   if (count > RDN_TASK_MAX_GROUPS) return fail(c, RDN_ERR_INVALID_ARG, "a task graph holds 1 to 16 task groups");
   std::vector<rdn::TaskGroupDesc> desc(count);
-  bool needs_env = false;
+  bool needs_env = false, uses_ao = false;
   for (uint32_t g = 0; g < count; g++) {
     rdn::TaskGroupDesc& d = desc[g];
     d.program = groups[g].program;
@@ -1163,9 +1169,10 @@ rdn_status rdn_task_graph_create(rdn_ctx* c, const rdn_task_group_desc* groups, 
     for (uint32_t k = 0; k < 4; k++) {
       d.spawn_type[k] = groups[g].spawn_type[k];
       d.spawn_op[k] = k < d.n_spawn ? groups[g].spawn_op[k] : 0u;
-      if (k < d.n_spawn && d.spawn_op[k] != RDN_TASK_SPAWN_ZERO) needs_env = true;
+      if (k < d.n_spawn && d.spawn_op[k] != RDN_TASK_SPAWN_ZERO) needs_env = uses_ao = true;
     }
-    if (d.program == RDN_TASK_PROGRAM_TRACE || d.map_op == RDN_TASK_MAP_AO_ACCUMULATE) needs_env = true;
+    if (d.program == RDN_TASK_PROGRAM_TRACE) needs_env = true;
+    if (d.map_op == RDN_TASK_MAP_AO_ACCUMULATE) needs_env = uses_ao = true;
   }
   const std::string bad = rdn::TaskGraph::validate(desc, capacity);
   if (!bad.empty()) return fail(c, RDN_ERR_INVALID_ARG, bad);
@@ -1174,6 +1181,7 @@ rdn_status rdn_task_graph_create(rdn_ctx* c, const rdn_task_group_desc* groups, 
   if (!tg) return fail(c, RDN_ERR_OOM, "out of host memory");
   tg->ctx = c;
   tg->needs_env = needs_env;
+  tg->uses_ao = uses_ao;
   cudaError_t e = cudaSetDevice(c->device);
   if (e != cudaSuccess) return cuda_fail(c, e, "cudaSetDevice");
   const std::string err = tg->graph.create(desc, capacity, c->sm_count, static_cast<cudaStream_t>(stream));
@@ -1225,7 +1233,7 @@ rdn_status run_rounds(rdn_task_graph* g, uint32_t rounds, const rdn_ao_desc* env
   if (g->needs_env) {
     if (!env) return fail(c, RDN_ERR_INVALID_ARG, "this graph traces or shades: pass an rdn_ao_desc environment");
     lk.lock();
-    rdn_status st = ao_env(c, env, p, a);
+    rdn_status st = ao_env(c, env, p, a, g->uses_ao);
     if (st != RDN_OK) return st;
     pp = &p;
     ap = &a;

@@ -109,3 +109,59 @@ def test_external_group_needs_its_poll(cuda):
     with pytest.raises(native.RdnError, match="rdn_task_graph_set_poll"):
         exe.execute(1)
     exe.dispatch_allocate_init_task(1, t)
+
+
+class QueryParams(C.Structure):
+    _fields_ = [("rays", C.c_void_p), ("out", C.c_void_p), ("count", C.c_uint32), ("trace_group", C.c_uint32),
+                ("closest_group", C.c_uint32), ("miss_group", C.c_uint32), ("ray_flags", C.c_uint32),
+                ("cull_mask", C.c_uint32)]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("flags", [0, 0x10])
+def test_external_ray_query_pipeline(tmp_path, cuda, flags):
+    """External ray generation / closest-hit / miss programs around the built-in
+    trace task: in reference order every hit equals the oracle's bit for bit."""
+    import numpy as np
+    import torch
+
+    from helpers import single_mesh_scene
+    from oracle import orc
+    from rendiation_gb300 import native
+    from rendiation_gb300 import raytracing as rt
+    from rendiation_gb300 import scenes
+    from rendiation_gb300 import task_graph as tg
+
+    lib = C.CDLL(build_extension(tmp_path))
+    mesh = scenes.heightfield(40, seed=4)
+    rays = np.concatenate([scenes.pinhole_rays(scenes.heightfield_camera(64, 48)),
+                           scenes.sphere_rays(2000, (0, 0, -0.2), (1, 1, 0.5), seed=9)])
+    n = rays.shape[0]
+    sc = single_mesh_scene(mesh)
+    S = sc.build_oracle()
+    expect, _ = S.trace(rays, ray_flags=flags, cull_mask=0xFF, threads=8)
+    P = sc.build_product()
+    d_rays = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).cuda()
+    out = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+    src = tg.DeviceTaskGraphBuildSource(capacity=n)
+    trace = src.define_task(tg.TraceTaskFuture(), 1, payload_words=16)
+    gen = src.define_task(tg.ExternalFuture(), 1, payload_words=1)
+    hit = src.define_task(tg.ExternalFuture(), 1, payload_words=24)
+    miss = src.define_task(tg.ExternalFuture(), 1, payload_words=16)
+    exe = src.build(P)
+    prm = QueryParams(d_rays.data_ptr(), out.data_ptr(), n, trace, hit, miss, flags, 0xFF)
+    for g, name in ((gen, "raygen_poll"), (hit, "record_hit_poll"), (miss, "record_miss_poll")):
+        exe.set_poll(g, C.cast(getattr(lib, name), C.c_void_p).value, C.addressof(prm))
+    env = native.AoDesc()
+    env.traversal = rt.TRAVERSAL_REFERENCE
+    exe.dispatch_allocate_init_task(n, gen, init=tg.INIT_INDEX)
+    exe.execute(4, env)
+    torch.cuda.synchronize()
+    assert exe.read_back_execution_states().is_empty() and exe.check_errors() == 0
+    got = out.cpu().numpy()
+    prim = got[:, 3].view(np.uint32)
+    assert np.array_equal(prim, expect["prim"])
+    h = expect["prim"] != orc.MISS
+    for k, name in enumerate(("t", "u", "v")):
+        assert np.array_equal(got[h, k].view(np.uint32), expect[name][h].view(np.uint32)), name
+    assert h.mean() > 0.3
