@@ -277,6 +277,15 @@ rdn_status rdn_trace(rdn_ctx* ctx, const rdn_trace_desc* desc, void* stream);
  * counts (slower; for measurement). */
 rdn_status rdn_trace_counted(rdn_ctx* ctx, const rdn_trace_desc* desc, void* stream, rdn_counters* out);
 
+/* Device view of the built structure for kernels of the caller's that trace
+ * with include/rdn_trace.cuh (any-hit programs of their own): fills `out`
+ * (host memory of *size bytes, at least the size this call reports in
+ * *size when out is NULL) with the traversal parameters of `traversal`,
+ * building the structure first if needed. Valid until the next rdn_build or
+ * a change to the sources. The ordered walks keep their stack in a 64-entry
+ * local array: RDN_ERR_UNSUPPORTED for a tree too deep for it. */
+rdn_status rdn_trace_params(rdn_ctx* ctx, uint32_t traversal, void* out, size_t* size);
+
 /* ---- wavefront executor -------------------------------------------- */
 
 /* Pinhole camera: ray(px, py) = normalize(forward + sx*right + sy*up) with

@@ -518,6 +518,32 @@ rdn_status rdn_trace(rdn_ctx* c, const rdn_trace_desc* desc, void* stream) {
   return RDN_OK;
 }
 
+rdn_status rdn_trace_params(rdn_ctx* c, uint32_t traversal, void* out, size_t* size) {
+  if (!c || !size) return fail(c, RDN_ERR_INVALID_ARG, "null context or size");
+  if (!out) {
+    *size = sizeof(rdn::TraceParams);
+    return RDN_OK;
+  }
+  if (*size < sizeof(rdn::TraceParams)) return fail(c, RDN_ERR_INVALID_ARG, "output smaller than the parameter block");
+  if (traversal > RDN_TRAVERSAL_ORDERED_WIDE) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
+  if (c->device < 0) return fail(c, RDN_ERR_UNSUPPORTED, "host-only context has no device structure");
+  std::lock_guard<std::mutex> lk(c->lock);
+  rdn_status st = ensure_built(c);
+  if (st != RDN_OK) return st;
+  rdn_trace_desc td;
+  std::memset(&td, 0, sizeof(td));
+  td.cull_mask = 0xFF;
+  td.traversal = traversal;
+  td.local_stack = 1;
+  rdn::TraceParams p;
+  fill_params(c, &td, p);
+  if (traversal != RDN_TRAVERSAL_REFERENCE && !p.local_stack)
+    return fail(c, RDN_ERR_UNSUPPORTED, "the tree is too deep for a 64-entry local traversal stack");
+  std::memcpy(out, &p, sizeof(p));
+  *size = sizeof(p);
+  return RDN_OK;
+}
+
 rdn_status rdn_trace_counted(rdn_ctx* c, const rdn_trace_desc* desc, void* stream, rdn_counters* out) {
   Range range_("rdn_trace_counted");
   rdn_status st = validate_trace(c, desc);

@@ -172,6 +172,24 @@ __device__ __forceinline__ uint32_t anyhit_policy(uint32_t mode, uint32_t primit
   return ANYHIT_ACCEPT;
 }
 
+// A candidate hit on non-opaque geometry, as an any-hit program sees it.
+struct AnyHitInfo {
+  uint32_t primitive;  // index within its geometry
+  uint32_t triangle;   // built triangle index
+  uint32_t instance;   // TLAS instance slot
+  uint32_t geometry;   // geometry slot
+  float t, u, v;       // world distance, barycentrics of vertices 1 and 2
+  bool front_facing;
+};
+
+// The fixed policies of anyhit_policy; traversals take any functor with the
+// same call (behaviour bits ANYHIT_ACCEPT / ANYHIT_END) in its place.
+struct BuiltinAnyHit {
+  __device__ __forceinline__ uint32_t operator()(const TraceParams& p, const AnyHitInfo& h) const {
+    return anyhit_policy(p.anyhit_mode, h.primitive, h.triangle, p.anyhit_mask);
+  }
+};
+
 struct RayCtx {
   float3 o, d, inv_d;
   float tmin, tmax;
@@ -184,10 +202,11 @@ struct RayCtx {
 
 // Tests the triangles of sorted range [k0, k1) and commits hits; returns true
 // when the search must end. Follows traverse_cpu.rs:133-193.
-template <bool COUNT>
+template <bool COUNT, class AH = BuiltinAnyHit>
 __device__ __forceinline__ bool leaf_triangles(const TraceParams& p, RayCtx& R, const InstanceRay& ir, uint32_t k0,
                                                uint32_t k1, uint32_t gslot, uint32_t inst_slot, bool is_opaque,
-                                               bool cull_enable, bool cull_back, uint32_t prim_start) {
+                                               bool cull_enable, bool cull_back, uint32_t prim_start,
+                                               const AH& anyhit = AH()) {
   for (uint32_t k = k0; k < k1; k++) {
     if (COUNT) R.tri_tests++;
     TriOut h;
@@ -198,7 +217,7 @@ __device__ __forceinline__ bool leaf_triangles(const TraceParams& p, RayCtx& R, 
     uint32_t behavior = ANYHIT_ACCEPT;
     if (!is_opaque) {
       const uint32_t tri = __ldg(p.redirect + k);
-      behavior = anyhit_policy(p.anyhit_mode, tri - prim_start, tri, p.anyhit_mask);
+      behavior = anyhit(p, AnyHitInfo{tri - prim_start, tri, inst_slot, gslot, distance, h.u, h.v, !(h.s < 0.0f)});
     }
     if (behavior & ANYHIT_ACCEPT) {
       R.far_world = distance;
@@ -218,10 +237,10 @@ __device__ __forceinline__ bool leaf_triangles(const TraceParams& p, RayCtx& R, 
 }
 
 // BLAS of one geometry, reference threaded order (traverse_cpu.rs:122-195).
-template <bool COUNT>
+template <bool COUNT, class AH = BuiltinAnyHit>
 __device__ __forceinline__ bool blas_threaded(const TraceParams& p, RayCtx& R, const InstanceRay& ir, uint32_t root,
                                               uint32_t gslot, uint32_t inst_slot, bool is_opaque, bool cull_enable,
-                                              bool cull_back, uint32_t prim_start) {
+                                              bool cull_back, uint32_t prim_start, const AH& anyhit = AH()) {
   uint32_t curr = root;
   while (curr != INVALID_NEXT) {
     if (COUNT) R.node_visits++;
@@ -233,8 +252,8 @@ __device__ __forceinline__ bool blas_threaded(const TraceParams& p, RayCtx& R, c
       curr = hit_next;
       if (hit_next == miss_next) {  // a leaf: hit and miss links are the same node
         const uint2 cr = __ldg(reinterpret_cast<const uint2*>(nd + 2));
-        if (leaf_triangles<COUNT>(p, R, ir, cr.x, cr.y, gslot, inst_slot, is_opaque, cull_enable, cull_back,
-                                  prim_start))
+        if (leaf_triangles<COUNT, AH>(p, R, ir, cr.x, cr.y, gslot, inst_slot, is_opaque, cull_enable, cull_back,
+                                      prim_start, anyhit))
           return true;
       }
     } else {
@@ -348,11 +367,12 @@ __device__ __forceinline__ uint32_t interior_step(const TraceParams& p, RayCtx& 
 // a leaf (or has finished), then the warp tests triangles together. Nodes are
 // visited in near-first order with the reference's box test; the speculation
 // only adds visits, never removes one, so the closest hit is unchanged.
-template <bool COUNT, int WIDTH>
+template <bool COUNT, int WIDTH, class AH = BuiltinAnyHit>
 __device__ __forceinline__ bool blas_speculative(const TraceParams& p, RayCtx& R, const InstanceRay& ir,
                                                  uint32_t root_node, uint32_t gslot, uint32_t inst_slot,
                                                  bool is_opaque, bool cull_enable, bool cull_back, uint32_t prim_start,
-                                                 uint2* stack, uint32_t stride, uint32_t depth) {
+                                                 uint2* stack, uint32_t stride, uint32_t depth,
+                                                 const AH& anyhit = AH()) {
   {
     if (COUNT) R.node_visits++;
     const float4* nd = reinterpret_cast<const float4*>(p.tri_forest + root_node);
@@ -381,8 +401,8 @@ __device__ __forceinline__ bool blas_speculative(const TraceParams& p, RayCtx& R
     }
     while (leaf != EMPTY_SLOT) {
       const uint2 lr = __ldg(p.leaves + (leaf & ~LEAF_BIT));
-      if (leaf_triangles<COUNT>(p, R, ir, lr.x, lr.y, gslot, inst_slot, is_opaque, cull_enable, cull_back,
-                                prim_start))
+      if (leaf_triangles<COUNT, AH>(p, R, ir, lr.x, lr.y, gslot, inst_slot, is_opaque, cull_enable, cull_back,
+                                    prim_start, anyhit))
         return true;
       leaf = EMPTY_SLOT;
       // the far may have shrunk: re-check the pending node before descending into it
@@ -399,9 +419,9 @@ __device__ __forceinline__ bool blas_speculative(const TraceParams& p, RayCtx& R
 
 // Full query of one ray (traverse_cpu.rs:52-245). R must hold the ray; on
 // return R.best holds the committed hit. `bad` reports an unbound TLAS index.
-template <int MODE, bool COUNT>
+template <int MODE, bool COUNT, class AH = BuiltinAnyHit>
 __device__ __forceinline__ void traverse_ray(const TraceParams& p, RayCtx& R, uint32_t tidx, uint2* stack,
-                                             uint32_t stride, bool& bad) {
+                                             uint32_t stride, bool& bad, const AH& anyhit = AH()) {
   R.inv_d = make_float3(1.0f / R.d.x, 1.0f / R.d.y, 1.0f / R.d.z);
   R.far_world = R.tmax;
   R.best.have = false;
@@ -448,13 +468,13 @@ __device__ __forceinline__ void traverse_ray(const TraceParams& p, RayCtx& R, ui
         if (!pass) continue;
         bool end;
         if (MODE == MODE_WIDE4)
-          end = blas_speculative<COUNT, 4>(p, R, ir, gm.x, g, ti, is_opaque, cull_enable, cull_back, gm.z, stack,
-                                           stride, p.stack_depth);
+          end = blas_speculative<COUNT, 4, AH>(p, R, ir, gm.x, g, ti, is_opaque, cull_enable, cull_back, gm.z, stack,
+                                               stride, p.stack_depth, anyhit);
         else if (MODE == MODE_BINARY)
-          end = blas_speculative<COUNT, 2>(p, R, ir, gm.x, g, ti, is_opaque, cull_enable, cull_back, gm.z, stack,
-                                           stride, p.stack_depth);
+          end = blas_speculative<COUNT, 2, AH>(p, R, ir, gm.x, g, ti, is_opaque, cull_enable, cull_back, gm.z, stack,
+                                               stride, p.stack_depth, anyhit);
         else
-          end = blas_threaded<COUNT>(p, R, ir, gm.x, g, ti, is_opaque, cull_enable, cull_back, gm.z);
+          end = blas_threaded<COUNT, AH>(p, R, ir, gm.x, g, ti, is_opaque, cull_enable, cull_back, gm.z, anyhit);
         if (end) {
           done = true;
           break;

@@ -31,7 +31,7 @@ EXPORTED_SYMBOLS = [
     "rdn_attr_paths_graph", "rdn_check_errors", "rdn_set_iteration_limit", "rdn_task_graph_create",
     "rdn_task_graph_destroy", "rdn_task_graph_dispatch_init", "rdn_task_graph_execute", "rdn_task_graph_states",
     "rdn_task_graph_debug", "rdn_task_graph_check_errors", "rdn_ao_pipeline_create", "rdn_ao_render_graph",
-    "rdn_ao_render", "rdn_ao_capture", "rdn_task_graph_capture", "rdn_task_graph_set_poll",
+    "rdn_ao_render", "rdn_ao_capture", "rdn_task_graph_capture", "rdn_task_graph_set_poll", "rdn_trace_params",
 ]
 
 
@@ -239,5 +239,7 @@ def lib() -> C.CDLL:
     L.rdn_task_graph_capture.restype = i32
     L.rdn_task_graph_set_poll.argtypes = [vp, u32, vp, vp]
     L.rdn_task_graph_set_poll.restype = i32
+    L.rdn_trace_params.argtypes = [vp, u32, vp, C.POINTER(C.c_size_t)]
+    L.rdn_trace_params.restype = i32
     _lib = L
     return L
