@@ -655,7 +655,9 @@ rdn_status rdn_task_graph_set_poll(rdn_task_graph* graph, uint32_t group, rdn_ta
  * that the device ends after the first round that leaves no task active: no
  * host round trip and no idle rounds. The graph is then empty, unless a spawn
  * found a pool full and its parent waits for ever (as in the reference). env is baked in, as for
- * rdn_task_graph_execute; a graph that traces needs the structure built. */
+ * rdn_task_graph_execute; a graph that traces needs the structure built. The
+ * task graph, the built structure and the buffers env names must outlive the
+ * captured graph. */
 rdn_status rdn_task_graph_capture(rdn_task_graph* graph, uint32_t group, uint32_t count, uint32_t init_op,
                                   uint32_t max_rounds, const rdn_ao_desc* env, rdn_graph** out);
 
