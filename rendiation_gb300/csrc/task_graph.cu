@@ -13,6 +13,11 @@
 // no host round trip inside a round, and a sequence of rounds can be captured
 // into a CUDA graph. The last-block pattern (a ticket counter) lets the first
 // blocks read the old sizes while only the last one writes the new ones.
+// record_until_empty captures the rounds as the body of a WHILE conditional
+// node that a one-warp check ends once no group has an active task.
+// Programs: the built-in chain and trace programs run in poll_kernel; an
+// external program's poll kernel (include/rdn_task.cuh) is launched by the
+// callback registered for its group, at the same point of the round.
 //
 // Deviations from the reference, both at exhaustion only: a bump list or the
 // empty pool that is full rejects the push or pop and sets an error bit,
