@@ -585,6 +585,42 @@ def bench_ao(args, P, S_field):
     return out
 
 
+def bench_task_graph(args, P):
+    """Throughput of the device task graph alone (no tracing): one million root
+    tasks of a chain future that spawns and awaits a child in group 1 (which
+    spawns and awaits one in group 2), then one more in group 2 - four tasks
+    per root, each spawned, polled, woken and cleaned up by the executor. One
+    dispatch plus its device-ended round loop, captured once and replayed."""
+    import torch
+
+    from rendiation_gb300 import task_graph as tg
+
+    roots = 1_000_000
+    src = tg.DeviceTaskGraphBuildSource(capacity=roots)
+    src.define_task(tg.BaseShaderFuture().then_spawn_task(1).then_spawn_task(2).map(), 1)
+    src.define_task(tg.BaseShaderFuture().then_spawn_task(2).map(), 1)
+    src.define_task(tg.BaseShaderFuture(), 1)
+    exe = src.build(P)
+    launch = exe.capture_until_empty(roots, 0, max_rounds=64)
+    for _ in range(args.warmup):
+        launch()
+    torch.cuda.synchronize()
+    assert exe.read_back_execution_states().is_empty() and exe.check_errors() == 0
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 10
+    e0.record(stream)
+    for _ in range(reps):
+        launch()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    tasks = 4 * roots
+    exe.close()
+    return {"workload": "1,000,000 roots x 4 tasks (chain futures over 3 groups), dispatch + device-ended round loop",
+            "ms": round(ms, 3), "mtasks_per_s": round(tasks / ms / 1e3, 1)}
+
+
 def bench_batched(args):
     """Batched multi-scene paths: 256 soups (log-uniform 1k..200k triangles),
     log-uniform 4k..256k rays per scene, <= 4 diffuse bounces with Russian
@@ -1180,6 +1216,7 @@ def main():
     ap.add_argument("--tune-cache", default=None, help="JSON file that keeps the autotuner's choices between runs")
     ap.add_argument("--no-batched-adjoint", action="store_true")
     ap.add_argument("--no-ao", action="store_true", help="skip the ambient-occlusion leg")
+    ap.add_argument("--no-task-graph", action="store_true", help="skip the task-graph throughput leg")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP32-vs-FP64 accuracy check")
     ap.add_argument("--diff-scenes", type=int, default=64)
     ap.add_argument("--scenes", type=int, default=256)
@@ -1206,6 +1243,8 @@ def main():
         out["accuracy_vs_fp64"] = accuracy_vs_fp64(P, S_field, cam)
     if not args.no_ao:
         out["ao"] = bench_ao(args, P, S_field if not args.no_cpu_baseline else None)
+    if not args.no_task_graph:
+        out["task_graph"] = bench_task_graph(args, P)
     if not args.no_batched:
         P.close()
         out["batched"] = bench_batched(args)
