@@ -1112,6 +1112,48 @@ std::string build_blas_device(const std::vector<DeviceGeometry>& geoms, uint32_t
   out.max_depth = L ? L - 1 : 0;
   out.nodes = T;
 
+  // The four-child collapse reads only the finished binary tree: its marks
+  // and numbering scan run on a side stream, overlapped with the subtree
+  // sizes, the pre-order numbering and their host round trips below; the
+  // emit waits for them.
+  struct SideStream {
+    cudaStream_t s = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+    ~SideStream() {
+      // before the scratch it reads is freed (on the main stream, by S's
+      // destructor, which runs after this one), also on an early error return
+      if (s) cudaStreamSynchronize(s);
+      if (join) cudaEventDestroy(join);
+      if (fork) cudaEventDestroy(fork);
+      if (s) cudaStreamDestroy(s);
+    }
+  } side;
+  uint32_t *croot, *level4, *index4, *max_level4;
+  CK(S.alloc(&croot, T));
+  CK(S.alloc(&level4, T));
+  CK(S.alloc(&index4, T));
+  CK(S.alloc(&max_level4, 1));
+  void* scan4 = nullptr;
+  if (T) CK(S.alloc(reinterpret_cast<char**>(&scan4), scan_scratch_bytes(T) + 256));
+  CK(cudaMemsetAsync(croot, 0, 4 * (size_t)(T ? T : 1), st));
+  CK(cudaMemsetAsync(level4, 0, 4 * (size_t)(T ? T : 1), st));
+  CK(cudaMemsetAsync(max_level4, 0, 4, st));
+  CK(cudaStreamCreateWithFlags(&side.s, cudaStreamNonBlocking));
+  CK(cudaEventCreateWithFlags(&side.fork, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&side.join, cudaEventDisableTiming));
+  CK(cudaEventRecord(side.fork, st));
+  CK(cudaStreamWaitEvent(side.s, side.fork, 0));
+  if (T) {
+    wide4_roots_kernel<<<blocks_for(G), kBlock, 0, side.s>>>(G, pool, croot, level4, max_level4);
+    for (uint32_t l = 0; l < L; l++) {
+      const uint32_t a = level_begin[l], W = level_begin[l + 1] - a;
+      wide4_mark_kernel<<<blocks_for(W), kBlock, 0, side.s>>>(a, W, pool, croot, level4, max_level4);
+    }
+    CK(scan_u32(croot, index4, T, false, 0, scan4, side.s));
+    CK(cudaGetLastError());
+  }
+  CK(cudaEventRecord(side.join, side.s));
+
   // subtree sizes, bottom-up
   uint32_t *size, *pre, *inner_at, *rank, *tree_end, *bvh_start, *root_code;
   CK(S.alloc(&size, T));
@@ -1190,24 +1232,9 @@ std::string build_blas_device(const std::vector<DeviceGeometry>& geoms, uint32_t
       else out.root_code4[g] = inner_roots++;
     }
   }
-  uint32_t *croot, *level4, *index4, *max_level4;
-  CK(S.alloc(&croot, T));
-  CK(S.alloc(&level4, T));
-  CK(S.alloc(&index4, T));
-  CK(S.alloc(&max_level4, 1));
-  CK(cudaMemsetAsync(croot, 0, 4 * (size_t)(T ? T : 1), st));
-  CK(cudaMemsetAsync(level4, 0, 4 * (size_t)(T ? T : 1), st));
-  CK(cudaMemsetAsync(max_level4, 0, 4, st));
   uint32_t tail4[3] = {0, 0, 0};  // index4[T-1], croot[T-1], deepest level
+  CK(cudaStreamWaitEvent(st, side.join, 0));
   if (T) {
-    wide4_roots_kernel<<<blocks_for(G), kBlock, 0, st>>>(G, pool, croot, level4, max_level4);
-    for (uint32_t l = 0; l < L; l++) {
-      const uint32_t a = level_begin[l], W = level_begin[l + 1] - a;
-      wide4_mark_kernel<<<blocks_for(W), kBlock, 0, st>>>(a, W, pool, croot, level4, max_level4);
-    }
-    void* scan4;
-    CK(S.alloc(reinterpret_cast<char**>(&scan4), scan_scratch_bytes(T) + 256));
-    CK(scan_u32(croot, index4, T, false, 0, scan4, st));
     wide4_emit_kernel<<<blocks_for(T), kBlock, 0, st>>>(T, pool, croot, index4, pre, rank, d.wide4_nodes.ptr);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(&tail4[0], index4 + (T - 1), 4, cudaMemcpyDeviceToHost, st));
