@@ -547,6 +547,15 @@ def bench_ao(args, P, S_field):
         c = counts.cpu().numpy()
         return e0.elapsed_time(e1) / reps, (int(c[0]) + int(c[1])) / reps
 
+    # launch shape of the fused kernel: block size and node layout, timed on the frame
+    shapes = {}
+    for trav in (rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_WIDE) if traversal != rt.TRAVERSAL_REFERENCE else (traversal,):
+        for block in (32, 64, 128):
+            descs["fused"].traversal, descs["fused"].block_size = trav, block
+            shapes[(trav, block)] = timed(lambda k: frame("fused", k))[0]
+    best = min(shapes, key=shapes.get)
+    descs["fused"].traversal, descs["fused"].block_size = best
+    out["fused_shape"] = {"traversal": {0: "binary", 1: "reference", 2: "wide"}[best[0]], "block": best[1]}
     ms, rays = timed(lambda k: frame("fused", k))
     out["rays_per_frame"] = rays
     out["fused_ms"], out["fused_mrays"] = round(ms, 4), round(rays / ms / 1e3, 1)

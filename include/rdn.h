@@ -612,7 +612,7 @@ typedef struct rdn_ao_desc {
   uint8_t* image;                 /* device, RGBA8 unorm, width * height texels, 4-byte aligned */
   uint32_t sbt_closest[2];        /* task graphs: closest-hit group of the camera and the occlusion ray */
   uint32_t sbt_miss;              /* task graphs: miss group of both rays */
-  uint32_t pad;
+  uint32_t block_size;            /* rdn_ao_render: threads per block, 32, 64 or 128 (0 = 128) */
   uint32_t* ray_counts;           /* device, nullable: [camera, occlusion] rays traced, added to */
   uint32_t* sample_counter;       /* device, nullable: when set, the frame reads its sample index from
                                      here instead of sample_count and adds one to it at its end, so

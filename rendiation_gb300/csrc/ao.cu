@@ -56,8 +56,9 @@ __global__ void __launch_bounds__(128) ao_kernel(TraceParams P, AoEnv A) {
 
 template <int MODE, bool LOCAL>
 cudaError_t launch_variant(const TraceParams& p, const AoEnv& a, cudaStream_t st) {
-  const uint32_t grid = (ao_dispatch_count(a.width, a.height) + 127) / 128;
-  const size_t smem = MODE != MODE_THREADED && !LOCAL ? (size_t)p.stack_depth * 128 * sizeof(uint2) : 0;
+  const uint32_t block = a.block ? a.block : 128;
+  const uint32_t grid = (ao_dispatch_count(a.width, a.height) + block - 1) / block;
+  const size_t smem = MODE != MODE_THREADED && !LOCAL ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
   static bool attr_done = false;
   if (!attr_done) {
     cudaError_t e =
@@ -65,7 +66,7 @@ cudaError_t launch_variant(const TraceParams& p, const AoEnv& a, cudaStream_t st
     if (e != cudaSuccess) return e;
     attr_done = true;
   }
-  ao_kernel<MODE, LOCAL><<<grid, 128, smem, st>>>(p, a);
+  ao_kernel<MODE, LOCAL><<<grid, block, smem, st>>>(p, a);
   return cudaGetLastError();
 }
 

@@ -1144,6 +1144,8 @@ rdn_status ao_env(rdn_ctx* c, const rdn_ao_desc* d, rdn::TraceParams& p, rdn::Ao
       return fail(c, RDN_ERR_INVALID_ARG, "AO frame size must be 1..2^31 pixels");
   }
   if (d->traversal > RDN_TRAVERSAL_ORDERED_WIDE) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
+  if (d->block_size && d->block_size != 32 && d->block_size != 64 && d->block_size != 128)
+    return fail(c, RDN_ERR_INVALID_ARG, "block_size must be 32, 64 or 128");
   rdn_status st = ensure_built(c);
   if (st != RDN_OK) return st;
   rdn_trace_desc td;
@@ -1171,6 +1173,7 @@ rdn_status ao_env(rdn_ctx* c, const rdn_ao_desc* d, rdn::TraceParams& p, rdn::Ao
   a.n_triangles = (uint32_t)(c->dev.indices.count / 3);
   a.ray_counts = d->ray_counts;
   a.sample_dev = d->sample_counter;
+  a.block = d->block_size;
   return RDN_OK;
 }
 

@@ -151,6 +151,7 @@ struct AoEnv {
   uint32_t n_triangles;     // built triangles
   uint32_t* ray_counts;     // nullable: [camera, occlusion] rays traced
   const uint32_t* sample_dev;  // nullable: the sample index, read at run time instead of sample_count
+  uint32_t block;              // fused kernel: threads per block (32, 64 or 128)
 };
 
 // Ray-generation tasks of a w x h AO frame: whole 8x4 pixel tiles, 32 per tile.

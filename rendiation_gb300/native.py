@@ -132,7 +132,7 @@ class AoDesc(C.Structure):
     _fields_ = [("view_projection_inv", C.c_float * 16), ("camera_position", C.c_float * 3), ("width", C.c_uint32),
                 ("height", C.c_uint32), ("sample_count", C.c_uint32), ("tlas_uniform", C.c_uint32),
                 ("traversal", C.c_uint32), ("normals", C.c_void_p), ("image", C.c_void_p),
-                ("sbt_closest", C.c_uint32 * 2), ("sbt_miss", C.c_uint32), ("pad", C.c_uint32),
+                ("sbt_closest", C.c_uint32 * 2), ("sbt_miss", C.c_uint32), ("block_size", C.c_uint32),
                 ("ray_counts", C.c_void_p), ("sample_counter", C.c_void_p)]
 
 

@@ -46,13 +46,13 @@ def run_oracle(scene, samples, normals=None):
     return img
 
 
-def run_gpu(scene, samples, traversal, mode, normals=None):
+def run_gpu(scene, samples, traversal, mode, normals=None, block_size=0):
     import torch
 
     P = scene.build_product()
     vp, eye = camera()
     nt = None if normals is None else torch.from_numpy(normals.reshape(-1)).cuda()
-    ao = tg.AmbientOcclusion(P, W, H, vp, eye, traversal=traversal, normals=nt, mode=mode)
+    ao = tg.AmbientOcclusion(P, W, H, vp, eye, traversal=traversal, normals=nt, mode=mode, block_size=block_size)
     for s in samples:
         ao.sample_count = s
         ao.render()
@@ -105,6 +105,26 @@ def test_graph_equals_fused(cuda):
         a, _, _ = run_gpu(scene, SAMPLES, traversal, "fused")
         b, _, _ = run_gpu(scene, SAMPLES, traversal, "graph")
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("block_size", [32, 64])
+def test_block_size_changes_no_texel(cuda, block_size):
+    scene = field_scene()
+    for traversal in (rt.TRAVERSAL_REFERENCE, rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_WIDE):
+        a, _, _ = run_gpu(scene, SAMPLES, traversal, "fused")
+        b, _, flags = run_gpu(scene, SAMPLES, traversal, "fused", block_size=block_size)
+        assert flags == (0, 0)
+        assert np.array_equal(a, b)
+
+
+def test_block_size_is_validated(cuda):
+    from rendiation_gb300 import native
+
+    P = field_scene().build_product()
+    vp, eye = camera()
+    ao = tg.AmbientOcclusion(P, W, H, vp, eye, block_size=96)
+    with pytest.raises(native.RdnError):
+        ao.render()
 
 
 def test_instanced_scene_with_transforms(cuda):
