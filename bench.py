@@ -625,9 +625,29 @@ def bench_task_graph(args, P):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / reps
     tasks = 4 * roots
+    # the same work as plain launches: dispatch, then the number of rounds that
+    # drains the graph (counted once from the host), issued by execute(rounds)
+    exe.dispatch_allocate_init_task(roots, 0)
+    rounds = 0
+    while not exe.read_back_execution_states().is_empty():
+        exe.execute(1)
+        rounds += 1
+    for _ in range(args.warmup):
+        exe.dispatch_allocate_init_task(roots, 0)
+        exe.execute(rounds)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        exe.dispatch_allocate_init_task(roots, 0)
+        exe.execute(rounds)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    assert exe.read_back_execution_states().is_empty() and exe.check_errors() == 0
+    plain_ms = e0.elapsed_time(e1) / reps
     exe.close()
     return {"workload": "1,000,000 roots x 4 tasks (chain futures over 3 groups), dispatch + device-ended round loop",
-            "ms": round(ms, 3), "mtasks_per_s": round(tasks / ms / 1e3, 1)}
+            "ms": round(ms, 3), "mtasks_per_s": round(tasks / ms / 1e3, 1), "rounds": rounds,
+            "plain_launches_ms": round(plain_ms, 3), "plain_launches_mtasks_per_s": round(tasks / plain_ms / 1e3, 1)}
 
 
 def bench_batched(args):
