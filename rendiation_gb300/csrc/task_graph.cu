@@ -15,8 +15,8 @@
 // blocks read the old sizes while only the last one writes the new ones.
 // record_until_empty captures the rounds as the body of a WHILE conditional
 // node that a one-warp check ends once no group has an active task.
-// Programs: the built-in chain and trace programs run in poll_kernel; an
-// external program's poll kernel (include/rdn_task.cuh) is launched by the
+// Programs: the built-in chain program runs in poll_chain_kernel, the trace
+// program in poll_kernel; an external program's poll kernel (include/rdn_task.cuh) is launched by the
 // callback registered for its group, at the same point of the round.
 //
 // Deviations from the reference, both at exhaustion only: a bump list or the
@@ -241,11 +241,10 @@ __device__ bool poll_trace(const TaskGraphDev& G, uint32_t g, uint32_t idx, cons
   return resolved;
 }
 
-template <int MODE, bool LOCAL>
-__global__ void __launch_bounds__(kPollThreads, 8) poll_kernel(const TaskGraphDev* __restrict__ Gp, uint32_t g,
-                                                            TraceParams P, AoEnv A) {
-  RDN_TRAVERSAL_STACK(LOCAL);
-  const TaskGraphDev& G = *Gp;
+// One thread per active entry of group g: poll(idx) runs the task's program,
+// then the poll is finalised.
+template <class Poll>
+__device__ __forceinline__ void poll_active(const TaskGraphDev& G, uint32_t g, const Poll& poll) {
   const TaskGroupDev& T = G.g[g];
   const GroupCtl* c = T.ctl;
   const uint32_t n = c->active.size;
@@ -257,13 +256,25 @@ __global__ void __launch_bounds__(kPollThreads, 8) poll_kernel(const TaskGraphDe
     const uint32_t pi = T.parent_index[idx], pt = T.parent_type[idx];
     if (pi != TASK_NO_PARENT && pt < G.n_groups)
       asm volatile("prefetch.global.L2 [%0];" ::"l"(G.g[pt].state + pi));
-    bool r;
-    if (T.program == TASK_PROGRAM_TRACE)
-      r = poll_trace<MODE>(G, g, idx, P, stack_ptr, stack_stride);
-    else
-      r = poll_chain(G, g, idx, P, A);
-    finalize(G, g, idx, r, pi, pt);
+    finalize(G, g, idx, poll(idx), pi, pt);
   }
+}
+
+template <int MODE, bool LOCAL>
+__global__ void __launch_bounds__(kPollThreads, 8) poll_kernel(const TaskGraphDev* __restrict__ Gp, uint32_t g,
+                                                            TraceParams P, AoEnv) {
+  RDN_TRAVERSAL_STACK(LOCAL);
+  const TaskGraphDev& G = *Gp;
+  poll_active(G, g, [&](uint32_t idx) { return poll_trace<MODE>(G, g, idx, P, stack_ptr, stack_stride); });
+}
+
+// Chain groups alone: without the traversal the kernel fits twice the resident
+// warps of poll_kernel, and its polls are chains of dependent loads that more
+// warps hide.
+__global__ void __launch_bounds__(kPollThreads, 8) poll_chain_kernel(const TaskGraphDev* __restrict__ Gp, uint32_t g,
+                                                                    TraceParams P, AoEnv A) {
+  const TaskGraphDev& G = *Gp;
+  poll_active(G, g, [&](uint32_t idx) { return poll_chain(G, g, idx, P, A); });
 }
 
 __device__ __forceinline__ uint32_t commit_alloc(uint32_t size, uint32_t bump, uint32_t cap) {
@@ -654,7 +665,11 @@ cudaError_t TaskGraph::poll(uint32_t g, const TraceParams* p, int mode, const Ao
     if (!ext_fn_[g]) return cudaErrorInvalidValue;
     return ext_fn_[g](G, g, T.cap, st, ext_user_[g]) == 0 ? cudaGetLastError() : cudaErrorLaunchFailure;
   }
-  if (T.program != TASK_PROGRAM_TRACE || !p) return launch_poll<MODE_THREADED, false>(G, g, P, A, grid, st);
+  if (T.program == TASK_PROGRAM_CHAIN) {
+    poll_chain_kernel<<<grid, kPollThreads, 0, st>>>(G, g, P, A);
+    return cudaGetLastError();
+  }
+  if (!p) return launch_poll<MODE_THREADED, false>(G, g, P, A, grid, st);
   if (mode == MODE_WIDE4)
     return P.local_stack ? launch_poll<MODE_WIDE4, true>(G, g, P, A, grid, st)
                          : launch_poll<MODE_WIDE4, false>(G, g, P, A, grid, st);
