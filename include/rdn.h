@@ -6,7 +6,7 @@
  * reference interface it replaces. The reference exposes Rust traits whose
  * device half returns shader-EDSL nodes, so the boundary a Rust host binds is
  * this C ABI: an `extern "C"` block plus a trait implementation that forwards
- * to it (see INTEGRATION.md).
+ * to it.
  *
  * Conventions
  *  - Every entry point returns rdn_status; nothing aborts or traps. The text
@@ -530,9 +530,11 @@ rdn_status rdn_radix_sort_u32(uint32_t* keys, uint32_t* values, uint32_t count, 
  * until exit. desc->scratch must be NULL and desc->scratch_bytes 0; launches
  * whose queues do not fit (rdn_wavefront_scratch_size() above the array size,
  * about 466,000 pixels) are rejected with RDN_ERR_INVALID_ARG. The call
- * allocates nothing. The first call on a device looks up the array's device
- * address, so make it before any stream capture. Every call reuses the same
- * array: calls that overlap on the GPU race and must be ordered by the caller. */
+ * allocates nothing: it never builds, so a structure created, deleted or bound
+ * since its last build is RDN_ERR_NOT_BUILT (call rdn_build first, which
+ * allocates). rdn_create looks up the array's device address for its device.
+ * Every call reuses the same array: calls that overlap on the GPU race and
+ * must be ordered by the caller. */
 #define RDN_WAVEFRONT_STATIC_SCRATCH_BYTES (32u * 1024u * 1024u)
 rdn_status rdn_wavefront_shadow_bounce_static(rdn_ctx* ctx, const rdn_wavefront_desc* desc, void* stream);
 

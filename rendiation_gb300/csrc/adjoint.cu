@@ -467,17 +467,14 @@ inline uint32_t recorded_grid(size_t items, int sm_count) {
 template <int MODE, bool LOCAL>
 cudaError_t launch_attr_paths_variant(const TraceParams& p, const PathAdjointParams& a, bool adjoint, uint32_t block,
                                       int sm_count, cudaStream_t stream) {
-  static bool done[2] = {false, false};
+  static std::atomic<uint64_t> done[2] = {};
   const void* fn = adjoint ? (const void*)attr_path_kernel<MODE, true, LOCAL>
                            : (const void*)attr_path_kernel<MODE, false, LOCAL>;
-  if (!done[adjoint]) {
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    if (e != cudaSuccess) return e;
-    done[adjoint] = true;
-  }
+  cudaError_t e = raise_smem_limit(done[adjoint], {fn});
+  if (e != cudaSuccess) return e;
   const size_t smem = MODE != MODE_THREADED && !LOCAL ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
   int per_sm = 0;
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (int)block, smem);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (int)block, smem);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
   uint32_t grid = (uint32_t)(sm_count * per_sm);
@@ -501,15 +498,10 @@ cudaError_t launch_attr_paths_mode(const TraceParams& p, const PathAdjointParams
 template <int MODE, bool LOCAL>
 cudaError_t launch_attr_variant(const TraceParams& p, const AdjointParams& a, bool adjoint, uint32_t block,
                                 cudaStream_t stream) {
-  static bool done[2] = {false, false};
-  if (!done[adjoint]) {
-    cudaError_t e = adjoint ? cudaFuncSetAttribute(attr_adjoint_kernel<MODE, LOCAL>,
-                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024)
-                            : cudaFuncSetAttribute(attr_forward_kernel<MODE, LOCAL>,
-                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    if (e != cudaSuccess) return e;
-    done[adjoint] = true;
-  }
+  static std::atomic<uint64_t> done[2] = {};
+  const cudaError_t e = raise_smem_limit(done[adjoint], {adjoint ? (const void*)attr_adjoint_kernel<MODE, LOCAL>
+                                                                 : (const void*)attr_forward_kernel<MODE, LOCAL>});
+  if (e != cudaSuccess) return e;
   const size_t smem = MODE != MODE_THREADED && !LOCAL ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
   const uint32_t grid = (a.count + block - 1) / block;
   if (adjoint) attr_adjoint_kernel<MODE, LOCAL><<<grid, block, smem, stream>>>(p, a);

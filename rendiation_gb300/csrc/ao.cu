@@ -59,13 +59,9 @@ cudaError_t launch_variant(const TraceParams& p, const AoEnv& a, cudaStream_t st
   const uint32_t block = a.block ? a.block : 128;
   const uint32_t grid = (ao_dispatch_count(a.width, a.height) + block - 1) / block;
   const size_t smem = MODE != MODE_THREADED && !LOCAL ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
-  static bool attr_done = false;
-  if (!attr_done) {
-    cudaError_t e =
-        cudaFuncSetAttribute(ao_kernel<MODE, LOCAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    if (e != cudaSuccess) return e;
-    attr_done = true;
-  }
+  static std::atomic<uint64_t> attr_done{0};
+  const cudaError_t e = raise_smem_limit(attr_done, {(const void*)ao_kernel<MODE, LOCAL>});
+  if (e != cudaSuccess) return e;
   ao_kernel<MODE, LOCAL><<<grid, block, smem, st>>>(p, a);
   return cudaGetLastError();
 }

@@ -344,15 +344,12 @@ cudaError_t prepare_paths(const TraceParams& p, const PathParams& q, int mode, u
   if (block == 0) block = 64;
   const int variant = path_variant(mode, p, q);
   const size_t smem = mode != MODE_THREADED && variant != 2 ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
-  static bool attr_done[3][3] = {};
+  static std::atomic<uint64_t> attr_done[3][3] = {};
   const void* fn = path_fn(mode, variant);
-  if (!attr_done[variant][mode]) {
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    if (e != cudaSuccess) return e;
-    attr_done[variant][mode] = true;
-  }
+  cudaError_t e = raise_smem_limit(attr_done[variant][mode], {fn});
+  if (e != cudaSuccess) return e;
   int per_sm = 0;
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (int)block, smem);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (int)block, smem);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
   // persistent grid, never larger than the primary queue needs

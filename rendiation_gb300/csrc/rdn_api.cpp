@@ -245,6 +245,50 @@ rdn_status ensure_built(rdn_ctx* c) {
   return do_build(c);
 }
 
+// Checks of the knobs that rdn_wavefront_shadow_bounce and its allocation-free
+// variant share (their scratch checks differ).
+rdn_status wavefront_check_knobs(rdn_ctx* c, const rdn_wavefront_desc* d) {
+  if (d->traversal > RDN_TRAVERSAL_ORDERED_WIDE) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
+  if (d->phases > 3) return fail(c, RDN_ERR_INVALID_ARG, "unknown phase mask");
+  if (d->refill > 32) return fail(c, RDN_ERR_INVALID_ARG, "refill must be 0..32");
+  if (d->local_stack > 1) return fail(c, RDN_ERR_INVALID_ARG, "local_stack must be 0 or 1");
+  if (d->register_tier > 2) return fail(c, RDN_ERR_INVALID_ARG, "register_tier must be 0, 1 or 2");
+  if (d->speculation > 31) return fail(c, RDN_ERR_INVALID_ARG, "speculation must be 0..31");
+  if (d->block_size && (d->block_size % 32 || d->block_size > 128))
+    return fail(c, RDN_ERR_INVALID_ARG, "block_size must be a multiple of 32 up to 128");
+  return RDN_OK;
+}
+
+// Launch parameters of both wavefront entry points (the queues are bound by
+// the caller); the structure must be built.
+void wavefront_fill(rdn_ctx* c, const rdn_wavefront_desc* d, rdn::TraceParams& p, rdn::WavefrontParams& w) {
+  rdn_trace_desc td;
+  std::memset(&td, 0, sizeof(td));
+  td.tlas_uniform = d->tlas_uniform;
+  td.cull_mask = 0xFF;
+  td.traversal = d->traversal;
+  fill_params(c, &td, p);
+  std::memset(&w, 0, sizeof(w));
+  const rdn_camera& cam = d->camera;
+  w.origin = make_float3(cam.origin[0], cam.origin[1], cam.origin[2]);
+  w.forward = make_float3(cam.forward[0], cam.forward[1], cam.forward[2]);
+  w.right = make_float3(cam.right[0], cam.right[1], cam.right[2]);
+  w.up = make_float3(cam.up[0], cam.up[1], cam.up[2]);
+  w.light = make_float3(d->light[0], d->light[1], d->light[2]);
+  w.tan_half = cam.tan_half;
+  w.aspect = cam.aspect;
+  w.width = d->camera.width;
+  w.height = d->camera.height;
+  w.sample_index = d->sample_index;
+  w.tlas = d->tlas_uniform;
+  w.out = reinterpret_cast<rdn::PixelResult*>(d->out);
+  w.ray_counts = d->ray_counts;
+  w.refill = d->refill;
+  w.local_stack = d->local_stack;
+  w.register_tier = d->register_tier;
+  p.spec_threshold = d->speculation;
+}
+
 }  // namespace
 
 extern "C" {
@@ -262,6 +306,8 @@ rdn_status rdn_create(rdn_ctx** out, int device) {
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_counters, 64);
     if (e == cudaSuccess) e = cudaMemset(c->d_counters, 0, 64);
+    // device address of the allocation-free entry point's static queue array
+    if (e == cudaSuccess) e = rdn::wavefront_static_prepare(device);
     if (e != cudaSuccess) {
       delete c;
       return e == cudaErrorMemoryAllocation ? RDN_ERR_OOM : RDN_ERR_CUDA;
@@ -585,44 +631,14 @@ rdn_status rdn_wavefront_shadow_bounce(rdn_ctx* c, const rdn_wavefront_desc* d, 
   if (d->scratch_bytes < rdn::wavefront_scratch_bytes(W, H)) return fail(c, RDN_ERR_INVALID_ARG, "scratch too small");
   if ((reinterpret_cast<uintptr_t>(d->scratch) & 255) || (reinterpret_cast<uintptr_t>(d->out) & 15))
     return fail(c, RDN_ERR_INVALID_ARG, "scratch must be 256-byte and output 16-byte aligned");
-  if (d->traversal > RDN_TRAVERSAL_ORDERED_WIDE) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
-  if (d->phases > 3) return fail(c, RDN_ERR_INVALID_ARG, "unknown phase mask");
-  if (d->refill > 32) return fail(c, RDN_ERR_INVALID_ARG, "refill must be 0..32");
-  if (d->local_stack > 1) return fail(c, RDN_ERR_INVALID_ARG, "local_stack must be 0 or 1");
-  if (d->register_tier > 2) return fail(c, RDN_ERR_INVALID_ARG, "register_tier must be 0, 1 or 2");
-  if (d->speculation > 31) return fail(c, RDN_ERR_INVALID_ARG, "speculation must be 0..31");
-  if (d->block_size && (d->block_size % 32 || d->block_size > 128))
-    return fail(c, RDN_ERR_INVALID_ARG, "block_size must be a multiple of 32 up to 128");
-  std::lock_guard<std::mutex> lk(c->lock);
-  rdn_status st = ensure_built(c);
+  rdn_status st = wavefront_check_knobs(c, d);
   if (st != RDN_OK) return st;
-  rdn_trace_desc td;
-  std::memset(&td, 0, sizeof(td));
-  td.tlas_uniform = d->tlas_uniform;
-  td.cull_mask = 0xFF;
-  td.traversal = d->traversal;
+  std::lock_guard<std::mutex> lk(c->lock);
+  st = ensure_built(c);
+  if (st != RDN_OK) return st;
   rdn::TraceParams p;
-  fill_params(c, &td, p);
   rdn::WavefrontParams w;
-  std::memset(&w, 0, sizeof(w));
-  const rdn_camera& cam = d->camera;
-  w.origin = make_float3(cam.origin[0], cam.origin[1], cam.origin[2]);
-  w.forward = make_float3(cam.forward[0], cam.forward[1], cam.forward[2]);
-  w.right = make_float3(cam.right[0], cam.right[1], cam.right[2]);
-  w.up = make_float3(cam.up[0], cam.up[1], cam.up[2]);
-  w.light = make_float3(d->light[0], d->light[1], d->light[2]);
-  w.tan_half = cam.tan_half;
-  w.aspect = cam.aspect;
-  w.width = W;
-  w.height = H;
-  w.sample_index = d->sample_index;
-  w.tlas = d->tlas_uniform;
-  w.out = reinterpret_cast<rdn::PixelResult*>(d->out);
-  w.ray_counts = d->ray_counts;
-  w.refill = d->refill;
-  w.local_stack = d->local_stack;
-  w.register_tier = d->register_tier;
-  p.spec_threshold = d->speculation;
+  wavefront_fill(c, d, p, w);
   rdn::wavefront_bind_scratch(w, d->scratch);
   cudaError_t e = cudaSetDevice(c->device);
   if (e == cudaSuccess)
@@ -1056,6 +1072,8 @@ rdn_status rdn_radix_sort_u32(uint32_t* keys, uint32_t* values, uint32_t count, 
 
 // Allocation-free wavefront: identical work to rdn_wavefront_shadow_bounce with
 // the queues in the library's static device array (see wavefront_static.cu).
+// A build allocates, so this entry point never builds: a structure changed
+// since its last build is RDN_ERR_NOT_BUILT.
 rdn_status rdn_wavefront_shadow_bounce_static(rdn_ctx* c, const rdn_wavefront_desc* d, void* stream) {
   Range range_("rdn_wavefront_shadow_bounce_static");
   if (!c || !d) return fail(c, RDN_ERR_INVALID_ARG, "null context or descriptor");
@@ -1072,44 +1090,14 @@ rdn_status rdn_wavefront_shadow_bounce_static(rdn_ctx* c, const rdn_wavefront_de
                     std::to_string(RDN_WAVEFRONT_STATIC_SCRATCH_BYTES) + " (about 466,000 pixels)");
   if (W && H && !d->out) return fail(c, RDN_ERR_INVALID_ARG, "null output");
   if (reinterpret_cast<uintptr_t>(d->out) & 15) return fail(c, RDN_ERR_INVALID_ARG, "output must be 16-byte aligned");
-  if (d->traversal > RDN_TRAVERSAL_ORDERED_WIDE) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
-  if (d->phases > 3) return fail(c, RDN_ERR_INVALID_ARG, "unknown phase mask");
-  if (d->refill > 32) return fail(c, RDN_ERR_INVALID_ARG, "refill must be 0..32");
-  if (d->local_stack > 1) return fail(c, RDN_ERR_INVALID_ARG, "local_stack must be 0 or 1");
-  if (d->register_tier > 2) return fail(c, RDN_ERR_INVALID_ARG, "register_tier must be 0, 1 or 2");
-  if (d->speculation > 31) return fail(c, RDN_ERR_INVALID_ARG, "speculation must be 0..31");
-  if (d->block_size && (d->block_size % 32 || d->block_size > 128))
-    return fail(c, RDN_ERR_INVALID_ARG, "block_size must be a multiple of 32 up to 128");
-  std::lock_guard<std::mutex> lk(c->lock);
-  rdn_status st = ensure_built(c);
+  rdn_status st = wavefront_check_knobs(c, d);
   if (st != RDN_OK) return st;
-  rdn_trace_desc td;
-  std::memset(&td, 0, sizeof(td));
-  td.tlas_uniform = d->tlas_uniform;
-  td.cull_mask = 0xFF;
-  td.traversal = d->traversal;
+  std::lock_guard<std::mutex> lk(c->lock);
+  if (c->dirty || !c->host)
+    return fail(c, RDN_ERR_NOT_BUILT, "structure changed since its last build: call rdn_build first (a build allocates)");
   rdn::TraceParams p;
-  fill_params(c, &td, p);
   rdn::WavefrontParams w;
-  std::memset(&w, 0, sizeof(w));
-  const rdn_camera& cam = d->camera;
-  w.origin = make_float3(cam.origin[0], cam.origin[1], cam.origin[2]);
-  w.forward = make_float3(cam.forward[0], cam.forward[1], cam.forward[2]);
-  w.right = make_float3(cam.right[0], cam.right[1], cam.right[2]);
-  w.up = make_float3(cam.up[0], cam.up[1], cam.up[2]);
-  w.light = make_float3(d->light[0], d->light[1], d->light[2]);
-  w.tan_half = cam.tan_half;
-  w.aspect = cam.aspect;
-  w.width = W;
-  w.height = H;
-  w.sample_index = d->sample_index;
-  w.tlas = d->tlas_uniform;
-  w.out = reinterpret_cast<rdn::PixelResult*>(d->out);
-  w.ray_counts = d->ray_counts;
-  w.refill = d->refill;
-  w.local_stack = d->local_stack;
-  w.register_tier = d->register_tier;
-  p.spec_threshold = d->speculation;
+  wavefront_fill(c, d, p, w);
   cudaError_t e = cudaSetDevice(c->device);
   if (e == cudaSuccess)
     e = rdn::launch_wavefront_static(p, w, mode_of(d->traversal), d->block_size, c->sm_count, d->phases,

@@ -5,7 +5,9 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
+#include <initializer_list>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -16,6 +18,24 @@
 namespace rdn {
 
 static const uint32_t INVALID_NEXT = 0xFFFFFFFFu;
+
+// Raises the dynamic shared-memory limit of the given kernels to 200 KB on the
+// current device, once per device. Function attributes belong to a device's
+// context, so `done` holds one bit per device (devices past 63 set it on every
+// call); concurrent first calls may both set the attribute, which is harmless.
+inline cudaError_t raise_smem_limit(std::atomic<uint64_t>& done, std::initializer_list<const void*> fns) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const uint64_t bit = dev < 64 ? (1ull << dev) : 0ull;
+  if (bit && (done.load(std::memory_order_acquire) & bit)) return cudaSuccess;
+  for (const void* f : fns) {
+    e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e != cudaSuccess) return e;
+  }
+  done.fetch_or(bit, std::memory_order_release);
+  return cudaSuccess;
+}
 
 struct f3 {
   float x, y, z;

@@ -491,13 +491,9 @@ template <int MODE, bool LOCAL>
 cudaError_t launch_poll(const TaskGraphDev* G, uint32_t g, const TraceParams& P, const AoEnv& A, uint32_t grid,
                         cudaStream_t st) {
   const size_t smem = MODE != MODE_THREADED && !LOCAL ? (size_t)P.stack_depth * kPollThreads * sizeof(uint2) : 0;
-  static bool attr_done = false;
-  if (!attr_done) {
-    cudaError_t e =
-        cudaFuncSetAttribute(poll_kernel<MODE, LOCAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    if (e != cudaSuccess) return e;
-    attr_done = true;
-  }
+  static std::atomic<uint64_t> attr_done{0};
+  const cudaError_t e = raise_smem_limit(attr_done, {(const void*)poll_kernel<MODE, LOCAL>});
+  if (e != cudaSuccess) return e;
   poll_kernel<MODE, LOCAL><<<grid, kPollThreads, smem, st>>>(G, g, P, A);
   return cudaGetLastError();
 }

@@ -16,44 +16,54 @@ template <int MODE, bool COUNT, bool LOCAL>
 __global__ void __launch_bounds__(256) trace_kernel(TraceParams p) {
   RDN_TRAVERSAL_STACK(LOCAL);
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= p.count) return;
-  const float4* rp = p.rays + 2 * (size_t)i;
-  const float4 r0 = __ldg(rp), r1 = __ldg(rp + 1);
-  RayCtx R;
-  R.o = make_float3(r0.x, r0.y, r0.z);
-  R.tmin = r0.w;
-  R.d = make_float3(r1.x, r1.y, r1.z);
-  R.tmax = r1.w;
-  R.cull_mask = p.cull_mask;
-  R.ray_flags = p.ray_flags;
-  const uint32_t tidx = p.tlas_idx ? __ldg(p.tlas_idx + i) : p.tlas_uniform;
-  bool bad;
-  traverse_ray<MODE, COUNT>(p, R, tidx, stack_ptr, stack_stride, bad);
+  // Lanes past the ray count stay alive (with zero counts) until the counter
+  // reduction, which reads every lane of the warp: block sizes are multiples of 32.
+  unsigned long long nv = 0, tt = 0, th = 0, bt = 0;
+  if (i < p.count) {
+    const float4* rp = p.rays + 2 * (size_t)i;
+    const float4 r0 = __ldg(rp), r1 = __ldg(rp + 1);
+    RayCtx R;
+    R.o = make_float3(r0.x, r0.y, r0.z);
+    R.tmin = r0.w;
+    R.d = make_float3(r1.x, r1.y, r1.z);
+    R.tmax = r1.w;
+    R.cull_mask = p.cull_mask;
+    R.ray_flags = p.ray_flags;
+    const uint32_t tidx = p.tlas_idx ? __ldg(p.tlas_idx + i) : p.tlas_uniform;
+    bool bad;
+    traverse_ray<MODE, COUNT>(p, R, tidx, stack_ptr, stack_stride, bad);
 
-  float4 out;
-  uint4 ext;
-  if (R.best.have) {
-    const uint4 gm = __ldg(reinterpret_cast<const uint4*>(p.tri_root + R.best.geom_slot));
-    const uint32_t prim = __ldg(p.redirect + R.best.k) - gm.z;
-    out = make_float4(R.best.t, R.best.u, R.best.v, __uint_as_float(prim));
-    ext = make_uint4(gm.y, R.best.inst, __ldg(&p.tlas_data[R.best.inst].instance_custom_index),
-                     (R.best.s < 0.0f) ? 0xFFu : 0xFEu);
-  } else {
-    out = make_float4(R.tmax, 0.0f, 0.0f, __uint_as_float(INVALID_NEXT));
-    ext = make_uint4(INVALID_NEXT, INVALID_NEXT, INVALID_NEXT, 0u);
-  }
-  reinterpret_cast<float4*>(p.hits)[i] = out;
-  if (p.hits_ext) reinterpret_cast<uint4*>(p.hits_ext)[i] = ext;
-  if (bad) atomicOr(p.error_word, 2u);
-  if (COUNT) {
-    unsigned long long nv = R.node_visits, tt = R.tri_tests, th = R.tri_hits, bt = bad ? 1ull : 0ull;
-    for (int off = 16; off > 0; off >>= 1) {
-      nv += __shfl_down_sync(__activemask(), nv, off);
-      tt += __shfl_down_sync(__activemask(), tt, off);
-      th += __shfl_down_sync(__activemask(), th, off);
-      bt += __shfl_down_sync(__activemask(), bt, off);
+    float4 out;
+    uint4 ext;
+    if (R.best.have) {
+      const uint4 gm = __ldg(reinterpret_cast<const uint4*>(p.tri_root + R.best.geom_slot));
+      const uint32_t prim = __ldg(p.redirect + R.best.k) - gm.z;
+      out = make_float4(R.best.t, R.best.u, R.best.v, __uint_as_float(prim));
+      ext = make_uint4(gm.y, R.best.inst, __ldg(&p.tlas_data[R.best.inst].instance_custom_index),
+                       (R.best.s < 0.0f) ? 0xFFu : 0xFEu);
+    } else {
+      out = make_float4(R.tmax, 0.0f, 0.0f, __uint_as_float(INVALID_NEXT));
+      ext = make_uint4(INVALID_NEXT, INVALID_NEXT, INVALID_NEXT, 0u);
     }
-    if ((threadIdx.x & 31) == 0) {
+    reinterpret_cast<float4*>(p.hits)[i] = out;
+    if (p.hits_ext) reinterpret_cast<uint4*>(p.hits_ext)[i] = ext;
+    if (bad) atomicOr(p.error_word, 2u);
+    if (COUNT) {
+      nv = R.node_visits;
+      tt = R.tri_tests;
+      th = R.tri_hits;
+      bt = bad ? 1ull : 0ull;
+    }
+  }
+  if (COUNT) {
+    __syncwarp();
+    for (int off = 16; off > 0; off >>= 1) {
+      nv += __shfl_down_sync(0xffffffffu, nv, off);
+      tt += __shfl_down_sync(0xffffffffu, tt, off);
+      th += __shfl_down_sync(0xffffffffu, th, off);
+      bt += __shfl_down_sync(0xffffffffu, bt, off);
+    }
+    if ((threadIdx.x & 31) == 0 && (nv | tt | th | bt)) {
       atomicAdd(p.counters + 0, nv);
       atomicAdd(p.counters + 1, tt);
       atomicAdd(p.counters + 2, th);
@@ -74,13 +84,9 @@ namespace {
 template <int MODE, bool COUNT, bool LOCAL>
 cudaError_t launch_trace_variant(const TraceParams& p, uint32_t block, uint32_t grid, cudaStream_t stream) {
   const size_t smem = MODE != MODE_THREADED && !LOCAL ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
-  static bool attr_done = false;
-  if (!attr_done) {
-    cudaError_t e = cudaFuncSetAttribute(trace_kernel<MODE, COUNT, LOCAL>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    if (e != cudaSuccess) return e;
-    attr_done = true;
-  }
+  static std::atomic<uint64_t> attr_done{0};
+  const cudaError_t e = raise_smem_limit(attr_done, {(const void*)trace_kernel<MODE, COUNT, LOCAL>});
+  if (e != cudaSuccess) return e;
   trace_kernel<MODE, COUNT, LOCAL><<<grid, block, smem, stream>>>(p);
   return cudaGetLastError();
 }

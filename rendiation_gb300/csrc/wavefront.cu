@@ -290,20 +290,11 @@ template <int MODE, bool LOCAL, int TIER>
 cudaError_t launch_wavefront_mode(const TraceParams& p, const WavefrontParams& w, uint32_t block, int sm_count,
                                   uint32_t phases, cudaStream_t stream) {
   const size_t smem = MODE != MODE_THREADED && !LOCAL ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
-  static bool attr_done = false;
-  if (!attr_done) {
-    cudaError_t e =
-        cudaFuncSetAttribute(primary_kernel<MODE, LOCAL, TIER>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(secondary_kernel<MODE, LOCAL, TIER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               200 * 1024);
-    if (e == cudaSuccess && MODE != MODE_THREADED)
-      e = cudaFuncSetAttribute(secondary_dynamic_kernel<MODE == MODE_THREADED ? MODE_BINARY : MODE>,
-                               cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    if (e != cudaSuccess) return e;
-    attr_done = true;
-  }
-  cudaError_t e;
+  static std::atomic<uint64_t> attr_done{0};
+  cudaError_t e = raise_smem_limit(
+      attr_done, {(const void*)primary_kernel<MODE, LOCAL, TIER>, (const void*)secondary_kernel<MODE, LOCAL, TIER>,
+                  (const void*)secondary_dynamic_kernel<MODE == MODE_THREADED ? MODE_BINARY : MODE>});
+  if (e != cudaSuccess) return e;
   if (phases & 1u) {
     e = cudaMemsetAsync(w.queue_count, 0, 64, stream);
     if (e != cudaSuccess) return e;

@@ -51,8 +51,12 @@ void wavefront_bind_scratch(WavefrontParams& w, void* scratch);
 cudaError_t launch_wavefront(const TraceParams& p, const WavefrontParams& w, int mode, uint32_t block,
                              int sm_count, uint32_t phases, cudaStream_t stream);
 
-// Same launch with the queues in the library's static device array
-// (wavefront_static.cu); `device` must be current.
+// Looks up the device address of the library's static queue array on
+// `device` (which must be current) and caches it; called when a context is
+// created for the device.
+cudaError_t wavefront_static_prepare(int device);
+// Same launch as launch_wavefront with the queues in that static array;
+// `device` must be current.
 cudaError_t launch_wavefront_static(const TraceParams& p, WavefrontParams w, int mode, uint32_t block,
                                     int sm_count, uint32_t phases, int device, cudaStream_t stream);
 

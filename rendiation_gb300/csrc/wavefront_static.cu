@@ -13,9 +13,10 @@
 // (32 MiB): every GPU that loads this library holds it until the process exits.
 // Host code cannot use the array's name as a device address (on the host it is
 // only a stand-in symbol), so the address is looked up with
-// cudaGetSymbolAddress once per device, with that device current, on the first
-// call that uses the device; that first call should therefore come before any
-// stream capture. The queue counters are cleared on the stream at the start of
+// cudaGetSymbolAddress, with the device current: once when a context is
+// created for the device (rdn_create), and again on every call whose stream is
+// not capturing, so that a module reloaded after cudaDeviceReset is picked up;
+// on a capturing stream the call keeps the cached address. The queue counters are cleared on the stream at the start of
 // every call (by the shared launcher), the queues themselves need no clearing.
 // All calls share the one array: calls that overlap on the GPU (different
 // streams, or several contexts on one device) race on it and must be ordered
@@ -40,11 +41,12 @@ constexpr int kMaxDevices = 64;
 std::mutex g_symbol_lock;
 void* g_symbol_addr[kMaxDevices] = {};
 
-// Device address of g_wavefront_scratch on `device` (which must be current).
-cudaError_t static_scratch_address(int device, void** out) {
+// Looks the address up again (refresh) or returns the cached one; `device`
+// must be current.
+cudaError_t static_scratch_address(int device, bool refresh, void** out) {
   if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
   std::lock_guard<std::mutex> lk(g_symbol_lock);
-  if (!g_symbol_addr[device]) {
+  if (refresh || !g_symbol_addr[device]) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_wavefront_scratch);
     if (e != cudaSuccess) return e;
@@ -56,10 +58,18 @@ cudaError_t static_scratch_address(int device, void** out) {
 
 }  // namespace
 
+cudaError_t wavefront_static_prepare(int device) {
+  void* unused = nullptr;
+  return static_scratch_address(device, true, &unused);
+}
+
 cudaError_t launch_wavefront_static(const TraceParams& p, WavefrontParams w, int mode, uint32_t block,
                                     int sm_count, uint32_t phases, int device, cudaStream_t stream) {
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  cudaError_t e = cudaStreamIsCapturing(stream, &cap);
+  if (e != cudaSuccess) return e;
   void* scratch = nullptr;
-  cudaError_t e = static_scratch_address(device, &scratch);
+  e = static_scratch_address(device, cap == cudaStreamCaptureStatusNone, &scratch);
   if (e != cudaSuccess) return e;
   wavefront_bind_scratch(w, scratch);
   return launch_wavefront(p, w, mode, block, sm_count, phases, stream);

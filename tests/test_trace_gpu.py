@@ -94,6 +94,19 @@ def test_counts_equal_reference_counters(soup, cuda):
         assert c2["tri_tests"] <= tot["tri_visit"]
 
 
+@pytest.mark.parametrize("count", [65_531, 31, 1])
+@pytest.mark.parametrize("block", [0, 96])
+def test_counts_with_a_partial_last_warp(soup, count, block, cuda):
+    """Ray counts that leave the last warp partly empty: the counter reduction
+    reads every lane of the warp, so lanes past the count must contribute zero."""
+    sc, S, P, rays = soup
+    sub = np.ascontiguousarray(rays[:count])
+    _, tot = run_oracle(S, sub)
+    hits = torch.zeros((count, 4), device="cuda")
+    c = P.trace_counted(to_dev(sub), hits, traversal=rt.TRAVERSAL_REFERENCE, block_size=block)
+    assert (c["node_visits"], c["tri_tests"], c["tri_hits"]) == (tot["bvh_visit"], tot["tri_visit"], tot["tri_hit"])
+
+
 @pytest.mark.parametrize("traversal", [rt.TRAVERSAL_REFERENCE] + ORDERED_MODES)
 def test_heightfield_random_rays(traversal, cuda):
     mesh = scenes.heightfield(128, seed=4)
