@@ -164,6 +164,22 @@ typedef struct rdn_hit_ext {
 #define RDN_TRAVERSAL_REFERENCE 1u
 #define RDN_TRAVERSAL_ORDERED_WIDE 2u
 
+/* Triangle test, OR-ed into any traversal value of any entry point.
+ * Without it (the default) every triangle is tested with the reference's
+ * formula (geometry/mod.rs:105-155): plane distance from the normalised
+ * normal, projected barycentrics. That formula is not watertight: a ray
+ * through an edge shared by two triangles can miss both, and a zero-area
+ * triangle (or a ray in a triangle's plane) gives t = NaN, which the
+ * reference accepts as a hit.
+ * RDN_INTERSECT_WATERTIGHT: the watertight f32 test of Woop, Benthin and Wald
+ * (JCGT 2013) on the shared vertex values: no ray passes between two
+ * triangles that share an edge, a NaN distance never hits, facing and culling
+ * follow the reference's rules. Hit/miss and primitive ids differ from the
+ * reference's only for rays at an exact distance tie, rays near a triangle
+ * edge, and rays the reference gives a NaN distance; t and the barycentrics
+ * are this test's own f32 values, not the reference's. */
+#define RDN_INTERSECT_WATERTIGHT 0x100u
+
 /* Fixed any-hit policies for non-opaque geometry, standing in for a user
  * any-hit shader (RayAnyHitBehavior, api/ty.rs:134-136). */
 #define RDN_ANYHIT_ACCEPT 0u

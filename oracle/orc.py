@@ -24,6 +24,7 @@ HIT_DTYPE = np.dtype(
      ("geometry", np.uint32), ("instance", np.uint32), ("custom", np.uint32), ("hit_kind", np.uint32)]
 )
 MISS = 0xFFFFFFFF
+RAY_DTYPE = np.dtype([("org", np.float32, 3), ("tmin", np.float32), ("dir", np.float32, 3), ("tmax", np.float32)])
 
 BUF_TLAS_BINDING, BUF_TLAS_BVH_ROOT, BUF_TLAS_BVH_FOREST, BUF_TLAS_DATA, BUF_TLAS_BOUNDING = 0, 1, 2, 3, 4
 BUF_BLAS_META_INFO, BUF_TRI_BVH_ROOT, BUF_TRI_BVH_FOREST, BUF_INDICES_REDIRECT, BUF_INDICES, BUF_VERTICES = 5, 6, 7, 8, 9, 10
@@ -64,9 +65,10 @@ def lib():
         L.orc_build_stats.argtypes = [vp, vp]
         L.orc_get_buffer.restype = C.c_size_t
         L.orc_get_buffer.argtypes = [vp, i32, vp, C.c_size_t]
-        L.orc_trace.argtypes = [vp, vp, u32, vp, u32, u32, u32, u32, vp, vp, vp, vp, i32, C.POINTER(C.c_double)]
+        L.orc_trace.argtypes = [vp, vp, u32, vp, u32, u32, u32, u32, vp, vp, vp, vp, i32, C.POINTER(C.c_double), i32]
         L.orc_nan_exposure.argtypes = [vp, vp, u32, vp, u32, u32, u32, vp, i32]
         L.orc_eval_fp64.argtypes = [vp, vp, u32, vp, vp]
+        L.orc_edge_margin.argtypes = [vp, vp, u32, vp, vp]
         L.orc_bruteforce_fp64.argtypes = [vp, vp, u32, u32, vp, i32]
         L.orc_intersect_triangle.argtypes = [vp, vp, C.c_float, C.c_float, vp, vp, vp, i32, i32, vp]
         L.orc_intersect_aabb.argtypes = [vp, vp, C.c_float, C.c_float, vp, vp]
@@ -77,7 +79,8 @@ def lib():
         L.orc_ao_render.argtypes = [vp, vp, vp, u32, u32, u32, u32, vp, vp, u32, u32, i32, vp,
                                     C.POINTER(C.c_double)]
         L.orc_wavefront_shadow_bounce.argtypes = [vp, vp, u32, u32, vp, u32, u32, u32, u32, vp, vp, i32,
-                                                  C.POINTER(C.c_double)]
+                                                  C.POINTER(C.c_double), i32]
+        L.orc_wavefront_pixel_rays.argtypes = [vp, vp, u32, u32, vp, u32, u32, vp, u32, vp, vp, i32, i32]
         _lib = L
     return _lib
 
@@ -164,8 +167,9 @@ class OracleSystem:
         return b.tobytes()
 
     def trace(self, rays: np.ndarray, tlas_idx=None, tlas_uniform=0, ray_flags=0, cull_mask=0xFF, anyhit_mode=0,
-              threads=1, counts=False, anyhit_mask=None):
-        """anyhit_mask: uint32 bit array over built triangles (anyhit_mode 3)."""
+              threads=1, counts=False, anyhit_mask=None, watertight=False):
+        """anyhit_mask: uint32 bit array over built triangles (anyhit_mode 3).
+        watertight: the watertight triangle test instead of the reference's."""
         rays = np.ascontiguousarray(rays)
         n = rays.shape[0]
         out = np.zeros(n, HIT_DTYPE)
@@ -176,7 +180,7 @@ class OracleSystem:
         mask = None if anyhit_mask is None else np.ascontiguousarray(anyhit_mask, np.uint32)
         self._check(self._L.orc_trace(self._h, _ptr(rays), n, _ptr(ti), tlas_uniform, ray_flags, cull_mask,
                                       anyhit_mode, _ptr(mask), _ptr(out), _ptr(rc), _ptr(tot), threads,
-                                      C.byref(sec)))
+                                      C.byref(sec), 1 if watertight else 0))
         totals = dict(zip(["tri_visit", "tri_hit", "bvh_visit", "bvh_hit", "far_assert", "bad_tlas"],
                           (int(x) for x in tot)))
         totals["seconds"] = sec.value
@@ -201,6 +205,15 @@ class OracleSystem:
                                           _ptr(np.ascontiguousarray(hits)), _ptr(out)))
         return out
 
+    def edge_margin(self, rays: np.ndarray, hits: np.ndarray) -> np.ndarray:
+        """Per hit: [FP64 distance of the ray's plane point to the triangle's
+        nearest edge (negative outside), f32 position error bound of the
+        reference's formula]; NaN for misses."""
+        out = np.zeros((rays.shape[0], 2), np.float64)
+        self._check(self._L.orc_edge_margin(self._h, _ptr(np.ascontiguousarray(rays)), rays.shape[0],
+                                            _ptr(np.ascontiguousarray(hits)), _ptr(out)))
+        return out
+
     def bruteforce_fp64(self, rays: np.ndarray, tlas_uniform=0, threads=4) -> np.ndarray:
         out = np.zeros((rays.shape[0], 5), np.float64)
         self._check(self._L.orc_bruteforce_fp64(self._h, _ptr(np.ascontiguousarray(rays)), rays.shape[0],
@@ -214,7 +227,7 @@ PIXEL_DTYPE = np.dtype([("primary_prim", np.uint32), ("primary_t", np.float32), 
 
 
 def wavefront_shadow_bounce(system: OracleSystem, cam_floats, width, height, light, sample_index=0, tlas=0,
-                            row0=0, row1=None, threads=1):
+                            row0=0, row1=None, threads=1, watertight=False):
     """The oracle's primary + shadow + bounce pipeline over rows [row0, row1).
     Returns (pixel records, [primary, shadow, bounce] rays, seconds)."""
     row1 = height if row1 is None else row1
@@ -225,8 +238,25 @@ def wavefront_shadow_bounce(system: OracleSystem, cam_floats, width, height, lig
     sec = C.c_double()
     system._check(system._L.orc_wavefront_shadow_bounce(system._h, _ptr(cam), width, height, _ptr(li), sample_index,
                                                         tlas, row0, row1, _ptr(out), _ptr(rays), threads,
-                                                        C.byref(sec)))
+                                                        C.byref(sec), 1 if watertight else 0))
     return out, [int(x) for x in rays], sec.value
+
+
+def wavefront_pixel_rays(system: OracleSystem, cam_floats, width, height, light, pixels, sample_index=0, tlas=0,
+                         threads=1, watertight=False):
+    """The oracle's primary, shadow and bounce rays of the given pixels (y * width + x).
+    Returns (primary rays, shadow rays, bounce rays, primary-hit flags); the
+    shadow and bounce rays of a pixel whose primary missed are zero."""
+    pixels = np.ascontiguousarray(pixels, np.uint32)
+    n = pixels.shape[0]
+    rays = np.zeros(3 * max(n, 1), RAY_DTYPE)
+    has = np.zeros(max(n, 1), np.uint8)
+    cam = np.ascontiguousarray(cam_floats, np.float32)
+    li = np.ascontiguousarray(light, np.float32)
+    system._check(system._L.orc_wavefront_pixel_rays(system._h, _ptr(cam), width, height, _ptr(li), sample_index,
+                                                     tlas, _ptr(pixels), n, _ptr(rays), _ptr(has), threads,
+                                                     1 if watertight else 0))
+    return (rays[0:3 * n:3].copy(), rays[1:3 * n:3].copy(), rays[2:3 * n:3].copy(), has[:n].astype(bool))
 
 
 PATH_DTYPE = np.dtype([("radiance", np.float32), ("depth_flags", np.uint32)])

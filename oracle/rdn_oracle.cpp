@@ -103,14 +103,18 @@ static void cull_triangle(uint32_t f, bool* cull_enable, bool* cull_back) {
 }
 
 // ---- intersectors ----
-static inline bool intersect_ray_aabb(V3 o, V3 d, float tmin, float tmax, V3 bmin, V3 bmax) {
+// far_scale: 1 is the reference's test; the watertight mode passes
+// 1 + 4 * 2^-23 >= 1 + 2 gamma_3 (Ize, "Robust BVH Ray Traversal", JCGT 2013)
+// so that rounding never rejects a box the ray touches.
+static const float WATERTIGHT_BOX_FAR_SCALE = 1.000000476837158203125f;
+static inline bool intersect_ray_aabb(V3 o, V3 d, float tmin, float tmax, V3 bmin, V3 bmax, float far_scale = 1.0f) {
   V3 inv_d = v3(1.0f, 1.0f, 1.0f) / d;
   V3 t0 = (bmin - o) * inv_d;
   V3 t1 = (bmax - o) * inv_d;
   V3 tn = vmin(t0, t1);
   V3 tf = vmax(t0, t1);
   float t_near_max = max_channel(tn);
-  float t_far_min = min_channel(tf);
+  float t_far_min = min_channel(tf) * far_scale;
   return t_near_max <= t_far_min && tmin < t_far_min && t_near_max < tmax;
 }
 
@@ -144,6 +148,59 @@ static inline TriResult intersect_ray_triangle(V3 origin, V3 direction, float ne
   float v = (uv * wu - uu * wv) * inverse_d;
   if (v < 0.0f || (u + v) > 1.0f) return miss;
   return TriResult{sign, t, u, v};
+}
+
+// Watertight f32 triangle test: Woop, Benthin and Wald, "Watertight
+// Ray/Triangle Intersection", JCGT 2(1), 2013 (sheared frame with the ray
+// along +z, 2D edge functions U, V, W). It is not part of the reference, which
+// only has the formula above; this is the oracle twin of the product's
+// optional watertight test, with the same operations in the same order:
+// kz = largest |d| component (lowest axis among equals), kx / ky the next two,
+// swapped when d[kz] < 0; Sz = 1/d[kz], Sx = d[kx]*Sz, Sy = d[ky]*Sz; an edge
+// function that rounds to 0 makes all three be recomputed as exact-sign
+// differences of products (TwoProduct by FMA) instead of the paper's double
+// fallback; t, u, v from one reciprocal of det; NaN never hits. det has the
+// opposite sign of the formula above's b, so culling and the facing sign
+// follow b's rules.
+static inline float pick3(V3 v, uint32_t k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+static inline float diff_products(float a, float b, float c, float d) {
+  float p = a * b, q = c * d;
+  float e = std::fma(a, b, -p), f = std::fma(c, d, -q);
+  return (p - q) + (e - f);
+}
+static inline TriResult intersect_ray_triangle_watertight(V3 o, V3 d, float near_, float far_, V3 v0, V3 v1, V3 v2,
+                                                          bool cull_enable, bool cull_back) {
+  TriResult miss{0.0f, 0.0f, 0.0f, 0.0f};
+  float adx = std::fabs(d.x), ady = std::fabs(d.y), adz = std::fabs(d.z);
+  uint32_t kz = adx >= ady ? (adx >= adz ? 0u : 2u) : (ady >= adz ? 1u : 2u);
+  uint32_t kx = kz == 2u ? 0u : kz + 1u;
+  uint32_t ky = kx == 2u ? 0u : kx + 1u;
+  if (pick3(d, kz) < 0.0f) std::swap(kx, ky);
+  V3 inv_d = v3(1.0f, 1.0f, 1.0f) / d;
+  float sz = pick3(inv_d, kz), sx = pick3(d, kx) * sz, sy = pick3(d, ky) * sz;
+  V3 A = v0 - o, B = v1 - o, C = v2 - o;
+  float akz = pick3(A, kz), bkz = pick3(B, kz), ckz = pick3(C, kz);
+  float ax = pick3(A, kx) - sx * akz, ay = pick3(A, ky) - sy * akz;
+  float bx = pick3(B, kx) - sx * bkz, by = pick3(B, ky) - sy * bkz;
+  float cx = pick3(C, kx) - sx * ckz, cy = pick3(C, ky) - sy * ckz;
+  float U = cx * by - cy * bx, V = ax * cy - ay * cx, W = bx * ay - by * ax;
+  if (U == 0.0f || V == 0.0f || W == 0.0f) {
+    U = diff_products(cx, by, cy, bx);
+    V = diff_products(ax, cy, ay, cx);
+    W = diff_products(bx, ay, by, ax);
+  }
+  if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return miss;
+  float det = (U + V) + W;
+  if (!(std::fabs(det) > 0.0f)) return miss;
+  if (cull_enable) {
+    bool pass = cull_back != (det > 0.0f);
+    if (!pass) return miss;
+  }
+  float T = (U * (sz * akz) + V * (sz * bkz)) + W * (sz * ckz);
+  float rcp = 1.0f / det;
+  float t = T * rcp;
+  if (!(t >= near_ && t <= far_)) return miss;
+  return TriResult{det > 0.0f ? -1.0f : 1.0f, t, V * rcp, W * rcp};
 }
 
 // ---- BVH builder ----
@@ -587,12 +644,13 @@ struct BvhIter {
   V3 o, d;
   RayRange range;
   uint32_t curr;
+  float far_scale;
   uint32_t next(Counters& cn, uint32_t* node_visits) {
     while (curr != INVALID_NEXT) {
       cn.bvh_visit++;
       (*node_visits)++;
       const DeviceBVHNode& n = bvh[curr];
-      if (intersect_ray_aabb(o, d, range.get_near(), range.get_far(), ld3(n.aabb_min), ld3(n.aabb_max))) {
+      if (intersect_ray_aabb(o, d, range.get_near(), range.get_far(), ld3(n.aabb_min), ld3(n.aabb_max), far_scale)) {
         uint32_t c0 = curr;
         curr = n.hit_next;
         if (n.hit_next == n.miss_next) {
@@ -618,9 +676,10 @@ static inline uint32_t any_hit_policy(uint32_t mode, uint32_t primitive_idx, uin
   return ANYHIT_ACCEPT;
 }
 
+// intersector: 0 the reference's triangle test, 1 the watertight test.
 static void traverse(const Built& B, const RayIn& ray, uint32_t tlas_idx, uint32_t ray_flags, uint32_t cull_mask,
                      uint32_t anyhit_mode, HitOut& out, Counters& cn, uint32_t* ray_counts,
-                     uint32_t* tri_out = nullptr, const uint32_t* anyhit_mask = nullptr) {
+                     uint32_t* tri_out = nullptr, const uint32_t* anyhit_mask = nullptr, int intersector = 0) {
   out = HitOut{ray.tmax, 0.0f, 0.0f, INVALID_NEXT, INVALID_NEXT, INVALID_NEXT, INVALID_NEXT, 0};
   uint32_t node_visits = 0, tri_tests = 0;
   bool have = false;
@@ -628,20 +687,21 @@ static void traverse(const Built& B, const RayIn& ray, uint32_t tlas_idx, uint32
   float far_cell = ray.tmax;
   RayRange ray_range{ray.tmin, &far_cell, 1.0f};
   V3 ro = ld3(ray.org), rd = ld3(ray.dir);
+  const float fs = intersector ? WATERTIGHT_BOX_FAR_SCALE : 1.0f;
   if (tlas_idx >= B.tlas_binding.size() || B.tlas_binding[tlas_idx] >= B.tlas_bvh_root.size()) {
     cn.bad_tlas++;
     if (ray_counts) ray_counts[0] = ray_counts[1] = 0;
     return;
   }
   uint32_t root = B.tlas_bvh_root[B.tlas_binding[tlas_idx]];
-  BvhIter tlas_iter{B.tlas_bvh_forest.data(), ro, rd, ray_range, root};
+  BvhIter tlas_iter{B.tlas_bvh_forest.data(), ro, rd, ray_range, root, fs};
   for (;;) {
     uint32_t hit_idx = tlas_iter.next(cn, &node_visits);
     if (hit_idx == INVALID_NEXT) break;
     const DeviceBVHNode& node = B.tlas_bvh_forest[hit_idx];
     for (uint32_t ti = node.content_range[0]; ti < node.content_range[1]; ti++) {
       const TlasBounding& tb = B.tlas_bounding[ti];
-      if (!intersect_ray_aabb(ro, rd, ray.tmin, ray.tmax, ld3(tb.world_min), ld3(tb.world_max))) continue;
+      if (!intersect_ray_aabb(ro, rd, ray.tmin, ray.tmax, ld3(tb.world_min), ld3(tb.world_max), fs)) continue;
       if ((cull_mask & tb.mask) == 0) continue;
       const DeviceInstance& inst = B.tlas_data[ti];
       uint32_t blas_idx = inst.acceleration_structure_handle;
@@ -663,7 +723,7 @@ static void traverse(const Built& B, const RayIn& ray, uint32_t tlas_idx, uint32
           if (!pass) continue;
           bool cull_enable, cull_back;
           cull_triangle(iflags, &cull_enable, &cull_back);
-          BvhIter it{B.tri_bvh_forest.data(), bo, bd, blas_range, g.bvh_root_idx};
+          BvhIter it{B.tri_bvh_forest.data(), bo, bd, blas_range, g.bvh_root_idx, fs};
           for (;;) {
             uint32_t leaf = it.next(cn, &node_visits);
             if (leaf == INVALID_NEXT) break;
@@ -674,8 +734,11 @@ static void traverse(const Built& B, const RayIn& ray, uint32_t tlas_idx, uint32
               V3 v0 = ld3(&B.vertices[i0 * 3]), v1 = ld3(&B.vertices[i1 * 3]), v2 = ld3(&B.vertices[i2 * 3]);
               cn.tri_visit++;
               tri_tests++;
-              TriResult r = intersect_ray_triangle(bo, bd, blas_range.get_near(), blas_range.get_far(), v0, v1, v2,
-                                                   cull_enable, cull_back);
+              TriResult r = intersector ? intersect_ray_triangle_watertight(bo, bd, blas_range.get_near(),
+                                                                            blas_range.get_far(), v0, v1, v2,
+                                                                            cull_enable, cull_back)
+                                        : intersect_ray_triangle(bo, bd, blas_range.get_near(), blas_range.get_far(),
+                                                                 v0, v1, v2, cull_enable, cull_back);
               if (r.s != 0.0f) {
                 float distance = r.t / distance_scaling;
                 uint32_t primitive_idx = tri_idx - g.primitive_start;
@@ -730,7 +793,7 @@ static bool nan_exposure(const Built& B, const RayIn& ray, uint32_t tlas_idx, ui
   float far_cell = ray.tmax;
   RayRange ray_range{ray.tmin, &far_cell, 1.0f};
   V3 ro = ld3(ray.org), rd = ld3(ray.dir);
-  BvhIter tlas_iter{B.tlas_bvh_forest.data(), ro, rd, ray_range, B.tlas_bvh_root[B.tlas_binding[tlas_idx]]};
+  BvhIter tlas_iter{B.tlas_bvh_forest.data(), ro, rd, ray_range, B.tlas_bvh_root[B.tlas_binding[tlas_idx]], 1.0f};
   for (;;) {
     uint32_t hit_idx = tlas_iter.next(cn, &visits);
     if (hit_idx == INVALID_NEXT) break;
@@ -756,7 +819,7 @@ static bool nan_exposure(const Built& B, const RayIn& ray, uint32_t tlas_idx, ui
         cull_geometry(iflags, g.geometry_flags, &pass, &is_opaque);
         if (!pass) continue;
         cull_triangle(iflags, &cull_enable, &cull_back);
-        BvhIter it{B.tri_bvh_forest.data(), bo, bd, blas_range, g.bvh_root_idx};
+        BvhIter it{B.tri_bvh_forest.data(), bo, bd, blas_range, g.bvh_root_idx, 1.0f};
         for (;;) {
           uint32_t leaf = it.next(cn, &visits);
           if (leaf == INVALID_NEXT) break;
@@ -780,7 +843,7 @@ static bool nan_exposure(const Built& B, const RayIn& ray, uint32_t tlas_idx, ui
 // (object-space) triangle, to state the FP32 result's error.
 static void eval_fp64(const Built& B, const RayIn& ray, const HitOut& h, double* out3) {
   out3[0] = out3[1] = out3[2] = NAN;
-  if (h.prim == INVALID_NEXT) return;
+  if (h.prim == INVALID_NEXT || h.instance >= B.tlas_data.size()) return;
   const DeviceInstance& inst = B.tlas_data[h.instance];
   uint32_t blas_idx = inst.acceleration_structure_handle;
   const BlasMetaInfo& bm = B.blas_meta_info[blas_idx];
@@ -789,6 +852,7 @@ static void eval_fp64(const Built& B, const RayIn& ray, const HitOut& h, double*
     if (B.tri_bvh_root[gi].geometry_idx == h.geometry) g = &B.tri_bvh_root[gi];
   if (!g) return;
   uint32_t tri_idx = h.prim + g->primitive_start;
+  if ((size_t)tri_idx * 3 + 2 >= B.indices.size()) return;
   double M[16];
   for (int i = 0; i < 16; i++) M[i] = inst.transform_inv[i];
   double o[3] = {ray.org[0], ray.org[1], ray.org[2]}, d[3] = {ray.dir[0], ray.dir[1], ray.dir[2]};
@@ -877,12 +941,13 @@ static const uint32_t RAY_FLAG_END_SEARCH = 0x04;
 
 static void wavefront_pixel(const Built& B, const Camera& cam, uint32_t W, uint32_t H, uint32_t px, uint32_t py,
                             V3 light, uint32_t sample_index, uint32_t tlas, PixelOut& o, Counters& cn,
-                            uint64_t* rays) {
+                            uint64_t* rays, int intersector = 0, RayIn* rays_out = nullptr) {
   V3 d = camera_dir(cam, px, py, W, H);
   RayIn r{{cam.origin.x, cam.origin.y, cam.origin.z}, 0.0f, {d.x, d.y, d.z}, F_INF};
   HitOut h;
   uint32_t tri = 0;
-  traverse(B, r, tlas, 0, 0xFFu, 0, h, cn, nullptr, &tri);
+  if (rays_out) rays_out[0] = r;
+  traverse(B, r, tlas, 0, 0xFFu, 0, h, cn, nullptr, &tri, nullptr, intersector);
   rays[0]++;
   o = PixelOut{h.prim, h.t, INVALID_NEXT, F32_MAX, 0u, 0u, 0.0f, h.instance};
   if (h.prim == INVALID_NEXT) return;
@@ -899,7 +964,8 @@ static void wavefront_pixel(const Built& B, const Camera& cam, uint32_t W, uint3
   float direct = rmax(0.0f, dot(nf, ldir)) / dist2;
   RayIn sr{{org.x, org.y, org.z}, F32_EPSILON, {ldir.x, ldir.y, ldir.z}, dist};
   HitOut sh;
-  traverse(B, sr, tlas, RAY_FLAG_END_SEARCH, 0xFFu, 0, sh, cn, nullptr);
+  if (rays_out) rays_out[1] = sr;
+  traverse(B, sr, tlas, RAY_FLAG_END_SEARCH, 0xFFu, 0, sh, cn, nullptr, nullptr, nullptr, intersector);
   rays[1]++;
   o.light = sh.prim == INVALID_NEXT ? 1u : 2u;
   o.direct = sh.prim == INVALID_NEXT ? direct : 0.0f;
@@ -910,7 +976,8 @@ static void wavefront_pixel(const Built& B, const Camera& cam, uint32_t W, uint3
   V3 bdir = cosine_sample_in_dir(nf, s0, s1);
   RayIn br{{org.x, org.y, org.z}, F32_EPSILON, {bdir.x, bdir.y, bdir.z}, F32_MAX};
   HitOut bh;
-  traverse(B, br, tlas, 0, 0xFFu, 0, bh, cn, nullptr);
+  if (rays_out) rays_out[2] = br;
+  traverse(B, br, tlas, 0, 0xFFu, 0, bh, cn, nullptr, nullptr, nullptr, intersector);
   rays[2]++;
   o.bounce_prim = bh.prim;
   o.bounce_t = bh.t;
@@ -1107,10 +1174,11 @@ size_t orc_get_buffer(void* cp, int which, void* dst, size_t cap) {
 // `tlas_uniform` is used for every ray). `ray_counts` (nullable) receives
 // [node visits, triangle tests] per ray; `totals` receives tri_visit, tri_hit,
 // bvh_visit, bvh_hit, far_assert, bad_tlas. Returns elapsed seconds of the
-// traversal loop in *seconds (nullable).
+// traversal loop in *seconds (nullable). intersector: 0 the reference's
+// triangle test, 1 the watertight test.
 int orc_trace(void* cp, const RayIn* rays, uint32_t n, const uint32_t* tlas_idx, uint32_t tlas_uniform,
               uint32_t ray_flags, uint32_t cull_mask, uint32_t anyhit_mode, const uint32_t* anyhit_mask, HitOut* out,
-              uint32_t* ray_counts, uint64_t* totals, int threads, double* seconds) {
+              uint32_t* ray_counts, uint64_t* totals, int threads, double* seconds, int intersector) {
   if (anyhit_mode == 3 && !anyhit_mask) return -1;
   Ctx& c = *(Ctx*)cp;
   if (!c.built) {
@@ -1125,7 +1193,7 @@ int orc_trace(void* cp, const RayIn* rays, uint32_t n, const uint32_t* tlas_idx,
     uint32_t s = (uint32_t)((uint64_t)n * w / threads), e = (uint32_t)((uint64_t)n * (w + 1) / threads);
     for (uint32_t i = s; i < e; i++)
       traverse(B, rays[i], tlas_idx ? tlas_idx[i] : tlas_uniform, ray_flags, cull_mask, anyhit_mode, out[i], cn[w],
-               ray_counts ? ray_counts + 2 * (size_t)i : nullptr, nullptr, anyhit_mask);
+               ray_counts ? ray_counts + 2 * (size_t)i : nullptr, nullptr, anyhit_mask, intersector);
   };
   if (threads == 1) {
     work(0);
@@ -1168,6 +1236,82 @@ int orc_nan_exposure(void* cp, const RayIn* rays, uint32_t n, const uint32_t* tl
   std::vector<std::thread> th;
   for (int w = 0; w < threads; w++) th.emplace_back(work, w);
   for (auto& t : th) t.join();
+  return 0;
+}
+
+// Test infrastructure: how far a reported hit lies from its triangle's edges,
+// against how far the reference's f32 formula can misplace the hit point.
+// out2 = [d, b] per ray: d = FP64 distance (object space) from the ray's
+// intersection with the triangle's plane to the nearest edge line of the
+// triangle, negative when the point lies outside it; b = 32 * 2^-24 *
+// max(t, |o - v0|) / |cos theta| + 1e-4 * (smallest altitude), the f32 position
+// error bound of the plane-distance formula (its t is a quotient whose
+// relative error grows as 1/|cos theta| for grazing rays) plus a floor of
+// 1e-4 in barycentric terms. NaN for misses.
+static void edge_margin(const Built& B, const RayIn& ray, const HitOut& h, double* out2) {
+  out2[0] = out2[1] = NAN;
+  if (h.prim == INVALID_NEXT || h.instance >= B.tlas_data.size()) return;
+  const DeviceInstance& inst = B.tlas_data[h.instance];
+  const BlasMetaInfo& bm = B.blas_meta_info[inst.acceleration_structure_handle];
+  const GeometryMetaInfo* g = nullptr;
+  for (uint32_t gi = bm.tri_root_range[0]; gi < bm.tri_root_range[1]; gi++)
+    if (B.tri_bvh_root[gi].geometry_idx == h.geometry) g = &B.tri_bvh_root[gi];
+  if (!g) return;
+  uint32_t tri_idx = h.prim + g->primitive_start;
+  if ((size_t)tri_idx * 3 + 2 >= B.indices.size()) return;
+  double M[16];
+  for (int i = 0; i < 16; i++) M[i] = inst.transform_inv[i];
+  double bo[4], bd[3];
+  for (int r = 0; r < 4; r++) bo[r] = ray.org[0] * M[r] + ray.org[1] * M[4 + r] + ray.org[2] * M[8 + r] + M[12 + r];
+  for (int r = 0; r < 3; r++) bo[r] /= bo[3];
+  for (int r = 0; r < 3; r++) bd[r] = ray.dir[0] * M[r] + ray.dir[1] * M[4 + r] + ray.dir[2] * M[8 + r];
+  double sc = std::sqrt(bd[0] * bd[0] + bd[1] * bd[1] + bd[2] * bd[2]);
+  for (int r = 0; r < 3; r++) bd[r] /= sc;
+  double v[3][3];
+  for (int k = 0; k < 3; k++)
+    for (int r = 0; r < 3; r++) v[k][r] = B.vertices[B.indices[tri_idx * 3 + k] * 3 + r];
+  auto sub = [](const double* a, const double* b, double* o) { for (int r = 0; r < 3; r++) o[r] = a[r] - b[r]; };
+  auto dotd = [](const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; };
+  auto crossd = [](const double* a, const double* b, double* o) {
+    o[0] = a[1] * b[2] - a[2] * b[1];
+    o[1] = a[2] * b[0] - a[0] * b[2];
+    o[2] = a[0] * b[1] - a[1] * b[0];
+  };
+  double e1[3], e2[3], n[3], w0[3];
+  sub(v[1], v[0], e1);
+  sub(v[2], v[0], e2);
+  crossd(e1, e2, n);
+  double nn = std::sqrt(dotd(n, n));
+  if (!(nn > 0.0)) return;
+  sub(bo, v[0], w0);
+  double bdn = dotd(n, bd);
+  double t = -dotd(n, w0) / bdn;
+  double p[3];
+  for (int r = 0; r < 3; r++) p[r] = bo[r] + t * bd[r];
+  // signed distance to each edge line within the plane: cross(edge, p - start) . n / (|edge| |n|)
+  double dist = INFINITY, min_alt = INFINITY;
+  for (int k = 0; k < 3; k++) {
+    const double* a = v[k];
+    const double* b = v[(k + 1) % 3];
+    double e[3], ap[3], c[3];
+    sub(b, a, e);
+    sub(p, a, ap);
+    crossd(e, ap, c);
+    double le = std::sqrt(dotd(e, e));
+    double dk = dotd(c, n) / (le * nn);
+    dist = std::min(dist, dk);
+    min_alt = std::min(min_alt, nn / le);
+  }
+  double cos_t = std::fabs(bdn) / nn;
+  double reach = std::max(std::fabs(t), std::sqrt(dotd(w0, w0)));
+  out2[0] = dist;
+  out2[1] = 32.0 * std::ldexp(1.0, -24) * reach / std::max(cos_t, 1e-30) + 1e-4 * min_alt;
+}
+
+int orc_edge_margin(void* cp, const RayIn* rays, uint32_t n, const HitOut* hits, double* out) {
+  Ctx& c = *(Ctx*)cp;
+  if (!c.built) return -1;
+  for (uint32_t i = 0; i < n; i++) edge_margin(*c.built, rays[i], hits[i], out + 2 * (size_t)i);
   return 0;
 }
 
@@ -1299,7 +1443,7 @@ int orc_select_nth(const float* keys, uint64_t* idx, size_t len, size_t index) {
 // 32 B pixel records; rays3 receives [primary, shadow, bounce] rays traced.
 int orc_wavefront_shadow_bounce(void* cp, const float* cam, uint32_t W, uint32_t H, const float* light,
                                 uint32_t sample_index, uint32_t tlas, uint32_t row0, uint32_t row1, void* out,
-                                uint64_t* rays3, int threads, double* seconds) {
+                                uint64_t* rays3, int threads, double* seconds, int intersector) {
   Ctx& c = *(Ctx*)cp;
   if (!c.built) {
     int rc = build_all(c);
@@ -1323,7 +1467,7 @@ int orc_wavefront_shadow_bounce(void* cp, const float* cam, uint32_t W, uint32_t
       if (y >= row1) break;
       for (uint32_t x = 0; x < W; x++)
         wavefront_pixel(B, cm, W, H, x, y, L, sample_index, tlas, po[(size_t)(y - row0) * W + x], cn[w],
-                        &rc[3 * (size_t)w]);
+                        &rc[3 * (size_t)w], intersector);
     }
   };
   std::vector<std::thread> th;
@@ -1340,6 +1484,42 @@ int orc_wavefront_shadow_bounce(void* cp, const float* cam, uint32_t W, uint32_t
   return 0;
 }
 
+
+// The rays of the given pixels of the same workload (for classifying
+// differences of those rays' results): rays[3 * i] = primary, rays[3 * i + 1]
+// = shadow, rays[3 * i + 2] = bounce ray of pixel pixels[i] (y * W + x);
+// has[i] = 1 when the pixel's primary ray hit (the shadow and bounce rays
+// exist), else 0 and those two rays zero.
+int orc_wavefront_pixel_rays(void* cp, const float* cam, uint32_t W, uint32_t H, const float* light,
+                                 uint32_t sample_index, uint32_t tlas, const uint32_t* pixels, uint32_t n,
+                                 RayIn* rays, uint8_t* has, int threads, int intersector) {
+  Ctx& c = *(Ctx*)cp;
+  if (!c.built) {
+    int rc = build_all(c);
+    if (rc) return rc;
+  }
+  const Built& B = *c.built;
+  Camera cm{ld3(cam), ld3(cam + 3), ld3(cam + 6), ld3(cam + 9), cam[12], cam[13]};
+  V3 L = ld3(light);
+  if (threads < 1) threads = 1;
+  auto work = [&](int w) {
+    Counters cn;
+    uint64_t rc3[3] = {0, 0, 0};
+    uint32_t s = (uint32_t)((uint64_t)n * w / threads), e = (uint32_t)((uint64_t)n * (w + 1) / threads);
+    for (uint32_t i = s; i < e; i++) {
+      PixelOut po;
+      RayIn* r3 = rays + 3 * (size_t)i;
+      std::memset(r3, 0, 3 * sizeof(RayIn));
+      const uint32_t x = pixels[i] % W, y = pixels[i] / W;
+      wavefront_pixel(B, cm, W, H, x, y, L, sample_index, tlas, po, cn, rc3, intersector, r3);
+      has[i] = po.primary_flags & 1u;
+    }
+  };
+  std::vector<std::thread> th;
+  for (int w = 0; w < threads; w++) th.emplace_back(work, w);
+  for (auto& t : th) t.join();
+  return 0;
+}
 
 // One AO sample for rows [row0, row1) of a width x height frame (see
 // orc_ao.h); image: width * height RGBA8 texels, updated in place. rays2

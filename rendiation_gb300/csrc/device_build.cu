@@ -724,6 +724,26 @@ __global__ void emit_nodes_kernel(uint32_t T, uint32_t G, const BNode* __restric
 }
 
 // indices_redirect and the 64 B triangle records in the sorted order.
+// One thread per sorted triangle: its three vertices, copied (no arithmetic).
+__global__ void emit_vertex_records_kernel(uint32_t N, const uint32_t* __restrict__ redirect,
+                                           const uint32_t* __restrict__ idx, const float* __restrict__ vtx,
+                                           VertexRecord* __restrict__ out) {
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < N; j += gridDim.x * blockDim.x) {
+    const uint32_t p = __ldg(redirect + j);
+    float v[9];
+    for (int k = 0; k < 3; k++) {
+      const float* q = vtx + 3 * (size_t)__ldg(idx + 3 * (size_t)p + k);
+      v[3 * k] = __ldg(q);
+      v[3 * k + 1] = __ldg(q + 1);
+      v[3 * k + 2] = __ldg(q + 2);
+    }
+    float4* o = reinterpret_cast<float4*>(out + j);
+    o[0] = make_float4(v[0], v[1], v[2], v[3]);
+    o[1] = make_float4(v[4], v[5], v[6], v[7]);
+    o[2] = make_float4(v[8], 0.0f, 0.0f, 0.0f);
+  }
+}
+
 __global__ void emit_primitives_kernel(uint32_t N, const uint32_t* __restrict__ order, const uint32_t* __restrict__ idx,
                                        const float* __restrict__ vtx, uint32_t* __restrict__ redirect,
                                        TriRecord* __restrict__ tris) {
@@ -1263,6 +1283,15 @@ std::string build_blas_device(const std::vector<DeviceGeometry>& geoms, uint32_t
   }
 #undef CK
   return std::string();
+}
+
+cudaError_t emit_vertex_records(const DeviceBuilt& d, cudaStream_t st) {
+  const uint32_t N = (uint32_t)d.indices_redirect.count;
+  if (N == 0) return cudaSuccess;
+  const uint32_t blocks = std::min<uint32_t>((N + kBlock - 1) / kBlock, 4096u);
+  emit_vertex_records_kernel<<<blocks, kBlock, 0, st>>>(N, d.indices_redirect.ptr, d.indices.ptr, d.vertices.ptr,
+                                                        d.vertex_records.ptr);
+  return cudaGetLastError();
 }
 
 }  // namespace rdn

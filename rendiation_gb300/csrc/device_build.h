@@ -40,4 +40,9 @@ struct DeviceBlasOut {
 std::string build_blas_device(const std::vector<DeviceGeometry>& geoms, uint32_t bin_size, uint32_t max_depth,
                               int sm_count, cudaMemPool_t pool, DeviceBuilt& d, DeviceBlasOut& out);
 
+// Writes d.vertex_records[j] = the three vertices of sorted triangle j
+// (d.indices_redirect, d.indices, d.vertices must be on the device), for j <
+// d.indices_redirect.count, on `st`.
+cudaError_t emit_vertex_records(const DeviceBuilt& d, cudaStream_t st);
+
 }  // namespace rdn

@@ -13,6 +13,7 @@
 #include "rdn_core.h"
 #include "trace_kernels.h"
 #include "adjoint.h"
+#include "device_build.h"
 #include "parallel.h"
 #include "paths.h"
 #include "task_graph.h"
@@ -61,6 +62,7 @@ void free_device(rdn::DeviceBuilt& d) {
   free_buf(d.blas_meta_info);
   free_buf(d.tri_bvh_root);
   free_buf(d.tri_records);
+  free_buf(d.vertex_records);
   free_buf(d.wide_nodes);
   free_buf(d.wide4_nodes);
   free_buf(d.geom_root_code4);
@@ -167,6 +169,21 @@ rdn_status do_build(rdn_ctx* c) {
       UP(wide4_nodes, wide4_nodes)
     }
 #undef UP
+    {
+      // vertices of every sorted triangle, for the watertight test, gathered on the device
+      const size_t n = d.indices_redirect.count;
+      e = cudaMalloc(&d.vertex_records.ptr, (n ? n : 1) * sizeof(rdn::VertexRecord));
+      if (e == cudaSuccess) {
+        d.vertex_records.count = n;
+        bytes += (n ? n : 1) * sizeof(rdn::VertexRecord);
+        e = n ? rdn::emit_vertex_records(d, 0) : cudaMemset(d.vertex_records.ptr, 0, sizeof(rdn::VertexRecord));
+      }
+      if (e == cudaSuccess) e = cudaStreamSynchronize(0);
+      if (e != cudaSuccess) {
+        free_device(d);
+        return cuda_fail(c, e, "vertex records");
+      }
+    }
     d.max_blas_depth = hb->max_blas_depth;
     d.max_wide4_depth = hb->max_wide4_depth;
     d.vertex_count = hb->n_vertices;
@@ -178,9 +195,13 @@ rdn_status do_build(rdn_ctx* c) {
   return RDN_OK;
 }
 
+// The walk order of a traversal value (RDN_INTERSECT_WATERTIGHT may be OR-ed in).
+uint32_t order_of(uint32_t traversal) { return traversal & ~RDN_INTERSECT_WATERTIGHT; }
+bool traversal_ok(uint32_t traversal) { return order_of(traversal) <= RDN_TRAVERSAL_ORDERED_WIDE; }
+
 int mode_of(uint32_t traversal) {
-  if (traversal == RDN_TRAVERSAL_REFERENCE) return rdn::MODE_THREADED;
-  if (traversal == RDN_TRAVERSAL_ORDERED_WIDE) return rdn::MODE_WIDE4;
+  if (order_of(traversal) == RDN_TRAVERSAL_REFERENCE) return rdn::MODE_THREADED;
+  if (order_of(traversal) == RDN_TRAVERSAL_ORDERED_WIDE) return rdn::MODE_WIDE4;
   return rdn::MODE_BINARY;
 }
 
@@ -217,9 +238,12 @@ rdn_status fill_params(rdn_ctx* c, const rdn_trace_desc* desc, rdn::TraceParams&
   p.geom_root_code4 = d.geom_root_code4.ptr;
   p.counters = reinterpret_cast<unsigned long long*>(c->d_counters);
   p.error_word = c->d_counters + 8;
-  p.local_stack = desc->local_stack && desc->traversal != RDN_TRAVERSAL_REFERENCE &&
+  p.local_stack = desc->local_stack && order_of(desc->traversal) != RDN_TRAVERSAL_REFERENCE &&
                   p.stack_depth <= rdn::kLocalStackEntries;
   p.iteration_limit = c->iteration_limit;
+  p.watertight = (desc->traversal & RDN_INTERSECT_WATERTIGHT) ? 1u : 0u;
+  p.box_far_scale = p.watertight ? rdn::kWatertightBoxFarScale : 1.0f;
+  p.verts = reinterpret_cast<const float4*>(d.vertex_records.ptr);
   return RDN_OK;
 }
 
@@ -230,7 +254,7 @@ rdn_status validate_trace(rdn_ctx* c, const rdn_trace_desc* desc) {
   if ((reinterpret_cast<uintptr_t>(desc->rays) & 15) || (reinterpret_cast<uintptr_t>(desc->hits) & 15) ||
       (reinterpret_cast<uintptr_t>(desc->hits_ext) & 15))
     return fail(c, RDN_ERR_INVALID_ARG, "ray and hit buffers must be 16-byte aligned");
-  if (desc->traversal > RDN_TRAVERSAL_ORDERED_WIDE) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
+  if (!traversal_ok(desc->traversal)) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
   if (desc->anyhit_mode > RDN_ANYHIT_PRIMITIVE_MASK) return fail(c, RDN_ERR_INVALID_ARG, "unknown any-hit mode");
   if (desc->anyhit_mode == RDN_ANYHIT_PRIMITIVE_MASK && !desc->anyhit_mask)
     return fail(c, RDN_ERR_INVALID_ARG, "RDN_ANYHIT_PRIMITIVE_MASK needs anyhit_mask");
@@ -248,7 +272,7 @@ rdn_status ensure_built(rdn_ctx* c) {
 // Checks of the knobs that rdn_wavefront_shadow_bounce and its allocation-free
 // variant share (their scratch checks differ).
 rdn_status wavefront_check_knobs(rdn_ctx* c, const rdn_wavefront_desc* d) {
-  if (d->traversal > RDN_TRAVERSAL_ORDERED_WIDE) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
+  if (!traversal_ok(d->traversal)) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
   if (d->phases > 3) return fail(c, RDN_ERR_INVALID_ARG, "unknown phase mask");
   if (d->refill > 32) return fail(c, RDN_ERR_INVALID_ARG, "refill must be 0..32");
   if (d->local_stack > 1) return fail(c, RDN_ERR_INVALID_ARG, "local_stack must be 0 or 1");
@@ -571,7 +595,7 @@ rdn_status rdn_trace_params(rdn_ctx* c, uint32_t traversal, void* out, size_t* s
     return RDN_OK;
   }
   if (*size < sizeof(rdn::TraceParams)) return fail(c, RDN_ERR_INVALID_ARG, "output smaller than the parameter block");
-  if (traversal > RDN_TRAVERSAL_ORDERED_WIDE) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
+  if (!traversal_ok(traversal)) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
   if (c->device < 0) return fail(c, RDN_ERR_UNSUPPORTED, "host-only context has no device structure");
   std::lock_guard<std::mutex> lk(c->lock);
   rdn_status st = ensure_built(c);
@@ -583,7 +607,7 @@ rdn_status rdn_trace_params(rdn_ctx* c, uint32_t traversal, void* out, size_t* s
   td.local_stack = 1;
   rdn::TraceParams p;
   fill_params(c, &td, p);
-  if (traversal != RDN_TRAVERSAL_REFERENCE && !p.local_stack)
+  if (order_of(traversal) != RDN_TRAVERSAL_REFERENCE && !p.local_stack)
     return fail(c, RDN_ERR_UNSUPPORTED, "the tree is too deep for a 64-entry local traversal stack");
   std::memcpy(out, &p, sizeof(p));
   *size = sizeof(p);
@@ -672,7 +696,7 @@ rdn_status prepare_path_launch(rdn_ctx* c, const rdn_path_desc* d, rdn::TracePar
   if ((reinterpret_cast<uintptr_t>(d->scratch) & 255) || (reinterpret_cast<uintptr_t>(d->rays) & 15) ||
       (reinterpret_cast<uintptr_t>(d->out) & 7))
     return fail(c, RDN_ERR_INVALID_ARG, "misaligned buffer");
-  if (d->traversal > RDN_TRAVERSAL_ORDERED_WIDE) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
+  if (!traversal_ok(d->traversal)) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
   if (d->block_size && (d->block_size % 32 || d->block_size > 128))
     return fail(c, RDN_ERR_INVALID_ARG, "block_size must be a multiple of 32 up to 128");
   if (!(d->rr_survive > 0.0f && d->rr_survive <= 1.0f)) return fail(c, RDN_ERR_INVALID_ARG, "rr_survive not in (0, 1]");
@@ -808,7 +832,7 @@ rdn_status prepare_attr(rdn_ctx* c, const rdn_attr_loss_desc* d, bool adjoint, r
   if (d->from_record > 1) return fail(c, RDN_ERR_INVALID_ARG, "from_record must be 0 or 1");
   if (adjoint && d->from_record && d->count && (!d->hit_tri || !d->hit_inst))
     return fail(c, RDN_ERR_INVALID_ARG, "from_record needs the hit_tri and hit_inst records of the forward");
-  if (d->traversal > RDN_TRAVERSAL_ORDERED_WIDE) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
+  if (!traversal_ok(d->traversal)) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
   if (d->block_size && (d->block_size % 32 || d->block_size > 128))
     return fail(c, RDN_ERR_INVALID_ARG, "block_size must be a multiple of 32 up to 128");
   rdn_status st = ensure_built(c);
@@ -892,7 +916,7 @@ rdn_status prepare_attr_paths(rdn_ctx* c, const rdn_attr_path_desc* d, bool adjo
   if ((reinterpret_cast<uintptr_t>(d->rays) & 15) || (reinterpret_cast<uintptr_t>(d->grad_vertices) & 15) ||
       (reinterpret_cast<uintptr_t>(d->seg_rays) & 15))
     return fail(c, RDN_ERR_INVALID_ARG, "rays, segment rays and gradients must be 16-byte aligned");
-  if (d->traversal > RDN_TRAVERSAL_ORDERED_WIDE) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
+  if (!traversal_ok(d->traversal)) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
   if (d->block_size && (d->block_size % 32 || d->block_size > 128))
     return fail(c, RDN_ERR_INVALID_ARG, "block_size must be a multiple of 32 up to 128");
   if (d->from_record > 1) return fail(c, RDN_ERR_INVALID_ARG, "from_record must be 0 or 1");
@@ -1131,7 +1155,7 @@ rdn_status ao_env(rdn_ctx* c, const rdn_ao_desc* d, rdn::TraceParams& p, rdn::Ao
     if (d->width == 0 || d->height == 0 || (uint64_t)d->width * d->height > 0x7FFFFFFFull)
       return fail(c, RDN_ERR_INVALID_ARG, "AO frame size must be 1..2^31 pixels");
   }
-  if (d->traversal > RDN_TRAVERSAL_ORDERED_WIDE) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
+  if (!traversal_ok(d->traversal)) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
   if (d->block_size && d->block_size != 32 && d->block_size != 64 && d->block_size != 128)
     return fail(c, RDN_ERR_INVALID_ARG, "block_size must be 32, 64 or 128");
   rdn_status st = ensure_built(c);

@@ -87,6 +87,13 @@ struct TriRecord {
   float q[16];
 };
 static_assert(sizeof(TriRecord) == 64, "64 B triangle");
+// The three vertices of a triangle, 48 B, in the same sorted order, for the
+// watertight test (which must see the shared vertex values themselves, not
+// edges rounded from them): q0 = (v0.xyz, v1.x) q1 = (v1.yz, v2.xy) q2 = (v2.z, 0, 0, 0).
+struct VertexRecord {
+  float q[12];
+};
+static_assert(sizeof(VertexRecord) == 48, "48 B vertex record");
 // Two-child node, 64 B: children's boxes and child codes.
 //   w0 = (c0.lo.x, c0.lo.y, c0.lo.z, c0.hi.x)  w1 = (c0.hi.y, c0.hi.z, c1.lo.x, c1.lo.y)
 //   w2 = (c1.lo.z, c1.hi.x, c1.hi.y, c1.hi.z)  w3 = (code0, code1, 0, 0)
@@ -170,6 +177,7 @@ struct DeviceBuilt {
   DevBuf<BlasMetaInfo> blas_meta_info;
   DevBuf<GeometryMetaInfo> tri_bvh_root;
   DevBuf<TriRecord> tri_records;
+  DevBuf<VertexRecord> vertex_records;
   DevBuf<WideNode> wide_nodes;
   DevBuf<Wide4Node> wide4_nodes;
   DevBuf<uint32_t> geom_root_code4;

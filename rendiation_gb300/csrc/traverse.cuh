@@ -63,15 +63,20 @@ __device__ __forceinline__ float signum_f(float x) {
 }
 
 // intersect_ray_aabb_cpu with the reciprocal direction precomputed (1/d is
-// the same IEEE value the reference forms per test).
+// the same IEEE value the reference forms per test). far_scale multiplies the
+// box's exit distance: 1 (exactly the reference's test) or, with the
+// watertight triangle test, kWatertightBoxFarScale, so that rounding cannot
+// reject a box the ray touches (Ize, "Robust BVH Ray Traversal", JCGT 2(2),
+// 2013: t_far * (1 + 2 gamma_3)); without it a ray through a shared vertex or
+// edge on a box face can skip the box that holds its triangle.
 __device__ __forceinline__ bool slab(float3 o, float3 inv_d, float tmin, float tmax, float lx, float ly, float lz,
-                                     float hx, float hy, float hz, float& t_near_max) {
+                                     float hx, float hy, float hz, float& t_near_max, float far_scale) {
   const float t0x = (lx - o.x) * inv_d.x, t0y = (ly - o.y) * inv_d.y, t0z = (lz - o.z) * inv_d.z;
   const float t1x = (hx - o.x) * inv_d.x, t1y = (hy - o.y) * inv_d.y, t1z = (hz - o.z) * inv_d.z;
   const float nx = fminf(t0x, t1x), ny = fminf(t0y, t1y), nz = fminf(t0z, t1z);
   const float fx = fmaxf(t0x, t1x), fy = fmaxf(t0y, t1y), fz = fmaxf(t0z, t1z);
   const float tn = fmaxf(fmaxf(nx, ny), nz);
-  const float tf = fminf(fminf(fx, fy), fz);
+  const float tf = fminf(fminf(fx, fy), fz) * far_scale;
   t_near_max = tn;
   return tn <= tf && tmin < tf && tn < tmax;
 }
@@ -107,6 +112,92 @@ __device__ __forceinline__ bool tri_test(const float4* __restrict__ rec, float3 
   r.u = u;
   r.v = v;
   r.s = signum_f(b);
+  return true;
+}
+
+// ---- watertight triangle test ----------------------------------------------
+// Woop, Benthin and Wald, "Watertight Ray/Triangle Intersection", Journal of
+// Computer Graphics Techniques 2(1), 2013: the ray is made the +z axis of a
+// sheared frame (kz = the largest |d| component, kx and ky the next two,
+// swapped when d[kz] < 0 to keep the winding), the triangle's vertices are
+// transformed into it and tested with 2D edge functions U, V, W. Two triangles
+// sharing an edge evaluate that edge's function on the same two vertices in
+// opposite order, and a*b - c*d in f32 is exactly antisymmetric under that
+// swap, so a ray can pass between them only if both see exactly 0 (then both
+// accept it): no ray leaks through a shared edge. Where a function rounds to 0
+// the three are recomputed as exact-sign differences of products (TwoProduct
+// by FMA), in place of the paper's double-precision fallback: every step stays
+// f32. Differences from the paper's listing: Sx = d[kx] * (1/d[kz]) (the
+// reciprocal the slab test already holds), t and the barycentrics from one
+// reciprocal of det, and NaN never hits. Facing: det has the opposite sign of
+// the reference's b = n.d, so culling and the hit kind follow b's rules.
+struct Shear {
+  uint32_t kx, ky, kz;
+  float sx, sy, sz;
+};
+
+__device__ __forceinline__ float pick(float3 v, uint32_t k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+
+// kz = the largest |component| (the lowest axis among equals).
+__device__ __forceinline__ Shear make_shear(float3 d, float3 inv_d) {
+  const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+  Shear s;
+  s.kz = ax >= ay ? (ax >= az ? 0u : 2u) : (ay >= az ? 1u : 2u);
+  uint32_t kx = s.kz == 2u ? 0u : s.kz + 1u;
+  uint32_t ky = kx == 2u ? 0u : kx + 1u;
+  if (pick(d, s.kz) < 0.0f) {
+    const uint32_t t = kx;
+    kx = ky;
+    ky = t;
+  }
+  s.kx = kx;
+  s.ky = ky;
+  s.sz = pick(inv_d, s.kz);
+  s.sx = pick(d, kx) * s.sz;
+  s.sy = pick(d, ky) * s.sz;
+  return s;
+}
+
+// a*b - c*d with the exact sign: the products' rounding errors by FMA
+// (TwoProduct), then (p - q) + (e - f). Antisymmetric like the plain form.
+__device__ __forceinline__ float diff_products(float a, float b, float c, float d) {
+  const float p = a * b, q = c * d;
+  const float e = __fmaf_rn(a, b, -p), f = __fmaf_rn(c, d, -q);
+  return (p - q) + (e - f);
+}
+
+__device__ __forceinline__ bool tri_test_watertight(const float4* __restrict__ rec, float3 o, const Shear& sh,
+                                                    float near_, float far_, bool cull_enable, bool cull_back,
+                                                    TriOut& r) {
+  const float4 q0 = __ldg(rec), q1 = __ldg(rec + 1), q2 = __ldg(rec + 2);
+  const float3 A = make_float3(q0.x - o.x, q0.y - o.y, q0.z - o.z);
+  const float3 B = make_float3(q0.w - o.x, q1.x - o.y, q1.y - o.z);
+  const float3 C = make_float3(q1.z - o.x, q1.w - o.y, q2.x - o.z);
+  const float akz = pick(A, sh.kz), bkz = pick(B, sh.kz), ckz = pick(C, sh.kz);
+  const float ax = pick(A, sh.kx) - sh.sx * akz, ay = pick(A, sh.ky) - sh.sy * akz;
+  const float bx = pick(B, sh.kx) - sh.sx * bkz, by = pick(B, sh.ky) - sh.sy * bkz;
+  const float cx = pick(C, sh.kx) - sh.sx * ckz, cy = pick(C, sh.ky) - sh.sy * ckz;
+  float U = cx * by - cy * bx, V = ax * cy - ay * cx, W = bx * ay - by * ax;
+  if (U == 0.0f || V == 0.0f || W == 0.0f) {
+    U = diff_products(cx, by, cy, bx);
+    V = diff_products(ax, cy, ay, cx);
+    W = diff_products(bx, ay, by, ax);
+  }
+  if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+  const float det = (U + V) + W;
+  if (!(fabsf(det) > 0.0f)) return false;
+  if (cull_enable) {
+    const bool pass = cull_back != (det > 0.0f);  // det > 0 <=> the reference's b < 0
+    if (!pass) return false;
+  }
+  const float T = (U * (sh.sz * akz) + V * (sh.sz * bkz)) + W * (sh.sz * ckz);
+  const float rcp = 1.0f / det;
+  const float t = T * rcp;
+  if (!(t >= near_ && t <= far_)) return false;
+  r.t = t;
+  r.u = V * rcp;
+  r.v = W * rcp;
+  r.s = det > 0.0f ? -1.0f : 1.0f;
   return true;
 }
 
@@ -211,7 +302,13 @@ __device__ __forceinline__ bool leaf_triangles(const TraceParams& p, RayCtx& R, 
     if (COUNT) R.tri_tests++;
     TriOut h;
     const float near_ = R.tmin * ir.scaling, far_ = R.far_world * ir.scaling;
-    if (!tri_test(p.tris + 4 * (size_t)k, ir.o, ir.d, near_, far_, cull_enable, cull_back, h)) continue;
+    if (p.watertight) {
+      if (!tri_test_watertight(p.verts + 3 * (size_t)k, ir.o, make_shear(ir.d, ir.inv_d), near_, far_, cull_enable,
+                               cull_back, h))
+        continue;
+    } else if (!tri_test(p.tris + 4 * (size_t)k, ir.o, ir.d, near_, far_, cull_enable, cull_back, h)) {
+      continue;
+    }
     if (COUNT) R.tri_hits++;
     const float distance = h.t / ir.scaling;
     uint32_t behavior = ANYHIT_ACCEPT;
@@ -248,7 +345,7 @@ __device__ __forceinline__ bool blas_threaded(const TraceParams& p, RayCtx& R, c
     const float4 a = __ldg(nd), b = __ldg(nd + 1);
     float tn;
     const uint32_t hit_next = __float_as_uint(a.w), miss_next = __float_as_uint(b.w);
-    if (slab(ir.o, ir.inv_d, R.tmin * ir.scaling, R.far_world * ir.scaling, a.x, a.y, a.z, b.x, b.y, b.z, tn)) {
+    if (slab(ir.o, ir.inv_d, R.tmin * ir.scaling, R.far_world * ir.scaling, a.x, a.y, a.z, b.x, b.y, b.z, tn, p.box_far_scale)) {
       curr = hit_next;
       if (hit_next == miss_next) {  // a leaf: hit and miss links are the same node
         const uint2 cr = __ldg(reinterpret_cast<const uint2*>(nd + 2));
@@ -309,8 +406,8 @@ __device__ __forceinline__ uint32_t interior_step(const TraceParams& p, RayCtx& 
     const uint2 cc = __ldg(reinterpret_cast<const uint2*>(w + 3));
     if (COUNT) R.node_visits += 2;
     float tn0, tn1;
-    const bool h0 = slab(ir.o, ir.inv_d, near_, far_, w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, tn0);
-    const bool h1 = slab(ir.o, ir.inv_d, near_, far_, w1.z, w1.w, w2.x, w2.y, w2.z, w2.w, tn1);
+    const bool h0 = slab(ir.o, ir.inv_d, near_, far_, w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, tn0, p.box_far_scale);
+    const bool h1 = slab(ir.o, ir.inv_d, near_, far_, w1.z, w1.w, w2.x, w2.y, w2.z, w2.w, tn1, p.box_far_scale);
     if (h0 && h1) {
       const bool second_first = tn1 < tn0;
       push_entry(p, stack, stride, sp, depth, second_first ? cc.x : cc.y, second_first ? tn0 : tn1);
@@ -331,19 +428,19 @@ __device__ __forceinline__ uint32_t interior_step(const TraceParams& p, RayCtx& 
     float t0 = inf, t1 = inf, t2 = inf, t3 = inf;
     uint32_t c0 = EMPTY_SLOT, c1 = EMPTY_SLOT, c2 = EMPTY_SLOT, c3 = EMPTY_SLOT;
     float tn;
-    if (cc.x != EMPTY_SLOT && slab(ir.o, ir.inv_d, near_, far_, lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, tn)) {
+    if (cc.x != EMPTY_SLOT && slab(ir.o, ir.inv_d, near_, far_, lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, tn, p.box_far_scale)) {
       t0 = tn;
       c0 = cc.x;
     }
-    if (cc.y != EMPTY_SLOT && slab(ir.o, ir.inv_d, near_, far_, lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, tn)) {
+    if (cc.y != EMPTY_SLOT && slab(ir.o, ir.inv_d, near_, far_, lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, tn, p.box_far_scale)) {
       t1 = tn;
       c1 = cc.y;
     }
-    if (cc.z != EMPTY_SLOT && slab(ir.o, ir.inv_d, near_, far_, lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, tn)) {
+    if (cc.z != EMPTY_SLOT && slab(ir.o, ir.inv_d, near_, far_, lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, tn, p.box_far_scale)) {
       t2 = tn;
       c2 = cc.z;
     }
-    if (cc.w != EMPTY_SLOT && slab(ir.o, ir.inv_d, near_, far_, lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, tn)) {
+    if (cc.w != EMPTY_SLOT && slab(ir.o, ir.inv_d, near_, far_, lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, tn, p.box_far_scale)) {
       t3 = tn;
       c3 = cc.w;
     }
@@ -378,7 +475,7 @@ __device__ __forceinline__ bool blas_speculative(const TraceParams& p, RayCtx& R
     const float4* nd = reinterpret_cast<const float4*>(p.tri_forest + root_node);
     const float4 a = __ldg(nd), b = __ldg(nd + 1);
     float tn;
-    if (!slab(ir.o, ir.inv_d, R.tmin * ir.scaling, R.far_world * ir.scaling, a.x, a.y, a.z, b.x, b.y, b.z, tn))
+    if (!slab(ir.o, ir.inv_d, R.tmin * ir.scaling, R.far_world * ir.scaling, a.x, a.y, a.z, b.x, b.y, b.z, tn, p.box_far_scale))
       return false;
   }
   uint32_t code = __ldg((WIDTH == 2 ? p.geom_root_code : p.geom_root_code4) + gslot);
@@ -443,7 +540,7 @@ __device__ __forceinline__ void traverse_ray(const TraceParams& p, RayCtx& R, ui
     const float4 a = __ldg(nd), b = __ldg(nd + 1);
     const uint32_t hit_next = __float_as_uint(a.w), miss_next = __float_as_uint(b.w);
     float tn;
-    if (!slab(R.o, R.inv_d, R.tmin * 1.0f, R.far_world * 1.0f, a.x, a.y, a.z, b.x, b.y, b.z, tn)) {
+    if (!slab(R.o, R.inv_d, R.tmin * 1.0f, R.far_world * 1.0f, a.x, a.y, a.z, b.x, b.y, b.z, tn, p.box_far_scale)) {
       curr = miss_next;
       continue;
     }
@@ -454,7 +551,7 @@ __device__ __forceinline__ void traverse_ray(const TraceParams& p, RayCtx& R, ui
       const float4* tb = reinterpret_cast<const float4*>(p.tlas_bounding + ti);
       const float4 ba = __ldg(tb), bb = __ldg(tb + 1);
       float tn2;
-      if (!slab(R.o, R.inv_d, R.tmin, R.tmax, ba.x, ba.y, ba.z, bb.x, bb.y, bb.z, tn2)) continue;
+      if (!slab(R.o, R.inv_d, R.tmin, R.tmax, ba.x, ba.y, ba.z, bb.x, bb.y, bb.z, tn2, p.box_far_scale)) continue;
       if ((R.cull_mask & __float_as_uint(ba.w)) == 0) continue;
       const DeviceInstance* inst = p.tlas_data + ti;
       const InstanceRay ir = to_instance(inst, R.o, R.d, R.ray_flags);
@@ -549,7 +646,7 @@ struct LaneWalk {
           const float4 a = __ldg(nd), b = __ldg(nd + 1);
           const uint32_t hit_next = __float_as_uint(a.w), miss_next = __float_as_uint(b.w);
           float tn;
-          if (!slab(R.o, R.inv_d, R.tmin * 1.0f, R.far_world * 1.0f, a.x, a.y, a.z, b.x, b.y, b.z, tn)) {
+          if (!slab(R.o, R.inv_d, R.tmin * 1.0f, R.far_world * 1.0f, a.x, a.y, a.z, b.x, b.y, b.z, tn, p.box_far_scale)) {
             tcur = miss_next;
             continue;
           }
@@ -569,7 +666,7 @@ struct LaneWalk {
           const float4* tb = reinterpret_cast<const float4*>(p.tlas_bounding + cur);
           const float4 ba = __ldg(tb), bb = __ldg(tb + 1);
           float tn2;
-          if (!slab(R.o, R.inv_d, R.tmin, R.tmax, ba.x, ba.y, ba.z, bb.x, bb.y, bb.z, tn2)) continue;
+          if (!slab(R.o, R.inv_d, R.tmin, R.tmax, ba.x, ba.y, ba.z, bb.x, bb.y, bb.z, tn2, p.box_far_scale)) continue;
           if ((R.cull_mask & __float_as_uint(ba.w)) == 0) continue;
           const DeviceInstance* inst = p.tlas_data + cur;
           ir = to_instance(inst, R.o, R.d, R.ray_flags);
@@ -594,7 +691,7 @@ struct LaneWalk {
           const float4* nd = reinterpret_cast<const float4*>(p.tri_forest + gm.x);
           const float4 a = __ldg(nd), b = __ldg(nd + 1);
           float tn;
-          if (!slab(ir.o, ir.inv_d, R.tmin * ir.scaling, R.far_world * ir.scaling, a.x, a.y, a.z, b.x, b.y, b.z, tn))
+          if (!slab(ir.o, ir.inv_d, R.tmin * ir.scaling, R.far_world * ir.scaling, a.x, a.y, a.z, b.x, b.y, b.z, tn, p.box_far_scale))
             continue;
           code = __ldg((WIDTH == 2 ? p.geom_root_code : p.geom_root_code4) + cur);
           code_tn = -inf;

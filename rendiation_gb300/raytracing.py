@@ -40,6 +40,9 @@ MISS = 0xFFFFFFFF
 TRAVERSAL_ORDERED = 0
 TRAVERSAL_REFERENCE = 1
 TRAVERSAL_ORDERED_WIDE = 2
+# OR-ed into a traversal value: the watertight triangle test (Woop, Benthin and
+# Wald 2013) instead of the reference's formula (geometry/mod.rs:105-155)
+INTERSECT_WATERTIGHT = 0x100
 SORT_NONE = 0
 SORT_SCENE_OCTANT = 1
 SORT_SCENE_OCTANT_CELL = 2

@@ -135,3 +135,42 @@ def classify(got, expect, oracle_sys=None, rays=None):
     return {"n": int(got.shape[0]), "identical": int(identical.sum()), "ties": int(tie.sum()),
             "other": int(other.sum()), "other_idx": np.nonzero(other)[0][:20].tolist(),
             "hit_mismatch": int((g_hit != e_hit).sum())}
+
+
+def tilted_grid(g: int = 33) -> scenes.Mesh:
+    """A g x g vertex grid on the tilted plane z = 0.3x + 0.2y over [0,1]^2, two
+    triangles per cell, consistently wound: every interior edge is shared by
+    two triangles that continue the same surface."""
+    xs = np.linspace(0.0, 1.0, g, dtype=np.float32)
+    X, Y = np.meshgrid(xs, xs, indexing="xy")
+    Z = (np.float32(0.3) * X + np.float32(0.2) * Y).astype(np.float32)
+    pos = np.stack([X, Y, Z], -1).reshape(-1, 3).astype(np.float32)
+    q = []
+    for j in range(g - 1):
+        for i in range(g - 1):
+            a = j * g + i
+            q += [a, a + 1, a + g + 1, a, a + g + 1, a + g]
+    return scenes.Mesh(pos, np.array(q, np.uint32))
+
+
+def edge_rays(mesh: scenes.Mesh, n: int, seed: int, margin: float = 1e-3, vertex_share: float = 0.1) -> np.ndarray:
+    """Rays aimed (in FP64) at points on triangle edges of `mesh` (a share of
+    them exactly at vertices), from the front side of a surface facing +z,
+    keeping only points at least `margin` inside [0,1]^2 (away from the mesh's
+    outer boundary)."""
+    rng = np.random.default_rng(seed)
+    pos = mesh.positions.reshape(-1, 3)
+    t3 = mesh.indices.reshape(-1, 3)
+    tri = rng.integers(0, t3.shape[0], n)
+    k = rng.integers(0, 3, n)
+    a = pos[t3[tri, k]].astype(np.float64)
+    b = pos[t3[tri, (k + 1) % 3]].astype(np.float64)
+    s = rng.random(n) * 0.98 + 0.01
+    s[: int(n * vertex_share)] = 0.0
+    p = a + (b - a) * s[:, None]
+    inner = (p[:, 0] > margin) & (p[:, 0] < 1 - margin) & (p[:, 1] > margin) & (p[:, 1] < 1 - margin)
+    p = p[inner]
+    d = rng.normal(size=(p.shape[0], 3))
+    d[:, 2] = -np.abs(d[:, 2]) - 0.5
+    d /= np.linalg.norm(d, axis=1)[:, None]
+    return scenes.make_rays((p - 1.5 * d).astype(np.float32), d.astype(np.float32))
