@@ -137,15 +137,43 @@ def measured_peak_gbs():
     return 6800.0, "fallback"
 
 
-def traffic_from_profile(workload: str, kernel: str):
-    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary, if any."""
+def profile_entry(workload: str, kernel: str) -> dict:
+    """The committed ncu figures of one kernel (profiles/traffic.json), or {}."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
     if not os.path.exists(p):
-        return None
+        return {}
     with open(p) as f:
-        d = json.load(f)
-    e = d.get(workload, {}).get(kernel)
-    return None if e is None else float(e["dram_bytes_per_launch"])
+        return json.load(f).get(workload, {}).get(kernel, {})
+
+
+def traffic_from_profile(workload: str, kernel: str):
+    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary, if any."""
+    e = profile_entry(workload, kernel)
+    return float(e["dram_bytes_per_launch"]) if "dram_bytes_per_launch" in e else None
+
+
+def measured_limits(workload: str, kernel: str, kernel_ms: float, peak_gbs: float, clocks: dict) -> dict:
+    """What the counters of the committed ncu capture say bounds the kernel:
+    dram_frac = measured DRAM bytes per launch over the live launch time, against
+    the measured HBM peak; issue_frac = warp instructions per launch against the
+    issue capacity of the launch (152 SMs x 4 schedulers x one instruction per
+    clock at the sampled median SM clock); simt = threads per warp instruction."""
+    e = profile_entry(workload, kernel)
+    if not e:
+        return {}
+    out = {}
+    if "dram_bytes_per_launch" in e:
+        out["dram_frac"] = round(e["dram_bytes_per_launch"] / (kernel_ms / 1e3) / 1e9 / peak_gbs, 4)
+    mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 2070.0
+    if "warp_instructions_per_launch" in e:
+        cap = 152 * 4 * float(mhz) * 1e6 * (kernel_ms / 1e3)
+        out["issue_frac"] = round(e["warp_instructions_per_launch"] / cap, 4)
+    if "threads_per_warp_instruction" in e:
+        out["simt_lanes_per_warp_instruction"] = e["threads_per_warp_instruction"]
+        out["limiter"] = (f"instruction issue with divergent lanes: {e['threads_per_warp_instruction']} of 32 lanes "
+                          f"per warp instruction, issue active {round(100 * e['issue_active'], 1)} %, DRAM "
+                          f"{e.get('dram_throughput_pct', '?')} % of peak (ncu, {e.get('source', 'profiles/')})")
+    return out
 
 
 # --------------------------------------------------------------------------- workloads
@@ -373,6 +401,9 @@ def bench_wavefront(args, ws, rank):
             "peak": peak,
             "unit": "GB/s",
             "frac": round(achieved / peak, 4),
+            "achieved_basis": ("algorithmic: per ray the reference order's node (48 B) and triangle (36 B) fetches "
+                               "plus ray and hit, over the launch; the ordered walk does that work with far fewer "
+                               "fetches, so frac can exceed 1 and does not measure bandwidth use"),
             "traffic": traffic_from_profile("wavefront", dom_name.split()[0]),
             "kernel": dom_name,
             "kernel_ms": round(dom_ms, 4),
@@ -382,11 +413,217 @@ def bench_wavefront(args, ws, rank):
                               "shadow": round(node_bytes_per_ray(c_sh, max(1, n_sh)), 1),
                               "bounce": round(node_bytes_per_ray(c_bo, max(1, n_bo)), 1)},
             "peak_kind": peak_kind,
+            **measured_limits("wavefront", dom_name.split()[0], dom_ms, peak, clk.summary()),
         },
         "clocks": clk.summary(),
         "build": build,
     }
-    return out, P, mesh, cam
+    return out, P, mesh, cam, wf
+
+
+def watertight_twin(P, wf, cam):
+    """A frame with wf's launch knobs and the watertight triangle test."""
+    from rendiation_gb300 import raytracing as rt
+
+    wt = rt.Wavefront(P, cam, LIGHT)
+    if wf.phase_config is not None:
+        (p1, p2) = wf.phase_config
+        wt.configure((p1[0] | rt.INTERSECT_WATERTIGHT,) + tuple(p1[1:]),
+                     (p2[0] | rt.INTERSECT_WATERTIGHT,) + tuple(p2[1:]), refill=wf.desc.refill)
+    else:
+        same = (wf.desc.traversal | rt.INTERSECT_WATERTIGHT, wf.desc.block_size, wf.desc.local_stack,
+                wf.desc.register_tier, wf.desc.speculation)
+        wt.configure(same, same, refill=wf.desc.refill)
+    return wt
+
+
+def parity_report(P, S_field, wf, cam, threads: int) -> dict:
+    """Parity of the timed configuration with the oracle (the CPU restatement
+    of the reference's path), every ray classified (oracle.parity): identical,
+    exact-distance tie, NaN-exposed, edge, other; `other` must be 0.
+      frame      the whole 1920x1080 frame of the wavefront leg with the
+                 autotuned knobs it was timed with, against the oracle's
+                 pipeline over the same frame;
+      soup10k    the plain closest-hit configuration: 10,000-triangle soup,
+                 256x256 pinhole rays, rdn_trace with the cfg0 leg's knobs;
+      watertight the frame's primary rays traced with the watertight test,
+                 against the reference's formula (near ties and edge cases
+                 only), and the watertight frame against the oracle's
+                 watertight pipeline."""
+    import torch
+
+    from oracle import orc
+    from oracle import parity
+    from rendiation_gb300 import raytracing as rt
+    from rendiation_gb300 import scenes
+
+    W, H = cam.width, cam.height
+    out = {}
+    sample = 77
+    wf.run(sample)
+    torch.cuda.synchronize()
+    got = wf.results()
+    t0 = time.perf_counter()
+    exp, _, sec = orc.wavefront_shadow_bounce(S_field, cam.as_floats(), W, H, LIGHT, sample, threads=threads)
+    out["frame"] = parity.classify_wavefront(S_field, cam, W, H, LIGHT, got, exp, sample, threads=threads)
+    out["frame"]["oracle_seconds"] = round(sec, 3)
+
+    # the plain closest-hit configuration
+    soup = scenes.triangle_soup(10_000, seed=0)
+    Ps = rt.AccelerationStructureSystem(device=0)
+    b = Ps.create_bottom_level_acceleration_structure([rt.BottomLevelAccelerationStructureBuildSource(soup.positions)])
+    Ps.bind_tlas([Ps.create_top_level_acceleration_structure([rt.TopLevelAccelerationStructureSourceInstance(b)])])
+    Ps.build(blas_bin_size=4, device_build=True)
+    Ss = orc.OracleSystem()
+    sb = Ss.create_blas([(soup.positions, None, 1)])
+    Ss.bind_tlas([Ss.create_tlas([{"blas": sb}])])
+    Ss.build(blas_bin_size=4)
+    srays = scenes.pinhole_rays(scenes.soup_camera())
+    d = torch.from_numpy(srays.view(np.float32).reshape(-1, 8).copy()).cuda()
+    hits = torch.empty((srays.shape[0], 4), device="cuda")
+    ext = torch.empty((srays.shape[0], 4), dtype=torch.int32, device="cuda")
+    Ps.trace(d, hits, ext, traversal=rt.TRAVERSAL_ORDERED_WIDE, local_stack=1)
+    torch.cuda.synchronize()
+    e_soup, _ = Ss.trace(srays, threads=threads)
+    _, out["soup10k"] = parity.classify_trace(Ss, srays, rt.hits_to_numpy(hits), ext.cpu().numpy().view(np.uint32),
+                                              e_soup, exact=True, threads=threads)
+    Ps.close()
+
+    # the watertight test against the reference's formula, on the frame's primary rays
+    prim = scenes.pinhole_rays(cam)
+    dp = torch.from_numpy(prim.view(np.float32).reshape(-1, 8).copy()).cuda()
+    hp = torch.empty((prim.shape[0], 4), device="cuda")
+    xp = torch.empty((prim.shape[0], 4), dtype=torch.int32, device="cuda")
+    P.trace(dp, hp, xp, traversal=rt.TRAVERSAL_ORDERED_WIDE | rt.INTERSECT_WATERTIGHT, local_stack=1)
+    torch.cuda.synchronize()
+    e_ref, _ = S_field.trace(prim, threads=threads)
+    g_wt = rt.hits_to_numpy(hp)
+    _, c = parity.classify_trace(S_field, prim, g_wt, xp.cpu().numpy().view(np.uint32), e_ref, exact=False,
+                                 threads=threads)
+    c["hits_reference_formula"] = int((e_ref["prim"] != orc.MISS).sum())
+    c["hits_watertight"] = int((g_wt["prim"] != orc.MISS).sum())
+    same = (g_wt["prim"] == e_ref["prim"]) & (e_ref["prim"] != orc.MISS)
+    c["max_rel_t_difference_same_triangle"] = float(np.max(np.abs(g_wt["t"][same].astype(np.float64) - e_ref["t"][same])
+                                                           / e_ref["t"][same])) if same.any() else 0.0
+    out["watertight_primaries_vs_reference_formula"] = c
+    # the watertight frame against the oracle's watertight pipeline
+    wt_frame = watertight_twin(P, wf, cam)
+    wt_frame.run(sample)
+    torch.cuda.synchronize()
+    exp_wt, _, _ = orc.wavefront_shadow_bounce(S_field, cam.as_floats(), W, H, LIGHT, sample, threads=threads,
+                                               watertight=True)
+    out["watertight_frame"] = parity.classify_wavefront(S_field, cam, W, H, LIGHT, wt_frame.results(), exp_wt, sample,
+                                                        watertight=True, threads=threads)
+    out["other_total"] = (out["frame"]["other"] + out["soup10k"]["other"]
+                          + out["watertight_primaries_vs_reference_formula"]["other"]
+                          + out["watertight_frame"]["other"])
+    out["seconds"] = round(time.perf_counter() - t0, 2)
+    out["threads"] = threads
+    return out
+
+
+def bench_watertight(args, P, wf, cam) -> dict:
+    """The wavefront frame with the watertight triangle test (same tuned knobs,
+    RDN_INTERSECT_WATERTIGHT OR-ed into both kernels' traversal), device-timed
+    like the main leg, against the reference's formula."""
+    import torch
+
+    from rendiation_gb300 import raytracing as rt
+
+    wt = watertight_twin(P, wf, cam)
+    stream = torch.cuda.current_stream()
+    res = {}
+    for name, frame in (("reference_formula", wf), ("watertight", wt)):
+        for s in range(args.warmup):
+            frame.run(500 + s)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = max(5, min(args.steps, 20))
+        e0.record(stream)
+        for s in range(reps):
+            frame.run(600 + s)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        rays = sum(frame.rays_traced())
+        res[name] = {"frame_ms": round(ms, 4), "mrays": round(rays / (ms / 1e3) / 1e6, 2), "rays_per_frame": rays}
+    res["watertight_over_reference_formula_time"] = round(res["watertight"]["frame_ms"]
+                                                          / res["reference_formula"]["frame_ms"], 4)
+    return res
+
+
+def bench_plain_soup(args) -> dict:
+    """The plain closest-hit configuration: 10,000-triangle soup (seeded;
+    centroids U[0,1]^3, vertex offsets U[-0.02,0.02]^3), SAH <= 4 per leaf,
+    256x256 pinhole rays from (0.5,0.5,-1.5) along +z, 60 degree vertical field
+    of view; rdn_trace per step. The structure (about 1.3 MB) is L2-resident, so
+    the bound is L2, not HBM: `l2_gbs` is the algorithmic bytes (reference-order
+    node and triangle fetches, rays and hits) over the device time. e2e: the
+    same query through the C ABI from pinned host rays to pinned host hits."""
+    import torch
+
+    from rendiation_gb300 import raytracing as rt
+    from rendiation_gb300 import scenes
+
+    soup = scenes.triangle_soup(10_000, seed=0)
+    P = rt.AccelerationStructureSystem(device=0)
+    b = P.create_bottom_level_acceleration_structure([rt.BottomLevelAccelerationStructureBuildSource(soup.positions)])
+    P.bind_tlas([P.create_top_level_acceleration_structure([rt.TopLevelAccelerationStructureSourceInstance(b)])])
+    P.build(blas_bin_size=4, device_build=True)
+    rays = scenes.pinhole_rays(scenes.soup_camera())
+    n = rays.shape[0]
+    d = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).cuda()
+    hits = torch.empty((n, 4), device="cuda")
+    stream = torch.cuda.current_stream()
+    cands = [(trav, block, local) for trav in (rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_WIDE)
+             for block in (32, 64, 128) for local in (0, 1)]
+
+    def time_ms(trav, block, local, reps=200):
+        for _ in range(5):
+            P.trace(d, hits, traversal=trav, block_size=block, local_stack=local)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            P.trace(d, hits, traversal=trav, block_size=block, local_stack=local)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    timings = {c: time_ms(*c, reps=50) for c in cands}
+    best = min(timings, key=timings.get)
+    ms = time_ms(*best, reps=max(200, args.steps * 10))
+    c_ref = P.trace_counted(d, hits, traversal=rt.TRAVERSAL_REFERENCE)
+    alg_bytes = n * node_bytes_per_ray(c_ref, n)
+    # e2e: pinned host rays in, pinned host hits out, every step
+    h_rays = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).pin_memory()
+    h_hits = torch.empty((n, 4), dtype=torch.float32).pin_memory()
+    for _ in range(5):
+        d.copy_(h_rays, non_blocking=True)
+        P.trace(d, hits, traversal=best[0], block_size=best[1], local_stack=best[2])
+        h_hits.copy_(hits, non_blocking=True)
+    torch.cuda.synchronize()
+    steps = max(50, args.steps)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        d.copy_(h_rays, non_blocking=True)
+        P.trace(d, hits, traversal=best[0], block_size=best[1], local_stack=best[2])
+        h_hits.copy_(hits, non_blocking=True)
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / steps
+    P.close()
+    return {
+        "workload": "soup 10,000 tris, 256x256 pinhole primaries, rdn_trace closest hit",
+        "knobs": {"traversal": best[0], "block": best[1], "local_stack": best[2]},
+        "device_ms": round(ms, 5),
+        "mrays": round(n / (ms / 1e3) / 1e6, 2),
+        "algorithmic_bytes_per_launch": int(alg_bytes),
+        "bytes_per_ray": round(node_bytes_per_ray(c_ref, n), 1),
+        "l2_gbs": round(alg_bytes / (ms / 1e3) / 1e9, 1),
+        "bound": "L2 (structure about 1.3 MB, L2-resident)",
+        "hbm_frac_algorithmic": round(alg_bytes / (ms / 1e3) / 1e9 / measured_peak_gbs()[0], 4),
+        "e2e": {"mrays": round(n / e2e_s / 1e6, 2), "ms": round(e2e_s * 1e3, 4), "h2d_bytes_per_step": n * 32,
+                "d2h_bytes_per_step": n * 16},
+    }
 
 
 def compare_builds(P, bin_size=4) -> dict:
@@ -721,17 +958,24 @@ def bench_batched(args):
     batched_ms = e0.elapsed_time(e1) / reps
     res_batched = batched.results()
 
-    # plain per-scene loop: the same executor, one scene per call
+    # plain per-scene loop: the same executor, one scene per call, with the
+    # launch knobs the batched graph was tuned to (node width, block, stack
+    # placement, leaf postponement, secondary schedule, sort key)
     L = native.lib()
     max_n = int(np.max(np.diff(b.ray_offsets)))
+    knobs = batched.desc
     size = C.c_size_t()
-    L.rdn_paths_scratch_size(max_n, 4, 0, C.byref(size))
+    L.rdn_paths_scratch_size(max_n, 4, knobs.sort_key, C.byref(size))
     scratch = torch.empty(size.value + 256, dtype=torch.uint8, device="cuda")
     sptr = (scratch.data_ptr() + 255) & ~255
     out = torch.empty((b.rays.shape[0], 2), dtype=torch.float32, device="cuda")
     desc = native.PathDesc()
     desc.max_bounces, desc.rr_start, desc.albedo, desc.rr_survive, desc.seed = 4, 2, 0.5, 0.5, 1
-    desc.traversal, desc.scratch, desc.scratch_bytes = traversal, sptr, size.value
+    desc.traversal, desc.scratch, desc.scratch_bytes = knobs.traversal, sptr, size.value
+    desc.block_size, desc.sort_key, desc.refill = knobs.block_size, knobs.sort_key, knobs.refill
+    desc.local_stack, desc.speculation = knobs.local_stack, knobs.speculation
+    plain_knobs = {"traversal": int(desc.traversal), "block": int(desc.block_size), "sort_key": int(desc.sort_key),
+                   "refill": int(desc.refill), "local": int(desc.local_stack), "spec": int(desc.speculation)}
 
     def plain_loop():
         for sidx in range(len(b.meshes)):
@@ -765,6 +1009,7 @@ def bench_batched(args):
         "plain_loop_mrays": round(total / (plain_ms / 1e3) / 1e6, 2),
         "plain_loop_ms": round(plain_ms, 3),
         "speedup_vs_plain_loop": round(plain_ms / batched_ms, 3),
+        "plain_loop_knobs": plain_knobs,
         "build": build,
         "escaped_fraction": round(float(np.mean(res_batched["depth_flags"] >> 31)), 4),
         "autotuned": tuned,
@@ -872,11 +1117,118 @@ def bench_adjoint(args):
     out["fwd_adjoint_over_fwd"] = round(out["forward_adjoint_ms"] / out["forward_ms"], 3)
     out["fwd_adjoint_retrace_over_fwd"] = round(out["forward_adjoint_retrace_ms"] / out["forward_ms"], 3)
     out["adjoint"] = "from the forward's recorded hits (8 B per ray); _retrace: hits traced again"
+    # gradient error at this configuration: one forward (recording the hits) and one adjoint
+    loss.zero_()
+    grad.zero_()
+    assert L.rdn_attr_loss_forward(P._h, C.byref(fwd_rec), sp) == 0
+    assert L.rdn_attr_loss_adjoint(P._h, C.byref(adj_rec), sp) == 0
+    torch.cuda.synchronize()
+    out["gradient_error"] = attr_loss_gradient_error(
+        mesh, attr.cpu().numpy(), scenes.pinhole_rays(cam), target.cpu().numpy(),
+        hit_tri.cpu().numpy().view(np.uint32), grad.cpu().numpy())
     out["local_stack"], out["speculation"] = local, spec
     out["loss"] = float(loss.item())
     out["workload"] = f"heightfield {n_grid}^2 ({mesh.triangle_count} tris), {res}x{res} rays, attribute loss"
     P.close()
     return out
+
+
+def attr_loss_gradient_error(mesh, attr, rays, targets, tri, grad, n_vertices=64, seed=23):
+    """Gradient error of the attribute loss at frozen visibility against FP64:
+    (1) the FP64 analytic gradient over every vertex some ray sees; (2) FP64
+    central differences on `n_vertices` random seen vertices (positions and
+    attribute), plain with h = 1e-4 as the configuration states, and
+    Richardson-extrapolated from h and h/2; (3) for every vertex whose plain
+    h = 1e-4 difference is off by more than 1e-3, the central difference at
+    h = 1e-4 .. 1e-7, showing it converge to the kernel's gradient (grazing rays
+    make u, v strongly nonlinear in the vertex positions, so the truncation
+    error of the h = 1e-4 difference is what disagrees)."""
+    idx = mesh.indices.reshape(-1, 3)
+    hit = tri != 0xFFFFFFFF
+    r = rays[hit]
+    tv = idx[tri[hit]]
+    tg = targets[hit].astype(np.float64)
+    pos = mesh.positions.astype(np.float64)
+    a = attr.astype(np.float64)
+    o = r["org"].astype(np.float64)
+    d = r["dir"].astype(np.float64)
+
+    def solve(p_, sel):
+        v = p_[tv[sel]]
+        M = np.stack([-d[sel], v[:, 1] - v[:, 0], v[:, 2] - v[:, 0]], axis=2)
+        x = np.linalg.solve(M, (o[sel] - v[:, 0])[..., None])[..., 0]
+        return x, M
+
+    def loss(p_, a_, sel):
+        x, _ = solve(p_, sel)
+        u, v = x[:, 1], x[:, 2]
+        t = tv[sel]
+        val = (1 - u - v) * a_[t[:, 0]] + u * a_[t[:, 1]] + v * a_[t[:, 2]]
+        return float(np.sum((val - tg[sel]) ** 2))
+
+    allr = np.arange(r.shape[0])
+    x, M = solve(pos, allr)
+    u, v = x[:, 1], x[:, 2]
+    val = (1 - u - v) * a[tv[:, 0]] + u * a[tv[:, 1]] + v * a[tv[:, 2]]
+    res = 2 * (val - tg)
+    G = np.stack([np.zeros_like(res), res * (a[tv[:, 1]] - a[tv[:, 0]]), res * (a[tv[:, 2]] - a[tv[:, 0]])], 1)
+    lam = np.linalg.solve(np.transpose(M, (0, 2, 1)), G[..., None])[..., 0]
+    ga, gp = np.zeros(a.shape[0]), np.zeros((a.shape[0], 3))
+    for k, wk in enumerate([1 - u - v, u, v]):
+        np.add.at(ga, tv[:, k], res * wk)
+        np.add.at(gp, tv[:, k], -wk[:, None] * lam)
+    g_pos, g_attr = grad[:, :3].astype(np.float64), grad[:, 3].astype(np.float64)
+    seen = np.unique(tv.reshape(-1))
+    norm_p = np.linalg.norm(gp[seen], axis=1)
+    floor_p = 1e-2 * np.median(norm_p[norm_p > 0])
+    floor_a = 1e-2 * np.median(np.abs(ga[seen][ga[seen] != 0]))
+    rel_p = np.linalg.norm(g_pos[seen] - gp[seen], axis=1) / np.maximum(norm_p, floor_p)
+    rel_a = np.abs(g_attr[seen] - ga[seen]) / np.maximum(np.abs(ga[seen]), floor_a)
+
+    rng = np.random.default_rng(seed)
+    pick = rng.choice(seen, size=min(n_vertices, seen.size), replace=False)
+
+    def central(vi, c, hh, sel):
+        if c < 3:
+            pp, pm = pos.copy(), pos.copy()
+            pp[vi, c] += hh
+            pm[vi, c] -= hh
+            return (loss(pp, a, sel) - loss(pm, a, sel)) / (2 * hh)
+        ap, am = a.copy(), a.copy()
+        ap[vi] += hh
+        am[vi] -= hh
+        return (loss(pos, ap, sel) - loss(pos, am, sel)) / (2 * hh)
+
+    plain, rich, conv = [], [], []
+    for vi in pick:
+        sel = np.nonzero(np.any(tv == vi, axis=1))[0]
+        got = np.array([*g_pos[vi], g_attr[vi]])
+        fd1 = np.array([central(vi, c, 1e-4, sel) for c in range(4)])
+        fd2 = np.array([central(vi, c, 5e-5, sel) for c in range(4)])
+        ri = (4 * fd2 - fd1) / 3
+        den = max(np.linalg.norm(ri[:3]), floor_p)
+        e_plain = np.linalg.norm(got[:3] - fd1[:3]) / den
+        e_rich = np.linalg.norm(got[:3] - ri[:3]) / den
+        e_attr = abs(got[3] - ri[3]) / max(abs(ri[3]), floor_a)
+        plain.append(float(e_plain))
+        rich.append(float(max(e_rich, e_attr)))
+        if e_plain > 1e-3:
+            series = {}
+            for hh in (1e-4, 1e-5, 1e-6, 1e-7):
+                f = np.array([central(vi, c, hh, sel) for c in range(3)])
+                series[f"{hh:.0e}"] = float(np.linalg.norm(got[:3] - f) / den)
+            conv.append({"vertex": int(vi), "rays": int(sel.size), "rel_error_by_h": series})
+    return {
+        "vertices_seen": int(seen.size),
+        "max_rel_vs_fp64_analytic_positions": float(rel_p.max()),
+        "max_rel_vs_fp64_analytic_attributes": float(rel_a.max()),
+        "fd_vertices": int(len(pick)),
+        "max_rel_vs_fp64_fd_h1e-4": float(max(plain)),
+        "median_rel_vs_fp64_fd_h1e-4": float(np.median(plain)),
+        "vertices_within_1e-3_of_fd_h1e-4": int(sum(e <= 1e-3 for e in plain)),
+        "max_rel_vs_fp64_fd_richardson": float(max(rich)),
+        "fd_convergence_of_vertices_over_1e-3": conv,
+    }
 
 
 def bench_batched_adjoint(args):
@@ -950,6 +1302,8 @@ def bench_batched_adjoint(args):
     as_bytes = P.device_bytes()
     loss = torch.zeros(1, dtype=torch.float64, device="cuda")
     grad = torch.zeros((nv, 4), device="cuda")
+    # device memory of the configuration's own form (hits recomputed in the backward, no tape)
+    peak_recompute = int(torch.cuda.max_memory_allocated() + as_bytes)
     # the forward's record of every segment (triangle, instance, ray): 40 B per segment
     tape_tri = torch.zeros(n * seg, dtype=torch.int32, device="cuda")
     tape_inst = torch.zeros(n * seg, dtype=torch.int32, device="cuda")
@@ -1021,6 +1375,13 @@ def bench_batched_adjoint(args):
     out["adjoint"] = ("from the forward's record of every segment (triangle, instance, ray; 40 B per segment), "
                       "one graph for forward + adjoint; _retrace: the adjoint traces the paths again")
     out["peak_hbm_bytes"] = int(torch.cuda.max_memory_allocated() + as_bytes)
+    # the configuration asks for hits recomputed in the backward pass, not stored per bounce
+    out["config_conforming"] = {
+        "form": "hits recomputed by tracing the paths again in the adjoint (no tape)",
+        "fwd_adjoint_over_fwd": out["fwd_adjoint_retrace_over_fwd"],
+        "forward_adjoint_mrays": out["forward_adjoint_retrace_mrays"],
+        "peak_hbm_bytes": peak_recompute,
+    }
     out["workload"] = (f"{n_scenes} heightfields {int(grids.min())}^2..{int(grids.max())}^2 "
                        f"({sum(m.triangle_count for m in meshes)} tris), {n} primaries, 2 bounces")
     out["gradient_error"] = batched_gradient_error(P, meshes, rays, tidx, attr, targets, seg)
@@ -1225,6 +1586,35 @@ def run_reference(args, ws, rank):
     }
 
 
+def headline(out: dict) -> dict:
+    """The metric's three figures in one place: the plain wavefront Mrays/s,
+    batched against the plain per-scene loop, forward + adjoint against forward
+    (the configuration's own form: hits recomputed in the backward), each at its
+    stated FP64 error and oracle parity."""
+    h = {"wavefront_mrays": out.get("value"), "wavefront_e2e_mrays": out.get("e2e", {}).get("value")}
+    if "batched" in out:
+        h["batched_over_plain_loop"] = out["batched"]["speedup_vs_plain_loop"]
+        h["batched_graph_mrays"] = out["batched"]["batched_graph_mrays"]
+    if "batched_adjoint" in out:
+        cc = out["batched_adjoint"].get("config_conforming", {})
+        h["fwd_adjoint_over_fwd_recompute"] = cc.get("fwd_adjoint_over_fwd")
+        h["fwd_adjoint_over_fwd_tape"] = out["batched_adjoint"].get("fwd_adjoint_over_fwd")
+    if "adjoint" in out and "gradient_error" in out["adjoint"]:
+        ge = out["adjoint"]["gradient_error"]
+        h["gradient_max_rel_vs_fp64_fd_h1e-4"] = ge["max_rel_vs_fp64_fd_h1e-4"]
+        h["gradient_max_rel_vs_fp64_fd_richardson"] = ge["max_rel_vs_fp64_fd_richardson"]
+        h["gradient_max_rel_vs_fp64_analytic"] = ge["max_rel_vs_fp64_analytic_positions"]
+    if "accuracy_vs_fp64" in out:
+        h["t_max_rel_error_vs_fp64"] = out["accuracy_vs_fp64"]["max_rel_t_error_vs_fp64_same_triangle"]
+    if "parity" in out:
+        fr = out["parity"]["frame"]
+        h["parity_other"] = out["parity"]["other_total"]
+        h["parity_frame_ties"] = {"primary": fr["primary"]["tie"], "bounce": fr["bounce"]["tie"]}
+        h["parity_frame_nan_exposed"] = {"primary": fr["primary"]["nan"], "shadow": fr["shadow"]["nan"],
+                                         "bounce": fr["bounce"]["nan"]}
+    return h
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1247,6 +1637,9 @@ def main():
     ap.add_argument("--no-ao", action="store_true", help="skip the ambient-occlusion leg")
     ap.add_argument("--no-task-graph", action="store_true", help="skip the task-graph throughput leg")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP32-vs-FP64 accuracy check")
+    ap.add_argument("--no-parity", action="store_true", help="skip the oracle parity report")
+    ap.add_argument("--no-watertight", action="store_true", help="skip the watertight-test frame timing")
+    ap.add_argument("--no-plain-soup", action="store_true", help="skip the plain 10k-soup closest-hit leg")
     ap.add_argument("--diff-scenes", type=int, default=64)
     ap.add_argument("--scenes", type=int, default=256)
     ap.add_argument("--batched-steps", type=int, default=5)
@@ -1265,11 +1658,18 @@ def main():
     torch.cuda.set_device(local)
     if ws > 1:
         torch.distributed.init_process_group("nccl")
-    out, P, mesh, cam = bench_wavefront(args, ws, rank)
-    # the oracle's copy of the heightfield (CPU), for the accuracy check and the CPU baseline
-    S_field = oracle_heightfield(mesh) if rank == 0 and not (args.no_accuracy and args.no_cpu_baseline) else None
+    out, P, mesh, cam, wf = bench_wavefront(args, ws, rank)
+    # the oracle's copy of the heightfield (CPU), for the accuracy and parity checks and the CPU baseline
+    need_oracle = not (args.no_accuracy and args.no_cpu_baseline and args.no_parity)
+    S_field = oracle_heightfield(mesh) if rank == 0 and need_oracle else None
     if S_field is not None and not args.no_accuracy:
         out["accuracy_vs_fp64"] = accuracy_vs_fp64(P, S_field, cam)
+    if not args.no_watertight:
+        out["watertight"] = bench_watertight(args, P, wf, cam)
+    if S_field is not None and not args.no_parity:
+        out["parity"] = parity_report(P, S_field, wf, cam, os.cpu_count() or 1)
+    if not args.no_plain_soup:
+        out["plain_soup10k"] = bench_plain_soup(args)
     if not args.no_ao:
         out["ao"] = bench_ao(args, P, S_field if not args.no_cpu_baseline else None)
     if not args.no_task_graph:
@@ -1285,6 +1685,7 @@ def main():
         if not args.no_cpu_baseline:
             cb, _ = cpu_baseline_wavefront(S_field, cam, os.cpu_count() or 1, budget_s=args.cpu_budget)
             out["cpu_baseline"] = cb
+        out["headline"] = headline(out)
         print(json.dumps(out), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()

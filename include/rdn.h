@@ -172,12 +172,15 @@ typedef struct rdn_hit_ext {
  * triangle (or a ray in a triangle's plane) gives t = NaN, which the
  * reference accepts as a hit.
  * RDN_INTERSECT_WATERTIGHT: the watertight f32 test of Woop, Benthin and Wald
- * (JCGT 2013) on the shared vertex values: no ray passes between two
- * triangles that share an edge, a NaN distance never hits, facing and culling
- * follow the reference's rules. Hit/miss and primitive ids differ from the
- * reference's only for rays at an exact distance tie, rays near a triangle
- * edge, and rays the reference gives a NaN distance; t and the barycentrics
- * are this test's own f32 values, not the reference's. */
+ * (JCGT 2013) on the shared vertex values, with box tests made conservative
+ * against rounding (exit distance times 1 + 2 gamma_3, Ize, JCGT 2013): no ray
+ * passes between two triangles that share an edge, a NaN distance never hits,
+ * facing and culling follow the reference's rules. One case keeps the
+ * reference box test's NaN rule: a ray with an exactly zero direction
+ * component that lies exactly in a box's face plane skips that box. Hit/miss
+ * and primitive ids differ from the reference's only for rays at an
+ * equal-distance tie, rays near a triangle edge, and rays the reference gives
+ * a NaN distance; t and the barycentrics are this test's own f32 values. */
 #define RDN_INTERSECT_WATERTIGHT 0x100u
 
 /* Fixed any-hit policies for non-opaque geometry, standing in for a user
@@ -468,6 +471,45 @@ rdn_status rdn_attr_loss_forward(rdn_ctx* ctx, const rdn_attr_loss_desc* desc, v
  * attributes and writes per-ray gradients with respect to origin and direction
  * (object space of the hit instance). */
 rdn_status rdn_attr_loss_adjoint(rdn_ctx* ctx, const rdn_attr_loss_desc* desc, void* stream);
+
+/* Differentiable hit query: the closest hit's distance t (the parameter along
+ * the ray's direction as given, which is the reference's reported distance,
+ * traverse_cpu.rs:157), its barycentrics u, v (weights of vertices 1 and 2,
+ * geometry/mod.rs:144-154) and the interpolated vertex attribute
+ * value = (1-u-v) a0 + u a1 + v a2 of the triangle that the traversal finds,
+ * all re-solved on that triangle in float-float (f32 FMA) arithmetic, so they
+ * can differ from rdn_trace's reference-formula values in the last bits, and
+ * by more for rays that graze the triangle. The adjoint takes the caller's
+ * upstream gradients of (t, u, v, value) per ray and returns, at frozen
+ * visibility, the gradients with respect to the vertex positions (object
+ * space of each BLAS, accumulated), the vertex attributes (accumulated), and
+ * each ray's origin and direction (world space; the instance transform's
+ * linear part is assumed affine). Misses write (tmax, 0, 0, 0) and get zero
+ * gradients. No counterpart in the reference: the differentiable form of its
+ * closest-hit query (traverse_cpu.rs:52-245). */
+typedef struct rdn_hit_diff_desc {
+  const rdn_ray* rays;          /* device */
+  uint32_t count;
+  uint32_t tlas_uniform;
+  const float* attributes;      /* device, nullable: one per built vertex; NULL: value = 0, no attribute gradient */
+  float* hit;                   /* device, nullable: 4 per ray, (t, u, v, value) (forward) */
+  uint32_t* hit_tri;            /* device, nullable: built triangle of each ray's hit, RDN_MISS (forward) */
+  uint32_t* hit_inst;           /* device, nullable: TLAS instance slot of each ray's hit (forward) */
+  const float* grad_hit;        /* device: 4 per ray, (dL/dt, dL/du, dL/dv, dL/dvalue) (adjoint) */
+  float* grad_vertices;         /* device: 4 per built vertex, (dL/dx, dL/dy, dL/dz, dL/dattr); accumulated
+                                   (adjoint; the caller zeroes it) */
+  float* grad_ray_origin;       /* device, nullable: 3 per ray (adjoint) */
+  float* grad_ray_direction;    /* device, nullable: 3 per ray (adjoint) */
+  uint32_t traversal;           /* RDN_TRAVERSAL_* (| RDN_INTERSECT_WATERTIGHT) */
+  uint32_t block_size;          /* 0 = 64 */
+  uint32_t from_record;         /* adjoint: 1 = differentiate the hits the forward recorded in hit_tri /
+                                   hit_inst instead of tracing the rays again */
+  uint32_t local_stack;         /* ordered walks: 1 = traversal stacks in local memory */
+  uint32_t speculation;         /* ordered walks: leaf postponement threshold, as in rdn_wavefront_desc */
+} rdn_hit_diff_desc;
+
+rdn_status rdn_hit_diff_forward(rdn_ctx* ctx, const rdn_hit_diff_desc* desc, void* stream);
+rdn_status rdn_hit_diff_adjoint(rdn_ctx* ctx, const rdn_hit_diff_desc* desc, void* stream);
 
 /* Differentiable paths over many scenes: every path is a primary ray (with its
  * own index into the bound TLAS list) followed by up to segments-1 cosine

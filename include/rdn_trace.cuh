@@ -52,7 +52,8 @@ struct Hit {
 // One query: MODE rdn::MODE_THREADED (the reference's order) or
 // rdn::MODE_WIDE4 / rdn::MODE_BINARY (ordered walks; Params from
 // rdn_trace_params with that traversal, whose stack fits this thread's
-// local array).
+// local array). Params asked for with RDN_INTERSECT_WATERTIGHT select the
+// watertight triangle test (both forms are compiled into the caller's kernel).
 template <int MODE, class AnyHit>
 __device__ inline Hit trace(const Params& p, const rdn_ray& ray, uint32_t tlas, uint32_t ray_flags,
                             uint32_t cull_mask, const AnyHit& anyhit) {
@@ -65,7 +66,10 @@ __device__ inline Hit trace(const Params& p, const rdn_ray& ray, uint32_t tlas, 
   R.ray_flags = ray_flags;
   R.cull_mask = cull_mask;
   bool bad;
-  rdn::dev::traverse_ray<MODE, false, AnyHit>(p, R, tlas, stack, 1u, bad, anyhit);
+  if (p.watertight)
+    rdn::dev::traverse_ray<MODE, false, AnyHit, true>(p, R, tlas, stack, 1u, bad, anyhit);
+  else
+    rdn::dev::traverse_ray<MODE, false, AnyHit, false>(p, R, tlas, stack, 1u, bad, anyhit);
   Hit h;
   h.unbound_tlas = bad;
   if (R.best.have) {

@@ -95,6 +95,7 @@ struct HitGeom {
   uint32_t i0, i1, i2;
   float w0, u, v;
   ff3 b1, b2;  // e2 x (-d) and (-d) x e1 in float-float (the adjoint's lambda)
+  ff3 c12;     // e1 x e2 (lambda's distance row)
   ff det;      // (-d) . (e1 x e2)
   float t_unnorm;  // hit distance in units of the unnormalised object-space direction
   ff wf, uf, vf;   // the three corner weights in float-float (w0, u, v round these)
@@ -140,6 +141,7 @@ __device__ __forceinline__ HitGeom hit_vertices_at(const TraceParams& p, const u
   h.v = h.vf.hi + h.vf.lo;
   h.w0 = h.wf.hi + h.wf.lo;
   h.det = det;
+  h.c12 = C12;
   h.b1 = ff3_cross(E2, ND);
   h.b2 = ff3_cross(ND, E1);
   return h;
@@ -173,7 +175,7 @@ __device__ __forceinline__ float residual(const HitGeom& h, float a0, float a1, 
   return d.hi + d.lo;
 }
 
-template <int MODE, bool LOCAL>
+template <int MODE, bool LOCAL, bool WT>
 __global__ void __launch_bounds__(128) attr_forward_kernel(TraceParams p, AdjointParams a) {
   RDN_TRAVERSAL_STACK(LOCAL);
   __shared__ double block_sum[4];
@@ -190,7 +192,7 @@ __global__ void __launch_bounds__(128) attr_forward_kernel(TraceParams p, Adjoin
     R.cull_mask = 0xFFu;
     R.ray_flags = 0u;
     bool bad;
-    traverse_ray<MODE, false>(p, R, a.tlas_uniform, stack_ptr, stack_stride, bad);
+    traverse_ray<MODE, false, BuiltinAnyHit, WT>(p, R, a.tlas_uniform, stack_ptr, stack_stride, bad);
     float value = 0.0f;
     if (R.best.have) {
       const InstanceRay ir = to_instance(p.tlas_data + R.best.inst, R.o, R.d, 0u);
@@ -217,7 +219,7 @@ __global__ void __launch_bounds__(128) attr_forward_kernel(TraceParams p, Adjoin
   }
 }
 
-template <int MODE, bool LOCAL>
+template <int MODE, bool LOCAL, bool WT>
 __global__ void __launch_bounds__(128) attr_adjoint_kernel(TraceParams p, AdjointParams a) {
   RDN_TRAVERSAL_STACK(LOCAL);
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -232,7 +234,7 @@ __global__ void __launch_bounds__(128) attr_adjoint_kernel(TraceParams p, Adjoin
   R.cull_mask = 0xFFu;
   R.ray_flags = 0u;
   bool bad;
-  traverse_ray<MODE, false>(p, R, a.tlas_uniform, stack_ptr, stack_stride, bad);
+  traverse_ray<MODE, false, BuiltinAnyHit, WT>(p, R, a.tlas_uniform, stack_ptr, stack_stride, bad);
   float3 go = make_float3(0.f, 0.f, 0.f), gd = go;
   if (R.best.have) {
     const InstanceRay ir = to_instance(p.tlas_data + R.best.inst, R.o, R.d, 0u);
@@ -247,9 +249,9 @@ __global__ void __launch_bounds__(128) attr_adjoint_kernel(TraceParams p, Adjoin
     atomicAdd(g + h.i0, make_float4(-h.w0 * lam.x, -h.w0 * lam.y, -h.w0 * lam.z, r * h.w0));
     atomicAdd(g + h.i1, make_float4(-h.u * lam.x, -h.u * lam.y, -h.u * lam.z, r * h.u));
     atomicAdd(g + h.i2, make_float4(-h.v * lam.x, -h.v * lam.y, -h.v * lam.z, r * h.v));
-    const float t_obj = R.best.t * ir.scaling;
+    // d(o + s d)/dd = s: s the hit's parameter along the object-space direction
     go = lam;
-    gd = make_float3(t_obj * lam.x, t_obj * lam.y, t_obj * lam.z);
+    gd = make_float3(h.t_unnorm * lam.x, h.t_unnorm * lam.y, h.t_unnorm * lam.z);
   }
   if (a.grad_ray_origin) {
     a.grad_ray_origin[3 * (size_t)i] = go.x;
@@ -276,7 +278,7 @@ __device__ __forceinline__ float3 scatter_vertex_grads(const HitGeom& h, const I
 }
 
 // Persistent warps over paths; ADJOINT selects the gradient pass.
-template <int MODE, bool ADJOINT, bool LOCAL>
+template <int MODE, bool ADJOINT, bool LOCAL, bool WT>
 __global__ void __launch_bounds__(128) attr_path_kernel(TraceParams p, PathAdjointParams a) {
   RDN_TRAVERSAL_STACK(LOCAL);
   __shared__ double block_sum[4];
@@ -310,7 +312,7 @@ __global__ void __launch_bounds__(128) attr_path_kernel(TraceParams p, PathAdjoi
         R.cull_mask = 0xFFu;
         R.ray_flags = 0u;
         bool bad;
-        traverse_ray<MODE, false>(p, R, tlas, stack_ptr, stack_stride, bad);
+        traverse_ray<MODE, false, BuiltinAnyHit, WT>(p, R, tlas, stack_ptr, stack_stride, bad);
         if (!R.best.have) {
           alive = false;
           if (!ADJOINT && a.targets) {
@@ -440,10 +442,9 @@ __global__ void __launch_bounds__(256) attr_recorded_adjoint_kernel(TraceParams 
       const float target = a.targets ? __ldg(a.targets + i) : 0.0f;
       const float r = 2.0f * residual(h, a0, a1, a2, target, &value) * a.grad_scale;
       const float3 lam = scatter_vertex_grads(h, ir, r, r * (a1 - a0), r * (a2 - a0), a.grad_vertices);
-      // object-space distance along the normalised direction: t_unnorm * |M3 d|
-      const float t_obj = h.t_unnorm * ir.scaling;
+      // d(o + s d)/dd = s: s the hit's parameter along the object-space direction
       go = lam;
-      gd = make_float3(t_obj * lam.x, t_obj * lam.y, t_obj * lam.z);
+      gd = make_float3(h.t_unnorm * lam.x, h.t_unnorm * lam.y, h.t_unnorm * lam.z);
     }
     if (a.grad_ray_origin) {
       a.grad_ray_origin[3 * (size_t)i] = go.x;
@@ -458,18 +459,143 @@ __global__ void __launch_bounds__(256) attr_recorded_adjoint_kernel(TraceParams 
   }
 }
 
+// ---- differentiable hit query (rdn_hit_diff_*) ------------------------------
+// Forward: per ray the closest hit's parameter t along the given direction (the
+// reference's reported distance, traverse_cpu.rs:157), the barycentrics (u, v)
+// and the interpolated attribute w0 a0 + u a1 + v a2, all re-solved on the hit
+// triangle in float-float. Adjoint: with the caller's upstream gradients
+// G = (dL/dt, dL/du, dL/dv, dL/dvalue) per ray,
+//   gu = G.u + G.value (a1 - a0), gv = G.v + G.value (a2 - a0),
+//   lambda = M^{-T} (G.t, gu, gv) = (G.t (e1 x e2) + gu (e2 x -d) + gv (-d x e1)) / det M,
+//   dL/dv_k = -w_k lambda, dL/da_k = G.value w_k (object space, accumulated),
+//   dL/do = L^T lambda, dL/dd = t L^T lambda (world space; L = the 3x3 of the
+//   instance's inverse transform, which maps world to object directions).
+__device__ __forceinline__ float3 to_world_covector(const DeviceInstance* inst, float3 g) {
+  const float* m = inst->transform_inv;
+  return make_float3(__ldg(m + 0) * g.x + __ldg(m + 1) * g.y + __ldg(m + 2) * g.z,
+                     __ldg(m + 4) * g.x + __ldg(m + 5) * g.y + __ldg(m + 6) * g.z,
+                     __ldg(m + 8) * g.x + __ldg(m + 9) * g.y + __ldg(m + 10) * g.z);
+}
+
+__device__ __forceinline__ void hit_diff_store(const AdjointParams& a, uint32_t i, float4 out, uint32_t tri,
+                                               uint32_t inst) {
+  if (a.hit_out) a.hit_out[i] = out;
+  if (a.hit_tri) a.hit_tri[i] = tri;
+  if (a.hit_inst) a.hit_inst[i] = inst;
+}
+
+template <int MODE, bool LOCAL, bool WT>
+__global__ void __launch_bounds__(128) hit_diff_forward_kernel(TraceParams p, AdjointParams a) {
+  RDN_TRAVERSAL_STACK(LOCAL);
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.count) return;
+  const float4 r0 = __ldg(a.rays + 2 * (size_t)i), r1 = __ldg(a.rays + 2 * (size_t)i + 1);
+  RayCtx R;
+  R.o = make_float3(r0.x, r0.y, r0.z);
+  R.tmin = r0.w;
+  R.d = make_float3(r1.x, r1.y, r1.z);
+  R.tmax = r1.w;
+  R.cull_mask = 0xFFu;
+  R.ray_flags = 0u;
+  bool bad;
+  traverse_ray<MODE, false, BuiltinAnyHit, WT>(p, R, a.tlas_uniform, stack_ptr, stack_stride, bad);
+  if (!R.best.have) {
+    hit_diff_store(a, i, make_float4(R.tmax, 0.0f, 0.0f, 0.0f), INVALID_NEXT, INVALID_NEXT);
+    return;
+  }
+  const InstanceRay ir = to_instance(p.tlas_data + R.best.inst, R.o, R.d, 0u);
+  const HitGeom h = hit_vertices(p, a.indices, a.vertices, R, ir);
+  float value = 0.0f;
+  if (a.attributes)
+    residual(h, __ldg(a.attributes + h.i0), __ldg(a.attributes + h.i1), __ldg(a.attributes + h.i2), 0.0f, &value);
+  hit_diff_store(a, i, make_float4(h.t_unnorm, h.u, h.v, value), __ldg(p.redirect + R.best.k), R.best.inst);
+}
+
+// The adjoint of one ray's hit (triangle `tri` of instance `inst`).
+__device__ __forceinline__ void hit_diff_scatter(const TraceParams& p, const AdjointParams& a, uint32_t i,
+                                                 uint32_t tri, uint32_t inst, float3 o, float3 d, float3& go,
+                                                 float3& gd) {
+  const InstanceRay ir = to_instance(p.tlas_data + inst, o, d, 0u);
+  const HitGeom h = hit_vertices_at(p, a.indices, a.vertices, tri, inst, d, ir);
+  const float4 G = __ldg(a.grad_hit + i);
+  float gu = G.y, gv = G.z;
+  if (a.attributes) {
+    const float a0 = __ldg(a.attributes + h.i0), a1 = __ldg(a.attributes + h.i1), a2 = __ldg(a.attributes + h.i2);
+    gu = gu + G.w * (a1 - a0);
+    gv = gv + G.w * (a2 - a0);
+  }
+  const ff GT{G.x, 0.f}, GU{gu, 0.f}, GV{gv, 0.f};
+  const float3 lam = make_float3(
+      ff_div(ff_add(ff_add(ff_mul(GT, h.c12.x), ff_mul(GU, h.b1.x)), ff_mul(GV, h.b2.x)), h.det),
+      ff_div(ff_add(ff_add(ff_mul(GT, h.c12.y), ff_mul(GU, h.b1.y)), ff_mul(GV, h.b2.y)), h.det),
+      ff_div(ff_add(ff_add(ff_mul(GT, h.c12.z), ff_mul(GU, h.b1.z)), ff_mul(GV, h.b2.z)), h.det));
+  float4* g = reinterpret_cast<float4*>(a.grad_vertices);
+  const float gval = a.attributes ? G.w : 0.0f;
+  atomicAdd(g + h.i0, make_float4(-h.w0 * lam.x, -h.w0 * lam.y, -h.w0 * lam.z, gval * h.w0));
+  atomicAdd(g + h.i1, make_float4(-h.u * lam.x, -h.u * lam.y, -h.u * lam.z, gval * h.u));
+  atomicAdd(g + h.i2, make_float4(-h.v * lam.x, -h.v * lam.y, -h.v * lam.z, gval * h.v));
+  go = to_world_covector(p.tlas_data + inst, lam);
+  gd = make_float3(h.t_unnorm * go.x, h.t_unnorm * go.y, h.t_unnorm * go.z);
+}
+
+__device__ __forceinline__ void hit_diff_store_ray_grads(const AdjointParams& a, uint32_t i, float3 go, float3 gd) {
+  if (a.grad_ray_origin) {
+    a.grad_ray_origin[3 * (size_t)i] = go.x;
+    a.grad_ray_origin[3 * (size_t)i + 1] = go.y;
+    a.grad_ray_origin[3 * (size_t)i + 2] = go.z;
+  }
+  if (a.grad_ray_direction) {
+    a.grad_ray_direction[3 * (size_t)i] = gd.x;
+    a.grad_ray_direction[3 * (size_t)i + 1] = gd.y;
+    a.grad_ray_direction[3 * (size_t)i + 2] = gd.z;
+  }
+}
+
+template <int MODE, bool LOCAL, bool WT>
+__global__ void __launch_bounds__(128) hit_diff_adjoint_kernel(TraceParams p, AdjointParams a) {
+  RDN_TRAVERSAL_STACK(LOCAL);
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.count) return;
+  const float4 r0 = __ldg(a.rays + 2 * (size_t)i), r1 = __ldg(a.rays + 2 * (size_t)i + 1);
+  RayCtx R;
+  R.o = make_float3(r0.x, r0.y, r0.z);
+  R.tmin = r0.w;
+  R.d = make_float3(r1.x, r1.y, r1.z);
+  R.tmax = r1.w;
+  R.cull_mask = 0xFFu;
+  R.ray_flags = 0u;
+  bool bad;
+  traverse_ray<MODE, false, BuiltinAnyHit, WT>(p, R, a.tlas_uniform, stack_ptr, stack_stride, bad);
+  float3 go = make_float3(0.f, 0.f, 0.f), gd = go;
+  if (R.best.have) hit_diff_scatter(p, a, i, __ldg(p.redirect + R.best.k), R.best.inst, R.o, R.d, go, gd);
+  hit_diff_store_ray_grads(a, i, go, gd);
+}
+
+__global__ void __launch_bounds__(256) hit_diff_recorded_adjoint_kernel(TraceParams p, AdjointParams a) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.count; i += gridDim.x * blockDim.x) {
+    const uint32_t tri = __ldg(a.hit_tri + i);
+    float3 go = make_float3(0.f, 0.f, 0.f), gd = go;
+    if (tri != INVALID_NEXT) {
+      const float4 r0 = __ldg(a.rays + 2 * (size_t)i), r1 = __ldg(a.rays + 2 * (size_t)i + 1);
+      hit_diff_scatter(p, a, i, tri, __ldg(a.hit_inst + i), make_float3(r0.x, r0.y, r0.z),
+                       make_float3(r1.x, r1.y, r1.z), go, gd);
+    }
+    hit_diff_store_ray_grads(a, i, go, gd);
+  }
+}
+
 inline uint32_t recorded_grid(size_t items, int sm_count) {
   const size_t need = (items + 255) / 256;
   const size_t cap = (size_t)(sm_count > 0 ? sm_count : 1) * 16;
   return (uint32_t)(need < cap ? (need ? need : 1) : cap);
 }
 
-template <int MODE, bool LOCAL>
+template <int MODE, bool LOCAL, bool WT>
 cudaError_t launch_attr_paths_variant(const TraceParams& p, const PathAdjointParams& a, bool adjoint, uint32_t block,
                                       int sm_count, cudaStream_t stream) {
   static std::atomic<uint64_t> done[2] = {};
-  const void* fn = adjoint ? (const void*)attr_path_kernel<MODE, true, LOCAL>
-                           : (const void*)attr_path_kernel<MODE, false, LOCAL>;
+  const void* fn = adjoint ? (const void*)attr_path_kernel<MODE, true, LOCAL, WT>
+                           : (const void*)attr_path_kernel<MODE, false, LOCAL, WT>;
   cudaError_t e = raise_smem_limit(done[adjoint], {fn});
   if (e != cudaSuccess) return e;
   const size_t smem = MODE != MODE_THREADED && !LOCAL ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
@@ -482,39 +608,70 @@ cudaError_t launch_attr_paths_variant(const TraceParams& p, const PathAdjointPar
   if (grid > need) grid = need;
   e = cudaMemsetAsync(a.work_counter, 0, 4, stream);
   if (e != cudaSuccess) return e;
-  if (adjoint) attr_path_kernel<MODE, true, LOCAL><<<grid, block, smem, stream>>>(p, a);
-  else attr_path_kernel<MODE, false, LOCAL><<<grid, block, smem, stream>>>(p, a);
+  if (adjoint) attr_path_kernel<MODE, true, LOCAL, WT><<<grid, block, smem, stream>>>(p, a);
+  else attr_path_kernel<MODE, false, LOCAL, WT><<<grid, block, smem, stream>>>(p, a);
   return cudaGetLastError();
 }
 
 template <int MODE>
 cudaError_t launch_attr_paths_mode(const TraceParams& p, const PathAdjointParams& a, bool adjoint, uint32_t block,
                                    int sm_count, cudaStream_t stream) {
-  if (MODE != MODE_THREADED && p.local_stack)
-    return launch_attr_paths_variant<MODE, MODE != MODE_THREADED>(p, a, adjoint, block, sm_count, stream);
-  return launch_attr_paths_variant<MODE, false>(p, a, adjoint, block, sm_count, stream);
+  const bool local = MODE != MODE_THREADED && p.local_stack;
+  if (p.watertight)
+    return local ? launch_attr_paths_variant<MODE, MODE != MODE_THREADED, true>(p, a, adjoint, block, sm_count, stream)
+                 : launch_attr_paths_variant<MODE, false, true>(p, a, adjoint, block, sm_count, stream);
+  return local ? launch_attr_paths_variant<MODE, MODE != MODE_THREADED, false>(p, a, adjoint, block, sm_count, stream)
+               : launch_attr_paths_variant<MODE, false, false>(p, a, adjoint, block, sm_count, stream);
 }
 
-template <int MODE, bool LOCAL>
+template <int MODE, bool LOCAL, bool WT>
 cudaError_t launch_attr_variant(const TraceParams& p, const AdjointParams& a, bool adjoint, uint32_t block,
                                 cudaStream_t stream) {
   static std::atomic<uint64_t> done[2] = {};
-  const cudaError_t e = raise_smem_limit(done[adjoint], {adjoint ? (const void*)attr_adjoint_kernel<MODE, LOCAL>
-                                                                 : (const void*)attr_forward_kernel<MODE, LOCAL>});
+  const cudaError_t e = raise_smem_limit(done[adjoint], {adjoint ? (const void*)attr_adjoint_kernel<MODE, LOCAL, WT>
+                                                                 : (const void*)attr_forward_kernel<MODE, LOCAL, WT>});
   if (e != cudaSuccess) return e;
   const size_t smem = MODE != MODE_THREADED && !LOCAL ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
   const uint32_t grid = (a.count + block - 1) / block;
-  if (adjoint) attr_adjoint_kernel<MODE, LOCAL><<<grid, block, smem, stream>>>(p, a);
-  else attr_forward_kernel<MODE, LOCAL><<<grid, block, smem, stream>>>(p, a);
+  if (adjoint) attr_adjoint_kernel<MODE, LOCAL, WT><<<grid, block, smem, stream>>>(p, a);
+  else attr_forward_kernel<MODE, LOCAL, WT><<<grid, block, smem, stream>>>(p, a);
   return cudaGetLastError();
 }
 
 template <int MODE>
 cudaError_t launch_attr_mode(const TraceParams& p, const AdjointParams& a, bool adjoint, uint32_t block,
                              cudaStream_t stream) {
-  if (MODE != MODE_THREADED && p.local_stack)
-    return launch_attr_variant<MODE, MODE != MODE_THREADED>(p, a, adjoint, block, stream);
-  return launch_attr_variant<MODE, false>(p, a, adjoint, block, stream);
+  const bool local = MODE != MODE_THREADED && p.local_stack;
+  if (p.watertight)
+    return local ? launch_attr_variant<MODE, MODE != MODE_THREADED, true>(p, a, adjoint, block, stream)
+                 : launch_attr_variant<MODE, false, true>(p, a, adjoint, block, stream);
+  return local ? launch_attr_variant<MODE, MODE != MODE_THREADED, false>(p, a, adjoint, block, stream)
+               : launch_attr_variant<MODE, false, false>(p, a, adjoint, block, stream);
+}
+
+template <int MODE, bool LOCAL, bool WT>
+cudaError_t launch_hit_diff_variant(const TraceParams& p, const AdjointParams& a, bool adjoint, uint32_t block,
+                                    cudaStream_t stream) {
+  static std::atomic<uint64_t> done[2] = {};
+  const cudaError_t e = raise_smem_limit(done[adjoint], {adjoint ? (const void*)hit_diff_adjoint_kernel<MODE, LOCAL, WT>
+                                                                 : (const void*)hit_diff_forward_kernel<MODE, LOCAL, WT>});
+  if (e != cudaSuccess) return e;
+  const size_t smem = MODE != MODE_THREADED && !LOCAL ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
+  const uint32_t grid = (a.count + block - 1) / block;
+  if (adjoint) hit_diff_adjoint_kernel<MODE, LOCAL, WT><<<grid, block, smem, stream>>>(p, a);
+  else hit_diff_forward_kernel<MODE, LOCAL, WT><<<grid, block, smem, stream>>>(p, a);
+  return cudaGetLastError();
+}
+
+template <int MODE>
+cudaError_t launch_hit_diff_mode(const TraceParams& p, const AdjointParams& a, bool adjoint, uint32_t block,
+                                 cudaStream_t stream) {
+  const bool local = MODE != MODE_THREADED && p.local_stack;
+  if (p.watertight)
+    return local ? launch_hit_diff_variant<MODE, MODE != MODE_THREADED, true>(p, a, adjoint, block, stream)
+                 : launch_hit_diff_variant<MODE, false, true>(p, a, adjoint, block, stream);
+  return local ? launch_hit_diff_variant<MODE, MODE != MODE_THREADED, false>(p, a, adjoint, block, stream)
+               : launch_hit_diff_variant<MODE, false, false>(p, a, adjoint, block, stream);
 }
 
 cudaError_t launch_attr(const TraceParams& p, const AdjointParams& a, int mode, bool adjoint, uint32_t block,
@@ -554,6 +711,19 @@ cudaError_t launch_attr_adjoint(const TraceParams& p, const AdjointParams& a, in
     return cudaGetLastError();
   }
   return launch_attr(p, a, mode, true, block, stream);
+}
+
+cudaError_t launch_hit_diff(const TraceParams& p, const AdjointParams& a, int mode, bool adjoint, uint32_t block,
+                            int sm_count, cudaStream_t stream) {
+  if (a.count == 0) return cudaSuccess;
+  if (adjoint && a.from_record) {
+    hit_diff_recorded_adjoint_kernel<<<recorded_grid(a.count, sm_count), 256, 0, stream>>>(p, a);
+    return cudaGetLastError();
+  }
+  if (block == 0) block = 64;
+  if (mode == MODE_WIDE4) return launch_hit_diff_mode<MODE_WIDE4>(p, a, adjoint, block, stream);
+  if (mode == MODE_BINARY) return launch_hit_diff_mode<MODE_BINARY>(p, a, adjoint, block, stream);
+  return launch_hit_diff_mode<MODE_THREADED>(p, a, adjoint, block, stream);
 }
 
 }  // namespace rdn

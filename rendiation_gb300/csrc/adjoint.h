@@ -25,6 +25,8 @@ struct AdjointParams {
   uint32_t* hit_tri;          // per ray, nullable: built triangle of the hit or ~0 (written by the forward)
   uint32_t* hit_inst;         // per ray, nullable: instance slot of the hit (written by the forward)
   bool from_record;           // adjoint: differentiate the recorded hits instead of tracing again
+  float4* hit_out;            // hit query forward: (t, u, v, value) per ray, nullable
+  const float4* grad_hit;     // hit query adjoint: (dL/dt, dL/du, dL/dv, dL/dvalue) per ray
 };
 
 // Multi-segment, multi-scene form: every path is a primary ray (its own TLAS
@@ -56,6 +58,11 @@ struct PathAdjointParams {
 
 cudaError_t launch_attr_paths(const TraceParams& p, const PathAdjointParams& a, int mode, bool adjoint,
                               uint32_t block, int sm_count, cudaStream_t stream);
+
+// Differentiable hit query: forward writes (t, u, v, value) per ray; adjoint
+// scatters the caller's upstream gradients of those to the vertices and rays.
+cudaError_t launch_hit_diff(const TraceParams& p, const AdjointParams& a, int mode, bool adjoint, uint32_t block,
+                            int sm_count, cudaStream_t stream);
 
 cudaError_t launch_attr_forward(const TraceParams& p, const AdjointParams& a, int mode, uint32_t block,
                                 cudaStream_t stream);

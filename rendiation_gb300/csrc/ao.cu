@@ -15,7 +15,7 @@ namespace {
 
 using namespace dev;
 
-template <int MODE, bool LOCAL>
+template <int MODE, bool LOCAL, bool WT>
 __global__ void __launch_bounds__(128) ao_kernel(TraceParams P, AoEnv A) {
   RDN_TRAVERSAL_STACK(LOCAL);
   uint32_t x, y;
@@ -30,7 +30,7 @@ __global__ void __launch_bounds__(128) ao_kernel(TraceParams P, AoEnv A) {
   R.ray_flags = RAY_FLAG_CULL_BACK;
   R.cull_mask = 0xFFFFFFFFu;
   bool bad;
-  traverse_ray<MODE, false>(P, R, A.tlas, stack_ptr, stack_stride, bad);
+  traverse_ray<MODE, false, BuiltinAnyHit, WT>(P, R, A.tlas, stack_ptr, stack_stride, bad);
   float payload = 1.0f;  // miss shader
   if (R.best.have) {
     const float3 hit = o + d * R.best.t;
@@ -44,7 +44,7 @@ __global__ void __launch_bounds__(128) ao_kernel(TraceParams P, AoEnv A) {
     S.ray_flags = RAY_FLAG_END_SEARCH;
     S.cull_mask = 0xFFFFFFFFu;
     bool bad2;
-    traverse_ray<MODE, false>(P, S, A.tlas, stack_ptr, stack_stride, bad2);
+    traverse_ray<MODE, false, BuiltinAnyHit, WT>(P, S, A.tlas, stack_ptr, stack_stride, bad2);
     bad |= bad2;
     payload = S.best.have ? 0.0f : 1.0f;  // secondary closest hit: occluded
   }
@@ -54,16 +54,21 @@ __global__ void __launch_bounds__(128) ao_kernel(TraceParams P, AoEnv A) {
   ao_accumulate(A, y * A.width + x, payload);
 }
 
-template <int MODE, bool LOCAL>
-cudaError_t launch_variant(const TraceParams& p, const AoEnv& a, cudaStream_t st) {
+template <int MODE, bool LOCAL, bool WT>
+cudaError_t launch_variant_wt(const TraceParams& p, const AoEnv& a, cudaStream_t st) {
   const uint32_t block = a.block ? a.block : 128;
   const uint32_t grid = (ao_dispatch_count(a.width, a.height) + block - 1) / block;
   const size_t smem = MODE != MODE_THREADED && !LOCAL ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
   static std::atomic<uint64_t> attr_done{0};
-  const cudaError_t e = raise_smem_limit(attr_done, {(const void*)ao_kernel<MODE, LOCAL>});
+  const cudaError_t e = raise_smem_limit(attr_done, {(const void*)ao_kernel<MODE, LOCAL, WT>});
   if (e != cudaSuccess) return e;
-  ao_kernel<MODE, LOCAL><<<grid, block, smem, st>>>(p, a);
+  ao_kernel<MODE, LOCAL, WT><<<grid, block, smem, st>>>(p, a);
   return cudaGetLastError();
+}
+
+template <int MODE, bool LOCAL>
+cudaError_t launch_variant(const TraceParams& p, const AoEnv& a, cudaStream_t st) {
+  return p.watertight ? launch_variant_wt<MODE, LOCAL, true>(p, a, st) : launch_variant_wt<MODE, LOCAL, false>(p, a, st);
 }
 
 __global__ void ao_advance_kernel(uint32_t* counter) { *counter += 1u; }

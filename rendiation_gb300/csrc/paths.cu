@@ -35,7 +35,7 @@ using namespace dev;
 
 // Queue of bounce b: rays (2 float4) and states {id, tlas, throughput, 0}.
 // from_user: bounce 0 reads the caller's primary rays instead of a queue.
-template <int MODE, bool LOCAL>
+template <int MODE, bool LOCAL, bool WT>
 __global__ void __launch_bounds__(128) path_kernel(TraceParams p, PathParams q, uint32_t bounce, bool from_user,
                                                    const float4* __restrict__ in_rays,
                                                    const uint4* __restrict__ in_state, float4* __restrict__ out_rays,
@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(128) path_kernel(TraceParams p, PathParams q, 
       R.cull_mask = 0xFFu;
       R.ray_flags = 0u;
       bool bad;
-      traverse_ray<MODE, false>(p, R, tlas, stack_ptr, stack_stride, bad);
+      traverse_ray<MODE, false, BuiltinAnyHit, WT>(p, R, tlas, stack_ptr, stack_stride, bad);
       if (!R.best.have) {
         q.out[id] = make_float2(throughput, __uint_as_float(bounce | RDN_PATH_ESCAPED));
       } else if (bounce == q.max_bounces) {
@@ -127,7 +127,7 @@ __global__ void __launch_bounds__(128) path_kernel(TraceParams p, PathParams q, 
 // directions are mixed anyway, so no coherence is lost by refilling. The
 // shading and the warp-aggregated append run for the lanes that finished in
 // the round; iterations are capped (error-word bit 2).
-template <int MODE>
+template <int MODE, bool WT>
 __global__ void __launch_bounds__(128, 8) path_dynamic_kernel(TraceParams p, PathParams q, uint32_t bounce,
                                                               bool from_user, const float4* __restrict__ in_rays,
                                                               const uint4* __restrict__ in_state,
@@ -141,7 +141,7 @@ __global__ void __launch_bounds__(128, 8) path_dynamic_kernel(TraceParams p, Pat
   uint32_t* work = q.work_counter + bounce;
   uint2* stack = smem_stack + threadIdx.x;
   const uint32_t threshold = q.refill < 1u ? 1u : (q.refill > 32u ? 32u : q.refill);
-  LaneWalk<WIDTH> L;
+  LaneWalk<WIDTH, WT> L;
   L.reset();
   uint32_t id = 0, tlas = 0;
   float throughput = 0.0f;
@@ -328,14 +328,41 @@ int path_variant(int mode, const TraceParams& p, const PathParams& q) {
   if (q.refill != 0) return 1;
   return p.local_stack ? 2 : 0;
 }
-const void* path_fn(int mode, int variant) {
+template <bool WT>
+const void* path_fn_wt(int mode, int variant) {
   if (mode == MODE_WIDE4)
-    return variant == 1 ? (const void*)path_dynamic_kernel<MODE_WIDE4>
-                        : (variant == 2 ? (const void*)path_kernel<MODE_WIDE4, true> : (const void*)path_kernel<MODE_WIDE4, false>);
+    return variant == 1 ? (const void*)path_dynamic_kernel<MODE_WIDE4, WT>
+                        : (variant == 2 ? (const void*)path_kernel<MODE_WIDE4, true, WT>
+                                        : (const void*)path_kernel<MODE_WIDE4, false, WT>);
   if (mode == MODE_BINARY)
-    return variant == 1 ? (const void*)path_dynamic_kernel<MODE_BINARY>
-                        : (variant == 2 ? (const void*)path_kernel<MODE_BINARY, true> : (const void*)path_kernel<MODE_BINARY, false>);
-  return (const void*)path_kernel<MODE_THREADED, false>;
+    return variant == 1 ? (const void*)path_dynamic_kernel<MODE_BINARY, WT>
+                        : (variant == 2 ? (const void*)path_kernel<MODE_BINARY, true, WT>
+                                        : (const void*)path_kernel<MODE_BINARY, false, WT>);
+  return (const void*)path_kernel<MODE_THREADED, false, WT>;
+}
+const void* path_fn(int mode, int variant, bool wt) {
+  return wt ? path_fn_wt<true>(mode, variant) : path_fn_wt<false>(mode, variant);
+}
+
+// One bounce launch of the variant chosen by path_variant.
+template <bool WT>
+void launch_bounce(int mode, int variant, uint32_t grid, uint32_t block, size_t smem, cudaStream_t stream,
+                   const TraceParams& p, const PathParams& q, uint32_t b, bool from_user, const float4* in_r,
+                   const uint4* in_s, float4* out_r, uint4* out_s) {
+  if (mode == MODE_WIDE4 && variant == 1)
+    path_dynamic_kernel<MODE_WIDE4, WT><<<grid, block, smem, stream>>>(p, q, b, from_user, in_r, in_s, out_r, out_s);
+  else if (mode == MODE_WIDE4 && variant == 2)
+    path_kernel<MODE_WIDE4, true, WT><<<grid, block, smem, stream>>>(p, q, b, from_user, in_r, in_s, out_r, out_s);
+  else if (mode == MODE_WIDE4)
+    path_kernel<MODE_WIDE4, false, WT><<<grid, block, smem, stream>>>(p, q, b, from_user, in_r, in_s, out_r, out_s);
+  else if (mode == MODE_BINARY && variant == 1)
+    path_dynamic_kernel<MODE_BINARY, WT><<<grid, block, smem, stream>>>(p, q, b, from_user, in_r, in_s, out_r, out_s);
+  else if (mode == MODE_BINARY && variant == 2)
+    path_kernel<MODE_BINARY, true, WT><<<grid, block, smem, stream>>>(p, q, b, from_user, in_r, in_s, out_r, out_s);
+  else if (mode == MODE_BINARY)
+    path_kernel<MODE_BINARY, false, WT><<<grid, block, smem, stream>>>(p, q, b, from_user, in_r, in_s, out_r, out_s);
+  else
+    path_kernel<MODE_THREADED, false, WT><<<grid, block, smem, stream>>>(p, q, b, from_user, in_r, in_s, out_r, out_s);
 }
 }  // namespace
 
@@ -344,9 +371,9 @@ cudaError_t prepare_paths(const TraceParams& p, const PathParams& q, int mode, u
   if (block == 0) block = 64;
   const int variant = path_variant(mode, p, q);
   const size_t smem = mode != MODE_THREADED && variant != 2 ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
-  static std::atomic<uint64_t> attr_done[3][3] = {};
-  const void* fn = path_fn(mode, variant);
-  cudaError_t e = raise_smem_limit(attr_done[variant][mode], {fn});
+  static std::atomic<uint64_t> attr_done[2][3][3] = {};
+  const void* fn = path_fn(mode, variant, p.watertight != 0);
+  cudaError_t e = raise_smem_limit(attr_done[p.watertight ? 1 : 0][variant][mode], {fn});
   if (e != cudaSuccess) return e;
   int per_sm = 0;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (int)block, smem);
@@ -404,20 +431,10 @@ cudaError_t record_paths(const TraceParams& p, const PathParams& q, int mode, ui
       out_r = (b & 1) ? ra : rb;
       out_s = (b & 1) ? sa : sb;
     }
-    if (mode == MODE_WIDE4 && variant == 1)
-      path_dynamic_kernel<MODE_WIDE4><<<grid, block, smem, stream>>>(p, q, b, from_user, in_r, in_s, out_r, out_s);
-    else if (mode == MODE_WIDE4 && variant == 2)
-      path_kernel<MODE_WIDE4, true><<<grid, block, smem, stream>>>(p, q, b, from_user, in_r, in_s, out_r, out_s);
-    else if (mode == MODE_WIDE4)
-      path_kernel<MODE_WIDE4, false><<<grid, block, smem, stream>>>(p, q, b, from_user, in_r, in_s, out_r, out_s);
-    else if (mode == MODE_BINARY && variant == 1)
-      path_dynamic_kernel<MODE_BINARY><<<grid, block, smem, stream>>>(p, q, b, from_user, in_r, in_s, out_r, out_s);
-    else if (mode == MODE_BINARY && variant == 2)
-      path_kernel<MODE_BINARY, true><<<grid, block, smem, stream>>>(p, q, b, from_user, in_r, in_s, out_r, out_s);
-    else if (mode == MODE_BINARY)
-      path_kernel<MODE_BINARY, false><<<grid, block, smem, stream>>>(p, q, b, from_user, in_r, in_s, out_r, out_s);
+    if (p.watertight)
+      launch_bounce<true>(mode, variant, grid, block, smem, stream, p, q, b, from_user, in_r, in_s, out_r, out_s);
     else
-      path_kernel<MODE_THREADED, false><<<grid, block, smem, stream>>>(p, q, b, from_user, in_r, in_s, out_r, out_s);
+      launch_bounce<false>(mode, variant, grid, block, smem, stream, p, q, b, from_user, in_r, in_s, out_r, out_s);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }

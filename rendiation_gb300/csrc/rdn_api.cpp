@@ -242,7 +242,6 @@ rdn_status fill_params(rdn_ctx* c, const rdn_trace_desc* desc, rdn::TraceParams&
                   p.stack_depth <= rdn::kLocalStackEntries;
   p.iteration_limit = c->iteration_limit;
   p.watertight = (desc->traversal & RDN_INTERSECT_WATERTIGHT) ? 1u : 0u;
-  p.box_far_scale = p.watertight ? rdn::kWatertightBoxFarScale : 1.0f;
   p.verts = reinterpret_cast<const float4*>(d.vertex_records.ptr);
   return RDN_OK;
 }
@@ -867,9 +866,87 @@ rdn_status prepare_attr(rdn_ctx* c, const rdn_attr_loss_desc* d, bool adjoint, r
   return RDN_OK;
 }
 
+rdn_status prepare_hit_diff(rdn_ctx* c, const rdn_hit_diff_desc* d, bool adjoint, rdn::TraceParams& p,
+                            rdn::AdjointParams& a) {
+  if (!c || !d) return fail(c, RDN_ERR_INVALID_ARG, "null context or descriptor");
+  if (c->device < 0) return fail(c, RDN_ERR_UNSUPPORTED, "host-only context cannot trace");
+  if (d->count && !d->rays) return fail(c, RDN_ERR_INVALID_ARG, "null rays");
+  if (adjoint && d->count && (!d->grad_hit || !d->grad_vertices))
+    return fail(c, RDN_ERR_INVALID_ARG, "the adjoint needs grad_hit and grad_vertices");
+  if ((reinterpret_cast<uintptr_t>(d->rays) & 15) || (reinterpret_cast<uintptr_t>(d->hit) & 15) ||
+      (reinterpret_cast<uintptr_t>(d->grad_hit) & 15) || (reinterpret_cast<uintptr_t>(d->grad_vertices) & 15))
+    return fail(c, RDN_ERR_INVALID_ARG, "rays, hits and gradients must be 16-byte aligned");
+  if (d->from_record > 1) return fail(c, RDN_ERR_INVALID_ARG, "from_record must be 0 or 1");
+  if (adjoint && d->from_record && d->count && (!d->hit_tri || !d->hit_inst))
+    return fail(c, RDN_ERR_INVALID_ARG, "from_record needs the hit_tri and hit_inst records of the forward");
+  if (!traversal_ok(d->traversal)) return fail(c, RDN_ERR_INVALID_ARG, "unknown traversal order");
+  if (d->block_size && (d->block_size % 32 || d->block_size > 128))
+    return fail(c, RDN_ERR_INVALID_ARG, "block_size must be a multiple of 32 up to 128");
+  if (d->local_stack > 1) return fail(c, RDN_ERR_INVALID_ARG, "local_stack must be 0 or 1");
+  if (d->speculation > 31) return fail(c, RDN_ERR_INVALID_ARG, "speculation must be 0..31");
+  rdn_status st = ensure_built(c);
+  if (st != RDN_OK) return st;
+  rdn_trace_desc td;
+  std::memset(&td, 0, sizeof(td));
+  td.tlas_uniform = d->tlas_uniform;
+  td.cull_mask = 0xFF;
+  td.traversal = d->traversal;
+  td.local_stack = d->local_stack;
+  fill_params(c, &td, p);
+  p.spec_threshold = d->speculation;
+  std::memset(&a, 0, sizeof(a));
+  a.rays = reinterpret_cast<const float4*>(d->rays);
+  a.count = d->count;
+  a.tlas_uniform = d->tlas_uniform;
+  a.indices = c->dev.indices.ptr;
+  a.vertices = c->dev.vertices.ptr;
+  a.attributes = d->attributes;
+  a.hit_out = reinterpret_cast<float4*>(d->hit);
+  a.hit_tri = d->hit_tri;
+  a.hit_inst = d->hit_inst;
+  a.grad_hit = reinterpret_cast<const float4*>(d->grad_hit);
+  a.grad_vertices = d->grad_vertices;
+  a.grad_ray_origin = d->grad_ray_origin;
+  a.grad_ray_direction = d->grad_ray_direction;
+  a.from_record = d->from_record != 0;
+  return RDN_OK;
+}
+
 }  // namespace
 
 extern "C" {
+
+rdn_status rdn_hit_diff_forward(rdn_ctx* c, const rdn_hit_diff_desc* d, void* stream) {
+  Range range_("rdn_hit_diff_forward");
+  if (!c) return RDN_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(c->lock);
+  rdn::TraceParams p;
+  rdn::AdjointParams a;
+  rdn_status st = prepare_hit_diff(c, d, false, p, a);
+  if (st != RDN_OK) return st;
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e == cudaSuccess)
+    e = rdn::launch_hit_diff(p, a, mode_of(d->traversal), false, d->block_size, c->sm_count,
+                             static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(c, e, "hit query forward");
+  return RDN_OK;
+}
+
+rdn_status rdn_hit_diff_adjoint(rdn_ctx* c, const rdn_hit_diff_desc* d, void* stream) {
+  Range range_("rdn_hit_diff_adjoint");
+  if (!c) return RDN_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(c->lock);
+  rdn::TraceParams p;
+  rdn::AdjointParams a;
+  rdn_status st = prepare_hit_diff(c, d, true, p, a);
+  if (st != RDN_OK) return st;
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e == cudaSuccess)
+    e = rdn::launch_hit_diff(p, a, mode_of(d->traversal), true, d->block_size, c->sm_count,
+                             static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(c, e, "hit query adjoint");
+  return RDN_OK;
+}
 
 rdn_status rdn_attr_loss_forward(rdn_ctx* c, const rdn_attr_loss_desc* d, void* stream) {
   Range range_("rdn_attr_loss_forward");

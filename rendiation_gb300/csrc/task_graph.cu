@@ -165,7 +165,7 @@ __device__ bool poll_chain(const TaskGraphDev& G, uint32_t g, uint32_t idx, cons
 // spawns the closest-hit or miss task of its trace call (resolving at once
 // when there is none to spawn); the task resolves in the poll that finds that
 // child finished, taking back the child's user payload.
-template <int MODE>
+template <int MODE, bool WT>
 __device__ bool poll_trace(const TaskGraphDev& G, uint32_t g, uint32_t idx, const TraceParams& P, uint2* stack,
                            uint32_t stride) {
   const TaskGroupDev& T = G.g[g];
@@ -181,7 +181,7 @@ __device__ bool poll_trace(const TaskGraphDev& G, uint32_t g, uint32_t idx, cons
     R.ray_flags = self[8];
     R.cull_mask = self[9];
     bool bad;
-    traverse_ray<MODE, false>(P, R, self[10], stack, stride, bad);
+    traverse_ray<MODE, false, BuiltinAnyHit, WT>(P, R, self[10], stack, stride, bad);
     if (bad) atomicOr(P.error_word, 2u);
     uint32_t target = TRACE_SUB_NOT_SPAWNED;
     if (R.best.have) {
@@ -260,12 +260,12 @@ __device__ __forceinline__ void poll_active(const TaskGraphDev& G, uint32_t g, c
   }
 }
 
-template <int MODE, bool LOCAL>
+template <int MODE, bool LOCAL, bool WT>
 __global__ void __launch_bounds__(kPollThreads, 8) poll_kernel(const TaskGraphDev* __restrict__ Gp, uint32_t g,
                                                             TraceParams P, AoEnv) {
   RDN_TRAVERSAL_STACK(LOCAL);
   const TaskGraphDev& G = *Gp;
-  poll_active(G, g, [&](uint32_t idx) { return poll_trace<MODE>(G, g, idx, P, stack_ptr, stack_stride); });
+  poll_active(G, g, [&](uint32_t idx) { return poll_trace<MODE, WT>(G, g, idx, P, stack_ptr, stack_stride); });
 }
 
 // Chain groups alone: without the traversal the kernel fits twice the resident
@@ -487,15 +487,22 @@ __global__ void loop_check_kernel(const TaskGraphDev* __restrict__ G, uint32_t* 
 
 uint32_t tiles_of(uint32_t cap) { return (cap + kTile - 1) / kTile; }
 
+template <int MODE, bool LOCAL, bool WT>
+cudaError_t launch_poll_wt(const TaskGraphDev* G, uint32_t g, const TraceParams& P, const AoEnv& A, uint32_t grid,
+                           cudaStream_t st) {
+  const size_t smem = MODE != MODE_THREADED && !LOCAL ? (size_t)P.stack_depth * kPollThreads * sizeof(uint2) : 0;
+  static std::atomic<uint64_t> attr_done{0};
+  const cudaError_t e = raise_smem_limit(attr_done, {(const void*)poll_kernel<MODE, LOCAL, WT>});
+  if (e != cudaSuccess) return e;
+  poll_kernel<MODE, LOCAL, WT><<<grid, kPollThreads, smem, st>>>(G, g, P, A);
+  return cudaGetLastError();
+}
+
 template <int MODE, bool LOCAL>
 cudaError_t launch_poll(const TaskGraphDev* G, uint32_t g, const TraceParams& P, const AoEnv& A, uint32_t grid,
                         cudaStream_t st) {
-  const size_t smem = MODE != MODE_THREADED && !LOCAL ? (size_t)P.stack_depth * kPollThreads * sizeof(uint2) : 0;
-  static std::atomic<uint64_t> attr_done{0};
-  const cudaError_t e = raise_smem_limit(attr_done, {(const void*)poll_kernel<MODE, LOCAL>});
-  if (e != cudaSuccess) return e;
-  poll_kernel<MODE, LOCAL><<<grid, kPollThreads, smem, st>>>(G, g, P, A);
-  return cudaGetLastError();
+  return P.watertight ? launch_poll_wt<MODE, LOCAL, true>(G, g, P, A, grid, st)
+                      : launch_poll_wt<MODE, LOCAL, false>(G, g, P, A, grid, st);
 }
 
 bool op_reads_trace_payload(uint32_t op) {

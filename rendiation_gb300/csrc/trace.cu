@@ -12,7 +12,7 @@ namespace {
 
 using namespace dev;
 
-template <int MODE, bool COUNT, bool LOCAL>
+template <int MODE, bool COUNT, bool LOCAL, bool WT>
 __global__ void __launch_bounds__(256) trace_kernel(TraceParams p) {
   RDN_TRAVERSAL_STACK(LOCAL);
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -31,7 +31,7 @@ __global__ void __launch_bounds__(256) trace_kernel(TraceParams p) {
     R.ray_flags = p.ray_flags;
     const uint32_t tidx = p.tlas_idx ? __ldg(p.tlas_idx + i) : p.tlas_uniform;
     bool bad;
-    traverse_ray<MODE, COUNT>(p, R, tidx, stack_ptr, stack_stride, bad);
+    traverse_ray<MODE, COUNT, BuiltinAnyHit, WT>(p, R, tidx, stack_ptr, stack_stride, bad);
 
     float4 out;
     uint4 ext;
@@ -81,14 +81,20 @@ uint32_t stack_entries(int mode, uint32_t max_binary_depth, uint32_t max_wide4_d
 }
 
 namespace {
-template <int MODE, bool COUNT, bool LOCAL>
-cudaError_t launch_trace_variant(const TraceParams& p, uint32_t block, uint32_t grid, cudaStream_t stream) {
+template <int MODE, bool COUNT, bool LOCAL, bool WT>
+cudaError_t launch_trace_wt(const TraceParams& p, uint32_t block, uint32_t grid, cudaStream_t stream) {
   const size_t smem = MODE != MODE_THREADED && !LOCAL ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
   static std::atomic<uint64_t> attr_done{0};
-  const cudaError_t e = raise_smem_limit(attr_done, {(const void*)trace_kernel<MODE, COUNT, LOCAL>});
+  const cudaError_t e = raise_smem_limit(attr_done, {(const void*)trace_kernel<MODE, COUNT, LOCAL, WT>});
   if (e != cudaSuccess) return e;
-  trace_kernel<MODE, COUNT, LOCAL><<<grid, block, smem, stream>>>(p);
+  trace_kernel<MODE, COUNT, LOCAL, WT><<<grid, block, smem, stream>>>(p);
   return cudaGetLastError();
+}
+
+template <int MODE, bool COUNT, bool LOCAL>
+cudaError_t launch_trace_variant(const TraceParams& p, uint32_t block, uint32_t grid, cudaStream_t stream) {
+  return p.watertight ? launch_trace_wt<MODE, COUNT, LOCAL, true>(p, block, grid, stream)
+                      : launch_trace_wt<MODE, COUNT, LOCAL, false>(p, block, grid, stream);
 }
 }  // namespace
 

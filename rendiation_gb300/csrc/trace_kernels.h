@@ -43,13 +43,12 @@ struct TraceParams {
   // iteration cap of the dynamic-fetch loops (0 = the built-in cap); on
   // reaching it a warp sets bit 2 of the error word and stops
   uint32_t iteration_limit;
-  // 1: the watertight triangle test over `verts` instead of the reference's
-  // formula over `tris` (which still gives the shading normal)
+  // 1: launch the kernels built for the watertight test (over `verts`, with
+  // conservative box tests) instead of the reference's formula over `tris`
+  // (which still gives the shading normal); kernels take the choice as a
+  // template argument, so the reference-formula kernels carry no cost for it
   uint32_t watertight;
   const float4* verts;  // 3 per triangle (VertexRecord), sorted order
-  // factor on every box test's exit distance: 1 (the reference's test) or,
-  // with the watertight test, kWatertightBoxFarScale (a conservative box test)
-  float box_far_scale;
 };
 
 // 1 + 2 gamma_3 (gamma_n = n u / (1 - n u), u = 2^-24) rounded up to f32:

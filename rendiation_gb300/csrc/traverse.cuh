@@ -63,20 +63,21 @@ __device__ __forceinline__ float signum_f(float x) {
 }
 
 // intersect_ray_aabb_cpu with the reciprocal direction precomputed (1/d is
-// the same IEEE value the reference forms per test). far_scale multiplies the
-// box's exit distance: 1 (exactly the reference's test) or, with the
-// watertight triangle test, kWatertightBoxFarScale, so that rounding cannot
-// reject a box the ray touches (Ize, "Robust BVH Ray Traversal", JCGT 2(2),
-// 2013: t_far * (1 + 2 gamma_3)); without it a ray through a shared vertex or
-// edge on a box face can skip the box that holds its triangle.
+// the same IEEE value the reference forms per test). WT (the watertight
+// triangle test) multiplies the box's exit distance by kWatertightBoxFarScale,
+// so that rounding cannot reject a box the ray touches (Ize, "Robust BVH Ray
+// Traversal", JCGT 2(2), 2013: t_far * (1 + 2 gamma_3)); without it a ray
+// through a shared vertex or edge on a box face can skip the box that holds
+// its triangle. Without WT the test is exactly the reference's.
+template <bool WT = false>
 __device__ __forceinline__ bool slab(float3 o, float3 inv_d, float tmin, float tmax, float lx, float ly, float lz,
-                                     float hx, float hy, float hz, float& t_near_max, float far_scale) {
+                                     float hx, float hy, float hz, float& t_near_max) {
   const float t0x = (lx - o.x) * inv_d.x, t0y = (ly - o.y) * inv_d.y, t0z = (lz - o.z) * inv_d.z;
   const float t1x = (hx - o.x) * inv_d.x, t1y = (hy - o.y) * inv_d.y, t1z = (hz - o.z) * inv_d.z;
   const float nx = fminf(t0x, t1x), ny = fminf(t0y, t1y), nz = fminf(t0z, t1z);
   const float fx = fmaxf(t0x, t1x), fy = fmaxf(t0y, t1y), fz = fmaxf(t0z, t1z);
   const float tn = fmaxf(fmaxf(nx, ny), nz);
-  const float tf = fminf(fminf(fx, fy), fz) * far_scale;
+  const float tf = WT ? fminf(fminf(fx, fy), fz) * kWatertightBoxFarScale : fminf(fminf(fx, fy), fz);
   t_near_max = tn;
   return tn <= tf && tmin < tf && tn < tmax;
 }
@@ -293,19 +294,19 @@ struct RayCtx {
 
 // Tests the triangles of sorted range [k0, k1) and commits hits; returns true
 // when the search must end. Follows traverse_cpu.rs:133-193.
-template <bool COUNT, class AH = BuiltinAnyHit>
+template <bool COUNT, class AH = BuiltinAnyHit, bool WT = false>
 __device__ __forceinline__ bool leaf_triangles(const TraceParams& p, RayCtx& R, const InstanceRay& ir, uint32_t k0,
                                                uint32_t k1, uint32_t gslot, uint32_t inst_slot, bool is_opaque,
                                                bool cull_enable, bool cull_back, uint32_t prim_start,
                                                const AH& anyhit = AH()) {
+  Shear sh;
+  if (WT) sh = make_shear(ir.d, ir.inv_d);
   for (uint32_t k = k0; k < k1; k++) {
     if (COUNT) R.tri_tests++;
     TriOut h;
     const float near_ = R.tmin * ir.scaling, far_ = R.far_world * ir.scaling;
-    if (p.watertight) {
-      if (!tri_test_watertight(p.verts + 3 * (size_t)k, ir.o, make_shear(ir.d, ir.inv_d), near_, far_, cull_enable,
-                               cull_back, h))
-        continue;
+    if (WT) {
+      if (!tri_test_watertight(p.verts + 3 * (size_t)k, ir.o, sh, near_, far_, cull_enable, cull_back, h)) continue;
     } else if (!tri_test(p.tris + 4 * (size_t)k, ir.o, ir.d, near_, far_, cull_enable, cull_back, h)) {
       continue;
     }
@@ -334,7 +335,7 @@ __device__ __forceinline__ bool leaf_triangles(const TraceParams& p, RayCtx& R, 
 }
 
 // BLAS of one geometry, reference threaded order (traverse_cpu.rs:122-195).
-template <bool COUNT, class AH = BuiltinAnyHit>
+template <bool COUNT, class AH = BuiltinAnyHit, bool WT = false>
 __device__ __forceinline__ bool blas_threaded(const TraceParams& p, RayCtx& R, const InstanceRay& ir, uint32_t root,
                                               uint32_t gslot, uint32_t inst_slot, bool is_opaque, bool cull_enable,
                                               bool cull_back, uint32_t prim_start, const AH& anyhit = AH()) {
@@ -345,12 +346,12 @@ __device__ __forceinline__ bool blas_threaded(const TraceParams& p, RayCtx& R, c
     const float4 a = __ldg(nd), b = __ldg(nd + 1);
     float tn;
     const uint32_t hit_next = __float_as_uint(a.w), miss_next = __float_as_uint(b.w);
-    if (slab(ir.o, ir.inv_d, R.tmin * ir.scaling, R.far_world * ir.scaling, a.x, a.y, a.z, b.x, b.y, b.z, tn, p.box_far_scale)) {
+    if (slab<WT>(ir.o, ir.inv_d, R.tmin * ir.scaling, R.far_world * ir.scaling, a.x, a.y, a.z, b.x, b.y, b.z, tn)) {
       curr = hit_next;
       if (hit_next == miss_next) {  // a leaf: hit and miss links are the same node
         const uint2 cr = __ldg(reinterpret_cast<const uint2*>(nd + 2));
-        if (leaf_triangles<COUNT, AH>(p, R, ir, cr.x, cr.y, gslot, inst_slot, is_opaque, cull_enable, cull_back,
-                                      prim_start, anyhit))
+        if (leaf_triangles<COUNT, AH, WT>(p, R, ir, cr.x, cr.y, gslot, inst_slot, is_opaque, cull_enable,
+                                          cull_back, prim_start, anyhit))
           return true;
       }
     } else {
@@ -395,7 +396,7 @@ __device__ __forceinline__ void push_entry(const TraceParams& p, uint2* stack, u
 // One interior-node step of the ordered walk: tests the children of node
 // `code`, pushes the farther hits and returns the nearest hit child (or the
 // next live stack entry when no child is hit).
-template <bool COUNT, int WIDTH>
+template <bool COUNT, int WIDTH, bool WT = false>
 __device__ __forceinline__ uint32_t interior_step(const TraceParams& p, RayCtx& R, const InstanceRay& ir, uint32_t code,
                                                   float& code_tn, uint2* stack, uint32_t stride, uint32_t& sp,
                                                   uint32_t depth) {
@@ -406,8 +407,8 @@ __device__ __forceinline__ uint32_t interior_step(const TraceParams& p, RayCtx& 
     const uint2 cc = __ldg(reinterpret_cast<const uint2*>(w + 3));
     if (COUNT) R.node_visits += 2;
     float tn0, tn1;
-    const bool h0 = slab(ir.o, ir.inv_d, near_, far_, w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, tn0, p.box_far_scale);
-    const bool h1 = slab(ir.o, ir.inv_d, near_, far_, w1.z, w1.w, w2.x, w2.y, w2.z, w2.w, tn1, p.box_far_scale);
+    const bool h0 = slab<WT>(ir.o, ir.inv_d, near_, far_, w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, tn0);
+    const bool h1 = slab<WT>(ir.o, ir.inv_d, near_, far_, w1.z, w1.w, w2.x, w2.y, w2.z, w2.w, tn1);
     if (h0 && h1) {
       const bool second_first = tn1 < tn0;
       push_entry(p, stack, stride, sp, depth, second_first ? cc.x : cc.y, second_first ? tn0 : tn1);
@@ -428,19 +429,19 @@ __device__ __forceinline__ uint32_t interior_step(const TraceParams& p, RayCtx& 
     float t0 = inf, t1 = inf, t2 = inf, t3 = inf;
     uint32_t c0 = EMPTY_SLOT, c1 = EMPTY_SLOT, c2 = EMPTY_SLOT, c3 = EMPTY_SLOT;
     float tn;
-    if (cc.x != EMPTY_SLOT && slab(ir.o, ir.inv_d, near_, far_, lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, tn, p.box_far_scale)) {
+    if (cc.x != EMPTY_SLOT && slab<WT>(ir.o, ir.inv_d, near_, far_, lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, tn)) {
       t0 = tn;
       c0 = cc.x;
     }
-    if (cc.y != EMPTY_SLOT && slab(ir.o, ir.inv_d, near_, far_, lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, tn, p.box_far_scale)) {
+    if (cc.y != EMPTY_SLOT && slab<WT>(ir.o, ir.inv_d, near_, far_, lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, tn)) {
       t1 = tn;
       c1 = cc.y;
     }
-    if (cc.z != EMPTY_SLOT && slab(ir.o, ir.inv_d, near_, far_, lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, tn, p.box_far_scale)) {
+    if (cc.z != EMPTY_SLOT && slab<WT>(ir.o, ir.inv_d, near_, far_, lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, tn)) {
       t2 = tn;
       c2 = cc.z;
     }
-    if (cc.w != EMPTY_SLOT && slab(ir.o, ir.inv_d, near_, far_, lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, tn, p.box_far_scale)) {
+    if (cc.w != EMPTY_SLOT && slab<WT>(ir.o, ir.inv_d, near_, far_, lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, tn)) {
       t3 = tn;
       c3 = cc.w;
     }
@@ -464,7 +465,7 @@ __device__ __forceinline__ uint32_t interior_step(const TraceParams& p, RayCtx& 
 // a leaf (or has finished), then the warp tests triangles together. Nodes are
 // visited in near-first order with the reference's box test; the speculation
 // only adds visits, never removes one, so the closest hit is unchanged.
-template <bool COUNT, int WIDTH, class AH = BuiltinAnyHit>
+template <bool COUNT, int WIDTH, class AH = BuiltinAnyHit, bool WT = false>
 __device__ __forceinline__ bool blas_speculative(const TraceParams& p, RayCtx& R, const InstanceRay& ir,
                                                  uint32_t root_node, uint32_t gslot, uint32_t inst_slot,
                                                  bool is_opaque, bool cull_enable, bool cull_back, uint32_t prim_start,
@@ -475,7 +476,7 @@ __device__ __forceinline__ bool blas_speculative(const TraceParams& p, RayCtx& R
     const float4* nd = reinterpret_cast<const float4*>(p.tri_forest + root_node);
     const float4 a = __ldg(nd), b = __ldg(nd + 1);
     float tn;
-    if (!slab(ir.o, ir.inv_d, R.tmin * ir.scaling, R.far_world * ir.scaling, a.x, a.y, a.z, b.x, b.y, b.z, tn, p.box_far_scale))
+    if (!slab<WT>(ir.o, ir.inv_d, R.tmin * ir.scaling, R.far_world * ir.scaling, a.x, a.y, a.z, b.x, b.y, b.z, tn))
       return false;
   }
   uint32_t code = __ldg((WIDTH == 2 ? p.geom_root_code : p.geom_root_code4) + gslot);
@@ -488,7 +489,7 @@ __device__ __forceinline__ bool blas_speculative(const TraceParams& p, RayCtx& R
   }
   while (code != EMPTY_SLOT || leaf != EMPTY_SLOT) {
     while (code != EMPTY_SLOT && !(code & LEAF_BIT)) {
-      code = interior_step<COUNT, WIDTH>(p, R, ir, code, code_tn, stack, stride, sp, depth);
+      code = interior_step<COUNT, WIDTH, WT>(p, R, ir, code, code_tn, stack, stride, sp, depth);
       if (code != EMPTY_SLOT && (code & LEAF_BIT) && leaf == EMPTY_SLOT) {
         leaf = code;
         code = pop_live(stack, stride, sp, R.far_world * ir.scaling, code_tn);
@@ -498,8 +499,8 @@ __device__ __forceinline__ bool blas_speculative(const TraceParams& p, RayCtx& R
     }
     while (leaf != EMPTY_SLOT) {
       const uint2 lr = __ldg(p.leaves + (leaf & ~LEAF_BIT));
-      if (leaf_triangles<COUNT, AH>(p, R, ir, lr.x, lr.y, gslot, inst_slot, is_opaque, cull_enable, cull_back,
-                                    prim_start, anyhit))
+      if (leaf_triangles<COUNT, AH, WT>(p, R, ir, lr.x, lr.y, gslot, inst_slot, is_opaque, cull_enable, cull_back,
+                                        prim_start, anyhit))
         return true;
       leaf = EMPTY_SLOT;
       // the far may have shrunk: re-check the pending node before descending into it
@@ -516,7 +517,7 @@ __device__ __forceinline__ bool blas_speculative(const TraceParams& p, RayCtx& R
 
 // Full query of one ray (traverse_cpu.rs:52-245). R must hold the ray; on
 // return R.best holds the committed hit. `bad` reports an unbound TLAS index.
-template <int MODE, bool COUNT, class AH = BuiltinAnyHit>
+template <int MODE, bool COUNT, class AH = BuiltinAnyHit, bool WT = false>
 __device__ __forceinline__ void traverse_ray(const TraceParams& p, RayCtx& R, uint32_t tidx, uint2* stack,
                                              uint32_t stride, bool& bad, const AH& anyhit = AH()) {
   R.inv_d = make_float3(1.0f / R.d.x, 1.0f / R.d.y, 1.0f / R.d.z);
@@ -540,7 +541,7 @@ __device__ __forceinline__ void traverse_ray(const TraceParams& p, RayCtx& R, ui
     const float4 a = __ldg(nd), b = __ldg(nd + 1);
     const uint32_t hit_next = __float_as_uint(a.w), miss_next = __float_as_uint(b.w);
     float tn;
-    if (!slab(R.o, R.inv_d, R.tmin * 1.0f, R.far_world * 1.0f, a.x, a.y, a.z, b.x, b.y, b.z, tn, p.box_far_scale)) {
+    if (!slab<WT>(R.o, R.inv_d, R.tmin * 1.0f, R.far_world * 1.0f, a.x, a.y, a.z, b.x, b.y, b.z, tn)) {
       curr = miss_next;
       continue;
     }
@@ -551,7 +552,7 @@ __device__ __forceinline__ void traverse_ray(const TraceParams& p, RayCtx& R, ui
       const float4* tb = reinterpret_cast<const float4*>(p.tlas_bounding + ti);
       const float4 ba = __ldg(tb), bb = __ldg(tb + 1);
       float tn2;
-      if (!slab(R.o, R.inv_d, R.tmin, R.tmax, ba.x, ba.y, ba.z, bb.x, bb.y, bb.z, tn2, p.box_far_scale)) continue;
+      if (!slab<WT>(R.o, R.inv_d, R.tmin, R.tmax, ba.x, ba.y, ba.z, bb.x, bb.y, bb.z, tn2)) continue;
       if ((R.cull_mask & __float_as_uint(ba.w)) == 0) continue;
       const DeviceInstance* inst = p.tlas_data + ti;
       const InstanceRay ir = to_instance(inst, R.o, R.d, R.ray_flags);
@@ -565,13 +566,13 @@ __device__ __forceinline__ void traverse_ray(const TraceParams& p, RayCtx& R, ui
         if (!pass) continue;
         bool end;
         if (MODE == MODE_WIDE4)
-          end = blas_speculative<COUNT, 4, AH>(p, R, ir, gm.x, g, ti, is_opaque, cull_enable, cull_back, gm.z, stack,
+          end = blas_speculative<COUNT, 4, AH, WT>(p, R, ir, gm.x, g, ti, is_opaque, cull_enable, cull_back, gm.z, stack,
                                                stride, p.stack_depth, anyhit);
         else if (MODE == MODE_BINARY)
-          end = blas_speculative<COUNT, 2, AH>(p, R, ir, gm.x, g, ti, is_opaque, cull_enable, cull_back, gm.z, stack,
+          end = blas_speculative<COUNT, 2, AH, WT>(p, R, ir, gm.x, g, ti, is_opaque, cull_enable, cull_back, gm.z, stack,
                                                stride, p.stack_depth, anyhit);
         else
-          end = blas_threaded<COUNT, AH>(p, R, ir, gm.x, g, ti, is_opaque, cull_enable, cull_back, gm.z, anyhit);
+          end = blas_threaded<COUNT, AH, WT>(p, R, ir, gm.x, g, ti, is_opaque, cull_enable, cull_back, gm.z, anyhit);
         if (end) {
           done = true;
           break;
@@ -591,7 +592,7 @@ __device__ __forceinline__ uint32_t walk_round_cap(const TraceParams& p) {
   return p.iteration_limit ? p.iteration_limit : kMaxWalkRounds;
 }
 
-template <int WIDTH>
+template <int WIDTH, bool WT = false>
 struct LaneWalk {
   RayCtx R;
   InstanceRay ir;
@@ -646,7 +647,7 @@ struct LaneWalk {
           const float4 a = __ldg(nd), b = __ldg(nd + 1);
           const uint32_t hit_next = __float_as_uint(a.w), miss_next = __float_as_uint(b.w);
           float tn;
-          if (!slab(R.o, R.inv_d, R.tmin * 1.0f, R.far_world * 1.0f, a.x, a.y, a.z, b.x, b.y, b.z, tn, p.box_far_scale)) {
+          if (!slab<WT>(R.o, R.inv_d, R.tmin * 1.0f, R.far_world * 1.0f, a.x, a.y, a.z, b.x, b.y, b.z, tn)) {
             tcur = miss_next;
             continue;
           }
@@ -666,7 +667,7 @@ struct LaneWalk {
           const float4* tb = reinterpret_cast<const float4*>(p.tlas_bounding + cur);
           const float4 ba = __ldg(tb), bb = __ldg(tb + 1);
           float tn2;
-          if (!slab(R.o, R.inv_d, R.tmin, R.tmax, ba.x, ba.y, ba.z, bb.x, bb.y, bb.z, tn2, p.box_far_scale)) continue;
+          if (!slab<WT>(R.o, R.inv_d, R.tmin, R.tmax, ba.x, ba.y, ba.z, bb.x, bb.y, bb.z, tn2)) continue;
           if ((R.cull_mask & __float_as_uint(ba.w)) == 0) continue;
           const DeviceInstance* inst = p.tlas_data + cur;
           ir = to_instance(inst, R.o, R.d, R.ray_flags);
@@ -691,7 +692,7 @@ struct LaneWalk {
           const float4* nd = reinterpret_cast<const float4*>(p.tri_forest + gm.x);
           const float4 a = __ldg(nd), b = __ldg(nd + 1);
           float tn;
-          if (!slab(ir.o, ir.inv_d, R.tmin * ir.scaling, R.far_world * ir.scaling, a.x, a.y, a.z, b.x, b.y, b.z, tn, p.box_far_scale))
+          if (!slab<WT>(ir.o, ir.inv_d, R.tmin * ir.scaling, R.far_world * ir.scaling, a.x, a.y, a.z, b.x, b.y, b.z, tn))
             continue;
           code = __ldg((WIDTH == 2 ? p.geom_root_code : p.geom_root_code4) + cur);
           code_tn = -inf;
@@ -726,7 +727,7 @@ struct LaneWalk {
         return;
       }
       while (code != EMPTY_SLOT && !(code & LEAF_BIT)) {
-        code = interior_step<false, WIDTH>(p, R, ir, code, code_tn, stack, stride, sp, p.stack_depth);
+        code = interior_step<false, WIDTH, WT>(p, R, ir, code, code_tn, stack, stride, sp, p.stack_depth);
         if (code != EMPTY_SLOT && (code & LEAF_BIT) && leaf == EMPTY_SLOT) {
           leaf = code;
           code = pop_live(stack, stride, sp, R.far_world * ir.scaling, code_tn);
@@ -735,7 +736,7 @@ struct LaneWalk {
       }
       while (leaf != EMPTY_SLOT) {
         const uint2 lr = __ldg(p.leaves + (leaf & ~LEAF_BIT));
-        if (leaf_triangles<false>(p, R, ir, lr.x, lr.y, gslot, inst_slot, is_opaque, cull_enable, cull_back,
+        if (leaf_triangles<false, BuiltinAnyHit, WT>(p, R, ir, lr.x, lr.y, gslot, inst_slot, is_opaque, cull_enable, cull_back,
                                   prim_start)) {
           code = leaf = EMPTY_SLOT;
           phase = WALK_DONE;  // the search ends (first hit accepted)

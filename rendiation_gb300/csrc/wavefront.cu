@@ -45,7 +45,7 @@ using namespace dev;
 // 2 = at least 9 blocks (56 registers, 36 warps, more spills).
 constexpr int min_blocks(int tier) { return tier == 1 ? 7 : (tier == 2 ? 9 : 0); }
 
-template <int MODE, bool LOCAL, int TIER>
+template <int MODE, bool LOCAL, int TIER, bool WT>
 __global__ void __launch_bounds__(128, min_blocks(TIER)) primary_kernel(TraceParams p, WavefrontParams w) {
   extern __shared__ uint2 smem_stack[];
   uint2 local_stack[LOCAL ? kLocalStackEntries : 1];
@@ -83,7 +83,7 @@ __global__ void __launch_bounds__(128, min_blocks(TIER)) primary_kernel(TracePar
       R.cull_mask = 0xFFu;
       R.ray_flags = 0u;
       bool bad;
-      traverse_ray<MODE, false>(p, R, w.tlas, stack, stride, bad);
+      traverse_ray<MODE, false, BuiltinAnyHit, WT>(p, R, w.tlas, stack, stride, bad);
       PixelResult out;
       out.primary_prim = INVALID_NEXT;
       out.primary_t = R.tmax;
@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(128, min_blocks(TIER)) primary_kernel(TracePar
   }
 }
 
-template <int MODE, bool LOCAL, int TIER>
+template <int MODE, bool LOCAL, int TIER, bool WT>
 __global__ void __launch_bounds__(128, min_blocks(TIER)) secondary_kernel(TraceParams p, WavefrontParams w) {
   extern __shared__ uint2 smem_stack[];
   uint2 local_stack[LOCAL ? kLocalStackEntries : 1];
@@ -165,7 +165,7 @@ __global__ void __launch_bounds__(128, min_blocks(TIER)) secondary_kernel(TraceP
       R.cull_mask = 0xFFu;
       R.ray_flags = shadow ? TF_END_SEARCH : 0u;
       bool bad;
-      traverse_ray<MODE, false>(p, R, w.tlas, stack, stride, bad);
+      traverse_ray<MODE, false, BuiltinAnyHit, WT>(p, R, w.tlas, stack, stride, bad);
       if (shadow) {
         PixelResult* o = w.out + w.shadow_pixel[q];
         o->light = R.best.have ? 2u : 1u;
@@ -197,7 +197,7 @@ __global__ void __launch_bounds__(128, min_blocks(TIER)) secondary_kernel(TraceP
 // 2 of the error word and stops.
 constexpr uint32_t kMaxWarpIterations = 1u << 24;
 
-template <int MODE>
+template <int MODE, bool WT>
 __global__ void __launch_bounds__(128, 8) secondary_dynamic_kernel(TraceParams p, WavefrontParams w) {
   extern __shared__ uint2 smem_stack[];
   constexpr int WIDTH = MODE == MODE_WIDE4 ? 4 : 2;
@@ -213,7 +213,7 @@ __global__ void __launch_bounds__(128, 8) secondary_dynamic_kernel(TraceParams p
   uint2* stack = smem_stack + threadIdx.x;
   const uint32_t stride = blockDim.x;
   const uint32_t threshold = w.refill < 1u ? 1u : (w.refill > 32u ? 32u : w.refill);
-  LaneWalk<WIDTH> L;
+  LaneWalk<WIDTH, WT> L;
   L.reset();
   uint32_t q = 0;
   bool exhausted = false;
@@ -286,14 +286,14 @@ void wavefront_bind_scratch(WavefrontParams& w, void* scratch) {
 }
 
 namespace {
-template <int MODE, bool LOCAL, int TIER>
+template <int MODE, bool LOCAL, int TIER, bool WT>
 cudaError_t launch_wavefront_mode(const TraceParams& p, const WavefrontParams& w, uint32_t block, int sm_count,
                                   uint32_t phases, cudaStream_t stream) {
   const size_t smem = MODE != MODE_THREADED && !LOCAL ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
   static std::atomic<uint64_t> attr_done{0};
   cudaError_t e = raise_smem_limit(
-      attr_done, {(const void*)primary_kernel<MODE, LOCAL, TIER>, (const void*)secondary_kernel<MODE, LOCAL, TIER>,
-                  (const void*)secondary_dynamic_kernel<MODE == MODE_THREADED ? MODE_BINARY : MODE>});
+      attr_done, {(const void*)primary_kernel<MODE, LOCAL, TIER, WT>, (const void*)secondary_kernel<MODE, LOCAL, TIER, WT>,
+                  (const void*)secondary_dynamic_kernel<MODE == MODE_THREADED ? MODE_BINARY : MODE, WT>});
   if (e != cudaSuccess) return e;
   if (phases & 1u) {
     e = cudaMemsetAsync(w.queue_count, 0, 64, stream);
@@ -301,13 +301,13 @@ cudaError_t launch_wavefront_mode(const TraceParams& p, const WavefrontParams& w
     // persistent primary grid: as many resident blocks as fill every SM, or
     // fewer when the frame has fewer 8x4 tiles than resident warps
     int per_sm1 = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm1, primary_kernel<MODE, LOCAL, TIER>, (int)block, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm1, primary_kernel<MODE, LOCAL, TIER, WT>, (int)block, smem);
     if (e != cudaSuccess) return e;
     if (per_sm1 < 1) per_sm1 = 1;
     const uint64_t tiles = (uint64_t)((w.width + 7) / 8) * ((w.height + 3) / 4);
     const uint64_t need = (tiles * 32 + block - 1) / block;
     const uint32_t grid1 = (uint32_t)std::min<uint64_t>((uint64_t)sm_count * per_sm1, need);
-    primary_kernel<MODE, LOCAL, TIER><<<grid1, block, smem, stream>>>(p, w);
+    primary_kernel<MODE, LOCAL, TIER, WT><<<grid1, block, smem, stream>>>(p, w);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
@@ -319,14 +319,14 @@ cudaError_t launch_wavefront_mode(const TraceParams& p, const WavefrontParams& w
   int per_sm = 0;
   constexpr int DMODE = MODE == MODE_THREADED ? MODE_BINARY : MODE;  // the threaded walk has no dynamic form
   if (dynamic)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, secondary_dynamic_kernel<DMODE>, (int)block, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, secondary_dynamic_kernel<DMODE, WT>, (int)block, smem);
   else
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, secondary_kernel<MODE, LOCAL, TIER>, (int)block, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, secondary_kernel<MODE, LOCAL, TIER, WT>, (int)block, smem);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
   const uint32_t grid2 = (uint32_t)(sm_count * per_sm);
-  if (dynamic) secondary_dynamic_kernel<DMODE><<<grid2, block, smem, stream>>>(p, w);
-  else secondary_kernel<MODE, LOCAL, TIER><<<grid2, block, smem, stream>>>(p, w);
+  if (dynamic) secondary_dynamic_kernel<DMODE, WT><<<grid2, block, smem, stream>>>(p, w);
+  else secondary_kernel<MODE, LOCAL, TIER, WT><<<grid2, block, smem, stream>>>(p, w);
   return cudaGetLastError();
 }
 }  // namespace
@@ -341,7 +341,9 @@ cudaError_t launch_wavefront(const TraceParams& p, const WavefrontParams& w, int
   const bool local = w.local_stack && mode != MODE_THREADED && p.stack_depth <= kLocalStackEntries;
   // register tiers apply to the local-stack kernels
   const uint32_t tier = local ? w.register_tier : 0u;
-#define RDN_WF(M, L, T) return launch_wavefront_mode<M, L, T>(p, w, block, sm_count, phases, stream)
+#define RDN_WF(M, L, T)                                                                      \
+  return p.watertight ? launch_wavefront_mode<M, L, T, true>(p, w, block, sm_count, phases, stream) \
+                      : launch_wavefront_mode<M, L, T, false>(p, w, block, sm_count, phases, stream)
   if (mode == MODE_WIDE4) {
     if (!local) RDN_WF(MODE_WIDE4, false, 0);
     if (tier == 1) RDN_WF(MODE_WIDE4, true, 1);

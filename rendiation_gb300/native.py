@@ -26,6 +26,7 @@ EXPORTED_SYMBOLS = [
     "rdn_trace", "rdn_trace_counted", "rdn_wavefront_scratch_size", "rdn_wavefront_shadow_bounce",
     "rdn_wavefront_shadow_bounce_static", "rdn_paths_scratch_size", "rdn_trace_paths", "rdn_trace_paths_graph",
     "rdn_graph_launch", "rdn_graph_destroy", "rdn_attr_loss_forward", "rdn_attr_loss_adjoint",
+    "rdn_hit_diff_forward", "rdn_hit_diff_adjoint",
     "rdn_scan_scratch_size", "rdn_scan_u32", "rdn_compact_scratch_size", "rdn_compact_u32",
     "rdn_radix_sort_scratch_size", "rdn_radix_sort_u32", "rdn_attr_paths_forward", "rdn_attr_paths_adjoint",
     "rdn_attr_paths_graph", "rdn_check_errors", "rdn_set_iteration_limit", "rdn_task_graph_create",
@@ -113,6 +114,14 @@ class AttrLossDesc(C.Structure):
                 ("speculation", C.c_uint32)]
 
 
+class HitDiffDesc(C.Structure):
+    _fields_ = [("rays", C.c_void_p), ("count", C.c_uint32), ("tlas_uniform", C.c_uint32),
+                ("attributes", C.c_void_p), ("hit", C.c_void_p), ("hit_tri", C.c_void_p), ("hit_inst", C.c_void_p),
+                ("grad_hit", C.c_void_p), ("grad_vertices", C.c_void_p), ("grad_ray_origin", C.c_void_p),
+                ("grad_ray_direction", C.c_void_p), ("traversal", C.c_uint32), ("block_size", C.c_uint32),
+                ("from_record", C.c_uint32), ("local_stack", C.c_uint32), ("speculation", C.c_uint32)]
+
+
 class AttrPathDesc(C.Structure):
     _fields_ = [("rays", C.c_void_p), ("tlas_idx", C.c_void_p), ("count", C.c_uint32), ("tlas_uniform", C.c_uint32),
                 ("segments", C.c_uint32), ("seed", C.c_uint32), ("attributes", C.c_void_p), ("targets", C.c_void_p),
@@ -195,6 +204,10 @@ def lib() -> C.CDLL:
     L.rdn_graph_launch.restype = i32
     L.rdn_graph_destroy.argtypes = [vp]
     L.rdn_graph_destroy.restype = i32
+    L.rdn_hit_diff_forward.argtypes = [vp, C.POINTER(HitDiffDesc), vp]
+    L.rdn_hit_diff_forward.restype = i32
+    L.rdn_hit_diff_adjoint.argtypes = [vp, C.POINTER(HitDiffDesc), vp]
+    L.rdn_hit_diff_adjoint.restype = i32
     L.rdn_attr_loss_forward.argtypes = [vp, C.POINTER(AttrLossDesc), vp]
     L.rdn_attr_loss_forward.restype = i32
     L.rdn_attr_loss_adjoint.argtypes = [vp, C.POINTER(AttrLossDesc), vp]

@@ -17,6 +17,7 @@ PAIRS = [
     ("rdn_build_stats", native.BuildStats), ("rdn_trace_desc", native.TraceDesc), ("rdn_counters", native.Counters),
     ("rdn_camera", native.Camera), ("rdn_wavefront_desc", native.WavefrontDesc), ("rdn_path_desc", native.PathDesc),
     ("rdn_attr_loss_desc", native.AttrLossDesc), ("rdn_attr_path_desc", native.AttrPathDesc),
+    ("rdn_hit_diff_desc", native.HitDiffDesc),
     ("rdn_task_group_desc", native.TaskGroupDesc), ("rdn_ao_desc", native.AoDesc),
 ]
 
