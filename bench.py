@@ -8,22 +8,34 @@ cosine-weighted diffuse bounce ray. One step = one frame of the wavefront
 executor (rdn_wavefront_shadow_bounce). Metric: Mrays/s over all rays traced.
 
 Further legs, each a key of the same JSON line (skipped with --no-<leg>):
+  parity           every ray of the timed frame (and of the plain soup, and of
+                   the watertight frame) classified against the oracle:
+                   identical / exact-distance tie / NaN-exposed / edge / other;
+  watertight       the frame with the watertight triangle test;
+  plain_soup10k    the plain closest-hit configuration (10k soup, 256^2 rays);
+  accuracy_vs_fp64 FP32 results against FP64 (same triangle, brute force);
+  ao, task_graph   the AO renderer and the device task graph;
   batched          256 triangle soups, up to 4 diffuse bounces with Russian
                    roulette, one persistent launch per bounce in a CUDA graph,
-                   against the plain per-scene launch loop;
+                   against the plain per-scene launch loop (same tuned knobs);
   adjoint          256x256 heightfield, 512x512 rays, attribute loss: forward
-                   and forward + adjoint;
+                   and forward + adjoint, gradient error against FP64;
   batched_adjoint  64 heightfields, primaries + 2 bounces, forward + adjoint in
                    one graph, gradient error against FP64;
-  cpu_baseline     the oracle's pipeline on the host cores (rank 0 only).
+  cpu_baseline     the oracle's pipeline on the host cores (rank 0 only);
+  headline         the metric's figures in one place.
 
 --impl reference times the reference's CPU path for the same workload: the
 oracle (a C++ restatement of the reference's CPU traversal, the Rust reference
 cannot be built here) on all host cores over a bounded sample of the frame.
 
-Multi-GPU: rays and frames are independent, so N ranks run N replicas of the
-workload (weak scaling, no collective on the data path); the timed region is
-bracketed by barriers and the max over ranks is reported.
+Multi-GPU (rendiation_gb300.partition): the frame is split into row bands, one
+per GPU (strong scaling: `value` is one frame's rays over the slowest rank's
+time); the batched legs split their scenes across GPUs balanced by triangles x
+rays; the single-scene adjoint splits its rays and sums the vertex gradients
+with one all-reduce after the backward. No other collective touches the data
+path; the timed regions are bracketed by barriers and the max over ranks is
+reported.
 """
 
 from __future__ import annotations
@@ -122,6 +134,17 @@ def max_over_ranks(seconds: float, ws: int, device) -> float:
     t = torch.tensor([seconds], dtype=torch.float64, device=device)
     torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
     return float(t.item())
+
+
+def sum_over_ranks(count: int, ws: int) -> int:
+    """Sum of an integer over the ranks (the rank's own value when alone)."""
+    if ws <= 1:
+        return int(count)
+    import torch
+
+    t = torch.tensor([int(count)], dtype=torch.int64, device="cuda" if torch.cuda.is_available() else "cpu")
+    torch.distributed.all_reduce(t)
+    return int(t.item())
 
 
 def replicas_value(rays_per_step: int, steps: int, ws: int, seconds: float) -> float:
@@ -230,7 +253,12 @@ def bench_wavefront(args, ws, rank):
     cam = scenes.heightfield_camera(W, H)
     traversal = {"reference": rt.TRAVERSAL_REFERENCE, "wide": rt.TRAVERSAL_ORDERED_WIDE}.get(
         args.traversal, rt.TRAVERSAL_ORDERED)
-    wf = rt.Wavefront(P, cam, LIGHT, traversal=traversal, block_size=args.block)
+    # N GPUs split the frame into row bands (rendiation_gb300.partition): each
+    # rank traces its band with the whole frame's rays and samplers
+    from rendiation_gb300.partition import row_bands
+
+    band = row_bands(H, ws)[rank]
+    wf = rt.Wavefront(P, cam, LIGHT, traversal=traversal, block_size=args.block, rows=band)
     stream = torch.cuda.current_stream()
     tuned = None
     if args.tune and args.traversal == "ordered":
@@ -323,13 +351,15 @@ def bench_wavefront(args, ws, rank):
     frame_ms = total_ms / args.steps
     elapsed = total_ms / 1000.0
     elapsed = max_over_ranks(elapsed, ws, "cuda")
-    value = replicas_value(rays_per_step, args.steps, ws, elapsed)
+    # whole-job rays of one frame: the bands' rays summed over ranks
+    frame_rays = sum_over_ranks(rays_per_step, ws)
+    value = frame_rays * args.steps / elapsed / 1e6
 
     # e2e through the C ABI: every step launches its frame and reads all of its
     # pixel records back into pinned host memory. Two output buffers: the copy
     # of frame k (copy stream) overlaps frame k+1 (compute stream); frame k+2
     # waits for that copy before it overwrites the buffer.
-    wf2 = rt.Wavefront(P, cam, LIGHT, traversal=traversal, block_size=args.block)
+    wf2 = rt.Wavefront(P, cam, LIGHT, traversal=traversal, block_size=args.block, rows=band)
     if wf.phase_config is not None:
         wf2.configure(*wf.phase_config, refill=wf.desc.refill)
     else:
@@ -359,7 +389,8 @@ def bench_wavefront(args, ws, rank):
     t0 = time.perf_counter()
     e2e_steps(400, args.steps)
     e2e_s = time.perf_counter() - t0
-    e2e_value = rays_per_step * args.steps / e2e_s / 1e6
+    e2e_s = max_over_ranks(e2e_s, ws, "cuda")
+    e2e_value = frame_rays * args.steps / e2e_s / 1e6
     d2h = int(wf.out.numel() * 4)
     h2d = C.sizeof(wf.desc)
 
@@ -378,14 +409,15 @@ def bench_wavefront(args, ws, rank):
         "warmup": args.warmup,
         "ms_per_step": round(frame_ms, 4),
         "higher_is_better": True,
-        "scaling": "weak",
+        "scaling": "strong",
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded heightfield, PCG64 seed 1)",
         "config": {
             "workload": f"wavefront primary+shadow+bounce, heightfield {args.grid}^2 "
                         f"({mesh.triangle_count} tris, SAH <=4/leaf), {W}x{H} primaries",
-            "rays_per_step": rays_per_step,
+            "rays_per_step": frame_rays,
+            "partition": f"{ws} row band(s) of the frame, one per GPU (strong scaling: one frame per step)",
             "rays_primary": n_prim, "rays_shadow": n_sh, "rays_bounce": n_bo,
             "traversal": args.traversal,
             "autotuned": tuned,
@@ -887,7 +919,7 @@ def bench_task_graph(args, P):
             "plain_launches_ms": round(plain_ms, 3), "plain_launches_mtasks_per_s": round(tasks / plain_ms / 1e3, 1)}
 
 
-def bench_batched(args):
+def bench_batched(args, ws=1, rank=0):
     """Batched multi-scene paths: 256 soups (log-uniform 1k..200k triangles),
     log-uniform 4k..256k rays per scene, <= 4 diffuse bounces with Russian
     roulette from bounce 2. One persistent launch per bounce for all scenes,
@@ -902,6 +934,11 @@ def bench_batched(args):
     from rendiation_gb300 import scenes
 
     b = scenes.batched_soups(n_scenes=args.scenes)
+    if ws > 1:  # each GPU takes a share of the scenes balanced by triangles x rays
+        from rendiation_gb300 import partition
+
+        costs = partition.scene_costs([m.triangle_count for m in b.meshes], np.diff(b.ray_offsets))
+        b = partition.batch_subset(b, partition.balanced_scenes(costs, ws)[rank])
     P = rt.AccelerationStructureSystem(device=0)
     for m in b.meshes:
         P.create_bottom_level_acceleration_structure([rt.BottomLevelAccelerationStructureBuildSource(m.positions)])
@@ -999,7 +1036,12 @@ def bench_batched(args):
     plain_ms = e0.elapsed_time(e1) / reps
     # per-scene seeds equal the batched ones only when ids match: compare statistics, not records
     total = int(sum(segs))
+    if ws > 1:  # whole-job figures: segments of every rank's scenes over the slowest rank
+        total = sum_over_ranks(total, ws)
+        batched_ms = max_over_ranks(batched_ms / 1e3, ws, "cuda") * 1e3
+        plain_ms = max_over_ranks(plain_ms / 1e3, ws, "cuda") * 1e3
     return {
+        "ranks": ws,
         "workload": f"{len(b.meshes)} soups, {sum(m.triangle_count for m in b.meshes)} tris, "
                     f"{b.rays.shape[0]} primaries, <=4 bounces, roulette p=0.5 from bounce 2",
         "segments_per_step": total,
@@ -1016,7 +1058,7 @@ def bench_batched(args):
     }
 
 
-def bench_adjoint(args):
+def bench_adjoint(args, ws=1, rank=0):
     """Differentiable closest hit: heightfield 256^2 (130,050 tris) with a
     per-vertex attribute uniform in [0,1], 512x512 primary rays, loss =
     sum (interpolated attribute - target)^2 with the target rendered from a
@@ -1038,8 +1080,14 @@ def bench_adjoint(args):
     rng = np.random.Generator(np.random.PCG64(17))
     attr = torch.from_numpy(rng.random(mesh.positions.shape[0]).astype(np.float32)).cuda()
     cam = scenes.PinholeCamera.look_at((0.5, -0.5, 0.8), (0.5, 0.5, 0.0), 20.0, res, res)
-    rays = torch.from_numpy(scenes.pinhole_rays(cam).view(np.float32).reshape(-1, 8).copy()).cuda()
-    n = res * res
+    rays_np = scenes.pinhole_rays(cam)
+    if ws > 1:  # each GPU takes a row band of the rays; vertex gradients are summed across GPUs
+        from rendiation_gb300.partition import row_bands
+
+        r0, r1 = row_bands(res, ws)[rank]
+        rays_np = np.ascontiguousarray(rays_np[r0 * res:r1 * res])
+    rays = torch.from_numpy(rays_np.view(np.float32).reshape(-1, 8).copy()).cuda()
+    n = rays_np.shape[0]
     traversal = {"reference": rt.TRAVERSAL_REFERENCE, "wide": rt.TRAVERSAL_ORDERED_WIDE}.get(
         args.traversal, rt.TRAVERSAL_ORDERED)
 
@@ -1100,6 +1148,10 @@ def bench_adjoint(args):
         if mode != "forward":
             grad.zero_()
             assert L.rdn_attr_loss_adjoint(P._h, C.byref(adj_rec if mode == "tape" else adj), sp) == 0
+            if ws > 1:
+                from rendiation_gb300.partition import sum_gradients
+
+                sum_gradients(grad)  # one all-reduce after the backward
 
     out = {}
     for name, w in (("forward", "forward"), ("forward_adjoint", "tape"), ("forward_adjoint_retrace", "retrace")):
@@ -1123,9 +1175,10 @@ def bench_adjoint(args):
     assert L.rdn_attr_loss_forward(P._h, C.byref(fwd_rec), sp) == 0
     assert L.rdn_attr_loss_adjoint(P._h, C.byref(adj_rec), sp) == 0
     torch.cuda.synchronize()
-    out["gradient_error"] = attr_loss_gradient_error(
-        mesh, attr.cpu().numpy(), scenes.pinhole_rays(cam), target.cpu().numpy(),
-        hit_tri.cpu().numpy().view(np.uint32), grad.cpu().numpy())
+    if ws == 1:  # (with several GPUs the gradient is the sum over every rank's rays)
+        out["gradient_error"] = attr_loss_gradient_error(
+            mesh, attr.cpu().numpy(), rays_np, target.cpu().numpy(), hit_tri.cpu().numpy().view(np.uint32),
+            grad.cpu().numpy())
     out["local_stack"], out["speculation"] = local, spec
     out["loss"] = float(loss.item())
     out["workload"] = f"heightfield {n_grid}^2 ({mesh.triangle_count} tris), {res}x{res} rays, attribute loss"
@@ -1231,7 +1284,7 @@ def attr_loss_gradient_error(mesh, attr, rays, targets, tri, grad, n_vertices=64
     }
 
 
-def bench_batched_adjoint(args):
+def bench_batched_adjoint(args, ws=1, rank=0):
     """Batched differentiable paths: 64 heightfields with vertex grids
     log-uniform in [64^2, 512^2] (octaves seeded per scene), each with a
     per-vertex attribute and 64k..1M primary rays (log-uniform) plus 2 diffuse
@@ -1254,9 +1307,14 @@ def bench_batched_adjoint(args):
     n_scenes, seg = args.diff_scenes, 3
     grids = np.sqrt(scenes.log_uniform_ints(n_scenes, 64 * 64, 512 * 512, 31)).astype(np.int64)
     nrays = scenes.log_uniform_ints(n_scenes, 64_000, 1_000_000, 32)
-    meshes = [scenes.heightfield(int(g), seed=100 + k) for k, g in enumerate(grids)]
-    jitter = [scenes.heightfield(int(g), seed=100 + k, jitter_sigma=0.005, jitter_seed=7000 + k)
-              for k, g in enumerate(grids)]
+    ids = list(range(n_scenes))
+    if ws > 1:  # each GPU takes a share of the scenes balanced by triangles x rays
+        from rendiation_gb300 import partition
+
+        ids = partition.balanced_scenes(partition.scene_costs(2 * (grids - 1) ** 2, nrays), ws)[rank]
+    meshes = [scenes.heightfield(int(grids[k]), seed=100 + k) for k in ids]
+    jitter = [scenes.heightfield(int(grids[k]), seed=100 + k, jitter_sigma=0.005, jitter_seed=7000 + k) for k in ids]
+    grids, nrays, n_scenes = grids[ids], nrays[ids], len(ids)
 
     def system(ms):
         P = rt.AccelerationStructureSystem(device=0)
@@ -1575,7 +1633,7 @@ def run_reference(args, ws, rank):
         "warmup": args.warmup,
         "ms_per_step": round(total_s * 1000.0 / args.steps, 3),
         "higher_is_better": True,
-        "scaling": "weak",
+        "scaling": "strong",
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded heightfield, PCG64 seed 1)",
@@ -1676,11 +1734,11 @@ def main():
         out["task_graph"] = bench_task_graph(args, P)
     if not args.no_batched:
         P.close()
-        out["batched"] = bench_batched(args)
+        out["batched"] = bench_batched(args, ws, rank)
     if not args.no_adjoint:
-        out["adjoint"] = bench_adjoint(args)
+        out["adjoint"] = bench_adjoint(args, ws, rank)
     if not args.no_batched_adjoint:
-        out["batched_adjoint"] = bench_batched_adjoint(args)
+        out["batched_adjoint"] = bench_batched_adjoint(args, ws, rank)
     if rank == 0:
         if not args.no_cpu_baseline:
             cb, _ = cpu_baseline_wavefront(S_field, cam, os.cpu_count() or 1, budget_s=args.cpu_budget)

@@ -354,6 +354,11 @@ typedef struct rdn_wavefront_desc {
                                 fewer resident warps), 2 = 56 (more warps, more spills) */
   uint32_t speculation;      /* ordered walks: a lane holding a leaf keeps descending while more than
                                 this many lanes of its warp still look for one (0 = until all have one) */
+  uint32_t row_offset;       /* a band of a taller frame: camera.height rows starting at row_offset of a */
+  uint32_t frame_height;     /* frame of frame_height rows (0 = camera.height: the whole frame). Camera
+                                rays and samplers are those of the whole frame's rows, so bands that
+                                tile a frame (one per GPU) give exactly its pixel records; out holds
+                                the band's width x camera.height records */
 } rdn_wavefront_desc;
 
 /* Scratch size for the secondary-ray queues of a width x height launch. */

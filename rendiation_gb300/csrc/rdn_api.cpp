@@ -279,6 +279,9 @@ rdn_status wavefront_check_knobs(rdn_ctx* c, const rdn_wavefront_desc* d) {
   if (d->speculation > 31) return fail(c, RDN_ERR_INVALID_ARG, "speculation must be 0..31");
   if (d->block_size && (d->block_size % 32 || d->block_size > 128))
     return fail(c, RDN_ERR_INVALID_ARG, "block_size must be a multiple of 32 up to 128");
+  const uint64_t fh = d->frame_height ? d->frame_height : d->camera.height;
+  if ((uint64_t)d->row_offset + d->camera.height > fh)
+    return fail(c, RDN_ERR_INVALID_ARG, "row_offset + camera.height exceeds frame_height");
   return RDN_OK;
 }
 
@@ -309,6 +312,8 @@ void wavefront_fill(rdn_ctx* c, const rdn_wavefront_desc* d, rdn::TraceParams& p
   w.refill = d->refill;
   w.local_stack = d->local_stack;
   w.register_tier = d->register_tier;
+  w.row0 = d->row_offset;
+  w.frame_height = d->frame_height ? d->frame_height : d->camera.height;
   p.spec_threshold = d->speculation;
 }
 

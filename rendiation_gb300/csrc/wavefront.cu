@@ -71,7 +71,7 @@ __global__ void __launch_bounds__(128, min_blocks(TIER)) primary_kernel(TracePar
     if (valid) {
       // camera ray (pixel centre), the same f32 steps as the host generator
       const float sx = (((float)px + 0.5f) / (float)w.width * 2.0f - 1.0f) * w.tan_half * w.aspect;
-      const float sy = (1.0f - ((float)py + 0.5f) / (float)w.height * 2.0f) * w.tan_half;
+      const float sy = (1.0f - ((float)(py + w.row0) + 0.5f) / (float)w.frame_height * 2.0f) * w.tan_half;
       const float3 d = normalize3(make_float3((w.forward.x + sx * w.right.x) + sy * w.up.x,
                                               (w.forward.y + sx * w.right.y) + sy * w.up.y,
                                               (w.forward.z + sx * w.right.z) + sy * w.up.z));
@@ -108,7 +108,7 @@ __global__ void __launch_bounds__(128, min_blocks(TIER)) primary_kernel(TracePar
         dist = sqrtf(dist2);
         ldir = normalize3(L);
         out.direct = fmaxf(0.0f, dot3(nf, ldir)) / dist2;  // kept only if the light is visible
-        uint32_t state = xxhash32(px, py, w.sample_index * 3u);
+        uint32_t state = xxhash32(px, py + w.row0, w.sample_index * 3u);
         const float s0 = sample_next(state);
         const float s1 = sample_next(state);
         bdir = cosine_sample_in_dir(nf, s0, s1);

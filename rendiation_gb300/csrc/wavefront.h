@@ -43,6 +43,8 @@ struct WavefrontParams {
   uint32_t local_stack;
   // register budget of the local-stack kernels: 0 default (64), 1 = 72, 2 = 56
   uint32_t register_tier;
+  // the launch covers rows [row0, row0 + height) of a frame of frame_height rows
+  uint32_t row0, frame_height;
 };
 
 size_t wavefront_scratch_bytes(uint32_t width, uint32_t height);

@@ -255,10 +255,20 @@ class Wavefront:
     torch CUDA tensors."""
 
     def __init__(self, system: AccelerationStructureSystem, camera, light, traversal=TRAVERSAL_ORDERED,
-                 tlas_uniform=0, block_size=0, refill=0):
+                 tlas_uniform=0, block_size=0, refill=0, rows=None):
+        """rows: (row0, row1), a band of the camera's frame: the launch traces
+        rows [row0, row1) with the whole frame's rays and samplers."""
+        import dataclasses
+
         import torch
 
         self.system = system
+        self.frame_camera = camera
+        row0, row1 = rows if rows is not None else (0, camera.height)
+        if not (0 <= row0 <= row1 <= camera.height):
+            raise ValueError(f"band {rows} outside the frame's {camera.height} rows")
+        self.rows = (row0, row1)
+        camera = dataclasses.replace(camera, height=row1 - row0)
         self.camera = camera
         self.n = camera.width * camera.height
         size = C.c_size_t()
@@ -280,6 +290,8 @@ class Wavefront:
         self.desc.scratch_bytes = size.value
         self.desc.ray_counts = self.ray_counts.data_ptr()
         self.desc.refill = refill
+        self.desc.row_offset = row0
+        self.desc.frame_height = self.frame_camera.height
         self.phase_config = None  # (primary, secondary) (traversal, block) when they differ
 
     def configure(self, primary, secondary, refill=None):
