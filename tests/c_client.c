@@ -1,14 +1,19 @@
 /* A host program that uses the library through its C ABI only (include/rdn.h
  * plus the CUDA runtime for device buffers), the way a Rust, Go or C++ host
  * binds it: one triangle geometry, one identity instance, a build, one batch
- * trace, results written to a file.
+ * trace and, when a frame file is given, one frame of the path tracer's first
+ * bounce (rdn_wavefront_shadow_bounce), results written to a file.
  *
- *   c_client <input> <output> <traversal> <device_build>
+ *   c_client <input> <output> <traversal> <device_build> [<frame>]
  *
  * input:  u32 vertex_count, u32 index_count (0 = non-indexed), u32 ray_count,
  *         f32 positions[3 * vertex_count], u32 indices[index_count],
  *         f32 rays[8 * ray_count] (org, tmin, dir, tmax)
- * output: rdn_hit[ray_count], rdn_hit_ext[ray_count], u32 error_flags
+ * frame:  u32 width, u32 height, u32 sample_index, f32 camera[14] (origin,
+ *         forward, right, up, tan_half, aspect), f32 light[3]
+ * output: rdn_hit[ray_count], rdn_hit_ext[ray_count], u32 error_flags, and with
+ *         a frame: rdn_pixel_result[width * height], u32 rays[3] (primary,
+ *         shadow, bounce), u32 error_flags
  *
  * Exit codes: 0 ok, 1 usage or file error, 2 an rdn_* call failed (its status
  * and rdn_last_error are printed), 3 a CUDA runtime call failed. */
@@ -41,8 +46,8 @@ static rdn_ctx* ctx = NULL;
 static int read_all(FILE* f, void* dst, size_t bytes) { return bytes == 0 || fread(dst, 1, bytes, f) == bytes; }
 
 int main(int argc, char** argv) {
-  if (argc != 5) {
-    fprintf(stderr, "usage: %s <input> <output> <traversal> <device_build>\n", argv[0]);
+  if (argc != 5 && argc != 6) {
+    fprintf(stderr, "usage: %s <input> <output> <traversal> <device_build> [<frame>]\n", argv[0]);
     return 1;
   }
   const uint32_t traversal = (uint32_t)atoi(argv[3]);
@@ -118,6 +123,58 @@ int main(int argc, char** argv) {
   fwrite(hits, sizeof(rdn_hit), nr, out);
   fwrite(ext, sizeof(rdn_hit_ext), nr, out);
   fwrite(&flags, 4, 1, out);
+
+  if (argc == 6) {
+    /* one frame of the path tracer's first bounce: caller-owned scratch sized by the library */
+    FILE* fr = fopen(argv[5], "rb");
+    if (!fr) return 1;
+    uint32_t fh[3];
+    float cam[14], light[3];
+    if (!read_all(fr, fh, sizeof fh) || !read_all(fr, cam, sizeof cam) || !read_all(fr, light, sizeof light))
+      return 1;
+    fclose(fr);
+    const size_t npix = (size_t)fh[0] * fh[1];
+    size_t scratch_bytes = 0;
+    CHECK(rdn_wavefront_scratch_size(fh[0], fh[1], &scratch_bytes));
+    void* d_scratch = NULL;
+    rdn_pixel_result* d_out = NULL;
+    uint32_t* d_counts = NULL;
+    CUCHECK(cudaMalloc(&d_scratch, scratch_bytes));
+    CUCHECK(cudaMalloc((void**)&d_out, sizeof(rdn_pixel_result) * npix + 32));
+    CUCHECK(cudaMalloc((void**)&d_counts, 16));
+    rdn_wavefront_desc w;
+    memset(&w, 0, sizeof w);
+    memcpy(w.camera.origin, cam, 12);
+    memcpy(w.camera.forward, cam + 3, 12);
+    memcpy(w.camera.right, cam + 6, 12);
+    memcpy(w.camera.up, cam + 9, 12);
+    w.camera.tan_half = cam[12];
+    w.camera.aspect = cam[13];
+    w.camera.width = fh[0];
+    w.camera.height = fh[1];
+    memcpy(w.light, light, 12);
+    w.sample_index = fh[2];
+    w.traversal = traversal;
+    w.out = d_out;
+    w.scratch = d_scratch;
+    w.scratch_bytes = scratch_bytes;
+    w.ray_counts = d_counts;
+    CHECK(rdn_wavefront_shadow_bounce(ctx, &w, NULL));
+    uint32_t wflags = 0;
+    CHECK(rdn_check_errors(ctx, NULL, &wflags));
+    rdn_pixel_result* px = (rdn_pixel_result*)malloc(sizeof(rdn_pixel_result) * npix + 32);
+    uint32_t counts[3];
+    if (!px) return 1;
+    CUCHECK(cudaMemcpy(px, d_out, sizeof(rdn_pixel_result) * npix, cudaMemcpyDeviceToHost));
+    CUCHECK(cudaMemcpy(counts, d_counts, sizeof counts, cudaMemcpyDeviceToHost));
+    fwrite(px, sizeof(rdn_pixel_result), npix, out);
+    fwrite(counts, 4, 3, out);
+    fwrite(&wflags, 4, 1, out);
+    free(px);
+    cudaFree(d_scratch);
+    cudaFree(d_out);
+    cudaFree(d_counts);
+  }
   fclose(out);
 
   cudaFree(d_rays);

@@ -91,3 +91,41 @@ def test_client_traces_like_the_oracle(tmp_path, traversal, device_build, cuda):
         same = (prim == expect["prim"]) | (hits[:, 0] == expect["t"])
         assert same.all()
     assert (expect["prim"] != orc.MISS).mean() > 0.3
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("traversal", [rt.TRAVERSAL_REFERENCE, rt.TRAVERSAL_ORDERED_WIDE])
+def test_client_renders_a_wavefront_frame_like_the_oracle(tmp_path, traversal, cuda):
+    """The encoder-side entry point through the C ABI alone: one frame of the
+    path tracer's first bounce (primary, shadow, bounce) with caller-owned
+    scratch; reference order equals the oracle's pipeline bit for bit."""
+    exe = compile_client(tmp_path)
+    mesh = scenes.heightfield(64, seed=2)
+    rays = scenes.pinhole_rays(scenes.heightfield_camera(16, 8))
+    write_input(tmp_path / "in.bin", mesh, rays)
+    cam = scenes.heightfield_camera(96, 64)
+    light = (0.2, 0.2, 2.0)
+    with open(tmp_path / "frame.bin", "wb") as f:
+        f.write(struct.pack("<III", cam.width, cam.height, 9))
+        f.write(np.asarray(cam.as_floats(), np.float32).tobytes())
+        f.write(np.asarray(light, np.float32).tobytes())
+    r = subprocess.run([exe, str(tmp_path / "in.bin"), str(tmp_path / "out.bin"), str(traversal), "1",
+                        str(tmp_path / "frame.bin")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    raw = open(tmp_path / "out.bin", "rb").read()
+    off = 32 * rays.shape[0] + 4
+    npix = cam.width * cam.height
+    got = np.frombuffer(raw[off:off + 32 * npix], rt.PIXEL_DTYPE)
+    counts = np.frombuffer(raw[off + 32 * npix:off + 32 * npix + 12], np.uint32)
+    flags = struct.unpack("<I", raw[off + 32 * npix + 12:off + 32 * npix + 16])[0]
+    assert flags == 0
+    S = single_mesh_scene(mesh).build_oracle()
+    exp, n_rays, _ = orc.wavefront_shadow_bounce(S, cam.as_floats(), cam.width, cam.height, light, 9, threads=8)
+    assert [int(x) for x in counts] == n_rays
+    if traversal == rt.TRAVERSAL_REFERENCE:
+        for f in exp.dtype.names:
+            assert np.array_equal(got[f].view(np.uint32), exp[f].view(np.uint32)), f
+    else:
+        from oracle import parity
+
+        assert parity.classify_wavefront(S, cam, cam.width, cam.height, light, got, exp, 9, threads=8)["other"] == 0
