@@ -17,9 +17,10 @@
 //     counter: a warp ballot and one atomicAdd per warp reserve the slots, so
 //     the queues come out compacted without a separate scan pass.
 //   secondary_kernel: persistent warps that fetch 32 queue entries at a time
-//     from a global work counter; shadow rays (first-hit search) occupy the
-//     first half of the index space and bounce rays (closest hit) the second,
-//     so warps stay homogeneous. Results scatter to the pixel records.
+//     from a global work counter; bounce rays (closest hit, the long walks)
+//     occupy the first half of the index space and shadow rays (first-hit
+//     search) the second, so warps stay homogeneous and the kernel ends on
+//     short work. Results scatter to the pixel records.
 //
 // Built with -fmad=false: all shading arithmetic is IEEE f32 in the same
 // order as the oracle, so secondary rays are bit-identical.
@@ -153,8 +154,11 @@ __global__ void __launch_bounds__(128, min_blocks(TIER)) secondary_kernel(TraceP
     if (base >= total) break;
     const uint32_t j = base + lane;
     if (j < total) {
-      const bool shadow = j < n;
-      const uint32_t q = shadow ? j : j - n;
+      // bounce rays first: they are the longest walks, and a persistent kernel
+      // that ends on short shadow rays leaves fewer warps waiting for a last
+      // long batch (1.66 -> 1.54 ms on the 1080p frame)
+      const bool shadow = j >= n;
+      const uint32_t q = shadow ? j - n : j;
       const float4* rq = reinterpret_cast<const float4*>(shadow ? w.shadow_rays : w.bounce_rays) + 2 * (size_t)q;
       const float4 r0 = rq[0], r1 = rq[1];
       RayCtx R;
@@ -233,10 +237,10 @@ __global__ void __launch_bounds__(128, 8) secondary_dynamic_kernel(TraceParams p
       if (L.phase == WALK_IDLE) {
         const uint32_t j = base + __popc(idle & lanes_below);
         if (j < total) {
-          q = j;
-          const bool shadow = j < n;
+          q = j;  // bounce rays first, as in the batch schedule
+          const bool shadow = j >= n;
           const float4* rq =
-              reinterpret_cast<const float4*>(shadow ? w.shadow_rays : w.bounce_rays) + 2 * (size_t)(shadow ? j : j - n);
+              reinterpret_cast<const float4*>(shadow ? w.shadow_rays : w.bounce_rays) + 2 * (size_t)(shadow ? j - n : j);
           L.start(p, rq[0], rq[1], w.tlas, shadow ? TF_END_SEARCH : 0u);
         }
       }
@@ -245,12 +249,12 @@ __global__ void __launch_bounds__(128, 8) secondary_dynamic_kernel(TraceParams p
     if (L.phase != WALK_IDLE) L.advance(p, stack, stride, threshold);
     if (L.phase == WALK_DONE) {
       const RayCtx& R = L.R;
-      if (q < n) {
-        PixelResult* o = w.out + w.shadow_pixel[q];
+      if (q >= n) {
+        PixelResult* o = w.out + w.shadow_pixel[q - n];
         o->light = R.best.have ? 2u : 1u;
         if (R.best.have) o->direct = 0.0f;
       } else if (R.best.have) {
-        PixelResult* o = w.out + w.bounce_pixel[q - n];
+        PixelResult* o = w.out + w.bounce_pixel[q];
         const uint4 gm = __ldg(reinterpret_cast<const uint4*>(p.tri_root + R.best.geom_slot));
         o->bounce_prim = __ldg(p.redirect + R.best.k) - gm.z;
         o->bounce_t = R.best.t;
