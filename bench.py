@@ -57,6 +57,15 @@ LIGHT = (0.2, 0.2, 2.0)
 METRIC = "Mrays/s closest-hit: batched & fwd+adjoint vs plain, at stated FP64 error"
 
 
+def algorithmic_roofline(alg_bytes: float, ms: float, basis: str) -> dict:
+    """The HBM roofline figure of one launch (or graph): algorithmic bytes over
+    its device time, against the measured HBM peak."""
+    peak, kind = measured_peak_gbs()
+    gbs = alg_bytes / (ms / 1e3) / 1e9
+    return {"bound": "hbm", "achieved": round(gbs, 1), "peak": peak, "unit": "GB/s", "frac": round(gbs / peak, 4),
+            "algorithmic_bytes": int(alg_bytes), "ms": round(ms, 4), "peak_kind": kind, "basis": basis}
+
+
 def node_bytes_per_ray(counts: dict, n: int) -> float:
     """Algorithmic bytes per ray: 32 (ray in) + 16 (hit out) + 48 per node visit
     + 36 per triangle test, visits and tests counted in the reference's traversal
@@ -1036,6 +1045,12 @@ def bench_batched(args, ws=1, rank=0):
     plain_ms = e0.elapsed_time(e1) / reps
     # per-scene seeds equal the batched ones only when ids match: compare statistics, not records
     total = int(sum(segs))
+    # roofline estimate: the primaries' reference-order fetches per ray (the
+    # path executor records no bounce rays), applied to every segment
+    h4 = torch.empty((rays.shape[0], 4), device="cuda")
+    c_prim = P.trace_counted(rays, h4, tlas_idx=tidx, traversal=rt.TRAVERSAL_REFERENCE)
+    b_prim = node_bytes_per_ray(c_prim, rays.shape[0])
+    del h4
     if ws > 1:  # whole-job figures: segments of every rank's scenes over the slowest rank
         total = sum_over_ranks(total, ws)
         batched_ms = max_over_ranks(batched_ms / 1e3, ws, "cuda") * 1e3
@@ -1051,6 +1066,9 @@ def bench_batched(args, ws=1, rank=0):
         "plain_loop_mrays": round(total / (plain_ms / 1e3) / 1e6, 2),
         "plain_loop_ms": round(plain_ms, 3),
         "speedup_vs_plain_loop": round(plain_ms / batched_ms, 3),
+        "roofline": {"batched_graph": algorithmic_roofline(
+            total * b_prim, batched_ms, "estimate: every segment costed at the primaries' mean reference-order fetches "
+            f"({b_prim:.0f} B per ray)")},
         "plain_loop_knobs": plain_knobs,
         "build": build,
         "escaped_fraction": round(float(np.mean(res_batched["depth_flags"] >> 31)), 4),
@@ -1175,6 +1193,21 @@ def bench_adjoint(args, ws=1, rank=0):
     assert L.rdn_attr_loss_forward(P._h, C.byref(fwd_rec), sp) == 0
     assert L.rdn_attr_loss_adjoint(P._h, C.byref(adj_rec), sp) == 0
     torch.cuda.synchronize()
+    # roofline: the reference order's fetches for these rays; the adjoint adds
+    # the 48 B float4 atomic scatter to three corners per hit
+    hits4 = torch.empty((n, 4), device="cuda")
+    c_ref = P.trace_counted(rays, hits4, traversal=rt.TRAVERSAL_REFERENCE)
+    b_ray = node_bytes_per_ray(c_ref, n) + 4.0  # + the attribute read
+    n_hit = int((hit_tri.cpu().numpy().view(np.uint32) != 0xFFFFFFFF).sum())
+    out["roofline"] = {
+        "forward": algorithmic_roofline(n * b_ray, out["forward_ms"],
+                                        "per ray 32 + 16 + 48 x node visits + 36 x triangle tests of the reference "
+                                        "order, + 4 B attribute"),
+        "forward_adjoint_retrace": algorithmic_roofline(2 * n * b_ray + 48.0 * n_hit, out["forward_adjoint_retrace_ms"],
+                                                        "forward twice (the adjoint traces again) + 48 B of atomic "
+                                                        "scatter per hit"),
+        "bytes_per_ray": round(b_ray, 1),
+    }
     if ws == 1:  # (with several GPUs the gradient is the sum over every rank's rays)
         out["gradient_error"] = attr_loss_gradient_error(
             mesh, attr.cpu().numpy(), rays_np, target.cpu().numpy(), hit_tri.cpu().numpy().view(np.uint32),
@@ -1419,12 +1452,25 @@ def bench_batched_adjoint(args, ws=1, rank=0):
     del tape_tri, tape_inst, tape_rays
     # segments traced per step (one forward pass records the segment triangles)
     seg_tri = torch.zeros(n * seg, dtype=torch.int32, device="cuda")
-    assert L.rdn_attr_paths_forward(P._h, C.byref(desc(seg_tri=seg_tri.data_ptr())), None) == 0
+    seg_rays = torch.zeros((n * seg, 8), device="cuda")
+    assert L.rdn_attr_paths_forward(P._h, C.byref(desc(seg_tri=seg_tri.data_ptr(), seg_rays=seg_rays.data_ptr())),
+                                    None) == 0
     torch.cuda.synchronize()
     tri_all = seg_tri.cpu().numpy().view(np.uint32).reshape(-1, seg)
     # a segment is traced when every earlier one hit
     traced = int(n + np.sum(tri_all[:, 0] != 0xFFFFFFFF) + np.sum((tri_all[:, 0] != 0xFFFFFFFF) & (tri_all[:, 1] != 0xFFFFFFFF)))
     out["segments_per_step"] = traced
+    # roofline: the reference order's fetches for every traced segment ray
+    live = np.ones((n, seg), bool)
+    live[:, 1] = tri_all[:, 0] != 0xFFFFFFFF
+    live[:, 2] = live[:, 1] & (tri_all[:, 1] != 0xFFFFFFFF)
+    sel = torch.from_numpy(np.nonzero(live.reshape(-1))[0]).cuda()
+    s_rays = seg_rays[sel].contiguous()
+    s_tidx = d_tidx.repeat_interleave(seg)[sel].contiguous()
+    h4 = torch.empty((s_rays.shape[0], 4), device="cuda")
+    c_seg = P.trace_counted(s_rays, h4, tlas_idx=s_tidx, traversal=rt.TRAVERSAL_REFERENCE)
+    b_seg = node_bytes_per_ray(c_seg, s_rays.shape[0]) + 4.0
+    del seg_rays, s_rays, h4
     out["forward_mrays"] = round(traced / (out["forward_ms"] / 1e3) / 1e6, 2)
     out["forward_adjoint_mrays"] = round(traced / (out["forward_adjoint_ms"] / 1e3) / 1e6, 2)
     out["fwd_adjoint_over_fwd"] = round(out["forward_adjoint_ms"] / out["forward_ms"], 3)
@@ -1434,6 +1480,15 @@ def bench_batched_adjoint(args, ws=1, rank=0):
                       "one graph for forward + adjoint; _retrace: the adjoint traces the paths again")
     out["peak_hbm_bytes"] = int(torch.cuda.max_memory_allocated() + as_bytes)
     # the configuration asks for hits recomputed in the backward pass, not stored per bounce
+    out["roofline"] = {
+        "forward": algorithmic_roofline(traced * b_seg, out["forward_ms"],
+                                        "per traced segment the reference order's fetches (counted on the recorded "
+                                        "segment rays) + 4 B attribute"),
+        "forward_adjoint_retrace": algorithmic_roofline(2 * traced * b_seg + 48.0 * traced,
+                                                        out["forward_adjoint_retrace_ms"],
+                                                        "forward twice + 48 B of atomic scatter per segment"),
+        "bytes_per_segment": round(b_seg, 1),
+    }
     out["config_conforming"] = {
         "form": "hits recomputed by tracing the paths again in the adjoint (no tape)",
         "fwd_adjoint_over_fwd": out["fwd_adjoint_retrace_over_fwd"],
