@@ -872,6 +872,89 @@ def bench_ao(args, P, S_field):
     return out
 
 
+def bench_path_tracing(args, P, S_field):
+    """The reference path tracer (feature/path_tracing) on the 1024^2
+    heightfield: one sample per pixel, max_path_depth 3, one directional light,
+    the default physical material, ACES tone map, progressive RGBA8 average.
+    Timed at the reference's own render size for a 1920x1080 frame
+    (clamp_size_by_area to 512^2 pixels: 682x384) and at the full 1920x1080.
+    Rays = core + shadow rays traced by the frame. A band of rows of the
+    clamped frame in the reference traversal order is compared with the
+    oracle bit for bit."""
+    import torch
+
+    from rendiation_gb300 import path_tracing as pt
+    from rendiation_gb300 import raytracing as rt
+    from rendiation_gb300 import task_graph as tg
+
+    lights = [pt.directional_light((3.0, 2.8, 2.5), (0.35, 0.25, -1.0))]
+    eye = (0.5, -0.35, 0.55)
+    stream = torch.cuda.current_stream()
+    out = {}
+    for name, (W, H) in (("clamped", pt.clamp_size_by_area(1920, 1080)), ("full_1080p", (1920, 1080))):
+        vp = tg.look_at_view_projection_inv(eye, (0.5, 0.5, 0.0), (0, 0, 1), 45.0, W / H, 0.01, 100.0)
+        R = pt.DeviceReferencePathTracingRenderer(P, W, H, vp, eye, lights=lights, background_color=(0.4, 0.5, 0.7),
+                                                  count_rays=True)
+        reps = 20
+
+        def timed(trav, block):
+            R.traversal, R.block_size = trav, block
+            for _ in range(args.warmup):
+                R.render()
+            R.ray_counts.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(reps):
+                R.render()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            c = R.ray_counts.cpu().numpy().view(np.uint32)
+            return e0.elapsed_time(e1) / reps, (int(c[0]) / reps, int(c[1]) / reps)
+
+        shapes = {}
+        travs = (rt.TRAVERSAL_REFERENCE,) if args.traversal == "reference" else (rt.TRAVERSAL_ORDERED,
+                                                                                  rt.TRAVERSAL_ORDERED_WIDE)
+        for trav in travs:
+            for block in (32, 64, 128):
+                shapes[(trav, block)] = timed(trav, block)[0]
+        best = min(shapes, key=shapes.get)
+        ms, (core, shadow) = timed(*best)
+        leg = {"size": [W, H], "ms_per_sample": round(ms, 4), "core_rays": core, "shadow_rays": shadow,
+               "mrays": round((core + shadow) / ms / 1e3, 1),
+               "shape": {"traversal": {0: "binary", 1: "reference", 2: "wide"}[best[0]], "block": best[1]},
+               "shapes_ms": {f"{k[0]}/{k[1]}": round(v, 4) for k, v in shapes.items()}}
+        if name == "clamped" and S_field is not None:
+            from oracle import orc
+
+            band = (H // 2 - 16, H // 2 + 16)
+            R2 = pt.DeviceReferencePathTracingRenderer(P, W, H, vp, eye, lights=lights,
+                                                       background_color=(0.4, 0.5, 0.7),
+                                                       traversal=rt.TRAVERSAL_REFERENCE, keep_radiance=True)
+            R2.render()
+            torch.cuda.synchronize()
+            img = np.zeros(W * H, np.uint32)
+            rad = np.zeros(W * H * 4, np.float32)
+            n, sec = orc.pt_render(S_field, vp, eye, W, H, img, lights=lights, bg=(0.4, 0.5, 0.7), rows=band,
+                                   radiance=rad, threads=os.cpu_count() or 1)
+            g = R2.result().reshape(-1, 4).astype(np.uint32)
+            gp = (g[:, 0] | (g[:, 1] << 8) | (g[:, 2] << 16) | (g[:, 3] << 24)).reshape(H, W)[band[0]:band[1]]
+            gr = R2.radiance.cpu().numpy().reshape(H, W, 4)[band[0]:band[1]]
+            wr = rad.reshape(H, W, 4)[band[0]:band[1]]
+            leg["parity_band_rows"] = list(band)
+            leg["parity_texels_identical"] = float(np.mean(gp == img.reshape(H, W)[band[0]:band[1]]))
+            leg["parity_radiance_bit_identical"] = float(np.mean((gr.view(np.uint32) == wr.view(np.uint32)).all(-1)))
+            leg["cpu_mrays"] = round((n[0] + n[1]) / sec / 1e6, 2)
+            leg["cpu_threads"] = os.cpu_count() or 1
+            leg["cpu_sample"] = f"rows {band[0]}..{band[1]} of the {W}x{H} frame (oracle, reference order)"
+        out[name] = leg
+    st, flags = P.check_errors()
+    assert st == 0 and flags == 0
+    out["workload"] = ("heightfield 1024^2 (2093058 tris), reference path tracer: max_path_depth 3, one "
+                       "directional light with a shadow ray per hit, default physical material (Lambertian + "
+                       "GGX), ACES tone map, running RGBA8 average; rays = core + shadow")
+    return out
+
+
 def bench_task_graph(args, P):
     """Throughput of the device task graph alone (no tracing): one million root
     tasks of a chain future that spawns and awaits a child in group 1 (which
@@ -1749,6 +1832,7 @@ def main():
     ap.add_argument("--no-batched-adjoint", action="store_true")
     ap.add_argument("--no-ao", action="store_true", help="skip the ambient-occlusion leg")
     ap.add_argument("--no-task-graph", action="store_true", help="skip the task-graph throughput leg")
+    ap.add_argument("--no-path-tracing", action="store_true", help="skip the reference path-tracer leg")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP32-vs-FP64 accuracy check")
     ap.add_argument("--no-parity", action="store_true", help="skip the oracle parity report")
     ap.add_argument("--no-watertight", action="store_true", help="skip the watertight-test frame timing")
@@ -1787,6 +1871,8 @@ def main():
         out["ao"] = bench_ao(args, P, S_field if not args.no_cpu_baseline else None)
     if not args.no_task_graph:
         out["task_graph"] = bench_task_graph(args, P)
+    if not args.no_path_tracing:
+        out["path_tracing"] = bench_path_tracing(args, P, S_field if not args.no_cpu_baseline else None)
     if not args.no_batched:
         P.close()
         out["batched"] = bench_batched(args, ws, rank)

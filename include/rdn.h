@@ -747,6 +747,98 @@ rdn_status rdn_ao_render(rdn_ctx* ctx, const rdn_ao_desc* desc, void* stream);
  * buffers alive while the graph is in use. */
 rdn_status rdn_ao_capture(rdn_ctx* ctx, rdn_task_graph* pipeline, const rdn_ao_desc* desc, rdn_graph** out);
 
+/* ---- Path tracing: DeviceReferencePathTracingRenderer::render
+ * (scene/rendering/gpu-ray-tracing/src/feature/path_tracing/mod.rs:127-235) ----
+ * One sample per pixel into a headless RGBA8 unorm buffer (the reference's
+ * radiance texture, frame_state.rs:12-20):
+ *   camera ray as rdn_ao_desc (xxhash32(x, y, sample_count) jitter,
+ *     view_projection_inv, camera_position), CULL_BACK_FACING over
+ *     [f32::EPSILON, f32::MAX], TLAS tlas_uniform        ray_gen.rs:95-161
+ *   closest hit: light index floor(next * count) from the sampler
+ *     xxhash32(x, y, 2 * sample_count), pmf 1 / count; a directional light
+ *     lights from -direction at distance f32::MAX with radiance illuminance and
+ *     pdf 1; its shadow ray ACCEPT_FIRST_HIT_AND_END_SEARCH over
+ *     [f32::EPSILON, f32::MAX] from offset_ray_hit(hit, geometric normal)
+ *                                                        ray_hit.rs:12-57, lighting_sampler.rs:86-125,
+ *                                                        lighting_bridge.rs:213-258, ray_util.rs:5-40
+ *   BRDF sample from xxhash32(x, y, 3 * sample_count): Lambertian + GGX /
+ *     Smith-GGX-correlated / Schlick mixed by mix(0.2, 1, max f0), alpha =
+ *     perceptual roughness^2                             ray_hit.rs:58-102, surface_bridge.rs:171-224
+ *   sampled radiance |n.l| * bsdf(v, l) * light radiance / pdf (0 when occluded)
+ *   ray generation: a miss adds throughput * miss radiance and ends the path;
+ *     a hit multiplies throughput by cos * brdf / max(pdf, 1e-4) and adds
+ *     throughput * sampled radiance; pdf == 0 ends it; at most max_path_depth
+ *     core rays                                          ray_gen.rs:101-150
+ *   tone map, then texel = (old * sample_count + ldr) / (sample_count + 1),
+ *     alpha 1                                            ray_gen.rs:160-177, tonemap.rs:53-200
+ * Every bounce of one path draws the same random numbers, as the reference's
+ * closest-hit shader seeds its samplers by pixel and sample count alone. A
+ * material's emissive channel reaches no pixel, as in the reference (its ray
+ * generation adds the surface radiance of misses only, which is zero). atan,
+ * sin, cos and pow are fixed polynomial evaluations (the oracle computes the
+ * same), not the GPU backend's builtins. */
+#define RDN_TONE_MAP_NONE 0u
+#define RDN_TONE_MAP_LINEAR 1u
+#define RDN_TONE_MAP_REINHARD 2u
+#define RDN_TONE_MAP_CINEON 3u
+#define RDN_TONE_MAP_ACES_FILMIC 4u  /* the reference's default (ToneMap::new, exposure 1) */
+#define RDN_PT_BACKGROUND_SOLID 0u   /* PTRayMissCtx::Solid: background_color */
+#define RDN_PT_BACKGROUND_TEST 1u    /* PTRayMissCtx::Test: 0.7 for direction.y > 0, else 0.3 */
+#define RDN_PT_MAX_PATH_DEPTH 3u     /* the reference's MAX_RAY_DEPTH (path_tracing/mod.rs:80) */
+
+/* DirectionalLightStorage's illuminance and direction (the direction light travels). */
+typedef struct rdn_pt_directional_light {
+  float illuminance[3];
+  float direction[3];
+} rdn_pt_directional_light;
+
+/* The channels PhysicalShading::construct_shading_impl reads
+ * (lighting/transport/src/surface/microfacet/device/direct_lighting.rs:14-59).
+ * workflow 0 (metallic): albedo = base_color (1 - metallic), f0 = base_color
+ * metallic + 0.16 reflectance^2 (1 - metallic). workflow 1 (specular): f0 =
+ * specular, albedo = base_color (1 - max channel of specular). A pixel whose
+ * instance has no material uses the reference's defaults (base colour 0.5,
+ * roughness 0.5, metallic 0, reflectance 0.5). */
+typedef struct rdn_pt_material {
+  float base_color[3];
+  float perceptual_roughness;
+  float emissive[3];
+  float metallic;
+  float specular[3];
+  float reflectance;
+  uint32_t workflow;
+  uint32_t reserved[3];
+} rdn_pt_material;
+
+typedef struct rdn_pt_desc {
+  float view_projection_inv[16];  /* Mat4 in the reference's memory order */
+  float camera_position[3];
+  uint32_t width, height;
+  uint32_t sample_count;          /* PTConfig.current_sample_count: samples already averaged into image */
+  uint32_t max_path_depth;        /* PTConfig.max_path_depth (RDN_PT_MAX_PATH_DEPTH in the reference) */
+  uint32_t tlas_uniform;
+  uint32_t traversal;             /* RDN_TRAVERSAL_* */
+  uint32_t tone_map;              /* RDN_TONE_MAP_* */
+  float exposure;
+  uint32_t background;            /* RDN_PT_BACKGROUND_* */
+  float background_color[3];
+  const rdn_pt_directional_light* lights; /* device, light_count entries (nullable when 0) */
+  uint32_t light_count;
+  uint32_t material_count;
+  const rdn_pt_material* materials;       /* device, nullable: every instance takes the default material */
+  const uint32_t* sm_to_material;         /* device, nullable: material of each instance custom index
+                                             (NULL: the custom index itself); out of range -> default */
+  uint32_t sm_count;                      /* entries of sm_to_material */
+  uint32_t block_size;                    /* 32, 64 or 128 (0 = 128) */
+  const float* normals;           /* device, nullable: 3 per built vertex (shading normals) */
+  uint8_t* image;                 /* device, RGBA8 unorm, width * height texels, 4-byte aligned */
+  float* radiance;                /* device, nullable, 16-byte aligned: per pixel the sample's HDR
+                                     radiance (x, y, z) and the core rays of its path (w) */
+  uint32_t* ray_counts;           /* device, nullable: [core, shadow] rays traced, added to */
+} rdn_pt_desc;
+
+rdn_status rdn_path_tracing_render(rdn_ctx* ctx, const rdn_pt_desc* desc, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

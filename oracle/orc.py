@@ -30,6 +30,63 @@ BUF_TLAS_BINDING, BUF_TLAS_BVH_ROOT, BUF_TLAS_BVH_FOREST, BUF_TLAS_DATA, BUF_TLA
 BUF_BLAS_META_INFO, BUF_TRI_BVH_ROOT, BUF_TRI_BVH_FOREST, BUF_INDICES_REDIRECT, BUF_INDICES, BUF_VERTICES = 5, 6, 7, 8, 9, 10
 
 
+# rdn_pt_material / rdn_pt_directional_light layouts (64 B / 24 B)
+PT_MATERIAL_DTYPE = np.dtype([("base_color", np.float32, 3), ("perceptual_roughness", np.float32),
+                              ("emissive", np.float32, 3), ("metallic", np.float32), ("specular", np.float32, 3),
+                              ("reflectance", np.float32), ("workflow", np.uint32), ("reserved", np.uint32, 3)])
+PT_LIGHT_DTYPE = np.dtype([("illuminance", np.float32, 3), ("direction", np.float32, 3)])
+
+
+class _PtScene(C.Structure):
+    _fields_ = [("max_depth", C.c_uint32), ("tone_map", C.c_uint32), ("background", C.c_uint32),
+                ("exposure", C.c_float), ("bg", C.c_float * 3), ("lights", C.c_void_p), ("light_count", C.c_uint32),
+                ("materials", C.c_void_p), ("material_count", C.c_uint32), ("sm_to_material", C.c_void_p),
+                ("sm_count", C.c_uint32)]
+
+
+def _pt_scene(lights, materials, sm_to_material, max_depth, tone_map, exposure, background, bg):
+    sc = _PtScene()
+    sc.max_depth, sc.tone_map, sc.background, sc.exposure = max_depth, tone_map, background, exposure
+    sc.bg[:] = [float(b) for b in bg]
+    keep = []
+    if lights is not None and len(lights):
+        la = np.ascontiguousarray(lights, PT_LIGHT_DTYPE)
+        keep.append(la)
+        sc.lights, sc.light_count = la.ctypes.data, len(la)
+    if materials is not None and len(materials):
+        ma = np.ascontiguousarray(materials, PT_MATERIAL_DTYPE)
+        keep.append(ma)
+        sc.materials, sc.material_count = ma.ctypes.data, len(ma)
+    if sm_to_material is not None:
+        sa = np.ascontiguousarray(sm_to_material, np.uint32)
+        keep.append(sa)
+        sc.sm_to_material, sc.sm_count = (sa.ctypes.data if len(sa) else None), len(sa)
+        if not len(sa):  # an empty table still routes every custom index to the default material
+            keep.append(np.zeros(1, np.uint32))
+            sc.sm_to_material = keep[-1].ctypes.data
+    return sc, keep
+
+
+def pt_surface_query(seed, view, normal, l2, materials=None, sm_to_material=None, sm_id=0):
+    """Oracle PT surface for tests: (direction, bsdf, pdf) of the BRDF sample
+    drawn from PCG state `seed`, (bsdf, pdf) at direction l2, and
+    (albedo, f0, alpha, estimate) of the surface."""
+    sc, keep = _pt_scene(None, materials, sm_to_material, 0, 0, 1.0, 0, (0, 0, 0))
+    o1, o2, o3 = np.zeros(7, np.float32), np.zeros(4, np.float32), np.zeros(8, np.float32)
+    v, n, l = (np.ascontiguousarray(a, np.float32) for a in (view, normal, l2))
+    lib().orc_pt_surface_query(C.byref(sc), sm_id, _ptr(v), _ptr(n), seed, _ptr(l), _ptr(o1), _ptr(o2), _ptr(o3))
+    return (o1[:3], o1[3:6], float(o1[6])), (o2[:3], float(o2[3])), (o3[:3], o3[3:6], float(o3[6]), float(o3[7]))
+
+
+def pt_math(op: str, x, arg=0) -> np.ndarray:
+    """The oracle's fixed-polynomial functions: atan, log2, exp2, pow22, tone (x channel of tone map `arg`)."""
+    code = {"atan": 0, "log2": 1, "exp2": 2, "pow22": 3, "tone": 4}[op]
+    xa = np.ascontiguousarray(x, np.float32)
+    y = np.zeros_like(xa)
+    lib().orc_pt_math(code, arg, _ptr(xa), _ptr(y), xa.size)
+    return y
+
+
 class _Geometry(C.Structure):
     _fields_ = [("positions", C.c_void_p), ("vertex_count", C.c_uint32), ("indices", C.c_void_p),
                 ("index_count", C.c_uint32), ("flags", C.c_uint32), ("type", C.c_uint32)]
@@ -81,6 +138,10 @@ def lib():
         L.orc_wavefront_shadow_bounce.argtypes = [vp, vp, u32, u32, vp, u32, u32, u32, u32, vp, vp, i32,
                                                   C.POINTER(C.c_double), i32]
         L.orc_wavefront_pixel_rays.argtypes = [vp, vp, u32, u32, vp, u32, u32, vp, u32, vp, vp, i32, i32]
+        L.orc_pt_render.argtypes = [vp, vp, vp, u32, u32, u32, u32, vp, vp, vp, vp, u32, u32, i32, i32, vp,
+                                    C.POINTER(C.c_double)]
+        L.orc_pt_surface_query.argtypes = [vp, u32, vp, vp, u32, vp, vp, vp, vp]
+        L.orc_pt_math.argtypes = [i32, u32, vp, vp, C.c_uint64]
         _lib = L
     return _lib
 
@@ -308,6 +369,32 @@ def select_nth(keys: np.ndarray, index: int) -> np.ndarray:
     idx = np.arange(keys.shape[0], dtype=np.uint64)
     lib().orc_select_nth(_ptr(keys), _ptr(idx), keys.shape[0], index)
     return idx
+
+
+def pt_render(system: OracleSystem, vp_inv, cam, width, height, image: np.ndarray, lights=None, materials=None,
+              sm_to_material=None, max_depth=3, tone_map=4, exposure=1.0, background=0, bg=(0.0, 0.0, 0.0),
+              sample_count=0, tlas=0, normals=None, rows=None, radiance: np.ndarray | None = None, intersector=0,
+              threads=4):
+    """One path-tracing sample into image (uint32 RGBA8 texels, width*height,
+    updated in place) for rows [r0, r1); radiance (float32 width*height*4,
+    optional) receives the sample's HDR radiance and core-ray count per pixel.
+    Returns ((core, shadow) rays traced, seconds)."""
+    vp = np.ascontiguousarray(vp_inv, np.float32)
+    cm = np.ascontiguousarray(cam, np.float32)
+    assert image.dtype == np.uint32 and image.size == width * height and image.flags.c_contiguous
+    if radiance is not None:
+        assert radiance.dtype == np.float32 and radiance.size == 4 * width * height and radiance.flags.c_contiguous
+    nrm = None if normals is None else np.ascontiguousarray(normals, np.float32)
+    sc, keep = _pt_scene(lights, materials, sm_to_material, max_depth, tone_map, exposure, background, bg)
+    r0, r1 = rows if rows is not None else (0, height)
+    rays = np.zeros(2, np.uint64)
+    sec = C.c_double()
+    rc = lib().orc_pt_render(system._h, _ptr(vp), _ptr(cm), width, height, sample_count, tlas, _ptr(nrm),
+                             C.byref(sc), _ptr(image), _ptr(radiance), r0, r1, intersector, threads, _ptr(rays),
+                             C.byref(sec))
+    system._check(rc)
+    del keep
+    return (int(rays[0]), int(rays[1])), sec.value
 
 
 def ao_render(system: OracleSystem, vp_inv, cam, width, height, image: np.ndarray, sample_count=0, tlas=0,

@@ -50,6 +50,7 @@
 #include "orc_select.h"
 #include "orc_shade.h"
 #include "orc_ao.h"
+#include "orc_pt.h"
 
 namespace orc {
 
@@ -1585,6 +1586,179 @@ int orc_ao_render(void* cp, const float* vp_inv, const float* cam, uint32_t W, u
     for (int w = 0; w < threads; w++) {
       rays2[0] += rc[2 * (size_t)w];
       rays2[1] += rc[2 * (size_t)w + 1];
+    }
+  }
+  return 0;
+}
+
+// One path-tracing sample for rows [row0, row1) of a width x height frame (see
+// orc_pt.h); image: width * height RGBA8 texels, updated in place; radiance
+// (nullable): 4 floats per pixel (HDR radiance of the sample, core rays of its
+// path). rays2 receives the core and shadow rays traced.
+int orc_pt_render(void* cp, const float* vp_inv, const float* cam, uint32_t W, uint32_t H, uint32_t sample_count,
+                  uint32_t tlas, const float* normals, const PtScene* scene, uint32_t* image, float* radiance,
+                  uint32_t row0, uint32_t row1, int intersector, int threads, uint64_t* rays2, double* seconds) {
+  Ctx& c = *(Ctx*)cp;
+  if (!c.built) {
+    int rc = build_all(c);
+    if (rc) return rc;
+  }
+  const Built& B = *c.built;
+  const PtScene& S = *scene;
+  AoView A;
+  memcpy(A.vp_inv, vp_inv, sizeof(A.vp_inv));
+  memcpy(A.cam, cam, sizeof(A.cam));
+  A.width = W;
+  A.height = H;
+  A.sample_count = sample_count;
+  if (row1 > H) row1 = H;
+  if (row0 > row1) row0 = row1;
+  if (threads < 1) threads = 1;
+  std::vector<Counters> cn(threads);
+  std::vector<uint64_t> rc(2 * (size_t)threads, 0);
+  std::atomic<uint32_t> next_row{row0};
+  auto t0 = std::chrono::steady_clock::now();
+  auto work = [&](int w) {
+    for (;;) {
+      const uint32_t y = next_row.fetch_add(1);
+      if (y >= row1) break;
+      for (uint32_t x = 0; x < W; x++) {
+        V3 o, d;
+        ao_camera_ray(A, x, y, &o, &d);
+        V3 throughput = v3(1.0f, 1.0f, 1.0f), rad = v3(0.0f, 0.0f, 0.0f);
+        uint32_t depth = 0, core = 0;
+        while (depth < S.max_depth) {
+          RayIn r{{o.x, o.y, o.z}, F32_EPSILON, {d.x, d.y, d.z}, F32_MAX};
+          HitOut h;
+          uint32_t tri = 0;
+          traverse(B, r, tlas, 0x10u, 0xFFFFFFFFu, 0, h, cn[w], nullptr, &tri, nullptr, intersector);
+          rc[2 * (size_t)w]++;
+          core++;
+          if (h.prim == INVALID_NEXT) {
+            const V3 s = pt_miss(S, d);
+            rad = v3((throughput.x * s.x + 0.0f) + rad.x, (throughput.y * s.y + 0.0f) + rad.y,
+                     (throughput.z * s.z + 0.0f) + rad.z);
+            break;
+          }
+          // closest hit: light sample, shadow ray
+          const V3 hit = o + d * h.t;
+          const float* m = B.tlas_data[h.instance].transform_inv;
+          const uint32_t i0 = B.indices[3 * (size_t)tri], i1 = B.indices[3 * (size_t)tri + 1],
+                         i2 = B.indices[3 * (size_t)tri + 2];
+          const float* P = B.vertices.data();
+          const V3 pa = v3(P[3 * (size_t)i0], P[3 * (size_t)i0 + 1], P[3 * (size_t)i0 + 2]);
+          const V3 pb = v3(P[3 * (size_t)i1], P[3 * (size_t)i1 + 1], P[3 * (size_t)i1 + 2]);
+          const V3 pc = v3(P[3 * (size_t)i2], P[3 * (size_t)i2 + 1], P[3 * (size_t)i2 + 2]);
+          V3 gn = normalize(normal_mat_mul(m, cross(pa - pb, pa - pc)));
+          if (dot(o - hit, gn) < 0.0f) gn = v3(-gn.x, -gn.y, -gn.z);
+          const V3 sn = ao_shading_normal(B.indices.data(), P, normals, m, tri, h.u, h.v, o, hit);
+          uint32_t ls = xxhash32(x, y, sample_count * 2u);
+          const float rnd = sample_next(ls);
+          const uint32_t n_lights = S.light_count;
+          uint32_t li = (uint32_t)std::floor(rnd * (float)n_lights);
+          const bool light_ok = n_lights != 0u;
+          if (li == n_lights && light_ok) li = li - 1u;
+          const float pmf = n_lights == 0u ? 0.0f : 1.0f / (float)n_lights;
+          V3 illum = v3(0.0f, 0.0f, 0.0f), dir = illum;
+          if (light_ok) {
+            illum = v3(S.lights[li].illuminance[0], S.lights[li].illuminance[1], S.lights[li].illuminance[2]);
+            dir = v3(S.lights[li].direction[0], S.lights[li].direction[1], S.lights[li].direction[2]);
+          }
+          const V3 ldir = v3(-dir.x, -dir.y, -dir.z);
+          const float pdf_l = 1.0f * pmf;
+          V3 lrad = light_ok ? v3(illum.x / pdf_l, illum.y / pdf_l, illum.z / pdf_l) : v3(0.0f, 0.0f, 0.0f);
+          const V3 origin = offset_ray_hit(hit, gn);
+          if (light_ok) {
+            RayIn sr{{origin.x, origin.y, origin.z}, F32_EPSILON, {ldir.x, ldir.y, ldir.z}, F32_MAX};
+            HitOut sh;
+            traverse(B, sr, tlas, RAY_FLAG_END_SEARCH, 0xFFFFFFFFu, 0, sh, cn[w], nullptr, nullptr, nullptr,
+                     intersector);
+            rc[2 * (size_t)w + 1]++;
+            if (sh.prim != INVALID_NEXT) lrad = v3(0.0f, 0.0f, 0.0f);
+          }
+          // map: BRDF sample and the direct light through the BRDF
+          const V3 view = v3(-d.x, -d.y, -d.z);
+          const PtSurface su = pt_surface(S, h.custom);
+          uint32_t bs = xxhash32(x, y, sample_count * 3u);
+          V3 brdf;
+          float pdf;
+          const V3 sdir = pt_sample(su, view, sn, bs, &brdf, &pdf);
+          const V3 brdf_l = pt_bsdf(su, view, ldir, sn);
+          const float light_dot = std::fabs(dot(sn, ldir));
+          const V3 sampled = v3((light_dot * brdf_l.x) * lrad.x, (light_dot * brdf_l.y) * lrad.y,
+                                (light_dot * brdf_l.z) * lrad.z);
+          // ray generation, hit branch
+          if (pdf == 0.0f) depth = S.max_depth;
+          depth = depth + 1u;
+          const float cosv = dot(sdir, sn);
+          const float pdf_c = rmax(pdf, 0.0001f);
+          throughput = v3(((throughput.x * cosv) * brdf.x) / pdf_c, ((throughput.y * cosv) * brdf.y) / pdf_c,
+                          ((throughput.z * cosv) * brdf.z) / pdf_c);
+          rad = v3(throughput.x * sampled.x + rad.x, throughput.y * sampled.y + rad.y,
+                   throughput.z * sampled.z + rad.z);
+          o = origin;
+          d = sdir;
+        }
+        const size_t pix = (size_t)y * W + x;
+        image[pix] = pt_accumulate(image[pix], sample_count, pt_tone_map(S, rad));
+        if (radiance) {
+          radiance[4 * pix] = rad.x;
+          radiance[4 * pix + 1] = rad.y;
+          radiance[4 * pix + 2] = rad.z;
+          radiance[4 * pix + 3] = (float)core;
+        }
+      }
+    }
+  };
+  std::vector<std::thread> th;
+  for (int w = 0; w < threads; w++) th.emplace_back(work, w);
+  for (auto& t : th) t.join();
+  auto t1 = std::chrono::steady_clock::now();
+  if (seconds) *seconds = std::chrono::duration<double>(t1 - t0).count();
+  if (rays2) {
+    rays2[0] = rays2[1] = 0;
+    for (int w = 0; w < threads; w++) {
+      rays2[0] += rc[2 * (size_t)w];
+      rays2[1] += rc[2 * (size_t)w + 1];
+    }
+  }
+  return 0;
+}
+
+// One PT surface query for tests: surface of material index sm_id under the
+// scene's tables, BRDF importance sample from `seed` at view v / normal n
+// (out: direction, bsdf, pdf), bsdf(v, l2, n) and pdf(v, l2, n) of a second
+// direction (out2: bsdf, pdf), and the surface (out3: albedo, f0, alpha, estimate).
+int orc_pt_surface_query(const PtScene* scene, uint32_t sm_id, const float* v, const float* n, uint32_t seed,
+                         const float* l2, float* out, float* out2, float* out3) {
+  const PtSurface su = pt_surface(*scene, sm_id);
+  const V3 vv = v3(v[0], v[1], v[2]), nn = v3(n[0], n[1], n[2]);
+  uint32_t st = seed;
+  V3 brdf;
+  float pdf;
+  const V3 l = pt_sample(su, vv, nn, st, &brdf, &pdf);
+  out[0] = l.x, out[1] = l.y, out[2] = l.z, out[3] = brdf.x, out[4] = brdf.y, out[5] = brdf.z, out[6] = pdf;
+  const V3 ll = v3(l2[0], l2[1], l2[2]);
+  const V3 b2 = pt_bsdf(su, vv, ll, nn);
+  out2[0] = b2.x, out2[1] = b2.y, out2[2] = b2.z, out2[3] = pt_pdf(su, vv, ll, nn);
+  out3[0] = su.albedo.x, out3[1] = su.albedo.y, out3[2] = su.albedo.z, out3[3] = su.f0.x, out3[4] = su.f0.y,
+  out3[5] = su.f0.z, out3[6] = su.alpha, out3[7] = su.estimate;
+  return 0;
+}
+
+// Elementwise fixed-polynomial functions for tests: op 0 atan, 1 log2, 2 exp2,
+// 3 pow(x, 2.2), 4 tone map of (x, x, x) with tone map `arg` and exposure 1 (x channel).
+int orc_pt_math(int op, uint32_t arg, const float* x, float* y, uint64_t n) {
+  PtScene S{};
+  S.tone_map = arg;
+  S.exposure = 1.0f;
+  for (uint64_t i = 0; i < n; i++) {
+    switch (op) {
+      case 0: y[i] = pt_atan(x[i]); break;
+      case 1: y[i] = pt_log2(x[i]); break;
+      case 2: y[i] = pt_exp2(x[i]); break;
+      case 3: y[i] = pt_pow(x[i], 2.2f); break;
+      default: y[i] = pt_tone_map(S, v3(x[i], x[i], x[i])).x; break;
     }
   }
   return 0;

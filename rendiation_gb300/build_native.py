@@ -34,6 +34,7 @@ UNITS = {
     "device_build.cu": ["-fmad=false"],
     "task_graph.cu": ["-fmad=false"],
     "ao.cu": ["-fmad=false"],
+    "pt.cu": ["-fmad=false"],
 }
 
 

@@ -93,17 +93,17 @@ __device__ __forceinline__ float3 normal_mat_mul(const float* m, float3 n) {
                      n.x * __ldg(m + 8) + n.y * __ldg(m + 9) + n.z * __ldg(m + 10));
 }
 
-// Shading normal of a hit (get_world_normal_impl), oriented like the reference:
-// the geometric normal towards the ray origin, the shading normal into the
-// geometric normal's hemisphere. Without vertex normals the shading normal is
-// the oriented geometric normal.
-__device__ __forceinline__ float3 ao_shading_normal(const AoEnv& A, const DeviceInstance* inst, uint32_t tri,
-                                                    float u, float v, float3 ro, float3 hit) {
+// Shading and geometric normals of a hit (get_world_normal_impl), oriented like
+// the reference: the geometric normal towards the ray origin, the shading
+// normal into the geometric normal's hemisphere. Without vertex normals the
+// shading normal is the oriented geometric normal.
+__device__ __forceinline__ float3 hit_normals(const AoEnv& A, const DeviceInstance* inst, uint32_t tri, float u,
+                                              float v, float3 ro, float3 hit, float3& geom) {
   const uint32_t i0 = __ldg(A.indices + 3 * (size_t)tri), i1 = __ldg(A.indices + 3 * (size_t)tri + 1),
                  i2 = __ldg(A.indices + 3 * (size_t)tri + 2);
   const float* m = inst->transform_inv;
   const float3 pa = ld_vertex(A.vertices, i0), pb = ld_vertex(A.vertices, i1), pc = ld_vertex(A.vertices, i2);
-  float3 geom = normalize3(normal_mat_mul(m, cross3(pa - pb, pa - pc)));
+  geom = normalize3(normal_mat_mul(m, cross3(pa - pb, pa - pc)));
   const float3 hto = ro - hit;
   if (dot3(hto, geom) < 0.0f) geom = make_float3(-geom.x, -geom.y, -geom.z);
   if (!A.normals) return geom;
@@ -113,6 +113,11 @@ __device__ __forceinline__ float3 ao_shading_normal(const AoEnv& A, const Device
   float3 shading = normalize3(normal_mat_mul(m, n));
   if (dot3(geom, shading) < 0.0f) shading = make_float3(-shading.x, -shading.y, -shading.z);
   return shading;
+}
+__device__ __forceinline__ float3 ao_shading_normal(const AoEnv& A, const DeviceInstance* inst, uint32_t tri,
+                                                    float u, float v, float3 ro, float3 hit) {
+  float3 geom;
+  return hit_normals(A, inst, tri, u, v, ro, hit, geom);
 }
 
 // radical_inverse_vdc: bit reversal, times 2^-32

@@ -16,6 +16,7 @@
 #include "device_build.h"
 #include "parallel.h"
 #include "paths.h"
+#include "pt.h"
 #include "task_graph.h"
 #include "wavefront.h"
 
@@ -1589,6 +1590,63 @@ rdn_status rdn_ao_capture(rdn_ctx* c, rdn_task_graph* pipeline, const rdn_ao_des
       c, "AO frame capture",
       [&](cudaStream_t s) { return pipeline ? ao_graph_frame(pipeline, d, s, true) : rdn_ao_render(c, d, s); },
       out);
+}
+
+static_assert(sizeof(rdn_pt_material) == sizeof(rdn::PtMaterial), "rdn_pt_material layout");
+static_assert(sizeof(rdn_pt_directional_light) == sizeof(rdn::PtLight), "rdn_pt_directional_light layout");
+
+rdn_status rdn_path_tracing_render(rdn_ctx* c, const rdn_pt_desc* d, void* stream) {
+  Range range_("rdn_path_tracing_render");
+  if (!c || !d) return fail(c, RDN_ERR_INVALID_ARG, "null context or descriptor");
+  if (c->device < 0) return fail(c, RDN_ERR_UNSUPPORTED, "host-only context cannot trace");
+  if (d->tone_map > RDN_TONE_MAP_ACES_FILMIC) return fail(c, RDN_ERR_INVALID_ARG, "unknown tone map");
+  if (d->background > RDN_PT_BACKGROUND_TEST) return fail(c, RDN_ERR_INVALID_ARG, "unknown background");
+  if (d->max_path_depth > 64) return fail(c, RDN_ERR_INVALID_ARG, "max_path_depth must be at most 64");
+  if (d->light_count && !d->lights) return fail(c, RDN_ERR_INVALID_ARG, "null lights with light_count > 0");
+  if (d->material_count && !d->materials)
+    return fail(c, RDN_ERR_INVALID_ARG, "null materials with material_count > 0");
+  if (d->sm_count && !d->sm_to_material)
+    return fail(c, RDN_ERR_INVALID_ARG, "null sm_to_material with sm_count > 0");
+  if ((reinterpret_cast<uintptr_t>(d->lights) & 3) || (reinterpret_cast<uintptr_t>(d->materials) & 3) ||
+      (reinterpret_cast<uintptr_t>(d->sm_to_material) & 3) || (reinterpret_cast<uintptr_t>(d->normals) & 3))
+    return fail(c, RDN_ERR_INVALID_ARG, "lights, materials, sm_to_material and normals must be 4-byte aligned");
+  if (reinterpret_cast<uintptr_t>(d->radiance) & 15)
+    return fail(c, RDN_ERR_INVALID_ARG, "radiance must be 16-byte aligned");
+  std::lock_guard<std::mutex> lk(c->lock);
+  rdn_ao_desc ad;
+  std::memset(&ad, 0, sizeof(ad));
+  std::memcpy(ad.view_projection_inv, d->view_projection_inv, sizeof(ad.view_projection_inv));
+  std::memcpy(ad.camera_position, d->camera_position, sizeof(ad.camera_position));
+  ad.width = d->width;
+  ad.height = d->height;
+  ad.sample_count = d->sample_count;
+  ad.tlas_uniform = d->tlas_uniform;
+  ad.traversal = d->traversal;
+  ad.normals = d->normals;
+  ad.image = d->image;
+  ad.block_size = d->block_size;
+  ad.ray_counts = d->ray_counts;
+  rdn::TraceParams p;
+  rdn::PtEnv e;
+  std::memset(&e, 0, sizeof(e));
+  rdn_status st = ao_env(c, &ad, p, e.view);
+  if (st != RDN_OK) return st;
+  e.max_depth = d->max_path_depth;
+  e.tone_map = d->tone_map;
+  e.exposure = d->exposure;
+  e.background = d->background;
+  std::memcpy(e.bg, d->background_color, sizeof(e.bg));
+  e.lights = reinterpret_cast<const rdn::PtLight*>(d->lights);
+  e.light_count = d->light_count;
+  e.materials = reinterpret_cast<const rdn::PtMaterial*>(d->materials);
+  e.material_count = d->material_count;
+  e.sm_to_material = d->sm_to_material;
+  e.sm_count = d->sm_count;
+  e.radiance = reinterpret_cast<float4*>(d->radiance);
+  cudaError_t err = cudaSetDevice(c->device);
+  if (err == cudaSuccess) err = rdn::launch_pt(p, e, mode_of(d->traversal), static_cast<cudaStream_t>(stream));
+  if (err != cudaSuccess) return cuda_fail(c, err, "path tracing launch");
+  return RDN_OK;
 }
 
 }  // extern "C"

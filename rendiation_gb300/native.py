@@ -33,6 +33,7 @@ EXPORTED_SYMBOLS = [
     "rdn_task_graph_destroy", "rdn_task_graph_dispatch_init", "rdn_task_graph_execute", "rdn_task_graph_states",
     "rdn_task_graph_debug", "rdn_task_graph_check_errors", "rdn_ao_pipeline_create", "rdn_ao_render_graph",
     "rdn_ao_render", "rdn_ao_capture", "rdn_task_graph_capture", "rdn_task_graph_set_poll", "rdn_trace_params",
+    "rdn_path_tracing_render",
 ]
 
 
@@ -146,6 +147,17 @@ class AoDesc(C.Structure):
                 ("ray_counts", C.c_void_p), ("sample_counter", C.c_void_p)]
 
 
+class PtDesc(C.Structure):
+    _fields_ = [("view_projection_inv", C.c_float * 16), ("camera_position", C.c_float * 3), ("width", C.c_uint32),
+                ("height", C.c_uint32), ("sample_count", C.c_uint32), ("max_path_depth", C.c_uint32),
+                ("tlas_uniform", C.c_uint32), ("traversal", C.c_uint32), ("tone_map", C.c_uint32),
+                ("exposure", C.c_float), ("background", C.c_uint32), ("background_color", C.c_float * 3),
+                ("lights", C.c_void_p), ("light_count", C.c_uint32), ("material_count", C.c_uint32),
+                ("materials", C.c_void_p), ("sm_to_material", C.c_void_p), ("sm_count", C.c_uint32),
+                ("block_size", C.c_uint32), ("normals", C.c_void_p), ("image", C.c_void_p), ("radiance", C.c_void_p),
+                ("ray_counts", C.c_void_p)]
+
+
 _lib = None
 
 
@@ -255,5 +267,7 @@ def lib() -> C.CDLL:
     L.rdn_task_graph_set_poll.restype = i32
     L.rdn_trace_params.argtypes = [vp, u32, vp, C.POINTER(C.c_size_t)]
     L.rdn_trace_params.restype = i32
+    L.rdn_path_tracing_render.argtypes = [vp, C.POINTER(PtDesc), vp]
+    L.rdn_path_tracing_render.restype = i32
     _lib = L
     return L

@@ -18,7 +18,7 @@ PAIRS = [
     ("rdn_camera", native.Camera), ("rdn_wavefront_desc", native.WavefrontDesc), ("rdn_path_desc", native.PathDesc),
     ("rdn_attr_loss_desc", native.AttrLossDesc), ("rdn_attr_path_desc", native.AttrPathDesc),
     ("rdn_hit_diff_desc", native.HitDiffDesc),
-    ("rdn_task_group_desc", native.TaskGroupDesc), ("rdn_ao_desc", native.AoDesc),
+    ("rdn_task_group_desc", native.TaskGroupDesc), ("rdn_ao_desc", native.AoDesc), ("rdn_pt_desc", native.PtDesc),
 ]
 
 
@@ -42,6 +42,28 @@ def header_layout(tmp_path_factory):
             s, f, v = line.split()
             layout[(s, f)] = int(v)
     return layout
+
+
+def test_path_tracing_records_match_header(header_layout, tmp_path):
+    """rdn_pt_material / rdn_pt_directional_light against the numpy record types."""
+    from rendiation_gb300 import path_tracing as pt
+
+    src = tmp_path / "pt.c"
+    names = {"rdn_pt_material": pt.MATERIAL_DTYPE, "rdn_pt_directional_light": pt.DIRECTIONAL_LIGHT_DTYPE}
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "rdn.h"', "int main(void) {"]
+    for cname, dt in names.items():
+        lines.append(f'  printf("{cname} sizeof %zu\\n", sizeof({cname}));')
+        for fname in dt.names:
+            lines.append(f'  printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    src.write_text("\n".join(lines + ["  return 0;", "}"]) + "\n")
+    exe = tmp_path / "pt"
+    subprocess.run(["gcc", "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
+    got = {(out[i], out[i + 1]): int(out[i + 2]) for i in range(0, len(out), 3)}
+    for cname, dt in names.items():
+        assert got[(cname, "sizeof")] == dt.itemsize
+        for fname in dt.names:
+            assert got[(cname, fname)] == dt.fields[fname][1], (cname, fname)
 
 
 @pytest.mark.parametrize("cname,py", PAIRS, ids=[p[0] for p in PAIRS])

@@ -1,0 +1,216 @@
+"""The reference path tracer (feature/path_tracing: ray_gen.rs, ray_hit.rs,
+ray_miss.rs, the lighting and surface bridges) as the fused CUDA frame
+(rdn_path_tracing_render) against the path-tracing oracle (oracle/orc_pt.h),
+over progressive samples. The reference traversal order: every RGBA8 texel and
+every HDR radiance bit-identical (NaN equal to NaN); the four-child walk:
+identical except pixels whose path meets an exact-distance tie."""
+
+import numpy as np
+import pytest
+
+import naive_fixture as nf
+from helpers import instanced_scene, orc, single_mesh_scene
+from rendiation_gb300 import native
+from rendiation_gb300 import path_tracing as pt
+from rendiation_gb300 import raytracing as rt
+from rendiation_gb300 import scenes
+from rendiation_gb300 import task_graph as tg
+
+pytestmark = pytest.mark.gpu
+
+W, H = 77, 45  # not a multiple of the 8x4 tile: the last tiles overhang the frame
+SAMPLES = (0, 1, 2)
+
+
+def vertex_normals(mesh):
+    p = mesh.positions.astype(np.float64)
+    t = mesh.indices.reshape(-1, 3)
+    fn = np.cross(p[t[:, 1]] - p[t[:, 0]], p[t[:, 2]] - p[t[:, 0]])
+    n = np.zeros_like(p)
+    for k in range(3):
+        np.add.at(n, t[:, k], fn)
+    n /= np.linalg.norm(n, axis=1, keepdims=True)
+    return n.astype(np.float32)
+
+
+MATERIALS = np.array([pt.metallic_material((0.8, 0.6, 0.3), 0.7, 0.0, 0.5),
+                      pt.metallic_material((0.9, 0.9, 0.95), 0.25, 1.0),
+                      pt.specular_material((0.2, 0.5, 0.7), 0.4, (0.3, 0.2, 0.1)),
+                      pt.metallic_material((0.5, 0.5, 0.5), 0.05, 0.3, 0.2)], pt.MATERIAL_DTYPE)
+LIGHTS = np.array([pt.directional_light((3.0, 2.5, 2.0), (0.3, 0.2, -1.0)),
+                   pt.directional_light((0.5, 0.7, 1.2), (-0.6, 0.4, -0.5)),
+                   pt.directional_light((1.0, 1.0, 1.0), (0.0, -0.2, -1.0))], pt.DIRECTIONAL_LIGHT_DTYPE)
+
+
+def field():
+    mesh = scenes.heightfield(48, seed=3, jitter_sigma=0.02)
+    eye = (0.5, -0.45, 0.75)
+    vp = tg.look_at_view_projection_inv(eye, (0.5, 0.5, 0.0), (0, 0, 1), 45.0, W / H)
+    return single_mesh_scene(mesh), mesh, vp, np.asarray(eye, np.float32)
+
+
+def instanced():
+    eye = (0.4, -2.6, 1.6)
+    vp = tg.look_at_view_projection_inv(eye, (0.4, 0.4, 0.3), (0, 0, 1), 50.0, W / H)
+    return instanced_scene(seed=2), None, vp, np.asarray(eye, np.float32)
+
+
+def fixture():
+    eye = (0.0, 0.0, 0.0)
+    vp = tg.look_at_view_projection_inv(eye, (0.0, 0.0, -1.0), (0, 1, 0), 90.0, W / H)
+    return nf.make_scene(), None, vp, np.asarray(eye, np.float32)
+
+
+SCENES = {"field": field, "instanced": instanced, "fixture": fixture}
+
+
+def run_pair(scene_fn, traversal=rt.TRAVERSAL_REFERENCE, with_normals=False, samples=SAMPLES, tlas=0, **kw):
+    import torch
+
+    scene, mesh, vp, eye = scene_fn()
+    normals = vertex_normals(mesh) if with_normals else None
+    S = scene.build_oracle()
+    img = np.zeros(W * H, np.uint32)
+    rad = np.zeros(W * H * 4, np.float32)
+    rays = [0, 0]
+    okw = {k: v for k, v in kw.items() if k not in ("block_size",)}
+    for s in samples:
+        r, _ = orc.pt_render(S, vp, eye, W, H, img, sample_count=s, normals=normals, radiance=rad, tlas=tlas,
+                             intersector=1 if traversal & rt.INTERSECT_WATERTIGHT else 0, threads=8, **okw)
+        rays[0] += r[0]
+        rays[1] += r[1]
+    P = scene.build_product()
+    nt = None if normals is None else torch.from_numpy(normals.reshape(-1)).cuda()
+    rk = dict(kw)
+    renames = {"max_depth": "max_path_depth", "bg": "background_color"}
+    rk = {renames.get(k, k): v for k, v in rk.items()}
+    R = pt.DeviceReferencePathTracingRenderer(P, W, H, vp, eye, normals=nt, traversal=traversal, tlas_uniform=tlas,
+                                              keep_radiance=True, count_rays=True, **rk)
+    for s in samples:
+        R.sample_count = s
+        R.render()
+    torch.cuda.synchronize()
+    assert P.check_errors() == (0, 0)
+    got = R.result().reshape(-1, 4).astype(np.uint32)
+    packed = got[:, 0] | (got[:, 1] << 8) | (got[:, 2] << 16) | (got[:, 3] << 24)
+    grad = R.radiance.cpu().numpy()
+    return img, rad, packed, grad, tuple(rays), R.rays_traced()
+
+
+def same_bits(a, b):
+    a, b = a.copy(), b.copy()
+    nan = np.isnan(a) & np.isnan(b)
+    a[nan] = 0
+    b[nan] = 0
+    return a.view(np.uint32) == b.view(np.uint32)
+
+
+# The reference's fixture runs with the watertight test: its sphere's zero-area
+# pole triangles give NaN distances under the reference's formula, and a NaN
+# hit position's bits (which differ between host and device NaNs) feed
+# offset_ray_hit's integer offset.
+@pytest.mark.parametrize("name,normals,tone", [
+    ("field", True, pt.TONE_MAP_ACES_FILMIC),
+    ("field", False, pt.TONE_MAP_REINHARD),
+    ("instanced", False, pt.TONE_MAP_ACES_FILMIC),
+    ("instanced", False, pt.TONE_MAP_CINEON),
+    ("fixture", False, pt.TONE_MAP_LINEAR),
+    ("fixture", False, pt.TONE_MAP_NONE),
+])
+def test_reference_order_is_bit_identical(cuda, name, normals, tone):
+    sm = [0, 1, 2, 3, 0, 1, 2, 3, 9, 1, 2, 3] if name == "instanced" else None
+    fixture_kw = dict(tlas=4, traversal=rt.TRAVERSAL_REFERENCE | rt.INTERSECT_WATERTIGHT) if name == "fixture" else {}
+    want_img, want_rad, img, rad, rays_o, rays_g = run_pair(
+        SCENES[name], with_normals=normals, tone_map=tone, lights=LIGHTS, materials=MATERIALS, sm_to_material=sm,
+        bg=(0.05, 0.1, 0.2), exposure=1.3, **fixture_kw)
+    assert np.array_equal(img, want_img)
+    assert same_bits(rad, want_rad).all()
+    assert rays_g == rays_o
+    r = want_rad.reshape(-1, 4)
+    # paths of every length up to 3, lit and shadowed pixels, some escaped to the background
+    assert set(np.unique(r[:, 3]).astype(int)) >= {1, 2, 3}
+    assert rays_o[1] > 0 and len(np.unique(want_img)) > 50
+
+
+def test_test_background_without_lights(cuda):
+    """PTRayMissCtx::Test and no light: no shadow ray, every pixel's radiance is
+    the throughput of its escaping path times 0.7 or 0.3."""
+    want_img, want_rad, img, rad, rays_o, rays_g = run_pair(
+        field, lights=None, materials=MATERIALS, background=pt.BACKGROUND_TEST, tone_map=pt.TONE_MAP_LINEAR)
+    assert np.array_equal(img, want_img) and same_bits(rad, want_rad).all()
+    assert rays_o[1] == 0 and rays_g == rays_o
+
+
+@pytest.mark.parametrize("depth", [0, 1, 5])
+def test_path_depth(cuda, depth):
+    want_img, want_rad, img, rad, rays_o, rays_g = run_pair(
+        instanced, max_depth=depth, lights=LIGHTS[:1], materials=MATERIALS, bg=(0.3, 0.3, 0.3))
+    assert np.array_equal(img, want_img) and same_bits(rad, want_rad).all()
+    assert rays_g == rays_o
+    assert np.max(want_rad.reshape(-1, 4)[:, 3]) == depth
+
+
+def test_watertight_intersector(cuda):
+    want_img, want_rad, img, rad, rays_o, rays_g = run_pair(
+        field, traversal=rt.TRAVERSAL_REFERENCE | rt.INTERSECT_WATERTIGHT, with_normals=True, lights=LIGHTS,
+        materials=MATERIALS)
+    assert np.array_equal(img, want_img) and same_bits(rad, want_rad).all()
+
+
+@pytest.mark.parametrize("traversal", [rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_WIDE])
+def test_ordered_walks_match_except_ties(cuda, traversal):
+    want_img, want_rad, img, rad, _, _ = run_pair(instanced, traversal=traversal, lights=LIGHTS, materials=MATERIALS)
+    assert (img == want_img).mean() > 0.995
+    assert same_bits(rad, want_rad).reshape(-1, 4).all(1).mean() > 0.995
+
+
+@pytest.mark.parametrize("block_size", [32, 64])
+def test_block_size_changes_no_pixel(cuda, block_size):
+    a = run_pair(field, traversal=rt.TRAVERSAL_ORDERED_WIDE, lights=LIGHTS, materials=MATERIALS)
+    b = run_pair(field, traversal=rt.TRAVERSAL_ORDERED_WIDE, lights=LIGHTS, materials=MATERIALS,
+                 block_size=block_size)
+    assert np.array_equal(a[2], b[2]) and same_bits(a[3], b[3]).all()
+
+
+def test_invalid_descriptors_are_rejected(cuda):
+    import torch
+
+    scene, _, vp, eye = field()
+    P = scene.build_product()
+    bad = [dict(tone_map=5), dict(background=2), dict(max_path_depth=65)]
+    for kw in bad:
+        R = pt.DeviceReferencePathTracingRenderer(P, W, H, vp, eye, **kw)
+        with pytest.raises(native.RdnError):
+            R.render()
+    R = pt.DeviceReferencePathTracingRenderer(P, W, H, vp, eye, keep_radiance=True)
+    d = R.desc()
+    d.radiance = R.radiance.data_ptr() + 4  # not 16-byte aligned
+    assert P._L.rdn_path_tracing_render(P._h, native.C.byref(d), None) == native.RDN_ERR_INVALID_ARG
+    d = R.desc()
+    d.light_count = 2  # with a null light array
+    assert P._L.rdn_path_tracing_render(P._h, native.C.byref(d), None) == native.RDN_ERR_INVALID_ARG
+    d = R.desc()
+    d.image = None
+    assert P._L.rdn_path_tracing_render(P._h, native.C.byref(d), None) == native.RDN_ERR_INVALID_ARG
+    torch.cuda.synchronize()
+    assert int(R.image.sum().item()) == 0  # nothing was written
+
+
+def test_render_accumulates_and_resets(cuda):
+    import torch
+
+    scene, _, vp, eye = field()
+    P = scene.build_product()
+    R = pt.DeviceReferencePathTracingRenderer(P, W, H, vp, eye, lights=LIGHTS, materials=MATERIALS,
+                                              traversal=rt.TRAVERSAL_ORDERED_WIDE)
+    for _ in range(4):
+        R.render()
+    torch.cuda.synchronize()
+    assert R.sample_count == 4
+    first = R.result().copy()
+    R.reset_sample()
+    for _ in range(4):
+        R.render()
+    torch.cuda.synchronize()
+    assert np.array_equal(R.result(), first)
+    assert np.all(first[..., 3] == 255)
