@@ -897,8 +897,8 @@ def bench_path_tracing(args, P, S_field):
                                                   count_rays=True)
         reps = 20
 
-        def timed(trav, block):
-            R.traversal, R.block_size = trav, block
+        def timed(trav, block, sched):
+            R.traversal, R.block_size, R.schedule = trav, block, sched
             for _ in range(args.warmup):
                 R.render()
             R.ray_counts.zero_()
@@ -914,15 +914,17 @@ def bench_path_tracing(args, P, S_field):
         shapes = {}
         travs = (rt.TRAVERSAL_REFERENCE,) if args.traversal == "reference" else (rt.TRAVERSAL_ORDERED,
                                                                                   rt.TRAVERSAL_ORDERED_WIDE)
-        for trav in travs:
-            for block in (32, 64, 128):
-                shapes[(trav, block)] = timed(trav, block)[0]
+        for sched in (pt.SCHEDULE_PIXEL, pt.SCHEDULE_REFILL):
+            for trav in travs:
+                for block in (32, 64, 128):
+                    shapes[(trav, block, sched)] = timed(trav, block, sched)[0]
         best = min(shapes, key=shapes.get)
         ms, (core, shadow) = timed(*best)
         leg = {"size": [W, H], "ms_per_sample": round(ms, 4), "core_rays": core, "shadow_rays": shadow,
                "mrays": round((core + shadow) / ms / 1e3, 1),
-               "shape": {"traversal": {0: "binary", 1: "reference", 2: "wide"}[best[0]], "block": best[1]},
-               "shapes_ms": {f"{k[0]}/{k[1]}": round(v, 4) for k, v in shapes.items()}}
+               "shape": {"traversal": {0: "binary", 1: "reference", 2: "wide"}[best[0]], "block": best[1],
+                         "schedule": ("pixel", "refill")[best[2]]},
+               "shapes_ms": {f"{('pixel', 'refill')[k[2]]}/{k[0]}/{k[1]}": round(v, 4) for k, v in shapes.items()}}
         if name == "clamped" and S_field is not None:
             from oracle import orc
 

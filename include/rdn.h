@@ -785,6 +785,9 @@ rdn_status rdn_ao_capture(rdn_ctx* ctx, rdn_task_graph* pipeline, const rdn_ao_d
 #define RDN_PT_BACKGROUND_SOLID 0u   /* PTRayMissCtx::Solid: background_color */
 #define RDN_PT_BACKGROUND_TEST 1u    /* PTRayMissCtx::Test: 0.7 for direction.y > 0, else 0.3 */
 #define RDN_PT_MAX_PATH_DEPTH 3u     /* the reference's MAX_RAY_DEPTH (path_tracing/mod.rs:80) */
+#define RDN_PT_SCHEDULE_PIXEL 0u     /* one thread per pixel, warps over 8x4 tiles */
+#define RDN_PT_SCHEDULE_REFILL 1u    /* persistent warps; a lane whose path ends takes the next pixel (the
+                                        frame uses the context's work counter: one frame in flight per context) */
 
 /* DirectionalLightStorage's illuminance and direction (the direction light travels). */
 typedef struct rdn_pt_directional_light {
@@ -835,6 +838,7 @@ typedef struct rdn_pt_desc {
   float* radiance;                /* device, nullable, 16-byte aligned: per pixel the sample's HDR
                                      radiance (x, y, z) and the core rays of its path (w) */
   uint32_t* ray_counts;           /* device, nullable: [core, shadow] rays traced, added to */
+  uint32_t schedule;              /* RDN_PT_SCHEDULE_*: how paths map to threads (no pixel changes) */
 } rdn_pt_desc;
 
 rdn_status rdn_path_tracing_render(rdn_ctx* ctx, const rdn_pt_desc* desc, void* stream);

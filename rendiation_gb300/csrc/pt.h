@@ -50,8 +50,10 @@ struct PtEnv {
   const uint32_t* sm_to_material;
   uint32_t sm_count;
   float4* radiance;  // nullable: per pixel (HDR radiance of this sample, core rays traced)
+  uint32_t schedule;  // 0 one thread per pixel; 1 persistent warps refilled with pixels as paths end
+  uint32_t* fetch;    // refill schedule: the frame's pixel counter (zeroed before the launch)
 };
 
-cudaError_t launch_pt(const TraceParams& p, const PtEnv& e, int mode, cudaStream_t st);
+cudaError_t launch_pt(const TraceParams& p, const PtEnv& e, int mode, int sm_count, cudaStream_t st);
 
 }  // namespace rdn

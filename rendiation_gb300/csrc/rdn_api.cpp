@@ -1612,6 +1612,7 @@ rdn_status rdn_path_tracing_render(rdn_ctx* c, const rdn_pt_desc* d, void* strea
     return fail(c, RDN_ERR_INVALID_ARG, "lights, materials, sm_to_material and normals must be 4-byte aligned");
   if (reinterpret_cast<uintptr_t>(d->radiance) & 15)
     return fail(c, RDN_ERR_INVALID_ARG, "radiance must be 16-byte aligned");
+  if (d->schedule > RDN_PT_SCHEDULE_REFILL) return fail(c, RDN_ERR_INVALID_ARG, "unknown schedule");
   std::lock_guard<std::mutex> lk(c->lock);
   rdn_ao_desc ad;
   std::memset(&ad, 0, sizeof(ad));
@@ -1643,8 +1644,11 @@ rdn_status rdn_path_tracing_render(rdn_ctx* c, const rdn_pt_desc* d, void* strea
   e.sm_to_material = d->sm_to_material;
   e.sm_count = d->sm_count;
   e.radiance = reinterpret_cast<float4*>(d->radiance);
+  e.schedule = d->schedule;
+  e.fetch = c->d_counters + 13;
   cudaError_t err = cudaSetDevice(c->device);
-  if (err == cudaSuccess) err = rdn::launch_pt(p, e, mode_of(d->traversal), static_cast<cudaStream_t>(stream));
+  if (err == cudaSuccess)
+    err = rdn::launch_pt(p, e, mode_of(d->traversal), c->sm_count, static_cast<cudaStream_t>(stream));
   if (err != cudaSuccess) return cuda_fail(c, err, "path tracing launch");
   return RDN_OK;
 }

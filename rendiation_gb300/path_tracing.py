@@ -29,6 +29,7 @@ from .raytracing import TRAVERSAL_ORDERED_WIDE, _check
 
 TONE_MAP_NONE, TONE_MAP_LINEAR, TONE_MAP_REINHARD, TONE_MAP_CINEON, TONE_MAP_ACES_FILMIC = 0, 1, 2, 3, 4
 BACKGROUND_SOLID, BACKGROUND_TEST = 0, 1
+SCHEDULE_PIXEL, SCHEDULE_REFILL = 0, 1
 MAX_RAY_DEPTH = 3  # path_tracing/mod.rs:80
 
 MATERIAL_DTYPE = np.dtype([("base_color", np.float32, 3), ("perceptual_roughness", np.float32),
@@ -89,7 +90,7 @@ class DeviceReferencePathTracingRenderer:
                  sm_to_material=None, normals=None, max_path_depth=MAX_RAY_DEPTH, tone_map=TONE_MAP_ACES_FILMIC,
                  exposure=1.0, background=BACKGROUND_SOLID, background_color=(0.0, 0.0, 0.0),
                  traversal=TRAVERSAL_ORDERED_WIDE, tlas_uniform=0, block_size=0, keep_radiance=False,
-                 count_rays=False):
+                 count_rays=False, schedule=SCHEDULE_REFILL):
         import torch
 
         self.system = system
@@ -120,6 +121,7 @@ class DeviceReferencePathTracingRenderer:
         self.tone_map, self.exposure = tone_map, exposure
         self.background, self.background_color = background, tuple(float(c) for c in background_color)
         self.traversal, self.tlas_uniform, self.block_size = traversal, tlas_uniform, block_size
+        self.schedule = schedule
         self.radiance = (torch.zeros(self.width * self.height * 4, dtype=torch.float32, device="cuda")
                          if keep_radiance else None)
         self.ray_counts = torch.zeros(2, dtype=torch.int32, device="cuda") if count_rays else None
@@ -144,6 +146,7 @@ class DeviceReferencePathTracingRenderer:
         d.image = self.image.data_ptr()
         d.radiance = self.radiance.data_ptr() if self.radiance is not None else None
         d.ray_counts = self.ray_counts.data_ptr() if self.ray_counts is not None else None
+        d.schedule = self.schedule
         return d
 
     def render(self, stream=None):

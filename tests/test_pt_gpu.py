@@ -5,6 +5,8 @@ over progressive samples. The reference traversal order: every RGBA8 texel and
 every HDR radiance bit-identical (NaN equal to NaN); the four-child walk:
 identical except pixels whose path meets an exact-distance tie."""
 
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -73,7 +75,7 @@ def run_pair(scene_fn, traversal=rt.TRAVERSAL_REFERENCE, with_normals=False, sam
     img = np.zeros(W * H, np.uint32)
     rad = np.zeros(W * H * 4, np.float32)
     rays = [0, 0]
-    okw = {k: v for k, v in kw.items() if k not in ("block_size",)}
+    okw = {k: v for k, v in kw.items() if k not in ("block_size", "schedule")}
     for s in samples:
         r, _ = orc.pt_render(S, vp, eye, W, H, img, sample_count=s, normals=normals, radiance=rad, tlas=tlas,
                              intersector=1 if traversal & rt.INTERSECT_WATERTIGHT else 0, threads=8, **okw)
@@ -164,6 +166,17 @@ def test_ordered_walks_match_except_ties(cuda, traversal):
     assert same_bits(rad, want_rad).reshape(-1, 4).all(1).mean() > 0.995
 
 
+@pytest.mark.parametrize("name", ["field", "instanced"])
+def test_schedules_change_no_pixel(cuda, name):
+    """One thread per pixel and persistent warps refilled with pixels as paths
+    end compute every pixel with the same operations."""
+    a = run_pair(SCENES[name], traversal=rt.TRAVERSAL_ORDERED_WIDE, lights=LIGHTS, materials=MATERIALS,
+                 schedule=pt.SCHEDULE_PIXEL)
+    b = run_pair(SCENES[name], traversal=rt.TRAVERSAL_ORDERED_WIDE, lights=LIGHTS, materials=MATERIALS,
+                 schedule=pt.SCHEDULE_REFILL)
+    assert np.array_equal(a[2], b[2]) and same_bits(a[3], b[3]).all() and a[5] == b[5]
+
+
 @pytest.mark.parametrize("block_size", [32, 64])
 def test_block_size_changes_no_pixel(cuda, block_size):
     a = run_pair(field, traversal=rt.TRAVERSAL_ORDERED_WIDE, lights=LIGHTS, materials=MATERIALS)
@@ -177,7 +190,7 @@ def test_invalid_descriptors_are_rejected(cuda):
 
     scene, _, vp, eye = field()
     P = scene.build_product()
-    bad = [dict(tone_map=5), dict(background=2), dict(max_path_depth=65)]
+    bad = [dict(tone_map=5), dict(background=2), dict(max_path_depth=65), dict(schedule=2)]
     for kw in bad:
         R = pt.DeviceReferencePathTracingRenderer(P, W, H, vp, eye, **kw)
         with pytest.raises(native.RdnError):
@@ -185,13 +198,13 @@ def test_invalid_descriptors_are_rejected(cuda):
     R = pt.DeviceReferencePathTracingRenderer(P, W, H, vp, eye, keep_radiance=True)
     d = R.desc()
     d.radiance = R.radiance.data_ptr() + 4  # not 16-byte aligned
-    assert P._L.rdn_path_tracing_render(P._h, native.C.byref(d), None) == native.RDN_ERR_INVALID_ARG
+    assert P._L.rdn_path_tracing_render(P._h, ctypes.byref(d), None) == -1  # RDN_ERR_INVALID_ARG
     d = R.desc()
     d.light_count = 2  # with a null light array
-    assert P._L.rdn_path_tracing_render(P._h, native.C.byref(d), None) == native.RDN_ERR_INVALID_ARG
+    assert P._L.rdn_path_tracing_render(P._h, ctypes.byref(d), None) == -1  # RDN_ERR_INVALID_ARG
     d = R.desc()
     d.image = None
-    assert P._L.rdn_path_tracing_render(P._h, native.C.byref(d), None) == native.RDN_ERR_INVALID_ARG
+    assert P._L.rdn_path_tracing_render(P._h, ctypes.byref(d), None) == -1  # RDN_ERR_INVALID_ARG
     torch.cuda.synchronize()
     assert int(R.image.sum().item()) == 0  # nothing was written
 
