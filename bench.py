@@ -897,8 +897,8 @@ def bench_path_tracing(args, P, S_field):
                                                   count_rays=True)
         reps = 20
 
-        def timed(trav, block, sched):
-            R.traversal, R.block_size, R.schedule = trav, block, sched
+        def timed(trav, block, sched, tier=0):
+            R.traversal, R.block_size, R.schedule, R.register_tier = trav, block, sched, tier
             for _ in range(args.warmup):
                 R.render()
             R.ray_counts.zero_()
@@ -919,12 +919,18 @@ def bench_path_tracing(args, P, S_field):
                 for block in (32, 64, 128):
                     shapes[(trav, block, sched)] = timed(trav, block, sched)[0]
         best = min(shapes, key=shapes.get)
-        ms, (core, shadow) = timed(*best)
+        tiers = {0: shapes[best]}
+        if best[2] == pt.SCHEDULE_REFILL and best[0] != rt.TRAVERSAL_REFERENCE:
+            for tier in (1, 2):
+                tiers[tier] = timed(*best, tier)[0]
+        tier = min(tiers, key=tiers.get)
+        ms, (core, shadow) = timed(*best, tier)
         leg = {"size": [W, H], "ms_per_sample": round(ms, 4), "core_rays": core, "shadow_rays": shadow,
                "mrays": round((core + shadow) / ms / 1e3, 1),
                "shape": {"traversal": {0: "binary", 1: "reference", 2: "wide"}[best[0]], "block": best[1],
-                         "schedule": ("pixel", "refill")[best[2]]},
-               "shapes_ms": {f"{('pixel', 'refill')[k[2]]}/{k[0]}/{k[1]}": round(v, 4) for k, v in shapes.items()}}
+                         "schedule": ("pixel", "refill")[best[2]], "register_tier": tier},
+               "shapes_ms": {f"{('pixel', 'refill')[k[2]]}/{k[0]}/{k[1]}": round(v, 4) for k, v in shapes.items()},
+               "register_tiers_ms": {str(k): round(v, 4) for k, v in tiers.items()}}
         if name == "clamped" and S_field is not None:
             from oracle import orc
 

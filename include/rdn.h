@@ -839,6 +839,9 @@ typedef struct rdn_pt_desc {
                                      radiance (x, y, z) and the core rays of its path (w) */
   uint32_t* ray_counts;           /* device, nullable: [core, shadow] rays traced, added to */
   uint32_t schedule;              /* RDN_PT_SCHEDULE_*: how paths map to threads (no pixel changes) */
+  uint32_t register_tier;         /* refill schedule, ordered walks with local stacks: register budget per
+                                     thread, 0 = compiler's choice, 1 = at most 96, 2 = at most 64 (no
+                                     pixel changes) */
 } rdn_pt_desc;
 
 rdn_status rdn_path_tracing_render(rdn_ctx* ctx, const rdn_pt_desc* desc, void* stream);

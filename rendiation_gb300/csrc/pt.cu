@@ -169,8 +169,13 @@ __global__ void __launch_bounds__(128) pt_kernel(TraceParams P, PtEnv E) {
   pt_count(E, core, shadow);
 }
 
-template <int MODE, bool LOCAL, bool WT>
-__global__ void __launch_bounds__(128) pt_refill_kernel(TraceParams P, PtEnv E, uint32_t total) {
+// Register budget of the refill kernel (local-stack walks): 0 = the
+// compiler's choice for 128-thread blocks, 1 = at least 5 such blocks per SM
+// (at most 96 registers), 2 = at least 8 (at most 64).
+constexpr int pt_min_blocks(int tier) { return tier == 1 ? 5 : (tier == 2 ? 8 : 0); }
+
+template <int MODE, bool LOCAL, bool WT, int TIER>
+__global__ void __launch_bounds__(128, pt_min_blocks(TIER)) pt_refill_kernel(TraceParams P, PtEnv E, uint32_t total) {
   RDN_TRAVERSAL_STACK(LOCAL);
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t sample = ao_sample(E.view);
@@ -220,31 +225,45 @@ __global__ void __launch_bounds__(128) pt_refill_kernel(TraceParams P, PtEnv E, 
   pt_count(E, core, shadow);
 }
 
+template <int MODE, bool LOCAL, bool WT, int TIER>
+cudaError_t launch_refill(const TraceParams& p, const PtEnv& e, int sm_count, uint32_t block, size_t smem,
+                          cudaStream_t st) {
+  static std::atomic<uint64_t> attr_done{0};
+  cudaError_t err = raise_smem_limit(attr_done, {(const void*)pt_refill_kernel<MODE, LOCAL, WT, TIER>});
+  if (err != cudaSuccess) return err;
+  const uint32_t total = ao_dispatch_count(e.view.width, e.view.height);
+  int per_sm = 0;
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pt_refill_kernel<MODE, LOCAL, WT, TIER>, (int)block,
+                                                      smem);
+  if (err != cudaSuccess) return err;
+  if (per_sm < 1) per_sm = 1;
+  uint32_t grid = (uint32_t)((sm_count > 0 ? sm_count : 1) * per_sm);
+  const uint32_t need = (total + block - 1) / block;
+  if (grid > need) grid = need;
+  err = cudaMemsetAsync(e.fetch, 0, 4, st);
+  if (err != cudaSuccess) return err;
+  pt_refill_kernel<MODE, LOCAL, WT, TIER><<<grid, block, smem, st>>>(p, e, total);
+  return cudaGetLastError();
+}
+
 template <int MODE, bool LOCAL, bool WT>
 cudaError_t launch_variant_wt(const TraceParams& p, const PtEnv& e, int sm_count, cudaStream_t st) {
   const uint32_t block = e.view.block ? e.view.block : 128;
   const uint32_t total = ao_dispatch_count(e.view.width, e.view.height);
   const size_t smem = MODE != MODE_THREADED && !LOCAL ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
-  static std::atomic<uint64_t> attr_done{0};
-  const cudaError_t err = raise_smem_limit(
-      attr_done, {(const void*)pt_kernel<MODE, LOCAL, WT>, (const void*)pt_refill_kernel<MODE, LOCAL, WT>});
-  if (err != cudaSuccess) return err;
   if (!e.schedule) {
+    static std::atomic<uint64_t> attr_done{0};
+    const cudaError_t err = raise_smem_limit(attr_done, {(const void*)pt_kernel<MODE, LOCAL, WT>});
+    if (err != cudaSuccess) return err;
     pt_kernel<MODE, LOCAL, WT><<<(total + block - 1) / block, block, smem, st>>>(p, e);
     return cudaGetLastError();
   }
-  int per_sm = 0;
-  cudaError_t oe =
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pt_refill_kernel<MODE, LOCAL, WT>, (int)block, smem);
-  if (oe != cudaSuccess) return oe;
-  if (per_sm < 1) per_sm = 1;
-  uint32_t grid = (uint32_t)((sm_count > 0 ? sm_count : 1) * per_sm);
-  const uint32_t need = (total + block - 1) / block;
-  if (grid > need) grid = need;
-  oe = cudaMemsetAsync(e.fetch, 0, 4, st);
-  if (oe != cudaSuccess) return oe;
-  pt_refill_kernel<MODE, LOCAL, WT><<<grid, block, smem, st>>>(p, e, total);
-  return cudaGetLastError();
+  // register tiers apply to the local-stack walks
+  if constexpr (LOCAL) {
+    if (e.register_tier == 1) return launch_refill<MODE, LOCAL, WT, 1>(p, e, sm_count, block, smem, st);
+    if (e.register_tier == 2) return launch_refill<MODE, LOCAL, WT, 2>(p, e, sm_count, block, smem, st);
+  }
+  return launch_refill<MODE, LOCAL, WT, 0>(p, e, sm_count, block, smem, st);
 }
 
 template <int MODE, bool LOCAL>

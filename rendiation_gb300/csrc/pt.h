@@ -52,6 +52,7 @@ struct PtEnv {
   float4* radiance;  // nullable: per pixel (HDR radiance of this sample, core rays traced)
   uint32_t schedule;  // 0 one thread per pixel; 1 persistent warps refilled with pixels as paths end
   uint32_t* fetch;    // refill schedule: the frame's pixel counter (zeroed before the launch)
+  uint32_t register_tier;  // refill schedule, local-stack walks: 0 compiler's choice, 1 <= 96, 2 <= 64 registers
 };
 
 cudaError_t launch_pt(const TraceParams& p, const PtEnv& e, int mode, int sm_count, cudaStream_t st);

@@ -1613,6 +1613,7 @@ rdn_status rdn_path_tracing_render(rdn_ctx* c, const rdn_pt_desc* d, void* strea
   if (reinterpret_cast<uintptr_t>(d->radiance) & 15)
     return fail(c, RDN_ERR_INVALID_ARG, "radiance must be 16-byte aligned");
   if (d->schedule > RDN_PT_SCHEDULE_REFILL) return fail(c, RDN_ERR_INVALID_ARG, "unknown schedule");
+  if (d->register_tier > 2) return fail(c, RDN_ERR_INVALID_ARG, "register_tier must be 0, 1 or 2");
   std::lock_guard<std::mutex> lk(c->lock);
   rdn_ao_desc ad;
   std::memset(&ad, 0, sizeof(ad));
@@ -1645,6 +1646,7 @@ rdn_status rdn_path_tracing_render(rdn_ctx* c, const rdn_pt_desc* d, void* strea
   e.sm_count = d->sm_count;
   e.radiance = reinterpret_cast<float4*>(d->radiance);
   e.schedule = d->schedule;
+  e.register_tier = d->register_tier;
   e.fetch = c->d_counters + 13;
   cudaError_t err = cudaSetDevice(c->device);
   if (err == cudaSuccess)

@@ -155,7 +155,7 @@ class PtDesc(C.Structure):
                 ("lights", C.c_void_p), ("light_count", C.c_uint32), ("material_count", C.c_uint32),
                 ("materials", C.c_void_p), ("sm_to_material", C.c_void_p), ("sm_count", C.c_uint32),
                 ("block_size", C.c_uint32), ("normals", C.c_void_p), ("image", C.c_void_p), ("radiance", C.c_void_p),
-                ("ray_counts", C.c_void_p), ("schedule", C.c_uint32)]
+                ("ray_counts", C.c_void_p), ("schedule", C.c_uint32), ("register_tier", C.c_uint32)]
 
 
 _lib = None

@@ -90,7 +90,7 @@ class DeviceReferencePathTracingRenderer:
                  sm_to_material=None, normals=None, max_path_depth=MAX_RAY_DEPTH, tone_map=TONE_MAP_ACES_FILMIC,
                  exposure=1.0, background=BACKGROUND_SOLID, background_color=(0.0, 0.0, 0.0),
                  traversal=TRAVERSAL_ORDERED_WIDE, tlas_uniform=0, block_size=0, keep_radiance=False,
-                 count_rays=False, schedule=SCHEDULE_REFILL):
+                 count_rays=False, schedule=SCHEDULE_REFILL, register_tier=0):
         import torch
 
         self.system = system
@@ -122,6 +122,7 @@ class DeviceReferencePathTracingRenderer:
         self.background, self.background_color = background, tuple(float(c) for c in background_color)
         self.traversal, self.tlas_uniform, self.block_size = traversal, tlas_uniform, block_size
         self.schedule = schedule
+        self.register_tier = register_tier
         self.radiance = (torch.zeros(self.width * self.height * 4, dtype=torch.float32, device="cuda")
                          if keep_radiance else None)
         self.ray_counts = torch.zeros(2, dtype=torch.int32, device="cuda") if count_rays else None
@@ -147,6 +148,7 @@ class DeviceReferencePathTracingRenderer:
         d.radiance = self.radiance.data_ptr() if self.radiance is not None else None
         d.ray_counts = self.ray_counts.data_ptr() if self.ray_counts is not None else None
         d.schedule = self.schedule
+        d.register_tier = self.register_tier
         return d
 
     def render(self, stream=None):

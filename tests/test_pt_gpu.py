@@ -75,7 +75,7 @@ def run_pair(scene_fn, traversal=rt.TRAVERSAL_REFERENCE, with_normals=False, sam
     img = np.zeros(W * H, np.uint32)
     rad = np.zeros(W * H * 4, np.float32)
     rays = [0, 0]
-    okw = {k: v for k, v in kw.items() if k not in ("block_size", "schedule")}
+    okw = {k: v for k, v in kw.items() if k not in ("block_size", "schedule", "register_tier")}
     for s in samples:
         r, _ = orc.pt_render(S, vp, eye, W, H, img, sample_count=s, normals=normals, radiance=rad, tlas=tlas,
                              intersector=1 if traversal & rt.INTERSECT_WATERTIGHT else 0, threads=8, **okw)
@@ -175,6 +175,10 @@ def test_schedules_change_no_pixel(cuda, name):
     b = run_pair(SCENES[name], traversal=rt.TRAVERSAL_ORDERED_WIDE, lights=LIGHTS, materials=MATERIALS,
                  schedule=pt.SCHEDULE_REFILL)
     assert np.array_equal(a[2], b[2]) and same_bits(a[3], b[3]).all() and a[5] == b[5]
+    for tier in (1, 2):  # register budgets of the refill kernel
+        c = run_pair(SCENES[name], traversal=rt.TRAVERSAL_ORDERED_WIDE, lights=LIGHTS, materials=MATERIALS,
+                     schedule=pt.SCHEDULE_REFILL, register_tier=tier)
+        assert np.array_equal(a[2], c[2]) and same_bits(a[3], c[3]).all() and a[5] == c[5]
 
 
 @pytest.mark.parametrize("block_size", [32, 64])
@@ -190,7 +194,7 @@ def test_invalid_descriptors_are_rejected(cuda):
 
     scene, _, vp, eye = field()
     P = scene.build_product()
-    bad = [dict(tone_map=5), dict(background=2), dict(max_path_depth=65), dict(schedule=2)]
+    bad = [dict(tone_map=5), dict(background=2), dict(max_path_depth=65), dict(schedule=2), dict(register_tier=3)]
     for kw in bad:
         R = pt.DeviceReferencePathTracingRenderer(P, W, H, vp, eye, **kw)
         with pytest.raises(native.RdnError):
