@@ -638,6 +638,7 @@ rdn_status rdn_wavefront_shadow_bounce_static(rdn_ctx* ctx, const rdn_wavefront_
 #define RDN_TASK_ERROR_NO_FREE_SLOT 0x1u  /* a spawn found the group's pool full (the task stays pending) */
 #define RDN_TASK_ERROR_ACTIVE_FULL 0x2u   /* an active-list push past capacity was dropped */
 #define RDN_TASK_ERROR_REMOVED_FULL 0x4u  /* a removed-list push past capacity was dropped */
+#define RDN_TASK_ERROR_LOOKBACK 0x8u      /* a compaction tile gave up waiting for its predecessor's count */
 
 /* Trace-call payload words of TRACE tasks and of the closest-hit / miss tasks
  * they spawn: [0..7] origin xyz, tmin, direction xyz, tmax; [8] ray flags;

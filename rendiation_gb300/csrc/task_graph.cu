@@ -1,18 +1,19 @@
 // Device task graph for sm_103a (see task_graph.h for the reference map).
 //
-// One execute round runs, for each group in order, four launches:
+// One execute round runs, for each group in order:
 //   drain    commit the active / empty / removed bump counters and move the
 //            removed indices to the end of the empty pool (prepare_execution)
 //   poll     one thread per active task: run its program, then finish it
 //            (wake the parent or clean up) or put it to sleep
-//   count    commit the active list, count the tasks still NOT_FINISHED_WAKEN
-//            per 1024-entry tile (GO_TO_SLEEP becomes SLEEP), and in the last
-//            block to finish, scan the tile counts
-//   scatter  write the kept indices, in order, to the other active buffer
+//   compact  commit the active list and keep the tasks still
+//            NOT_FINISHED_WAKEN, in order (GO_TO_SLEEP becomes SLEEP), in one
+//            pass over 1024-entry tiles with decoupled look-back
+// The compaction of group g and the drain of group g + 1 run in one launch
+// (bookkeep_kernel), so a round of n groups takes 2n launches.
 // The committed sizes live in a 64 B control block per group in device memory:
 // no host round trip inside a round, and a sequence of rounds can be captured
-// into a CUDA graph. The last-block pattern (a ticket counter) lets the first
-// blocks read the old sizes while only the last one writes the new ones.
+// into a CUDA graph. The drain's last-block pattern (a ticket counter) lets the
+// first blocks read the old sizes while only the last one writes the new ones.
 // record_until_empty captures the rounds as the body of a WHILE conditional
 // node that a one-warp check ends once no group has an active task.
 // Programs: the built-in chain program runs in poll_chain_kernel, the trace
@@ -260,12 +261,39 @@ __device__ __forceinline__ void poll_active(const TaskGraphDev& G, uint32_t g, c
   }
 }
 
+// Trace polls: persistent warps take 32 consecutive active entries at a time
+// from the group's poll counter, so a warp whose rays end early takes more and
+// the grid is sized by residency, not by the pool's capacity.
+template <class Poll>
+__device__ __forceinline__ void poll_active_fetch(const TaskGraphDev& G, uint32_t g, const Poll& poll) {
+  const TaskGroupDev& T = G.g[g];
+  GroupCtl* c = T.ctl;
+  const uint32_t n = c->active.size;
+  const uint32_t* list = T.active[c->sel];
+  const uint32_t lane = threadIdx.x & 31u;
+  for (;;) {
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(&c->poll_next, 32u);
+    base = __shfl_sync(0xFFFFFFFFu, base, 0);
+    if (base >= n) break;
+    const uint32_t i = base + lane;
+    if (i < n) {
+      const uint32_t idx = list[i];
+      const uint32_t pi = T.parent_index[idx], pt = T.parent_type[idx];
+      if (pi != TASK_NO_PARENT && pt < G.n_groups)
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(G.g[pt].state + pi));
+      finalize(G, g, idx, poll(idx), pi, pt);
+    }
+  }
+}
+
 template <int MODE, bool LOCAL, bool WT>
 __global__ void __launch_bounds__(kPollThreads, 8) poll_kernel(const TaskGraphDev* __restrict__ Gp, uint32_t g,
                                                             TraceParams P, AoEnv) {
   RDN_TRAVERSAL_STACK(LOCAL);
   const TaskGraphDev& G = *Gp;
-  poll_active(G, g, [&](uint32_t idx) { return poll_trace<MODE, WT>(G, g, idx, P, stack_ptr, stack_stride); });
+  poll_active_fetch(G, g,
+                    [&](uint32_t idx) { return poll_trace<MODE, WT>(G, g, idx, P, stack_ptr, stack_stride); });
 }
 
 // Chain groups alone: without the traversal the kernel fits twice the resident
@@ -284,8 +312,10 @@ __device__ __forceinline__ uint32_t commit_dealloc(uint32_t size, uint32_t bump)
   return bump > size ? 0u : size - bump;
 }
 
-// prepare_execution: commit the three bump lists, drain removed -> empty.
-__global__ void __launch_bounds__(256) drain_kernel(TaskGroupDev T, uint32_t* ticket) {
+// prepare_execution of group T, one of nb blocks: commit the three bump lists,
+// drain removed -> empty; the last block writes the committed sizes and opens
+// the group's next compaction (tile counter 0, next epoch).
+__device__ __forceinline__ void drain_part(const TaskGroupDev& T, uint32_t b, uint32_t nb, uint32_t* ticket) {
   GroupCtl* c = T.ctl;
   __shared__ uint32_t s_removed, s_empty, s_last;
   if (threadIdx.x == 0) {
@@ -294,11 +324,11 @@ __global__ void __launch_bounds__(256) drain_kernel(TaskGroupDev T, uint32_t* ti
   }
   __syncthreads();
   const uint32_t n = s_removed, off = s_empty;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+  for (uint32_t i = b * blockDim.x + threadIdx.x; i < n; i += nb * blockDim.x)
     if (off + i < T.cap) T.empty[off + i] = T.removed[i];
   __threadfence();
   __syncthreads();
-  if (threadIdx.x == 0) s_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  if (threadIdx.x == 0) s_last = atomicAdd(ticket, 1u) == nb - 1;
   __syncthreads();
   if (s_last && threadIdx.x == 0) {
     __threadfence();
@@ -310,6 +340,9 @@ __global__ void __launch_bounds__(256) drain_kernel(TaskGroupDev T, uint32_t* ti
     c->removed.bump = 0u;
     c->drain_n = n;
     c->drain_off = off;
+    c->tile_next = 0u;
+    c->poll_next = 0u;
+    c->epoch = c->epoch + 1u;
     *ticket = 0u;
   }
 }
@@ -334,101 +367,151 @@ __device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t* warp_sums) {
   return t;
 }
 
-// Commit of the active list and first half of the compaction
-// (ActiveTaskCompact); the last block scans the tile counts and writes the
-// new size.
-__global__ void __launch_bounds__(kCompactThreads) compact_count_kernel(TaskGroupDev T, uint32_t ntiles,
-                                                                        uint32_t* ticket) {
-  GroupCtl* c = T.ctl;
-  __shared__ uint32_t s_n, s_sel, s_last, warp_sums[kCompactThreads / 32];
-  if (threadIdx.x == 0) {
-    s_n = commit_alloc(c->active.size, c->active.bump, T.cap);
-    s_sel = c->sel;
-  }
-  __syncthreads();
-  const uint32_t n = s_n;
-  const uint32_t* list = T.active[s_sel];
-  uint32_t kept = 0;
-  const uint32_t base = blockIdx.x * kTile;
-  for (uint32_t j = 0; j < kTile / kCompactThreads; j++) {
-    const uint32_t i = base + j * kCompactThreads + threadIdx.x;
-    if (i < n) {
-      const uint32_t idx = list[i];
-      const uint32_t st = T.state[idx];
-      if (st == TASK_GO_TO_SLEEP) T.state[idx] = TASK_NOT_FINISHED_SLEEP;
-      kept += st == TASK_NOT_FINISHED_WAKEN;
-    }
-  }
-  const uint32_t total = block_sum(kept, warp_sums);
-  if (threadIdx.x == 0) T.tile_offsets[blockIdx.x] = total;
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) s_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
-  __syncthreads();
-  if (!s_last) return;
-  __threadfence();
-  // exclusive scan of the tile counts, kCompactThreads at a time
-  __shared__ uint32_t s_carry;
-  if (threadIdx.x == 0) s_carry = 0;
-  __syncthreads();
-  for (uint32_t b0 = 0; b0 < ntiles; b0 += kCompactThreads) {
-    const uint32_t t = b0 + threadIdx.x;
-    const uint32_t v = t < ntiles ? *((volatile uint32_t*)(T.tile_offsets + t)) : 0u;
-    uint32_t x = v;
-    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
-      if (lane >= (uint32_t)o) x += y;
-    }
-    if (lane == 31) warp_sums[warp] = x;
-    __syncthreads();
-    uint32_t before = s_carry;
-    for (uint32_t w = 0; w < warp; w++) before += warp_sums[w];
-    if (t < ntiles) T.tile_offsets[t] = before + x - v;
-    __syncthreads();
-    if (threadIdx.x == kCompactThreads - 1) s_carry = before + x;
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    c->compact_n = n;
-    c->src_sel = s_sel;
-    c->sel = s_sel ^ 1u;
-    c->active.size = s_carry;
-    c->active.bump = 0u;
-    *ticket = 0u;
-  }
+__device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
-// Second half of the compaction: kept indices, in order, to the other buffer.
-__global__ void __launch_bounds__(kCompactThreads) compact_scatter_kernel(TaskGroupDev T) {
-  const GroupCtl* c = T.ctl;
-  const uint32_t n = c->compact_n;
-  const uint32_t base = blockIdx.x * kTile;
-  if (base >= n) return;
-  const uint32_t* src = T.active[c->src_sel];
-  uint32_t* dst = T.active[c->src_sel ^ 1u];
-  __shared__ uint32_t warp_counts[kCompactThreads / 32];
-  uint32_t offset = T.tile_offsets[blockIdx.x];
-  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-  for (uint32_t j = 0; j < kTile / kCompactThreads; j++) {
+constexpr unsigned long long kTileAggregate = 1ull, kTileInclusive = 2ull;
+constexpr uint32_t kLookbackLimit = 1u << 22;  // predecessor polls before a tile gives up
+
+// One 1024-entry tile of the compaction (see compact_part).
+__device__ __forceinline__ void compact_tile(const TaskGroupDev& T, GroupCtl* c, uint32_t tile, uint32_t n,
+                                             uint32_t used, uint32_t sel, uint32_t* err, uint32_t& s_excl,
+                                             uint32_t* warp_sums) {
+  const uint32_t s_epoch = c->epoch & 0x3FFFFFFFu;
+  const uint32_t* list = T.active[sel];
+  const uint32_t base = tile * kTile;
+  constexpr uint32_t kPer = kTile / kCompactThreads;
+  uint32_t idx[kPer];
+  bool keep[kPer];
+  uint32_t kept = 0;
+#pragma unroll
+  for (uint32_t j = 0; j < kPer; j++) {
     const uint32_t i = base + j * kCompactThreads + threadIdx.x;
-    uint32_t idx = 0;
-    bool keep = false;
+    idx[j] = 0u;
+    keep[j] = false;
     if (i < n) {
-      idx = src[i];
-      keep = T.state[idx] == TASK_NOT_FINISHED_WAKEN;
+      idx[j] = list[i];
+      const uint32_t st = T.state[idx[j]];
+      if (st == TASK_GO_TO_SLEEP) T.state[idx[j]] = TASK_NOT_FINISHED_SLEEP;
+      keep[j] = st == TASK_NOT_FINISHED_WAKEN;
     }
-    const uint32_t ballot = __ballot_sync(0xFFFFFFFFu, keep);
-    if (lane == 0) warp_counts[warp] = __popc(ballot);
+    kept += keep[j];
+  }
+  const uint32_t total = block_sum(kept, warp_sums);
+  if (threadIdx.x < 32) {
+    // warp 0: publish the tile's count, then look back 32 descriptors at a
+    // time (lane l reads tile p - l) until the nearest inclusive prefix
+    const uint32_t lane = threadIdx.x;
+    const unsigned long long ep = (unsigned long long)s_epoch << 34;
+    uint32_t excl = 0;
+    if (tile == 0) {
+      if (lane == 0) st_release(T.tile_desc, ep | (kTileInclusive << 32) | total);
+    } else {
+      if (lane == 0) st_release(T.tile_desc + tile, ep | (kTileAggregate << 32) | total);
+      int p = (int)tile - 1;
+      uint32_t polls = 0;
+      while (p >= 0) {
+        const int q = p - (int)lane;
+        bool ready = true, incl = true;
+        uint32_t val = 0;
+        if (q >= 0) {
+          const unsigned long long v = ld_acquire(T.tile_desc + q);
+          const unsigned long long status = (v >> 32) & 3ull;
+          ready = (uint32_t)(v >> 34) == s_epoch && status != 0ull;
+          incl = status == kTileInclusive;
+          val = (uint32_t)v;
+        }
+        if (!__all_sync(0xFFFFFFFFu, ready)) {
+          if (++polls > kLookbackLimit) {  // uniform across the warp
+            if (lane == 0) atomicOr(err, TASK_ERR_LOOKBACK);
+            break;
+          }
+          continue;
+        }
+        const uint32_t incl_mask = __ballot_sync(0xFFFFFFFFu, incl);
+        // lanes up to the nearest inclusive descriptor (the lowest such lane) contribute
+        const uint32_t stop = incl_mask ? (uint32_t)(__ffs(incl_mask) - 1) : 31u;
+        uint32_t part = lane <= stop ? val : 0u;
+        for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xFFFFFFFFu, part, o);
+        excl += part;
+        if (incl_mask) break;
+        p -= 32;
+      }
+      if (lane == 0) st_release(T.tile_desc + tile, ep | (kTileInclusive << 32) | (excl + total));
+    }
+    if (lane == 0) s_excl = excl;
+  }
+  __syncthreads();
+  uint32_t* dst = T.active[sel ^ 1u];
+  uint32_t offset = s_excl;
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (uint32_t j = 0; j < kPer; j++) {
+    const uint32_t ballot = __ballot_sync(0xFFFFFFFFu, keep[j]);
+    if (lane == 0) warp_sums[warp] = __popc(ballot);
     __syncthreads();
     uint32_t before = offset;
-    for (uint32_t w = 0; w < warp; w++) before += warp_counts[w];
-    if (keep) dst[before + __popc(ballot & ((1u << lane) - 1u))] = idx;
+    for (uint32_t w = 0; w < warp; w++) before += warp_sums[w];
+    if (keep[j]) dst[before + __popc(ballot & ((1u << lane) - 1u))] = idx[j];
     uint32_t round = 0;
-    for (uint32_t w = 0; w < kCompactThreads / 32; w++) round += warp_counts[w];
+    for (uint32_t w = 0; w < kCompactThreads / 32; w++) round += warp_sums[w];
     __syncthreads();
     offset += round;
   }
+  if (threadIdx.x == 0 && tile == (used ? used - 1u : 0u)) {
+    c->compact_n = n;
+    c->src_sel = sel;
+    c->sel = sel ^ 1u;
+    c->active.size = used ? s_excl + total : 0u;
+    c->active.bump = 0u;
+  }
+}
+
+// Commit of the active list and its compaction (ActiveTaskCompact) in one
+// pass: each block takes the next 1024-entry tile, keeps the tasks still
+// NOT_FINISHED_WAKEN (GO_TO_SLEEP becomes SLEEP), publishes its count and
+// finds its offset by looking back over the descriptors of the tiles before
+// it (decoupled look-back, Merrill and Garland 2016), then writes its kept
+// indices, in order, to the other active buffer. Tiles are handed out in
+// block arrival order, so every tile a block waits for belongs to a block
+// that is already running. The block of the last tile writes the new size.
+__device__ __forceinline__ void compact_part(const TaskGroupDev& T, uint32_t* err) {
+  GroupCtl* c = T.ctl;
+  __shared__ uint32_t s_tile, s_n, s_sel, s_epoch, s_excl, warp_sums[kCompactThreads / 32];
+  if (threadIdx.x == 0) {
+    s_n = commit_alloc(c->active.size, c->active.bump, T.cap);
+    s_sel = c->sel;
+    s_epoch = c->epoch & 0x3FFFFFFFu;
+  }
+  __syncthreads();
+  const uint32_t n = s_n, sel = s_sel;
+  const uint32_t used = (n + kTile - 1) / kTile;
+  // a block arriving after the last tile's block finished reads a size no
+  // larger than the one the tiles were cut from, and takes no tile
+  for (;;) {
+    if (threadIdx.x == 0) s_tile = atomicAdd(&c->tile_next, 1u);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    __syncthreads();
+    if (tile >= (used ? used : 1u)) return;
+    compact_tile(T, c, tile, n, used, sel, err, s_excl, warp_sums);
+  }
+}
+
+// Bookkeeping between two polls, one launch: blocks [0, nc) compact group Tc
+// after its poll, blocks [nc, nc + nd) drain group Td before its poll. The two
+// groups' lists are disjoint, so the reference's order (compact g, then
+// prepare g + 1) holds. nc = 0 or nd = 0 runs one part alone.
+__global__ void __launch_bounds__(kCompactThreads) bookkeep_kernel(TaskGroupDev Tc, uint32_t nc, TaskGroupDev Td,
+                                                                   uint32_t nd, uint32_t* ticket, uint32_t* err) {
+  if (blockIdx.x < nc) compact_part(Tc, err);
+  else drain_part(Td, blockIdx.x - nc, nd, ticket);
 }
 
 // TaskGroupExecutorResource::init: empty pool = 1..cap, fallback task 0.
@@ -587,7 +670,7 @@ std::string TaskGraph::create(const std::vector<TaskGroupDesc>& groups, uint32_t
     }
     const size_t rec = (size_t)T.cap + 1;
     const size_t words = rec * 3 + rec * d.payload_words + rec * kTaskLocalWords + (size_t)T.cap * 4 +
-                         tiles_of(T.cap) + 64;
+                         2 * (size_t)tiles_of(T.cap) + 66;
     void* mem = nullptr;
     e = cudaMalloc(&mem, words * 4);
     if (e != cudaSuccess) return std::string("cudaMalloc: ") + cudaGetErrorString(e);
@@ -613,7 +696,8 @@ std::string TaskGraph::create(const std::vector<TaskGroupDesc>& groups, uint32_t
     w += T.cap;
     T.empty = w;
     w += T.cap;
-    T.tile_offsets = w;
+    w += (reinterpret_cast<uintptr_t>(w) & 7u) ? 1 : 0;  // 8-byte aligned tile descriptors
+    T.tile_desc = reinterpret_cast<unsigned long long*>(w);
     T.ctl = ctls + g;
     const uint32_t grid = std::min<uint32_t>((T.cap + 255) / 256, (uint32_t)sm_count_ * 8);
     init_kernel<<<grid, 256, 0, st>>>(T);
@@ -632,27 +716,34 @@ std::string TaskGraph::create(const std::vector<TaskGroupDesc>& groups, uint32_t
   return "";
 }
 
-cudaError_t TaskGraph::prepare(uint32_t g, cudaStream_t st) {
-  const TaskGroupDev& T = dev_.g[g];
-  const uint32_t grid = std::max<uint32_t>(1, std::min<uint32_t>((T.cap + 255) / 256, (uint32_t)sm_count_ * 4));
-  drain_kernel<<<grid, 256, 0, st>>>(T, dev_.error + 2 + 2 * g);
+// compact group gc (kNone: no compaction) and drain group gd (kNone: none) in one launch
+cudaError_t TaskGraph::bookkeep(uint32_t gc, uint32_t gd, cudaStream_t st) {
+  constexpr uint32_t kNone = 0xFFFFFFFFu;
+  // persistent blocks: the compaction's take tiles in turn, the drain's stride over the removed list
+  const uint32_t nc = gc == kNone ? 0u : std::min<uint32_t>(tiles_of(dev_.g[gc].cap), (uint32_t)sm_count_ * 8);
+  uint32_t nd = 0;
+  if (gd != kNone)
+    nd = std::max<uint32_t>(1, std::min<uint32_t>((dev_.g[gd].cap + 255) / 256, (uint32_t)sm_count_));
+  if (nc + nd == 0) return cudaSuccess;
+  const TaskGroupDev& Tc = dev_.g[gc == kNone ? 0u : gc];
+  const TaskGroupDev& Td = dev_.g[gd == kNone ? 0u : gd];
+  bookkeep_kernel<<<nc + nd, kCompactThreads, 0, st>>>(Tc, nc, Td, nd, dev_.error + 2 + 2 * (gd == kNone ? 0u : gd),
+                                                       dev_.error);
   return cudaGetLastError();
 }
 
-cudaError_t TaskGraph::compact(uint32_t g, cudaStream_t st) {
-  const TaskGroupDev& T = dev_.g[g];
-  const uint32_t nt = tiles_of(T.cap);
-  compact_count_kernel<<<nt, kCompactThreads, 0, st>>>(T, nt, dev_.error + 3 + 2 * g);
-  compact_scatter_kernel<<<nt, kCompactThreads, 0, st>>>(T);
-  return cudaGetLastError();
-}
+cudaError_t TaskGraph::prepare(uint32_t g, cudaStream_t st) { return bookkeep(0xFFFFFFFFu, g, st); }
+
+cudaError_t TaskGraph::compact(uint32_t g, cudaStream_t st) { return bookkeep(g, 0xFFFFFFFFu, st); }
 
 cudaError_t TaskGraph::poll(uint32_t g, const TraceParams* p, int mode, const AoEnv* ao, cudaStream_t st) {
   const TaskGroupDev& T = dev_.g[g];
-  // one thread per possible active entry: blocks past the committed size exit
-  // at once, and a block's traversals do not queue behind one another as in
-  // a grid-stride loop (divergent trace polls finish when their slowest ray does)
-  const uint32_t grid = std::max<uint32_t>(1, (T.cap + kPollThreads - 1) / kPollThreads);
+  // chain polls: one thread per possible active entry (blocks past the
+  // committed size exit at once; their polls are chains of dependent loads
+  // that want every task's loads in flight); trace polls: persistent warps
+  // that fetch entries, so that divergent rays do not hold a block's slot
+  const uint32_t cap_blocks = std::max<uint32_t>(1, (T.cap + kPollThreads - 1) / kPollThreads);
+  const uint32_t grid = cap_blocks;
   TraceParams P;
   AoEnv A;
   if (p)
@@ -672,14 +763,16 @@ cudaError_t TaskGraph::poll(uint32_t g, const TraceParams* p, int mode, const Ao
     poll_chain_kernel<<<grid, kPollThreads, 0, st>>>(G, g, P, A);
     return cudaGetLastError();
   }
-  if (!p) return launch_poll<MODE_THREADED, false>(G, g, P, A, grid, st);
+  // the trace poll's launch bounds guarantee 8 resident blocks per SM
+  const uint32_t tgrid = std::min<uint32_t>(cap_blocks, (uint32_t)sm_count_ * 8);
+  if (!p) return launch_poll<MODE_THREADED, false>(G, g, P, A, tgrid, st);
   if (mode == MODE_WIDE4)
-    return P.local_stack ? launch_poll<MODE_WIDE4, true>(G, g, P, A, grid, st)
-                         : launch_poll<MODE_WIDE4, false>(G, g, P, A, grid, st);
+    return P.local_stack ? launch_poll<MODE_WIDE4, true>(G, g, P, A, tgrid, st)
+                         : launch_poll<MODE_WIDE4, false>(G, g, P, A, tgrid, st);
   if (mode == MODE_BINARY)
-    return P.local_stack ? launch_poll<MODE_BINARY, true>(G, g, P, A, grid, st)
-                         : launch_poll<MODE_BINARY, false>(G, g, P, A, grid, st);
-  return launch_poll<MODE_THREADED, false>(G, g, P, A, grid, st);
+    return P.local_stack ? launch_poll<MODE_BINARY, true>(G, g, P, A, tgrid, st)
+                         : launch_poll<MODE_BINARY, false>(G, g, P, A, tgrid, st);
+  return launch_poll<MODE_THREADED, false>(G, g, P, A, tgrid, st);
 }
 
 cudaError_t TaskGraph::dispatch_init(uint32_t group, uint32_t count, uint32_t init_op, cudaStream_t st) {
@@ -691,14 +784,18 @@ cudaError_t TaskGraph::dispatch_init(uint32_t group, uint32_t count, uint32_t in
   return cudaGetLastError();
 }
 
+// A round is, for each group in order, prepare (drain), poll, compact. The
+// compaction of group g and the drain of group g + 1 touch disjoint lists and
+// share one launch, so a round of n groups takes 2n launches.
 cudaError_t TaskGraph::execute(uint32_t rounds, const TraceParams* p, int mode, const AoEnv* ao, cudaStream_t st) {
+  const uint32_t n = dev_.n_groups;
   for (uint32_t r = 0; r < rounds; r++) {
-    for (uint32_t g = 0; g < dev_.n_groups; g++) {
-      cudaError_t e = prepare(g, st);
-      if (e == cudaSuccess) e = poll(g, p, mode, ao, st);
-      if (e == cudaSuccess) e = compact(g, st);
-      if (e != cudaSuccess) return e;
+    cudaError_t e = prepare(0, st);
+    for (uint32_t g = 0; g < n && e == cudaSuccess; g++) {
+      e = poll(g, p, mode, ao, st);
+      if (e == cudaSuccess) e = bookkeep(g, g + 1 < n ? g + 1 : 0xFFFFFFFFu, st);
     }
+    if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
 }

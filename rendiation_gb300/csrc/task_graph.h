@@ -56,6 +56,7 @@ constexpr uint32_t TRACE_SUB_SPAWN_FAILED = 0xFFFFFFFEu;
 constexpr uint32_t TASK_ERR_NO_FREE_SLOT = 0x1;  // spawn found the empty pool exhausted
 constexpr uint32_t TASK_ERR_ACTIVE_FULL = 0x2;   // an active-list push past the list's capacity
 constexpr uint32_t TASK_ERR_REMOVED_FULL = 0x4;  // a removed-list push past its capacity
+constexpr uint32_t TASK_ERR_LOOKBACK = 0x8;      // a compaction tile waited past its limit for a predecessor
 
 // Task local words (the reference's per-task future state): [0] base future
 // polled once, [1..4] child handles of the chain's spawn stages, [5] trace
@@ -108,7 +109,10 @@ struct GroupCtl {
   uint32_t drain_n;    // removed entries the drain copies
   uint32_t drain_off;  // where they go in the empty pool
   uint32_t compact_n;  // committed active size the compaction reads
-  uint32_t pad[5];
+  uint32_t tile_next;  // next compaction tile to hand out (reset by the drain)
+  uint32_t epoch;      // compaction generation: tile descriptors of older ones read as unset
+  uint32_t poll_next;  // next active entry a trace poll's warp takes (reset by the drain)
+  uint32_t pad[2];
 };
 static_assert(sizeof(GroupCtl) == 64, "64 B control block");
 
@@ -121,7 +125,7 @@ struct TaskGroupDev {
   uint32_t* active[2];
   uint32_t* removed;
   uint32_t* empty;
-  uint32_t* tile_offsets;  // compaction scratch, one per tile
+  unsigned long long* tile_desc;  // compaction tile descriptors: epoch (30 bits) | status (2) | count (32)
   GroupCtl* ctl;
   uint32_t cap;  // max_in_flight * capacity; the pool holds cap + 1 records
   uint32_t payload_words;
@@ -209,6 +213,7 @@ class TaskGraph {
  private:
   cudaError_t prepare(uint32_t g, cudaStream_t st);
   cudaError_t compact(uint32_t g, cudaStream_t st);
+  cudaError_t bookkeep(uint32_t gc, uint32_t gd, cudaStream_t st);
   cudaError_t poll(uint32_t g, const TraceParams* p, int mode, const AoEnv* ao, cudaStream_t st);
 
   TaskGraphDev dev_{};
