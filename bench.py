@@ -852,7 +852,7 @@ def bench_ao(args, P, S_field):
         d.sample_counter = None
         out[mode + "_captured_ms"], out[mode + "_captured_mrays"] = round(ms, 4), round(rays_c / ms / 1e3, 1)
     out["graph_over_fused"] = round(out["graph_ms"] / out["fused_ms"], 2)
-    out["graph_launches_per_frame"] = 3 + 8 * 5 * 4
+    out["graph_launches_per_frame"] = 3 + 8 * (1 + 5 * 2)  # per round: drain, then a poll and a bookkeep per group
     out["captured"] = "rdn_ao_capture: one CUDA graph per frame, sample index read from a device counter"
     st, flags = P.check_errors()
     assert st == 0 and flags == 0
