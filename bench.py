@@ -914,13 +914,13 @@ def bench_path_tracing(args, P, S_field):
         shapes = {}
         travs = (rt.TRAVERSAL_REFERENCE,) if args.traversal == "reference" else (rt.TRAVERSAL_ORDERED,
                                                                                   rt.TRAVERSAL_ORDERED_WIDE)
-        for sched in (pt.SCHEDULE_PIXEL, pt.SCHEDULE_REFILL):
+        for sched in (pt.SCHEDULE_PIXEL, pt.SCHEDULE_REFILL, pt.SCHEDULE_WAVEFRONT):
             for trav in travs:
                 for block in (32, 64, 128):
                     shapes[(trav, block, sched)] = timed(trav, block, sched)[0]
         best = min(shapes, key=shapes.get)
         tiers = {0: shapes[best]}
-        if best[2] == pt.SCHEDULE_REFILL and best[0] != rt.TRAVERSAL_REFERENCE:
+        if best[2] != pt.SCHEDULE_PIXEL and best[0] != rt.TRAVERSAL_REFERENCE:
             for tier in (1, 2):
                 tiers[tier] = timed(*best, tier)[0]
         tier = min(tiers, key=tiers.get)
@@ -928,8 +928,9 @@ def bench_path_tracing(args, P, S_field):
         leg = {"size": [W, H], "ms_per_sample": round(ms, 4), "core_rays": core, "shadow_rays": shadow,
                "mrays": round((core + shadow) / ms / 1e3, 1),
                "shape": {"traversal": {0: "binary", 1: "reference", 2: "wide"}[best[0]], "block": best[1],
-                         "schedule": ("pixel", "refill")[best[2]], "register_tier": tier},
-               "shapes_ms": {f"{('pixel', 'refill')[k[2]]}/{k[0]}/{k[1]}": round(v, 4) for k, v in shapes.items()},
+                         "schedule": ("pixel", "refill", "wavefront")[best[2]], "register_tier": tier},
+               "shapes_ms": {f"{('pixel', 'refill', 'wavefront')[k[2]]}/{k[0]}/{k[1]}": round(v, 4)
+                             for k, v in shapes.items()},
                "register_tiers_ms": {str(k): round(v, 4) for k, v in tiers.items()}}
         if name == "clamped" and S_field is not None:
             from oracle import orc

@@ -789,6 +789,9 @@ rdn_status rdn_ao_capture(rdn_ctx* ctx, rdn_task_graph* pipeline, const rdn_ao_d
 #define RDN_PT_SCHEDULE_PIXEL 0u     /* one thread per pixel, warps over 8x4 tiles */
 #define RDN_PT_SCHEDULE_REFILL 1u    /* persistent warps; a lane whose path ends takes the next pixel (the
                                         frame uses the context's work counter: one frame in flight per context) */
+#define RDN_PT_SCHEDULE_WAVEFRONT 2u /* one pass per ray kind and depth over queues of paths, the path state in
+                                        the caller's scratch (rdn_pt_scratch_size): warps trace camera, bounce
+                                        or shadow rays only */
 
 /* DirectionalLightStorage's illuminance and direction (the direction light travels). */
 typedef struct rdn_pt_directional_light {
@@ -840,11 +843,16 @@ typedef struct rdn_pt_desc {
                                      radiance (x, y, z) and the core rays of its path (w) */
   uint32_t* ray_counts;           /* device, nullable: [core, shadow] rays traced, added to */
   uint32_t schedule;              /* RDN_PT_SCHEDULE_*: how paths map to threads (no pixel changes) */
-  uint32_t register_tier;         /* refill schedule, ordered walks with local stacks: register budget per
-                                     thread, 0 = compiler's choice, 1 = at most 96, 2 = at most 64 (no
-                                     pixel changes) */
+  uint32_t register_tier;         /* refill and wavefront schedules, ordered walks with local stacks:
+                                     register budget per thread, 0 = compiler's choice, 1 = at most 96,
+                                     2 = at most 64 (no pixel changes) */
+  void* scratch;                  /* device, 256-byte aligned, >= rdn_pt_scratch_size(): wavefront schedule */
+  size_t scratch_bytes;
 } rdn_pt_desc;
 
+/* Scratch of the wavefront schedule for a width x height frame: 112 B of path
+ * state and two 4 B queue entries per pixel. */
+rdn_status rdn_pt_scratch_size(uint32_t width, uint32_t height, size_t* bytes);
 rdn_status rdn_path_tracing_render(rdn_ctx* ctx, const rdn_pt_desc* desc, void* stream);
 
 #ifdef __cplusplus

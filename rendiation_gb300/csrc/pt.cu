@@ -10,11 +10,15 @@
 //   refill  persistent warps: a lane whose path ends takes the next pixel
 //           (warp-aggregated atomic on a frame counter), so warps stay full
 //           until the frame runs out (Aila and Laine 2009, "persistent
-//           while-while" with dynamic fetch, at path granularity).
-// Both compute each pixel with the same operations. Built with -fmad=false:
+//           while-while" with dynamic fetch, at path granularity);
+//   wavefront  one pass per ray kind and depth over queues of pixel indices,
+//           the path state in HBM between passes: every warp traces rays of
+//           one kind (camera, bounce or shadow).
+// All compute each pixel with the same operations. Built with -fmad=false:
 // see pt.cuh.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 
 #include "pt.cuh"
@@ -225,6 +229,149 @@ __global__ void __launch_bounds__(128, pt_min_blocks(TIER)) pt_refill_kernel(Tra
   pt_count(E, core, shadow);
 }
 
+// ---- wavefront schedule ----
+// Path state word-major (word k of pixel i at state[k * n_pix + i]):
+// o 0-2, d 3-5, throughput 6-8, radiance 9-11, shading normal 12-14,
+// shadow origin 15-17, light direction 18-20, light radiance 21-23, sm_id 24,
+// depth 25, core rays 26, shadow rays 27.
+__device__ __forceinline__ void pt_st3(uint32_t* s, uint32_t n, uint32_t k, uint32_t i, float3 v) {
+  s[(size_t)k * n + i] = __float_as_uint(v.x);
+  s[(size_t)(k + 1) * n + i] = __float_as_uint(v.y);
+  s[(size_t)(k + 2) * n + i] = __float_as_uint(v.z);
+}
+__device__ __forceinline__ float3 pt_ld3(const uint32_t* s, uint32_t n, uint32_t k, uint32_t i) {
+  return make_float3(__uint_as_float(s[(size_t)k * n + i]), __uint_as_float(s[(size_t)(k + 1) * n + i]),
+                     __uint_as_float(s[(size_t)(k + 2) * n + i]));
+}
+__device__ __forceinline__ void pt_save(const PtWave& W, uint32_t i, const PtPath& q) {
+  uint32_t* s = W.state;
+  const uint32_t n = W.n_pix;
+  pt_st3(s, n, 0, i, q.o);
+  pt_st3(s, n, 3, i, q.d);
+  pt_st3(s, n, 6, i, q.throughput);
+  pt_st3(s, n, 9, i, q.radiance);
+  pt_st3(s, n, 12, i, q.sn);
+  pt_st3(s, n, 15, i, q.origin);
+  pt_st3(s, n, 18, i, q.ldir);
+  pt_st3(s, n, 21, i, q.lrad);
+  s[(size_t)24 * n + i] = q.sm_id;
+  s[(size_t)25 * n + i] = q.depth;
+  s[(size_t)26 * n + i] = q.core;
+  s[(size_t)27 * n + i] = q.shadow;
+}
+__device__ __forceinline__ void pt_load(const PtWave& W, uint32_t i, uint32_t width, PtPath& q) {
+  const uint32_t* s = W.state;
+  const uint32_t n = W.n_pix;
+  q.x = i % width;
+  q.y = i / width;
+  q.o = pt_ld3(s, n, 0, i);
+  q.d = pt_ld3(s, n, 3, i);
+  q.throughput = pt_ld3(s, n, 6, i);
+  q.radiance = pt_ld3(s, n, 9, i);
+  q.sn = pt_ld3(s, n, 12, i);
+  q.origin = pt_ld3(s, n, 15, i);
+  q.ldir = pt_ld3(s, n, 18, i);
+  q.lrad = pt_ld3(s, n, 21, i);
+  q.sm_id = s[(size_t)24 * n + i];
+  q.depth = s[(size_t)25 * n + i];
+  q.core = s[(size_t)26 * n + i];
+  q.shadow = s[(size_t)27 * n + i];
+}
+
+// One pass of the wavefront schedule: persistent warps take 32 queue entries
+// at a time; each lane traces its path's next ray (all core rays or all
+// shadow rays: with lights the passes alternate core, shadow, core, ...,
+// since every core hit casts a shadow ray and every shadow ray is followed by
+// a core ray), advances the path and queues it for the next pass or resolves
+// its pixel. Pass 0 starts the paths from the camera, 8x4 pixel tiles per warp.
+template <int MODE, bool LOCAL, bool WT, int TIER>
+__global__ void __launch_bounds__(128, pt_min_blocks(TIER))
+    pt_pass_kernel(TraceParams P, PtEnv E, PtWave W, uint32_t pass, uint32_t shadow_pass) {
+  RDN_TRAVERSAL_STACK(LOCAL);
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t sample = ao_sample(E.view);
+  const uint32_t width = E.view.width;
+  const uint32_t total = pass == 0 ? ao_dispatch_count(E.view.width, E.view.height) : W.counters[pass - 1];
+  const uint32_t* qin = W.queue[(pass + 1) & 1];
+  uint32_t* qout = W.queue[pass & 1];
+  uint32_t* fetch = W.counters + kPtMaxPasses + pass;
+  uint32_t core = 0, shadow = 0;
+  bool bad = false;
+  for (;;) {
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(fetch, 32u);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= total) break;
+    const uint32_t i = base + lane;
+    PtPath q;
+    uint32_t pix = 0;
+    bool live = false;
+    if (i < total) {
+      if (pass == 0) {
+        uint32_t x, y;
+        if (ao_pixel(E.view, i, x, y)) {
+          pt_begin(E, q, x, y);
+          pix = y * width + x;
+          live = E.max_depth != 0u;
+          if (!live) pt_finish(E, q);  // a path of no rays resolves at once
+        }
+      } else {
+        pix = qin[i];
+        pt_load(W, pix, width, q);
+        q.shadow_phase = shadow_pass != 0u;
+        live = true;
+      }
+    }
+    bool cont = false;
+    if (live) {
+      RayCtx R;
+      pt_ray(q, R);
+      bool b;
+      traverse_ray<MODE, false, BuiltinAnyHit, WT>(P, R, E.view.tlas, stack_ptr, stack_stride, b);
+      bad |= b;
+      if (pt_advance(P, E, sample, q, R)) {
+        pt_finish(E, q);
+        core += q.core;
+        shadow += q.shadow;
+      } else {
+        pt_save(W, pix, q);
+        cont = true;
+      }
+    }
+    const uint32_t slot = warp_append(W.counters + pass, cont);
+    if (cont) qout[slot] = pix;
+  }
+  if (bad) atomicOr(P.error_word, 2u);
+  pt_count(E, core, shadow);
+}
+
+template <int MODE, bool LOCAL, bool WT, int TIER>
+cudaError_t launch_passes(const TraceParams& p, const PtEnv& e, const PtWave& w, int sm_count, uint32_t block,
+                          size_t smem, cudaStream_t st) {
+  static std::atomic<uint64_t> attr_done{0};
+  cudaError_t err = raise_smem_limit(attr_done, {(const void*)pt_pass_kernel<MODE, LOCAL, WT, TIER>});
+  if (err != cudaSuccess) return err;
+  int per_sm = 0;
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pt_pass_kernel<MODE, LOCAL, WT, TIER>, (int)block,
+                                                      smem);
+  if (err != cudaSuccess) return err;
+  if (per_sm < 1) per_sm = 1;
+  const uint32_t total = ao_dispatch_count(e.view.width, e.view.height);
+  uint32_t grid = (uint32_t)((sm_count > 0 ? sm_count : 1) * per_sm);
+  const uint32_t need = (total + block - 1) / block;
+  if (grid > need) grid = need;
+  err = cudaMemsetAsync(w.counters, 0, 2 * kPtMaxPasses * sizeof(uint32_t), st);
+  if (err != cudaSuccess) return err;
+  const bool lights = e.light_count != 0u;
+  const uint32_t passes = std::max<uint32_t>(1u, lights ? 2u * e.max_depth : e.max_depth);
+  for (uint32_t pass = 0; pass < passes; pass++) {
+    pt_pass_kernel<MODE, LOCAL, WT, TIER><<<grid, block, smem, st>>>(p, e, w, pass, lights ? (pass & 1u) : 0u);
+    err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+  }
+  return cudaSuccess;
+}
+
 template <int MODE, bool LOCAL, bool WT, int TIER>
 cudaError_t launch_refill(const TraceParams& p, const PtEnv& e, int sm_count, uint32_t block, size_t smem,
                           cudaStream_t st) {
@@ -247,10 +394,17 @@ cudaError_t launch_refill(const TraceParams& p, const PtEnv& e, int sm_count, ui
 }
 
 template <int MODE, bool LOCAL, bool WT>
-cudaError_t launch_variant_wt(const TraceParams& p, const PtEnv& e, int sm_count, cudaStream_t st) {
+cudaError_t launch_variant_wt(const TraceParams& p, const PtEnv& e, const PtWave* w, int sm_count, cudaStream_t st) {
   const uint32_t block = e.view.block ? e.view.block : 128;
   const uint32_t total = ao_dispatch_count(e.view.width, e.view.height);
   const size_t smem = MODE != MODE_THREADED && !LOCAL ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
+  if (e.schedule == 2u) {
+    if constexpr (LOCAL) {
+      if (e.register_tier == 1) return launch_passes<MODE, LOCAL, WT, 1>(p, e, *w, sm_count, block, smem, st);
+      if (e.register_tier == 2) return launch_passes<MODE, LOCAL, WT, 2>(p, e, *w, sm_count, block, smem, st);
+    }
+    return launch_passes<MODE, LOCAL, WT, 0>(p, e, *w, sm_count, block, smem, st);
+  }
   if (!e.schedule) {
     static std::atomic<uint64_t> attr_done{0};
     const cudaError_t err = raise_smem_limit(attr_done, {(const void*)pt_kernel<MODE, LOCAL, WT>});
@@ -267,22 +421,44 @@ cudaError_t launch_variant_wt(const TraceParams& p, const PtEnv& e, int sm_count
 }
 
 template <int MODE, bool LOCAL>
-cudaError_t launch_variant(const TraceParams& p, const PtEnv& e, int sm_count, cudaStream_t st) {
-  return p.watertight ? launch_variant_wt<MODE, LOCAL, true>(p, e, sm_count, st)
-                      : launch_variant_wt<MODE, LOCAL, false>(p, e, sm_count, st);
+cudaError_t launch_variant(const TraceParams& p, const PtEnv& e, const PtWave* w, int sm_count, cudaStream_t st) {
+  return p.watertight ? launch_variant_wt<MODE, LOCAL, true>(p, e, w, sm_count, st)
+                      : launch_variant_wt<MODE, LOCAL, false>(p, e, w, sm_count, st);
 }
+
+constexpr size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 }  // namespace
 
-cudaError_t launch_pt(const TraceParams& p, const PtEnv& e, int mode, int sm_count, cudaStream_t st) {
+size_t pt_scratch_bytes(uint32_t width, uint32_t height) {
+  const size_t n = (size_t)width * height;
+  return align256(n * kPtStateWords * 4) + 2 * align256(n * 4) + align256(2 * kPtMaxPasses * 4);
+}
+
+PtWave pt_wave_layout(void* scratch, uint32_t width, uint32_t height) {
+  const size_t n = (size_t)width * height;
+  char* b = static_cast<char*>(scratch);
+  PtWave w;
+  w.n_pix = (uint32_t)n;
+  w.state = reinterpret_cast<uint32_t*>(b);
+  b += align256(n * kPtStateWords * 4);
+  w.queue[0] = reinterpret_cast<uint32_t*>(b);
+  b += align256(n * 4);
+  w.queue[1] = reinterpret_cast<uint32_t*>(b);
+  b += align256(n * 4);
+  w.counters = reinterpret_cast<uint32_t*>(b);
+  return w;
+}
+
+cudaError_t launch_pt(const TraceParams& p, const PtEnv& e, const PtWave* w, int mode, int sm_count, cudaStream_t st) {
   if (e.view.width == 0 || e.view.height == 0) return cudaSuccess;
   if (mode == MODE_WIDE4)
-    return p.local_stack ? launch_variant<MODE_WIDE4, true>(p, e, sm_count, st)
-                         : launch_variant<MODE_WIDE4, false>(p, e, sm_count, st);
+    return p.local_stack ? launch_variant<MODE_WIDE4, true>(p, e, w, sm_count, st)
+                         : launch_variant<MODE_WIDE4, false>(p, e, w, sm_count, st);
   if (mode == MODE_BINARY)
-    return p.local_stack ? launch_variant<MODE_BINARY, true>(p, e, sm_count, st)
-                         : launch_variant<MODE_BINARY, false>(p, e, sm_count, st);
-  return launch_variant<MODE_THREADED, false>(p, e, sm_count, st);
+    return p.local_stack ? launch_variant<MODE_BINARY, true>(p, e, w, sm_count, st)
+                         : launch_variant<MODE_BINARY, false>(p, e, w, sm_count, st);
+  return launch_variant<MODE_THREADED, false>(p, e, w, sm_count, st);
 }
 
 }  // namespace rdn

@@ -50,11 +50,26 @@ struct PtEnv {
   const uint32_t* sm_to_material;
   uint32_t sm_count;
   float4* radiance;  // nullable: per pixel (HDR radiance of this sample, core rays traced)
-  uint32_t schedule;  // 0 one thread per pixel; 1 persistent warps refilled with pixels as paths end
+  uint32_t schedule;  // 0 one thread per pixel; 1 persistent warps refilled with pixels as paths end;
+                      // 2 wavefront passes over path queues (PtWave)
   uint32_t* fetch;    // refill schedule: the frame's pixel counter (zeroed before the launch)
   uint32_t register_tier;  // refill schedule, local-stack walks: 0 compiler's choice, 1 <= 96, 2 <= 64 registers
 };
 
-cudaError_t launch_pt(const TraceParams& p, const PtEnv& e, int mode, int sm_count, cudaStream_t st);
+// Wavefront schedule: path state of every pixel in HBM and queues of pixel
+// indices between passes (one pass per ray kind and depth).
+constexpr uint32_t kPtStateWords = 28;
+constexpr uint32_t kPtMaxPasses = 2 * 64;
+struct PtWave {
+  uint32_t* state;     // kPtStateWords x n_pix, word-major
+  uint32_t* queue[2];  // n_pix entries each: pass p reads queue[(p + 1) & 1], appends to queue[p & 1]
+  uint32_t* counters;  // [0, kPtMaxPasses): entries appended by pass p; then the passes' fetch counters
+  uint32_t n_pix;
+};
+size_t pt_scratch_bytes(uint32_t width, uint32_t height);
+// Carves the scratch (256-byte aligned, pt_scratch_bytes) into a PtWave.
+PtWave pt_wave_layout(void* scratch, uint32_t width, uint32_t height);
+
+cudaError_t launch_pt(const TraceParams& p, const PtEnv& e, const PtWave* w, int mode, int sm_count, cudaStream_t st);
 
 }  // namespace rdn

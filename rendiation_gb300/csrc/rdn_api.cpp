@@ -1592,6 +1592,12 @@ rdn_status rdn_ao_capture(rdn_ctx* c, rdn_task_graph* pipeline, const rdn_ao_des
       out);
 }
 
+rdn_status rdn_pt_scratch_size(uint32_t width, uint32_t height, size_t* bytes) {
+  if (!bytes || (uint64_t)width * height > 0x7FFFFFFFull) return RDN_ERR_INVALID_ARG;
+  *bytes = rdn::pt_scratch_bytes(width, height);
+  return RDN_OK;
+}
+
 static_assert(sizeof(rdn_pt_material) == sizeof(rdn::PtMaterial), "rdn_pt_material layout");
 static_assert(sizeof(rdn_pt_directional_light) == sizeof(rdn::PtLight), "rdn_pt_directional_light layout");
 
@@ -1612,7 +1618,13 @@ rdn_status rdn_path_tracing_render(rdn_ctx* c, const rdn_pt_desc* d, void* strea
     return fail(c, RDN_ERR_INVALID_ARG, "lights, materials, sm_to_material and normals must be 4-byte aligned");
   if (reinterpret_cast<uintptr_t>(d->radiance) & 15)
     return fail(c, RDN_ERR_INVALID_ARG, "radiance must be 16-byte aligned");
-  if (d->schedule > RDN_PT_SCHEDULE_REFILL) return fail(c, RDN_ERR_INVALID_ARG, "unknown schedule");
+  if (d->schedule > RDN_PT_SCHEDULE_WAVEFRONT) return fail(c, RDN_ERR_INVALID_ARG, "unknown schedule");
+  if (d->schedule == RDN_PT_SCHEDULE_WAVEFRONT) {
+    if (!d->scratch || (reinterpret_cast<uintptr_t>(d->scratch) & 255))
+      return fail(c, RDN_ERR_INVALID_ARG, "the wavefront schedule needs 256-byte aligned scratch");
+    if (d->scratch_bytes < rdn::pt_scratch_bytes(d->width, d->height))
+      return fail(c, RDN_ERR_INVALID_ARG, "scratch smaller than rdn_pt_scratch_size()");
+  }
   if (d->register_tier > 2) return fail(c, RDN_ERR_INVALID_ARG, "register_tier must be 0, 1 or 2");
   std::lock_guard<std::mutex> lk(c->lock);
   rdn_ao_desc ad;
@@ -1648,9 +1660,12 @@ rdn_status rdn_path_tracing_render(rdn_ctx* c, const rdn_pt_desc* d, void* strea
   e.schedule = d->schedule;
   e.register_tier = d->register_tier;
   e.fetch = c->d_counters + 13;
+  rdn::PtWave w;
+  std::memset(&w, 0, sizeof(w));
+  if (d->schedule == RDN_PT_SCHEDULE_WAVEFRONT) w = rdn::pt_wave_layout(d->scratch, d->width, d->height);
   cudaError_t err = cudaSetDevice(c->device);
   if (err == cudaSuccess)
-    err = rdn::launch_pt(p, e, mode_of(d->traversal), c->sm_count, static_cast<cudaStream_t>(stream));
+    err = rdn::launch_pt(p, e, &w, mode_of(d->traversal), c->sm_count, static_cast<cudaStream_t>(stream));
   if (err != cudaSuccess) return cuda_fail(c, err, "path tracing launch");
   return RDN_OK;
 }

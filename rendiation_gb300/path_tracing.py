@@ -29,7 +29,7 @@ from .raytracing import TRAVERSAL_ORDERED_WIDE, _check
 
 TONE_MAP_NONE, TONE_MAP_LINEAR, TONE_MAP_REINHARD, TONE_MAP_CINEON, TONE_MAP_ACES_FILMIC = 0, 1, 2, 3, 4
 BACKGROUND_SOLID, BACKGROUND_TEST = 0, 1
-SCHEDULE_PIXEL, SCHEDULE_REFILL = 0, 1
+SCHEDULE_PIXEL, SCHEDULE_REFILL, SCHEDULE_WAVEFRONT = 0, 1, 2
 MAX_RAY_DEPTH = 3  # path_tracing/mod.rs:80
 
 MATERIAL_DTYPE = np.dtype([("base_color", np.float32, 3), ("perceptual_roughness", np.float32),
@@ -127,6 +127,18 @@ class DeviceReferencePathTracingRenderer:
                          if keep_radiance else None)
         self.ray_counts = torch.zeros(2, dtype=torch.int32, device="cuda") if count_rays else None
         self.sample_count = 0
+        self._scratch = None
+
+    def _scratch_ptr(self):
+        """Path state and queues of the wavefront schedule (allocated on first use)."""
+        if self._scratch is None:
+            import torch
+
+            size = C.c_size_t()
+            _check(self.system._h, self.system._L.rdn_pt_scratch_size(self.width, self.height, C.byref(size)))
+            self._scratch = torch.empty(size.value + 256, dtype=torch.uint8, device="cuda")
+            self._scratch_bytes = size.value
+        return (self._scratch.data_ptr() + 255) & ~255, self._scratch_bytes
 
     def desc(self) -> native.PtDesc:
         d = native.PtDesc()
@@ -149,6 +161,8 @@ class DeviceReferencePathTracingRenderer:
         d.ray_counts = self.ray_counts.data_ptr() if self.ray_counts is not None else None
         d.schedule = self.schedule
         d.register_tier = self.register_tier
+        if self.schedule == SCHEDULE_WAVEFRONT:
+            d.scratch, d.scratch_bytes = self._scratch_ptr()
         return d
 
     def render(self, stream=None):

@@ -168,17 +168,28 @@ def test_ordered_walks_match_except_ties(cuda, traversal):
 
 @pytest.mark.parametrize("name", ["field", "instanced"])
 def test_schedules_change_no_pixel(cuda, name):
-    """One thread per pixel and persistent warps refilled with pixels as paths
-    end compute every pixel with the same operations."""
+    """One thread per pixel, persistent warps refilled with pixels as paths
+    end, and wavefront passes over path queues compute every pixel with the
+    same operations, at every register budget."""
     a = run_pair(SCENES[name], traversal=rt.TRAVERSAL_ORDERED_WIDE, lights=LIGHTS, materials=MATERIALS,
                  schedule=pt.SCHEDULE_PIXEL)
-    b = run_pair(SCENES[name], traversal=rt.TRAVERSAL_ORDERED_WIDE, lights=LIGHTS, materials=MATERIALS,
-                 schedule=pt.SCHEDULE_REFILL)
-    assert np.array_equal(a[2], b[2]) and same_bits(a[3], b[3]).all() and a[5] == b[5]
-    for tier in (1, 2):  # register budgets of the refill kernel
-        c = run_pair(SCENES[name], traversal=rt.TRAVERSAL_ORDERED_WIDE, lights=LIGHTS, materials=MATERIALS,
-                     schedule=pt.SCHEDULE_REFILL, register_tier=tier)
-        assert np.array_equal(a[2], c[2]) and same_bits(a[3], c[3]).all() and a[5] == c[5]
+    for sched in (pt.SCHEDULE_REFILL, pt.SCHEDULE_WAVEFRONT):
+        for tier in (0, 1, 2):
+            c = run_pair(SCENES[name], traversal=rt.TRAVERSAL_ORDERED_WIDE, lights=LIGHTS, materials=MATERIALS,
+                         schedule=sched, register_tier=tier)
+            assert np.array_equal(a[2], c[2]) and same_bits(a[3], c[3]).all() and a[5] == c[5], (sched, tier)
+
+
+@pytest.mark.parametrize("lights", [None, LIGHTS[:1]])
+@pytest.mark.parametrize("depth", [0, 1, 5])
+def test_wavefront_schedule_matches_the_oracle(cuda, lights, depth):
+    """The wavefront passes in the reference order: without lights every pass
+    traces core rays, with lights the passes alternate core and shadow rays."""
+    want_img, want_rad, img, rad, rays_o, rays_g = run_pair(
+        instanced, max_depth=depth, lights=lights, materials=MATERIALS, bg=(0.3, 0.3, 0.3),
+        schedule=pt.SCHEDULE_WAVEFRONT)
+    assert np.array_equal(img, want_img) and same_bits(rad, want_rad).all()
+    assert rays_g == rays_o
 
 
 @pytest.mark.parametrize("block_size", [32, 64])
@@ -194,7 +205,7 @@ def test_invalid_descriptors_are_rejected(cuda):
 
     scene, _, vp, eye = field()
     P = scene.build_product()
-    bad = [dict(tone_map=5), dict(background=2), dict(max_path_depth=65), dict(schedule=2), dict(register_tier=3)]
+    bad = [dict(tone_map=5), dict(background=2), dict(max_path_depth=65), dict(schedule=3), dict(register_tier=3)]
     for kw in bad:
         R = pt.DeviceReferencePathTracingRenderer(P, W, H, vp, eye, **kw)
         with pytest.raises(native.RdnError):
@@ -208,6 +219,13 @@ def test_invalid_descriptors_are_rejected(cuda):
     assert P._L.rdn_path_tracing_render(P._h, ctypes.byref(d), None) == -1  # RDN_ERR_INVALID_ARG
     d = R.desc()
     d.image = None
+    assert P._L.rdn_path_tracing_render(P._h, ctypes.byref(d), None) == -1  # RDN_ERR_INVALID_ARG
+    R.schedule = pt.SCHEDULE_WAVEFRONT
+    d = R.desc()
+    d.scratch_bytes -= 256  # too small
+    assert P._L.rdn_path_tracing_render(P._h, ctypes.byref(d), None) == -1  # RDN_ERR_INVALID_ARG
+    d = R.desc()
+    d.scratch += 16  # not 256-byte aligned
     assert P._L.rdn_path_tracing_render(P._h, ctypes.byref(d), None) == -1  # RDN_ERR_INVALID_ARG
     torch.cuda.synchronize()
     assert int(R.image.sum().item()) == 0  # nothing was written
