@@ -1542,6 +1542,8 @@ def bench_batched_adjoint(args, ws=1, rank=0):
     L.rdn_graph_destroy(gr)
     L.rdn_graph_destroy(gf)
     del tape_tri, tape_inst, tape_rays
+    # device memory of the timed forms (before the counting below allocates its own buffers)
+    peak_timed = int(torch.cuda.max_memory_allocated() + as_bytes)
     # segments traced per step (one forward pass records the segment triangles)
     seg_tri = torch.zeros(n * seg, dtype=torch.int32, device="cuda")
     seg_rays = torch.zeros((n * seg, 8), device="cuda")
@@ -1570,7 +1572,7 @@ def bench_batched_adjoint(args, ws=1, rank=0):
     out["fwd_adjoint_retrace_over_fwd"] = round(out["forward_adjoint_retrace_ms"] / out["forward_ms"], 3)
     out["adjoint"] = ("from the forward's record of every segment (triangle, instance, ray; 40 B per segment), "
                       "one graph for forward + adjoint; _retrace: the adjoint traces the paths again")
-    out["peak_hbm_bytes"] = int(torch.cuda.max_memory_allocated() + as_bytes)
+    out["peak_hbm_bytes"] = peak_timed
     # the configuration asks for hits recomputed in the backward pass, not stored per bounce
     out["roofline"] = {
         "forward": algorithmic_roofline(traced * b_seg, out["forward_ms"],
