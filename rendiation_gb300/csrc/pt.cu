@@ -137,6 +137,35 @@ __device__ __forceinline__ void pt_finish(const PtEnv& E, const PtPath& q) {
   if (E.radiance) E.radiance[pixel] = make_float4(q.radiance.x, q.radiance.y, q.radiance.z, (float)q.core);
 }
 
+// A path's state parked in shared memory while its ray is traced, so that
+// the traversal's registers are not held alongside it (word k of thread t at
+// [k][t], conflict-free; blocks of at most 128 threads). A static array: with
+// the park area in dynamic shared memory, indexed by blockDim.x, the compiler
+// kept more registers and the 1080p sample took 3.38 ms instead of 3.05 ms.
+constexpr uint32_t kPtStash = 26;
+__device__ __forceinline__ void pt_park(float (*stash)[128], const PtPath& q) {
+  const uint32_t t = threadIdx.x;
+  const float v[kPtStash] = {q.o.x, q.o.y, q.o.z, q.d.x, q.d.y, q.d.z, q.throughput.x, q.throughput.y,
+                             q.throughput.z, q.radiance.x, q.radiance.y, q.radiance.z, q.sn.x, q.sn.y, q.sn.z,
+                             q.origin.x, q.origin.y, q.origin.z, q.ldir.x, q.ldir.y, q.ldir.z, q.lrad.x, q.lrad.y,
+                             q.lrad.z, __uint_as_float(q.sm_id), __uint_as_float(q.depth)};
+#pragma unroll
+  for (uint32_t k = 0; k < kPtStash; k++) stash[k][t] = v[k];
+}
+__device__ __forceinline__ void pt_unpark(float (*stash)[128], PtPath& q) {
+  const uint32_t t = threadIdx.x;
+  q.o = make_float3(stash[0][t], stash[1][t], stash[2][t]);
+  q.d = make_float3(stash[3][t], stash[4][t], stash[5][t]);
+  q.throughput = make_float3(stash[6][t], stash[7][t], stash[8][t]);
+  q.radiance = make_float3(stash[9][t], stash[10][t], stash[11][t]);
+  q.sn = make_float3(stash[12][t], stash[13][t], stash[14][t]);
+  q.origin = make_float3(stash[15][t], stash[16][t], stash[17][t]);
+  q.ldir = make_float3(stash[18][t], stash[19][t], stash[20][t]);
+  q.lrad = make_float3(stash[21][t], stash[22][t], stash[23][t]);
+  q.sm_id = __float_as_uint(stash[24][t]);
+  q.depth = __float_as_uint(stash[25][t]);
+}
+
 __device__ __forceinline__ void pt_count(const PtEnv& E, uint32_t core, uint32_t shadow) {
   if (!E.view.ray_counts) return;
   const uint32_t c = __reduce_add_sync(0xffffffffu, core), s = __reduce_add_sync(0xffffffffu, shadow);
@@ -149,6 +178,7 @@ __device__ __forceinline__ void pt_count(const PtEnv& E, uint32_t core, uint32_t
 template <int MODE, bool LOCAL, bool WT>
 __global__ void __launch_bounds__(128) pt_kernel(TraceParams P, PtEnv E) {
   RDN_TRAVERSAL_STACK(LOCAL);
+  __shared__ float stash[kPtStash][128];
   uint32_t x, y;
   const bool valid = ao_pixel(E.view, blockIdx.x * blockDim.x + threadIdx.x, x, y);
   uint32_t core = 0, shadow = 0;
@@ -160,9 +190,11 @@ __global__ void __launch_bounds__(128) pt_kernel(TraceParams P, PtEnv E) {
     while (!done) {
       RayCtx R;
       pt_ray(q, R);
+      pt_park(stash, q);
       bool b;
       traverse_ray<MODE, false, BuiltinAnyHit, WT>(P, R, E.view.tlas, stack_ptr, stack_stride, b);
       bad |= b;
+      pt_unpark(stash, q);
       done = pt_advance(P, E, sample, q, R);
     }
     if (bad) atomicOr(P.error_word, 2u);
@@ -181,6 +213,7 @@ constexpr int pt_min_blocks(int tier) { return tier == 1 ? 5 : (tier == 2 ? 8 : 
 template <int MODE, bool LOCAL, bool WT, int TIER>
 __global__ void __launch_bounds__(128, pt_min_blocks(TIER)) pt_refill_kernel(TraceParams P, PtEnv E, uint32_t total) {
   RDN_TRAVERSAL_STACK(LOCAL);
+  __shared__ float stash[kPtStash][128];
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t sample = ao_sample(E.view);
   PtPath q;
@@ -214,9 +247,11 @@ __global__ void __launch_bounds__(128, pt_min_blocks(TIER)) pt_refill_kernel(Tra
     if (active) {
       RayCtx R;
       pt_ray(q, R);
+      pt_park(stash, q);
       bool b;
       traverse_ray<MODE, false, BuiltinAnyHit, WT>(P, R, E.view.tlas, stack_ptr, stack_stride, b);
       bad |= b;
+      pt_unpark(stash, q);
       if (pt_advance(P, E, sample, q, R)) {
         pt_finish(E, q);
         core += q.core;
@@ -288,6 +323,7 @@ template <int MODE, bool LOCAL, bool WT, int TIER>
 __global__ void __launch_bounds__(128, pt_min_blocks(TIER))
     pt_pass_kernel(TraceParams P, PtEnv E, PtWave W, uint32_t pass, uint32_t shadow_pass) {
   RDN_TRAVERSAL_STACK(LOCAL);
+  __shared__ float stash[kPtStash][128];
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t sample = ao_sample(E.view);
   const uint32_t width = E.view.width;
@@ -326,9 +362,11 @@ __global__ void __launch_bounds__(128, pt_min_blocks(TIER))
     if (live) {
       RayCtx R;
       pt_ray(q, R);
+      pt_park(stash, q);
       bool b;
       traverse_ray<MODE, false, BuiltinAnyHit, WT>(P, R, E.view.tlas, stack_ptr, stack_stride, b);
       bad |= b;
+      pt_unpark(stash, q);
       if (pt_advance(P, E, sample, q, R)) {
         pt_finish(E, q);
         core += q.core;
