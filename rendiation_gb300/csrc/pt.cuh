@@ -129,7 +129,8 @@ __device__ __forceinline__ float pow5(float x) {
   return (x2 * x2) * x;
 }
 
-// tbn(normal) * v (Frisvad's basis, the reference's revised form)
+// tbn(normal) * v: the orthonormal basis of Duff et al. 2017 ("Building an
+// Orthonormal Basis, Revisited"), as shader/library/src/sampling.rs:70-83 builds it
 __device__ __forceinline__ float3 tbn_mul(float3 n, float3 v) {
   const float sign = n.z < 0.0f ? -1.0f : 1.0f;
   const float a = -1.0f / (sign + n.z);
