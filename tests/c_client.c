@@ -2,18 +2,24 @@
  * plus the CUDA runtime for device buffers), the way a Rust, Go or C++ host
  * binds it: one triangle geometry, one identity instance, a build, one batch
  * trace and, when a frame file is given, one frame of the path tracer's first
- * bounce (rdn_wavefront_shadow_bounce), results written to a file.
+ * bounce (rdn_wavefront_shadow_bounce), and when a second file is given, one
+ * sample of the reference path tracer (rdn_path_tracing_render), results
+ * written to a file.
  *
- *   c_client <input> <output> <traversal> <device_build> [<frame>]
+ *   c_client <input> <output> <traversal> <device_build> [<frame> [<path-traced frame>]]
  *
  * input:  u32 vertex_count, u32 index_count (0 = non-indexed), u32 ray_count,
  *         f32 positions[3 * vertex_count], u32 indices[index_count],
  *         f32 rays[8 * ray_count] (org, tmin, dir, tmax)
  * frame:  u32 width, u32 height, u32 sample_index, f32 camera[14] (origin,
  *         forward, right, up, tan_half, aspect), f32 light[3]
+ * path-traced frame: u32 width, u32 height, u32 sample_count, u32 max_path_depth,
+ *         f32 view_projection_inv[16], f32 camera_position[3], f32 light[6]
+ *         (illuminance, direction)
  * output: rdn_hit[ray_count], rdn_hit_ext[ray_count], u32 error_flags, and with
  *         a frame: rdn_pixel_result[width * height], u32 rays[3] (primary,
- *         shadow, bounce), u32 error_flags
+ *         shadow, bounce), u32 error_flags; with a path-traced frame: u8
+ *         rgba[4 * width * height], u32 rays[2] (core, shadow), u32 error_flags
  *
  * Exit codes: 0 ok, 1 usage or file error, 2 an rdn_* call failed (its status
  * and rdn_last_error are printed), 3 a CUDA runtime call failed. */
@@ -47,7 +53,8 @@ static int read_all(FILE* f, void* dst, size_t bytes) { return bytes == 0 || fre
 
 int main(int argc, char** argv) {
   if (argc != 5 && argc != 6) {
-    fprintf(stderr, "usage: %s <input> <output> <traversal> <device_build> [<frame>]\n", argv[0]);
+    fprintf(stderr, "usage: %s <input> <output> <traversal> <device_build> [<frame> [<path-traced frame>]]\n",
+            argv[0]);
     return 1;
   }
   const uint32_t traversal = (uint32_t)atoi(argv[3]);
@@ -124,7 +131,7 @@ int main(int argc, char** argv) {
   fwrite(ext, sizeof(rdn_hit_ext), nr, out);
   fwrite(&flags, 4, 1, out);
 
-  if (argc == 6) {
+  if (argc >= 6) {
     /* one frame of the path tracer's first bounce: caller-owned scratch sized by the library */
     FILE* fr = fopen(argv[5], "rb");
     if (!fr) return 1;
@@ -174,6 +181,66 @@ int main(int argc, char** argv) {
     cudaFree(d_scratch);
     cudaFree(d_out);
     cudaFree(d_counts);
+  }
+  if (argc >= 7) {
+    /* one sample of the reference path tracer (rdn_path_tracing_render): the
+     * wavefront schedule with caller-owned scratch, one directional light,
+     * the default material; the RGBA8 image and the ray counts are written out */
+    FILE* fp = fopen(argv[6], "rb");
+    if (!fp) return 1;
+    uint32_t ph[4];  /* width, height, sample_count, max_path_depth */
+    float pv[16 + 3 + 6];  /* view_projection_inv, camera position, light illuminance + direction */
+    if (!read_all(fp, ph, sizeof ph) || !read_all(fp, pv, sizeof pv)) return 1;
+    fclose(fp);
+    const size_t npix = (size_t)ph[0] * ph[1];
+    size_t scratch_bytes = 0;
+    CHECK(rdn_pt_scratch_size(ph[0], ph[1], &scratch_bytes));
+    void* d_scratch = NULL;
+    uint8_t* d_image = NULL;
+    uint32_t* d_counts = NULL;
+    rdn_pt_directional_light* d_light = NULL;
+    CUCHECK(cudaMalloc(&d_scratch, scratch_bytes));
+    CUCHECK(cudaMalloc((void**)&d_image, 4 * npix));
+    CUCHECK(cudaMemset(d_image, 0, 4 * npix));
+    CUCHECK(cudaMalloc((void**)&d_counts, 8));
+    CUCHECK(cudaMemset(d_counts, 0, 8));
+    CUCHECK(cudaMalloc((void**)&d_light, sizeof(rdn_pt_directional_light)));
+    CUCHECK(cudaMemcpy(d_light, pv + 19, sizeof(rdn_pt_directional_light), cudaMemcpyHostToDevice));
+    rdn_pt_desc pd;
+    memset(&pd, 0, sizeof pd);
+    memcpy(pd.view_projection_inv, pv, 64);
+    memcpy(pd.camera_position, pv + 16, 12);
+    pd.width = ph[0];
+    pd.height = ph[1];
+    pd.sample_count = ph[2];
+    pd.max_path_depth = ph[3];
+    pd.traversal = traversal;
+    pd.tone_map = RDN_TONE_MAP_ACES_FILMIC;
+    pd.exposure = 1.0f;
+    pd.background = RDN_PT_BACKGROUND_SOLID;
+    pd.lights = d_light;
+    pd.light_count = 1;
+    pd.image = d_image;
+    pd.ray_counts = d_counts;
+    pd.schedule = RDN_PT_SCHEDULE_WAVEFRONT;
+    pd.scratch = d_scratch;
+    pd.scratch_bytes = scratch_bytes;
+    CHECK(rdn_path_tracing_render(ctx, &pd, NULL));
+    uint32_t pflags = 0;
+    CHECK(rdn_check_errors(ctx, NULL, &pflags));
+    uint8_t* img = (uint8_t*)malloc(4 * npix + 16);
+    uint32_t pcounts[2];
+    if (!img) return 1;
+    CUCHECK(cudaMemcpy(img, d_image, 4 * npix, cudaMemcpyDeviceToHost));
+    CUCHECK(cudaMemcpy(pcounts, d_counts, sizeof pcounts, cudaMemcpyDeviceToHost));
+    fwrite(img, 4, npix, out);
+    fwrite(pcounts, 4, 2, out);
+    fwrite(&pflags, 4, 1, out);
+    free(img);
+    cudaFree(d_scratch);
+    cudaFree(d_image);
+    cudaFree(d_counts);
+    cudaFree(d_light);
   }
   fclose(out);
 

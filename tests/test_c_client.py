@@ -129,3 +129,47 @@ def test_client_renders_a_wavefront_frame_like_the_oracle(tmp_path, traversal, c
         from oracle import parity
 
         assert parity.classify_wavefront(S, cam, cam.width, cam.height, light, got, exp, 9, threads=8)["other"] == 0
+
+
+@pytest.mark.gpu
+def test_client_path_traces_like_the_oracle(tmp_path, cuda):
+    """rdn_path_tracing_render through the C ABI alone (the wavefront schedule
+    with caller scratch, one directional light, the default material): the
+    reference order's RGBA8 image equals the oracle's byte for byte."""
+    from rendiation_gb300 import path_tracing as pt
+    from rendiation_gb300 import task_graph as tg
+
+    exe = compile_client(tmp_path)
+    mesh = scenes.heightfield(64, seed=2)
+    rays = scenes.pinhole_rays(scenes.heightfield_camera(16, 8))
+    write_input(tmp_path / "in.bin", mesh, rays)
+    cam = scenes.heightfield_camera(24, 16)
+    light = (0.2, 0.2, 2.0)
+    with open(tmp_path / "frame.bin", "wb") as f:
+        f.write(struct.pack("<III", cam.width, cam.height, 1))
+        f.write(np.asarray(cam.as_floats(), np.float32).tobytes())
+        f.write(np.asarray(light, np.float32).tobytes())
+    W, H = 40, 28
+    eye = (0.5, -0.45, 0.75)
+    vp = tg.look_at_view_projection_inv(eye, (0.5, 0.5, 0.0), (0, 0, 1), 45.0, W / H)
+    sun = pt.directional_light((3.0, 2.5, 2.0), (0.3, 0.2, -1.0))
+    with open(tmp_path / "pt.bin", "wb") as f:
+        f.write(struct.pack("<IIII", W, H, 2, 3))
+        f.write(np.asarray(vp, np.float32).tobytes())
+        f.write(np.asarray(eye, np.float32).tobytes())
+        f.write(np.asarray(sun["illuminance"], np.float32).tobytes())
+        f.write(np.asarray(sun["direction"], np.float32).tobytes())
+    r = subprocess.run([exe, str(tmp_path / "in.bin"), str(tmp_path / "out.bin"), str(rt.TRAVERSAL_REFERENCE), "1",
+                        str(tmp_path / "frame.bin"), str(tmp_path / "pt.bin")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    raw = open(tmp_path / "out.bin", "rb").read()
+    off = 32 * rays.shape[0] + 4 + 32 * cam.width * cam.height + 16
+    img = np.frombuffer(raw[off:off + 4 * W * H], np.uint32)
+    counts = np.frombuffer(raw[off + 4 * W * H:off + 4 * W * H + 8], np.uint32)
+    flags = struct.unpack("<I", raw[off + 4 * W * H + 8:off + 4 * W * H + 12])[0]
+    assert flags == 0
+    S = single_mesh_scene(mesh).build_oracle()
+    want = np.zeros(W * H, np.uint32)
+    n, _ = orc.pt_render(S, vp, eye, W, H, want, lights=[sun], sample_count=2, threads=8)
+    assert np.array_equal(img, want)
+    assert tuple(int(c) for c in counts) == n
