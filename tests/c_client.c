@@ -52,7 +52,7 @@ static rdn_ctx* ctx = NULL;
 static int read_all(FILE* f, void* dst, size_t bytes) { return bytes == 0 || fread(dst, 1, bytes, f) == bytes; }
 
 int main(int argc, char** argv) {
-  if (argc != 5 && argc != 6) {
+  if (argc < 5 || argc > 7) {
     fprintf(stderr, "usage: %s <input> <output> <traversal> <device_build> [<frame> [<path-traced frame>]]\n",
             argv[0]);
     return 1;
