@@ -785,6 +785,10 @@ rdn_status rdn_ao_capture(rdn_ctx* ctx, rdn_task_graph* pipeline, const rdn_ao_d
 #define RDN_TONE_MAP_ACES_FILMIC 4u  /* the reference's default (ToneMap::new, exposure 1) */
 #define RDN_PT_BACKGROUND_SOLID 0u   /* PTRayMissCtx::Solid: background_color */
 #define RDN_PT_BACKGROUND_TEST 1u    /* PTRayMissCtx::Test: 0.7 for direction.y > 0, else 0.3 */
+#define RDN_PT_BACKGROUND_ENV_CUBE 2u /* PTRayMissCtx::EnvCube: env_cube sampled along env_transform applied to
+                                        the direction (M (d, 1) / w), times env_intensity: the major axis's face
+                                        (ties x, y, z), bilinear over texel centres clamped to the face, level 0
+                                        (f32 weights, no filtering across faces) */
 #define RDN_PT_MAX_PATH_DEPTH 3u     /* the reference's MAX_RAY_DEPTH (path_tracing/mod.rs:80) */
 #define RDN_PT_SCHEDULE_PIXEL 0u     /* one thread per pixel, warps over 8x4 tiles */
 #define RDN_PT_SCHEDULE_REFILL 1u    /* persistent warps; a lane whose path ends takes the next pixel (the
@@ -848,6 +852,11 @@ typedef struct rdn_pt_desc {
                                      2 = at most 64 (no pixel changes) */
   void* scratch;                  /* device, 256-byte aligned, >= rdn_pt_scratch_size(): wavefront schedule */
   size_t scratch_bytes;
+  const float* env_cube;          /* device, 16-byte aligned: RDN_PT_BACKGROUND_ENV_CUBE's six faces (+X, -X,
+                                     +Y, -Y, +Z, -Z), each env_size rows (t) of env_size RGBA f32 texels (s) */
+  uint32_t env_size;
+  float env_transform[16];        /* IblShaderInfoForBackground.transform, Mat4 in the reference's memory order */
+  float env_intensity;            /* IblShaderInfoForBackground.intensity */
 } rdn_pt_desc;
 
 /* Scratch of the wavefront schedule for a width x height frame: 112 B of path

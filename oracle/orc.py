@@ -41,14 +41,23 @@ class _PtScene(C.Structure):
     _fields_ = [("max_depth", C.c_uint32), ("tone_map", C.c_uint32), ("background", C.c_uint32),
                 ("exposure", C.c_float), ("bg", C.c_float * 3), ("lights", C.c_void_p), ("light_count", C.c_uint32),
                 ("materials", C.c_void_p), ("material_count", C.c_uint32), ("sm_to_material", C.c_void_p),
-                ("sm_count", C.c_uint32)]
+                ("sm_count", C.c_uint32), ("env", C.c_void_p), ("env_size", C.c_uint32),
+                ("env_transform", C.c_float * 16), ("env_intensity", C.c_float)]
 
 
-def _pt_scene(lights, materials, sm_to_material, max_depth, tone_map, exposure, background, bg):
+def _pt_scene(lights, materials, sm_to_material, max_depth, tone_map, exposure, background, bg, env_cube=None,
+              env_transform=None, env_intensity=1.0):
     sc = _PtScene()
     sc.max_depth, sc.tone_map, sc.background, sc.exposure = max_depth, tone_map, background, exposure
     sc.bg[:] = [float(b) for b in bg]
     keep = []
+    if env_cube is not None:
+        cube = np.ascontiguousarray(env_cube, np.float32)
+        keep.append(cube)
+        sc.env, sc.env_size = cube.ctypes.data, cube.shape[1]
+    m = np.asarray(env_transform if env_transform is not None else np.eye(4), np.float32)
+    sc.env_transform[:] = [float(v) for v in m.T.reshape(-1)]  # columns, the reference's memory order
+    sc.env_intensity = env_intensity
     if lights is not None and len(lights):
         la = np.ascontiguousarray(lights, PT_LIGHT_DTYPE)
         keep.append(la)
@@ -374,7 +383,7 @@ def select_nth(keys: np.ndarray, index: int) -> np.ndarray:
 def pt_render(system: OracleSystem, vp_inv, cam, width, height, image: np.ndarray, lights=None, materials=None,
               sm_to_material=None, max_depth=3, tone_map=4, exposure=1.0, background=0, bg=(0.0, 0.0, 0.0),
               sample_count=0, tlas=0, normals=None, rows=None, radiance: np.ndarray | None = None, intersector=0,
-              threads=4):
+              threads=4, env_cube=None, env_transform=None, env_intensity=1.0):
     """One path-tracing sample into image (uint32 RGBA8 texels, width*height,
     updated in place) for rows [r0, r1); radiance (float32 width*height*4,
     optional) receives the sample's HDR radiance and core-ray count per pixel.
@@ -385,7 +394,8 @@ def pt_render(system: OracleSystem, vp_inv, cam, width, height, image: np.ndarra
     if radiance is not None:
         assert radiance.dtype == np.float32 and radiance.size == 4 * width * height and radiance.flags.c_contiguous
     nrm = None if normals is None else np.ascontiguousarray(normals, np.float32)
-    sc, keep = _pt_scene(lights, materials, sm_to_material, max_depth, tone_map, exposure, background, bg)
+    sc, keep = _pt_scene(lights, materials, sm_to_material, max_depth, tone_map, exposure, background, bg,
+                         env_cube, env_transform, env_intensity)
     r0, r1 = rows if rows is not None else (0, height)
     rays = np.zeros(2, np.uint64)
     sec = C.c_double()

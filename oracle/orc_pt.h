@@ -7,7 +7,8 @@
 //                                                        ray_gen.rs:95-102, camera.rs:66-100
 //   core ray: CULL_BACK_FACING_TRIANGLES over [f32::EPSILON, f32::MAX], TLAS 0
 //                                                        ray_gen.rs:141-159, api/ty.rs:49-56
-//   miss: solid colour or the test gradient              ray_miss.rs:10-28,136-152
+//   miss: solid colour, the test gradient or the environment cube
+//                                                        ray_miss.rs:10-28,136-152
 //   closest hit: world position o + d t, shading / geometric normal
 //     (get_world_normal_impl), light sample with PCGRandomSampler(xxhash32(x, y,
 //     2 sample_count)), shadow ray ACCEPT_FIRST_HIT_AND_END_SEARCH over
@@ -47,6 +48,7 @@
 // exp2(2.2 log2 x) from frexp, the atanh series and the Taylor series of
 // e^(f ln 2); the unorm8 store rounds to nearest even.
 #pragma once
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 
@@ -84,6 +86,10 @@ struct PtScene {
   uint32_t material_count;
   const uint32_t* sm_to_material;
   uint32_t sm_count;
+  const float* env;  // 6 faces (+X -X +Y -Y +Z -Z) x env_size rows x env_size RGBA texels
+  uint32_t env_size;
+  float env_transform[16];
+  float env_intensity;
 };
 
 static inline float pt_mix(float lo, float hi, float t) { return lo * (1.0f - t) + hi * t; }
@@ -276,8 +282,61 @@ static inline V3 pt_sample(const PtSurface& s, V3 v, V3 n, uint32_t& state, V3* 
   return l;
 }
 
+// PTRayMissCtx::EnvCube (ray_miss.rs:139-147): transform_dir (M (d, 1) / w,
+// shader/library/src/lib.rs:13-16), the major axis's face (ties x, y, z) with
+// the standard face coordinates, bilinear over texel centres clamped to the
+// face's edge, f32 weights; black for a non-finite or zero direction.
+static inline V3 env_texel(const PtScene& S, uint32_t f, int i, int j) {
+  const float* t = S.env + 4 * (((size_t)f * S.env_size + (uint32_t)j) * S.env_size + (uint32_t)i);
+  return v3(t[0], t[1], t[2]);
+}
+static inline V3 lerp3(V3 a, V3 b, float f) {
+  return v3(a.x * (1.0f - f) + b.x * f, a.y * (1.0f - f) + b.y * f, a.z * (1.0f - f) + b.z * f);
+}
+static inline V3 pt_env(const PtScene& S, V3 d) {
+  const float* m = S.env_transform;
+  const float rx = d.x * m[0] + d.y * m[4] + d.z * m[8] + 1.0f * m[12];
+  const float ry = d.x * m[1] + d.y * m[5] + d.z * m[9] + 1.0f * m[13];
+  const float rz = d.x * m[2] + d.y * m[6] + d.z * m[10] + 1.0f * m[14];
+  const float rw = d.x * m[3] + d.y * m[7] + d.z * m[11] + 1.0f * m[15];
+  const float x = rx / rw, y = ry / rw, z = rz / rw;
+  const float ax = std::fabs(x), ay = std::fabs(y), az = std::fabs(z);
+  if (!(ax <= 3.0e38f && ay <= 3.0e38f && az <= 3.0e38f) || (ax == 0.0f && ay == 0.0f && az == 0.0f))
+    return v3(0.0f, 0.0f, 0.0f);
+  uint32_t face;
+  float sc, tc, ma;
+  if (ax >= ay && ax >= az) {
+    face = x >= 0.0f ? 0u : 1u;
+    sc = x >= 0.0f ? -z : z;
+    tc = -y;
+    ma = ax;
+  } else if (ay >= az) {
+    face = y >= 0.0f ? 2u : 3u;
+    sc = x;
+    tc = y >= 0.0f ? z : -z;
+    ma = ay;
+  } else {
+    face = z >= 0.0f ? 4u : 5u;
+    sc = z >= 0.0f ? x : -x;
+    tc = -y;
+    ma = az;
+  }
+  const float n = (float)S.env_size;
+  const float u = ((sc / ma + 1.0f) * 0.5f) * n - 0.5f;
+  const float v = ((tc / ma + 1.0f) * 0.5f) * n - 0.5f;
+  const float u0 = std::floor(u), v0 = std::floor(v);
+  const float fu = u - u0, fv = v - v0;
+  const int last = (int)S.env_size - 1;
+  const int i0 = std::min(std::max((int)u0, 0), last), i1 = std::min(std::max((int)u0 + 1, 0), last);
+  const int j0 = std::min(std::max((int)v0, 0), last), j1 = std::min(std::max((int)v0 + 1, 0), last);
+  const V3 c = lerp3(lerp3(env_texel(S, face, i0, j0), env_texel(S, face, i1, j0), fu),
+                     lerp3(env_texel(S, face, i0, j1), env_texel(S, face, i1, j1), fu), fv);
+  return c * S.env_intensity;
+}
+
 static inline V3 pt_miss(const PtScene& S, V3 d) {
   if (S.background == 1u) return d.y > 0.0f ? v3(0.7f, 0.7f, 0.7f) : v3(0.3f, 0.3f, 0.3f);
+  if (S.background == 2u) return pt_env(S, d);
   return v3(S.bg[0], S.bg[1], S.bg[2]);
 }
 

@@ -10,7 +10,8 @@
 //   mix(0.2, 1, max f0): bsdf, pdf and importance sample
 //                                        lighting/transport/src/surface/microfacet/device/{mod,diffuse,specular}.rs
 //   tbn, concentric disk                 shader/library/src/sampling.rs:72-119
-//   miss radiance (solid colour, test)   path_tracing/ray_miss.rs:136-152
+//   miss radiance (solid colour, test, environment cube)
+//                                        path_tracing/ray_miss.rs:136-152
 //   tone maps                            content/texture/gpu-process/src/tonemap.rs:53-200
 //
 // The reference's shaders evaluate atan, sin, cos and pow with the GPU
@@ -272,9 +273,68 @@ __device__ __forceinline__ float3 pt_sample(const PtSurface& s, float3 v, float3
   return l;
 }
 
+// Texel (i, j) of cube face f.
+__device__ __forceinline__ float3 env_texel(const PtEnv& E, uint32_t f, int i, int j) {
+  const float4 c = __ldg(E.env + ((size_t)f * E.env_size + (uint32_t)j) * E.env_size + (uint32_t)i);
+  return make_float3(c.x, c.y, c.z);
+}
+__device__ __forceinline__ float3 lerp3(float3 a, float3 b, float f) {
+  return make_float3(a.x * (1.0f - f) + b.x * f, a.y * (1.0f - f) + b.y * f, a.z * (1.0f - f) + b.z * f);
+}
+
+// EnvCube: transform_dir (shader/library/src/lib.rs:13-16: M (d, 1), divided
+// by w), then the cube face of the major axis (ties: x before y before z) with
+// the standard face coordinates, bilinear over texel centres, clamped to the
+// face's edge, at level 0; times the intensity (ray_miss.rs:139-147). The
+// reference samples a GPU cube texture: its filter weights are the texture
+// unit's fixed-point ones and it blends across face edges; here the weights
+// are f32 and each face is clamped to its own edge. A non-finite or zero
+// direction samples black.
+__device__ __forceinline__ float3 pt_env(const PtEnv& E, float3 d) {
+  const float* m = E.env_transform;
+  const float rx = d.x * m[0] + d.y * m[4] + d.z * m[8] + 1.0f * m[12];
+  const float ry = d.x * m[1] + d.y * m[5] + d.z * m[9] + 1.0f * m[13];
+  const float rz = d.x * m[2] + d.y * m[6] + d.z * m[10] + 1.0f * m[14];
+  const float rw = d.x * m[3] + d.y * m[7] + d.z * m[11] + 1.0f * m[15];
+  const float x = rx / rw, y = ry / rw, z = rz / rw;
+  const float ax = fabsf(x), ay = fabsf(y), az = fabsf(z);
+  if (!(ax <= 3.0e38f && ay <= 3.0e38f && az <= 3.0e38f) || (ax == 0.0f && ay == 0.0f && az == 0.0f))
+    return splat3(0.0f);
+  uint32_t face;
+  float sc, tc, ma;
+  if (ax >= ay && ax >= az) {
+    face = x >= 0.0f ? 0u : 1u;
+    sc = x >= 0.0f ? -z : z;
+    tc = -y;
+    ma = ax;
+  } else if (ay >= az) {
+    face = y >= 0.0f ? 2u : 3u;
+    sc = x;
+    tc = y >= 0.0f ? z : -z;
+    ma = ay;
+  } else {
+    face = z >= 0.0f ? 4u : 5u;
+    sc = z >= 0.0f ? x : -x;
+    tc = -y;
+    ma = az;
+  }
+  const float n = (float)E.env_size;
+  const float u = ((sc / ma + 1.0f) * 0.5f) * n - 0.5f;
+  const float v = ((tc / ma + 1.0f) * 0.5f) * n - 0.5f;
+  const float u0 = floorf(u), v0 = floorf(v);
+  const float fu = u - u0, fv = v - v0;
+  const int last = (int)E.env_size - 1;
+  const int i0 = min(max((int)u0, 0), last), i1 = min(max((int)u0 + 1, 0), last);
+  const int j0 = min(max((int)v0, 0), last), j1 = min(max((int)v0 + 1, 0), last);
+  const float3 c = lerp3(lerp3(env_texel(E, face, i0, j0), env_texel(E, face, i1, j0), fu),
+                         lerp3(env_texel(E, face, i0, j1), env_texel(E, face, i1, j1), fu), fv);
+  return c * E.env_intensity;
+}
+
 // PTRayMissCtxInvocation::sample_radiance
 __device__ __forceinline__ float3 pt_miss(const PtEnv& E, float3 d) {
   if (E.background == PT_BACKGROUND_TEST) return d.y > 0.0f ? splat3(0.7f) : splat3(0.3f);
+  if (E.background == PT_BACKGROUND_ENV_CUBE) return pt_env(E, d);
   return make_float3(E.bg[0], E.bg[1], E.bg[2]);
 }
 

@@ -34,7 +34,7 @@ static_assert(sizeof(PtLight) == 24, "24 B light");
 
 constexpr uint32_t PT_TONE_NONE = 0, PT_TONE_LINEAR = 1, PT_TONE_REINHARD = 2, PT_TONE_CINEON = 3,
                    PT_TONE_ACES = 4;
-constexpr uint32_t PT_BACKGROUND_SOLID = 0, PT_BACKGROUND_TEST = 1;
+constexpr uint32_t PT_BACKGROUND_SOLID = 0, PT_BACKGROUND_TEST = 1, PT_BACKGROUND_ENV_CUBE = 2;
 
 struct PtEnv {
   AoEnv view;  // camera, frame size, sample index, TLAS, built arrays, normals, RGBA8 image, ray counts
@@ -54,6 +54,10 @@ struct PtEnv {
                       // 2 wavefront passes over path queues (PtWave)
   uint32_t* fetch;    // refill schedule: the frame's pixel counter (zeroed before the launch)
   uint32_t register_tier;  // refill schedule, local-stack walks: 0 compiler's choice, 1 <= 96, 2 <= 64 registers
+  const float4* env;       // environment cube: 6 faces (+X -X +Y -Y +Z -Z) of env_size^2 RGBA texels, rows of t
+  uint32_t env_size;
+  float env_transform[16];  // Mat4, reference memory order
+  float env_intensity;
 };
 
 // Wavefront schedule: path state of every pixel in HBM and queues of pixel

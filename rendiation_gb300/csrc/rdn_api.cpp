@@ -1606,7 +1606,10 @@ rdn_status rdn_path_tracing_render(rdn_ctx* c, const rdn_pt_desc* d, void* strea
   if (!c || !d) return fail(c, RDN_ERR_INVALID_ARG, "null context or descriptor");
   if (c->device < 0) return fail(c, RDN_ERR_UNSUPPORTED, "host-only context cannot trace");
   if (d->tone_map > RDN_TONE_MAP_ACES_FILMIC) return fail(c, RDN_ERR_INVALID_ARG, "unknown tone map");
-  if (d->background > RDN_PT_BACKGROUND_TEST) return fail(c, RDN_ERR_INVALID_ARG, "unknown background");
+  if (d->background > RDN_PT_BACKGROUND_ENV_CUBE) return fail(c, RDN_ERR_INVALID_ARG, "unknown background");
+  if (d->background == RDN_PT_BACKGROUND_ENV_CUBE &&
+      (!d->env_cube || d->env_size == 0 || d->env_size > 16384 || (reinterpret_cast<uintptr_t>(d->env_cube) & 15)))
+    return fail(c, RDN_ERR_INVALID_ARG, "the environment cube needs 16-byte aligned faces of 1..16384 texels");
   if (d->max_path_depth > 64) return fail(c, RDN_ERR_INVALID_ARG, "max_path_depth must be at most 64");
   if (d->light_count && !d->lights) return fail(c, RDN_ERR_INVALID_ARG, "null lights with light_count > 0");
   if (d->material_count && !d->materials)
@@ -1659,6 +1662,10 @@ rdn_status rdn_path_tracing_render(rdn_ctx* c, const rdn_pt_desc* d, void* strea
   e.radiance = reinterpret_cast<float4*>(d->radiance);
   e.schedule = d->schedule;
   e.register_tier = d->register_tier;
+  e.env = reinterpret_cast<const float4*>(d->env_cube);
+  e.env_size = d->env_size;
+  std::memcpy(e.env_transform, d->env_transform, sizeof(e.env_transform));
+  e.env_intensity = d->env_intensity;
   e.fetch = c->d_counters + 13;
   rdn::PtWave w;
   std::memset(&w, 0, sizeof(w));

@@ -156,7 +156,8 @@ class PtDesc(C.Structure):
                 ("materials", C.c_void_p), ("sm_to_material", C.c_void_p), ("sm_count", C.c_uint32),
                 ("block_size", C.c_uint32), ("normals", C.c_void_p), ("image", C.c_void_p), ("radiance", C.c_void_p),
                 ("ray_counts", C.c_void_p), ("schedule", C.c_uint32), ("register_tier", C.c_uint32),
-                ("scratch", C.c_void_p), ("scratch_bytes", C.c_size_t)]
+                ("scratch", C.c_void_p), ("scratch_bytes", C.c_size_t), ("env_cube", C.c_void_p),
+                ("env_size", C.c_uint32), ("env_transform", C.c_float * 16), ("env_intensity", C.c_float)]
 
 
 _lib = None

@@ -28,7 +28,7 @@ from . import native
 from .raytracing import TRAVERSAL_ORDERED_WIDE, _check
 
 TONE_MAP_NONE, TONE_MAP_LINEAR, TONE_MAP_REINHARD, TONE_MAP_CINEON, TONE_MAP_ACES_FILMIC = 0, 1, 2, 3, 4
-BACKGROUND_SOLID, BACKGROUND_TEST = 0, 1
+BACKGROUND_SOLID, BACKGROUND_TEST, BACKGROUND_ENV_CUBE = 0, 1, 2
 SCHEDULE_PIXEL, SCHEDULE_REFILL, SCHEDULE_WAVEFRONT = 0, 1, 2
 MAX_RAY_DEPTH = 3  # path_tracing/mod.rs:80
 
@@ -90,7 +90,8 @@ class DeviceReferencePathTracingRenderer:
                  sm_to_material=None, normals=None, max_path_depth=MAX_RAY_DEPTH, tone_map=TONE_MAP_ACES_FILMIC,
                  exposure=1.0, background=BACKGROUND_SOLID, background_color=(0.0, 0.0, 0.0),
                  traversal=TRAVERSAL_ORDERED_WIDE, tlas_uniform=0, block_size=0, keep_radiance=False,
-                 count_rays=False, schedule=SCHEDULE_REFILL, register_tier=0):
+                 count_rays=False, schedule=SCHEDULE_REFILL, register_tier=0, env_cube=None, env_transform=None,
+                 env_intensity=1.0):
         import torch
 
         self.system = system
@@ -123,6 +124,16 @@ class DeviceReferencePathTracingRenderer:
         self.traversal, self.tlas_uniform, self.block_size = traversal, tlas_uniform, block_size
         self.schedule = schedule
         self.register_tier = register_tier
+        # environment cube (BACKGROUND_ENV_CUBE): float32 (6, size, size, 4), faces +X -X +Y -Y +Z -Z
+        self._env = None
+        self.env_size = 0
+        if env_cube is not None:
+            cube = np.ascontiguousarray(env_cube, np.float32)
+            assert cube.ndim == 4 and cube.shape[0] == 6 and cube.shape[1] == cube.shape[2] and cube.shape[3] == 4
+            self.env_size = cube.shape[1]
+            self._env = torch.from_numpy(cube.reshape(-1).copy()).cuda()
+        self.env_transform = np.asarray(env_transform if env_transform is not None else np.eye(4), np.float32)
+        self.env_intensity = float(env_intensity)
         self.radiance = (torch.zeros(self.width * self.height * 4, dtype=torch.float32, device="cuda")
                          if keep_radiance else None)
         self.ray_counts = torch.zeros(2, dtype=torch.int32, device="cuda") if count_rays else None
@@ -161,6 +172,10 @@ class DeviceReferencePathTracingRenderer:
         d.ray_counts = self.ray_counts.data_ptr() if self.ray_counts is not None else None
         d.schedule = self.schedule
         d.register_tier = self.register_tier
+        d.env_cube = self._env.data_ptr() if self._env is not None else None
+        d.env_size = self.env_size
+        d.env_transform[:] = [float(v) for v in self.env_transform.T.reshape(-1)]  # columns, reference order
+        d.env_intensity = self.env_intensity
         if self.schedule == SCHEDULE_WAVEFRONT:
             d.scratch, d.scratch_bytes = self._scratch_ptr()
         return d

@@ -281,3 +281,75 @@ def test_one_bounce_frame_against_float64():
     got = np.stack([img & 0xFF, (img >> 8) & 0xFF, (img >> 16) & 0xFF], 1)
     assert np.max(np.abs(got - np.rint(q))) <= 1
     assert np.all((img >> 24) == 255)
+
+
+def env_sample64(cube, m, d, intensity):
+    """Cube-map lookup in float64: M (d, 1) / w, the major axis's face, bilinear over texel centres clamped to
+    the face (the convention rdn_pt_desc.env_cube documents)."""
+    r = m @ np.array([d[0], d[1], d[2], 1.0])
+    x, y, z = r[:3] / r[3]
+    ax, ay, az = abs(x), abs(y), abs(z)
+    if ax >= ay and ax >= az:
+        face, sc, tc, ma = (0, -z, -y, ax) if x >= 0 else (1, z, -y, ax)
+    elif ay >= az:
+        face, sc, tc, ma = (2, x, z, ay) if y >= 0 else (3, x, -z, ay)
+    else:
+        face, sc, tc, ma = (4, x, -y, az) if z >= 0 else (5, -x, -y, az)
+    n = cube.shape[1]
+    u = (sc / ma + 1) / 2 * n - 0.5
+    v = (tc / ma + 1) / 2 * n - 0.5
+    i0, j0 = int(np.floor(u)), int(np.floor(v))
+    fu, fv = u - i0, v - j0
+    c = lambda i, j: cube[face, min(max(j, 0), n - 1), min(max(i, 0), n - 1), :3].astype(np.float64)
+    top = c(i0, j0) * (1 - fu) + c(i0 + 1, j0) * fu
+    bot = c(i0, j0 + 1) * (1 - fu) + c(i0 + 1, j0 + 1) * fu
+    return (top * (1 - fv) + bot * fv) * intensity
+
+
+def test_env_cube_background_against_float64():
+    """Camera rays that all miss sample the environment cube (PTRayMissCtx::EnvCube): each pixel's radiance
+    against a float64 lookup of the same direction."""
+    W, H = 24, 18
+    mesh = scenes.Mesh(np.array([[50, 50, 50], [51, 50, 50], [50, 51, 50]], np.float32), np.arange(3, dtype=np.uint32))
+    S = single_mesh_scene(mesh).build_oracle()
+    rng = np.random.default_rng(9)
+    cube = rng.random((6, 8, 8, 4)).astype(np.float32)
+    a = 0.6
+    rot = np.array([[np.cos(a), -np.sin(a), 0, 0], [np.sin(a), np.cos(a), 0, 0], [0, 0, 1, 0], [0, 0, 0, 1]])
+    for eye, target in (((0, 0, 0), (1, 0.2, 0.1)), ((0, 0, 0), (-0.3, -1, 0.4)), ((0, 0, 0), (0.2, 0.1, -1))):
+        vp = tg.look_at_view_projection_inv(eye, target, (0, 0, 1) if abs(target[2]) < 0.9 else (0, 1, 0), 100.0,
+                                            W / H)
+        img = np.zeros(W * H, np.uint32)
+        rad = np.zeros(W * H * 4, np.float32)
+        orc.pt_render(S, vp, np.asarray(eye, np.float32), W, H, img, max_depth=3, tone_map=pt.TONE_MAP_NONE,
+                      background=pt.BACKGROUND_ENV_CUBE, env_cube=cube, env_transform=rot, env_intensity=1.5,
+                      radiance=rad, threads=2)
+        rad = rad.reshape(H, W, 4)
+        assert np.all(rad[..., 3] == 1.0)  # one core ray each, a miss
+        for y in range(H):
+            for x in range(W):
+                nx = pcg_states(xxhash32(x, y, 0))
+                ux, uy = x / W + nx() / W, y / H + nx() / H
+                r = np.asarray(vp, np.float64).reshape(4, 4).T @ np.array([2 * ux - 1, -(2 * uy - 1), 1.0, 1.0])
+                d = r[:3] / r[3] - np.asarray(eye, np.float64)
+                d /= np.linalg.norm(d)
+                want = env_sample64(cube, rot, d, 1.5)
+                assert np.allclose(rad[y, x, :3], want, atol=2e-4), (x, y, rad[y, x], want)
+
+
+def test_env_cube_faces_and_texel_centres():
+    """Directions through texel centres of each face return the texel itself (times the intensity)."""
+    mesh = scenes.Mesh(np.array([[50, 50, 50], [51, 50, 50], [50, 51, 50]], np.float32), np.arange(3, dtype=np.uint32))
+    S = single_mesh_scene(mesh).build_oracle()
+    cube = np.zeros((6, 2, 2, 4), np.float32)
+    for f in range(6):
+        cube[f, :, :, :3] = (f + 1) / 10.0
+    # a 1x1 frame looking straight along each axis: the ray passes the face centre (4 texels of equal value)
+    for f, (target, up) in enumerate((((1, 0, 0), (0, 0, 1)), ((-1, 0, 0), (0, 0, 1)), ((0, 1, 0), (0, 0, 1)),
+                                      ((0, -1, 0), (0, 0, 1)), ((0, 0, 1), (0, 1, 0)), ((0, 0, -1), (0, 1, 0)))):
+        vp = tg.look_at_view_projection_inv((0, 0, 0), target, up, 1.0, 1.0)
+        img = np.zeros(1, np.uint32)
+        rad = np.zeros(4, np.float32)
+        orc.pt_render(S, vp, np.zeros(3, np.float32), 1, 1, img, tone_map=pt.TONE_MAP_NONE,
+                      background=pt.BACKGROUND_ENV_CUBE, env_cube=cube, env_intensity=2.0, radiance=rad, threads=1)
+        assert np.allclose(rad[:3], 2.0 * (f + 1) / 10.0, rtol=1e-6), (f, rad)

@@ -249,3 +249,28 @@ def test_render_accumulates_and_resets(cuda):
     torch.cuda.synchronize()
     assert np.array_equal(R.result(), first)
     assert np.all(first[..., 3] == 255)
+
+
+@pytest.mark.parametrize("schedule", [pt.SCHEDULE_PIXEL, pt.SCHEDULE_REFILL, pt.SCHEDULE_WAVEFRONT])
+def test_environment_cube_background(cuda, schedule):
+    """PTRayMissCtx::EnvCube: escaping paths sample a rotated, scaled cube map;
+    every texel and radiance bit-identical to the oracle in reference order."""
+    rng = np.random.default_rng(12)
+    cube = rng.random((6, 16, 16, 4)).astype(np.float32)
+    a = 0.9
+    rot = np.array([[1, 0, 0, 0], [0, np.cos(a), -np.sin(a), 0], [0, np.sin(a), np.cos(a), 0], [0, 0, 0, 1]])
+    want_img, want_rad, img, rad, rays_o, rays_g = run_pair(
+        field, with_normals=True, lights=LIGHTS[:2], materials=MATERIALS, background=pt.BACKGROUND_ENV_CUBE,
+        env_cube=cube, env_transform=rot, env_intensity=1.7, schedule=schedule)
+    assert np.array_equal(img, want_img) and same_bits(rad, want_rad).all()
+    assert rays_g == rays_o
+    # some paths escaped to the environment
+    assert len(np.unique(want_rad.reshape(-1, 4)[:, 3])) > 1
+
+
+def test_environment_cube_needs_a_map(cuda):
+    scene, _, vp, eye = field()
+    P = scene.build_product()
+    R = pt.DeviceReferencePathTracingRenderer(P, W, H, vp, eye, background=pt.BACKGROUND_ENV_CUBE)
+    with pytest.raises(native.RdnError):
+        R.render()
