@@ -857,12 +857,21 @@ typedef struct rdn_pt_desc {
   uint32_t env_size;
   float env_transform[16];        /* IblShaderInfoForBackground.transform, Mat4 in the reference's memory order */
   float env_intensity;            /* IblShaderInfoForBackground.intensity */
+  uint32_t* sample_counter;       /* device, nullable: when set, the frame reads its sample index from here
+                                     instead of sample_count and adds one to it at its end, so that a
+                                     captured frame (rdn_pt_capture) advances by itself */
 } rdn_pt_desc;
 
 /* Scratch of the wavefront schedule for a width x height frame: 112 B of path
  * state and two 4 B queue entries per pixel. */
 rdn_status rdn_pt_scratch_size(uint32_t width, uint32_t height, size_t* bytes);
 rdn_status rdn_path_tracing_render(rdn_ctx* ctx, const rdn_pt_desc* desc, void* stream);
+/* One path-traced sample captured into an executable CUDA graph: the
+ * descriptor is baked in; with desc->sample_counter set each rdn_graph_launch
+ * draws the next sample (PTRenderState::next_sample on the device). The
+ * context's structure must stay built and the buffers alive while the graph
+ * is in use; one replay at a time per context with the refill schedule. */
+rdn_status rdn_pt_capture(rdn_ctx* ctx, const rdn_pt_desc* desc, rdn_graph** out);
 
 #ifdef __cplusplus
 }

@@ -1621,6 +1621,8 @@ rdn_status rdn_path_tracing_render(rdn_ctx* c, const rdn_pt_desc* d, void* strea
     return fail(c, RDN_ERR_INVALID_ARG, "lights, materials, sm_to_material and normals must be 4-byte aligned");
   if (reinterpret_cast<uintptr_t>(d->radiance) & 15)
     return fail(c, RDN_ERR_INVALID_ARG, "radiance must be 16-byte aligned");
+  if (reinterpret_cast<uintptr_t>(d->sample_counter) & 3)
+    return fail(c, RDN_ERR_INVALID_ARG, "sample_counter must be 4-byte aligned");
   if (d->schedule > RDN_PT_SCHEDULE_WAVEFRONT) return fail(c, RDN_ERR_INVALID_ARG, "unknown schedule");
   if (d->schedule == RDN_PT_SCHEDULE_WAVEFRONT) {
     if (!d->scratch || (reinterpret_cast<uintptr_t>(d->scratch) & 255))
@@ -1643,6 +1645,7 @@ rdn_status rdn_path_tracing_render(rdn_ctx* c, const rdn_pt_desc* d, void* strea
   ad.image = d->image;
   ad.block_size = d->block_size;
   ad.ray_counts = d->ray_counts;
+  ad.sample_counter = d->sample_counter;
   rdn::TraceParams p;
   rdn::PtEnv e;
   std::memset(&e, 0, sizeof(e));
@@ -1673,8 +1676,21 @@ rdn_status rdn_path_tracing_render(rdn_ctx* c, const rdn_pt_desc* d, void* strea
   cudaError_t err = cudaSetDevice(c->device);
   if (err == cudaSuccess)
     err = rdn::launch_pt(p, e, &w, mode_of(d->traversal), c->sm_count, static_cast<cudaStream_t>(stream));
+  if (err == cudaSuccess && d->sample_counter)
+    err = rdn::launch_ao_advance(d->sample_counter, static_cast<cudaStream_t>(stream));
   if (err != cudaSuccess) return cuda_fail(c, err, "path tracing launch");
   return RDN_OK;
+}
+
+rdn_status rdn_pt_capture(rdn_ctx* c, const rdn_pt_desc* d, rdn_graph** out) {
+  Range range_("rdn_pt_capture");
+  if (!c || !d || !out) return fail(c, RDN_ERR_INVALID_ARG, "null context, descriptor or output");
+  *out = nullptr;
+  if (c->device < 0) return fail(c, RDN_ERR_UNSUPPORTED, "host-only context cannot trace");
+  rdn_status st = require_built(c);
+  if (st != RDN_OK) return st;
+  return capture_graph(
+      c, "path-traced frame capture", [&](cudaStream_t s) { return rdn_path_tracing_render(c, d, s); }, out);
 }
 
 }  // extern "C"

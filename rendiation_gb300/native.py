@@ -33,7 +33,7 @@ EXPORTED_SYMBOLS = [
     "rdn_task_graph_destroy", "rdn_task_graph_dispatch_init", "rdn_task_graph_execute", "rdn_task_graph_states",
     "rdn_task_graph_debug", "rdn_task_graph_check_errors", "rdn_ao_pipeline_create", "rdn_ao_render_graph",
     "rdn_ao_render", "rdn_ao_capture", "rdn_task_graph_capture", "rdn_task_graph_set_poll", "rdn_trace_params",
-    "rdn_path_tracing_render", "rdn_pt_scratch_size",
+    "rdn_path_tracing_render", "rdn_pt_scratch_size", "rdn_pt_capture",
 ]
 
 
@@ -157,7 +157,8 @@ class PtDesc(C.Structure):
                 ("block_size", C.c_uint32), ("normals", C.c_void_p), ("image", C.c_void_p), ("radiance", C.c_void_p),
                 ("ray_counts", C.c_void_p), ("schedule", C.c_uint32), ("register_tier", C.c_uint32),
                 ("scratch", C.c_void_p), ("scratch_bytes", C.c_size_t), ("env_cube", C.c_void_p),
-                ("env_size", C.c_uint32), ("env_transform", C.c_float * 16), ("env_intensity", C.c_float)]
+                ("env_size", C.c_uint32), ("env_transform", C.c_float * 16), ("env_intensity", C.c_float),
+                ("sample_counter", C.c_void_p)]
 
 
 _lib = None
@@ -273,5 +274,7 @@ def lib() -> C.CDLL:
     L.rdn_path_tracing_render.restype = i32
     L.rdn_pt_scratch_size.argtypes = [u32, u32, C.POINTER(C.c_size_t)]
     L.rdn_pt_scratch_size.restype = i32
+    L.rdn_pt_capture.argtypes = [vp, C.POINTER(PtDesc), C.POINTER(vp)]
+    L.rdn_pt_capture.restype = i32
     _lib = L
     return L

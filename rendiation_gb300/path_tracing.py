@@ -180,6 +180,27 @@ class DeviceReferencePathTracingRenderer:
             d.scratch, d.scratch_bytes = self._scratch_ptr()
         return d
 
+    def capture(self, counter):
+        """One sample captured into a CUDA graph (rdn_pt_capture) that reads its
+        sample index from `counter` (a CUDA int32 tensor of one element) and
+        advances it; returns a callable that replays the sample."""
+        d = self.desc()
+        d.sample_counter = counter.data_ptr()
+        g = C.c_void_p()
+        _check(self.system._h, self.system._L.rdn_pt_capture(self.system._h, C.byref(d), C.byref(g)))
+        L = self.system._L
+
+        class Frame:
+            def __call__(self_inner, stream=None):
+                st = L.rdn_graph_launch(g, _stream(stream))
+                if st != native.RDN_OK:
+                    raise native.RdnError(st, "rdn_graph_launch")
+
+            def __del__(self_inner):
+                L.rdn_graph_destroy(g)
+
+        return Frame()
+
     def render(self, stream=None):
         d = self.desc()
         _check(self.system._h, self.system._L.rdn_path_tracing_render(self.system._h, C.byref(d), _stream(stream)))

@@ -274,3 +274,27 @@ def test_environment_cube_needs_a_map(cuda):
     R = pt.DeviceReferencePathTracingRenderer(P, W, H, vp, eye, background=pt.BACKGROUND_ENV_CUBE)
     with pytest.raises(native.RdnError):
         R.render()
+
+
+@pytest.mark.parametrize("schedule", [pt.SCHEDULE_REFILL, pt.SCHEDULE_WAVEFRONT])
+def test_captured_sample_advances_itself(cuda, schedule):
+    """rdn_pt_capture: a sample that reads its index from a device counter and
+    advances it; three replays equal three samples drawn with host-side counts."""
+    import torch
+
+    scene, _, vp, eye = field()
+    P = scene.build_product()
+    kw = dict(lights=LIGHTS, materials=MATERIALS, traversal=rt.TRAVERSAL_ORDERED_WIDE, schedule=schedule)
+    ref = pt.DeviceReferencePathTracingRenderer(P, W, H, vp, eye, **kw)
+    for s in (5, 6, 7):
+        ref.sample_count = s
+        ref.render()
+    cap = pt.DeviceReferencePathTracingRenderer(P, W, H, vp, eye, **kw)
+    counter = torch.tensor([5], dtype=torch.int32, device="cuda")
+    frame = cap.capture(counter)
+    for _ in range(3):
+        frame()
+    torch.cuda.synchronize()
+    assert int(counter.item()) == 8
+    assert np.array_equal(cap.result(), ref.result())
+    assert P.check_errors() == (0, 0)
