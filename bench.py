@@ -932,6 +932,22 @@ def bench_path_tracing(args, P, S_field):
                "shapes_ms": {f"{('pixel', 'refill', 'wavefront')[k[2]]}/{k[0]}/{k[1]}": round(v, 4)
                              for k, v in shapes.items()},
                "register_tiers_ms": {str(k): round(v, 4) for k, v in tiers.items()}}
+        # the same sample captured once (rdn_pt_capture) and replayed: it reads and advances a device
+        # sample counter, so every replay draws the next sample without host work
+        counter = torch.zeros(1, dtype=torch.int32, device="cuda")
+        frame = R.capture(counter)
+        for _ in range(args.warmup):
+            frame()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            frame()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        cms = e0.elapsed_time(e1) / reps
+        leg["captured_ms_per_sample"] = round(cms, 4)
+        leg["captured_mrays"] = round((core + shadow) / cms / 1e3, 1)
+        del frame
         if name == "clamped" and S_field is not None:
             from oracle import orc
 
