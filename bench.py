@@ -1835,6 +1835,11 @@ def headline(out: dict) -> dict:
         h["parity_frame_ties"] = {"primary": fr["primary"]["tie"], "bounce": fr["bounce"]["tie"]}
         h["parity_frame_nan_exposed"] = {"primary": fr["primary"]["nan"], "shadow": fr["shadow"]["nan"],
                                          "bounce": fr["bounce"]["nan"]}
+    if "path_tracing" in out:
+        ptl = out["path_tracing"]
+        h["path_tracer_mrays"] = {k: ptl[k]["mrays"] for k in ("clamped", "full_1080p") if k in ptl}
+        if "parity_texels_identical" in ptl.get("clamped", {}):
+            h["path_tracer_parity_texels_identical"] = ptl["clamped"]["parity_texels_identical"]
     return h
 
 
