@@ -298,3 +298,19 @@ def test_captured_sample_advances_itself(cuda, schedule):
     assert int(counter.item()) == 8
     assert np.array_equal(cap.result(), ref.result())
     assert P.check_errors() == (0, 0)
+
+
+def test_edge_materials(cuda):
+    """Materials at the ends of their ranges: a perfect mirror (roughness 0: GGX's D is 0/0 = NaN, and
+    every sample takes the specular lobe), roughness 1, zero reflectance, a black specular colour. NaN
+    radiance must match NaN, and the texels (where saturate and the unorm store see it) bit for bit."""
+    mats = np.array([pt.metallic_material((1.0, 1.0, 1.0), 0.0, 1.0),
+                     pt.metallic_material((0.3, 0.6, 0.9), 1.0, 0.0, 0.0),
+                     pt.specular_material((0.7, 0.7, 0.7), 0.3, (0.0, 0.0, 0.0)),
+                     pt.metallic_material((0.0, 0.0, 0.0), 0.5, 0.5, 1.0)], pt.MATERIAL_DTYPE)
+    for tone in (pt.TONE_MAP_ACES_FILMIC, pt.TONE_MAP_NONE):
+        want_img, want_rad, img, rad, rays_o, rays_g = run_pair(
+            instanced, lights=LIGHTS, materials=mats, sm_to_material=[0, 1, 2, 3, 0, 1, 2, 3, 0, 1, 2, 3],
+            tone_map=tone, bg=(0.2, 0.3, 0.4))
+        assert np.array_equal(img, want_img) and same_bits(rad, want_rad).all()
+        assert rays_g == rays_o
