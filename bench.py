@@ -834,6 +834,16 @@ def bench_ao(args, P, S_field):
     best = min(shapes, key=shapes.get)
     descs["fused"].traversal, descs["fused"].block_size = best
     out["fused_shape"] = {"traversal": {0: "binary", 1: "reference", 2: "wide"}[best[0]], "block": best[1]}
+    # leaf postponement threshold of the ordered walks, per form, timed on the frame
+    if traversal != rt.TRAVERSAL_REFERENCE:
+        for mode in ("fused", "graph"):
+            spec_ms = {}
+            for k in (0, 2, 4, 8, 16):
+                descs[mode].speculation = k
+                spec_ms[k] = timed(lambda i: frame(mode, i))[0]
+            descs[mode].speculation = min(spec_ms, key=spec_ms.get)
+            out[mode + "_speculation"] = descs[mode].speculation
+            out[mode + "_speculation_ms"] = {str(k): round(v, 4) for k, v in spec_ms.items()}
     ms, rays = timed(lambda k: frame("fused", k))
     out["rays_per_frame"] = rays
     out["fused_ms"], out["fused_mrays"] = round(ms, 4), round(rays / ms / 1e3, 1)
@@ -897,8 +907,8 @@ def bench_path_tracing(args, P, S_field):
                                                   count_rays=True)
         reps = 20
 
-        def timed(trav, block, sched, tier=0):
-            R.traversal, R.block_size, R.schedule, R.register_tier = trav, block, sched, tier
+        def timed(trav, block, sched, tier=0, spec=0):
+            R.traversal, R.block_size, R.schedule, R.register_tier, R.speculation = trav, block, sched, tier, spec
             for _ in range(args.warmup):
                 R.render()
             R.ray_counts.zero_()
@@ -924,14 +934,21 @@ def bench_path_tracing(args, P, S_field):
             for tier in (1, 2):
                 tiers[tier] = timed(*best, tier)[0]
         tier = min(tiers, key=tiers.get)
-        ms, (core, shadow) = timed(*best, tier)
+        specs = {0: tiers[tier]}
+        if best[0] != rt.TRAVERSAL_REFERENCE:
+            for k in (2, 4, 8, 16):
+                specs[k] = timed(*best, tier, k)[0]
+        spec = min(specs, key=specs.get)
+        ms, (core, shadow) = timed(*best, tier, spec)
         leg = {"size": [W, H], "ms_per_sample": round(ms, 4), "core_rays": core, "shadow_rays": shadow,
                "mrays": round((core + shadow) / ms / 1e3, 1),
                "shape": {"traversal": {0: "binary", 1: "reference", 2: "wide"}[best[0]], "block": best[1],
-                         "schedule": ("pixel", "refill", "wavefront")[best[2]], "register_tier": tier},
+                         "schedule": ("pixel", "refill", "wavefront")[best[2]], "register_tier": tier,
+                         "speculation": spec},
                "shapes_ms": {f"{('pixel', 'refill', 'wavefront')[k[2]]}/{k[0]}/{k[1]}": round(v, 4)
                              for k, v in shapes.items()},
-               "register_tiers_ms": {str(k): round(v, 4) for k, v in tiers.items()}}
+               "register_tiers_ms": {str(k): round(v, 4) for k, v in tiers.items()},
+               "speculation_ms": {str(k): round(v, 4) for k, v in specs.items()}}
         # the same sample captured once (rdn_pt_capture) and replayed: it reads and advances a device
         # sample counter, so every replay draws the next sample without host work
         counter = torch.zeros(1, dtype=torch.int32, device="cuda")

@@ -20,7 +20,10 @@
  *    default stream). Acceleration-structure buffers are owned by the context.
  *  - Create/delete/bind/build take the context's lock (the reference's
  *    Arc<RwLock> write lock, naive/mod.rs:497-609); traces on distinct
- *    streams may run concurrently once the structure is built.
+ *    streams may run concurrently once the structure is built. Persistent
+ *    kernels that claim work from a counter of the context (the refill path
+ *    tracer, the differentiable paths) allow one call of each kind in flight
+ *    per context.
  */
 #ifndef RDN_H
 #define RDN_H
@@ -683,6 +686,8 @@ typedef struct rdn_ao_desc {
   uint32_t* sample_counter;       /* device, nullable: when set, the frame reads its sample index from
                                      here instead of sample_count and adds one to it at its end, so
                                      that a captured frame (rdn_ao_capture) advances by itself */
+  uint32_t speculation;           /* ordered walks: leaf postponement threshold, as in rdn_wavefront_desc
+                                     (the fused kernel and the task graph's trace programs) */
 } rdn_ao_desc;
 
 typedef struct rdn_task_graph rdn_task_graph;
@@ -860,6 +865,7 @@ typedef struct rdn_pt_desc {
   uint32_t* sample_counter;       /* device, nullable: when set, the frame reads its sample index from here
                                      instead of sample_count and adds one to it at its end, so that a
                                      captured frame (rdn_pt_capture) advances by itself */
+  uint32_t speculation;           /* ordered walks: leaf postponement threshold, as in rdn_wavefront_desc */
 } rdn_pt_desc;
 
 /* Scratch of the wavefront schedule for a width x height frame: 112 B of path

@@ -1269,6 +1269,7 @@ rdn_status ao_env(rdn_ctx* c, const rdn_ao_desc* d, rdn::TraceParams& p, rdn::Ao
   a.ray_counts = d->ray_counts;
   a.sample_dev = d->sample_counter;
   a.block = d->block_size;
+  p.spec_threshold = d->speculation;
   return RDN_OK;
 }
 
@@ -1646,6 +1647,7 @@ rdn_status rdn_path_tracing_render(rdn_ctx* c, const rdn_pt_desc* d, void* strea
   ad.block_size = d->block_size;
   ad.ray_counts = d->ray_counts;
   ad.sample_counter = d->sample_counter;
+  ad.speculation = d->speculation;
   rdn::TraceParams p;
   rdn::PtEnv e;
   std::memset(&e, 0, sizeof(e));

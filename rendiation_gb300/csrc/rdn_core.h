@@ -219,7 +219,10 @@ struct rdn_ctx {
   bool dirty = true;
   std::unique_ptr<rdn::HostBuilt> host;
   rdn::DeviceBuilt dev;
-  uint32_t* d_counters = nullptr;  // 4 x u64 counters + error words
+  // 16 words: 0-7 four u64 trace counters, 8 error word, 12 work counter of
+  // the differentiable paths, 13 path tracer's pixel fetch. Calls of one
+  // context that use the same word must not overlap on the GPU.
+  uint32_t* d_counters = nullptr;
   uint32_t iteration_limit = 0;     // cap of the dynamic-fetch loops (0 = built-in)
   cudaMemPool_t build_pool = nullptr;  // stream-ordered scratch of device builds, kept for the next build
   double build_seconds = 0.0, upload_seconds = 0.0, device_seconds = 0.0;

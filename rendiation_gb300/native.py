@@ -144,7 +144,7 @@ class AoDesc(C.Structure):
                 ("height", C.c_uint32), ("sample_count", C.c_uint32), ("tlas_uniform", C.c_uint32),
                 ("traversal", C.c_uint32), ("normals", C.c_void_p), ("image", C.c_void_p),
                 ("sbt_closest", C.c_uint32 * 2), ("sbt_miss", C.c_uint32), ("block_size", C.c_uint32),
-                ("ray_counts", C.c_void_p), ("sample_counter", C.c_void_p)]
+                ("ray_counts", C.c_void_p), ("sample_counter", C.c_void_p), ("speculation", C.c_uint32)]
 
 
 class PtDesc(C.Structure):
@@ -158,7 +158,7 @@ class PtDesc(C.Structure):
                 ("ray_counts", C.c_void_p), ("schedule", C.c_uint32), ("register_tier", C.c_uint32),
                 ("scratch", C.c_void_p), ("scratch_bytes", C.c_size_t), ("env_cube", C.c_void_p),
                 ("env_size", C.c_uint32), ("env_transform", C.c_float * 16), ("env_intensity", C.c_float),
-                ("sample_counter", C.c_void_p)]
+                ("sample_counter", C.c_void_p), ("speculation", C.c_uint32)]
 
 
 _lib = None

@@ -84,14 +84,17 @@ class DeviceReferencePathTracingRenderer:
     are numpy arrays (DIRECTIONAL_LIGHT_DTYPE, MATERIAL_DTYPE, uint32) copied to
     the device once; ``normals`` is a CUDA float tensor of 3 per built vertex
     or None. With ``keep_radiance`` the last sample's HDR radiance and path
-    length per pixel are kept in ``radiance`` (float32, width*height*4)."""
+    length per pixel are kept in ``radiance`` (float32, width*height*4).
+    ``speculation`` is the ordered walks' leaf postponement threshold (a lane
+    holding a leaf keeps descending while more than this many lanes of its
+    warp still look for one)."""
 
     def __init__(self, system, width, height, view_projection_inv, camera_position, lights=None, materials=None,
                  sm_to_material=None, normals=None, max_path_depth=MAX_RAY_DEPTH, tone_map=TONE_MAP_ACES_FILMIC,
                  exposure=1.0, background=BACKGROUND_SOLID, background_color=(0.0, 0.0, 0.0),
                  traversal=TRAVERSAL_ORDERED_WIDE, tlas_uniform=0, block_size=0, keep_radiance=False,
                  count_rays=False, schedule=SCHEDULE_REFILL, register_tier=0, env_cube=None, env_transform=None,
-                 env_intensity=1.0):
+                 env_intensity=1.0, speculation=0):
         import torch
 
         self.system = system
@@ -124,6 +127,7 @@ class DeviceReferencePathTracingRenderer:
         self.traversal, self.tlas_uniform, self.block_size = traversal, tlas_uniform, block_size
         self.schedule = schedule
         self.register_tier = register_tier
+        self.speculation = speculation
         # environment cube (BACKGROUND_ENV_CUBE): float32 (6, size, size, 4), faces +X -X +Y -Y +Z -Z
         self._env = None
         self.env_size = 0
@@ -172,6 +176,7 @@ class DeviceReferencePathTracingRenderer:
         d.ray_counts = self.ray_counts.data_ptr() if self.ray_counts is not None else None
         d.schedule = self.schedule
         d.register_tier = self.register_tier
+        d.speculation = self.speculation
         d.env_cube = self._env.data_ptr() if self._env is not None else None
         d.env_size = self.env_size
         d.env_transform[:] = [float(v) for v in self.env_transform.T.reshape(-1)]  # columns, reference order

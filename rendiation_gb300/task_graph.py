@@ -264,7 +264,7 @@ class AmbientOcclusion:
     pipeline (rdn_ao_render_graph)."""
 
     def __init__(self, system, width, height, view_projection_inv, camera_position, traversal=TRAVERSAL_ORDERED_WIDE,
-                 tlas_uniform=0, normals=None, mode="fused", block_size=0):
+                 tlas_uniform=0, normals=None, mode="fused", block_size=0, speculation=0):
         import torch
 
         self.system = system
@@ -278,6 +278,7 @@ class AmbientOcclusion:
         self.sample_count = 0
         self.mode = mode
         self.block_size = block_size  # fused kernel's threads per block: 32, 64 or 128 (0 = 128)
+        self.speculation = speculation  # ordered walks: leaf postponement threshold (0 = wait for the warp)
         self.graph = None
         if mode == "graph":
             h = C.c_void_p()
@@ -295,6 +296,7 @@ class AmbientOcclusion:
         if counter is not None:
             d.sample_counter = counter.data_ptr()
         d.block_size = self.block_size
+        d.speculation = self.speculation
         return d
 
     def capture(self, counter):

@@ -46,13 +46,14 @@ def run_oracle(scene, samples, normals=None):
     return img
 
 
-def run_gpu(scene, samples, traversal, mode, normals=None, block_size=0):
+def run_gpu(scene, samples, traversal, mode, normals=None, block_size=0, speculation=0):
     import torch
 
     P = scene.build_product()
     vp, eye = camera()
     nt = None if normals is None else torch.from_numpy(normals.reshape(-1)).cuda()
-    ao = tg.AmbientOcclusion(P, W, H, vp, eye, traversal=traversal, normals=nt, mode=mode, block_size=block_size)
+    ao = tg.AmbientOcclusion(P, W, H, vp, eye, traversal=traversal, normals=nt, mode=mode, block_size=block_size,
+                             speculation=speculation)
     for s in samples:
         ao.sample_count = s
         ao.render()
@@ -95,6 +96,19 @@ def test_four_child_walk_matches_except_ties(cuda, mode):
     scene = field_scene()
     want = run_oracle(scene, SAMPLES)
     got, _, flags = run_gpu(scene, SAMPLES, rt.TRAVERSAL_ORDERED_WIDE, mode)
+    assert flags == (0, 0)
+    assert (got == want).mean() > 0.995
+
+
+@pytest.mark.parametrize("mode", ["fused", "graph"])
+@pytest.mark.parametrize("speculation", [4, 16])
+def test_leaf_postponement_threshold(cuda, mode, speculation):
+    """A lane holding a leaf that keeps descending while more than k lanes of
+    its warp look for one only adds node visits: texels stay those of the
+    oracle up to exact-distance ties."""
+    scene = field_scene()
+    want = run_oracle(scene, SAMPLES)
+    got, _, flags = run_gpu(scene, SAMPLES, rt.TRAVERSAL_ORDERED_WIDE, mode, speculation=speculation)
     assert flags == (0, 0)
     assert (got == want).mean() > 0.995
 

@@ -75,7 +75,7 @@ def run_pair(scene_fn, traversal=rt.TRAVERSAL_REFERENCE, with_normals=False, sam
     img = np.zeros(W * H, np.uint32)
     rad = np.zeros(W * H * 4, np.float32)
     rays = [0, 0]
-    okw = {k: v for k, v in kw.items() if k not in ("block_size", "schedule", "register_tier")}
+    okw = {k: v for k, v in kw.items() if k not in ("block_size", "schedule", "register_tier", "speculation")}
     for s in samples:
         r, _ = orc.pt_render(S, vp, eye, W, H, img, sample_count=s, normals=normals, radiance=rad, tlas=tlas,
                              intersector=1 if traversal & rt.INTERSECT_WATERTIGHT else 0, threads=8, **okw)
@@ -162,6 +162,14 @@ def test_watertight_intersector(cuda):
 @pytest.mark.parametrize("traversal", [rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_WIDE])
 def test_ordered_walks_match_except_ties(cuda, traversal):
     want_img, want_rad, img, rad, _, _ = run_pair(instanced, traversal=traversal, lights=LIGHTS, materials=MATERIALS)
+    assert (img == want_img).mean() > 0.995
+    assert same_bits(rad, want_rad).reshape(-1, 4).all(1).mean() > 0.995
+
+
+@pytest.mark.parametrize("speculation", [4, 16])
+def test_leaf_postponement_threshold(cuda, speculation):
+    want_img, want_rad, img, rad, _, _ = run_pair(instanced, traversal=rt.TRAVERSAL_ORDERED_WIDE, lights=LIGHTS,
+                                                  materials=MATERIALS, speculation=speculation)
     assert (img == want_img).mean() > 0.995
     assert same_bits(rad, want_rad).reshape(-1, 4).all(1).mean() > 0.995
 
