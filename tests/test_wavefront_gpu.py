@@ -11,40 +11,44 @@ from helpers import orc, rt, scenes, single_mesh_scene
 pytestmark = pytest.mark.gpu
 
 LIGHT = (0.2, 0.2, 2.0)
+# a light just above the field (heights within +-0.092): about 37 % of the
+# frame's shadow rays hit the terrain, so first-hit searches end on a hit
+LOW_LIGHT = (0.5, 0.5, 0.12)
 
 
-def run_both(mesh, cam, traversal, sample_index=0, bins=4, refill=0, **knobs):
+def run_both(mesh, cam, traversal, sample_index=0, bins=4, refill=0, light=LIGHT, **knobs):
     sc = single_mesh_scene(mesh, bins=bins)
     S, P = sc.build_oracle(), sc.build_product()
-    wf = rt.Wavefront(P, cam, LIGHT, traversal=traversal, refill=refill)
+    wf = rt.Wavefront(P, cam, light, traversal=traversal, refill=refill)
     for k, v in knobs.items():
         setattr(wf.desc, k, v)
     wf.run(sample_index)
     torch.cuda.synchronize()
     got = wf.results()
-    exp, rays, _ = orc.wavefront_shadow_bounce(S, cam.as_floats(), cam.width, cam.height, LIGHT, sample_index,
+    exp, rays, _ = orc.wavefront_shadow_bounce(S, cam.as_floats(), cam.width, cam.height, light, sample_index,
                                                threads=4)
     return got, exp, rays, wf.rays_traced()
 
 
-@pytest.mark.parametrize("sample_index", [0, 5])
-def test_wavefront_reference_order_bit_identical(sample_index, cuda):
+@pytest.mark.parametrize("sample_index,light", [(0, LIGHT), (5, LIGHT), (2, LOW_LIGHT)])
+def test_wavefront_reference_order_bit_identical(sample_index, light, cuda):
     mesh = scenes.heightfield(128, seed=1)
     cam = scenes.heightfield_camera(160, 96)
-    got, exp, rays, counts = run_both(mesh, cam, rt.TRAVERSAL_REFERENCE, sample_index)
+    got, exp, rays, counts = run_both(mesh, cam, rt.TRAVERSAL_REFERENCE, sample_index, light=light)
     assert counts == tuple(rays)
     assert rays[1] > 0.9 * rays[0]  # the field fills the frame
     for f in exp.dtype.names:
         assert np.array_equal(got[f].view(np.uint32), exp[f].view(np.uint32)), f
 
 
+@pytest.mark.parametrize("light", [LIGHT, LOW_LIGHT])
 @pytest.mark.parametrize("refill", [0, 1, 8, 32])
 @pytest.mark.parametrize("traversal", [rt.TRAVERSAL_ORDERED, rt.TRAVERSAL_ORDERED_WIDE])
-def test_wavefront_ordered_matches_except_ties(traversal, refill, cuda):
+def test_wavefront_ordered_matches_except_ties(traversal, refill, light, cuda):
     """refill > 0: the dynamic-fetch secondary schedule."""
     mesh = scenes.heightfield(128, seed=1)
     cam = scenes.heightfield_camera(160, 96)
-    got, exp, rays, counts = run_both(mesh, cam, traversal, refill=refill)
+    got, exp, rays, counts = run_both(mesh, cam, traversal, refill=refill, light=light)
     assert counts == tuple(rays)
     same_primary = (got["primary_prim"] == exp["primary_prim"]) & (got["primary_t"] == exp["primary_t"])
     tie = (~same_primary) & (got["primary_t"] == exp["primary_t"])
@@ -67,8 +71,8 @@ def test_shadow_rays_on_the_two_child_walk(local_stack, tier, cuda):
     and direct term; bounce rays keep the four-child walk."""
     mesh = scenes.heightfield(128, seed=1)
     cam = scenes.heightfield_camera(160, 96)
-    got, exp, rays, counts = run_both(mesh, cam, rt.TRAVERSAL_ORDERED_WIDE, sample_index=4, shadow_walk=1,
-                                      local_stack=local_stack, register_tier=tier)
+    got, exp, rays, counts = run_both(mesh, cam, rt.TRAVERSAL_ORDERED_WIDE, sample_index=4, light=LOW_LIGHT,
+                                      shadow_walk=1, local_stack=local_stack, register_tier=tier)
     assert counts == tuple(rays)
     ok = (got["primary_prim"] == exp["primary_prim"]) & (got["primary_t"] == exp["primary_t"])
     assert ok.mean() > 0.999
