@@ -303,17 +303,9 @@ def bench_wavefront(args, ws, rank):
         s2 = tuner.tune("wavefront-secondary-speculation", [dict(b2, spec=k) for k in (0, 2, 4, 8, 16)],
                         run_phase(2))
         b1, b2 = s1.best, s2.best
-        # third stage (four-child batch schedule): shadow rays on the two-child walk
-        if b2["traversal"] == rt.TRAVERSAL_ORDERED_WIDE and not b2.get("refill", 0):
-            def run_shadow(c):
-                wf.desc.shadow_walk = c["shadow2"]
-                run_phase(2)(c)
-
-            s3 = tuner.tune("wavefront-secondary-shadow-walk", [dict(b2, shadow2=k) for k in (0, 1)], run_shadow)
-            b2 = s3.best
         wf.configure((b1["traversal"], b1["block"], b1.get("local", 0), b1.get("regs", 0), b1.get("spec", 0)),
                      (b2["traversal"], b2["block"], b2.get("local", 0), b2.get("regs", 0), b2.get("spec", 0)),
-                     refill=b2.get("refill", 0), shadow_walk=b2.get("shadow2", 0))
+                     refill=b2.get("refill", 0))
         tuned = {"primary": b1, "secondary": b2}
 
     # one frame to learn the ray counts, then the reference-order visit counts of those rays

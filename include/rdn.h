@@ -362,9 +362,6 @@ typedef struct rdn_wavefront_desc {
                                 rays and samplers are those of the whole frame's rows, so bands that
                                 tile a frame (one per GPU) give exactly its pixel records; out holds
                                 the band's width x camera.height records */
-  uint32_t shadow_walk;      /* RDN_TRAVERSAL_ORDERED_WIDE with refill 0: 1 = the secondary kernel traces
-                                the shadow rays with the two-child walk (fewer box tests before the first
-                                hit ends the search) and the bounce rays with the four-child walk */
 } rdn_wavefront_desc;
 
 /* Scratch size for the secondary-ray queues of a width x height launch. */

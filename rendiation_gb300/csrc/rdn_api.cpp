@@ -278,7 +278,6 @@ rdn_status wavefront_check_knobs(rdn_ctx* c, const rdn_wavefront_desc* d) {
   if (d->local_stack > 1) return fail(c, RDN_ERR_INVALID_ARG, "local_stack must be 0 or 1");
   if (d->register_tier > 2) return fail(c, RDN_ERR_INVALID_ARG, "register_tier must be 0, 1 or 2");
   if (d->speculation > 31) return fail(c, RDN_ERR_INVALID_ARG, "speculation must be 0..31");
-  if (d->shadow_walk > 1) return fail(c, RDN_ERR_INVALID_ARG, "shadow_walk must be 0 or 1");
   if (d->block_size && (d->block_size % 32 || d->block_size > 128))
     return fail(c, RDN_ERR_INVALID_ARG, "block_size must be a multiple of 32 up to 128");
   const uint64_t fh = d->frame_height ? d->frame_height : d->camera.height;
@@ -316,7 +315,6 @@ void wavefront_fill(rdn_ctx* c, const rdn_wavefront_desc* d, rdn::TraceParams& p
   w.register_tier = d->register_tier;
   w.row0 = d->row_offset;
   w.frame_height = d->frame_height ? d->frame_height : d->camera.height;
-  w.shadow_walk = d->shadow_walk;
   p.spec_threshold = d->speculation;
 }
 

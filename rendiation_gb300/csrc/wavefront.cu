@@ -133,11 +133,7 @@ __global__ void __launch_bounds__(128, min_blocks(TIER)) primary_kernel(TracePar
   }
 }
 
-// SH2 (four-child kernels only): shadow rays take the two-child walk, which
-// tests fewer boxes before a first hit ends the search; bounce rays keep the
-// four-child walk. The two-child walk's stack needs at most the binary tree's
-// depth + 1 entries, never more than the four-child walk's 3 * depth + 1.
-template <int MODE, bool LOCAL, int TIER, bool WT, bool SH2 = false>
+template <int MODE, bool LOCAL, int TIER, bool WT>
 __global__ void __launch_bounds__(128, min_blocks(TIER)) secondary_kernel(TraceParams p, WavefrontParams w) {
   extern __shared__ uint2 smem_stack[];
   uint2 local_stack[LOCAL ? kLocalStackEntries : 1];
@@ -173,8 +169,7 @@ __global__ void __launch_bounds__(128, min_blocks(TIER)) secondary_kernel(TraceP
       R.cull_mask = 0xFFu;
       R.ray_flags = shadow ? TF_END_SEARCH : 0u;
       bool bad;
-      if (SH2 && shadow) traverse_ray<MODE_BINARY, false, BuiltinAnyHit, WT>(p, R, w.tlas, stack, stride, bad);
-      else traverse_ray<MODE, false, BuiltinAnyHit, WT>(p, R, w.tlas, stack, stride, bad);
+      traverse_ray<MODE, false, BuiltinAnyHit, WT>(p, R, w.tlas, stack, stride, bad);
       if (shadow) {
         PixelResult* o = w.out + w.shadow_pixel[q];
         o->light = R.best.have ? 2u : 1u;
@@ -300,10 +295,8 @@ cudaError_t launch_wavefront_mode(const TraceParams& p, const WavefrontParams& w
                                   uint32_t phases, cudaStream_t stream) {
   const size_t smem = MODE != MODE_THREADED && !LOCAL ? (size_t)p.stack_depth * block * sizeof(uint2) : 0;
   static std::atomic<uint64_t> attr_done{0};
-  constexpr bool kWide = MODE == MODE_WIDE4;
   cudaError_t e = raise_smem_limit(
       attr_done, {(const void*)primary_kernel<MODE, LOCAL, TIER, WT>, (const void*)secondary_kernel<MODE, LOCAL, TIER, WT>,
-                  (const void*)secondary_kernel<MODE, LOCAL, TIER, WT, kWide>,
                   (const void*)secondary_dynamic_kernel<MODE == MODE_THREADED ? MODE_BINARY : MODE, WT>});
   if (e != cudaSuccess) return e;
   if (phases & 1u) {
@@ -329,19 +322,14 @@ cudaError_t launch_wavefront_mode(const TraceParams& p, const WavefrontParams& w
   const bool dynamic = MODE != MODE_THREADED && w.refill != 0u && !LOCAL;
   int per_sm = 0;
   constexpr int DMODE = MODE == MODE_THREADED ? MODE_BINARY : MODE;  // the threaded walk has no dynamic form
-  const bool sh2 = kWide && w.shadow_walk != 0u && !dynamic;
   if (dynamic)
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, secondary_dynamic_kernel<DMODE, WT>, (int)block, smem);
-  else if (sh2)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, secondary_kernel<MODE, LOCAL, TIER, WT, kWide>,
-                                                      (int)block, smem);
   else
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, secondary_kernel<MODE, LOCAL, TIER, WT>, (int)block, smem);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
   const uint32_t grid2 = (uint32_t)(sm_count * per_sm);
   if (dynamic) secondary_dynamic_kernel<DMODE, WT><<<grid2, block, smem, stream>>>(p, w);
-  else if (sh2) secondary_kernel<MODE, LOCAL, TIER, WT, kWide><<<grid2, block, smem, stream>>>(p, w);
   else secondary_kernel<MODE, LOCAL, TIER, WT><<<grid2, block, smem, stream>>>(p, w);
   return cudaGetLastError();
 }

@@ -45,8 +45,6 @@ struct WavefrontParams {
   uint32_t register_tier;
   // the launch covers rows [row0, row0 + height) of a frame of frame_height rows
   uint32_t row0, frame_height;
-  // four-child walk, batch schedule: 1 = shadow rays take the two-child walk
-  uint32_t shadow_walk;
 };
 
 size_t wavefront_scratch_bytes(uint32_t width, uint32_t height);

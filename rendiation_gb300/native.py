@@ -94,7 +94,7 @@ class WavefrontDesc(C.Structure):
                 ("out", C.c_void_p), ("scratch", C.c_void_p), ("scratch_bytes", C.c_size_t),
                 ("ray_counts", C.c_void_p), ("phases", C.c_uint32), ("refill", C.c_uint32),
                 ("local_stack", C.c_uint32), ("register_tier", C.c_uint32), ("speculation", C.c_uint32),
-                ("row_offset", C.c_uint32), ("frame_height", C.c_uint32), ("shadow_walk", C.c_uint32)]
+                ("row_offset", C.c_uint32), ("frame_height", C.c_uint32)]
 
 
 class PathDesc(C.Structure):

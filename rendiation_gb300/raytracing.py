@@ -294,15 +294,13 @@ class Wavefront:
         self.desc.frame_height = self.frame_camera.height
         self.phase_config = None  # (primary, secondary) (traversal, block) when they differ
 
-    def configure(self, primary, secondary, refill=None, shadow_walk=None):
+    def configure(self, primary, secondary, refill=None):
         """Per-kernel (traversal, block_size[, local_stack[, register_tier[,
         speculation]]]); a frame then issues one call per kernel. refill: secondary schedule (0 = batches of 32 rays
-        per warp, k = dynamic fetch whenever k lanes of a warp are idle); shadow_walk: 1 = a four-child
-        secondary kernel traces its shadow rays with the two-child walk; None keeps the current value."""
+        per warp, k = dynamic fetch whenever k lanes of a warp are idle); None
+        keeps the current one."""
         if refill is not None:
             self.desc.refill = refill
-        if shadow_walk is not None:
-            self.desc.shadow_walk = shadow_walk
         primary = tuple(primary) + (0,) * (5 - len(primary))
         secondary = tuple(secondary) + (0,) * (5 - len(secondary))
         if primary == secondary:

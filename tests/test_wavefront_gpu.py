@@ -62,38 +62,6 @@ def test_wavefront_ordered_matches_except_ties(traversal, refill, light, cuda):
     assert np.all(bsame[ok])
 
 
-@pytest.mark.parametrize("local_stack", [0, 1])
-@pytest.mark.parametrize("tier", [0, 2])
-def test_shadow_rays_on_the_two_child_walk(local_stack, tier, cuda):
-    """shadow_walk = 1: the four-child secondary kernel traces its shadow rays
-    with the two-child walk. Shadow visibility is a hit/miss answer, so every
-    pixel whose primary hit equals the oracle's has the oracle's light flag
-    and direct term; bounce rays keep the four-child walk."""
-    mesh = scenes.heightfield(128, seed=1)
-    cam = scenes.heightfield_camera(160, 96)
-    got, exp, rays, counts = run_both(mesh, cam, rt.TRAVERSAL_ORDERED_WIDE, sample_index=4, light=LOW_LIGHT,
-                                      shadow_walk=1, local_stack=local_stack, register_tier=tier)
-    assert counts == tuple(rays)
-    ok = (got["primary_prim"] == exp["primary_prim"]) & (got["primary_t"] == exp["primary_t"])
-    assert ok.mean() > 0.999
-    lit = exp["light"][ok]
-    assert (lit == 2).any() and (lit == 1).any()  # both shadowed and lit pixels
-    assert np.array_equal(got["light"][ok], lit)
-    assert np.array_equal(got["direct"][ok].view(np.uint32), exp["direct"][ok].view(np.uint32))
-    bsame = (got["bounce_prim"] == exp["bounce_prim"]) | (got["bounce_t"] == exp["bounce_t"])
-    assert np.all(bsame[ok])
-
-
-def test_shadow_walk_is_validated(cuda):
-    mesh = scenes.heightfield(32, seed=1)
-    cam = scenes.heightfield_camera(32, 16)
-    P = single_mesh_scene(mesh).build_product()
-    wf = rt.Wavefront(P, cam, LIGHT, traversal=rt.TRAVERSAL_ORDERED_WIDE)
-    wf.desc.shadow_walk = 2
-    with pytest.raises(RuntimeError, match="shadow_walk"):
-        wf.run(0)
-
-
 def test_wavefront_soup_camera(cuda):
     mesh = scenes.triangle_soup(5000, seed=2)
     cam = scenes.soup_camera(64, 48)
