@@ -20,9 +20,9 @@ W, H = 96, 72
 SAMPLES = (150, 200, 250)
 
 
-def camera():
+def camera(w=W, h=H):
     eye = (0.5, -0.45, 0.75)
-    vp = tg.look_at_view_projection_inv(eye, (0.5, 0.5, 0.0), (0, 0, 1), 45.0, W / H, 0.01, 100.0)
+    vp = tg.look_at_view_projection_inv(eye, (0.5, 0.5, 0.0), (0, 0, 1), 45.0, w / h, 0.01, 100.0)
     return vp, np.asarray(eye, np.float32)
 
 
@@ -37,22 +37,22 @@ def vertex_normals(mesh):
     return n.astype(np.float32)
 
 
-def run_oracle(scene, samples, normals=None):
+def run_oracle(scene, samples, normals=None, w=W, h=H):
     S = scene.build_oracle()
-    vp, eye = camera()
-    img = np.zeros(W * H, np.uint32)
+    vp, eye = camera(w, h)
+    img = np.zeros(w * h, np.uint32)
     for s in samples:
-        orc.ao_render(S, vp, eye, W, H, img, sample_count=s, normals=normals, threads=8)
+        orc.ao_render(S, vp, eye, w, h, img, sample_count=s, normals=normals, threads=8)
     return img
 
 
-def run_gpu(scene, samples, traversal, mode, normals=None, block_size=0, speculation=0):
+def run_gpu(scene, samples, traversal, mode, normals=None, block_size=0, speculation=0, w=W, h=H):
     import torch
 
     P = scene.build_product()
-    vp, eye = camera()
+    vp, eye = camera(w, h)
     nt = None if normals is None else torch.from_numpy(normals.reshape(-1)).cuda()
-    ao = tg.AmbientOcclusion(P, W, H, vp, eye, traversal=traversal, normals=nt, mode=mode, block_size=block_size,
+    ao = tg.AmbientOcclusion(P, w, h, vp, eye, traversal=traversal, normals=nt, mode=mode, block_size=block_size,
                              speculation=speculation)
     for s in samples:
         ao.sample_count = s
@@ -111,6 +111,22 @@ def test_leaf_postponement_threshold(cuda, mode, speculation):
     got, _, flags = run_gpu(scene, SAMPLES, rt.TRAVERSAL_ORDERED_WIDE, mode, speculation=speculation)
     assert flags == (0, 0)
     assert (got == want).mean() > 0.995
+
+
+@pytest.mark.parametrize("mode", ["fused", "graph"])
+@pytest.mark.parametrize("size", [(53, 29), (1, 1), (9, 5)])
+def test_ragged_frames(cuda, mode, size):
+    """Frames that are not whole 8x4 tiles: the tiles' overhanging pixels
+    neither trace nor write; every texel of the frame is the oracle's."""
+    w, h = size
+    scene = field_scene()
+    want = run_oracle(scene, SAMPLES, w=w, h=h)
+    got, ao, flags = run_gpu(scene, SAMPLES, rt.TRAVERSAL_REFERENCE, mode, w=w, h=h)
+    assert flags == (0, 0)
+    assert got.shape == (w * h,)
+    assert np.array_equal(got, want)
+    if mode == "graph":
+        assert ao.graph.read_back_execution_states().is_empty()
 
 
 def test_graph_equals_fused(cuda):

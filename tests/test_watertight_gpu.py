@@ -84,23 +84,24 @@ def test_flags_instances_reference_order(inst_scene, flags, anyhit, cuda):  # no
     assert_bit_identical(got, ext, expect)
 
 
+@pytest.mark.parametrize("light", [LIGHT, (0.5, 0.5, 0.12)])  # the second light is shadowed by the terrain
 @pytest.mark.parametrize("traversal", [rt.TRAVERSAL_REFERENCE, rt.TRAVERSAL_ORDERED_WIDE])
-def test_wavefront_watertight(traversal, cuda):
+def test_wavefront_watertight(traversal, light, cuda):
     import torch
 
     mesh = scenes.heightfield(128, seed=1)
     cam = scenes.heightfield_camera(160, 96)
     sc = single_mesh_scene(mesh)
     S, P = sc.build_oracle(), sc.build_product()
-    wf = rt.Wavefront(P, cam, LIGHT, traversal=traversal | WT)
+    wf = rt.Wavefront(P, cam, light, traversal=traversal | WT)
     wf.run(4)
     torch.cuda.synchronize()
     got = wf.results()
-    exp, rays, _ = orc.wavefront_shadow_bounce(S, cam.as_floats(), cam.width, cam.height, LIGHT, 4, threads=8,
+    exp, rays, _ = orc.wavefront_shadow_bounce(S, cam.as_floats(), cam.width, cam.height, light, 4, threads=8,
                                                watertight=True)
     assert wf.rays_traced() == tuple(rays)
     if traversal == rt.TRAVERSAL_REFERENCE:
         for f in exp.dtype.names:
             assert np.array_equal(got[f].view(np.uint32), exp[f].view(np.uint32)), f
-    res = parity.classify_wavefront(S, cam, cam.width, cam.height, LIGHT, got, exp, 4, watertight=True, threads=8)
+    res = parity.classify_wavefront(S, cam, cam.width, cam.height, light, got, exp, 4, watertight=True, threads=8)
     assert res["other"] == 0, res

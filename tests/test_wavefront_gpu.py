@@ -62,6 +62,25 @@ def test_wavefront_ordered_matches_except_ties(traversal, refill, light, cuda):
     assert np.all(bsame[ok])
 
 
+@pytest.mark.parametrize("size", [(45, 23), (1, 1), (7, 3)])
+@pytest.mark.parametrize("traversal", [rt.TRAVERSAL_REFERENCE, rt.TRAVERSAL_ORDERED_WIDE])
+def test_ragged_frames(size, traversal, cuda):
+    """Frames that are not whole 8x4 tiles: the primary kernel's overhanging
+    lanes neither trace nor enqueue, and every record is the oracle's."""
+    mesh = scenes.heightfield(64, seed=5)
+    cam = scenes.heightfield_camera(*size)
+    got, exp, rays, counts = run_both(mesh, cam, traversal, sample_index=1, light=LOW_LIGHT)
+    assert counts == tuple(rays)
+    assert len(got) == size[0] * size[1]
+    if traversal == rt.TRAVERSAL_REFERENCE:
+        for f in exp.dtype.names:
+            assert np.array_equal(got[f].view(np.uint32), exp[f].view(np.uint32)), f
+    else:
+        ok = (got["primary_prim"] == exp["primary_prim"]) & (got["primary_t"] == exp["primary_t"])
+        assert np.all(ok | (got["primary_t"] == exp["primary_t"]))
+        assert np.array_equal(got["light"][ok], exp["light"][ok])
+
+
 def test_wavefront_soup_camera(cuda):
     mesh = scenes.triangle_soup(5000, seed=2)
     cam = scenes.soup_camera(64, 48)
