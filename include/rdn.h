@@ -735,7 +735,7 @@ rdn_status rdn_task_graph_capture(rdn_task_graph* graph, uint32_t group, uint32_
 /* The reference's AO pipeline as a task graph (feature/ao.rs:162-313 on
  * trace_ray): group 0 ray-trace task (max_in_flight 2), 1 ray generation,
  * 2 primary closest hit, 3 occlusion closest hit, 4 miss; capacity = the
- * frame rounded up to whole 8x4 pixel tiles. rdn_ao_render_graph dispatches
+ * frame rounded up to whole 4x8 pixel tiles (4 wide, 8 tall). rdn_ao_render_graph dispatches
  * one ray-generation task per pixel of those tiles (32 consecutive tasks per
  * tile, so that a warp traces neighbouring pixels; tasks past the frame
  * resolve without tracing) and runs 8 rounds (the reference's
@@ -795,7 +795,7 @@ rdn_status rdn_ao_capture(rdn_ctx* ctx, rdn_task_graph* pipeline, const rdn_ao_d
                                         (ties x, y, z), bilinear over texel centres clamped to the face, level 0
                                         (f32 weights, no filtering across faces) */
 #define RDN_PT_MAX_PATH_DEPTH 3u     /* the reference's MAX_RAY_DEPTH (path_tracing/mod.rs:80) */
-#define RDN_PT_SCHEDULE_PIXEL 0u     /* one thread per pixel, warps over 8x4 tiles */
+#define RDN_PT_SCHEDULE_PIXEL 0u     /* one thread per pixel, warps over 4x8 tiles */
 #define RDN_PT_SCHEDULE_REFILL 1u    /* persistent warps; a lane whose path ends takes the next pixel (the
                                         frame uses the context's work counter: one frame in flight per context) */
 #define RDN_PT_SCHEDULE_WAVEFRONT 2u /* one pass per ray kind and depth over queues of paths, the path state in

@@ -1,6 +1,6 @@
 // Fused ambient-occlusion frame for sm_103a: the reference AO renderer's ray
 // generation, primary closest hit, occlusion ray and miss shaders
-// (feature/ao.rs:193-296) as one kernel, one thread per pixel, warps over 8x4
+// (feature/ao.rs:193-296) as one kernel, one thread per pixel, warps over 4x8
 // pixel tiles. It computes what the task-graph form of the same pipeline
 // computes, without the task pools. Built with -fmad=false: see ao.cuh.
 #include <cuda_runtime.h>

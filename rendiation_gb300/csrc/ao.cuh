@@ -47,13 +47,13 @@ __device__ __forceinline__ void sincos_reduced(float phi, float& s, float& c) {
   }
 }
 
-// Pixel of dispatch index i: each run of 32 indices covers an 8x4 tile, tiles
-// in row order (a warp traces one tile). Indices of the tiles' overhang past
+// Pixel of dispatch index i: each run of 32 indices covers a 4x8 tile (4 wide,
+// 8 tall), tiles in row order (a warp traces one tile). Indices of the tiles' overhang past
 // the frame return false.
 __device__ __forceinline__ bool ao_pixel(const AoEnv& A, uint32_t i, uint32_t& x, uint32_t& y) {
-  const uint32_t tiles_x = (A.width + 7) / 8, t = i >> 5, lane = i & 31u;
-  x = (t % tiles_x) * 8 + (lane & 7u);
-  y = (t / tiles_x) * 4 + (lane >> 3);
+  const uint32_t tiles_x = (A.width + 3) / 4, t = i >> 5, lane = i & 31u;
+  x = (t % tiles_x) * 4 + (lane & 3u);
+  y = (t / tiles_x) * 8 + (lane >> 2);
   return x < A.width && y < A.height;
 }
 

@@ -5,7 +5,7 @@
 // (PtPath) advanced one ray at a time: the core ray and the shadow ray of a hit
 // take turns through one traversal call site, so the kernel holds one inlined
 // traversal instead of two. Two schedules:
-//   fused   one thread per pixel, warps over 8x4 pixel tiles; a warp runs until
+//   fused   one thread per pixel, warps over 4x8 pixel tiles; a warp runs until
 //           its longest path ends;
 //   refill  persistent warps: a lane whose path ends takes the next pixel
 //           (warp-aggregated atomic on a frame counter), so warps stay full
@@ -318,7 +318,7 @@ __device__ __forceinline__ void pt_load(const PtWave& W, uint32_t i, uint32_t wi
 // shadow rays: with lights the passes alternate core, shadow, core, ...,
 // since every core hit casts a shadow ray and every shadow ray is followed by
 // a core ray), advances the path and queues it for the next pass or resolves
-// its pixel. Pass 0 starts the paths from the camera, 8x4 pixel tiles per warp.
+// its pixel. Pass 0 starts the paths from the camera, 4x8 pixel tiles per warp.
 template <int MODE, bool LOCAL, bool WT, int TIER>
 __global__ void __launch_bounds__(128, pt_min_blocks(TIER))
     pt_pass_kernel(TraceParams P, PtEnv E, PtWave W, uint32_t pass, uint32_t shadow_pass) {

@@ -1520,7 +1520,7 @@ rdn_status rdn_ao_pipeline_create(rdn_ctx* c, uint32_t width, uint32_t height, v
   g[4].max_in_flight = 1;
   g[4].payload_words = 16;
   g[4].map_op = RDN_TASK_MAP_STORE_ONE;
-  // one ray-generation task per dispatch index, 8x4 pixel tiles (ao_pixel)
+  // one ray-generation task per dispatch index, 4x8 pixel tiles (ao_pixel)
   rdn_status st = rdn_task_graph_create(c, g, 5, rdn::ao_dispatch_count(width, height), stream, out);
   if (st != RDN_OK) return st;
   (*out)->ao_pipeline = true;

@@ -158,9 +158,9 @@ struct AoEnv {
   uint32_t block;              // fused kernel: threads per block (32, 64 or 128)
 };
 
-// Ray-generation tasks of a w x h AO frame: whole 8x4 pixel tiles, 32 per tile.
+// Ray-generation tasks of a w x h AO frame: whole 4x8 pixel tiles, 32 per tile.
 __host__ __device__ inline uint32_t ao_dispatch_count(uint32_t w, uint32_t h) {
-  return ((w + 7) / 8) * ((h + 3) / 4) * 32;
+  return ((w + 3) / 4) * ((h + 7) / 8) * 32;
 }
 
 struct TaskGroupDesc {

@@ -10,8 +10,8 @@
 // (scene/rendering/gpu-ray-tracing/src/feature/path_tracing/{ray_gen.rs,ray_hit.rs})
 // is two kernels:
 //
-//   primary_kernel: one thread per pixel, persistent warps that claim 8x4
-//     pixel tiles from a counter. Pinhole ray -> closest hit -> geometric normal facing the ray ->
+//   primary_kernel: one thread per pixel, persistent warps that claim 4x8
+//     pixel tiles (4 wide, 8 tall) from a counter. Pinhole ray -> closest hit -> geometric normal facing the ray ->
 //     offset_ray_hit origin -> one shadow ray to the point light and one
 //     cosine-weighted bounce ray, appended to two queues that share one
 //     counter: a warp ballot and one atomicAdd per warp reserve the slots, so
@@ -53,17 +53,17 @@ __global__ void __launch_bounds__(128, min_blocks(TIER)) primary_kernel(TracePar
   uint2* const stack = LOCAL ? local_stack : smem_stack + threadIdx.x;
   const uint32_t stride = LOCAL ? 1u : blockDim.x;
   const uint32_t lane = threadIdx.x & 31u;
-  const uint32_t tiles_x = (w.width + 7u) / 8u;
-  const uint32_t tiles = tiles_x * ((w.height + 3u) / 4u);
-  // persistent: each warp claims 8x4 pixel tiles from a counter until none is
+  const uint32_t tiles_x = (w.width + 3u) / 4u;
+  const uint32_t tiles = tiles_x * ((w.height + 7u) / 8u);
+  // persistent: each warp claims 4x8 pixel tiles from a counter until none is
   // left, so that a warp that finishes early does not wait for its block
   for (;;) {
     uint32_t tile = 0;
     if (lane == 0) tile = atomicAdd(w.tile_counter, 1u);
     tile = __shfl_sync(0xffffffffu, tile, 0);
     if (tile >= tiles) break;
-    const uint32_t px = (tile % tiles_x) * 8u + (lane & 7u);
-    const uint32_t py = (tile / tiles_x) * 4u + (lane >> 3);
+    const uint32_t px = (tile % tiles_x) * 4u + (lane & 3u);
+    const uint32_t py = (tile / tiles_x) * 8u + (lane >> 2);
     const bool valid = px < w.width && py < w.height;
 
     bool want = false;
@@ -303,12 +303,12 @@ cudaError_t launch_wavefront_mode(const TraceParams& p, const WavefrontParams& w
     e = cudaMemsetAsync(w.queue_count, 0, 64, stream);
     if (e != cudaSuccess) return e;
     // persistent primary grid: as many resident blocks as fill every SM, or
-    // fewer when the frame has fewer 8x4 tiles than resident warps
+    // fewer when the frame has fewer 4x8 tiles than resident warps
     int per_sm1 = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm1, primary_kernel<MODE, LOCAL, TIER, WT>, (int)block, smem);
     if (e != cudaSuccess) return e;
     if (per_sm1 < 1) per_sm1 = 1;
-    const uint64_t tiles = (uint64_t)((w.width + 7) / 8) * ((w.height + 3) / 4);
+    const uint64_t tiles = (uint64_t)((w.width + 3) / 4) * ((w.height + 7) / 8);
     const uint64_t need = (tiles * 32 + block - 1) / block;
     const uint32_t grid1 = (uint32_t)std::min<uint64_t>((uint64_t)sm_count * per_sm1, need);
     primary_kernel<MODE, LOCAL, TIER, WT><<<grid1, block, smem, stream>>>(p, w);

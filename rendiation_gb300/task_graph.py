@@ -283,7 +283,7 @@ class AmbientOcclusion:
         if mode == "graph":
             h = C.c_void_p()
             _check(system._h, system._L.rdn_ao_pipeline_create(system._h, width, height, _stream(None), C.byref(h)))
-            src = DeviceTaskGraphBuildSource(capacity=((width + 7) // 8) * ((height + 3) // 4) * 32)
+            src = DeviceTaskGraphBuildSource(capacity=((width + 3) // 4) * ((height + 7) // 8) * 32)
             for mif in (2, 1, 1, 1, 1):
                 src.tasks.append(_TaskDef(ShaderFuture(), mif, 1))
             self.graph = DeviceTaskGraphExecutor(system, src, _handle=h)

@@ -116,7 +116,7 @@ def test_leaf_postponement_threshold(cuda, mode, speculation):
 @pytest.mark.parametrize("mode", ["fused", "graph"])
 @pytest.mark.parametrize("size", [(53, 29), (1, 1), (9, 5)])
 def test_ragged_frames(cuda, mode, size):
-    """Frames that are not whole 8x4 tiles: the tiles' overhanging pixels
+    """Frames that are not whole 4x8 tiles: the tiles' overhanging pixels
     neither trace nor write; every texel of the frame is the oracle's."""
     w, h = size
     scene = field_scene()

@@ -20,7 +20,7 @@ from rendiation_gb300 import task_graph as tg
 
 pytestmark = pytest.mark.gpu
 
-W, H = 77, 45  # not a multiple of the 8x4 tile: the last tiles overhang the frame
+W, H = 77, 45  # not a multiple of the 4x8 tile: the last tiles overhang the frame
 SAMPLES = (0, 1, 2)
 
 

@@ -65,7 +65,7 @@ def test_wavefront_ordered_matches_except_ties(traversal, refill, light, cuda):
 @pytest.mark.parametrize("size", [(45, 23), (1, 1), (7, 3)])
 @pytest.mark.parametrize("traversal", [rt.TRAVERSAL_REFERENCE, rt.TRAVERSAL_ORDERED_WIDE])
 def test_ragged_frames(size, traversal, cuda):
-    """Frames that are not whole 8x4 tiles: the primary kernel's overhanging
+    """Frames that are not whole 4x8 tiles: the primary kernel's overhanging
     lanes neither trace nor enqueue, and every record is the oracle's."""
     mesh = scenes.heightfield(64, seed=5)
     cam = scenes.heightfield_camera(*size)
