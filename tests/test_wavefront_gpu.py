@@ -81,6 +81,31 @@ def test_ragged_frames(size, traversal, cuda):
         assert np.array_equal(got["light"][ok], exp["light"][ok])
 
 
+@pytest.mark.parametrize("traversal", [rt.TRAVERSAL_REFERENCE, rt.TRAVERSAL_ORDERED_WIDE])
+def test_axis_parallel_camera_rays(traversal, cuda):
+    """A camera straight above the middle of a 65x65-vertex field: the middle
+    column and row of a 33x33 frame have direction components of exactly 0,
+    and their origin lies on the grid line x = 0.5, a plane of many node
+    boxes. The slab test then meets 0 * inf = NaN, which only the full
+    min / max test handles as the reference does; the other rays of the same
+    warps test boxes by their near and far planes."""
+    mesh = scenes.heightfield(65, seed=4)
+    cam = scenes.PinholeCamera.look_at((0.5, 0.5, 2.0), (0.5, 0.5, 0.0), 40.0, 33, 33)
+    assert cam.forward[0] == 0.0 and cam.forward[1] == 0.0
+    got, exp, rays, counts = run_both(mesh, cam, traversal, sample_index=2, light=LOW_LIGHT)
+    assert counts == tuple(rays)
+    if traversal == rt.TRAVERSAL_REFERENCE:
+        for f in exp.dtype.names:
+            assert np.array_equal(got[f].view(np.uint32), exp[f].view(np.uint32)), f
+    else:
+        same = (got["primary_prim"] == exp["primary_prim"]) & (got["primary_t"] == exp["primary_t"])
+        assert np.all(same | (got["primary_t"] == exp["primary_t"]))
+        assert np.array_equal(got["primary_flags"], exp["primary_flags"])
+        assert np.array_equal(got["light"][same], exp["light"][same])
+        bsame = (got["bounce_prim"] == exp["bounce_prim"]) | (got["bounce_t"] == exp["bounce_t"])
+        assert np.all(bsame[same])
+
+
 def test_wavefront_soup_camera(cuda):
     mesh = scenes.triangle_soup(5000, seed=2)
     cam = scenes.soup_camera(64, 48)
