@@ -242,8 +242,12 @@ def reference_counts_of_queues(P, wf, n_secondary):
     base = wf.scratch_ptr - wf.scratch.data_ptr()
     up = lambda b: (b + 255) & ~255  # noqa: E731
     sh = wf.scratch[base + 256: base + 256 + n_secondary * 32].view(torch.float32).reshape(-1, 8)
+    # bounce rays: the grazing bin from the queue's front, the steep bin at its back
+    n_front, n_back = (int(c) for c in wf.scratch[base + 8: base + 16].view(torch.int32).cpu().tolist())
+    assert n_front + n_back == n_secondary
     bo_off = base + 256 + up(n * 32)
-    bo = wf.scratch[bo_off: bo_off + n_secondary * 32].view(torch.float32).reshape(-1, 8)
+    bo_all = wf.scratch[bo_off: bo_off + n * 32].view(torch.float32).reshape(-1, 8)
+    bo = torch.cat([bo_all[:n_front], bo_all[n - n_back:]])
     h2 = torch.empty((max(1, n_secondary), 4), dtype=torch.float32, device="cuda")
     c_sh = P.trace_counted(sh.contiguous(), h2, traversal=rt.TRAVERSAL_REFERENCE,
                            ray_flags=rt.RAY_FLAG_ACCEPT_FIRST_HIT_AND_END_SEARCH)

@@ -46,6 +46,17 @@ using namespace dev;
 // 2 = at least 9 blocks (56 registers, 36 warps, more spills).
 constexpr int min_blocks(int tier) { return tier == 1 ? 7 : (tier == 2 ? 9 : 0); }
 
+// Bounce rays leaving their surface at a cosine of at least 1/sqrt(2) (half
+// of a cosine-weighted sample) go to the back bin of the bounce queue.
+constexpr float kSteepBounceCos = 0.70710678f;
+
+// Queue entry of the j-th bounce ray of the secondary kernel's index space:
+// the n_front grazing rays from the queue's front, then the steep ones from
+// its back (entry cap - 1 down).
+__device__ __forceinline__ uint32_t bounce_entry(uint32_t j, uint32_t n_front, uint32_t cap) {
+  return j < n_front ? j : cap - 1u - (j - n_front);
+}
+
 template <int MODE, bool LOCAL, int TIER, bool WT>
 __global__ void __launch_bounds__(128, min_blocks(TIER)) primary_kernel(TraceParams p, WavefrontParams w) {
   extern __shared__ uint2 smem_stack[];
@@ -68,7 +79,7 @@ __global__ void __launch_bounds__(128, min_blocks(TIER)) primary_kernel(TracePar
 
     bool want = false;
     float3 org = make_float3(0.f, 0.f, 0.f), ldir = org, bdir = org;
-    float dist = 0.0f;
+    float dist = 0.0f, bcos = 0.0f;
     if (valid) {
       // camera ray (pixel centre), the same f32 steps as the host generator
       const float sx = (((float)px + 0.5f) / (float)w.width * 2.0f - 1.0f) * w.tan_half * w.aspect;
@@ -113,22 +124,39 @@ __global__ void __launch_bounds__(128, min_blocks(TIER)) primary_kernel(TracePar
         const float s0 = sample_next(state);
         const float s1 = sample_next(state);
         bdir = cosine_sample_in_dir(nf, s0, s1);
+        bcos = dot3(bdir, nf);
         want = true;
       }
       w.out[(size_t)py * w.width + px] = out;
     }
-    // compacted append of both secondary rays (one counter for the pair)
-    const uint32_t slot = warp_append(w.queue_count, want);
+    // compacted appends: shadow rays to their queue; bounce rays to two bins of
+    // theirs, grazing ones (the longer walks) from its front and steep ones
+    // from its back, so that a warp of the secondary kernel traces rays of
+    // like walk lengths. One 64-bit atomic per warp counts both bins (low and
+    // high word); the shadow slot is the sum of the two bases plus the lane's
+    // rank, so the shadow queue stays dense. Every lane of the warp is here.
+    const bool steep = want && bcos >= kSteepBounceCos;
+    const uint32_t m_want = __ballot_sync(0xffffffffu, want), m_steep = __ballot_sync(0xffffffffu, steep);
+    const uint32_t m_front = m_want & ~m_steep;
+    unsigned long long bases = 0ull;
+    if (lane == 0 && m_want)
+      bases = atomicAdd(w.bins, (unsigned long long)__popc(m_front) | ((unsigned long long)__popc(m_steep) << 32));
+    bases = __shfl_sync(0xffffffffu, bases, 0);
+    const uint32_t below = (1u << lane) - 1u;
+    const uint32_t front = (uint32_t)bases + __popc(m_front & below);
+    const uint32_t back = (uint32_t)(bases >> 32) + __popc(m_steep & below);
+    const uint32_t slot = (uint32_t)bases + (uint32_t)(bases >> 32) + __popc(m_want & below);
     if (want) {
       const uint32_t pix = py * w.width + px;
       float4* sq = reinterpret_cast<float4*>(w.shadow_rays) + 2 * (size_t)slot;
       sq[0] = make_float4(org.x, org.y, org.z, F32_EPSILON);
       sq[1] = make_float4(ldir.x, ldir.y, ldir.z, dist);
-      float4* bq = reinterpret_cast<float4*>(w.bounce_rays) + 2 * (size_t)slot;
+      const uint32_t bslot = steep ? w.width * w.height - 1u - back : front;
+      float4* bq = reinterpret_cast<float4*>(w.bounce_rays) + 2 * (size_t)bslot;
       bq[0] = make_float4(org.x, org.y, org.z, F32_EPSILON);
       bq[1] = make_float4(bdir.x, bdir.y, bdir.z, F32_MAX);
       w.shadow_pixel[slot] = pix;
-      w.bounce_pixel[slot] = pix;
+      w.bounce_pixel[bslot] = pix;
     }
   }
 }
@@ -139,7 +167,9 @@ __global__ void __launch_bounds__(128, min_blocks(TIER)) secondary_kernel(TraceP
   uint2 local_stack[LOCAL ? kLocalStackEntries : 1];
   uint2* const stack = LOCAL ? local_stack : smem_stack + threadIdx.x;
   const uint32_t stride = LOCAL ? 1u : blockDim.x;
-  const uint32_t n = *(volatile uint32_t*)w.queue_count;
+  const unsigned long long bins = *(volatile unsigned long long*)w.bins;
+  const uint32_t n_front = (uint32_t)bins, n = n_front + (uint32_t)(bins >> 32);
+  const uint32_t cap = w.width * w.height;
   const uint32_t total = 2u * n;
   const uint32_t lane = threadIdx.x & 31u;
   if (blockIdx.x == 0 && threadIdx.x == 0 && w.ray_counts) {
@@ -158,7 +188,7 @@ __global__ void __launch_bounds__(128, min_blocks(TIER)) secondary_kernel(TraceP
       // that ends on short shadow rays leaves fewer warps waiting for a last
       // long batch (1.66 -> 1.54 ms on the 1080p frame)
       const bool shadow = j >= n;
-      const uint32_t q = shadow ? j - n : j;
+      const uint32_t q = shadow ? j - n : bounce_entry(j, n_front, cap);
       const float4* rq = reinterpret_cast<const float4*>(shadow ? w.shadow_rays : w.bounce_rays) + 2 * (size_t)q;
       const float4 r0 = rq[0], r1 = rq[1];
       RayCtx R;
@@ -205,7 +235,9 @@ template <int MODE, bool WT>
 __global__ void __launch_bounds__(128, 8) secondary_dynamic_kernel(TraceParams p, WavefrontParams w) {
   extern __shared__ uint2 smem_stack[];
   constexpr int WIDTH = MODE == MODE_WIDE4 ? 4 : 2;
-  const uint32_t n = *(volatile uint32_t*)w.queue_count;
+  const unsigned long long bins = *(volatile unsigned long long*)w.bins;
+  const uint32_t n_front = (uint32_t)bins, n = n_front + (uint32_t)(bins >> 32);
+  const uint32_t cap = w.width * w.height;
   const uint32_t total = 2u * n;
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t lanes_below = (1u << lane) - 1u;
@@ -239,8 +271,8 @@ __global__ void __launch_bounds__(128, 8) secondary_dynamic_kernel(TraceParams p
         if (j < total) {
           q = j;  // bounce rays first, as in the batch schedule
           const bool shadow = j >= n;
-          const float4* rq =
-              reinterpret_cast<const float4*>(shadow ? w.shadow_rays : w.bounce_rays) + 2 * (size_t)(shadow ? j - n : j);
+          const float4* rq = reinterpret_cast<const float4*>(shadow ? w.shadow_rays : w.bounce_rays) +
+                             2 * (size_t)(shadow ? j - n : bounce_entry(j, n_front, cap));
           L.start(p, rq[0], rq[1], w.tlas, shadow ? TF_END_SEARCH : 0u);
         }
       }
@@ -254,7 +286,7 @@ __global__ void __launch_bounds__(128, 8) secondary_dynamic_kernel(TraceParams p
         o->light = R.best.have ? 2u : 1u;
         if (R.best.have) o->direct = 0.0f;
       } else if (R.best.have) {
-        PixelResult* o = w.out + w.bounce_pixel[q];
+        PixelResult* o = w.out + w.bounce_pixel[bounce_entry(q, n_front, cap)];
         const uint4 gm = __ldg(reinterpret_cast<const uint4*>(p.tri_root + R.best.geom_slot));
         o->bounce_prim = __ldg(p.redirect + R.best.k) - gm.z;
         o->bounce_t = R.best.t;
@@ -277,6 +309,7 @@ void wavefront_bind_scratch(WavefrontParams& w, void* scratch) {
   auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
   char* s = static_cast<char*>(scratch);
   w.queue_count = reinterpret_cast<uint32_t*>(s);
+  w.bins = reinterpret_cast<unsigned long long*>(s + 8);
   w.tile_counter = reinterpret_cast<uint32_t*>(s + 16);
   w.work_counter = reinterpret_cast<uint32_t*>(s + 64);
   size_t off = 256;

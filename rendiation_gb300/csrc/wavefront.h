@@ -28,7 +28,11 @@ struct WavefrontParams {
   PixelResult* out;
   uint32_t* ray_counts;  // nullable: [primary, shadow, bounce]
   // scratch (wavefront_bind_scratch)
-  uint32_t* queue_count;
+  uint32_t* queue_count;   // start of the 64 B the primary launch zeroes
+  // bounce-queue bins (inside those 64 B): low word the grazing rays at the
+  // queue's front, high word the steep rays at its back; their sum is the
+  // count of shadow rays and of bounce rays
+  unsigned long long* bins;
   uint32_t* tile_counter;  // primary tiles claimed (inside the 64 B the launch zeroes at queue_count)
   uint32_t* work_counter;
   void* shadow_rays;
