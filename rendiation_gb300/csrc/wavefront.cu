@@ -46,9 +46,10 @@ using namespace dev;
 // 2 = at least 9 blocks (56 registers, 36 warps, more spills).
 constexpr int min_blocks(int tier) { return tier == 1 ? 7 : (tier == 2 ? 9 : 0); }
 
-// Bounce rays leaving their surface at a cosine of at least 1/sqrt(2) (half
-// of a cosine-weighted sample) go to the back bin of the bounce queue.
-constexpr float kSteepBounceCos = 0.70710678f;
+// Bounce rays leaving their surface at a cosine of at least 1/2 (three
+// quarters of a cosine-weighted sample) go to the back bin of the bounce
+// queue; the grazing quarter, the longest walks, to its front.
+constexpr float kSteepBounceCos = 0.5f;
 
 // Queue entry of the j-th bounce ray of the secondary kernel's index space:
 // the n_front grazing rays from the queue's front, then the steep ones from
