@@ -13,14 +13,16 @@
 //   primary_kernel: one thread per pixel, persistent warps that claim 4x8
 //     pixel tiles (4 wide, 8 tall) from a counter. Pinhole ray -> closest hit -> geometric normal facing the ray ->
 //     offset_ray_hit origin -> one shadow ray to the point light and one
-//     cosine-weighted bounce ray, appended to two queues that share one
-//     counter: a warp ballot and one atomicAdd per warp reserve the slots, so
-//     the queues come out compacted without a separate scan pass.
+//     cosine-weighted bounce ray. The shadow queue and the two bins of the
+//     bounce queue (grazing rays at its front, steep rays at its back) are
+//     filled through warp ballots and one 64-bit atomicAdd per warp, so the
+//     queues come out compacted without a separate scan pass.
 //   secondary_kernel: persistent warps that fetch 32 queue entries at a time
-//     from a global work counter; bounce rays (closest hit, the long walks)
-//     occupy the first half of the index space and shadow rays (first-hit
-//     search) the second, so warps stay homogeneous and the kernel ends on
-//     short work. Results scatter to the pixel records.
+//     from a global work counter; the grazing bounce rays, then the steep
+//     ones (closest hit, the long walks), occupy the first half of the index
+//     space and shadow rays (first-hit search) the second, so warps stay
+//     homogeneous and the kernel ends on short work. Results scatter to the
+//     pixel records.
 //
 // Built with -fmad=false: all shading arithmetic is IEEE f32 in the same
 // order as the oracle, so secondary rays are bit-identical.
